@@ -1,0 +1,248 @@
+/*
+ * swave.h - C-ABI of the GB300 acoustic wave-equation engine (libswave.so).
+ *
+ * The engine replaces the hot path of the seismic suite's libwave:
+ * the 8th-order / 5-level finite-difference propagator with Higdon absorbing
+ * boundaries, sinc / nearest-node source injection and receiver extraction,
+ * snapshot saving, the RTM / LSRTM / AFWI imaging conditions, the Born
+ * secondary source, and the FWI objective/gradient plus its FP64 L-BFGS
+ * update.  Every compute step runs in hand-written sm_103a CUDA kernels;
+ * there is no CPU fallback.
+ *
+ * Conventions
+ *  - All arrays are host arrays owned by the caller, read or written only
+ *    during the call.  Device memory is owned by the context.
+ *  - Model / image arrays are Fortran order, z fastest: a(nz, nx, ny).
+ *  - Traces are trace-major, time fastest: trace r, sample it (1-based in
+ *    the reference) lives at tr[r*nt + it-1].
+ *  - Snapshots: wave(nz, nx, ny, ntsnap) with ntsnap = nt/snapi.
+ *  - Coordinates are physical (z, x, y) triples in the same units as the
+ *    grid origin and spacing.
+ *  - Every entry point returns an sw_status; sw_last_error() gives text.
+ *  - One context per host thread; calls on one context are serialised.
+ */
+#ifndef SWAVE_H
+#define SWAVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference aborts through erexit() instead
+ * (e.g. libs/libwave/ReadSouVelRho.f90:650-756); these codes carry the
+ * same conditions back to the caller. */
+typedef enum sw_status {
+  SW_OK = 0,
+  SW_BAD_PARAM = 1,      /* invalid sizes, vel_check failure, bad coords    */
+  SW_OOM_ADMISSION = 2,  /* the work does not fit the device memory budget  */
+  SW_TIMEOUT = 3,        /* a bounded device-side wait ran out              */
+  SW_NUMERIC = 4,        /* NaN / Inf detected                              */
+  SW_CUDA_ERR = 5,       /* a CUDA runtime call failed                      */
+  SW_UNSUPPORTED = 6     /* option not built (mirror / free surface / rho)  */
+} sw_status;
+
+/* Subset of GeneralParam (libs/libwave/GeneralParamTypes.f90:9-48) that the
+ * propagation path reads.  nz/nx/ny are the (windowed) model sizes, i.e.
+ * model%nz, model%nxw, model%nyw; oz/ox/oy the window origin
+ * (genpar%omodel).  ny = 1 and twoD = 1 for 2D. */
+typedef struct sw_genpar {
+  int twoD;
+  int nz, nx, ny;
+  float dz, dx, dy;
+  float oz, ox, oy;
+  float dt;
+  int nt;
+  int ntaper;      /* padding cells per side (ReadParam.f90:19, default 20) */
+  int lsinc;       /* sinc length (ReadParam.f90:24, default 7)             */
+  int snapi;       /* snapshot decimation (ReadParam.f90:20, default 4)     */
+  int surf_type, shot_type, rec_type;   /* only 0 is built                 */
+  float fmax;      /* used by vel_check only                                */
+} sw_genpar;
+
+/* The procedure arguments of propagator_acoustic
+ * (libs/libwave/Propagator.f90:27-120) become enum selectors. */
+typedef enum sw_fd_scheme {
+  SW_FD_FORWARD = 0,  /* FD_2nd_{2D,3D}_derivatives_scalar_forward_grid   */
+  SW_FD_ADJOINT = 1   /* FD_2nd_{2D,3D}_derivatives_scalar_adjoint_grid   */
+} sw_fd_scheme;
+
+typedef enum sw_injection {
+  SW_INJ_NONE = 0,
+  SW_INJ_SINC = 1,        /* Injection_sinc          (Injection.f90:151)    */
+  SW_INJ_SIMPLE = 2,      /* Injection_simple_noomp  (Injection.f90:63)     */
+  SW_INJ_LSRTM_SINC = 3   /* Injection_LSRTM_sinc    (Injection.f90:239)    */
+} sw_injection;
+
+typedef enum sw_extraction {
+  SW_EXT_NONE = 0,
+  SW_EXT_SINC = 1,         /* Extraction_array_sinc        (Extraction.f90:109) */
+  SW_EXT_SIMPLE_AFWI = 2,  /* Extraction_array_simple_afwi (Extraction.f90:71)  */
+  SW_EXT_LSRTM_SINC = 3,   /* Extraction_array_LSRTM_sinc  (Extraction.f90:217) */
+  SW_EXT_SINC_AFWI = 4     /* Extraction_array_sinc_afwi   (Extraction.f90:137) */
+} sw_extraction;
+
+typedef enum sw_imaging {
+  SW_IMG_NONE = 0,
+  SW_IMG_RTM = 1,    /* Imaging_condition_sourceonly_from_memory (Imaging.f90:228) */
+  SW_IMG_LSRTM = 2,  /* Imaging_condition_LSRTM_sourceonly_...   (Imaging.f90:698) */
+  SW_IMG_AFWI = 3,   /* Imaging_condition_AFWI_from_memory       (Imaging.f90:371) */
+  SW_IMG_BORN = 4    /* Injection_Born                           (Imaging.f90:747) */
+} sw_imaging;
+
+/* One propagation = one call of propagator_acoustic. */
+typedef struct sw_prop_desc {
+  sw_genpar g;
+  int tmin, tmax, tstep;   /* genpar%tmin/tmax/tstep (tstep = +1 or -1) */
+  int fd_scheme;           /* sw_fd_scheme  */
+  int injection;           /* sw_injection  */
+  int extraction;          /* sw_extraction */
+  int extract_wave;        /* 1: Extraction_wavefield into io.wave       */
+  int imaging;             /* sw_imaging    */
+} sw_prop_desc;
+
+/* Arrays of one propagation.  vel is the unpadded window velocity; the
+ * engine pads it by edge replication exactly like model_pad
+ * (ReadSouVelRho.f90:545-596).  NULL is allowed for every array the
+ * selected options do not use. */
+typedef struct sw_prop_io {
+  const float *vel;         /* nz*nx*ny                                    */
+  int nsou;
+  const float *sou_coord;   /* 3*nsou  (z,x,y)                             */
+  const float *sou_trace;   /* nsou*nt                                     */
+  int nrec;
+  const float *rec_coord;   /* 3*nrec                                      */
+  float *rec_trace;         /* nrec*nt, accumulated (+=) like trace(it,1)  */
+  float *wave;              /* nz*nx*ny*ntsnap: written by extract_wave,
+                               read by the imaging conditions              */
+  float *image;             /* nz*nx*ny accumulator (imagesmall)           */
+  float *illum;             /* nz*nx*ny accumulator (illumsmall)           */
+  const float *ref;         /* nz*nx*ny reflectivity for SW_IMG_BORN       */
+  float *final_u2;          /* optional: padded u2 after the last step,
+                               (nz+2nt+8)*(nx+2nt+8)*(ny>1?ny+2nt+8:1)    */
+} sw_prop_io;
+
+typedef struct sw_ctx sw_ctx;
+
+/* Context: one CUDA stream, a device-buffer arena, graph cache, counters. */
+int sw_ctx_create(int device, sw_ctx **out);
+int sw_ctx_destroy(sw_ctx *ctx);
+const char *sw_last_error(const sw_ctx *ctx);
+
+/* Library version string and the CUDA arch it was built for. */
+const char *sw_version(void);
+
+/* vel_check (ReadSouVelRho.f90:603-756): Courant <= 0.45 (2D) / 0.35 (3D)
+ * and >= 2 samples per minimum wavelength.  Returns SW_OK or SW_BAD_PARAM;
+ * *courant and *samplerate receive the computed numbers.  Host only. */
+int sw_vel_check(const sw_genpar *g, const float *vel, float *courant,
+                 float *samplerate);
+
+/* propagator_acoustic (Propagator.f90:27-270) for one shot.  Step order per
+ * time sample (Propagator.f90:168-234): extract(u2) -> snapshot(u2) ->
+ * [imaging(u2) if tstep=-1] -> stencil(u2->u3) -> inject(u3) ->
+ * [Born source(u3) if tstep=+1] -> 5-level time update -> Higdon -> rotate. */
+int sw_propagate(sw_ctx *ctx, const sw_prop_desc *d, const sw_prop_io *io);
+
+/* ---- Operator drivers (progs/{modeling,rtm,afwi}: to_disk_to_memory_*.f90) -
+ * Snapshots stay in device memory between the two propagations. */
+
+/* Acoustic modelling: forward, Injection_sinc, Extraction_array_sinc
+ * (progs/modeling/Acoustic_modeling.f90:115-123). */
+int sw_modeling(sw_ctx *ctx, const sw_genpar *g, const float *vel,
+                const float *sou_coord, const float *wavelet,
+                int nrec, const float *rec_coord, float *data,
+                float *final_u2);
+
+/* RTM_to_memory (progs/rtm/to_disk_to_memory_RTM.f90:358-492): forward with
+ * snapshots, backward with the 2D adjoint (3D forward) stencil injecting the
+ * data, zero-lag imaging.  image/illum are nz*nx*ny, overwritten. */
+int sw_rtm(sw_ctx *ctx, const sw_genpar *g, const float *vel,
+           const float *sou_coord, const float *wavelet,
+           int nrec, const float *rec_coord, const float *data,
+           float *image, float *illum);
+
+/* BORN_to_memory (progs/modeling/to_disk_to_memory_BORN.f90:123-220).
+ * wavelet must already be the 2nd time derivative (readsou with Born=T,
+ * ReadSouVelRho.f90:318-326; see sw_born_wavelet).  data is overwritten. */
+int sw_born(sw_ctx *ctx, const sw_genpar *g, const float *vel,
+            const float *ref, const float *sou_coord, const float *wavelet,
+            int nrec, const float *rec_coord, float *data);
+
+/* LSRTM_to_memory (progs/rtm/to_disk_to_memory_RTM.f90:494-580): the Born
+ * adjoint.  image/illum overwritten. */
+int sw_lsrtm(sw_ctx *ctx, const sw_genpar *g, const float *vel,
+             const float *sou_coord, const float *wavelet,
+             int nrec, const float *rec_coord, const float *data,
+             float *image, float *illum);
+
+/* readsou's Born/LSRTM preprocessing (ReadSouVelRho.f90:318-326): in place
+ * centred 2nd difference / dt^2. */
+int sw_born_wavelet(float *wavelet, int nt, float dt);
+
+/* ---- FWI objective / gradient (progs/afwi/compute_function_gradient.f90) */
+
+typedef struct sw_fwi_shot {
+  float sou_coord[3];
+  int nrec;
+  const float *rec_coord;   /* 3*nrec                                    */
+  const float *dobs;        /* nrec*nt observed data                     */
+  const float *mute;        /* nrec*nt mute mask (NULL = all ones)       */
+  float *resid;             /* optional out: nrec*nt residual            */
+} sw_fwi_shot;
+
+typedef struct sw_fwi_desc {
+  sw_genpar g;              /* full-model geometry: nz, nx, ny, origins    */
+  float aperture_x, aperture_y;
+  float illu_pow;           /* invparam%illupow (default 1)               */
+  int smooth_rect1, smooth_rect2, smooth_rect3;  /* triangle2 half-widths  */
+  int smooth_doz, smooth_dox, smooth_doy;
+} sw_fwi_desc;
+
+/* compute_fct_gdt (compute_function_gradient.f90:208-350): for every shot
+ * window + pad the model, AMOD (forward, nearest-node extraction,
+ * snapshots), residual/misfit (FP64), AGRAD (backward with the AFWI imaging
+ * condition), scatter-add into the full grid; then scaling, illumination
+ * normalisation, mask, triangle smoothing, mask.  vel/grad/illum/mask are
+ * nz*nx*ny.  *f receives the FP64 misfit. */
+int sw_fwi_fct_gdt(sw_ctx *ctx, const sw_fwi_desc *d, const float *vel,
+                   const float *wavelet, int nshot, const sw_fwi_shot *shots,
+                   const float *vpmask, double *f, float *grad, float *illum);
+
+/* ---- L-BFGS (libs/libinv/lbfgs.f:49-558, FP64 on the device) ----------
+ * Reverse communication exactly like LBFGS(): the caller evaluates f and g
+ * at x whenever *iflag returns 1, and calls again. */
+typedef struct sw_lbfgs sw_lbfgs;
+int sw_lbfgs_create(sw_ctx *ctx, int n, int m, double xmin, double xmax,
+                    const float *mask, int bound_type, int freeze_soft,
+                    const double *xinit, sw_lbfgs **out);
+int sw_lbfgs_destroy(sw_lbfgs *s);
+/* x: n doubles (in/out), f, g: n doubles.  iflag (in/out) and info (out)
+ * follow LBFGS: iflag=0 on the first call; 1 = evaluate and call again;
+ * 0 = converged; <0 = error.  *myinfo = 1 when an iteration completed. */
+int sw_lbfgs_step(sw_lbfgs *s, double *x, double f, const double *g,
+                  double eps, double xtol, int *iflag, int *myinfo);
+/* Scalars of the last step: [iter, nfun, stp, gnorm, ys, yy, dginit, dg]. */
+int sw_lbfgs_diag(const sw_lbfgs *s, double *out8);
+
+/* ---- Instrumentation ----------------------------------------------------- */
+typedef struct sw_stats {
+  uint64_t launches_total;      /* kernels launched by this context          */
+  uint64_t launches_step;       /* fused stencil/time-update launches        */
+  uint64_t points_updated;      /* compute-domain point updates              */
+  double   step_kernel_ms;      /* event-timed total of the fused kernel
+                                   (only while profiling is on)              */
+  uint64_t step_kernel_timed;   /* number of timed fused-kernel launches     */
+  uint64_t step_bytes;          /* algorithmic bytes of those launches       */
+} sw_stats;
+int sw_ctx_get_stats(const sw_ctx *ctx, sw_stats *out);
+int sw_ctx_reset_stats(sw_ctx *ctx);
+/* on=1: bracket every fused-kernel launch with CUDA events. */
+int sw_ctx_set_profiling(sw_ctx *ctx, int on);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWAVE_H */

@@ -1,0 +1,245 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+CPU-baseline legs of bench.py.  Parity status of the oracle: unpinned (see
+oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+
+def _types():
+    from seismic_gb300 import SwFwiDesc, SwFwiShot, SwGenpar, SwPropDesc, SwPropIO
+    return SwGenpar, SwPropDesc, SwPropIO, SwFwiDesc, SwFwiShot
+
+
+class OrPropIO64(C.Structure):
+    _fields_ = [("vel", _dp), ("nsou", C.c_int), ("sou_coord", _dp), ("sou_trace", _dp),
+                ("nrec", C.c_int), ("rec_coord", _dp), ("rec_trace", _dp), ("wave", _dp),
+                ("image", _dp), ("illum", _dp), ("ref", _dp), ("final_u2", _dp)]
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        from seismic_gb300.build import build_oracle
+        build_oracle()
+    lib = C.CDLL(LIB_PATH)
+    G, D, IO, FD, FS = _types()
+    g, d = C.POINTER(G), C.POINTER(D)
+    sig = {
+        "oracle_propagate_f32": [d, C.POINTER(IO)],
+        "oracle_propagate_f64": [d, C.POINTER(OrPropIO64)],
+        "oracle_modeling_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp],
+        "oracle_modeling_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp],
+        "oracle_rtm_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp],
+        "oracle_born_f32": [g, _fp, _fp, _fp, _fp, C.c_int, _fp, _fp],
+        "oracle_born_f64": [g, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp],
+        "oracle_lsrtm_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp],
+        "oracle_lsrtm_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp],
+        "oracle_born_wavelet": [_fp, C.c_int, C.c_float],
+        "oracle_vel_check": [g, _fp, _fp, _fp],
+        "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
+        "oracle_triangle2": [_fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                             C.c_int, C.c_int],
+        "oracle_lbfgs_step": [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
+                              C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.oracle_mksinc.argtypes = [_fp, C.c_int, C.c_float]
+    lib.oracle_mksinc.restype = None
+    lib.oracle_lbfgs_create.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _fp, C.c_int,
+                                        C.c_int, _dp]
+    lib.oracle_lbfgs_create.restype = C.c_void_p
+    lib.oracle_lbfgs_destroy.argtypes = [C.c_void_p]
+    lib.oracle_lbfgs_destroy.restype = None
+    lib.oracle_lbfgs_diag.argtypes = [C.c_void_p, _dp]
+    lib.oracle_lbfgs_diag.restype = None
+    _lib = lib
+    return lib
+
+
+def _f(a):
+    a = np.ascontiguousarray(a, np.float32)
+    return a, a.ctypes.data_as(_fp)
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+def _chk(code, what):
+    if code != 0:
+        raise RuntimeError(f"oracle {what} failed with status {code}")
+
+
+def modeling(g, vel, sou, wavelet, rec, final_u2=False, f64=False):
+    lib = load()
+    from seismic_gb300 import padded_shape
+    nrec = np.asarray(rec).size // 3
+    if f64:
+        v, pv = _d(vel); s, ps = _d(sou); w, pw = _d(wavelet); r, pr = _d(rec)
+        data = np.zeros((nrec, g.nt)); fu = np.zeros(padded_shape(g)) if final_u2 else None
+        _chk(lib.oracle_modeling_f64(C.byref(g), pv, ps, pw, nrec, pr, data.ctypes.data_as(_dp),
+                                     fu.ctypes.data_as(_dp) if fu is not None else None), "modeling")
+    else:
+        v, pv = _f(vel); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec)
+        data = np.zeros((nrec, g.nt), np.float32)
+        fu = np.zeros(padded_shape(g), np.float32) if final_u2 else None
+        _chk(lib.oracle_modeling_f32(C.byref(g), pv, ps, pw, nrec, pr, data.ctypes.data_as(_fp),
+                                     fu.ctypes.data_as(_fp) if fu is not None else None), "modeling")
+    return (data, fu) if final_u2 else data
+
+
+def rtm(g, vel, sou, wavelet, rec, data):
+    lib = load()
+    v, pv = _f(vel); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec); d, pd = _f(data)
+    n = g.nz * g.nx * g.ny
+    im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    _chk(lib.oracle_rtm_f32(C.byref(g), pv, ps, pw, r.size // 3, pr, pd, im.ctypes.data_as(_fp),
+                            il.ctypes.data_as(_fp)), "rtm")
+    return im, il
+
+
+def lsrtm(g, vel, sou, wavelet, rec, data, f64=False):
+    lib = load()
+    n = g.nz * g.nx * g.ny
+    if f64:
+        v, pv = _d(vel); s, ps = _d(sou); w, pw = _d(wavelet); r, pr = _d(rec); d, pd = _d(data)
+        im, il = np.zeros(n), np.zeros(n)
+        _chk(lib.oracle_lsrtm_f64(C.byref(g), pv, ps, pw, r.size // 3, pr, pd,
+                                  im.ctypes.data_as(_dp), il.ctypes.data_as(_dp)), "lsrtm")
+    else:
+        v, pv = _f(vel); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec); d, pd = _f(data)
+        im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        _chk(lib.oracle_lsrtm_f32(C.byref(g), pv, ps, pw, r.size // 3, pr, pd,
+                                  im.ctypes.data_as(_fp), il.ctypes.data_as(_fp)), "lsrtm")
+    return im, il
+
+
+def born(g, vel, ref, sou, wavelet, rec, f64=False):
+    lib = load()
+    nrec = np.asarray(rec).size // 3
+    if f64:
+        v, pv = _d(vel); f, pf = _d(ref); s, ps = _d(sou); w, pw = _d(wavelet); r, pr = _d(rec)
+        data = np.zeros((nrec, g.nt))
+        _chk(lib.oracle_born_f64(C.byref(g), pv, pf, ps, pw, nrec, pr, data.ctypes.data_as(_dp)),
+             "born")
+    else:
+        v, pv = _f(vel); f, pf = _f(ref); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec)
+        data = np.zeros((nrec, g.nt), np.float32)
+        _chk(lib.oracle_born_f32(C.byref(g), pv, pf, ps, pw, nrec, pr, data.ctypes.data_as(_fp)),
+             "born")
+    return data
+
+
+def propagate(desc, vel, sou_coord=None, sou_trace=None, rec_coord=None, rec_trace=None,
+              wave=None, image=None, illum=None, ref=None, final_u2=None):
+    lib = load()
+    _, _, IO, _, _ = _types()
+    io = IO()
+    keep = []
+    v, io.vel = _f(vel); keep.append(v)
+    if sou_coord is not None:
+        a, io.sou_coord = _f(sou_coord); b, io.sou_trace = _f(sou_trace); keep += [a, b]
+        io.nsou = a.size // 3
+    if rec_coord is not None:
+        a, io.rec_coord = _f(rec_coord); keep.append(a)
+        io.nrec = a.size // 3
+        io.rec_trace = rec_trace.ctypes.data_as(_fp)
+    for name, arr in (("wave", wave), ("image", image), ("illum", illum), ("final_u2", final_u2)):
+        if arr is not None:
+            assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"]
+            setattr(io, name, arr.ctypes.data_as(_fp))
+    if ref is not None:
+        a, io.ref = _f(ref); keep.append(a)
+    _chk(lib.oracle_propagate_f32(C.byref(desc), C.byref(io)), "propagate")
+
+
+def fwi_fct_gdt(desc, vel, wavelet, shots, vpmask=None):
+    lib = load()
+    _, _, _, _, FS = _types()
+    arr = (FS * len(shots))()
+    keep = []
+    for i, s in enumerate(shots):
+        rc, prc = _f(s["rec"]); dob, pdo = _f(s["dobs"])
+        keep += [rc, dob]
+        arr[i].sou_coord[:] = [float(v) for v in s["sou"]]
+        arr[i].nrec = rc.size // 3
+        arr[i].rec_coord, arr[i].dobs = prc, pdo
+        if s.get("mute") is not None:
+            mu, pmu = _f(s["mute"]); keep.append(mu); arr[i].mute = pmu
+    g = desc.g
+    n = g.nz * g.nx * g.ny
+    grad, illum = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    f = C.c_double()
+    v, pv = _f(vel); w, pw = _f(wavelet)
+    m, pm = (_f(vpmask) if vpmask is not None else (None, None))
+    _chk(lib.oracle_fwi_fct_gdt(C.byref(desc), pv, pw, len(shots), arr, pm, C.byref(f),
+                                grad.ctypes.data_as(_fp), illum.ctypes.data_as(_fp)), "fwi")
+    return f.value, grad, illum
+
+
+def mksinc(lsinc: int, shift: float) -> np.ndarray:
+    lib = load()
+    out = np.zeros(lsinc, np.float32)
+    lib.oracle_mksinc(out.ctypes.data_as(_fp), lsinc, shift)
+    return out
+
+
+def triangle2(uu, n1, n2, n3, rect1, rect2, rect3, doz, dox, doy):
+    lib = load()
+    u = np.ascontiguousarray(uu, np.float32).copy()
+    _chk(lib.oracle_triangle2(u.ctypes.data_as(_fp), n1, n2, n3, rect1, rect2, rect3, doz, dox,
+                              doy), "triangle2")
+    return u
+
+
+class LBFGS:
+    def __init__(self, n, m=5, xmin=1500.0, xmax=4500.0, mask=None, bound_type=2,
+                 freeze_soft=True, xinit=None):
+        lib = load()
+        self.lib = lib
+        self.mask = np.ones(n, np.float32) if mask is None else np.ascontiguousarray(mask, np.float32)
+        self.xinit = np.zeros(n) if xinit is None else np.ascontiguousarray(xinit, np.float64)
+        self.h = lib.oracle_lbfgs_create(n, m, xmin, xmax, self.mask.ctypes.data_as(_fp),
+                                         bound_type, int(freeze_soft),
+                                         self.xinit.ctypes.data_as(_dp))
+        self.iflag = C.c_int(0)
+        self.myinfo = C.c_int(0)
+
+    def step(self, x, f, g, eps=1e-20, xtol=np.finfo(float).eps):
+        self.myinfo.value = 0
+        gg = np.ascontiguousarray(g, np.float64)
+        _chk(self.lib.oracle_lbfgs_step(self.h, x.ctypes.data_as(_dp), float(f),
+                                        gg.ctypes.data_as(_dp), eps, xtol, C.byref(self.iflag),
+                                        C.byref(self.myinfo)), "lbfgs")
+        return self.iflag.value, self.myinfo.value
+
+    def diag(self):
+        out = np.zeros(8)
+        self.lib.oracle_lbfgs_diag(self.h, out.ctypes.data_as(_dp))
+        return out
+
+    def __del__(self):
+        try:
+            self.lib.oracle_lbfgs_destroy(self.h)
+        except Exception:
+            pass

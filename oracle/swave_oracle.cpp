@@ -1,0 +1,1584 @@
+// swave_oracle.cpp - CPU restatement of the reference acoustic path.
+//
+// TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for the CUDA engine
+// and the timed CPU baseline.  Parity status: UNPINNED (no compilable
+// reference, no golden vectors in the reference tree).
+//
+// Every routine cites the Fortran it restates (paths relative to the
+// reference project root).  Arithmetic is written in the Fortran evaluation
+// order and must be compiled with -ffp-contract=off.  The template parameter
+// T is float for the parity build and double for the FP64 twin.
+
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Bounds and padded arrays
+// ---------------------------------------------------------------------------
+
+// FDbounds as set by readvel / copy_window_vel_gath for
+// shot_type = surf_type = 0 (libs/libwave/ReadSouVelRho.f90:456-470,
+// libs/libwave/ExtractPadModel.f90:483-498).
+struct Bounds {
+  int nmin1, nmax1, nmin2, nmax2, nmin3, nmax3, nbound;
+};
+
+static Bounds make_bounds(const sw_genpar &g) {
+  Bounds b;
+  b.nmin1 = -g.ntaper + 1;
+  b.nmax1 = g.nz + g.ntaper;
+  b.nmin2 = -g.ntaper + 1;
+  b.nmax2 = g.nx + g.ntaper;
+  if (!g.twoD) {
+    b.nmin3 = -g.ntaper + 1;
+    b.nmax3 = g.ny + g.ntaper;
+    b.nbound = 4;
+  } else {
+    b.nmin3 = 1;
+    b.nmax3 = 1;
+    b.nbound = 0;
+  }
+  return b;
+}
+
+// A Fortran array u(nmin1-4:nmax1+4, nmin2-4:nmax2+4,
+// nmin3-nbound:nmax3+nbound), column major.
+template <class T> struct F3 {
+  std::vector<T> v;
+  int lo1 = 0, lo2 = 0, lo3 = 0, n1 = 0, n2 = 0, n3 = 0;
+  void init(const Bounds &b) {
+    lo1 = b.nmin1 - 4;
+    lo2 = b.nmin2 - 4;
+    lo3 = b.nmin3 - b.nbound;
+    n1 = b.nmax1 + 4 - lo1 + 1;
+    n2 = b.nmax2 + 4 - lo2 + 1;
+    n3 = b.nmax3 + b.nbound - lo3 + 1;
+    v.assign((size_t)n1 * n2 * n3, T(0));
+  }
+  inline T &operator()(int i, int j, int k) {
+    return v[(size_t)(i - lo1) +
+             (size_t)n1 * ((size_t)(j - lo2) + (size_t)n2 * (size_t)(k - lo3))];
+  }
+  inline T operator()(int i, int j, int k) const {
+    return v[(size_t)(i - lo1) +
+             (size_t)n1 * ((size_t)(j - lo2) + (size_t)n2 * (size_t)(k - lo3))];
+  }
+};
+
+// model_pad (libs/libwave/ReadSouVelRho.f90:545-596): copy the nz*nx*ny
+// window into (1:nz,1:nx,1:ny) and replicate the edges outwards.
+template <class T, class S>
+static void model_pad(const S *tmp, F3<T> &f, const Bounds &b, int nz, int nx,
+                      int ny, bool twoD) {
+  for (int k = 1; k <= ny; ++k)
+    for (int j = 1; j <= nx; ++j)
+      for (int i = 1; i <= nz; ++i)
+        f(i, j, k) = (T)tmp[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * (k - 1))];
+  for (int k = 1; k <= ny; ++k)
+    for (int j = 1; j <= nx; ++j) {
+      for (int i = b.nmin1 - 4; i <= 0; ++i) f(i, j, k) = f(1, j, k);
+      for (int i = nz + 1; i <= b.nmax1 + 4; ++i) f(i, j, k) = f(nz, j, k);
+    }
+  for (int k = 1; k <= ny; ++k) {
+    for (int j = b.nmin2 - 4; j <= 0; ++j)
+      for (int i = b.nmin1 - 4; i <= b.nmax1 + 4; ++i) f(i, j, k) = f(i, 1, k);
+    for (int j = nx + 1; j <= b.nmax2 + 4; ++j)
+      for (int i = b.nmin1 - 4; i <= b.nmax1 + 4; ++i) f(i, j, k) = f(i, nx, k);
+  }
+  if (!twoD) {
+    for (int k = b.nmin3 - b.nbound; k <= 0; ++k)
+      for (int j = b.nmin2 - 4; j <= b.nmax2 + 4; ++j)
+        for (int i = b.nmin1 - 4; i <= b.nmax1 + 4; ++i) f(i, j, k) = f(i, j, 1);
+    for (int k = ny + 1; k <= b.nmax3 + b.nbound; ++k)
+      for (int j = b.nmin2 - 4; j <= b.nmax2 + 4; ++j)
+        for (int i = b.nmin1 - 4; i <= b.nmax1 + 4; ++i) f(i, j, k) = f(i, j, ny);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Coefficients (libs/libwave/FDcoefs.f90:25-36, FDtypes.f90:50-80)
+// ---------------------------------------------------------------------------
+template <class T> struct Coefs {
+  T c0x, c1x, c2x, c3x, c4x, c0y, c1y, c2y, c3y, c4y, c0z, c1z, c2z, c3z, c4z;
+};
+
+template <class T> static Coefs<T> make_coefs(const sw_genpar &g) {
+  // FD_acoustic_init_coefs: -205/72, 8/5, -1/5, 8/315, -1/560.
+  const T c0 = T(-205.) / T(72.), c1 = T(8.) / T(5), c2 = T(-1.) / T(5.),
+          c3 = T(8.) / T(315.), c4 = T(-1.) / T(560.);
+  // FD_types_assign_scaled_coefs, coefpower = 2 (scalar wave equation).
+  const T dxi = T(1.) / (T)g.dx, dyi = T(1.) / (T)g.dy, dzi = T(1.) / (T)g.dz;
+  const T px = dxi * dxi, py = dyi * dyi, pz = dzi * dzi;
+  Coefs<T> c;
+  c.c0x = c0 * px; c.c1x = c1 * px; c.c2x = c2 * px; c.c3x = c3 * px; c.c4x = c4 * px;
+  c.c0y = c0 * py; c.c1y = c1 * py; c.c2y = c2 * py; c.c3y = c3 * py; c.c4y = c4 * py;
+  c.c0z = c0 * pz; c.c1z = c1 * pz; c.c2z = c2 * pz; c.c3z = c3 * pz; c.c4z = c4 * pz;
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// Stencils (libs/libwave/FDderivatives.f90)
+// ---------------------------------------------------------------------------
+
+// FD_2nd_2D_derivatives_scalar_forward_grid (FDderivatives.f90:715-743).
+template <class T>
+static void stencil2d_fwd(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
+                          F3<T> &u3, const F3<T> &vel) {
+#pragma omp parallel for schedule(static)
+  for (int j = b.nmin2; j <= b.nmax2; ++j)
+    for (int i = b.nmin1; i <= b.nmax1; ++i) {
+      T tz = c.c0z * u2(i, j, 1);
+      tz = tz + c.c1z * (u2(i + 1, j, 1) + u2(i - 1, j, 1));
+      tz = tz + c.c2z * (u2(i + 2, j, 1) + u2(i - 2, j, 1));
+      tz = tz + c.c3z * (u2(i + 3, j, 1) + u2(i - 3, j, 1));
+      tz = tz + c.c4z * (u2(i + 4, j, 1) + u2(i - 4, j, 1));
+      T tx = c.c0x * u2(i, j, 1);
+      tx = tx + c.c1x * (u2(i, j + 1, 1) + u2(i, j - 1, 1));
+      tx = tx + c.c2x * (u2(i, j + 2, 1) + u2(i, j - 2, 1));
+      tx = tx + c.c3x * (u2(i, j + 3, 1) + u2(i, j - 3, 1));
+      tx = tx + c.c4x * (u2(i, j + 4, 1) + u2(i, j - 4, 1));
+      const T v = vel(i, j, 1);
+      u3(i, j, 1) = (v * v) * (tx + tz);
+    }
+}
+
+// FD_2nd_3D_derivatives_scalar_forward_grid (FDderivatives.f90:97-131).
+template <class T>
+static void stencil3d_fwd(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
+                          F3<T> &u3, const F3<T> &vel) {
+#pragma omp parallel for schedule(static)
+  for (int k = b.nmin3; k <= b.nmax3; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        T tz = c.c0z * u2(i, j, k);
+        tz = tz + c.c1z * (u2(i + 1, j, k) + u2(i - 1, j, k));
+        tz = tz + c.c2z * (u2(i + 2, j, k) + u2(i - 2, j, k));
+        tz = tz + c.c3z * (u2(i + 3, j, k) + u2(i - 3, j, k));
+        tz = tz + c.c4z * (u2(i + 4, j, k) + u2(i - 4, j, k));
+        T tx = c.c0x * u2(i, j, k);
+        tx = tx + c.c1x * (u2(i, j + 1, k) + u2(i, j - 1, k));
+        tx = tx + c.c2x * (u2(i, j + 2, k) + u2(i, j - 2, k));
+        tx = tx + c.c3x * (u2(i, j + 3, k) + u2(i, j - 3, k));
+        tx = tx + c.c4x * (u2(i, j + 4, k) + u2(i, j - 4, k));
+        T ty = c.c0y * u2(i, j, k);
+        ty = ty + c.c1y * (u2(i, j, k + 1) + u2(i, j, k - 1));
+        ty = ty + c.c2y * (u2(i, j, k + 2) + u2(i, j, k - 2));
+        ty = ty + c.c3y * (u2(i, j, k + 3) + u2(i, j, k - 3));
+        ty = ty + c.c4y * (u2(i, j, k + 4) + u2(i, j, k - 4));
+        const T v = vel(i, j, k);
+        u3(i, j, k) = (v * v) * ((tx + tz) + ty);
+      }
+}
+
+// FD_2nd_2D_derivatives_scalar_adjoint_grid (FDderivatives.f90:847-891):
+// u3 = Laplacian(v^2 u2) with the vel index clamped to the compute domain.
+template <class T>
+static void stencil2d_adj(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
+                          F3<T> &u3, const F3<T> &vel) {
+#pragma omp parallel for schedule(static)
+  for (int j = b.nmin2; j <= b.nmax2; ++j) {
+    int jp[5], jm[5];
+    for (int l = 1; l <= 4; ++l) {
+      jp[l] = std::min(b.nmax2, j + l);
+      jm[l] = std::max(b.nmin2, j - l);
+    }
+    for (int i = b.nmin1; i <= b.nmax1; ++i) {
+      int ip[5], im[5];
+      for (int l = 1; l <= 4; ++l) {
+        ip[l] = std::min(b.nmax1, i + l);
+        im[l] = std::max(b.nmin1, i - l);
+      }
+      auto w = [&](int ii, int jj, int vi, int vj) -> T {
+        const T v = vel(vi, vj, 1);
+        return (v * v) * u2(ii, jj, 1);
+      };
+      T tz = c.c0z * w(i, j, i, j);
+      tz = tz + c.c1z * (w(i + 1, j, ip[1], j) + w(i - 1, j, im[1], j));
+      tz = tz + c.c2z * (w(i + 2, j, ip[2], j) + w(i - 2, j, im[2], j));
+      tz = tz + c.c3z * (w(i + 3, j, ip[3], j) + w(i - 3, j, im[3], j));
+      tz = tz + c.c4z * (w(i + 4, j, ip[4], j) + w(i - 4, j, im[4], j));
+      T tx = c.c0x * w(i, j, i, j);
+      tx = tx + c.c1x * (w(i, j + 1, i, jp[1]) + w(i, j - 1, i, jm[1]));
+      tx = tx + c.c2x * (w(i, j + 2, i, jp[2]) + w(i, j - 2, i, jm[2]));
+      tx = tx + c.c3x * (w(i, j + 3, i, jp[3]) + w(i, j - 3, i, jm[3]));
+      tx = tx + c.c4x * (w(i, j + 4, i, jp[4]) + w(i, j - 4, i, jm[4]));
+      u3(i, j, 1) = tx + tz;
+    }
+  }
+}
+
+// FD_2nd_3D_derivatives_scalar_adjoint_grid (FDderivatives.f90:780-819):
+// tmp = vel**2 * u2 over the whole padded array, then the Laplacian.
+template <class T>
+static void stencil3d_adj(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
+                          F3<T> &u3, const F3<T> &vel, F3<T> &tmp) {
+  const size_t n = u2.v.size();
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < n; ++q) {
+    const T v = vel.v[q];
+    tmp.v[q] = (v * v) * u2.v[q];
+  }
+#pragma omp parallel for schedule(static)
+  for (int k = b.nmin3; k <= b.nmax3; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        T tz = c.c0z * tmp(i, j, k);
+        tz = tz + c.c1z * (tmp(i + 1, j, k) + tmp(i - 1, j, k));
+        tz = tz + c.c2z * (tmp(i + 2, j, k) + tmp(i - 2, j, k));
+        tz = tz + c.c3z * (tmp(i + 3, j, k) + tmp(i - 3, j, k));
+        tz = tz + c.c4z * (tmp(i + 4, j, k) + tmp(i - 4, j, k));
+        T tx = c.c0x * tmp(i, j, k);
+        tx = tx + c.c1x * (tmp(i, j + 1, k) + tmp(i, j - 1, k));
+        tx = tx + c.c2x * (tmp(i, j + 2, k) + tmp(i, j - 2, k));
+        tx = tx + c.c3x * (tmp(i, j + 3, k) + tmp(i, j - 3, k));
+        tx = tx + c.c4x * (tmp(i, j + 4, k) + tmp(i, j - 4, k));
+        T ty = c.c0y * tmp(i, j, k);
+        ty = ty + c.c1y * (tmp(i, j, k + 1) + tmp(i, j, k - 1));
+        ty = ty + c.c2y * (tmp(i, j, k + 2) + tmp(i, j, k - 2));
+        ty = ty + c.c3y * (tmp(i, j, k + 3) + tmp(i, j, k - 3));
+        ty = ty + c.c4y * (tmp(i, j, k + 4) + tmp(i, j, k - 4));
+        u3(i, j, k) = (tx + tz) + ty;
+      }
+}
+
+// FD_2nd_time_derivative_grid (FDderivatives.f90:960-982):
+// u3 = (20 u2 - 6 u1 - 4 u0 + u_1 + 12 dt^2 u3) / 11 on the compute domain.
+template <class T>
+static void time_update(const Bounds &b, T dt, const F3<T> &u2, const F3<T> &u1,
+                        const F3<T> &u0, const F3<T> &um1, F3<T> &u3) {
+  const T div11 = T(1.) / T(11);
+  const T dt2 = dt * dt;
+  const T k12 = T(12.) * dt2;
+#pragma omp parallel for schedule(static)
+  for (int k = b.nmin3; k <= b.nmax3; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        T a = T(20.) * u2(i, j, k);
+        a = a - T(6.) * u1(i, j, k);
+        a = a - T(4.) * u0(i, j, k);
+        a = a + um1(i, j, k);
+        a = a + k12 * u3(i, j, k);
+        u3(i, j, k) = a * div11;
+      }
+}
+
+// ---------------------------------------------------------------------------
+// Higdon absorbing boundary (libs/libwave/Boundary.f90)
+// ---------------------------------------------------------------------------
+
+// Higdon_coeff (Boundary.f90:66-87), beta1 = 1, beta2 = 0.7, weight = 0.5.
+template <class T> static void higdon_coeff(T nu, T *coeff) {
+  const T beta1 = T(1.0), beta2 = T(0.7), weight = T(0.5);
+  T fdum = (beta1 + nu) * (T(1) - weight);
+  const T qx = (weight * (beta1 + nu) - nu) / fdum;
+  const T qt = (weight * (beta1 + nu) - beta1) / fdum;
+  const T qxt = weight / (weight - T(1));
+  fdum = (beta2 + nu) * (T(1) - weight);
+  const T rx = (weight * (beta2 + nu) - nu) / fdum;
+  const T rt = (weight * (beta2 + nu) - beta2) / fdum;
+  const T rxt = weight / (weight - T(1));
+  coeff[0] = qx + rx;
+  coeff[1] = qx * rx;
+  coeff[2] = qt + rt;
+  coeff[3] = ((qx * rt + qt * rx) + qxt) + rxt;
+  coeff[4] = qx * rxt + rx * qxt;
+  coeff[5] = qt * rt;
+  coeff[6] = qt * rxt + rt * qxt;
+  coeff[7] = qxt * rxt;
+}
+
+template <class T> struct Higdon {
+  // gz(16, nmin2:nmax2, nmin3:nmax3), gx(16, nmin1:nmax1, nmin3:nmax3),
+  // gy(16, nmin1:nmax1, nmin2:nmax2) (Propagator.f90:152-154).
+  std::vector<T> gz, gx, gy;
+  int n1, n2, n3;
+  Bounds b;
+  T *Gz(int j, int k) { return &gz[16 * ((size_t)(j - b.nmin2) + (size_t)n2 * (k - b.nmin3))]; }
+  T *Gx(int i, int k) { return &gx[16 * ((size_t)(i - b.nmin1) + (size_t)n1 * (k - b.nmin3))]; }
+  T *Gy(int i, int j) { return &gy[16 * ((size_t)(i - b.nmin1) + (size_t)n1 * (j - b.nmin2))]; }
+};
+
+// Higdon (Boundary.f90:17-63).
+template <class T>
+static void higdon_init(Higdon<T> &h, const Bounds &b, const F3<T> &vel, T dt,
+                        const sw_genpar &g) {
+  h.b = b;
+  h.n1 = b.nmax1 - b.nmin1 + 1;
+  h.n2 = b.nmax2 - b.nmin2 + 1;
+  h.n3 = b.nmax3 - b.nmin3 + 1;
+  h.gz.assign(16 * (size_t)h.n2 * h.n3, T(0));
+  h.gx.assign(16 * (size_t)h.n1 * h.n3, T(0));
+  h.gy.assign(16 * (size_t)h.n1 * h.n2, T(0));
+  const T dxi = T(1.) / (T)g.dx, dyi = T(1.) / (T)g.dy, dzi = T(1.) / (T)g.dz;
+  for (int k = b.nmin3; k <= b.nmax3; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      higdon_coeff<T>((vel(b.nmin1, j, k) * dt) * dzi, h.Gz(j, k));
+      higdon_coeff<T>((vel(b.nmax1, j, k) * dt) * dzi, h.Gz(j, k) + 8);
+    }
+  for (int k = b.nmin3; k <= b.nmax3; ++k)
+    for (int i = b.nmin1; i <= b.nmax1; ++i) {
+      higdon_coeff<T>((vel(i, b.nmin2, k) * dt) * dxi, h.Gx(i, k));
+      higdon_coeff<T>((vel(i, b.nmax2, k) * dt) * dxi, h.Gx(i, k) + 8);
+    }
+  if (b.nmax3 > 1)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        higdon_coeff<T>((vel(i, j, b.nmin3) * dt) * dyi, h.Gy(i, j));
+        higdon_coeff<T>((vel(i, j, b.nmax3) * dt) * dyi, h.Gy(i, j) + 8);
+      }
+}
+
+// Higdon_factor (Boundary.f90:366-447) called from Boundary_3d as
+// (u0, u1, u2) = (grid%u1, grid%u2, grid%u3).  a/b/c are the three time
+// levels along the line at offsets 0, s, 2s.
+template <class T>
+static inline T higdon_sum(const T *g, T u3p1, T u3p2, T u2p0, T u2p1, T u2p2,
+                           T u1p0, T u1p1, T u1p2) {
+  T f = g[0] * u3p1;
+  f = f + g[1] * u3p2;
+  f = f + g[2] * u2p0;
+  f = f + g[3] * u2p1;
+  f = f + g[4] * u2p2;
+  f = f + g[5] * u1p0;
+  f = f + g[6] * u1p1;
+  f = f + g[7] * u1p2;
+  return -f;
+}
+
+// Boundary_3d (Boundary.f90:89-184) for surf_type = 0 (nz0 = nmin1).
+template <class T>
+static void boundary(Higdon<T> &h, const Bounds &b, const F3<T> &u1,
+                     const F3<T> &u2, F3<T> &u3) {
+  const int nst = 3;
+  const int nz0 = b.nmin1;
+#pragma omp parallel for schedule(static)
+  for (int k = b.nmin3; k <= b.nmax3; ++k) {
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      const T *g = h.Gz(j, k);
+      for (int i = nz0 + nst; i >= b.nmin1 - 4; --i)
+        u3(i, j, k) = higdon_sum(g, u3(i + 1, j, k), u3(i + 2, j, k), u2(i, j, k),
+                                 u2(i + 1, j, k), u2(i + 2, j, k), u1(i, j, k),
+                                 u1(i + 1, j, k), u1(i + 2, j, k));
+      for (int i = b.nmax1 - nst; i <= b.nmax1 + 4; ++i)
+        u3(i, j, k) = higdon_sum(g + 8, u3(i - 1, j, k), u3(i - 2, j, k), u2(i, j, k),
+                                 u2(i - 1, j, k), u2(i - 2, j, k), u1(i, j, k),
+                                 u1(i - 1, j, k), u1(i - 2, j, k));
+    }
+    for (int j = b.nmin2 + nst; j >= b.nmin2 - 4; --j)
+      for (int i = nz0; i <= b.nmax1; ++i) {
+        const T *g = h.Gx(i, k);
+        u3(i, j, k) = higdon_sum(g, u3(i, j + 1, k), u3(i, j + 2, k), u2(i, j, k),
+                                 u2(i, j + 1, k), u2(i, j + 2, k), u1(i, j, k),
+                                 u1(i, j + 1, k), u1(i, j + 2, k));
+      }
+    for (int j = b.nmax2 - nst; j <= b.nmax2 + 4; ++j)
+      for (int i = nz0; i <= b.nmax1; ++i) {
+        const T *g = h.Gx(i, k) + 8;
+        u3(i, j, k) = higdon_sum(g, u3(i, j - 1, k), u3(i, j - 2, k), u2(i, j, k),
+                                 u2(i, j - 1, k), u2(i, j - 2, k), u1(i, j, k),
+                                 u1(i, j - 1, k), u1(i, j - 2, k));
+      }
+  }
+  if (b.nbound > 0) {
+#pragma omp parallel for schedule(static)
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      for (int k = b.nmin3 + nst; k >= b.nmin3 - 4; --k)
+        for (int i = nz0; i <= b.nmax1; ++i) {
+          const T *g = h.Gy(i, j);
+          u3(i, j, k) = higdon_sum(g, u3(i, j, k + 1), u3(i, j, k + 2), u2(i, j, k),
+                                   u2(i, j, k + 1), u2(i, j, k + 2), u1(i, j, k),
+                                   u1(i, j, k + 1), u1(i, j, k + 2));
+        }
+      for (int k = b.nmax3 - nst; k <= b.nmax3 + 4; ++k)
+        for (int i = nz0; i <= b.nmax1; ++i) {
+          const T *g = h.Gy(i, j) + 8;
+          u3(i, j, k) = higdon_sum(g, u3(i, j, k - 1), u3(i, j, k - 2), u2(i, j, k),
+                                   u2(i, j, k - 1), u2(i, j, k - 2), u1(i, j, k),
+                                   u1(i, j, k - 1), u1(i, j, k - 2));
+        }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sinc weights and positions
+// ---------------------------------------------------------------------------
+static inline float t_sin(float x) { return sinf(x); }
+static inline double t_sin(double x) { return sin(x); }
+static inline float t_cos(float x) { return cosf(x); }
+static inline double t_cos(double x) { return cos(x); }
+static inline long t_nint(float x) { return lroundf(x); }
+static inline long t_nint(double x) { return lround(x); }
+
+// mksinc (libs/libwave/Interpolate.f90:15-42).
+template <class T> static void mksinc(T *sinc, int lsinc, T shift) {
+  const T pi = T(3.141592654);
+  T fsum = T(0.);
+  for (int n = 1; n <= lsinc; ++n) {
+    T fact;
+    if (n <= (int)((T)(lsinc / 2 + 1) + shift))
+      fact = ((T)(n - 1) - shift) / (T)(lsinc / 2);
+    else
+      fact = ((T)(lsinc - n) + shift) / (T)(lsinc / 2);
+    if (fact <= T(0.)) fact = T(0.);
+    const T pos = pi * ((T)(n - (lsinc / 2 + 1)) - shift);
+    if (std::fabs(pos) > T(0.005f))
+      sinc[n - 1] = (fact * t_sin(pos)) / pos;
+    else
+      sinc[n - 1] = fact * (T(1.) - (pos * pos) / T(6.));
+    fsum = fsum + sinc[n - 1];
+  }
+  for (int n = 1; n <= lsinc; ++n) sinc[n - 1] = sinc[n - 1] / fsum;
+}
+
+// find_i_d (libs/libwave/ModelSpaceTypes.f90:144-151).
+template <class T>
+static void find_i_d(int &ielev, T &delev, T elev, T orig, T delta) {
+  ielev = (int)t_nint((elev - orig) / delta) + 1;
+  delev = elev - (orig + (T)(ielev - 1) * delta);
+}
+
+template <class T> struct Pos {
+  int ic[3];
+  T dc[3];
+  std::vector<T> sz, sx, sy;   // sinc weights per axis
+};
+
+// ModelSpace_compute_xyz_positions (ModelSpaceTypes.f90:112-124) plus the
+// per-trace sinc weights of Injection_source_sinc_* / Extraction_1trace_*
+// (computed once: they do not depend on the time step).
+template <class T>
+static bool make_positions(const sw_genpar &g, const Bounds &b, int n,
+                           const T *coord, std::vector<Pos<T>> &out,
+                           bool need_sinc) {
+  out.resize(n);
+  const T om[3] = {(T)g.oz, (T)g.ox, (T)(g.twoD ? 0.f : g.oy)};
+  const T de[3] = {(T)g.dz, (T)g.dx, (T)(g.twoD ? 1.f : g.dy)};
+  const int half = g.lsinc / 2;
+  for (int r = 0; r < n; ++r) {
+    Pos<T> &p = out[r];
+    for (int a = 0; a < 3; ++a) find_i_d<T>(p.ic[a], p.dc[a], coord[3 * r + a], om[a], de[a]);
+    if (g.twoD && p.ic[2] != 1) return false;
+    const int hw = need_sinc ? half : 0;
+    if (p.ic[0] - hw < b.nmin1 - 4 || p.ic[0] + hw > b.nmax1 + 4) return false;
+    if (p.ic[1] - hw < b.nmin2 - 4 || p.ic[1] + hw > b.nmax2 + 4) return false;
+    if (!g.twoD && (p.ic[2] - hw < b.nmin3 - 4 || p.ic[2] + hw > b.nmax3 + 4)) return false;
+    if (need_sinc) {
+      p.sz.resize(g.lsinc);
+      p.sx.resize(g.lsinc);
+      p.sy.resize(g.lsinc);
+      mksinc<T>(p.sz.data(), g.lsinc, p.dc[0] / de[0]);
+      mksinc<T>(p.sx.data(), g.lsinc, p.dc[1] / de[1]);
+      mksinc<T>(p.sy.data(), g.lsinc, p.dc[2] / de[2]);
+    }
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Tapers (libs/libwave/Taper.f90:14-44)
+// ---------------------------------------------------------------------------
+template <class T> static void cos_sin_taper(std::vector<T> &a, int ntaper, int n) {
+  const T pi = T(3.14159265359);
+  const int m = std::min(ntaper, n);
+  for (int i = 1; i <= m; ++i) {
+    const T s = t_sin((pi * (T)(i - 1)) / (T)(2 * (m - 1)));
+    a[i - 1] = s * s;
+  }
+  const int i0 = std::max(1, n - ntaper);
+  for (int i = i0; i <= n; ++i) {
+    const T c = t_cos((pi * (T)(i - i0)) / (T)(2 * ntaper));
+    a[i - 1] = c * c;
+  }
+}
+
+template <class T>
+static void compute_taper(int nxw, int nyw, std::vector<T> &tx, std::vector<T> &ty) {
+  tx.assign(nxw, T(1.));
+  ty.assign(nyw, T(1.));
+  cos_sin_taper(tx, std::min(nxw / 2, 10), nxw);
+  if (nyw > 1) cos_sin_taper(ty, std::min(nyw / 2, 10), nyw);
+}
+
+// ---------------------------------------------------------------------------
+// propagator_acoustic (libs/libwave/Propagator.f90:27-270)
+// ---------------------------------------------------------------------------
+template <class T> struct IO {
+  const T *vel;
+  int nsou;
+  const T *sou_coord;
+  const T *sou_trace;
+  int nrec;
+  const T *rec_coord;
+  T *rec_trace;
+  T *wave;
+  T *image;
+  T *illum;
+  const T *ref;
+  T *final_u2;
+};
+
+static int check_genpar(const sw_genpar &g) {
+  if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0) return SW_UNSUPPORTED;
+  if (g.nz < 1 || g.nx < 1 || g.ny < 1 || g.nt < 1 || g.ntaper < 1 || g.snapi < 1)
+    return SW_BAD_PARAM;
+  if (g.lsinc < 3 || (g.lsinc % 2) == 0) return SW_BAD_PARAM;
+  if (g.twoD && g.ny != 1) return SW_BAD_PARAM;
+  if (!(g.dz > 0.f) || !(g.dx > 0.f) || (!g.twoD && !(g.dy > 0.f)) || !(g.dt > 0.f))
+    return SW_BAD_PARAM;
+  return SW_OK;
+}
+
+template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) {
+  const sw_genpar &g = d.g;
+  int st = check_genpar(g);
+  if (st) return st;
+  if (d.tstep != 1 && d.tstep != -1) return SW_BAD_PARAM;
+  const Bounds b = make_bounds(g);
+  const int nt = g.nt;
+  const int ntsnap = nt / g.snapi;
+  const int nz = g.nz, nx = g.nx, ny = g.ny;
+
+  F3<T> vel, ua, ub, uc, ud, ue, tmp;
+  vel.init(b);
+  model_pad(io.vel, vel, b, nz, nx, ny, g.twoD != 0);
+  // allocateUSpace + zeroUSpace (Propagator.f90:144-145).
+  ua.init(b); ub.init(b); uc.init(b); ud.init(b); ue.init(b);
+  if (!g.twoD && d.fd_scheme == SW_FD_ADJOINT) tmp.init(b);
+  F3<T> *um1 = &ua, *u0 = &ub, *u1 = &uc, *u2 = &ud, *u3 = &ue;
+
+  const Coefs<T> c = make_coefs<T>(g);
+  Higdon<T> hig;
+  higdon_init(hig, b, vel, (T)g.dt, g);
+
+  std::vector<Pos<T>> spos, rpos;
+  const bool inj_sinc = d.injection == SW_INJ_SINC || d.injection == SW_INJ_LSRTM_SINC;
+  const bool ext_sinc = d.extraction == SW_EXT_SINC || d.extraction == SW_EXT_LSRTM_SINC ||
+                        d.extraction == SW_EXT_SINC_AFWI;
+  if (d.injection != SW_INJ_NONE && io.nsou > 0)
+    if (!make_positions<T>(g, b, io.nsou, io.sou_coord, spos, inj_sinc)) return SW_BAD_PARAM;
+  if (d.extraction != SW_EXT_NONE && io.nrec > 0)
+    if (!make_positions<T>(g, b, io.nrec, io.rec_coord, rpos, ext_sinc)) return SW_BAD_PARAM;
+
+  std::vector<T> taperx, tapery;
+  if (d.imaging != SW_IMG_NONE) compute_taper<T>(nx, ny, taperx, tapery);
+
+  const int half = g.lsinc / 2;
+  const T dprod2 = (T)g.dz * (T)g.dx;
+  const T inv_d2 = T(1) / dprod2;
+  const T inv_d3 = T(1) / (dprod2 * (T)g.dy);
+  const T xsnap = (T)g.dt * (T)g.snapi;
+  const T dt2snap = xsnap * xsnap;   // genpar%dt2 (compute_function_gradient.f90:237)
+  int wcounter = 0, mcounter = 0;
+
+  const size_t n3w = (size_t)nz * nx * ny;
+  auto W = [&](int i, int j, int k, int s) -> T & {
+    return io.wave[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * ((k - 1) + (size_t)ny * (s - 1)))];
+  };
+  auto M = [&](T *a, int i, int j, int k) -> T & {
+    return a[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * (k - 1))];
+  };
+  (void)n3w;
+
+  const int nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
+  int it = d.tmin;
+  for (int s = 0; s < nsteps; ++s, it += d.tstep) {
+    // ExtractData(u2) (Propagator.f90:176-178).
+    if (d.extraction != SW_EXT_NONE && io.nrec > 0) {
+      for (int r = 0; r < io.nrec; ++r) {
+        const Pos<T> &p = rpos[r];
+        T &tr = io.rec_trace[(size_t)r * nt + (it - 1)];
+        if (d.extraction == SW_EXT_SIMPLE_AFWI) {
+          // Extraction_array_simple_afwi_noomp (Extraction.f90:71-107).
+          tr = tr + (*u2)(p.ic[0], p.ic[1], g.twoD ? 1 : p.ic[2]);
+          continue;
+        }
+        T v;
+        if (d.extraction == SW_EXT_SINC) {
+          // Extraction_array_sinc: v**2 in 2D, v in 3D (Extraction.f90:120-131).
+          if (g.twoD) {
+            const T vv = vel(p.ic[0], p.ic[1], 1);
+            v = vv * vv;
+          } else {
+            v = vel(p.ic[0], p.ic[1], p.ic[2]);
+          }
+        } else if (d.extraction == SW_EXT_LSRTM_SINC) {
+          v = g.twoD ? inv_d2 : inv_d3;   // Extraction.f90:232-243
+        } else {
+          v = T(1.);                       // Extraction.f90:137-162
+        }
+        if (g.twoD) {
+          // Extraction_1trace_sinc_xy (Extraction.f90:511-560).
+          for (int j = -half; j <= half; ++j)
+            for (int i = -half; i <= half; ++i)
+              tr = tr + ((v * (*u2)(i + p.ic[0], j + p.ic[1], 1)) * p.sz[half + i]) * p.sx[half + j];
+        } else {
+          // Extraction_1trace_sinc_xyz (Extraction.f90:276-337); the y
+          // weight is the x sinc column (sinc(maxy+1+k,2)).
+          for (int k = -half; k <= half; ++k)
+            for (int j = -half; j <= half; ++j)
+              for (int i = -half; i <= half; ++i)
+                tr = tr + (((v * (*u2)(i + p.ic[0], j + p.ic[1], k + p.ic[2])) * p.sz[half + i]) *
+                           p.sx[half + j]) * p.sx[half + k];
+        }
+      }
+    }
+    // ExtractWave(u2) = Extraction_wavefield (Extraction.f90:562-601).
+    if (d.extract_wave && (it % g.snapi) == 0) {
+      ++wcounter;
+      if (wcounter <= ntsnap) {
+        for (int k = 1; k <= ny; ++k)
+          for (int j = 1; j <= nx; ++j)
+            for (int i = 1; i <= nz; ++i) W(i, j, k, wcounter) = (*u2)(i, j, k);
+      }
+    }
+    // ImagingCondition(u2) for tstep = -1 (Propagator.f90:192-194).
+    if (d.imaging != SW_IMG_NONE && d.imaging != SW_IMG_BORN && d.tstep == -1 &&
+        (it % g.snapi) == 0) {
+      ++mcounter;
+      const int index = ntsnap - mcounter + 1;
+      if (index >= 1) {
+        const int ip1 = std::min(index + 1, ntsnap);
+        const int im1 = std::max(index - 1, 1);
+        for (int k = 1; k <= ny; ++k)
+          for (int j = 1; j <= nx; ++j) {
+            const T taper = taperx[j - 1] * tapery[k - 1];
+            for (int i = 1; i <= nz; ++i) {
+              const T u = (*u2)(i, j, k);
+              const T w = W(i, j, k, index);
+              T &im = M(io.image, i, j, k);
+              T &il = M(io.illum, i, j, k);
+              if (d.imaging == SW_IMG_RTM) {
+                // Imaging.f90:265-266
+                im = im + (u * w) * taper;
+              } else if (d.imaging == SW_IMG_LSRTM) {
+                // Imaging.f90:735-736
+                im = im + (((T(2) * taper) * u) * w) / vel(i, j, k);
+              } else {
+                // Imaging.f90:410-412
+                const T v = vel(i, j, k);
+                const T t = ((W(i, j, k, im1) - T(2) * w) + W(i, j, k, ip1)) /
+                            (dt2snap * ((v * v) * v));
+                im = im + (u * t) * taper;
+              }
+              il = il + (w * w) * taper;
+            }
+          }
+      }
+    }
+    // Boundary_set_free_surface_grid: no-op for surf_type = 0.
+    // FD_scheme(u2 -> u3) (Propagator.f90:202).
+    if (d.fd_scheme == SW_FD_FORWARD) {
+      if (g.twoD) stencil2d_fwd(c, b, *u2, *u3, vel);
+      else stencil3d_fwd(c, b, *u2, *u3, vel);
+    } else {
+      if (g.twoD) stencil2d_adj(c, b, *u2, *u3, vel);
+      else stencil3d_adj(c, b, *u2, *u3, vel, tmp);
+    }
+    // Injection(u3) (Propagator.f90:208-209).
+    if (d.injection != SW_INJ_NONE) {
+      for (int r = 0; r < io.nsou; ++r) {
+        const Pos<T> &p = spos[r];
+        const T tr = io.sou_trace[(size_t)r * nt + (it - 1)];
+        const int k1 = g.twoD ? 1 : p.ic[2];
+        if (d.injection == SW_INJ_SIMPLE) {
+          // Injection_simple_noomp + Injection_source_simple_xyz
+          // (Injection.f90:63-104,561-591).
+          const T vv = vel(p.ic[0], p.ic[1], k1);
+          const T v2r = vv * vv;
+          (*u3)(p.ic[0], p.ic[1], k1) = (*u3)(p.ic[0], p.ic[1], k1) + v2r * tr;
+          continue;
+        }
+        T v2r;
+        if (d.injection == SW_INJ_SINC) {
+          const T vv = vel(p.ic[0], p.ic[1], k1);
+          v2r = vv * vv;
+        } else {
+          v2r = g.twoD ? inv_d2 : inv_d3;   // Injection.f90:258-270
+        }
+        const T a = v2r * tr;
+        if (g.twoD) {
+          // Injection_source_sinc_xz (Injection.f90:402-456).
+          for (int j = -half; j <= half; ++j)
+            for (int i = -half; i <= half; ++i) {
+              T &u = (*u3)(i + p.ic[0], j + p.ic[1], 1);
+              u = u + (a * p.sz[half + i]) * p.sx[half + j];
+            }
+        } else {
+          // Injection_source_sinc_xyz (Injection.f90:274-338), x sinc on y.
+          for (int k = -half; k <= half; ++k)
+            for (int j = -half; j <= half; ++j)
+              for (int i = -half; i <= half; ++i) {
+                T &u = (*u3)(i + p.ic[0], j + p.ic[1], k + p.ic[2]);
+                u = u + ((a * p.sz[half + i]) * p.sx[half + j]) * p.sx[half + k];
+              }
+        }
+      }
+    }
+    // Born secondary source on u3 for tstep = +1 (Propagator.f90:212-214,
+    // Injection_Born Imaging.f90:747-788).
+    if (d.imaging == SW_IMG_BORN && d.tstep == 1 && (it % g.snapi) == 0) {
+      ++mcounter;
+      if (mcounter <= ntsnap) {
+        for (int k = 1; k <= ny; ++k)
+          for (int j = 1; j <= nx; ++j) {
+            const T taper = taperx[j - 1] * tapery[k - 1];
+            for (int i = 1; i <= nz; ++i) {
+              T &u = (*u3)(i, j, k);
+              const T rf = io.ref[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * (k - 1))];
+              u = u + (((T(2) * taper) * rf) * W(i, j, k, mcounter)) / vel(i, j, k);
+            }
+          }
+      }
+    }
+    // TimeDer (Propagator.f90:218), Higdon (Propagator.f90:222-228).
+    time_update(b, (T)g.dt, *u2, *u1, *u0, *um1, *u3);
+    boundary(hig, b, *u1, *u2, *u3);
+    // FDswaptime_pointer (FDswaptimes.f90:14-24).
+    F3<T> *t = um1;
+    um1 = u0; u0 = u1; u1 = u2; u2 = u3; u3 = t;
+  }
+  if (io.final_u2) std::memcpy(io.final_u2, u2->v.data(), u2->v.size() * sizeof(T));
+  return SW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drivers
+// ---------------------------------------------------------------------------
+template <class T>
+static sw_prop_desc base_desc(const sw_genpar &g, int fwd) {
+  sw_prop_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.g = g;
+  if (fwd) { d.tmin = 1; d.tmax = g.nt; d.tstep = 1; }
+  else { d.tmin = g.nt; d.tmax = 1; d.tstep = -1; }
+  return d;
+}
+
+template <class T>
+static int modeling(const sw_genpar &g, const T *vel, const T *sou_coord,
+                    const T *wavelet, int nrec, const T *rec_coord, T *data,
+                    T *final_u2) {
+  // progs/modeling/Acoustic_modeling.f90:115-123.
+  sw_prop_desc d = base_desc<T>(g, 1);
+  d.fd_scheme = SW_FD_FORWARD;
+  d.injection = SW_INJ_SINC;
+  d.extraction = SW_EXT_SINC;
+  IO<T> io{};
+  io.vel = vel;
+  io.nsou = 1; io.sou_coord = sou_coord; io.sou_trace = wavelet;
+  io.nrec = nrec; io.rec_coord = rec_coord; io.rec_trace = data;
+  io.final_u2 = final_u2;
+  std::fill(data, data + (size_t)nrec * g.nt, T(0));
+  return propagate<T>(d, io);
+}
+
+template <class T>
+static int rtm_like(const sw_genpar &g, const T *vel, const T *sou_coord,
+                    const T *wavelet, int nrec, const T *rec_coord, const T *data,
+                    T *image, T *illum, bool lsrtm) {
+  // RTM_to_memory / LSRTM_to_memory (progs/rtm/to_disk_to_memory_RTM.f90:358-580).
+  const int ntsnap = g.nt / g.snapi;
+  const size_t n3 = (size_t)g.nz * g.nx * g.ny;
+  std::vector<T> wave(n3 * (size_t)std::max(ntsnap, 1), T(0));
+  sw_prop_desc d = base_desc<T>(g, 1);
+  d.fd_scheme = SW_FD_FORWARD;
+  d.injection = SW_INJ_SINC;
+  d.extract_wave = 1;
+  IO<T> io{};
+  io.vel = vel;
+  io.nsou = 1; io.sou_coord = sou_coord; io.sou_trace = wavelet;
+  io.wave = wave.data();
+  int st = propagate<T>(d, io);
+  if (st) return st;
+  std::fill(image, image + n3, T(0));
+  std::fill(illum, illum + n3, T(0));
+  sw_prop_desc b = base_desc<T>(g, 0);
+  if (lsrtm) {
+    b.fd_scheme = SW_FD_ADJOINT;
+    b.injection = SW_INJ_LSRTM_SINC;
+    b.imaging = SW_IMG_LSRTM;
+  } else {
+    b.fd_scheme = g.twoD ? SW_FD_ADJOINT : SW_FD_FORWARD;
+    b.injection = SW_INJ_SINC;
+    b.imaging = SW_IMG_RTM;
+  }
+  IO<T> jo{};
+  jo.vel = vel;
+  jo.nsou = nrec; jo.sou_coord = rec_coord; jo.sou_trace = data;
+  jo.wave = wave.data();
+  jo.image = image; jo.illum = illum;
+  return propagate<T>(b, jo);
+}
+
+template <class T>
+static int born(const sw_genpar &g, const T *vel, const T *ref, const T *sou_coord,
+                const T *wavelet, int nrec, const T *rec_coord, T *data) {
+  // BORN_to_memory (progs/modeling/to_disk_to_memory_BORN.f90:123-220).
+  const int ntsnap = g.nt / g.snapi;
+  const size_t n3 = (size_t)g.nz * g.nx * g.ny;
+  std::vector<T> wave(n3 * (size_t)std::max(ntsnap, 1), T(0));
+  sw_prop_desc d = base_desc<T>(g, 1);
+  d.fd_scheme = SW_FD_FORWARD;
+  d.injection = SW_INJ_SINC;
+  d.extract_wave = 1;
+  IO<T> io{};
+  io.vel = vel;
+  io.nsou = 1; io.sou_coord = sou_coord; io.sou_trace = wavelet;
+  io.wave = wave.data();
+  int st = propagate<T>(d, io);
+  if (st) return st;
+  std::fill(data, data + (size_t)nrec * g.nt, T(0));
+  sw_prop_desc b = base_desc<T>(g, 1);
+  b.fd_scheme = SW_FD_FORWARD;
+  b.injection = SW_INJ_NONE;     // no sou: Injection is never called
+  b.extraction = SW_EXT_LSRTM_SINC;
+  b.imaging = SW_IMG_BORN;
+  IO<T> jo{};
+  jo.vel = vel;
+  jo.nrec = nrec; jo.rec_coord = rec_coord; jo.rec_trace = data;
+  jo.wave = wave.data();
+  jo.ref = ref;
+  return propagate<T>(b, jo);
+}
+
+// ---------------------------------------------------------------------------
+// FWI objective / gradient
+// ---------------------------------------------------------------------------
+
+// triangle / boxconv (libs/libwave/Smoothing.f90:140-229).
+static void boxconv(int nb, int nx, const float *xx, float *yy) {
+  const int ny = nx + nb - 1;
+  std::vector<float> bb(nx + nb, 0.f);
+  bb[0] = xx[0];
+  for (int i = 2; i <= nx; ++i) bb[i - 1] = bb[i - 2] + xx[i - 1];
+  for (int i = nx + 1; i <= ny; ++i) bb[i - 1] = bb[i - 2];
+  for (int i = 1; i <= nb; ++i) yy[i - 1] = bb[i - 1];
+  for (int i = nb + 1; i <= ny; ++i) yy[i - 1] = bb[i - 1] - bb[i - nb - 1];
+  for (int i = 1; i <= ny; ++i) yy[i - 1] = yy[i - 1] / (float)nb;
+}
+
+static void triangle(int nr, int n12, const float *uu, float *vv) {
+  std::vector<float> pp(n12 + nr - 1), qq(n12 + 2 * nr - 1), tt(n12);
+  for (int i = 0; i < n12; ++i) qq[i] = uu[i];
+  if (n12 == 1) {
+    tt[0] = qq[0];
+  } else {
+    boxconv(nr, n12, qq.data(), pp.data());
+    const int np = nr + n12 - 1;
+    boxconv(nr, np, pp.data(), qq.data());
+    for (int i = 1; i <= n12; ++i) tt[i - 1] = qq[i + nr - 2];
+    for (int i = 1; i <= nr - 1; ++i) tt[i - 1] = tt[i - 1] + qq[nr - i - 1];
+    for (int i = 1; i <= nr - 1; ++i)
+      tt[n12 - i] = tt[n12 - i] + qq[n12 + (nr - 1) + i - 1];
+  }
+  for (int i = 0; i < n12; ++i) vv[i] = tt[i];
+}
+
+// triangle2 (Smoothing.f90:87-138).  The reference's y pass uses rect1/n1
+// and its x pass copies uu=ss inside the i3 loop; both only matter in 3D and
+// read unset memory there, so the 3D passes use the intended rect3/n3 and a
+// single copy after the loop.
+static int triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2,
+                     int rect3, bool doz, bool dox, bool doy) {
+  auto U = [&](int i1, int i2, int i3) -> float & {
+    return uu[(size_t)i1 + (size_t)n1 * (i2 + (size_t)n2 * i3)];
+  };
+  if ((dox && (rect2 < 1 || rect2 > n2)) || (doz && (rect1 < 1 || rect1 > n1)) ||
+      (doy && (rect3 < 1 || rect3 > n3)))
+    return SW_BAD_PARAM;
+  std::vector<float> ss((size_t)n1 * n2 * n3);
+  std::vector<float> a, bq;
+  if (dox) {
+    a.resize(n2); bq.resize(n2);
+    for (int i3 = 0; i3 < n3; ++i3)
+      for (int i1 = 0; i1 < n1; ++i1) {
+        for (int i2 = 0; i2 < n2; ++i2) a[i2] = U(i1, i2, i3);
+        triangle(rect2, n2, a.data(), bq.data());
+        for (int i2 = 0; i2 < n2; ++i2) ss[(size_t)i1 + (size_t)n1 * (i2 + (size_t)n2 * i3)] = bq[i2];
+      }
+    std::memcpy(uu, ss.data(), ss.size() * sizeof(float));
+  }
+  if (doz) {
+    a.resize(n1); bq.resize(n1);
+    for (int i3 = 0; i3 < n3; ++i3)
+      for (int i2 = 0; i2 < n2; ++i2) {
+        triangle(rect1, n1, &U(0, i2, i3), bq.data());
+        for (int i1 = 0; i1 < n1; ++i1) ss[(size_t)i1 + (size_t)n1 * (i2 + (size_t)n2 * i3)] = bq[i1];
+      }
+    std::memcpy(uu, ss.data(), ss.size() * sizeof(float));
+  }
+  if (doy) {
+    a.resize(n3); bq.resize(n3);
+    for (int i2 = 0; i2 < n2; ++i2)
+      for (int i1 = 0; i1 < n1; ++i1) {
+        for (int i3 = 0; i3 < n3; ++i3) a[i3] = U(i1, i2, i3);
+        triangle(rect3, n3, a.data(), bq.data());
+        for (int i3 = 0; i3 < n3; ++i3) ss[(size_t)i1 + (size_t)n1 * (i2 + (size_t)n2 * i3)] = bq[i3];
+      }
+    std::memcpy(uu, ss.data(), ss.size() * sizeof(float));
+  }
+  return SW_OK;
+}
+
+// Shot window: extract_coord_source_receiver_patch
+// (ExtractPadModel.f90:19-85) and copy_window_vel_gath (ExtractPadModel.f90:
+// 395-507) with mod_window_pad(adj=.true.) (ExtractPadModel.f90:509-549).
+struct Window {
+  float oxw, oyw, endx, endy;
+  int nxw, nyw;
+};
+
+static int shot_window(const sw_fwi_desc &d, const sw_fwi_shot &s, Window &w) {
+  const sw_genpar &g = d.g;
+  const float sx = s.sou_coord[1], sy = s.sou_coord[2];
+  if (s.nrec < 1) return SW_BAD_PARAM;
+  float gx1 = s.rec_coord[1], gy1 = s.rec_coord[2], gxn = gx1, gyn = gy1;
+  for (int i = 1; i < s.nrec; ++i) {
+    gx1 = std::min(gx1, s.rec_coord[3 * i + 1]);
+    gxn = std::max(gxn, s.rec_coord[3 * i + 1]);
+    gy1 = std::min(gy1, s.rec_coord[3 * i + 2]);
+    gyn = std::max(gyn, s.rec_coord[3 * i + 2]);
+  }
+  const float minx = std::min(sx, gx1), miny = std::min(sy, gy1);
+  const float maxx = std::max(sx, gxn), maxy = std::max(sy, gyn);
+  const float mx1 = (gx1 + sx) / 2, mxn = (gxn + sx) / 2;
+  const float my1 = (gy1 + sy) / 2, myn = (gyn + sy) / 2;
+  const float cx = mx1 + std::fabs(mxn - mx1) / 2;
+  const float cy = my1 + std::fabs(myn - my1) / 2;
+  w.oxw = std::min(minx, cx - d.aperture_x / 2);
+  w.endx = std::max(maxx, cx + d.aperture_x / 2);
+  w.oyw = std::min(miny, cy - d.aperture_y / 2);
+  w.endy = std::max(maxy, cy + d.aperture_y / 2);
+  w.nxw = (int)lroundf((w.endx - w.oxw) / g.dx) + 1;
+  w.nyw = (int)lroundf((w.endy - w.oyw) / g.dy) + 1;
+  if (g.twoD) { w.nyw = 1; w.oyw = g.oy; }
+  return SW_OK;
+}
+
+static void window_vel(const sw_genpar &g, const Window &w, const float *big, float *small) {
+  for (int j = 1; j <= w.nyw; ++j) {
+    const float cy = (float)(j - 1) * g.dy + w.oyw;
+    const int iy = (int)lroundf((cy - g.oy) / g.dy) + 1;
+    const int iy1 = std::min(g.ny, std::max(1, iy));
+    for (int i = 1; i <= w.nxw; ++i) {
+      const float cx = (float)(i - 1) * g.dx + w.oxw;
+      const int ix = (int)lroundf((cx - g.ox) / g.dx) + 1;
+      const int ix1 = std::min(g.nx, std::max(1, ix));
+      for (int l = 0; l < g.nz; ++l)
+        small[(size_t)l + (size_t)g.nz * ((i - 1) + (size_t)w.nxw * (j - 1))] =
+            0.f + big[(size_t)l + (size_t)g.nz * ((ix1 - 1) + (size_t)g.nx * (iy1 - 1))];
+    }
+  }
+}
+
+// mod_copy_image (ExtractPadModel.f90:662-697).
+static void copy_image(const sw_genpar &g, const Window &w, const float *ims,
+                       const float *ils, float *image, float *illum) {
+  for (int j = 1; j <= w.nyw; ++j) {
+    const float cy = (float)(j - 1) * g.dy + w.oyw;
+    const int iy = (int)lroundf((cy - g.oy) / g.dy) + 1;
+    if (iy < 1 || iy > g.ny) continue;
+    for (int i = 1; i <= w.nxw; ++i) {
+      const float cx = (float)(i - 1) * g.dx + w.oxw;
+      const int ix = (int)lroundf((cx - g.ox) / g.dx) + 1;
+      if (ix < 1 || ix > g.nx) continue;
+      for (int l = 0; l < g.nz; ++l) {
+        const size_t o = (size_t)l + (size_t)g.nz * ((ix - 1) + (size_t)g.nx * (iy - 1));
+        const size_t s = (size_t)l + (size_t)g.nz * ((i - 1) + (size_t)w.nxw * (j - 1));
+        image[o] = image[o] + ims[s];
+        illum[o] = illum[o] + ils[s];
+      }
+    }
+  }
+}
+
+static int fwi_fct_gdt(const sw_fwi_desc &d, const float *vel, const float *wavelet,
+                       int nshot, const sw_fwi_shot *shots, const float *vpmask,
+                       double *f, float *grad, float *illum_out) {
+  const sw_genpar &G = d.g;
+  const size_t nfull = (size_t)G.nz * G.nx * G.ny;
+  const int nt = G.nt;
+  std::vector<float> gradacc(nfull, 0.f), illacc(nfull, 0.f);
+  double fsum = 0.;
+  long ntotaltraces = 0;
+  for (int is = 0; is < nshot; ++is) {
+    const sw_fwi_shot &s = shots[is];
+    Window w;
+    int st = shot_window(d, s, w);
+    if (st) return st;
+    sw_genpar g = G;
+    g.nx = w.nxw;
+    g.ny = w.nyw;
+    g.ox = w.oxw;
+    g.oy = w.oyw;
+    const size_t nw = (size_t)g.nz * g.nx * g.ny;
+    std::vector<float> vsmall(nw);
+    window_vel(G, w, vel, vsmall.data());
+    const int ntsnap = nt / g.snapi;
+    std::vector<float> wave(nw * (size_t)std::max(ntsnap, 1), 0.f);
+    std::vector<float> dmod((size_t)s.nrec * nt, 0.f);
+    // AMOD_to_memory (progs/afwi/to_disk_to_memory_AMOD.f90:27-82).
+    sw_prop_desc a = base_desc<float>(g, 1);
+    a.fd_scheme = SW_FD_FORWARD;
+    a.injection = SW_INJ_SINC;
+    a.extraction = SW_EXT_SIMPLE_AFWI;
+    a.extract_wave = 1;
+    IO<float> io{};
+    io.vel = vsmall.data();
+    io.nsou = 1; io.sou_coord = s.sou_coord; io.sou_trace = wavelet;
+    io.nrec = s.nrec; io.rec_coord = s.rec_coord; io.rec_trace = dmod.data();
+    io.wave = wave.data();
+    st = propagate<float>(a, io);
+    if (st) return st;
+    // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40),
+    // L2 norm (libs/libinv/Norm.f90:26-28,95-97).
+    for (int r = 0; r < s.nrec; ++r) {
+      float *dm = &dmod[(size_t)r * nt];
+      const float *dob = &s.dobs[(size_t)r * nt];
+      const float *mu = s.mute ? &s.mute[(size_t)r * nt] : nullptr;
+      double ssum = 0.;
+      for (int t = 0; t < nt; ++t) {
+        const float m = mu ? mu[t] : 1.f;
+        dm[t] = m * (dob[t] - dm[t]);
+        ssum = ssum + (double)dm[t] * (double)dm[t];
+      }
+      fsum = fsum + ssum / 2;
+      if (s.resid) std::memcpy(&s.resid[(size_t)r * nt], dm, sizeof(float) * nt);
+      for (int t = 0; t < nt; ++t) {
+        const float m = mu ? mu[t] : 1.f;
+        dm[t] = m * dm[t];
+      }
+    }
+    ntotaltraces += s.nrec;
+    // AGRAD_to_memory (progs/afwi/to_disk_to_memory_AGRAD.f90:27-79).
+    std::vector<float> ims(nw, 0.f), ils(nw, 0.f);
+    sw_prop_desc b = base_desc<float>(g, 0);
+    b.fd_scheme = SW_FD_FORWARD;
+    b.injection = SW_INJ_SIMPLE;
+    b.imaging = SW_IMG_AFWI;
+    IO<float> jo{};
+    jo.vel = vsmall.data();
+    jo.nsou = s.nrec; jo.sou_coord = s.rec_coord; jo.sou_trace = dmod.data();
+    jo.wave = wave.data();
+    jo.image = ims.data(); jo.illum = ils.data();
+    st = propagate<float>(b, jo);
+    if (st) return st;
+    copy_image(G, w, ims.data(), ils.data(), gradacc.data(), illacc.data());
+  }
+  // Post-processing (compute_function_gradient.f90:314-343).
+  for (size_t q = 0; q < nfull; ++q) {
+    if (d.illu_pow != 1.f) illacc[q] = powf(illacc[q], d.illu_pow);
+  }
+  const double scaling = (double)(2 * (long)nt * ntotaltraces);
+  fsum = fsum / scaling;
+  const float sscal = (float)scaling;
+  float maxil = illacc[0];
+  double ss = 0.;
+  for (size_t q = 0; q < nfull; ++q) {
+    gradacc[q] = (2.f * gradacc[q]) / sscal;
+    maxil = std::max(maxil, illacc[q]);
+    ss = ss + (double)illacc[q] * (double)illacc[q];
+  }
+  const double rmsil = std::sqrt(ss / (double)nfull);
+  for (size_t q = 0; q < nfull; ++q) {
+    illacc[q] = (float)((double)(illacc[q] + maxil / 10000.f) / rmsil);
+    gradacc[q] = gradacc[q] / illacc[q];
+    gradacc[q] = gradacc[q] * (vpmask ? vpmask[q] : 1.f);
+  }
+  int st = triangle2(gradacc.data(), G.nz, G.nx, G.ny, d.smooth_rect1, d.smooth_rect2,
+                     d.smooth_rect3, d.smooth_doz != 0, d.smooth_dox != 0,
+                     d.smooth_doy != 0);
+  if (st) return st;
+  for (size_t q = 0; q < nfull; ++q) gradacc[q] = gradacc[q] * (vpmask ? vpmask[q] : 1.f);
+  *f = fsum;
+  std::memcpy(grad, gradacc.data(), nfull * sizeof(float));
+  if (illum_out) std::memcpy(illum_out, illacc.data(), nfull * sizeof(float));
+  return SW_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// L-BFGS (libs/libinv/lbfgs.f)
+// ---------------------------------------------------------------------------
+struct or_lbfgs {
+  int n, m;
+  double xmin, xmax;
+  std::vector<float> mask;
+  int boundt;
+  bool type;
+  std::vector<double> xinit;
+  std::vector<double> w;     // 1-based, N*(2M+1)+2M
+  std::vector<double> diag;  // 1-based
+  // LBFGS SAVE state
+  int iter = 0, nfun = 0, point = 0, ispt = 0, iypt = 0, npt = 0, bound = 0, info = 0,
+      nfev = 0, maxfev = 20, cp = 0;
+  double stp = 0, stp1 = 0, ftol = 1e-4, gnorm = 0, xnorm = 0, ys = 0, yy = 0;
+  bool finish = false;
+  // MCSRCH SAVE state
+  int infoc = 0;
+  bool brackt = false, stage1 = true;
+  double dg = 0, dgm = 0, dginit = 0, dgtest = 0, dgx = 0, dgxm = 0, dgy = 0, dgym = 0,
+         finit = 0, ftest1 = 0, fm = 0, fx = 0, fxm = 0, fy = 0, fym = 0, stx = 0, sty = 0,
+         stmin = 0, stmax = 0, width = 0, width1 = 0;
+};
+
+namespace {
+// COMMON /LB3/ from BLOCK DATA LB2 (lbfgs.f:636-641).
+const double kGTOL = 0.9, kSTPMIN = 1.0e-20, kSTPMAX = 1.0e+20;
+
+// ddot with the reference's unroll-by-5 summation order (blas.f:58-90).
+double ddot(int n, const double *dx, const double *dy) {
+  double dtemp = 0.0;
+  if (n <= 0) return 0.0;
+  const int m = n % 5;
+  for (int i = 0; i < m; ++i) dtemp = dtemp + dx[i] * dy[i];
+  if (n < 5) return dtemp;
+  for (int i = m; i < n; i += 5)
+    dtemp = dtemp + dx[i] * dy[i] + dx[i + 1] * dy[i + 1] + dx[i + 2] * dy[i + 2] +
+            dx[i + 3] * dy[i + 3] + dx[i + 4] * dy[i + 4];
+  return dtemp;
+}
+
+// FREEZE_X (lbfgs.f:1-43).
+void freeze_x(const or_lbfgs &s, double *x) {
+  if (s.type) {
+    for (int i = 0; i < s.n; ++i) {
+      x[i] = std::max(s.xmin, x[i]);
+      x[i] = std::min(s.xmax, x[i]);
+    }
+  } else {
+    for (int i = 0; i < s.n; ++i)
+      if (s.mask[i] != 0.f && s.mask[i] != 2.f) {
+        x[i] = std::max(s.xmin, x[i]);
+        x[i] = std::min(s.xmax, x[i]);
+      }
+    for (int i = 0; i < s.n; ++i)
+      if (s.mask[i] == 0.f || s.mask[i] == 2.f) x[i] = s.xinit[i];
+  }
+}
+
+// MCSTEP (lbfgs.f:985-1210).
+void mcstep(double &stx, double &fx, double &dx, double &sty, double &fy, double &dy,
+            double &stp, double fp, double dp, bool &brackt, double stpmin,
+            double stpmax, int &info) {
+  info = 0;
+  if ((brackt && (stp <= std::min(stx, sty) || stp >= std::max(stx, sty))) ||
+      dx * (stp - stx) >= 0.0 || stpmax < stpmin)
+    return;
+  const double sgnd = dp * (dx / std::fabs(dx));
+  bool bound;
+  double theta, s, gamma, p, q, r, stpc, stpq, stpf;
+  if (fp > fx) {
+    info = 1;
+    bound = true;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp < stx) gamma = -gamma;
+    p = (gamma - dx) + theta;
+    q = ((gamma - dx) + gamma) + dp;
+    r = p / q;
+    stpc = stx + r * (stp - stx);
+    stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2) * (stp - stx);
+    if (std::fabs(stpc - stx) < std::fabs(stpq - stx))
+      stpf = stpc;
+    else
+      stpf = stpc + (stpq - stpc) / 2;
+    brackt = true;
+  } else if (sgnd < 0.0) {
+    info = 2;
+    bound = false;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp > stx) gamma = -gamma;
+    p = (gamma - dp) + theta;
+    q = ((gamma - dp) + gamma) + dx;
+    r = p / q;
+    stpc = stp + r * (stx - stp);
+    stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    if (std::fabs(stpc - stp) > std::fabs(stpq - stp))
+      stpf = stpc;
+    else
+      stpf = stpq;
+    brackt = true;
+  } else if (std::fabs(dp) < std::fabs(dx)) {
+    info = 3;
+    bound = true;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt(std::max(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+    if (stp > stx) gamma = -gamma;
+    p = (gamma - dp) + theta;
+    q = (gamma + (dx - dp)) + gamma;
+    r = p / q;
+    if (r < 0.0 && gamma != 0.0)
+      stpc = stp + r * (stx - stp);
+    else if (stp > stx)
+      stpc = stpmax;
+    else
+      stpc = stpmin;
+    stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    if (brackt) {
+      if (std::fabs(stp - stpc) < std::fabs(stp - stpq))
+        stpf = stpc;
+      else
+        stpf = stpq;
+    } else {
+      if (std::fabs(stp - stpc) > std::fabs(stp - stpq))
+        stpf = stpc;
+      else
+        stpf = stpq;
+    }
+  } else {
+    info = 4;
+    bound = false;
+    if (brackt) {
+      theta = 3 * (fp - fy) / (sty - stp) + dy + dp;
+      s = std::max(std::max(std::fabs(theta), std::fabs(dy)), std::fabs(dp));
+      gamma = s * std::sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+      if (stp > sty) gamma = -gamma;
+      p = (gamma - dp) + theta;
+      q = ((gamma - dp) + gamma) + dy;
+      r = p / q;
+      stpc = stp + r * (sty - stp);
+      stpf = stpc;
+    } else if (stp > stx) {
+      stpf = stpmax;
+    } else {
+      stpf = stpmin;
+    }
+  }
+  if (fp > fx) {
+    sty = stp; fy = fp; dy = dp;
+  } else {
+    if (sgnd < 0.0) { sty = stx; fy = fx; dy = dx; }
+    stx = stp; fx = fp; dx = dp;
+  }
+  stpf = std::min(stpmax, stpf);
+  stpf = std::max(stpmin, stpf);
+  stp = stpf;
+  // The literal 0.66 is a REAL constant in the F77 source.
+  const double p66s = (double)0.66f;
+  if (brackt && bound) {
+    if (sty > stx)
+      stp = std::min(stx + p66s * (sty - stx), stp);
+    else
+      stp = std::max(stx + p66s * (sty - stx), stp);
+  }
+}
+
+// MCSRCH (lbfgs.f:652-982).  s = search direction, wa = work (DIAG).
+void mcsrch(or_lbfgs &S, double *x, double f, const double *g, const double *s,
+            double &stp, double ftol, double xtol, int maxfev, int &info, int &nfev,
+            double *wa) {
+  const int n = S.n;
+  const double p5 = 0.5, p66 = 0.66, xtrapf = 4.0, zero = 0.0;
+  if (info == -1) goto L45;
+  S.infoc = 1;
+  if (n <= 0 || stp <= zero || ftol < zero || kGTOL < zero || xtol < zero ||
+      kSTPMIN < zero || kSTPMAX < kSTPMIN || maxfev <= 0)
+    return;
+  S.dginit = zero;
+  for (int j = 0; j < n; ++j) S.dginit = S.dginit + g[j] * s[j];
+  if (S.dginit >= zero) return;
+  S.brackt = false;
+  S.stage1 = true;
+  nfev = 0;
+  S.finit = f;
+  S.dgtest = ftol * S.dginit;
+  S.width = kSTPMAX - kSTPMIN;
+  S.width1 = S.width / p5;
+  for (int j = 0; j < n; ++j) wa[j] = x[j];
+  S.stx = zero; S.fx = S.finit; S.dgx = S.dginit;
+  S.sty = zero; S.fy = S.finit; S.dgy = S.dginit;
+L30:
+  if (S.brackt) {
+    S.stmin = std::min(S.stx, S.sty);
+    S.stmax = std::max(S.stx, S.sty);
+  } else {
+    S.stmin = S.stx;
+    S.stmax = stp + xtrapf * (stp - S.stx);
+  }
+  stp = std::max(stp, kSTPMIN);
+  stp = std::min(stp, kSTPMAX);
+  if ((S.brackt && (stp <= S.stmin || stp >= S.stmax)) || nfev >= maxfev - 1 ||
+      S.infoc == 0 || (S.brackt && S.stmax - S.stmin <= xtol * S.stmax))
+    stp = S.stx;
+  for (int j = 0; j < n; ++j) x[j] = wa[j] + stp * s[j];
+  if (S.boundt == 1) freeze_x(S, x);
+  info = -1;
+  return;
+L45:
+  info = 0;
+  nfev = nfev + 1;
+  S.dg = zero;
+  for (int j = 0; j < n; ++j) S.dg = S.dg + g[j] * s[j];
+  S.ftest1 = S.finit + stp * S.dgtest;
+  if ((S.brackt && (stp <= S.stmin || stp >= S.stmax)) || S.infoc == 0) info = 6;
+  if (stp == kSTPMAX && f <= S.ftest1 && S.dg <= S.dgtest) info = 5;
+  if (stp == kSTPMIN && (f > S.ftest1 || S.dg >= S.dgtest)) info = 4;
+  if (nfev >= maxfev) info = 3;
+  if (S.brackt && S.stmax - S.stmin <= xtol * S.stmax) info = 2;
+  if (f <= S.ftest1 && std::fabs(S.dg) <= kGTOL * (-S.dginit)) info = 1;
+  if (info != 0) return;
+  if (S.stage1 && f <= S.ftest1 && S.dg >= std::min(ftol, kGTOL) * S.dginit) S.stage1 = false;
+  if (S.stage1 && f <= S.fx && f > S.ftest1) {
+    S.fm = f - stp * S.dgtest;
+    S.fxm = S.fx - S.stx * S.dgtest;
+    S.fym = S.fy - S.sty * S.dgtest;
+    S.dgm = S.dg - S.dgtest;
+    S.dgxm = S.dgx - S.dgtest;
+    S.dgym = S.dgy - S.dgtest;
+    mcstep(S.stx, S.fxm, S.dgxm, S.sty, S.fym, S.dgym, stp, S.fm, S.dgm, S.brackt,
+           S.stmin, S.stmax, S.infoc);
+    S.fx = S.fxm + S.stx * S.dgtest;
+    S.fy = S.fym + S.sty * S.dgtest;
+    S.dgx = S.dgxm + S.dgtest;
+    S.dgy = S.dgym + S.dgtest;
+  } else {
+    mcstep(S.stx, S.fx, S.dgx, S.sty, S.fy, S.dgy, stp, f, S.dg, S.brackt, S.stmin,
+           S.stmax, S.infoc);
+  }
+  if (S.brackt) {
+    if (std::fabs(S.sty - S.stx) >= p66 * S.width1) stp = S.stx + p5 * (S.sty - S.stx);
+    S.width1 = S.width;
+    S.width = std::fabs(S.sty - S.stx);
+  }
+  goto L30;
+}
+
+// LBFGS (lbfgs.f:49-558), DIAGCO = .false.
+int lbfgs(or_lbfgs &S, double *x, double f, const double *g, double eps, double xtol,
+          int &iflag, int &myinfo) {
+  const int n = S.n, m = S.m;
+  double *W = S.w.data();      // W[1..]
+  double *DIAG = S.diag.data(); // DIAG[1..]
+  if (iflag == 0) goto L10;
+  if (iflag == 1) goto L172;
+  if (iflag == 2) goto L100;
+  return SW_BAD_PARAM;
+L10:
+  S.iter = 0;
+  if (n <= 0 || m <= 0) { iflag = -3; return SW_OK; }
+  S.nfun = 1;
+  S.point = 0;
+  S.finish = false;
+  for (int i = 1; i <= n; ++i) DIAG[i] = 1.0;
+  S.ispt = n + 2 * m;
+  S.iypt = S.ispt + n * m;
+  for (int i = 1; i <= n; ++i) W[S.ispt + i] = -g[i - 1] * DIAG[i];
+  S.gnorm = std::sqrt(ddot(n, g, g));
+  {
+    const double xnorm2 = std::sqrt(ddot(n, x, x));
+    if (S.boundt == 0) S.stp1 = 1.0 / S.gnorm;
+    else S.stp1 = xnorm2 / S.gnorm / 100;
+  }
+  S.ftol = 1.0e-4;
+  S.maxfev = 20;
+L80:
+  S.iter = S.iter + 1;
+  S.info = 0;
+  S.bound = S.iter - 1;
+  if (S.iter == 1) goto L165;
+  if (S.iter > m) S.bound = m;
+  S.ys = 0.0;
+  for (int j = 1; j <= n; ++j) S.ys = S.ys + W[S.iypt + S.npt + j] * W[S.ispt + S.npt + j];
+  S.yy = 0.0;
+  for (int j = 1; j <= n; ++j) S.yy = S.yy + W[S.iypt + S.npt + j] * W[S.iypt + S.npt + j];
+  for (int i = 1; i <= n; ++i) DIAG[i] = S.ys / S.yy;
+L100:
+  S.cp = S.point;
+  if (S.point == 0) S.cp = m;
+  W[n + S.cp] = 1.0 / S.ys;
+  for (int i = 1; i <= n; ++i) W[i] = -g[i - 1];
+  S.cp = S.point;
+  for (int i = 1; i <= S.bound; ++i) {
+    S.cp = S.cp - 1;
+    if (S.cp == -1) S.cp = m - 1;
+    double sq = 0.0;
+    for (int j = 1; j <= n; ++j) sq = sq + W[S.ispt + S.cp * n + j] * W[j];
+    const int inmc = n + m + S.cp + 1;
+    const int iycn = S.iypt + S.cp * n;
+    W[inmc] = W[n + S.cp + 1] * sq;
+    for (int j = 1; j <= n; ++j) W[j] = W[j] - W[inmc] * W[iycn + j];
+  }
+  for (int i = 1; i <= n; ++i) W[i] = DIAG[i] * W[i];
+  for (int i = 1; i <= S.bound; ++i) {
+    double yr = 0.0;
+    for (int j = 1; j <= n; ++j) yr = yr + W[S.iypt + S.cp * n + j] * W[j];
+    double beta = W[n + S.cp + 1] * yr;
+    const int inmc = n + m + S.cp + 1;
+    beta = W[inmc] - beta;
+    const int iscn = S.ispt + S.cp * n;
+    for (int j = 1; j <= n; ++j) W[j] = W[j] + beta * W[iscn + j];
+    S.cp = S.cp + 1;
+    if (S.cp == m) S.cp = 0;
+  }
+  for (int i = 1; i <= n; ++i) W[S.ispt + S.point * n + i] = W[i];
+L165:
+  S.nfev = 0;
+  S.stp = 1.0;
+  if (S.iter == 1) S.stp = S.stp1;
+  for (int i = 1; i <= n; ++i) W[i] = g[i - 1];
+L172:
+  mcsrch(S, x, f, g, &W[S.ispt + S.point * n + 1], S.stp, S.ftol, xtol, S.maxfev, S.info,
+         S.nfev, &DIAG[1]);
+  if (S.info == -1) { iflag = 1; return SW_OK; }
+  if (S.info != 1) { iflag = -1; return SW_OK; }
+  S.nfun = S.nfun + S.nfev;
+  myinfo = S.info;
+  if (S.boundt == 2 && S.info == 1) freeze_x(S, x);
+  S.npt = S.point * n;
+  for (int i = 1; i <= n; ++i) {
+    W[S.ispt + S.npt + i] = S.stp * W[S.ispt + S.npt + i];
+    W[S.iypt + S.npt + i] = g[i - 1] - W[i];
+  }
+  S.point = S.point + 1;
+  if (S.point == m) S.point = 0;
+  S.gnorm = std::sqrt(ddot(n, g, g));
+  S.xnorm = std::sqrt(ddot(n, x, x));
+  S.xnorm = std::max(1.0, S.xnorm);
+  if (S.gnorm / S.xnorm <= eps) S.finish = true;
+  if (S.finish) { iflag = 0; return SW_OK; }
+  goto L80;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C entry points
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int oracle_propagate_f32(const sw_prop_desc *d, const sw_prop_io *io) {
+  IO<float> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
+              io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2};
+  return propagate<float>(*d, o);
+}
+
+int oracle_propagate_f64(const sw_prop_desc *d, const or_prop_io64 *io) {
+  IO<double> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
+               io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2};
+  return propagate<double>(*d, o);
+}
+
+int oracle_modeling_f32(const sw_genpar *g, const float *vel, const float *sou_coord,
+                        const float *wavelet, int nrec, const float *rec_coord,
+                        float *data, float *final_u2) {
+  return modeling<float>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, final_u2);
+}
+int oracle_modeling_f64(const sw_genpar *g, const double *vel, const double *sou_coord,
+                        const double *wavelet, int nrec, const double *rec_coord,
+                        double *data, double *final_u2) {
+  return modeling<double>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, final_u2);
+}
+int oracle_rtm_f32(const sw_genpar *g, const float *vel, const float *sou_coord,
+                   const float *wavelet, int nrec, const float *rec_coord,
+                   const float *data, float *image, float *illum) {
+  return rtm_like<float>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, image,
+                         illum, false);
+}
+int oracle_born_f32(const sw_genpar *g, const float *vel, const float *ref,
+                    const float *sou_coord, const float *wavelet, int nrec,
+                    const float *rec_coord, float *data) {
+  return born<float>(*g, vel, ref, sou_coord, wavelet, nrec, rec_coord, data);
+}
+int oracle_born_f64(const sw_genpar *g, const double *vel, const double *ref,
+                    const double *sou_coord, const double *wavelet, int nrec,
+                    const double *rec_coord, double *data) {
+  return born<double>(*g, vel, ref, sou_coord, wavelet, nrec, rec_coord, data);
+}
+int oracle_lsrtm_f32(const sw_genpar *g, const float *vel, const float *sou_coord,
+                     const float *wavelet, int nrec, const float *rec_coord,
+                     const float *data, float *image, float *illum) {
+  return rtm_like<float>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, image,
+                         illum, true);
+}
+int oracle_lsrtm_f64(const sw_genpar *g, const double *vel, const double *sou_coord,
+                     const double *wavelet, int nrec, const double *rec_coord,
+                     const double *data, double *image, double *illum) {
+  return rtm_like<double>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, image,
+                          illum, true);
+}
+
+// readsou Born/LSRTM branch (ReadSouVelRho.f90:318-326).
+int oracle_born_wavelet(float *w, int nt, float dt) {
+  if (nt < 1) return SW_BAD_PARAM;
+  std::vector<float> tr(w, w + nt);
+  for (int i = 0; i < nt; ++i) w[i] = 0.f;
+  for (int it = 2; it <= nt - 1; ++it)
+    w[it - 1] = w[it - 1] + ((-2 * tr[it - 1] + tr[it - 2]) + tr[it]) / (dt * dt);
+  return SW_OK;
+}
+
+// vel_check (ReadSouVelRho.f90:603-756).
+int oracle_vel_check(const sw_genpar *g, const float *vel, float *courant, float *samplerate) {
+  const size_t n = (size_t)g->nz * g->nx * g->ny;
+  float vmax = vel[0], vmin = vel[0];
+  for (size_t q = 1; q < n; ++q) { vmax = std::max(vmax, vel[q]); vmin = std::min(vmin, vel[q]); }
+  const float stab_cond = g->twoD ? 0.45f : 0.35f;
+  float stab;
+  if (g->twoD) stab = vmax * g->dt / std::min(g->dz, g->dx);
+  else stab = vmax * g->dt / std::min(std::min(g->dz, g->dx), g->dy);
+  const float lambdamin = vmin / g->fmax;
+  float sr;
+  if (g->twoD) sr = lambdamin / std::max(g->dz, g->dx);
+  else sr = lambdamin / std::max(std::max(g->dz, g->dx), g->dy);
+  if (courant) *courant = stab;
+  if (samplerate) *samplerate = sr;
+  if (stab > stab_cond) return SW_BAD_PARAM;
+  if (sr < 2.0f) return SW_BAD_PARAM;
+  return SW_OK;
+}
+
+int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel, const float *wavelet,
+                       int nshot, const sw_fwi_shot *shots, const float *vpmask,
+                       double *f, float *grad, float *illum) {
+  return fwi_fct_gdt(*d, vel, wavelet, nshot, shots, vpmask, f, grad, illum);
+}
+
+int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2, int rect3,
+                     int doz, int dox, int doy) {
+  return triangle2(uu, n1, n2, n3, rect1, rect2, rect3, doz != 0, dox != 0, doy != 0);
+}
+
+void oracle_mksinc(float *sinc, int lsinc, float shift) { mksinc<float>(sinc, lsinc, shift); }
+
+or_lbfgs *oracle_lbfgs_create(int n, int m, double xmin, double xmax, const float *mask,
+                              int bound_type, int freeze_soft, const double *xinit) {
+  or_lbfgs *s = new or_lbfgs();
+  s->n = n; s->m = m; s->xmin = xmin; s->xmax = xmax;
+  s->mask.assign(mask, mask + n);
+  s->boundt = bound_type;
+  s->type = freeze_soft != 0;
+  s->xinit.assign(xinit, xinit + n);
+  s->w.assign((size_t)n * (2 * m + 1) + 2 * m + 1, 0.0);
+  s->diag.assign((size_t)n + 1, 0.0);
+  return s;
+}
+void oracle_lbfgs_destroy(or_lbfgs *s) { delete s; }
+int oracle_lbfgs_step(or_lbfgs *s, double *x, double f, const double *g, double eps,
+                      double xtol, int *iflag, int *myinfo) {
+  return lbfgs(*s, x, f, g, eps, xtol, *iflag, *myinfo);
+}
+void oracle_lbfgs_diag(const or_lbfgs *s, double *o) {
+  o[0] = s->iter; o[1] = s->nfun; o[2] = s->stp; o[3] = s->gnorm;
+  o[4] = s->ys; o[5] = s->yy; o[6] = s->dginit; o[7] = s->dg;
+}
+
+}  // extern "C"

@@ -1,0 +1,345 @@
+"""seismic_gb300: GB300-native acoustic wave-equation engine (libswave).
+
+Python mirror of the C-ABI in include/swave.h, shaped after the reference's
+operator plug-in interface (propagator_acoustic, libs/libwave/Propagator.f90)
+and its drivers (RTM_to_memory, BORN_to_memory, LSRTM_to_memory,
+compute_fct_gdt, l_bfgs).  All compute runs in libswave.so's CUDA kernels;
+importing this package on a machine where the library cannot be loaded
+raises, there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = _build.LIB
+
+# Status codes (sw_status).
+SW_OK, SW_BAD_PARAM, SW_OOM_ADMISSION, SW_TIMEOUT, SW_NUMERIC, SW_CUDA_ERR, SW_UNSUPPORTED = range(7)
+STATUS_NAMES = {0: "SW_OK", 1: "SW_BAD_PARAM", 2: "SW_OOM_ADMISSION", 3: "SW_TIMEOUT",
+                4: "SW_NUMERIC", 5: "SW_CUDA_ERR", 6: "SW_UNSUPPORTED"}
+# Procedure selectors of propagator_acoustic.
+FD_FORWARD, FD_ADJOINT = 0, 1
+INJ_NONE, INJ_SINC, INJ_SIMPLE, INJ_LSRTM_SINC = 0, 1, 2, 3
+EXT_NONE, EXT_SINC, EXT_SIMPLE_AFWI, EXT_LSRTM_SINC, EXT_SINC_AFWI = 0, 1, 2, 3, 4
+IMG_NONE, IMG_RTM, IMG_LSRTM, IMG_AFWI, IMG_BORN = 0, 1, 2, 3, 4
+
+
+class SwGenpar(C.Structure):
+    """sw_genpar: the GeneralParam fields the propagation path reads."""
+    _fields_ = [("twoD", C.c_int), ("nz", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+                ("dz", C.c_float), ("dx", C.c_float), ("dy", C.c_float),
+                ("oz", C.c_float), ("ox", C.c_float), ("oy", C.c_float),
+                ("dt", C.c_float), ("nt", C.c_int), ("ntaper", C.c_int), ("lsinc", C.c_int),
+                ("snapi", C.c_int), ("surf_type", C.c_int), ("shot_type", C.c_int),
+                ("rec_type", C.c_int), ("fmax", C.c_float)]
+
+
+class SwPropDesc(C.Structure):
+    _fields_ = [("g", SwGenpar), ("tmin", C.c_int), ("tmax", C.c_int), ("tstep", C.c_int),
+                ("fd_scheme", C.c_int), ("injection", C.c_int), ("extraction", C.c_int),
+                ("extract_wave", C.c_int), ("imaging", C.c_int)]
+
+
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+
+
+class SwPropIO(C.Structure):
+    _fields_ = [("vel", _fp), ("nsou", C.c_int), ("sou_coord", _fp), ("sou_trace", _fp),
+                ("nrec", C.c_int), ("rec_coord", _fp), ("rec_trace", _fp), ("wave", _fp),
+                ("image", _fp), ("illum", _fp), ("ref", _fp), ("final_u2", _fp)]
+
+
+class SwFwiShot(C.Structure):
+    _fields_ = [("sou_coord", C.c_float * 3), ("nrec", C.c_int), ("rec_coord", _fp),
+                ("dobs", _fp), ("mute", _fp), ("resid", _fp)]
+
+
+class SwFwiDesc(C.Structure):
+    _fields_ = [("g", SwGenpar), ("aperture_x", C.c_float), ("aperture_y", C.c_float),
+                ("illu_pow", C.c_float), ("smooth_rect1", C.c_int), ("smooth_rect2", C.c_int),
+                ("smooth_rect3", C.c_int), ("smooth_doz", C.c_int), ("smooth_dox", C.c_int),
+                ("smooth_doy", C.c_int)]
+
+
+class SwStats(C.Structure):
+    _fields_ = [("launches_total", C.c_uint64), ("launches_step", C.c_uint64),
+                ("points_updated", C.c_uint64), ("step_kernel_ms", C.c_double),
+                ("step_kernel_timed", C.c_uint64), ("step_bytes", C.c_uint64)]
+
+
+# Every symbol of include/swave.h with its signature.
+_SIGS = {
+    "sw_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "sw_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "sw_last_error": (C.c_char_p, [C.c_void_p]),
+    "sw_version": (C.c_char_p, []),
+    "sw_vel_check": (C.c_int, [C.POINTER(SwGenpar), _fp, _fp, _fp]),
+    "sw_propagate": (C.c_int, [C.c_void_p, C.POINTER(SwPropDesc), C.POINTER(SwPropIO)]),
+    "sw_modeling": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp]),
+    "sw_rtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
+    "sw_born": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
+    "sw_lsrtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
+    "sw_born_wavelet": (C.c_int, [_fp, C.c_int, C.c_float]),
+    "sw_fwi_fct_gdt": (C.c_int, [C.c_void_p, C.POINTER(SwFwiDesc), _fp, _fp, C.c_int,
+                                 C.POINTER(SwFwiShot), _fp, _dp, _fp, _fp]),
+    "sw_lbfgs_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, _fp,
+                                  C.c_int, C.c_int, _dp, C.POINTER(C.c_void_p)]),
+    "sw_lbfgs_destroy": (C.c_int, [C.c_void_p]),
+    "sw_lbfgs_step": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
+                                C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sw_lbfgs_diag": (C.c_int, [C.c_void_p, _dp]),
+    "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
+    "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
+    "sw_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+}
+
+_lib = None
+
+
+class SwaveError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads libswave.so (built by build.py).  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libswave.so not found at {p}: run seismic_gb300.build.build_library()")
+    lib = C.CDLL(p)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _f32(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_fp)
+
+
+def dptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def make_genpar(nz, nx, ny=1, dz=10.0, dx=10.0, dy=1.0, oz=0.0, ox=0.0, oy=0.0, dt=1e-3,
+                nt=1000, ntaper=20, lsinc=7, snapi=4, twoD=None, fmax=30.0) -> SwGenpar:
+    """GeneralParam defaults follow read_3D_params (libs/libwave/ReadParam.f90:18-53)."""
+    if twoD is None:
+        twoD = ny == 1
+    return SwGenpar(int(twoD), nz, nx, ny, dz, dx, dy if not twoD else 1.0, oz, ox, oy, dt, nt,
+                    ntaper, lsinc, snapi, 0, 0, 0, fmax)
+
+
+def padded_shape(g: SwGenpar) -> tuple[int, int, int]:
+    """(n3p, n2p, n1p) of the padded arrays u(nmin1-4:nmax1+4, ...)."""
+    n1p = g.nz + 2 * g.ntaper + 8
+    n2p = g.nx + 2 * g.ntaper + 8
+    n3p = 1 if g.twoD else g.ny + 2 * g.ntaper + 8
+    return (n3p, n2p, n1p)
+
+
+class Context:
+    """One CUDA stream + device buffers (sw_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = C.c_void_p()
+        code = self.lib.sw_ctx_create(device, C.byref(h))
+        if code != SW_OK:
+            raise SwaveError(code, "sw_ctx_create failed (is a CUDA device visible?)")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sw_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, code: int):
+        if code != SW_OK:
+            raise SwaveError(code, (self.lib.sw_last_error(self.h) or b"").decode())
+
+    # -- instrumentation -------------------------------------------------
+    def stats(self) -> dict:
+        s = SwStats()
+        self._check(self.lib.sw_ctx_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in SwStats._fields_}
+
+    def reset_stats(self):
+        self._check(self.lib.sw_ctx_reset_stats(self.h))
+
+    def set_profiling(self, on: bool):
+        self._check(self.lib.sw_ctx_set_profiling(self.h, int(bool(on))))
+
+    # -- propagator_acoustic ----------------------------------------------
+    def propagate(self, desc: SwPropDesc, vel, sou_coord=None, sou_trace=None, rec_coord=None,
+                  rec_trace=None, wave=None, image=None, illum=None, ref=None, final_u2=None):
+        """sw_propagate; array arguments are modified in place like the reference."""
+        io = SwPropIO()
+        vel = _f32(vel)
+        io.vel = fptr(vel)
+        keep = [vel]
+        if sou_coord is not None:
+            sc, st = _f32(sou_coord), _f32(sou_trace)
+            keep += [sc, st]
+            io.nsou, io.sou_coord, io.sou_trace = sc.size // 3, fptr(sc), fptr(st)
+        if rec_coord is not None:
+            rc = _f32(rec_coord)
+            keep.append(rc)
+            io.nrec, io.rec_coord, io.rec_trace = rc.size // 3, fptr(rc), fptr(rec_trace)
+        io.wave, io.image, io.illum = fptr(wave), fptr(image), fptr(illum)
+        if ref is not None:
+            ref = _f32(ref)
+            keep.append(ref)
+        io.ref = fptr(ref)
+        io.final_u2 = fptr(final_u2)
+        self._check(self.lib.sw_propagate(self.h, C.byref(desc), C.byref(io)))
+
+    # -- drivers -----------------------------------------------------------
+    def modeling(self, g: SwGenpar, vel, sou_coord, wavelet, rec_coord, final_u2=False):
+        vel, sc, w, rc = _f32(vel), _f32(sou_coord), _f32(wavelet), _f32(rec_coord)
+        nrec = rc.size // 3
+        data = np.zeros((nrec, g.nt), np.float32)
+        fu = np.zeros(padded_shape(g), np.float32) if final_u2 else None
+        self._check(self.lib.sw_modeling(self.h, C.byref(g), fptr(vel), fptr(sc), fptr(w), nrec,
+                                         fptr(rc), fptr(data), fptr(fu)))
+        return (data, fu) if final_u2 else data
+
+    def rtm(self, g, vel, sou_coord, wavelet, rec_coord, data):
+        vel, sc, w, rc, d = _f32(vel), _f32(sou_coord), _f32(wavelet), _f32(rec_coord), _f32(data)
+        n = g.nz * g.nx * g.ny
+        image, illum = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        self._check(self.lib.sw_rtm(self.h, C.byref(g), fptr(vel), fptr(sc), fptr(w), rc.size // 3,
+                                    fptr(rc), fptr(d), fptr(image), fptr(illum)))
+        return image, illum
+
+    def lsrtm(self, g, vel, sou_coord, wavelet, rec_coord, data):
+        vel, sc, w, rc, d = _f32(vel), _f32(sou_coord), _f32(wavelet), _f32(rec_coord), _f32(data)
+        n = g.nz * g.nx * g.ny
+        image, illum = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        self._check(self.lib.sw_lsrtm(self.h, C.byref(g), fptr(vel), fptr(sc), fptr(w),
+                                      rc.size // 3, fptr(rc), fptr(d), fptr(image), fptr(illum)))
+        return image, illum
+
+    def born(self, g, vel, ref, sou_coord, wavelet, rec_coord):
+        vel, r, sc, w, rc = _f32(vel), _f32(ref), _f32(sou_coord), _f32(wavelet), _f32(rec_coord)
+        nrec = rc.size // 3
+        data = np.zeros((nrec, g.nt), np.float32)
+        self._check(self.lib.sw_born(self.h, C.byref(g), fptr(vel), fptr(r), fptr(sc), fptr(w),
+                                     nrec, fptr(rc), fptr(data)))
+        return data
+
+    def fwi_fct_gdt(self, desc: SwFwiDesc, vel, wavelet, shots, vpmask=None, want_resid=False):
+        """compute_fct_gdt.  shots: list of dicts(sou=(z,x,y), rec=(n,3), dobs=(n,nt), mute=...)."""
+        g = desc.g
+        vel, w = _f32(vel), _f32(wavelet)
+        arr = (SwFwiShot * len(shots))()
+        keep = []
+        resids = []
+        for i, s in enumerate(shots):
+            rc, dob = _f32(s["rec"]), _f32(s["dobs"])
+            mu = _f32(s["mute"]) if s.get("mute") is not None else None
+            keep += [rc, dob, mu]
+            arr[i].sou_coord[:] = [float(v) for v in s["sou"]]
+            arr[i].nrec = rc.size // 3
+            arr[i].rec_coord, arr[i].dobs, arr[i].mute = fptr(rc), fptr(dob), fptr(mu)
+            r = np.zeros((rc.size // 3, g.nt), np.float32) if want_resid else None
+            resids.append(r)
+            arr[i].resid = fptr(r)
+        n = g.nz * g.nx * g.ny
+        grad, illum = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        f = C.c_double(0.0)
+        m = _f32(vpmask) if vpmask is not None else None
+        self._check(self.lib.sw_fwi_fct_gdt(self.h, C.byref(desc), fptr(vel), fptr(w), len(shots),
+                                            arr, fptr(m), C.byref(f), fptr(grad), fptr(illum)))
+        return (f.value, grad, illum, resids) if want_resid else (f.value, grad, illum)
+
+
+class LBFGS:
+    """Reverse-communication L-BFGS (LBFGS, libs/libinv/lbfgs.f) on the device."""
+
+    def __init__(self, ctx: Context, n: int, m: int = 5, xmin=1500.0, xmax=4500.0, mask=None,
+                 bound_type: int = 2, freeze_soft: bool = True, xinit=None):
+        self.ctx = ctx
+        mask = np.ones(n, np.float32) if mask is None else _f32(mask)
+        xinit = np.zeros(n) if xinit is None else np.ascontiguousarray(xinit, np.float64)
+        self._keep = (mask, xinit)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.sw_lbfgs_create(ctx.h, n, m, xmin, xmax, fptr(mask), bound_type,
+                                           int(freeze_soft), dptr(xinit), C.byref(h)))
+        self.h = h
+        self.iflag = C.c_int(0)
+        self.myinfo = C.c_int(0)
+
+    def step(self, x: np.ndarray, f: float, g: np.ndarray, eps=1e-20, xtol=np.finfo(float).eps):
+        self.myinfo.value = 0
+        self.ctx._check(self.ctx.lib.sw_lbfgs_step(self.h, dptr(x), float(f),
+                                                   dptr(np.ascontiguousarray(g, np.float64)),
+                                                   eps, xtol, C.byref(self.iflag),
+                                                   C.byref(self.myinfo)))
+        return self.iflag.value, self.myinfo.value
+
+    def diag(self) -> np.ndarray:
+        out = np.zeros(8)
+        self.ctx._check(self.ctx.lib.sw_lbfgs_diag(self.h, dptr(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sw_lbfgs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def vel_check(g: SwGenpar, vel) -> tuple[int, float, float]:
+    lib = load_library()
+    v = _f32(vel)
+    a, b = C.c_float(), C.c_float()
+    code = lib.sw_vel_check(C.byref(g), fptr(v), C.byref(a), C.byref(b))
+    return code, a.value, b.value
+
+
+def born_wavelet(w, dt: float) -> np.ndarray:
+    lib = load_library()
+    w = _f32(w).copy()
+    code = lib.sw_born_wavelet(fptr(w), w.size, dt)
+    if code != SW_OK:
+        raise SwaveError(code, "sw_born_wavelet")
+    return w

@@ -1,0 +1,833 @@
+// engine.cu - host side of libswave: context, device buffers, the
+// propagation driver (propagator_acoustic) and the operator drivers.
+//
+// Host arithmetic that feeds the kernels (sinc weights, tapers, positions)
+// restates the reference in float, compiled with -ffp-contract=off, so the
+// weights are bit-identical to the reference formulas evaluated in IEEE
+// single precision.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/swave.h"
+#include "engine.h"
+#include "swave_dev.cuh"
+
+using namespace swave;
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+
+int sw_ctx_create(int device, sw_ctx **out) {
+  if (!out) return SW_BAD_PARAM;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return SW_CUDA_ERR;
+  if (device < 0 || device >= ndev) return SW_BAD_PARAM;
+  if (cudaSetDevice(device) != cudaSuccess) return SW_CUDA_ERR;
+  sw_ctx *c = new sw_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return SW_CUDA_ERR;
+  }
+  *out = c;
+  return SW_OK;
+}
+
+int sw_ctx_destroy(sw_ctx *c) {
+  if (!c) return SW_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->bufs) cudaFree(kv.second.p);
+  for (auto &e : c->ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return SW_OK;
+}
+
+const char *sw_last_error(const sw_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+const char *sw_version(void) { return "swave 0.1 (sm_103a, FP32 wavefields, FP64 reductions)"; }
+
+int sw_ctx_get_stats(const sw_ctx *c, sw_stats *o) {
+  if (!c || !o) return SW_BAD_PARAM;
+  *o = c->stats;
+  return SW_OK;
+}
+int sw_ctx_reset_stats(sw_ctx *c) {
+  if (!c) return SW_BAD_PARAM;
+  std::memset(&c->stats, 0, sizeof(c->stats));
+  return SW_OK;
+}
+int sw_ctx_set_profiling(sw_ctx *c, int on) {
+  if (!c) return SW_BAD_PARAM;
+  c->profiling = on != 0;
+  return SW_OK;
+}
+
+namespace swave {
+
+int fail(sw_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(sw_ctx *c, cudaError_t e, const char *what) {
+  return fail(c, SW_CUDA_ERR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Grow-only named device buffers owned by the context.
+void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st) {
+  if (bytes == 0) bytes = 16;
+  DBuf &b = c->bufs[name];
+  if (b.cap < bytes) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.cap = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *st = fail(c, e == cudaErrorMemoryAllocation ? SW_OOM_ADMISSION : SW_CUDA_ERR,
+                 "cudaMalloc(%s, %zu bytes): %s", name.c_str(), bytes, cudaGetErrorString(e));
+      return nullptr;
+    }
+    b.cap = bytes;
+  }
+  return b.p;
+}
+
+int check_genpar(sw_ctx *c, const sw_genpar &g) {
+  if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0)
+    return fail(c, SW_UNSUPPORTED, "surf_type/shot_type/rec_type != 0 is not built");
+  if (g.nz < 1 || g.nx < 1 || g.ny < 1 || g.nt < 1 || g.ntaper < 4 || g.snapi < 1)
+    return fail(c, SW_BAD_PARAM, "bad sizes nz=%d nx=%d ny=%d nt=%d ntaper=%d snapi=%d", g.nz,
+                g.nx, g.ny, g.nt, g.ntaper, g.snapi);
+  if (g.lsinc < 3 || (g.lsinc % 2) == 0 || g.lsinc > 15)
+    return fail(c, SW_BAD_PARAM, "lsinc must be odd in [3,15], got %d", g.lsinc);
+  if (g.twoD && g.ny != 1) return fail(c, SW_BAD_PARAM, "twoD requires ny = 1");
+  if (!(g.dz > 0.f) || !(g.dx > 0.f) || (!g.twoD && !(g.dy > 0.f)) || !(g.dt > 0.f))
+    return fail(c, SW_BAD_PARAM, "non-positive spacing or dt");
+  return SW_OK;
+}
+
+// FDbounds for shot_type = surf_type = 0 (ReadSouVelRho.f90:456-470).
+Geom make_geom(const sw_genpar &g) {
+  Geom G;
+  G.nmin1 = -g.ntaper + 1;
+  G.nmax1 = g.nz + g.ntaper;
+  G.nmin2 = -g.ntaper + 1;
+  G.nmax2 = g.nx + g.ntaper;
+  if (!g.twoD) {
+    G.nmin3 = -g.ntaper + 1;
+    G.nmax3 = g.ny + g.ntaper;
+    G.nbound = 4;
+  } else {
+    G.nmin3 = 1;
+    G.nmax3 = 1;
+    G.nbound = 0;
+  }
+  G.lo1 = G.nmin1 - 4;
+  G.lo2 = G.nmin2 - 4;
+  G.lo3 = G.nmin3 - G.nbound;
+  G.n1p = G.nmax1 + 4 - G.lo1 + 1;
+  G.n2p = G.nmax2 + 4 - G.lo2 + 1;
+  G.n3p = G.nmax3 + G.nbound - G.lo3 + 1;
+  G.ld1 = (G.n1p + 31) / 32 * 32;
+  G.nz = g.nz;
+  G.nx = g.nx;
+  G.ny = g.ny;
+  G.twoD = g.twoD;
+  return G;
+}
+
+// FD_acoustic_init_coefs + FD_types_assign_scaled_coefs (FDcoefs.f90:25-36,
+// FDtypes.f90:50-80), coefpower = 2.
+Coefs make_coefs(const sw_genpar &g) {
+  const float c0 = -205.f / 72.f, c1 = 8.f / 5.f, c2 = -1.f / 5.f, c3 = 8.f / 315.f,
+              c4 = -1.f / 560.f;
+  const float dxi = 1.f / g.dx, dyi = 1.f / g.dy, dzi = 1.f / g.dz;
+  const float px = dxi * dxi, py = dyi * dyi, pz = dzi * dzi;
+  Coefs c;
+  c.c0x = c0 * px; c.c1x = c1 * px; c.c2x = c2 * px; c.c3x = c3 * px; c.c4x = c4 * px;
+  c.c0y = c0 * py; c.c1y = c1 * py; c.c2y = c2 * py; c.c3y = c3 * py; c.c4y = c4 * py;
+  c.c0z = c0 * pz; c.c1z = c1 * pz; c.c2z = c2 * pz; c.c3z = c3 * pz; c.c4z = c4 * pz;
+  return c;
+}
+
+// mksinc (Interpolate.f90:15-42), evaluated once per trace.
+void mksinc(float *sinc, int lsinc, float shift) {
+  const float pi = 3.141592654f;
+  float fsum = 0.f;
+  for (int n = 1; n <= lsinc; ++n) {
+    float fact;
+    if (n <= (int)((float)(lsinc / 2 + 1) + shift))
+      fact = ((float)(n - 1) - shift) / (float)(lsinc / 2);
+    else
+      fact = ((float)(lsinc - n) + shift) / (float)(lsinc / 2);
+    if (fact <= 0.f) fact = 0.f;
+    const float pos = pi * ((float)(n - (lsinc / 2 + 1)) - shift);
+    if (std::fabs(pos) > 0.005f)
+      sinc[n - 1] = (fact * sinf(pos)) / pos;
+    else
+      sinc[n - 1] = fact * (1.f - (pos * pos) / 6.f);
+    fsum = fsum + sinc[n - 1];
+  }
+  for (int n = 1; n <= lsinc; ++n) sinc[n - 1] = sinc[n - 1] / fsum;
+}
+
+// find_i_d (ModelSpaceTypes.f90:144-151) for the three axes.
+void positions(const sw_genpar &g, int n, const float *coord, std::vector<int> &ic,
+               std::vector<float> &dc) {
+  ic.resize(3 * (size_t)n);
+  dc.resize(3 * (size_t)n);
+  const float om[3] = {g.oz, g.ox, g.twoD ? 0.f : g.oy};
+  const float de[3] = {g.dz, g.dx, g.twoD ? 1.f : g.dy};
+  for (int r = 0; r < n; ++r)
+    for (int a = 0; a < 3; ++a) {
+      const float e = coord[3 * r + a];
+      const int ie = (int)lroundf((e - om[a]) / de[a]) + 1;
+      ic[3 * r + a] = ie;
+      dc[3 * r + a] = e - (om[a] + (float)(ie - 1) * de[a]);
+    }
+}
+
+// compute_taper / cos_sin_taper (Taper.f90:14-44).
+static void cos_sin_taper(std::vector<float> &a, int ntaper, int n) {
+  const float pi = 3.14159265359f;
+  const int m = std::min(ntaper, n);
+  for (int i = 1; i <= m; ++i) {
+    const float s = sinf((pi * (float)(i - 1)) / (float)(2 * (m - 1)));
+    a[i - 1] = s * s;
+  }
+  const int i0 = std::max(1, n - ntaper);
+  for (int i = i0; i <= n; ++i) {
+    const float cc = cosf((pi * (float)(i - i0)) / (float)(2 * ntaper));
+    a[i - 1] = cc * cc;
+  }
+}
+void compute_taper(int nxw, int nyw, std::vector<float> &tx, std::vector<float> &ty) {
+  tx.assign(nxw, 1.f);
+  ty.assign(nyw, 1.f);
+  cos_sin_taper(tx, std::min(nxw / 2, 10), nxw);
+  if (nyw > 1) cos_sin_taper(ty, std::min(nyw / 2, 10), nyw);
+}
+
+static inline float host_vel(const sw_genpar &g, const float *vp, int i, int j, int k) {
+  const int ii = std::min(std::max(i, 1), g.nz), jj = std::min(std::max(j, 1), g.nx),
+            kk = std::min(std::max(k, 1), g.ny);
+  return vp[(size_t)(ii - 1) + (size_t)g.nz * ((jj - 1) + (size_t)g.nx * (kk - 1))];
+}
+
+// Builds the injection plan: a box covering every contribution and, per box
+// cell, the contributions in source order.
+int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
+                    const float *sou_coord, const float *vel_phys, InjPlan &plan) {
+  plan.on = 0;
+  if (mode == SW_INJ_NONE || nsou <= 0) return SW_OK;
+  std::vector<int> ic;
+  std::vector<float> dc;
+  positions(g, nsou, sou_coord, ic, dc);
+  const bool sinc = mode == SW_INJ_SINC || mode == SW_INJ_LSRTM_SINC;
+  const int h = sinc ? g.lsinc / 2 : 0;
+  const int ls = g.lsinc;
+  const float de[3] = {g.dz, g.dx, g.twoD ? 1.f : g.dy};
+  int bi0 = 1 << 30, bi1 = -(1 << 30), bj0 = bi0, bj1 = bi1, bk0 = bi0, bk1 = bi1;
+  for (int r = 0; r < nsou; ++r) {
+    const int i = ic[3 * r], j = ic[3 * r + 1], k = g.twoD ? 1 : ic[3 * r + 2];
+    if (g.twoD && ic[3 * r + 2] != 1)
+      return fail(c, SW_BAD_PARAM, "2D source %d has a non-zero y coordinate", r);
+    const int hk = g.twoD ? 0 : h;
+    if (i - h < G.nmin1 || i + h > G.nmax1 || j - h < G.nmin2 || j + h > G.nmax2 ||
+        k - hk < G.nmin3 || k + hk > G.nmax3)
+      return fail(c, SW_BAD_PARAM, "source %d footprint leaves the compute domain", r);
+    bi0 = std::min(bi0, i - h); bi1 = std::max(bi1, i + h);
+    bj0 = std::min(bj0, j - h); bj1 = std::max(bj1, j + h);
+    bk0 = std::min(bk0, k - hk); bk1 = std::max(bk1, k + hk);
+  }
+  const long long nb = (long long)(bi1 - bi0 + 1) * (bj1 - bj0 + 1) * (bk1 - bk0 + 1);
+  struct Tmp { int cell; InjEntry e; };
+  std::vector<Tmp> all;
+  const long long per = sinc ? (long long)ls * ls * (g.twoD ? 1 : ls) : 1;
+  all.reserve((size_t)(per * nsou));
+  std::vector<float> sz(ls), sx(ls), sy(ls);
+  const float inv_d2 = 1.f / (g.dz * g.dx);
+  const float inv_d3 = 1.f / ((g.dz * g.dx) * g.dy);
+  for (int r = 0; r < nsou; ++r) {
+    const int i0 = ic[3 * r], j0 = ic[3 * r + 1], k0 = g.twoD ? 1 : ic[3 * r + 2];
+    float v2r;
+    if (mode == SW_INJ_LSRTM_SINC) {
+      v2r = g.twoD ? inv_d2 : inv_d3;
+    } else {
+      const float vv = host_vel(g, vel_phys, i0, j0, k0);
+      v2r = vv * vv;
+    }
+    auto cell = [&](int i, int j, int k) {
+      return (int)((i - bi0) + (long long)(bi1 - bi0 + 1) * ((j - bj0) + (long long)(bj1 - bj0 + 1) * (k - bk0)));
+    };
+    if (!sinc) {
+      all.push_back({cell(i0, j0, k0), {r, v2r, 1.f, 1.f, 1.f}});
+      continue;
+    }
+    mksinc(sz.data(), ls, dc[3 * r] / de[0]);
+    mksinc(sx.data(), ls, dc[3 * r + 1] / de[1]);
+    if (g.twoD) {
+      for (int j = -h; j <= h; ++j)
+        for (int i = -h; i <= h; ++i)
+          all.push_back({cell(i0 + i, j0 + j, 1), {r, v2r, sz[h + i], sx[h + j], 1.f}});
+    } else {
+      // Injection_source_sinc_xyz weights y with the x sinc column
+      // (Injection.f90:314).
+      for (int k = -h; k <= h; ++k)
+        for (int j = -h; j <= h; ++j)
+          for (int i = -h; i <= h; ++i)
+            all.push_back({cell(i0 + i, j0 + j, k0 + k), {r, v2r, sz[h + i], sx[h + j], sx[h + k]}});
+    }
+  }
+  // Stable counting sort by cell keeps source order inside a cell.
+  std::vector<int> off((size_t)nb + 1, 0);
+  for (auto &t : all) off[(size_t)t.cell + 1]++;
+  for (long long b = 0; b < nb; ++b) off[(size_t)b + 1] += off[(size_t)b];
+  std::vector<int> pos(off.begin(), off.end() - 1);
+  std::vector<InjEntry> ent(all.size());
+  for (auto &t : all) ent[(size_t)pos[(size_t)t.cell]++] = t.e;
+  plan.on = 1;
+  plan.bi0 = bi0; plan.bi1 = bi1; plan.bj0 = bj0; plan.bj1 = bj1; plan.bk0 = bk0; plan.bk1 = bk1;
+  plan.off = std::move(off);
+  plan.ent = std::move(ent);
+  return SW_OK;
+}
+
+int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nrec,
+                     const float *rec_coord, ExtPlan &plan) {
+  plan.on = 0;
+  if (mode == SW_EXT_NONE || nrec <= 0) return SW_OK;
+  std::vector<float> dc;
+  positions(g, nrec, rec_coord, plan.ic, dc);
+  const int h = g.lsinc / 2, ls = g.lsinc;
+  const bool sinc = mode != SW_EXT_SIMPLE_AFWI;
+  const float de[3] = {g.dz, g.dx, g.twoD ? 1.f : g.dy};
+  plan.wz.assign((size_t)nrec * ls, 0.f);
+  plan.wx.assign((size_t)nrec * ls, 0.f);
+  for (int r = 0; r < nrec; ++r) {
+    const int i = plan.ic[3 * r], j = plan.ic[3 * r + 1], k = plan.ic[3 * r + 2];
+    if (g.twoD && k != 1) return fail(c, SW_BAD_PARAM, "2D receiver %d has non-zero y", r);
+    const int hh = sinc ? h : 0;
+    const int kk = g.twoD ? 1 : k;
+    const int hk = g.twoD ? 0 : hh;
+    if (i - hh < G.lo1 || i + hh > G.nmax1 + 4 || j - hh < G.lo2 || j + hh > G.nmax2 + 4 ||
+        kk - hk < G.lo3 || kk + hk > G.nmax3 + G.nbound)
+      return fail(c, SW_BAD_PARAM, "receiver %d footprint leaves the padded grid", r);
+    if (sinc) {
+      mksinc(&plan.wz[(size_t)r * ls], ls, dc[3 * r] / de[0]);
+      mksinc(&plan.wx[(size_t)r * ls], ls, dc[3 * r + 1] / de[1]);
+    }
+  }
+  plan.on = 1;
+  plan.mode = mode;
+  plan.nrec = nrec;
+  return SW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// One propagation on device-resident fields (propagator_acoustic)
+// ---------------------------------------------------------------------------
+
+int propagate_dev(sw_ctx *c, const sw_prop_desc &d, const DevIO &io) {
+  const sw_genpar &g = d.g;
+  int st = check_genpar(c, g);
+  if (st) return st;
+  if (d.tstep != 1 && d.tstep != -1) return fail(c, SW_BAD_PARAM, "tstep must be +-1");
+  const Geom G = make_geom(g);
+  const Coefs C = make_coefs(g);
+  const int nt = g.nt;
+  const int ntsnap = nt / g.snapi;
+  const size_t fbytes = (size_t)G.total() * sizeof(float);
+  const size_t nphys = (size_t)g.nz * g.nx * g.ny;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+
+  // Five wavefields (allocateUSpace + zeroUSpace, Propagator.f90:144-145).
+  float *f[5];
+  for (int q = 0; q < 5; ++q) {
+    f[q] = (float *)dbuf(c, "u" + std::to_string(q), fbytes, &st);
+    if (!f[q]) return st;
+    if ((e = cudaMemsetAsync(f[q], 0, fbytes, s)) != cudaSuccess) return cuda_fail(c, e, "memset");
+  }
+  float *tmp = nullptr;
+  const bool adj3d = !g.twoD && d.fd_scheme == SW_FD_ADJOINT;
+  if (adj3d) {
+    tmp = (float *)dbuf(c, "v2u", fbytes, &st);
+    if (!tmp) return st;
+    if ((e = cudaMemsetAsync(tmp, 0, fbytes, s)) != cudaSuccess) return cuda_fail(c, e, "memset");
+  }
+  // Higdon coefficients (Boundary.f90:17-63).
+  const long long n1 = G.nmax1 - G.nmin1 + 1, n2 = G.nmax2 - G.nmin2 + 1, n3 = G.nmax3 - G.nmin3 + 1;
+  float *gz = (float *)dbuf(c, "gz", 16 * n2 * n3 * sizeof(float), &st);
+  float *gx = (float *)dbuf(c, "gx", 16 * n1 * n3 * sizeof(float), &st);
+  float *gy = (float *)dbuf(c, "gy", 16 * n1 * n2 * sizeof(float), &st);
+  if (!gz || !gx || !gy) return st;
+  if ((e = launch_higdon_coeffs(G, io.vel_pad, g.dt, 1.f / g.dx, 1.f / g.dy, 1.f / g.dz, gz, gx,
+                                gy, s)) != cudaSuccess)
+    return cuda_fail(c, e, "higdon coeffs");
+  c->stats.launches_total++;
+
+  // Injection plan.
+  InjPlan inj;
+  if ((st = build_injection(c, g, G, d.injection, io.nsou, io.sou_coord, io.vel_phys_host, inj)))
+    return st;
+  int *d_off = nullptr;
+  InjEntry *d_ent = nullptr;
+  if (inj.on) {
+    d_off = (int *)dbuf(c, "inj_off", inj.off.size() * sizeof(int), &st);
+    d_ent = (InjEntry *)dbuf(c, "inj_ent", inj.ent.size() * sizeof(InjEntry), &st);
+    if (!d_off || !d_ent) return st;
+    cudaMemcpyAsync(d_off, inj.off.data(), inj.off.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if ((e = cudaMemcpyAsync(d_ent, inj.ent.data(), inj.ent.size() * sizeof(InjEntry),
+                             cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_fail(c, e, "upload injection plan");
+    // The host plan must outlive the async copies.
+    cudaStreamSynchronize(s);
+  }
+  // Extraction plan.
+  ExtPlan ext;
+  if ((st = build_extraction(c, g, G, d.extraction, io.nrec, io.rec_coord, ext))) return st;
+  int *d_ric = nullptr;
+  float *d_wz = nullptr, *d_wx = nullptr;
+  if (ext.on) {
+    d_ric = (int *)dbuf(c, "ext_ic", ext.ic.size() * sizeof(int), &st);
+    d_wz = (float *)dbuf(c, "ext_wz", ext.wz.size() * sizeof(float), &st);
+    d_wx = (float *)dbuf(c, "ext_wx", ext.wx.size() * sizeof(float), &st);
+    if (!d_ric || !d_wz || !d_wx) return st;
+    cudaMemcpyAsync(d_ric, ext.ic.data(), ext.ic.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_wz, ext.wz.data(), ext.wz.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_wx, ext.wx.data(), ext.wx.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+  }
+  // Tapers for the imaging conditions (compute_taper, Taper.f90:14-28).
+  float *d_tx = nullptr, *d_ty = nullptr;
+  if (d.imaging != SW_IMG_NONE) {
+    std::vector<float> tx, ty;
+    compute_taper(g.nx, g.ny, tx, ty);
+    d_tx = (float *)dbuf(c, "taperx", tx.size() * sizeof(float), &st);
+    d_ty = (float *)dbuf(c, "tapery", ty.size() * sizeof(float), &st);
+    if (!d_tx || !d_ty) return st;
+    cudaMemcpyAsync(d_tx, tx.data(), tx.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_ty, ty.data(), ty.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);
+  }
+
+  StepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = G;
+  a.c = C;
+  a.vel = io.vel_pad;
+  a.k12 = 12.f * (g.dt * g.dt);
+  a.div11 = 1.f / 11.f;
+  a.inj_on = inj.on;
+  a.bi0 = inj.bi0; a.bi1 = inj.bi1; a.bj0 = inj.bj0; a.bj1 = inj.bj1; a.bk0 = inj.bk0; a.bk1 = inj.bk1;
+  a.inj_off = d_off;
+  a.inj_ent = d_ent;
+  a.src_tr = io.sou_trace_dev;
+  a.nt = nt;
+  a.ref = io.ref_dev;
+  a.taperx = d_tx;
+  a.tapery = d_ty;
+  a.image = io.image_dev;
+  a.illum = io.illum_dev;
+  {
+    const float xs = g.dt * (float)g.snapi;
+    a.dt2snap = xs * xs;  // genpar%dt2 (compute_function_gradient.f90:237)
+  }
+  ExtArgs ea;
+  std::memset(&ea, 0, sizeof(ea));
+  ea.g = G;
+  ea.nrec = ext.nrec;
+  ea.nt = nt;
+  ea.half = g.lsinc / 2;
+  ea.mode = ext.mode;
+  ea.ic = d_ric;
+  ea.wz = d_wz;
+  ea.wx = d_wx;
+  ea.vel = io.vel_pad;
+  ea.tr = io.rec_trace_dev;
+  if (d.extraction == SW_EXT_LSRTM_SINC)
+    ea.vconst = g.twoD ? 1.f / (g.dz * g.dx) : 1.f / ((g.dz * g.dx) * g.dy);
+  else
+    ea.vconst = 1.f;
+  HigArgs ha;
+  ha.g = G;
+  ha.gz = gz;
+  ha.gx = gx;
+  ha.gy = gy;
+
+  // Rotating time levels (FDswaptime_pointer, FDswaptimes.f90:14-24).
+  int um1 = 0, u0 = 1, u1 = 2, u2 = 3, u3 = 4;
+  int wcounter = 0, mcounter = 0;
+  const long long npts = n1 * n2 * n3;
+  const int nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
+  int it = d.tmin;
+  for (int step = 0; step < nsteps; ++step, it += d.tstep) {
+    if (ext.on) {
+      ea.it = it;
+      ea.u2 = f[u2];
+      if ((e = launch_extract(ea, s)) != cudaSuccess) return cuda_fail(c, e, "extract");
+      c->stats.launches_total++;
+    }
+    a.u2 = f[u2]; a.u1 = f[u1]; a.u0 = f[u0]; a.um1 = f[um1]; a.u3 = f[u3];
+    a.lap_src = f[u2];
+    a.it = it;
+    a.snap_on = 0;
+    a.img = 0;
+    a.born_on = 0;
+    const bool snapstep = (it % g.snapi) == 0;
+    if (d.extract_wave && snapstep) {
+      ++wcounter;
+      if (wcounter <= ntsnap) {
+        a.snap_on = 1;
+        a.snap_out = io.wave_dev + (size_t)(wcounter - 1) * nphys;
+      }
+    }
+    if (d.imaging != SW_IMG_NONE && d.imaging != SW_IMG_BORN && d.tstep == -1 && snapstep) {
+      ++mcounter;
+      const int index = ntsnap - mcounter + 1;
+      if (index >= 1) {
+        a.img = d.imaging;
+        a.w0 = io.wave_dev + (size_t)(index - 1) * nphys;
+        a.wm1 = io.wave_dev + (size_t)(std::max(index - 1, 1) - 1) * nphys;
+        a.wp1 = io.wave_dev + (size_t)(std::min(index + 1, ntsnap) - 1) * nphys;
+      }
+    }
+    if (d.imaging == SW_IMG_BORN && d.tstep == 1 && snapstep) {
+      ++mcounter;
+      if (mcounter <= ntsnap) {
+        a.born_on = 1;
+        a.w0 = io.wave_dev + (size_t)(mcounter - 1) * nphys;
+      }
+    }
+    if (adj3d) {
+      if ((e = launch_v2u(G, io.vel_pad, f[u2], tmp, s)) != cudaSuccess) return cuda_fail(c, e, "v2u");
+      a.lap_src = tmp;
+      c->stats.launches_total++;
+    }
+    const bool timed = c->profiling;
+    if (timed) {
+      if (c->ev.size() < 2) {
+        c->ev.resize(2);
+        cudaEventCreate(&c->ev[0]);
+        cudaEventCreate(&c->ev[1]);
+      }
+      cudaEventRecord(c->ev[0], s);
+    }
+    if ((e = launch_step(a, g.twoD && d.fd_scheme == SW_FD_ADJOINT, s)) != cudaSuccess)
+      return cuda_fail(c, e, "step");
+    if (timed) {
+      cudaEventRecord(c->ev[1], s);
+      cudaEventSynchronize(c->ev[1]);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+      c->stats.step_kernel_ms += ms;
+      c->stats.step_kernel_timed++;
+      c->stats.step_bytes += (uint64_t)npts * 24ull;
+    }
+    c->stats.launches_total++;
+    c->stats.launches_step++;
+    c->stats.points_updated += (uint64_t)npts;
+    ha.u3 = f[u3];
+    ha.u2 = f[u2];
+    ha.u1 = f[u1];
+    int nl = 0;
+    if ((e = launch_higdon(ha, s, &nl)) != cudaSuccess) return cuda_fail(c, e, "higdon");
+    c->stats.launches_total += nl;
+    const int t = um1;
+    um1 = u0; u0 = u1; u1 = u2; u2 = u3; u3 = t;
+  }
+  if (io.final_u2_host) {
+    // Dense padded layout without the leading-dimension rounding.
+    e = cudaMemcpy2DAsync(io.final_u2_host, (size_t)G.n1p * sizeof(float), f[u2],
+                          (size_t)G.ld1 * sizeof(float), (size_t)G.n1p * sizeof(float),
+                          (size_t)G.n2p * G.n3p, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "download u2");
+  }
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(c, e, "propagate");
+  return SW_OK;
+}
+
+// Uploads the physical velocity and pads it on the device.
+int upload_velocity(sw_ctx *c, const sw_genpar &g, const float *vel, const char *slot,
+                    float **vel_pad) {
+  int st = SW_OK;
+  const Geom G = make_geom(g);
+  const size_t nphys = (size_t)g.nz * g.nx * g.ny;
+  float *vp = (float *)dbuf(c, std::string(slot) + "_phys", nphys * sizeof(float), &st);
+  float *pad = (float *)dbuf(c, slot, (size_t)G.total() * sizeof(float), &st);
+  if (!vp || !pad) return st;
+  cudaError_t e = cudaMemcpyAsync(vp, vel, nphys * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "upload vel");
+  if ((e = launch_pad_velocity(G, vp, pad, c->stream)) != cudaSuccess) return cuda_fail(c, e, "pad");
+  c->stats.launches_total++;
+  *vel_pad = pad;
+  return SW_OK;
+}
+
+int upload(sw_ctx *c, const char *slot, const void *h, size_t bytes, void **d) {
+  int st = SW_OK;
+  void *p = dbuf(c, slot, bytes, &st);
+  if (!p) return st;
+  if (h) {
+    cudaError_t e = cudaMemcpyAsync(p, h, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "upload");
+  } else {
+    cudaError_t e = cudaMemsetAsync(p, 0, bytes, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "memset");
+  }
+  *d = p;
+  return SW_OK;
+}
+
+int download(sw_ctx *c, void *h, const void *d, size_t bytes) {
+  cudaError_t e = cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "download");
+  return SW_OK;
+}
+
+}  // namespace swave
+
+// ---------------------------------------------------------------------------
+// Public entry points
+// ---------------------------------------------------------------------------
+
+int sw_vel_check(const sw_genpar *g, const float *vel, float *courant, float *samplerate) {
+  if (!g || !vel) return SW_BAD_PARAM;
+  const size_t n = (size_t)g->nz * g->nx * g->ny;
+  float vmax = vel[0], vmin = vel[0];
+  for (size_t q = 1; q < n; ++q) {
+    vmax = std::max(vmax, vel[q]);
+    vmin = std::min(vmin, vel[q]);
+  }
+  // vel_check (ReadSouVelRho.f90:629-656, 669-753).
+  const float stab_cond = g->twoD ? 0.45f : 0.35f;
+  const float stab = g->twoD ? vmax * g->dt / std::min(g->dz, g->dx)
+                             : vmax * g->dt / std::min(std::min(g->dz, g->dx), g->dy);
+  const float lambdamin = vmin / g->fmax;
+  const float sr = g->twoD ? lambdamin / std::max(g->dz, g->dx)
+                           : lambdamin / std::max(std::max(g->dz, g->dx), g->dy);
+  if (courant) *courant = stab;
+  if (samplerate) *samplerate = sr;
+  if (stab > stab_cond || sr < 2.0f) return SW_BAD_PARAM;
+  return SW_OK;
+}
+
+int sw_propagate(sw_ctx *c, const sw_prop_desc *d, const sw_prop_io *io) {
+  if (!c || !d || !io || !io->vel) return SW_BAD_PARAM;
+  cudaSetDevice(c->device);
+  const sw_genpar &g = d->g;
+  int st = check_genpar(c, g);
+  if (st) return st;
+  const int nt = g.nt, ntsnap = nt / g.snapi;
+  const size_t nphys = (size_t)g.nz * g.nx * g.ny;
+  DevIO dio;
+  if ((st = upload_velocity(c, g, io->vel, "vel", &dio.vel_pad))) return st;
+  dio.vel_phys_host = io->vel;
+  dio.nsou = d->injection != SW_INJ_NONE ? io->nsou : 0;
+  dio.sou_coord = io->sou_coord;
+  void *p = nullptr;
+  if (dio.nsou > 0) {
+    if (!io->sou_coord || !io->sou_trace) return fail(c, SW_BAD_PARAM, "missing source arrays");
+    if ((st = upload(c, "sou_tr", io->sou_trace, (size_t)dio.nsou * nt * sizeof(float), &p))) return st;
+    dio.sou_trace_dev = (float *)p;
+  }
+  dio.nrec = d->extraction != SW_EXT_NONE ? io->nrec : 0;
+  dio.rec_coord = io->rec_coord;
+  if (dio.nrec > 0) {
+    if (!io->rec_coord || !io->rec_trace) return fail(c, SW_BAD_PARAM, "missing receiver arrays");
+    if ((st = upload(c, "rec_tr", io->rec_trace, (size_t)dio.nrec * nt * sizeof(float), &p))) return st;
+    dio.rec_trace_dev = (float *)p;
+  }
+  const bool need_wave = d->extract_wave || d->imaging != SW_IMG_NONE;
+  if (need_wave) {
+    if (!io->wave) return fail(c, SW_BAD_PARAM, "wave array required");
+    if ((st = upload(c, "wave", io->wave, nphys * std::max(ntsnap, 1) * sizeof(float), &p))) return st;
+    dio.wave_dev = (float *)p;
+  }
+  const bool img = d->imaging != SW_IMG_NONE && d->imaging != SW_IMG_BORN;
+  if (img) {
+    if (!io->image || !io->illum) return fail(c, SW_BAD_PARAM, "image/illum required");
+    if ((st = upload(c, "image", io->image, nphys * sizeof(float), &p))) return st;
+    dio.image_dev = (float *)p;
+    if ((st = upload(c, "illum", io->illum, nphys * sizeof(float), &p))) return st;
+    dio.illum_dev = (float *)p;
+  }
+  if (d->imaging == SW_IMG_BORN) {
+    if (!io->ref) return fail(c, SW_BAD_PARAM, "ref required");
+    if ((st = upload(c, "ref", io->ref, nphys * sizeof(float), &p))) return st;
+    dio.ref_dev = (float *)p;
+  }
+  dio.final_u2_host = io->final_u2;
+  if ((st = propagate_dev(c, *d, dio))) return st;
+  if (dio.nrec > 0 && (st = download(c, io->rec_trace, dio.rec_trace_dev, (size_t)dio.nrec * nt * sizeof(float))))
+    return st;
+  if (d->extract_wave &&
+      (st = download(c, io->wave, dio.wave_dev, nphys * std::max(ntsnap, 1) * sizeof(float))))
+    return st;
+  if (img) {
+    if ((st = download(c, io->image, dio.image_dev, nphys * sizeof(float)))) return st;
+    if ((st = download(c, io->illum, dio.illum_dev, nphys * sizeof(float)))) return st;
+  }
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "sw_propagate");
+  return SW_OK;
+}
+
+static sw_prop_desc base_desc(const sw_genpar &g, bool fwd) {
+  sw_prop_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.g = g;
+  if (fwd) { d.tmin = 1; d.tmax = g.nt; d.tstep = 1; }
+  else { d.tmin = g.nt; d.tmax = 1; d.tstep = -1; }
+  return d;
+}
+
+int sw_modeling(sw_ctx *c, const sw_genpar *g, const float *vel, const float *sou_coord,
+                const float *wavelet, int nrec, const float *rec_coord, float *data,
+                float *final_u2) {
+  if (!c || !g || !vel || !sou_coord || !wavelet || !data || (nrec > 0 && !rec_coord))
+    return SW_BAD_PARAM;
+  std::fill(data, data + (size_t)nrec * g->nt, 0.f);
+  sw_prop_desc d = base_desc(*g, true);
+  d.fd_scheme = SW_FD_FORWARD;
+  d.injection = SW_INJ_SINC;
+  d.extraction = SW_EXT_SINC;
+  sw_prop_io io;
+  std::memset(&io, 0, sizeof(io));
+  io.vel = vel;
+  io.nsou = 1; io.sou_coord = sou_coord; io.sou_trace = wavelet;
+  io.nrec = nrec; io.rec_coord = rec_coord; io.rec_trace = data;
+  io.final_u2 = final_u2;
+  return sw_propagate(c, &d, &io);
+}
+
+// Forward with device snapshots, then a backward or Born propagation that
+// reads them (RTM_to_memory, LSRTM_to_memory, BORN_to_memory).
+static int two_pass(sw_ctx *c, const sw_genpar &g, const float *vel, const float *ref,
+                    const float *sou_coord, const float *wavelet, int nrec,
+                    const float *rec_coord, const float *data_in, float *data_out,
+                    float *image, float *illum, int kind) {
+  cudaSetDevice(c->device);
+  int st = check_genpar(c, g);
+  if (st) return st;
+  const int nt = g.nt, ntsnap = nt / g.snapi;
+  const size_t nphys = (size_t)g.nz * g.nx * g.ny;
+  DevIO f;
+  if ((st = upload_velocity(c, g, vel, "vel", &f.vel_pad))) return st;
+  f.vel_phys_host = vel;
+  void *p = nullptr;
+  if ((st = upload(c, "sou_tr", wavelet, (size_t)nt * sizeof(float), &p))) return st;
+  f.sou_trace_dev = (float *)p;
+  f.nsou = 1;
+  f.sou_coord = sou_coord;
+  if ((st = upload(c, "wave", nullptr, nphys * std::max(ntsnap, 1) * sizeof(float), &p))) return st;
+  f.wave_dev = (float *)p;
+  sw_prop_desc d = base_desc(g, true);
+  d.fd_scheme = SW_FD_FORWARD;
+  d.injection = SW_INJ_SINC;
+  d.extract_wave = 1;
+  if ((st = propagate_dev(c, d, f))) return st;
+
+  DevIO b;
+  b.vel_pad = f.vel_pad;
+  b.vel_phys_host = vel;
+  b.wave_dev = f.wave_dev;
+  sw_prop_desc e2;
+  if (kind == 2) {  // Born
+    e2 = base_desc(g, true);
+    e2.fd_scheme = SW_FD_FORWARD;
+    e2.injection = SW_INJ_NONE;
+    e2.extraction = SW_EXT_LSRTM_SINC;
+    e2.imaging = SW_IMG_BORN;
+    if ((st = upload(c, "ref", ref, nphys * sizeof(float), &p))) return st;
+    b.ref_dev = (float *)p;
+    b.nrec = nrec;
+    b.rec_coord = rec_coord;
+    if ((st = upload(c, "rec_tr", nullptr, (size_t)nrec * nt * sizeof(float), &p))) return st;
+    b.rec_trace_dev = (float *)p;
+  } else {
+    e2 = base_desc(g, false);
+    if (kind == 0) {  // RTM
+      e2.fd_scheme = g.twoD ? SW_FD_ADJOINT : SW_FD_FORWARD;
+      e2.injection = SW_INJ_SINC;
+      e2.imaging = SW_IMG_RTM;
+    } else {          // LSRTM
+      e2.fd_scheme = SW_FD_ADJOINT;
+      e2.injection = SW_INJ_LSRTM_SINC;
+      e2.imaging = SW_IMG_LSRTM;
+    }
+    b.nsou = nrec;
+    b.sou_coord = rec_coord;
+    if ((st = upload(c, "dat_tr", data_in, (size_t)nrec * nt * sizeof(float), &p))) return st;
+    b.sou_trace_dev = (float *)p;
+    if ((st = upload(c, "image", nullptr, nphys * sizeof(float), &p))) return st;
+    b.image_dev = (float *)p;
+    if ((st = upload(c, "illum", nullptr, nphys * sizeof(float), &p))) return st;
+    b.illum_dev = (float *)p;
+  }
+  if ((st = propagate_dev(c, e2, b))) return st;
+  if (kind == 2) {
+    if ((st = download(c, data_out, b.rec_trace_dev, (size_t)nrec * nt * sizeof(float)))) return st;
+  } else {
+    if ((st = download(c, image, b.image_dev, nphys * sizeof(float)))) return st;
+    if ((st = download(c, illum, b.illum_dev, nphys * sizeof(float)))) return st;
+  }
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "two_pass");
+  return SW_OK;
+}
+
+int sw_rtm(sw_ctx *c, const sw_genpar *g, const float *vel, const float *sou_coord,
+           const float *wavelet, int nrec, const float *rec_coord, const float *data,
+           float *image, float *illum) {
+  if (!c || !g || !vel || !sou_coord || !wavelet || !rec_coord || !data || !image || !illum)
+    return SW_BAD_PARAM;
+  return two_pass(c, *g, vel, nullptr, sou_coord, wavelet, nrec, rec_coord, data, nullptr, image,
+                  illum, 0);
+}
+
+int sw_lsrtm(sw_ctx *c, const sw_genpar *g, const float *vel, const float *sou_coord,
+             const float *wavelet, int nrec, const float *rec_coord, const float *data,
+             float *image, float *illum) {
+  if (!c || !g || !vel || !sou_coord || !wavelet || !rec_coord || !data || !image || !illum)
+    return SW_BAD_PARAM;
+  return two_pass(c, *g, vel, nullptr, sou_coord, wavelet, nrec, rec_coord, data, nullptr, image,
+                  illum, 1);
+}
+
+int sw_born(sw_ctx *c, const sw_genpar *g, const float *vel, const float *ref,
+            const float *sou_coord, const float *wavelet, int nrec, const float *rec_coord,
+            float *data) {
+  if (!c || !g || !vel || !ref || !sou_coord || !wavelet || !rec_coord || !data)
+    return SW_BAD_PARAM;
+  return two_pass(c, *g, vel, ref, sou_coord, wavelet, nrec, rec_coord, nullptr, data, nullptr,
+                  nullptr, 2);
+}
+
+int sw_born_wavelet(float *w, int nt, float dt) {
+  if (!w || nt < 1) return SW_BAD_PARAM;
+  // readsou, Born/LSRTM branch (ReadSouVelRho.f90:318-326).
+  std::vector<float> tr(w, w + nt);
+  for (int i = 0; i < nt; ++i) w[i] = 0.f;
+  for (int it = 2; it <= nt - 1; ++it)
+    w[it - 1] = w[it - 1] + ((-2 * tr[it - 1] + tr[it - 2]) + tr[it]) / (dt * dt);
+  return SW_OK;
+}

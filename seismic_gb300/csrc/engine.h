@@ -1,0 +1,73 @@
+// engine.h - host-side internals of libswave shared by engine.cu and fwi.cu.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/swave.h"
+#include "swave_dev.cuh"
+
+struct DBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+};
+
+struct sw_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::map<std::string, DBuf> bufs;
+  std::vector<cudaEvent_t> ev;
+  bool profiling = false;
+  sw_stats stats{};
+};
+
+namespace swave {
+
+struct InjPlan {
+  int on = 0;
+  int bi0 = 0, bi1 = 0, bj0 = 0, bj1 = 0, bk0 = 0, bk1 = 0;
+  std::vector<int> off;
+  std::vector<InjEntry> ent;
+};
+
+struct ExtPlan {
+  int on = 0, mode = 0, nrec = 0;
+  std::vector<int> ic;
+  std::vector<float> wz, wx;
+};
+
+// Device-side arrays of one propagation (host coordinates are kept to build
+// the injection / extraction plans).
+struct DevIO {
+  float *vel_pad = nullptr;
+  const float *vel_phys_host = nullptr;
+  int nsou = 0;
+  const float *sou_coord = nullptr;
+  const float *sou_trace_dev = nullptr;
+  int nrec = 0;
+  const float *rec_coord = nullptr;
+  float *rec_trace_dev = nullptr;
+  float *wave_dev = nullptr;
+  float *image_dev = nullptr;
+  float *illum_dev = nullptr;
+  const float *ref_dev = nullptr;
+  float *final_u2_host = nullptr;
+};
+
+int fail(sw_ctx *c, int code, const char *fmt, ...);
+int cuda_fail(sw_ctx *c, cudaError_t e, const char *what);
+void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st);
+int check_genpar(sw_ctx *c, const sw_genpar &g);
+Geom make_geom(const sw_genpar &g);
+Coefs make_coefs(const sw_genpar &g);
+void mksinc(float *sinc, int lsinc, float shift);
+void compute_taper(int nxw, int nyw, std::vector<float> &tx, std::vector<float> &ty);
+int propagate_dev(sw_ctx *c, const sw_prop_desc &d, const DevIO &io);
+int upload_velocity(sw_ctx *c, const sw_genpar &g, const float *vel, const char *slot,
+                    float **vel_pad);
+int upload(sw_ctx *c, const char *slot, const void *h, size_t bytes, void **d);
+int download(sw_ctx *c, void *h, const void *d, size_t bytes);
+
+}  // namespace swave

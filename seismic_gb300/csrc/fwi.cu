@@ -1,0 +1,828 @@
+// fwi.cu - FWI objective/gradient driver and the FP64 L-BFGS of libswave.
+//
+// compute_fct_gdt (progs/afwi/compute_function_gradient.f90:208-350) runs
+// shot by shot on the device; the misfit is accumulated in FP64 in the
+// reference's trace order.  The L-BFGS keeps its correction pairs and
+// search vectors in HBM in FP64 (libs/libinv/lbfgs.f:49-558); only the
+// scalar line-search logic (MCSRCH/MCSTEP) runs on the host.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swave.h"
+#include "engine.h"
+#include "swave_dev.cuh"
+
+using namespace swave;
+
+namespace {
+
+constexpr int kRedBlocks = 296;  // 2 x 148: fixed partition => deterministic sums
+constexpr int kRedThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Post-processing kernels (compute_function_gradient.f90:332-343)
+// ---------------------------------------------------------------------------
+__global__ void k_illu_pow(long long n, float p, float *il) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    il[q] = powf(il[q], p);
+}
+
+// Per-block partial max(illum) and sum(dprod(illum, illum)); also scales the
+// gradient: grad = 2*grad/sngl(scaling).
+__global__ void k_grad_scale_stats(long long n, float sscal, float *grad, const float *il,
+                                   float *pmax, double *psum) {
+  __shared__ float smax[kRedThreads];
+  __shared__ double ssum[kRedThreads];
+  float m = -INFINITY;
+  double s = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    grad[q] = (2.0f * grad[q]) / sscal;
+    const float v = il[q];
+    m = fmaxf(m, v);
+    s = s + (double)v * (double)v;
+  }
+  smax[threadIdx.x] = m;
+  ssum[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      smax[threadIdx.x] = fmaxf(smax[threadIdx.x], smax[threadIdx.x + w]);
+      ssum[threadIdx.x] = ssum[threadIdx.x] + ssum[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pmax[blockIdx.x] = smax[0];
+    psum[blockIdx.x] = ssum[0];
+  }
+}
+
+__global__ void k_final_stats(int nb, long long n, const float *pmax, const double *psum,
+                              float *maxil, double *rmsil) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float m = pmax[0];
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) {
+    m = fmaxf(m, pmax[b]);
+    s = s + psum[b];
+  }
+  *maxil = m;
+  *rmsil = sqrt(s / (double)n);
+}
+
+// illu = (illu + maxval/10000)/sqrt(sum(dprod)/size); grad = grad/illu*mask.
+__global__ void k_normalise(long long n, const float *maxil, const double *rmsil, float *il,
+                            float *grad, const float *mask) {
+  const float m = *maxil;
+  const double r = *rmsil;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float v = (float)((double)(il[q] + m / 10000.f) / r);
+    il[q] = v;
+    float g = grad[q] / v;
+    g = g * (mask ? mask[q] : 1.0f);
+    grad[q] = g;
+  }
+}
+
+__global__ void k_mask(long long n, float *grad, const float *mask) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    grad[q] = grad[q] * (mask ? mask[q] : 1.0f);
+}
+
+// triangle (Smoothing.f90:140-181) with boxconv (Smoothing.f90:194-227): one
+// thread per line; element e of line l is at base(l) + e*estride.  The
+// three work vectors of each line live in `scratch`.
+__device__ void d_boxconv(int nb, int nx, const float *xx, float *yy, float *bb) {
+  const int ny = nx + nb - 1;
+  bb[0] = xx[0];
+  for (int i = 2; i <= nx; ++i) bb[i - 1] = bb[i - 2] + xx[i - 1];
+  for (int i = nx + 1; i <= ny; ++i) bb[i - 1] = bb[i - 2];
+  for (int i = 1; i <= nb; ++i) yy[i - 1] = bb[i - 1];
+  for (int i = nb + 1; i <= ny; ++i) yy[i - 1] = bb[i - 1] - bb[i - nb - 1];
+  for (int i = 1; i <= ny; ++i) yy[i - 1] = yy[i - 1] / (float)nb;
+}
+
+__global__ void k_triangle(int n12, int nr, int nlines, int lines_inner, long long lstride_in,
+                           long long lstride_out, long long estride, const float *uu, float *vv,
+                           float *scratch) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nlines) return;
+  // Line l = (a, b) with a < lines_inner fastest.
+  const int la = l % lines_inner, lb = l / lines_inner;
+  const long long base = (long long)la * lstride_in + (long long)lb * lstride_out;
+  const long long per = 4LL * (n12 + 2 * nr);
+  float *qq = scratch + (long long)l * per;
+  float *pp = qq + (n12 + 2 * nr);
+  float *bb = pp + (n12 + 2 * nr);
+  float *tt = bb + (n12 + 2 * nr);
+  for (int i = 0; i < n12; ++i) qq[i] = uu[base + i * estride];
+  if (n12 == 1) {
+    tt[0] = qq[0];
+  } else {
+    d_boxconv(nr, n12, qq, pp, bb);
+    const int np = nr + n12 - 1;
+    d_boxconv(nr, np, pp, qq, bb);
+    for (int i = 1; i <= n12; ++i) tt[i - 1] = qq[i + nr - 2];
+    for (int i = 1; i <= nr - 1; ++i) tt[i - 1] = tt[i - 1] + qq[nr - i - 1];
+    for (int i = 1; i <= nr - 1; ++i) tt[n12 - i] = tt[n12 - i] + qq[n12 + (nr - 1) + i - 1];
+  }
+  for (int i = 0; i < n12; ++i) vv[base + i * estride] = tt[i];
+}
+
+// ---------------------------------------------------------------------------
+// FP64 vector kernels for the L-BFGS
+// ---------------------------------------------------------------------------
+__global__ void k_dot_partial(long long n, const double *a, const double *b, double *part) {
+  __shared__ double sh[kRedThreads];
+  double s = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    s = s + a[q] * b[q];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_sum_partials(int nb, const double *part, double *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s = s + part[b];
+  *out = s;
+}
+
+// y = a*x + y  (a on host)
+__global__ void k_axpy(long long n, double a, const double *x, double *y) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    y[q] = y[q] + a * x[q];
+}
+// y = y - a*x
+__global__ void k_aymx(long long n, double a, const double *x, double *y) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    y[q] = y[q] - a * x[q];
+}
+// y = a*y
+__global__ void k_scal(long long n, double a, double *y) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    y[q] = a * y[q];
+}
+// y = -x*d (d scalar; DIAG is uniform when DIAGCO = .false.)
+__global__ void k_negmul(long long n, const double *x, double d, double *y) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    y[q] = -x[q] * d;
+}
+// z = x - y
+__global__ void k_sub(long long n, const double *x, const double *y, double *z) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    z[q] = x[q] - y[q];
+}
+// x = wa + stp*s
+__global__ void k_step_x(long long n, const double *wa, double stp, const double *s, double *x) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    x[q] = wa[q] + stp * s[q];
+}
+// FREEZE_X (lbfgs.f:1-43)
+__global__ void k_freeze(long long n, int type, double xmin, double xmax, const float *mask,
+                         const double *xinit, double *x) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    double v = x[q];
+    if (type) {
+      v = fmax(xmin, v);
+      v = fmin(xmax, v);
+    } else {
+      const float m = mask[q];
+      if (m != 0.f && m != 2.f) {
+        v = fmax(xmin, v);
+        v = fmin(xmax, v);
+      }
+      if (m == 0.f || m == 2.f) v = xinit[q];
+    }
+    x[q] = v;
+  }
+}
+
+inline int gsz(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)std::max(1LL, std::min(b, 152LL * 8));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// compute_fct_gdt
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Window {
+  float oxw, oyw, endx, endy;
+  int nxw, nyw;
+};
+
+// extract_coord_source_receiver_patch (ExtractPadModel.f90:19-85) and the
+// window size of copy_window_vel_gath (ExtractPadModel.f90:446-451).
+int shot_window(sw_ctx *c, const sw_fwi_desc &d, const sw_fwi_shot &s, Window &w) {
+  const sw_genpar &g = d.g;
+  if (s.nrec < 1 || !s.rec_coord || !s.dobs) return fail(c, SW_BAD_PARAM, "shot without receivers");
+  const float sx = s.sou_coord[1], sy = s.sou_coord[2];
+  float gx1 = s.rec_coord[1], gy1 = s.rec_coord[2], gxn = gx1, gyn = gy1;
+  for (int i = 1; i < s.nrec; ++i) {
+    gx1 = std::min(gx1, s.rec_coord[3 * i + 1]);
+    gxn = std::max(gxn, s.rec_coord[3 * i + 1]);
+    gy1 = std::min(gy1, s.rec_coord[3 * i + 2]);
+    gyn = std::max(gyn, s.rec_coord[3 * i + 2]);
+  }
+  const float minx = std::min(sx, gx1), miny = std::min(sy, gy1);
+  const float maxx = std::max(sx, gxn), maxy = std::max(sy, gyn);
+  const float mx1 = (gx1 + sx) / 2, mxn = (gxn + sx) / 2;
+  const float my1 = (gy1 + sy) / 2, myn = (gyn + sy) / 2;
+  const float cx = mx1 + std::fabs(mxn - mx1) / 2;
+  const float cy = my1 + std::fabs(myn - my1) / 2;
+  w.oxw = std::min(minx, cx - d.aperture_x / 2);
+  w.endx = std::max(maxx, cx + d.aperture_x / 2);
+  w.oyw = std::min(miny, cy - d.aperture_y / 2);
+  w.endy = std::max(maxy, cy + d.aperture_y / 2);
+  w.nxw = (int)lroundf((w.endx - w.oxw) / g.dx) + 1;
+  w.nyw = (int)lroundf((w.endy - w.oyw) / g.dy) + 1;
+  if (g.twoD) {
+    w.nyw = 1;
+    w.oyw = g.oy;
+  }
+  if (w.nxw < 4 || w.nyw < 1) return fail(c, SW_BAD_PARAM, "degenerate shot window");
+  return SW_OK;
+}
+
+}  // namespace
+
+int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const float *wavelet,
+                   int nshot, const sw_fwi_shot *shots, const float *vpmask, double *f,
+                   float *grad, float *illum) {
+  if (!c || !dp || !vel || !wavelet || nshot < 1 || !shots || !f || !grad) return SW_BAD_PARAM;
+  cudaSetDevice(c->device);
+  const sw_fwi_desc &d = *dp;
+  const sw_genpar &G = d.g;
+  int st = check_genpar(c, G);
+  if (st) return st;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  const long long nfull = (long long)G.nz * G.nx * G.ny;
+  const int nt = G.nt;
+  void *p = nullptr;
+  if ((st = upload(c, "fwi_vel", vel, nfull * sizeof(float), &p))) return st;
+  const float *dvel = (const float *)p;
+  if ((st = upload(c, "fwi_grad", nullptr, nfull * sizeof(float), &p))) return st;
+  float *dgrad = (float *)p;
+  if ((st = upload(c, "fwi_illum", nullptr, nfull * sizeof(float), &p))) return st;
+  float *dill = (float *)p;
+  if ((st = upload(c, "sou_tr", wavelet, (size_t)nt * sizeof(float), &p))) return st;
+  const float *dwav = (const float *)p;
+
+  double fsum = 0.0;
+  long long ntotal = 0;
+  std::vector<float> hv;
+  std::vector<double> part;
+  for (int is = 0; is < nshot; ++is) {
+    const sw_fwi_shot &sh = shots[is];
+    Window w;
+    if ((st = shot_window(c, d, sh, w))) return st;
+    sw_genpar g = G;
+    g.nx = w.nxw;
+    g.ny = w.nyw;
+    g.ox = w.oxw;
+    g.oy = w.oyw;
+    const Geom Gw = make_geom(g);
+    const size_t nw = (size_t)g.nz * g.nx * g.ny;
+    const int ntsnap = nt / g.snapi;
+    // copy_window_vel_gath: window the model on the device, then pad.
+    float *vsmall = (float *)dbuf(c, "vel_phys", nw * sizeof(float), &st);
+    float *vpad = (float *)dbuf(c, "vel", (size_t)Gw.total() * sizeof(float), &st);
+    if (!vsmall || !vpad) return st;
+    if ((e = launch_window_vel(G.nz, G.nx, G.ny, G.ox, G.oy, G.dx, G.dy, w.nxw, w.nyw, w.oxw,
+                               w.oyw, dvel, vsmall, s)) != cudaSuccess)
+      return cuda_fail(c, e, "window vel");
+    if ((e = launch_pad_velocity(Gw, vsmall, vpad, s)) != cudaSuccess) return cuda_fail(c, e, "pad");
+    c->stats.launches_total += 2;
+    // Host copy of the window velocity: the injection weights v^2 at the
+    // source node are part of the injection plan.
+    hv.resize(nw);
+    if ((st = download(c, hv.data(), vsmall, nw * sizeof(float)))) return st;
+    cudaStreamSynchronize(s);
+    // AMOD_to_memory (to_disk_to_memory_AMOD.f90:27-82).
+    DevIO a;
+    a.vel_pad = vpad;
+    a.vel_phys_host = hv.data();
+    a.nsou = 1;
+    a.sou_coord = sh.sou_coord;
+    a.sou_trace_dev = dwav;
+    a.nrec = sh.nrec;
+    a.rec_coord = sh.rec_coord;
+    if ((st = upload(c, "rec_tr", nullptr, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
+    a.rec_trace_dev = (float *)p;
+    if ((st = upload(c, "wave", nullptr, nw * std::max(ntsnap, 1) * sizeof(float), &p))) return st;
+    a.wave_dev = (float *)p;
+    sw_prop_desc fd;
+    std::memset(&fd, 0, sizeof(fd));
+    fd.g = g;
+    fd.tmin = 1; fd.tmax = nt; fd.tstep = 1;
+    fd.fd_scheme = SW_FD_FORWARD;
+    fd.injection = SW_INJ_SINC;
+    fd.extraction = SW_EXT_SIMPLE_AFWI;
+    fd.extract_wave = 1;
+    if ((st = propagate_dev(c, fd, a))) return st;
+    // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40).
+    float *ddobs = nullptr, *dmute = nullptr, *dres = nullptr;
+    if ((st = upload(c, "dobs", sh.dobs, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
+    ddobs = (float *)p;
+    if (sh.mute) {
+      if ((st = upload(c, "mute", sh.mute, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
+      dmute = (float *)p;
+    }
+    if (sh.resid) {
+      dres = (float *)dbuf(c, "resid", (size_t)sh.nrec * nt * sizeof(float), &st);
+      if (!dres) return st;
+    }
+    double *dpart = (double *)dbuf(c, "fpart", (size_t)sh.nrec * sizeof(double), &st);
+    if (!dpart) return st;
+    if ((e = launch_residual(sh.nrec, nt, ddobs, dmute, a.rec_trace_dev, dres, dpart, s)) !=
+        cudaSuccess)
+      return cuda_fail(c, e, "residual");
+    c->stats.launches_total++;
+    part.resize(sh.nrec);
+    if ((st = download(c, part.data(), dpart, (size_t)sh.nrec * sizeof(double)))) return st;
+    if (sh.resid && (st = download(c, sh.resid, dres, (size_t)sh.nrec * nt * sizeof(float)))) return st;
+    // AGRAD_to_memory (to_disk_to_memory_AGRAD.f90:27-79).
+    DevIO b;
+    b.vel_pad = vpad;
+    b.vel_phys_host = hv.data();
+    b.nsou = sh.nrec;
+    b.sou_coord = sh.rec_coord;
+    b.sou_trace_dev = a.rec_trace_dev;
+    b.wave_dev = a.wave_dev;
+    if ((st = upload(c, "image", nullptr, nw * sizeof(float), &p))) return st;
+    b.image_dev = (float *)p;
+    if ((st = upload(c, "illum", nullptr, nw * sizeof(float), &p))) return st;
+    b.illum_dev = (float *)p;
+    sw_prop_desc bd;
+    std::memset(&bd, 0, sizeof(bd));
+    bd.g = g;
+    bd.tmin = nt; bd.tmax = 1; bd.tstep = -1;
+    bd.fd_scheme = SW_FD_FORWARD;
+    bd.injection = SW_INJ_SIMPLE;
+    bd.imaging = SW_IMG_AFWI;
+    if ((st = propagate_dev(c, bd, b))) return st;
+    // mod_copy_image (ExtractPadModel.f90:662-697), shots in order.
+    if ((e = launch_copy_image(G.nz, G.nx, G.ny, G.ox, G.oy, G.dx, G.dy, w.nxw, w.nyw, w.oxw,
+                               w.oyw, b.image_dev, b.illum_dev, dgrad, dill, s)) != cudaSuccess)
+      return cuda_fail(c, e, "copy image");
+    c->stats.launches_total++;
+    cudaStreamSynchronize(s);
+    for (int r = 0; r < sh.nrec; ++r) fsum = fsum + part[r];
+    ntotal += sh.nrec;
+  }
+  // Post-processing (compute_function_gradient.f90:314-343).
+  if (d.illu_pow != 1.f) {
+    k_illu_pow<<<gsz(nfull), 256, 0, s>>>(nfull, d.illu_pow, dill);
+    c->stats.launches_total++;
+  }
+  const double scaling = (double)(2LL * nt * ntotal);
+  float *pmax = (float *)dbuf(c, "red_pmax", kRedBlocks * sizeof(float), &st);
+  double *psum = (double *)dbuf(c, "red_psum", kRedBlocks * sizeof(double), &st);
+  float *maxil = (float *)dbuf(c, "red_maxil", sizeof(float), &st);
+  double *rmsil = (double *)dbuf(c, "red_rmsil", sizeof(double), &st);
+  if (!pmax || !psum || !maxil || !rmsil) return st;
+  k_grad_scale_stats<<<kRedBlocks, kRedThreads, 0, s>>>(nfull, (float)scaling, dgrad, dill, pmax,
+                                                       psum);
+  k_final_stats<<<1, 32, 0, s>>>(kRedBlocks, nfull, pmax, psum, maxil, rmsil);
+  float *dmask = nullptr;
+  if (vpmask) {
+    if ((st = upload(c, "vpmask", vpmask, nfull * sizeof(float), &p))) return st;
+    dmask = (float *)p;
+  }
+  k_normalise<<<gsz(nfull), 256, 0, s>>>(nfull, maxil, rmsil, dill, dgrad, dmask);
+  c->stats.launches_total += 3;
+  // triangle2 (Smoothing.f90:87-138); y pass with rect3/n3 (see the oracle).
+  const int n1 = G.nz, n2 = G.nx, n3 = G.ny;
+  float *tmpb = (float *)dbuf(c, "tri_out", nfull * sizeof(float), &st);
+  if (!tmpb) return st;
+  auto tri = [&](int n12, int nr, int nlines, int inner, long long ls_in, long long ls_out,
+                 long long es) -> int {
+    if (nr < 1 || nr > n12) return fail(c, SW_BAD_PARAM, "triangle radius %d out of range", nr);
+    const size_t per = 4ull * (size_t)(n12 + 2 * nr);
+    float *scr = (float *)dbuf(c, "tri_scr", per * (size_t)nlines * sizeof(float), &st);
+    if (!scr) return st;
+    k_triangle<<<(nlines + 127) / 128, 128, 0, s>>>(n12, nr, nlines, inner, ls_in, ls_out, es,
+                                                    dgrad, tmpb, scr);
+    cudaError_t ee = cudaMemcpyAsync(dgrad, tmpb, nfull * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    c->stats.launches_total++;
+    return ee == cudaSuccess ? SW_OK : cuda_fail(c, ee, "triangle");
+  };
+  if (d.smooth_dox && (st = tri(n2, d.smooth_rect2, n1 * n3, n1, 1, (long long)n1 * n2, n1))) return st;
+  if (d.smooth_doz && (st = tri(n1, d.smooth_rect1, n2 * n3, n2, n1, (long long)n1 * n2, 1))) return st;
+  if (d.smooth_doy && n3 > 1 &&
+      (st = tri(n3, d.smooth_rect3, n1 * n2, n1, 1, n1, (long long)n1 * n2)))
+    return st;
+  k_mask<<<gsz(nfull), 256, 0, s>>>(nfull, dgrad, dmask);
+  c->stats.launches_total++;
+  if ((st = download(c, grad, dgrad, nfull * sizeof(float)))) return st;
+  if (illum && (st = download(c, illum, dill, nfull * sizeof(float)))) return st;
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "fwi");
+  *f = fsum / scaling;
+  return SW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// L-BFGS (libs/libinv/lbfgs.f) with device-resident FP64 vectors
+// ---------------------------------------------------------------------------
+struct sw_lbfgs {
+  sw_ctx *c;
+  int n, m;
+  double xmin, xmax;
+  int boundt, type;
+  float *mask = nullptr;     // device
+  double *xinit = nullptr;   // device
+  double *S = nullptr;       // m search steps, n each
+  double *Y = nullptr;       // m gradient differences
+  double *w0 = nullptr;      // W(1..N)
+  double *wa = nullptr;      // DIAG used as MCSRCH work array
+  double *x = nullptr, *g = nullptr;
+  double *part = nullptr, *res = nullptr;
+  std::vector<double> rho, alpha;   // W(N+1..N+M), W(N+M+1..N+2M)
+  // LBFGS SAVE state
+  int iter = 0, nfun = 0, point = 0, npt = 0, bound = 0, info = 0, nfev = 0, maxfev = 20, cp = 0;
+  double stp = 0, stp1 = 0, ftol = 1e-4, gnorm = 0, xnorm = 0, ys = 0, yy = 0, diag = 1.0;
+  bool finish = false;
+  // MCSRCH SAVE state
+  int infoc = 0;
+  bool brackt = false, stage1 = true;
+  double dg = 0, dgm = 0, dginit = 0, dgtest = 0, dgx = 0, dgxm = 0, dgy = 0, dgym = 0, finit = 0,
+         ftest1 = 0, fm = 0, fx = 0, fxm = 0, fy = 0, fym = 0, stx = 0, sty = 0, stmin = 0,
+         stmax = 0, width = 0, width1 = 0;
+};
+
+namespace {
+const double kGTOL = 0.9, kSTPMIN = 1.0e-20, kSTPMAX = 1.0e+20;
+
+double ddot(sw_lbfgs &L, const double *a, const double *b) {
+  cudaStream_t s = L.c->stream;
+  k_dot_partial<<<kRedBlocks, kRedThreads, 0, s>>>(L.n, a, b, L.part);
+  k_sum_partials<<<1, 32, 0, s>>>(kRedBlocks, L.part, L.res);
+  L.c->stats.launches_total += 2;
+  double h = 0.0;
+  cudaMemcpyAsync(&h, L.res, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  return h;
+}
+
+void freeze(sw_lbfgs &L, double *x) {
+  k_freeze<<<gsz(L.n), 256, 0, L.c->stream>>>(L.n, L.type, L.xmin, L.xmax, L.mask, L.xinit, x);
+  L.c->stats.launches_total++;
+}
+
+// MCSTEP (lbfgs.f:985-1210); identical scalar code to the oracle.
+void mcstep(double &stx, double &fx, double &dx, double &sty, double &fy, double &dy, double &stp,
+            double fp, double dp, bool &brackt, double stpmin, double stpmax, int &info) {
+  info = 0;
+  if ((brackt && (stp <= std::min(stx, sty) || stp >= std::max(stx, sty))) ||
+      dx * (stp - stx) >= 0.0 || stpmax < stpmin)
+    return;
+  const double sgnd = dp * (dx / std::fabs(dx));
+  bool bound;
+  double theta, s, gamma, p, q, r, stpc, stpq, stpf;
+  if (fp > fx) {
+    info = 1;
+    bound = true;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp < stx) gamma = -gamma;
+    p = (gamma - dx) + theta;
+    q = ((gamma - dx) + gamma) + dp;
+    r = p / q;
+    stpc = stx + r * (stp - stx);
+    stpq = stx + ((dx / ((fx - fp) / (stp - stx) + dx)) / 2) * (stp - stx);
+    stpf = (std::fabs(stpc - stx) < std::fabs(stpq - stx)) ? stpc : stpc + (stpq - stpc) / 2;
+    brackt = true;
+  } else if (sgnd < 0.0) {
+    info = 2;
+    bound = false;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt((theta / s) * (theta / s) - (dx / s) * (dp / s));
+    if (stp > stx) gamma = -gamma;
+    p = (gamma - dp) + theta;
+    q = ((gamma - dp) + gamma) + dx;
+    r = p / q;
+    stpc = stp + r * (stx - stp);
+    stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    stpf = (std::fabs(stpc - stp) > std::fabs(stpq - stp)) ? stpc : stpq;
+    brackt = true;
+  } else if (std::fabs(dp) < std::fabs(dx)) {
+    info = 3;
+    bound = true;
+    theta = 3 * (fx - fp) / (stp - stx) + dx + dp;
+    s = std::max(std::max(std::fabs(theta), std::fabs(dx)), std::fabs(dp));
+    gamma = s * std::sqrt(std::max(0.0, (theta / s) * (theta / s) - (dx / s) * (dp / s)));
+    if (stp > stx) gamma = -gamma;
+    p = (gamma - dp) + theta;
+    q = (gamma + (dx - dp)) + gamma;
+    r = p / q;
+    if (r < 0.0 && gamma != 0.0) stpc = stp + r * (stx - stp);
+    else if (stp > stx) stpc = stpmax;
+    else stpc = stpmin;
+    stpq = stp + (dp / (dp - dx)) * (stx - stp);
+    if (brackt) stpf = (std::fabs(stp - stpc) < std::fabs(stp - stpq)) ? stpc : stpq;
+    else stpf = (std::fabs(stp - stpc) > std::fabs(stp - stpq)) ? stpc : stpq;
+  } else {
+    info = 4;
+    bound = false;
+    if (brackt) {
+      theta = 3 * (fp - fy) / (sty - stp) + dy + dp;
+      s = std::max(std::max(std::fabs(theta), std::fabs(dy)), std::fabs(dp));
+      gamma = s * std::sqrt((theta / s) * (theta / s) - (dy / s) * (dp / s));
+      if (stp > sty) gamma = -gamma;
+      p = (gamma - dp) + theta;
+      q = ((gamma - dp) + gamma) + dy;
+      r = p / q;
+      stpc = stp + r * (sty - stp);
+      stpf = stpc;
+    } else if (stp > stx) {
+      stpf = stpmax;
+    } else {
+      stpf = stpmin;
+    }
+  }
+  if (fp > fx) {
+    sty = stp; fy = fp; dy = dp;
+  } else {
+    if (sgnd < 0.0) { sty = stx; fy = fx; dy = dx; }
+    stx = stp; fx = fp; dx = dp;
+  }
+  stpf = std::min(stpmax, stpf);
+  stpf = std::max(stpmin, stpf);
+  stp = stpf;
+  const double p66s = (double)0.66f;  // REAL literal in the F77 source
+  if (brackt && bound) {
+    if (sty > stx) stp = std::min(stx + p66s * (sty - stx), stp);
+    else stp = std::max(stx + p66s * (sty - stx), stp);
+  }
+}
+
+// MCSRCH (lbfgs.f:652-982) with device vectors.
+void mcsrch(sw_lbfgs &L, double f, const double *s, double xtol) {
+  const double p5 = 0.5, p66 = 0.66, xtrapf = 4.0, zero = 0.0;
+  cudaStream_t st = L.c->stream;
+  if (L.info == -1) goto L45;
+  L.infoc = 1;
+  if (L.n <= 0 || L.stp <= zero || L.ftol < zero || xtol < zero || L.maxfev <= 0) return;
+  L.dginit = ddot(L, L.g, s);
+  if (L.dginit >= zero) return;
+  L.brackt = false;
+  L.stage1 = true;
+  L.nfev = 0;
+  L.finit = f;
+  L.dgtest = L.ftol * L.dginit;
+  L.width = kSTPMAX - kSTPMIN;
+  L.width1 = L.width / p5;
+  cudaMemcpyAsync(L.wa, L.x, (size_t)L.n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  L.stx = zero; L.fx = L.finit; L.dgx = L.dginit;
+  L.sty = zero; L.fy = L.finit; L.dgy = L.dginit;
+L30:
+  if (L.brackt) {
+    L.stmin = std::min(L.stx, L.sty);
+    L.stmax = std::max(L.stx, L.sty);
+  } else {
+    L.stmin = L.stx;
+    L.stmax = L.stp + xtrapf * (L.stp - L.stx);
+  }
+  L.stp = std::max(L.stp, kSTPMIN);
+  L.stp = std::min(L.stp, kSTPMAX);
+  if ((L.brackt && (L.stp <= L.stmin || L.stp >= L.stmax)) || L.nfev >= L.maxfev - 1 ||
+      L.infoc == 0 || (L.brackt && L.stmax - L.stmin <= xtol * L.stmax))
+    L.stp = L.stx;
+  k_step_x<<<gsz(L.n), 256, 0, st>>>(L.n, L.wa, L.stp, s, L.x);
+  L.c->stats.launches_total++;
+  if (L.boundt == 1) freeze(L, L.x);
+  L.info = -1;
+  return;
+L45:
+  L.info = 0;
+  L.nfev = L.nfev + 1;
+  L.dg = ddot(L, L.g, s);
+  L.ftest1 = L.finit + L.stp * L.dgtest;
+  if ((L.brackt && (L.stp <= L.stmin || L.stp >= L.stmax)) || L.infoc == 0) L.info = 6;
+  if (L.stp == kSTPMAX && f <= L.ftest1 && L.dg <= L.dgtest) L.info = 5;
+  if (L.stp == kSTPMIN && (f > L.ftest1 || L.dg >= L.dgtest)) L.info = 4;
+  if (L.nfev >= L.maxfev) L.info = 3;
+  if (L.brackt && L.stmax - L.stmin <= xtol * L.stmax) L.info = 2;
+  if (f <= L.ftest1 && std::fabs(L.dg) <= kGTOL * (-L.dginit)) L.info = 1;
+  if (L.info != 0) return;
+  if (L.stage1 && f <= L.ftest1 && L.dg >= std::min(L.ftol, kGTOL) * L.dginit) L.stage1 = false;
+  if (L.stage1 && f <= L.fx && f > L.ftest1) {
+    L.fm = f - L.stp * L.dgtest;
+    L.fxm = L.fx - L.stx * L.dgtest;
+    L.fym = L.fy - L.sty * L.dgtest;
+    L.dgm = L.dg - L.dgtest;
+    L.dgxm = L.dgx - L.dgtest;
+    L.dgym = L.dgy - L.dgtest;
+    mcstep(L.stx, L.fxm, L.dgxm, L.sty, L.fym, L.dgym, L.stp, L.fm, L.dgm, L.brackt, L.stmin,
+           L.stmax, L.infoc);
+    L.fx = L.fxm + L.stx * L.dgtest;
+    L.fy = L.fym + L.sty * L.dgtest;
+    L.dgx = L.dgxm + L.dgtest;
+    L.dgy = L.dgym + L.dgtest;
+  } else {
+    mcstep(L.stx, L.fx, L.dgx, L.sty, L.fy, L.dgy, L.stp, f, L.dg, L.brackt, L.stmin, L.stmax,
+           L.infoc);
+  }
+  if (L.brackt) {
+    if (std::fabs(L.sty - L.stx) >= p66 * L.width1) L.stp = L.stx + p5 * (L.sty - L.stx);
+    L.width1 = L.width;
+    L.width = std::fabs(L.sty - L.stx);
+  }
+  goto L30;
+}
+
+void free_lbfgs(sw_lbfgs *L) {
+  for (void *q : {(void *)L->mask, (void *)L->xinit, (void *)L->S, (void *)L->Y, (void *)L->w0,
+                  (void *)L->wa, (void *)L->x, (void *)L->g, (void *)L->part, (void *)L->res})
+    if (q) cudaFree(q);
+}
+
+}  // namespace
+
+int sw_lbfgs_create(sw_ctx *c, int n, int m, double xmin, double xmax, const float *mask,
+                    int bound_type, int freeze_soft, const double *xinit, sw_lbfgs **out) {
+  if (!c || n <= 0 || m <= 0 || !out || !mask || !xinit) return SW_BAD_PARAM;
+  cudaSetDevice(c->device);
+  sw_lbfgs *L = new sw_lbfgs();
+  L->c = c;
+  L->n = n;
+  L->m = m;
+  L->xmin = xmin;
+  L->xmax = xmax;
+  L->boundt = bound_type;
+  L->type = freeze_soft != 0;
+  L->rho.assign(m + 1, 0.0);
+  L->alpha.assign(m + 1, 0.0);
+  const size_t nb = (size_t)n * sizeof(double);
+  bool ok = cudaMalloc(&L->mask, (size_t)n * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&L->xinit, nb) == cudaSuccess &&
+            cudaMalloc(&L->S, nb * m) == cudaSuccess && cudaMalloc(&L->Y, nb * m) == cudaSuccess &&
+            cudaMalloc(&L->w0, nb) == cudaSuccess && cudaMalloc(&L->wa, nb) == cudaSuccess &&
+            cudaMalloc(&L->x, nb) == cudaSuccess && cudaMalloc(&L->g, nb) == cudaSuccess &&
+            cudaMalloc(&L->part, kRedBlocks * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&L->res, sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    free_lbfgs(L);
+    delete L;
+    return fail(c, SW_OOM_ADMISSION, "L-BFGS state of n=%d m=%d does not fit", n, m);
+  }
+  cudaMemcpy(L->mask, mask, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(L->xinit, xinit, nb, cudaMemcpyHostToDevice);
+  cudaMemset(L->S, 0, nb * m);
+  cudaMemset(L->Y, 0, nb * m);
+  *out = L;
+  return SW_OK;
+}
+
+int sw_lbfgs_destroy(sw_lbfgs *L) {
+  if (!L) return SW_OK;
+  cudaSetDevice(L->c->device);
+  cudaStreamSynchronize(L->c->stream);
+  free_lbfgs(L);
+  delete L;
+  return SW_OK;
+}
+
+int sw_lbfgs_diag(const sw_lbfgs *L, double *o) {
+  if (!L || !o) return SW_BAD_PARAM;
+  o[0] = L->iter; o[1] = L->nfun; o[2] = L->stp; o[3] = L->gnorm;
+  o[4] = L->ys; o[5] = L->yy; o[6] = L->dginit; o[7] = L->dg;
+  return SW_OK;
+}
+
+// LBFGS (lbfgs.f:49-558) with DIAGCO = .false.
+int sw_lbfgs_step(sw_lbfgs *Lp, double *xh, double f, const double *gh, double eps, double xtol,
+                  int *iflag, int *myinfo) {
+  if (!Lp || !xh || !gh || !iflag || !myinfo) return SW_BAD_PARAM;
+  sw_lbfgs &L = *Lp;
+  sw_ctx *c = L.c;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n = L.n, m = L.m;
+  const size_t nb = (size_t)n * sizeof(double);
+  cudaMemcpyAsync(L.x, xh, nb, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(L.g, gh, nb, cudaMemcpyHostToDevice, s);
+  double *Sv = nullptr;
+  if (*iflag == 0) goto L10;
+  if (*iflag == 1) goto L172;
+  if (*iflag == 2) goto L100;
+  return fail(c, SW_BAD_PARAM, "iflag must be 0, 1 or 2");
+L10:
+  L.iter = 0;
+  L.nfun = 1;
+  L.point = 0;
+  L.finish = false;
+  L.diag = 1.0;
+  k_negmul<<<gsz(n), 256, 0, s>>>(n, L.g, L.diag, L.S);  // W(ISPT+I) = -G(I)*DIAG(I)
+  c->stats.launches_total++;
+  L.gnorm = std::sqrt(ddot(L, L.g, L.g));
+  {
+    const double xnorm2 = std::sqrt(ddot(L, L.x, L.x));
+    L.stp1 = (L.boundt == 0) ? 1.0 / L.gnorm : xnorm2 / L.gnorm / 100;
+  }
+  L.ftol = 1.0e-4;
+  L.maxfev = 20;
+L80:
+  L.iter = L.iter + 1;
+  L.info = 0;
+  L.bound = L.iter - 1;
+  if (L.iter == 1) goto L165;
+  if (L.iter > m) L.bound = m;
+  L.ys = ddot(L, L.Y + L.npt, L.S + L.npt);
+  L.yy = ddot(L, L.Y + L.npt, L.Y + L.npt);
+  L.diag = L.ys / L.yy;
+L100:
+  L.cp = L.point;
+  if (L.point == 0) L.cp = m;
+  L.rho[L.cp] = 1.0 / L.ys;   // W(N+CP)
+  k_negmul<<<gsz(n), 256, 0, s>>>(n, L.g, 1.0, L.w0);   // W(I) = -G(I)
+  c->stats.launches_total++;
+  L.cp = L.point;
+  for (int i = 1; i <= L.bound; ++i) {
+    L.cp = L.cp - 1;
+    if (L.cp == -1) L.cp = m - 1;
+    const double sq = ddot(L, L.S + (size_t)L.cp * n, L.w0);
+    L.alpha[L.cp + 1] = L.rho[L.cp + 1] * sq;   // W(INMC) = W(N+CP+1)*SQ
+    k_aymx<<<gsz(n), 256, 0, s>>>(n, L.alpha[L.cp + 1], L.Y + (size_t)L.cp * n, L.w0);
+    c->stats.launches_total++;
+  }
+  k_scal<<<gsz(n), 256, 0, s>>>(n, L.diag, L.w0);   // W(I) = DIAG(I)*W(I)
+  c->stats.launches_total++;
+  for (int i = 1; i <= L.bound; ++i) {
+    const double yr = ddot(L, L.Y + (size_t)L.cp * n, L.w0);
+    double beta = L.rho[L.cp + 1] * yr;
+    beta = L.alpha[L.cp + 1] - beta;
+    k_axpy<<<gsz(n), 256, 0, s>>>(n, beta, L.S + (size_t)L.cp * n, L.w0);
+    c->stats.launches_total++;
+    L.cp = L.cp + 1;
+    if (L.cp == m) L.cp = 0;
+  }
+  cudaMemcpyAsync(L.S + (size_t)L.point * n, L.w0, nb, cudaMemcpyDeviceToDevice, s);
+L165:
+  L.nfev = 0;
+  L.stp = 1.0;
+  if (L.iter == 1) L.stp = L.stp1;
+  cudaMemcpyAsync(L.w0, L.g, nb, cudaMemcpyDeviceToDevice, s);   // W(I) = G(I)
+L172:
+  Sv = L.S + (size_t)L.point * n;
+  mcsrch(L, f, Sv, xtol);
+  if (L.info == -1) {
+    *iflag = 1;
+    cudaMemcpyAsync(xh, L.x, nb, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return SW_OK;
+  }
+  if (L.info != 1) {
+    *iflag = -1;
+    cudaStreamSynchronize(s);
+    return SW_OK;
+  }
+  L.nfun = L.nfun + L.nfev;
+  *myinfo = L.info;
+  if (L.boundt == 2 && L.info == 1) freeze(L, L.x);
+  L.npt = L.point * n;
+  k_scal<<<gsz(n), 256, 0, s>>>(n, L.stp, L.S + L.npt);            // S = STP*S
+  k_sub<<<gsz(n), 256, 0, s>>>(n, L.g, L.w0, L.Y + L.npt);         // Y = G - W
+  c->stats.launches_total += 2;
+  L.point = L.point + 1;
+  if (L.point == m) L.point = 0;
+  L.gnorm = std::sqrt(ddot(L, L.g, L.g));
+  L.xnorm = std::sqrt(ddot(L, L.x, L.x));
+  L.xnorm = std::max(1.0, L.xnorm);
+  if (L.gnorm / L.xnorm <= eps) L.finish = true;
+  if (L.finish) {
+    *iflag = 0;
+    cudaMemcpyAsync(xh, L.x, nb, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    return SW_OK;
+  }
+  goto L80;
+}

@@ -1,0 +1,124 @@
+// swave_dev.cuh - device-side layout and kernel interfaces of libswave.
+//
+// Wavefields live in HBM in the reference's padded Fortran layout
+// u(nmin1-4:nmax1+4, nmin2-4:nmax2+4, nmin3-nbound:nmax3+nbound), z fastest,
+// with the z extent rounded up to a multiple of 32 floats so that every
+// (x, y) column starts on a 128-byte boundary.
+//
+// All kernels that reproduce reference arithmetic are compiled with
+// --fmad=false and spell out the Fortran evaluation order, so they produce
+// the same IEEE-754 results as the CPU restatement.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace swave {
+
+// Padded-grid geometry (FDbounds + padded extents).
+struct Geom {
+  int nmin1, nmax1, nmin2, nmax2, nmin3, nmax3, nbound;
+  int lo1, lo2, lo3;      // lower bounds of the padded array
+  int n1p, n2p, n3p;      // padded extents
+  int ld1;                // leading dimension (>= n1p, multiple of 32)
+  int nz, nx, ny;         // physical window
+  int twoD;
+  __host__ __device__ inline long long idx(int i, int j, int k) const {
+    return (long long)(i - lo1) +
+           (long long)ld1 * ((long long)(j - lo2) + (long long)n2p * (long long)(k - lo3));
+  }
+  __host__ __device__ inline long long plane() const { return (long long)ld1 * n2p; }
+  __host__ __device__ inline long long total() const { return plane() * n3p; }
+  // physical (1..nz, 1..nx, 1..ny) -> dense nz*nx*ny offset
+  __host__ __device__ inline long long pidx(int i, int j, int k) const {
+    return (long long)(i - 1) + (long long)nz * ((long long)(j - 1) + (long long)nx * (k - 1));
+  }
+};
+
+struct Coefs {
+  float c0x, c1x, c2x, c3x, c4x, c0y, c1y, c2y, c3y, c4y, c0z, c1z, c2z, c3z, c4z;
+};
+
+// One injection contribution: u3 += (((v2r*trace[tr][it])*wz)*wx)*wy.
+// Unused weights are 1.0f, which leaves the product unchanged.
+struct InjEntry {
+  int tr;
+  float v2r, wz, wx, wy;
+};
+
+// Arguments of the fused step kernel.
+struct StepArgs {
+  Geom g;
+  Coefs c;
+  const float *u2, *u1, *u0, *um1;
+  float *u3;
+  const float *vel;      // padded velocity
+  const float *lap_src;  // 3D adjoint: v^2*u2 (padded); else == u2
+  float k12;             // 12*dt^2
+  float div11;           // 1/11
+  // injection box [bi0..bi1]x[bj0..bj1]x[bk0..bk1] with dense CSR offsets
+  int inj_on;
+  int bi0, bi1, bj0, bj1, bk0, bk1;
+  const int *inj_off;
+  const InjEntry *inj_ent;
+  const float *src_tr;   // nsrc*nt, trace-major
+  int it, nt;
+  // Born secondary source: u3 += (((2*taper)*ref)*w)/vel
+  int born_on;
+  const float *ref;      // physical nz*nx*ny
+  const float *taperx, *tapery;
+  // snapshot of u2 into a dense nz*nx*ny slot
+  int snap_on;
+  float *snap_out;
+  // imaging on u2 (tstep = -1): 1 RTM, 2 LSRTM, 3 AFWI
+  int img;
+  const float *w0, *wm1, *wp1;
+  float *image, *illum;
+  float dt2snap;
+};
+
+// Arguments of the receiver-extraction kernel.
+struct ExtArgs {
+  Geom g;
+  int nrec, nt, it, half, mode;   // mode: sw_extraction
+  const int *ic;                  // 3*nrec Fortran indices
+  const float *wz, *wx;           // lsinc*nrec sinc weights
+  const float *u2, *vel;
+  float vconst;                   // LSRTM / afwi constant factor
+  float *tr;                      // nrec*nt
+};
+
+// Higdon coefficient arrays, coefficient-major for coalesced reads:
+// gz[c][k][j], gx[c][k][i], gy[c][j][i] with c = 0..15.
+struct HigArgs {
+  Geom g;
+  const float *gz, *gx, *gy;
+  float *u3;
+  const float *u2, *u1;
+};
+
+// Launchers (kernels.cu).
+cudaError_t launch_pad_velocity(const Geom &g, const float *vel_phys, float *vel_pad,
+                                cudaStream_t s);
+cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
+                                 float dyi, float dzi, float *gz, float *gx, float *gy,
+                                 cudaStream_t s);
+cudaError_t launch_step(const StepArgs &a, int adjoint2d, cudaStream_t s);
+cudaError_t launch_v2u(const Geom &g, const float *vel, const float *u2, float *out,
+                       cudaStream_t s);
+cudaError_t launch_higdon(const HigArgs &a, cudaStream_t s, int *nlaunch);
+cudaError_t launch_extract(const ExtArgs &a, cudaStream_t s);
+
+// FWI helpers (kernels.cu).
+cudaError_t launch_window_vel(int nz, int nx, int ny, float ox, float oy, float dx, float dy,
+                              int nxw, int nyw, float oxw, float oyw, const float *big,
+                              float *small, cudaStream_t s);
+cudaError_t launch_copy_image(int nz, int nx, int ny, float ox, float oy, float dx, float dy,
+                              int nxw, int nyw, float oxw, float oyw, const float *ims,
+                              const float *ils, float *image, float *illum, cudaStream_t s);
+cudaError_t launch_residual(int nrec, int nt, const float *dobs, const float *mute,
+                            float *dmod, float *resid, double *partial, cudaStream_t s);
+
+}  // namespace swave

@@ -1,0 +1,128 @@
+"""Seeded synthetic models, wavelets and acquisition geometries.
+
+The reference's own workflows read field models (Marmousi, BP, Volve) that
+are not available; these generators reproduce the shapes, spacings and
+value ranges of the benchmark configurations instead:
+
+* ``config1``: nz=201 x nx=401, 10 m, three flat layers 1500/2000/2500 m/s
+  (interfaces at z=600 m and z=1300 m) with a +10 % Gaussian anomaly
+  (sigma 150 m) at z=1000 m, x=2000 m; one 15 Hz Ricker at the surface
+  centre; 401 receivers at depth index 2; 40-cell padding; dt=1 ms, 2000
+  steps.
+* ``layered_faulted``: dipping layers, normal faults with 20-80 m throw and
+  3 % multiplicative correlated noise, clipped to [1500, 4700] m/s (the
+  generator of the batched RTM, Born and FWI configurations).
+* ``rtm_shots``: 37.5 m shot spacing, per-shot split-spread aperture of
+  3-6 km and record length of 3-4 s.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def ricker(f0: float, dt: float, nt: int, t0: float | None = None) -> np.ndarray:
+    """Ricker wavelet (1 - 2 pi^2 f^2 tau^2) exp(-pi^2 f^2 tau^2), tau = t - t0."""
+    if t0 is None:
+        t0 = 1.5 / f0
+    t = np.arange(nt, dtype=np.float64) * dt - t0
+    a = (math.pi * f0 * t) ** 2
+    return ((1.0 - 2.0 * a) * np.exp(-a)).astype(np.float32)
+
+
+def config1_model() -> dict:
+    nz, nx, d = 201, 401, 10.0
+    z = np.arange(nz) * d
+    x = np.arange(nx) * d
+    Z, X = np.meshgrid(z, x, indexing="ij")
+    v = np.where(Z < 600.0, 1500.0, np.where(Z < 1300.0, 2000.0, 2500.0))
+    r2 = (Z - 1000.0) ** 2 + (X - 2000.0) ** 2
+    v = v * (1.0 + 0.1 * np.exp(-r2 / (2 * 150.0 ** 2)))
+    # Fortran order a(nz, nx): z fastest -> store as (nx, nz) C array.
+    vel = np.ascontiguousarray(v.T, dtype=np.float32)
+    return {"nz": nz, "nx": nx, "d": d, "vel": vel}
+
+
+def config1(nt: int = 2000) -> dict:
+    """Plain 2D modelling case (CPU-runnable) with the acquisition above."""
+    from . import make_genpar
+    m = config1_model()
+    g = make_genpar(m["nz"], m["nx"], 1, dz=10.0, dx=10.0, dt=1e-3, nt=nt, ntaper=40,
+                    lsinc=7, snapi=4, fmax=45.0)
+    sou = np.array([0.0, 2000.0, 0.0], np.float32)
+    rec = np.zeros((m["nx"], 3), np.float32)
+    rec[:, 0] = 10.0            # Fortran z index 2
+    rec[:, 1] = np.arange(m["nx"]) * 10.0
+    w = ricker(15.0, 1e-3, nt, 0.1)
+    return {"g": g, "vel": m["vel"], "sou": sou, "rec": rec, "wavelet": w}
+
+
+def _smooth_noise(rng, shape, corr: float) -> np.ndarray:
+    from scipy.ndimage import gaussian_filter
+    n = rng.standard_normal(shape)
+    n = gaussian_filter(n, sigma=corr, mode="reflect")
+    return n / max(n.std(), 1e-12)
+
+
+def layered_faulted(nz: int, nx: int, d: float, seed: int, nlayers: int = 40, nfaults: int = 6,
+                    noise: float = 0.03, corr: float = 5.0, vmin: float = 1500.0,
+                    vmax: float = 4700.0) -> np.ndarray:
+    """Returns vel as a C array of shape (nx, nz) (Fortran a(nz, nx))."""
+    rng = np.random.default_rng(seed)
+    zmax, xmax = (nz - 1) * d, (nx - 1) * d
+    z = np.arange(nz) * d
+    x = np.arange(nx) * d
+    Z, X = np.meshgrid(z, x, indexing="ij")
+    Zeff = Z.copy()
+    for _ in range(nfaults):
+        xf = rng.uniform(0.1, 0.9) * xmax
+        slope = math.tan(math.radians(rng.uniform(55.0, 70.0))) * rng.choice([-1.0, 1.0])
+        throw = rng.uniform(20.0, 80.0)
+        hanging = X > xf + Z / slope
+        Zeff = np.where(hanging, Zeff - throw, Zeff)
+    depths = np.sort(rng.uniform(0.03, 0.97, nlayers)) * zmax
+    dips = rng.uniform(-0.1, 0.1, nlayers)
+    xc = 0.5 * xmax
+    idx = np.zeros((nz, nx), np.int32)
+    for k in range(nlayers):
+        idx += (Zeff > depths[k] + dips[k] * (X - xc)).astype(np.int32)
+    base = vmin + (vmax - 300.0 - vmin) * (np.arange(nlayers + 1) / nlayers)
+    jitter = rng.uniform(-120.0, 120.0, nlayers + 1)
+    vl = np.clip(base + jitter, vmin, vmax)
+    v = vl[idx]
+    v = v * (1.0 + noise * _smooth_noise(rng, (nz, nx), corr))
+    v = np.clip(v, vmin, vmax)
+    return np.ascontiguousarray(v.T, dtype=np.float32)
+
+
+def smooth(vel: np.ndarray, d: float, sigma_m: float) -> np.ndarray:
+    from scipy.ndimage import gaussian_filter
+    return np.ascontiguousarray(gaussian_filter(vel.astype(np.float64), sigma=sigma_m / d,
+                                                mode="nearest"), dtype=np.float32)
+
+
+def rtm_shots(nx: int, d: float, nshot: int, spacing: float, seed: int, dt: float,
+              ap_range=(3000.0, 6000.0), rec_len=(3.0, 4.0), rec_step: int = 3,
+              x0: float | None = None) -> list[dict]:
+    """Surface shots with their own receiver spread and record length."""
+    rng = np.random.default_rng(seed)
+    xmax = (nx - 1) * d
+    if x0 is None:
+        x0 = 0.5 * (xmax - (nshot - 1) * spacing)
+    shots = []
+    for s in range(nshot):
+        sx = x0 + s * spacing
+        ap = rng.uniform(*ap_range)
+        lo = max(0.0, sx - ap / 2)
+        hi = min(xmax, sx + ap / 2)
+        lo = math.floor(lo / d) * d
+        hi = math.floor(hi / d) * d
+        rx = np.arange(lo, hi + 0.5 * d, rec_step * d, dtype=np.float64)
+        rec = np.zeros((rx.size, 3), np.float32)
+        rec[:, 0] = d           # depth index 2
+        rec[:, 1] = rx
+        nt = int(round(rng.uniform(*rec_len) / dt))
+        shots.append({"sou": np.array([0.0, sx, 0.0], np.float32), "rec": rec, "nt": nt,
+                      "lo": lo, "hi": max(hi, rx[-1])})
+    return shots
