@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark: batched 2D shot RTM (zero-lag imaging, illumination-normalised
+image) on a 751 x 2301 grid at 4 m, dt 0.375 ms, 3-4 s records, 3-6 km
+per-shot apertures, 20 Hz Ricker, shots every 37.5 m.
+
+One step = the RTM (forward propagation with snapshots + backward
+propagation with imaging) of one batch of shots that advance together in
+the same kernel launches.  Metric: FD point updates per second over the
+compute domain (interior + 2*ntaper per axis), whole job, and the fused step
+kernel's fraction of the measured HBM bandwidth.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N>1) every rank migrates its own shots (weak scaling) and the
+stacked images are summed with one all-reduce at the end of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NZ, NX, D = 751, 2301, 4.0
+DT = 3.75e-4          # the stated 0.4 ms violates the scheme's Courant limit
+SNAPI = 4
+NTAPER = 20
+F0 = 20.0
+NSHOT_SURVEY = 240
+SPACING = 37.5
+BYTES_PER_POINT = 24  # u2, u1, u0, u_1, vel read + u3 written, FP32
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# Workload
+# ---------------------------------------------------------------------------
+def make_workload(nt_cap: int | None = None):
+    from seismic_gb300 import make_genpar, synth
+    vel = synth.layered_faulted(NZ, NX, D, seed=2)          # (nx, nz) = Fortran (nz, nx)
+    shots = synth.rtm_shots(NX, D, NSHOT_SURVEY, SPACING, seed=2, dt=DT)
+    if nt_cap:
+        for s in shots:
+            s["nt"] = min(s["nt"], nt_cap)
+    ntmax = max(s["nt"] for s in shots)
+    g = make_genpar(NZ, NX, 1, dz=D, dx=D, dt=DT, nt=ntmax, ntaper=NTAPER, lsinc=7,
+                    snapi=SNAPI, fmax=50.0)
+    w = synth.ricker(F0, DT, ntmax)
+    return g, vel, w, shots
+
+
+def window_of(shot):
+    """Columns [i0, i0+nxw) of the shot window (aperture 0: source + spread)."""
+    lo = min(shot["lo"], float(shot["sou"][1]))
+    hi = max(shot["hi"], float(shot["sou"][1]))
+    i0 = int(round(lo / D))
+    nxw = int(round((hi - lo) / D)) + 1
+    return i0, nxw
+
+
+def model_data(ctx, g, vel, w, shot):
+    """Observed data of one shot: forward modelling on its window."""
+    import seismic_gb300 as sw
+    i0, nxw = window_of(shot)
+    gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=shot["nt"], ntaper=NTAPER,
+                        lsinc=7, snapi=SNAPI)
+    return ctx.modeling(gw, vel[i0:i0 + nxw], shot["sou"], w[: shot["nt"]], shot["rec"])
+
+
+def shot_points(shot, forward_and_back=True):
+    i0, nxw = window_of(shot)
+    n1 = NZ + 2 * NTAPER
+    n2 = nxw + 2 * NTAPER
+    return n1 * n2 * shot["nt"] * (2 if forward_and_back else 1)
+
+
+# ---------------------------------------------------------------------------
+# Clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (a restatement of the reference CPU path)
+# ---------------------------------------------------------------------------
+def cpu_sample(g, vel, w, shot, nsteps: int) -> dict:
+    """Times the oracle's RTM of one shot truncated to nsteps samples."""
+    import seismic_gb300 as sw
+    from oracle import bind as oracle
+    i0, nxw = window_of(shot)
+    gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=nsteps, ntaper=NTAPER,
+                        lsinc=7, snapi=SNAPI)
+    rng = np.random.default_rng(0)
+    data = rng.standard_normal((shot["rec"].shape[0], nsteps)).astype(np.float32) * 1e-3
+    oracle.load()
+    t0 = time.perf_counter()
+    oracle.rtm(gw, vel[i0:i0 + nxw], shot["sou"], w[:nsteps], shot["rec"], data)
+    dt = time.perf_counter() - t0
+    pts = (NZ + 2 * NTAPER) * (nxw + 2 * NTAPER) * nsteps * 2
+    return {"seconds": dt, "points": pts}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    g, vel, w, shots = make_workload()
+    nsteps = args.cpu_steps
+    res = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_sample(g, vel, w, shots[k % len(shots)], nsteps)
+        if k >= args.warmup:
+            res.append(r)
+    secs = sum(r["seconds"] for r in res)
+    pts = sum(r["points"] for r in res)
+    v = pts / secs / 1e9
+    cores = cpu_threads()
+    sample = (f"RTM (forward + backward, {nsteps} of the 8000-10667 time samples) of one "
+              f"{NZ}x(window) shot per step, {args.steps} steps")
+    line = {
+        "impl": "reference", "metric": "fd_gpts_per_s", "value": v, "unit": "Gpts/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / max(1, len(res)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args, None),
+        "cpu_baseline": {"value": v, "unit": "Gpts/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args, batch):
+    return {"workload": "batched 2D shot RTM with illumination-normalised stacking",
+            "grid": [NZ, NX], "spacing_m": D, "dt_s": DT, "ntaper": NTAPER, "snapi": SNAPI,
+            "record_s": [3.0, 4.0], "aperture_m": [3000, 6000], "shot_spacing_m": SPACING,
+            "survey_shots": NSHOT_SURVEY, "shots_per_step": batch, "ricker_hz": F0,
+            "l2": "inputs larger than L2 (snapshots of every shot in HBM)",
+            "bytes_per_point": BYTES_PER_POINT}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots-per-step", type=int, default=16)
+    ap.add_argument("--cpu-steps", type=int, default=240)
+    ap.add_argument("--nt-cap", type=int, default=0, help="truncate records (debug)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    import seismic_gb300 as sw
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    ctx = sw.Context(local)
+    g, vel, w, shots = make_workload(args.nt_cap or None)
+    B = args.shots_per_step
+    nsteps = args.warmup + args.steps
+    # Shots of this rank: rank r takes every ws-th shot of the survey.
+    mine = shots[rank::ws]
+    per_step = [mine[(k * B + q) % len(mine)] for k in range(nsteps) for q in range(B)]
+    # Observed data: modelled on each shot's window (untimed setup).
+    distinct = {}
+    t0 = time.perf_counter()
+    for s in per_step:
+        key = float(s["sou"][1])
+        if key not in distinct:
+            distinct[key] = model_data(ctx, g, vel, w, s)
+    log(f"[rank {rank}] modelled {len(distinct)} shots in {time.perf_counter() - t0:.1f}s")
+    job_shots = [{"sou": s["sou"], "rec": s["rec"], "data": distinct[float(s["sou"][1])]}
+                 for s in per_step]
+    job = sw.RTMJob(ctx, g, vel, w, job_shots)
+    job.set_batch(B)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # Warm-up steps.
+    for k in range(args.warmup):
+        job.run(k * B, B)
+    barrier()
+    # Timed region: inputs resident in HBM; events bracket the fused kernel.
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    t_start = time.perf_counter()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    points = 0
+    for k in range(args.warmup, nsteps):
+        job.run(k * B, B)
+        points += sum(shot_points(s) for s in per_step[k * B:(k + 1) * B])
+    if ws > 1:
+        im = torch.from_numpy(job.result(normalised=False)[0]).cuda()
+        torch.distributed.all_reduce(im)
+    ev1.record()
+    barrier()
+    elapsed = time.perf_counter() - t_start
+    ev_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    ctx.set_profiling(False)
+    st = ctx.stats()
+    last_batch, _ = job.info()
+    secs = elapsed
+    if ws > 1:
+        t = torch.tensor([secs], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        secs = float(t.item())
+        p = torch.tensor([float(points)], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(p)
+        points_all = float(p.item())
+    else:
+        points_all = float(points)
+    value = points_all / secs / 1e9
+    # Roofline of the fused step kernel (CUDA events around every launch).
+    peak, peak_kind = measured_peak()
+    kern_s = st["step_kernel_ms"] / 1e3
+    nl = max(1, st["step_kernel_timed"])
+    achieved = (st["step_bytes"] / nl) / (kern_s / nl) / 1e9 if kern_s > 0 else None
+    traffic = None
+    prof_json = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
+    if os.path.exists(prof_json):
+        try:
+            pj = json.load(open(prof_json))
+            traffic = pj.get("bytes_per_point") and pj["bytes_per_point"] * (st["step_bytes"] / nl) / BYTES_PER_POINT
+        except Exception:
+            traffic = None
+    # End to end through the public API with host buffers (one step's shots).
+    e2e_line = None
+    if rank == 0:
+        sel = job_shots[args.warmup * B:(args.warmup + 1) * B]
+        pin = lambda a: _pinned(torch, a)
+        hshots = [{"sou": s["sou"], "rec": s["rec"], "data": pin(s["data"])} for s in sel]
+        hvel = pin(vel)
+        hw = pin(w)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        j2 = sw.RTMJob(ctx, g, hvel, hw, hshots)
+        j2.set_batch(B)
+        j2.run()
+        im, il, nm = j2.result(normalised=True)
+        j2.close()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        pts_e2e = sum(shot_points(s) for s in per_step[args.warmup * B:(args.warmup + 1) * B])
+        h2d = hvel.nbytes + hw.nbytes + sum(s["data"].nbytes + s["rec"].nbytes for s in hshots)
+        d2h = im.nbytes + il.nbytes + nm.nbytes
+        e2e_line = {"value": pts_e2e / e2e_s / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)}
+    # CPU baseline (rank 0, N=1 only): a bounded sample of the same workload.
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        r = cpu_sample(g, vel, w, per_step[0], args.cpu_steps)
+        cpu = {"value": r["points"] / r["seconds"] / 1e9, "unit": "Gpts/s", "cores": cpu_threads(),
+               "kind": "port",
+               "sample": f"oracle RTM of one shot window, {args.cpu_steps} of its time samples, "
+                         f"forward + backward ({r['seconds']:.1f} s)"}
+    if rank == 0:
+        line = {
+            "metric": "fd_gpts_per_s", "value": value, "unit": "Gpts/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded faulted layered model, data modelled by the engine)",
+            "config": workload_config(args, last_batch),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_kind": peak_kind, "kernel": "k_bstep (fused stencil + time update)",
+                         "avg_launch_ms": (st["step_kernel_ms"] / nl),
+                         "launches_timed": st["step_kernel_timed"]},
+            "cpu_baseline": cpu, "e2e": e2e_line, "clocks": clk,
+            "gpu_launches": int(st["launches_total"]),
+            "timed_event_ms": ev_ms,
+        }
+        print(json.dumps(line), flush=True)
+    job.close()
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def _pinned(torch, a: np.ndarray) -> np.ndarray:
+    t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+    t.numpy()[...] = a
+    return t.numpy()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -182,6 +182,43 @@ int sw_lsrtm(sw_ctx *ctx, const sw_genpar *g, const float *vel,
  * centred 2nd difference / dt^2. */
 int sw_born_wavelet(float *wavelet, int nt, float dt);
 
+/* ---- Multi-shot RTM job (3DRTM.f90 per shot + compute_mig's stacking) ---
+ * Shots of uneven aperture and record length are windowed out of one model
+ * (extract_coord_source_receiver_patch + copy_window_vel_gath,
+ * ExtractPadModel.f90:19-85,395-507), migrated with RTM_to_memory
+ * (to_disk_to_memory_RTM.f90:358-492) and stacked into the full grid with
+ * mod_copy_image (ExtractPadModel.f90:662-697).  Many shots advance in the
+ * same kernel launches; the number per batch is set by their HBM footprint
+ * (snapshots dominate).  All inputs are copied to device memory at
+ * creation. */
+typedef struct sw_shot {
+  float sou_coord[3];
+  int nrec;
+  const float *rec_coord;   /* 3*nrec                                    */
+  const float *data;        /* nrec*nt observed traces                   */
+  int nt;                   /* record length of this shot, <= model g.nt */
+} sw_shot;
+
+typedef struct sw_rtm_job sw_rtm_job;
+/* model: full-grid geometry (nz, nx, ny, spacing, origins, dt, nt = the
+ * longest record, ntaper, lsinc, snapi); vel: nz*nx*ny; wavelet: g.nt. */
+int sw_rtm_job_create(sw_ctx *ctx, const sw_genpar *model, float aperture_x,
+                      float aperture_y, const float *vel, const float *wavelet,
+                      int nshot, const sw_shot *shots, sw_rtm_job **out);
+/* Admission: at most max_shots per batch and at most mem_fraction of the
+ * free device memory (defaults 64 and 0.85). */
+int sw_rtm_job_set_batch(sw_rtm_job *job, int max_shots, double mem_fraction);
+/* Migrates shots [first, first+count) and adds them to the job's image. */
+int sw_rtm_job_run(sw_rtm_job *job, int first, int count);
+/* Shots per batch used by the last run, and compute-domain point updates. */
+int sw_rtm_job_info(const sw_rtm_job *job, int *last_batch, uint64_t *points);
+/* image, illum: stacked nz*nx*ny sums; image_norm: image divided by the
+ * normalised illumination (compute_function_gradient.f90:452-453).  Any
+ * pointer may be NULL. */
+int sw_rtm_job_result(sw_rtm_job *job, float *image, float *illum, float *image_norm);
+int sw_rtm_job_reset(sw_rtm_job *job);
+int sw_rtm_job_destroy(sw_rtm_job *job);
+
 /* ---- FWI objective / gradient (progs/afwi/compute_function_gradient.f90) */
 
 typedef struct sw_fwi_shot {

@@ -53,6 +53,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "oracle_born_wavelet": [_fp, C.c_int, C.c_float],
         "oracle_vel_check": [g, _fp, _fp, _fp],
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
+        "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],
+        "oracle_stencil_f64": [g, C.c_int, _dp, _dp, _dp],
         "oracle_triangle2": [_fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                              C.c_int, C.c_int],
         "oracle_lbfgs_step": [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
@@ -195,6 +197,31 @@ def fwi_fct_gdt(desc, vel, wavelet, shots, vpmask=None):
     _chk(lib.oracle_fwi_fct_gdt(C.byref(desc), pv, pw, len(shots), arr, pm, C.byref(f),
                                 grad.ctypes.data_as(_fp), illum.ctypes.data_as(_fp)), "fwi")
     return f.value, grad, illum
+
+
+def rtm_job(model, vel, wavelet, shots, aperture_x=0.0, aperture_y=0.0):
+    """Stacked RTM over shots (dicts as for seismic_gb300.make_shots)."""
+    lib = load()
+    from seismic_gb300 import make_shots
+    arr, keep = make_shots(shots)
+    n = model.nz * model.nx * model.ny
+    im, il, nm = (np.zeros(n, np.float32) for _ in range(3))
+    v, pv = _f(vel); w, pw = _f(wavelet)
+    _chk(lib.oracle_rtm_job(C.byref(model), aperture_x, aperture_y, pv, pw, len(shots),
+                            C.cast(arr, C.c_void_p), im.ctypes.data_as(_fp),
+                            il.ctypes.data_as(_fp), nm.ctypes.data_as(_fp)), "rtm_job")
+    return im, il, nm
+
+
+def stencil_f64(g, vel, u2, adjoint=False):
+    """Applies the FD stencil once to a padded field u2 (shape padded_shape(g))."""
+    lib = load()
+    v, pv = _d(vel)
+    a, pa = _d(u2)
+    out = np.zeros_like(a)
+    _chk(lib.oracle_stencil_f64(C.byref(g), int(adjoint), pv, pa, out.ctypes.data_as(_dp)),
+         "stencil")
+    return out
 
 
 def mksinc(lsinc: int, shift: float) -> np.ndarray:

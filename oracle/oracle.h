@@ -86,6 +86,11 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel,
                        const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum);
 
+/* Multi-shot RTM stacking, same meaning as sw_rtm_job_* run over all shots. */
+int oracle_rtm_job(const sw_genpar *model, float apx, float apy, const float *vel,
+                   const float *wavelet, int nshot, const sw_shot *shots, float *image,
+                   float *illum, float *image_norm);
+
 /* LBFGS (libs/libinv/lbfgs.f:49-558) with its SAVE state in a handle. */
 typedef struct or_lbfgs or_lbfgs;
 or_lbfgs *oracle_lbfgs_create(int n, int m, double xmin, double xmax,
@@ -99,6 +104,10 @@ void oracle_lbfgs_diag(const or_lbfgs *s, double *out8);
 /* triangle2 smoothing (libs/libwave/Smoothing.f90:87-138), in place. */
 int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2,
                      int rect3, int doz, int dox, int doy);
+
+/* One stencil application on a padded FP64 field (analytic tests). */
+int oracle_stencil_f64(const sw_genpar *g, int adjoint, const double *vel,
+                       const double *u2, double *u3);
 
 /* mksinc (libs/libwave/Interpolate.f90:15-42). */
 void oracle_mksinc(float *sinc, int lsinc, float shift);

@@ -1005,6 +1005,54 @@ static void copy_image(const sw_genpar &g, const Window &w, const float *ims,
   }
 }
 
+// compute_mig-style stacking of RTM_to_memory images
+// (compute_function_gradient.f90:352-470, to_disk_to_memory_RTM.f90:358-492).
+static int rtm_job(const sw_genpar &M, float apx, float apy, const float *vel,
+                   const float *wavelet, int nshot, const sw_shot *shots, float *image,
+                   float *illum, float *image_norm) {
+  const size_t nfull = (size_t)M.nz * M.nx * M.ny;
+  std::vector<float> im(nfull, 0.f), il(nfull, 0.f);
+  sw_fwi_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.g = M;
+  d.aperture_x = apx;
+  d.aperture_y = apy;
+  for (int is = 0; is < nshot; ++is) {
+    const sw_shot &s = shots[is];
+    sw_fwi_shot fs;
+    std::memset(&fs, 0, sizeof(fs));
+    std::memcpy(fs.sou_coord, s.sou_coord, sizeof(fs.sou_coord));
+    fs.nrec = s.nrec;
+    fs.rec_coord = s.rec_coord;
+    Window w;
+    int st = shot_window(d, fs, w);
+    if (st) return st;
+    sw_genpar g = M;
+    g.nx = w.nxw; g.ny = w.nyw; g.ox = w.oxw; g.oy = w.oyw; g.nt = s.nt;
+    const size_t nw = (size_t)g.nz * g.nx * g.ny;
+    std::vector<float> vs(nw), ims(nw), ils(nw);
+    window_vel(M, w, vel, vs.data());
+    st = rtm_like<float>(g, vs.data(), s.sou_coord, wavelet, s.nrec, s.rec_coord, s.data,
+                         ims.data(), ils.data(), false);
+    if (st) return st;
+    copy_image(M, w, ims.data(), ils.data(), im.data(), il.data());
+  }
+  if (image) std::memcpy(image, im.data(), nfull * sizeof(float));
+  if (illum) std::memcpy(illum, il.data(), nfull * sizeof(float));
+  if (image_norm) {
+    float m = il[0];
+    double ss = 0.;
+    for (size_t q = 0; q < nfull; ++q) {
+      m = std::max(m, il[q]);
+      ss = ss + (double)il[q] * (double)il[q];
+    }
+    const double r = std::sqrt(ss / (double)nfull);
+    for (size_t q = 0; q < nfull; ++q)
+      image_norm[q] = im[q] / (float)((double)(il[q] + m / 10000.f) / r);
+  }
+  return SW_OK;
+}
+
 static int fwi_fct_gdt(const sw_fwi_desc &d, const float *vel, const float *wavelet,
                        int nshot, const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum_out) {
@@ -1550,6 +1598,36 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel, const float *wave
                        int nshot, const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum) {
   return fwi_fct_gdt(*d, vel, wavelet, nshot, shots, vpmask, f, grad, illum);
+}
+
+int oracle_rtm_job(const sw_genpar *model, float apx, float apy, const float *vel,
+                   const float *wavelet, int nshot, const sw_shot *shots, float *image,
+                   float *illum, float *image_norm) {
+  return rtm_job(*model, apx, apy, vel, wavelet, nshot, shots, image, illum, image_norm);
+}
+
+// One application of the scalar stencil (forward: v^2 Lap u; adjoint:
+// Lap(v^2 u)) on a padded field; the compute domain of out is overwritten.
+int oracle_stencil_f64(const sw_genpar *g, int adjoint, const double *vel,
+                       const double *u2, double *u3) {
+  int st = check_genpar(*g);
+  if (st) return st;
+  const Bounds b = make_bounds(*g);
+  F3<double> v, a, o, t;
+  v.init(b); a.init(b); o.init(b);
+  model_pad(vel, v, b, g->nz, g->nx, g->ny, g->twoD != 0);
+  std::memcpy(a.v.data(), u2, a.v.size() * sizeof(double));
+  std::memcpy(o.v.data(), u3, o.v.size() * sizeof(double));
+  const Coefs<double> c = make_coefs<double>(*g);
+  if (!adjoint) {
+    if (g->twoD) stencil2d_fwd(c, b, a, o, v);
+    else stencil3d_fwd(c, b, a, o, v);
+  } else {
+    if (g->twoD) stencil2d_adj(c, b, a, o, v);
+    else { t.init(b); stencil3d_adj(c, b, a, o, v, t); }
+  }
+  std::memcpy(u3, o.v.data(), o.v.size() * sizeof(double));
+  return SW_OK;
 }
 
 int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2, int rect3,

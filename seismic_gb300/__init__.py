@@ -68,6 +68,11 @@ class SwFwiDesc(C.Structure):
                 ("smooth_doy", C.c_int)]
 
 
+class SwShot(C.Structure):
+    _fields_ = [("sou_coord", C.c_float * 3), ("nrec", C.c_int), ("rec_coord", _fp),
+                ("data", _fp), ("nt", C.c_int)]
+
+
 class SwStats(C.Structure):
     _fields_ = [("launches_total", C.c_uint64), ("launches_step", C.c_uint64),
                 ("points_updated", C.c_uint64), ("step_kernel_ms", C.c_double),
@@ -95,6 +100,14 @@ _SIGS = {
     "sw_lbfgs_step": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sw_lbfgs_diag": (C.c_int, [C.c_void_p, _dp]),
+    "sw_rtm_job_create": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), C.c_float, C.c_float, _fp,
+                                    _fp, C.c_int, C.POINTER(SwShot), C.POINTER(C.c_void_p)]),
+    "sw_rtm_job_set_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "sw_rtm_job_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "sw_rtm_job_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
+    "sw_rtm_job_result": (C.c_int, [C.c_void_p, _fp, _fp, _fp]),
+    "sw_rtm_job_reset": (C.c_int, [C.c_void_p]),
+    "sw_rtm_job_destroy": (C.c_int, [C.c_void_p]),
     "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
     "sw_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
@@ -285,6 +298,69 @@ class Context:
         self._check(self.lib.sw_fwi_fct_gdt(self.h, C.byref(desc), fptr(vel), fptr(w), len(shots),
                                             arr, fptr(m), C.byref(f), fptr(grad), fptr(illum)))
         return (f.value, grad, illum, resids) if want_resid else (f.value, grad, illum)
+
+
+def make_shots(shots) -> tuple:
+    """sw_shot array from dicts(sou=(z,x,y), rec=(n,3), data=(n,nt)); returns (array, keep)."""
+    arr = (SwShot * len(shots))()
+    keep = []
+    for i, s in enumerate(shots):
+        rc, d = _f32(s["rec"]), _f32(s["data"])
+        keep += [rc, d]
+        arr[i].sou_coord[:] = [float(v) for v in s["sou"]]
+        arr[i].nrec = rc.size // 3
+        arr[i].rec_coord, arr[i].data = fptr(rc), fptr(d)
+        arr[i].nt = int(d.shape[-1]) if d.ndim == 2 else int(s["nt"])
+    return arr, keep
+
+
+class RTMJob:
+    """Multi-shot RTM (sw_rtm_job_*): windows, HBM admission, stacking."""
+
+    def __init__(self, ctx: Context, model: SwGenpar, vel, wavelet, shots, aperture_x=0.0,
+                 aperture_y=0.0):
+        self.ctx = ctx
+        self.g = model
+        arr, keep = make_shots(shots)
+        v, w = _f32(vel), _f32(wavelet)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.sw_rtm_job_create(ctx.h, C.byref(model), aperture_x, aperture_y,
+                                             fptr(v), fptr(w), len(shots), arr, C.byref(h)))
+        self.h = h
+        self.nshot = len(shots)
+
+    def set_batch(self, max_shots: int, mem_fraction: float = 0.85):
+        self.ctx._check(self.ctx.lib.sw_rtm_job_set_batch(self.h, max_shots, mem_fraction))
+
+    def run(self, first: int = 0, count: int | None = None):
+        count = self.nshot - first if count is None else count
+        self.ctx._check(self.ctx.lib.sw_rtm_job_run(self.h, first, count))
+
+    def info(self) -> tuple[int, int]:
+        b, p = C.c_int(), C.c_uint64()
+        self.ctx._check(self.ctx.lib.sw_rtm_job_info(self.h, C.byref(b), C.byref(p)))
+        return b.value, p.value
+
+    def result(self, normalised: bool = True):
+        n = self.g.nz * self.g.nx * self.g.ny
+        im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        nm = np.zeros(n, np.float32) if normalised else None
+        self.ctx._check(self.ctx.lib.sw_rtm_job_result(self.h, fptr(im), fptr(il), fptr(nm)))
+        return (im, il, nm) if normalised else (im, il)
+
+    def reset(self):
+        self.ctx._check(self.ctx.lib.sw_rtm_job_reset(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sw_rtm_job_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class LBFGS:

@@ -1,0 +1,408 @@
+// batch.cu - multi-shot time-step kernels (compiled with --fmad=false).
+//
+// One launch of each kernel covers every shot of a batch; the time step s
+// comes from a device counter so that the launches of all steps are
+// identical and graph-capturable.  The arithmetic restates the reference
+// loops in their evaluation order (file:line cited at each kernel).
+#include "batch.cuh"
+
+namespace swave {
+
+__device__ __forceinline__ int find_shot(const int *start, int n, int idx) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= idx) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Number of snapshot steps (it multiple of snapi) met so far in this phase,
+// counting the current one: the value of wfld%counter / model%counter in
+// Extraction_wavefield (Extraction.f90:574-575) and the imaging conditions
+// (Imaging.f90:242-244, 760-762).
+__device__ __forceinline__ int snap_count(const ShotDev &S, int it) {
+  if (S.tstep > 0) return it / S.snapi - (S.tmin - 1) / S.snapi;
+  return S.tmin / S.snapi - (it - 1) / S.snapi;
+}
+
+__device__ __forceinline__ float lap_axis(const float *__restrict__ u, long long p, long long s,
+                                          float c0, float c1, float c2, float c3, float c4) {
+  float t = c0 * u[p];
+  t = t + c1 * (u[p + s] + u[p - s]);
+  t = t + c2 * (u[p + 2 * s] + u[p - 2 * s]);
+  t = t + c3 * (u[p + 3 * s] + u[p - 3 * s]);
+  t = t + c4 * (u[p + 4 * s] + u[p - 4 * s]);
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// Fused step: stencil -> injection -> Born source -> 5-level time update,
+// with the snapshot and imaging reads of u2 (Propagator.f90:182-218).
+// ---------------------------------------------------------------------------
+template <bool TWO_D>
+__global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
+  const int b = find_shot(t.step_tiles, t.nshots, blockIdx.x);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
+  const int ntz = (n1 + 31) >> 5, ntx = (n2 + 7) >> 3;
+  int local = blockIdx.x - t.step_tiles[b];
+  const int tz = local % ntz;
+  local /= ntz;
+  const int tx = local % ntx;
+  const int kk = local / ntx;
+  const int i = g.nmin1 + tz * 32 + threadIdx.x;
+  const int j = g.nmin2 + tx * 8 + threadIdx.y;
+  const int k = TWO_D ? 1 : g.nmin3 + kk;
+  if (i > g.nmax1 || j > g.nmax2) return;
+  const int it = S.tmin + s * S.tstep;
+  const float *__restrict__ um1 = S.f[s % 5];
+  const float *__restrict__ u0 = S.f[(s + 1) % 5];
+  const float *__restrict__ u1 = S.f[(s + 2) % 5];
+  const float *__restrict__ u2 = S.f[(s + 3) % 5];
+  float *__restrict__ u3 = S.f[(s + 4) % 5];
+  const long long p = g.idx(i, j, k);
+  const long long L = g.ld1;
+  const Coefs &c = S.c;
+  float sv;
+  if (TWO_D && S.adj2d) {
+    // FD_2nd_2D_derivatives_scalar_adjoint_grid (FDderivatives.f90:847-891):
+    // vel indices clamped to the compute domain.
+    const float *__restrict__ v = S.vel;
+    auto w = [&](long long pu, long long pv) -> float {
+      const float vv = v[pv];
+      return (vv * vv) * u2[pu];
+    };
+    long long pz[5], mz[5], px[5], mx[5];
+#pragma unroll
+    for (int l = 1; l <= 4; ++l) {
+      pz[l] = p + (min(g.nmax1, i + l) - i);
+      mz[l] = p - (i - max(g.nmin1, i - l));
+      px[l] = p + L * (min(g.nmax2, j + l) - j);
+      mx[l] = p - L * (j - max(g.nmin2, j - l));
+    }
+    float tzz = c.c0z * w(p, p);
+    tzz = tzz + c.c1z * (w(p + 1, pz[1]) + w(p - 1, mz[1]));
+    tzz = tzz + c.c2z * (w(p + 2, pz[2]) + w(p - 2, mz[2]));
+    tzz = tzz + c.c3z * (w(p + 3, pz[3]) + w(p - 3, mz[3]));
+    tzz = tzz + c.c4z * (w(p + 4, pz[4]) + w(p - 4, mz[4]));
+    float txx = c.c0x * w(p, p);
+    txx = txx + c.c1x * (w(p + L, px[1]) + w(p - L, mx[1]));
+    txx = txx + c.c2x * (w(p + 2 * L, px[2]) + w(p - 2 * L, mx[2]));
+    txx = txx + c.c3x * (w(p + 3 * L, px[3]) + w(p - 3 * L, mx[3]));
+    txx = txx + c.c4x * (w(p + 4 * L, px[4]) + w(p - 4 * L, mx[4]));
+    sv = txx + tzz;
+  } else {
+    // FD_2nd_{2D,3D}_derivatives_scalar_forward_grid (FDderivatives.f90:
+    // 715-743, 97-131).  For the 3D adjoint (FDderivatives.f90:780-819)
+    // the Laplacian acts on v^2*u2 and the v^2 factor is skipped.
+    const float *__restrict__ u = (!TWO_D && S.adj3d) ? S.v2u : u2;
+    const float tzz = lap_axis(u, p, 1, c.c0z, c.c1z, c.c2z, c.c3z, c.c4z);
+    const float txx = lap_axis(u, p, L, c.c0x, c.c1x, c.c2x, c.c3x, c.c4x);
+    if (TWO_D) {
+      const float vv = S.vel[p];
+      sv = (vv * vv) * (txx + tzz);
+    } else {
+      const float tyy = lap_axis(u, p, g.plane(), c.c0y, c.c1y, c.c2y, c.c3y, c.c4y);
+      if (S.adj3d) {
+        sv = (txx + tzz) + tyy;
+      } else {
+        const float vv = S.vel[p];
+        sv = (vv * vv) * ((txx + tzz) + tyy);
+      }
+    }
+  }
+  // Injection (Injection.f90:151-456, 561-591): contributions in source order.
+  if (S.inj_on && i >= S.bi0 && i <= S.bi1 && j >= S.bj0 && j <= S.bj1 && k >= S.bk0 &&
+      k <= S.bk1) {
+    const int bx = (i - S.bi0) + (S.bi1 - S.bi0 + 1) * ((j - S.bj0) + (S.bj1 - S.bj0 + 1) * (k - S.bk0));
+    const int e1 = S.inj_off[bx + 1];
+    for (int e = S.inj_off[bx]; e < e1; ++e) {
+      const InjEntry E = S.inj_ent[e];
+      const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
+      sv = sv + (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
+    }
+  }
+  const bool phys = i >= 1 && i <= g.nz && j >= 1 && j <= g.nx && k >= 1 && k <= g.ny;
+  const bool snapstep = (it % S.snapi) == 0;
+  int cnt = 0;
+  long long pp = 0;
+  float taper = 1.f;
+  if (phys) {
+    pp = g.pidx(i, j, k);
+    if (S.taperx) taper = S.taperx[j - 1] * S.tapery[k - 1];
+    if (snapstep) cnt = snap_count(S, it);
+  }
+  const long long nphys = (long long)g.nz * g.nx * g.ny;
+  // Injection_Born (Imaging.f90:747-788), tstep = +1 only.
+  if (S.imaging == 4 && S.tstep > 0 && phys && snapstep && cnt <= S.ntsnap) {
+    const float *w0 = S.wave + (long long)(cnt - 1) * nphys;
+    sv = sv + (((2.0f * taper) * S.ref[pp]) * w0[pp]) / S.vel[p];
+  }
+  // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
+  const float u2c = u2[p];
+  float a = 20.0f * u2c;
+  a = a - 6.0f * u1[p];
+  a = a - 4.0f * u0[p];
+  a = a + um1[p];
+  a = a + S.k12 * sv;
+  u3[p] = a * S.div11;
+  if (phys && snapstep) {
+    // Extraction_wavefield (Extraction.f90:562-601).
+    if (S.extract_wave && cnt <= S.ntsnap) S.wave[(long long)(cnt - 1) * nphys + pp] = u2c;
+    // Imaging conditions on u2 before the step, tstep = -1 (Propagator.f90:192-194).
+    if (S.imaging >= 1 && S.imaging <= 3 && S.tstep < 0) {
+      const int index = S.ntsnap - cnt + 1;
+      if (index >= 1) {
+        const float w = S.wave[(long long)(index - 1) * nphys + pp];
+        float im = S.image[pp];
+        if (S.imaging == 1) {
+          im = im + (u2c * w) * taper;                            // Imaging.f90:265
+        } else if (S.imaging == 2) {
+          im = im + (((2.0f * taper) * u2c) * w) / S.vel[p];      // Imaging.f90:735
+        } else {
+          const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
+          const float vv = S.vel[p];
+          const float tt = ((S.wave[(long long)(im1 - 1) * nphys + pp] - 2.0f * w) +
+                            S.wave[(long long)(ip1 - 1) * nphys + pp]) /
+                           (S.dt2snap * ((vv * vv) * vv));
+          im = im + (u2c * tt) * taper;                           // Imaging.f90:410-411
+        }
+        S.image[pp] = im;
+        S.illum[pp] = S.illum[pp] + (w * w) * taper;
+      }
+    }
+  }
+}
+
+// v^2*u2 over the padded array (FDderivatives.f90:789-790), 3D adjoint only.
+__global__ void k_bv2u(BatchTables t, int s_off) {
+  const int b = find_shot(t.v2u_blocks, t.nshots, blockIdx.x);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (!S.adj3d || s >= S.nsteps) return;
+  const float *__restrict__ u2 = S.f[(s + 3) % 5];
+  const long long n = S.g.total();
+  const int nb = t.v2u_blocks[b + 1] - t.v2u_blocks[b];
+  for (long long q = (long long)(blockIdx.x - t.v2u_blocks[b]) * blockDim.x + threadIdx.x; q < n;
+       q += (long long)nb * blockDim.x) {
+    const float v = S.vel[q];
+    S.v2u[q] = (v * v) * u2[q];
+  }
+}
+
+// Sinc gather of one receiver in the loop order of Extraction_1trace_sinc_xy
+// (Extraction.f90:511-560) / _xyz (Extraction.f90:276-337).  H is the
+// half-width when known at compile time (lsinc = 7), else -1.
+template <int H>
+__device__ __forceinline__ float sinc_gather(const ShotDev &S, const Geom &g,
+                                             const float *__restrict__ u2, int r, int i0, int j0,
+                                             int k0, float v, float tr) {
+  const int h = H > 0 ? H : S.ext_half;
+  const int ls = 2 * h + 1;
+  const float *wz = S.wz + (long long)r * ls, *wx = S.wx + (long long)r * ls;
+  if (g.twoD) {
+#pragma unroll
+    for (int jj = -h; jj <= h; ++jj) {
+      const long long pj = g.idx(i0, j0 + jj, 1);
+#pragma unroll
+      for (int ii = -h; ii <= h; ++ii) tr = tr + ((v * u2[pj + ii]) * wz[h + ii]) * wx[h + jj];
+    }
+  } else {
+    for (int kq = -h; kq <= h; ++kq)
+#pragma unroll
+      for (int jj = -h; jj <= h; ++jj) {
+        const long long pj = g.idx(i0, j0 + jj, k0 + kq);
+#pragma unroll
+        for (int ii = -h; ii <= h; ++ii)
+          tr = tr + (((v * u2[pj + ii]) * wz[h + ii]) * wx[h + jj]) * wx[h + kq];
+      }
+  }
+  return tr;
+}
+
+// ---------------------------------------------------------------------------
+// Receiver extraction (Extraction.f90:71-135, 217-247, 276-337, 511-560):
+// one thread per receiver, the sinc sum in the reference loop order.
+// ---------------------------------------------------------------------------
+__global__ void k_bextract(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ntot = t.rec_start[t.nshots];
+  if (q >= ntot) return;
+  const int b = find_shot(t.rec_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps || S.ext_mode == 0) return;
+  const int r = q - t.rec_start[b];
+  const int it = S.tmin + s * S.tstep;
+  const Geom &g = S.g;
+  const float *__restrict__ u2 = S.f[(s + 3) % 5];
+  const int i0 = S.ric[3 * r], j0 = S.ric[3 * r + 1], k0 = g.twoD ? 1 : S.ric[3 * r + 2];
+  float *trp = S.rec_tr + (long long)r * S.nt + (it - 1);
+  float tr = *trp;
+  if (S.ext_mode == 2) {  // Extraction_array_simple_afwi_noomp
+    *trp = tr + u2[g.idx(i0, j0, k0)];
+    return;
+  }
+  float v;
+  if (S.ext_mode == 1) {  // Extraction_array_sinc: v**2 in 2D, v in 3D
+    const float vv = S.vel[g.idx(i0, j0, k0)];
+    v = g.twoD ? vv * vv : vv;
+  } else {
+    v = S.vconst;
+  }
+  if (S.ext_half == 3) tr = sinc_gather<3>(S, g, u2, r, i0, j0, k0, v, tr);
+  else tr = sinc_gather<-1>(S, g, u2, r, i0, j0, k0, v, tr);
+  *trp = tr;
+}
+
+// ---------------------------------------------------------------------------
+// Higdon recurrences (Boundary_3d, Boundary.f90:89-184; Higdon_factor,
+// Boundary.f90:366-447).  One thread per line normal to the edge.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float hsum(const float *__restrict__ gc, long long cs, float a, float b,
+                                      float cc, float d, float e, float f, float gg, float h) {
+  float r = gc[0] * a;
+  r = r + gc[cs] * b;
+  r = r + gc[2 * cs] * cc;
+  r = r + gc[3 * cs] * d;
+  r = r + gc[4 * cs] * e;
+  r = r + gc[5 * cs] * f;
+  r = r + gc[6 * cs] * gg;
+  r = r + gc[7 * cs] * h;
+  return -r;
+}
+
+__global__ void k_bhiggz(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.hz_start[t.nshots]) return;
+  const int b = find_shot(t.hz_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  const long long l = q - t.hz_start[b];
+  const long long cs = (long long)n2 * n3;
+  const int j = g.nmin2 + (int)(l % n2), k = g.nmin3 + (int)(l / n2);
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  const float *gc = S.gz + l;
+  const long long p0 = g.idx(0, j, k);
+  for (int i = g.nmin1 + 3; i >= g.nmin1 - 4; --i) {
+    const long long p = p0 + i;
+    u3[p] = hsum(gc, cs, u3[p + 1], u3[p + 2], u2[p], u2[p + 1], u2[p + 2], u1[p], u1[p + 1],
+                 u1[p + 2]);
+  }
+  gc += 8 * cs;
+  for (int i = g.nmax1 - 3; i <= g.nmax1 + 4; ++i) {
+    const long long p = p0 + i;
+    u3[p] = hsum(gc, cs, u3[p - 1], u3[p - 2], u2[p], u2[p - 1], u2[p - 2], u1[p], u1[p - 1],
+                 u1[p - 2]);
+  }
+}
+
+__global__ void k_bhiggx(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.hx_start[t.nshots]) return;
+  const int b = find_shot(t.hx_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n1 = g.nmax1 - g.nmin1 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  const long long l = q - t.hx_start[b];
+  const long long cs = (long long)n1 * n3;
+  const int i = g.nmin1 + (int)(l % n1), k = g.nmin3 + (int)(l / n1);
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  const long long L = g.ld1;
+  const float *gc = S.gx + l;
+  for (int j = g.nmin2 + 3; j >= g.nmin2 - 4; --j) {
+    const long long p = g.idx(i, j, k);
+    u3[p] = hsum(gc, cs, u3[p + L], u3[p + 2 * L], u2[p], u2[p + L], u2[p + 2 * L], u1[p],
+                 u1[p + L], u1[p + 2 * L]);
+  }
+  gc += 8 * cs;
+  for (int j = g.nmax2 - 3; j <= g.nmax2 + 4; ++j) {
+    const long long p = g.idx(i, j, k);
+    u3[p] = hsum(gc, cs, u3[p - L], u3[p - 2 * L], u2[p], u2[p - L], u2[p - 2 * L], u1[p],
+                 u1[p - L], u1[p - 2 * L]);
+  }
+}
+
+__global__ void k_bhiggy(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.hy_start[t.nshots]) return;
+  const int b = find_shot(t.hy_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps || S.g.nbound == 0) return;
+  const Geom &g = S.g;
+  const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
+  const long long l = q - t.hy_start[b];
+  const long long cs = (long long)n1 * n2;
+  const int i = g.nmin1 + (int)(l % n1), j = g.nmin2 + (int)(l / n1);
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  const long long P = g.plane();
+  const float *gc = S.gy + l;
+  for (int k = g.nmin3 + 3; k >= g.nmin3 - 4; --k) {
+    const long long p = g.idx(i, j, k);
+    u3[p] = hsum(gc, cs, u3[p + P], u3[p + 2 * P], u2[p], u2[p + P], u2[p + 2 * P], u1[p],
+                 u1[p + P], u1[p + 2 * P]);
+  }
+  gc += 8 * cs;
+  for (int k = g.nmax3 - 3; k <= g.nmax3 + 4; ++k) {
+    const long long p = g.idx(i, j, k);
+    u3[p] = hsum(gc, cs, u3[p - P], u3[p - 2 * P], u2[p], u2[p - P], u2[p - 2 * P], u1[p],
+                 u1[p - P], u1[p - 2 * P]);
+  }
+}
+
+__global__ void k_counter_add(int *counter, int add) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *counter += add;
+}
+
+cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
+                              int n_hz, int n_hx, int n_hy, int n_v2u, int has_ext, int has_3d,
+                              int has_adj3d, cudaStream_t s, int *nlaunch,
+                              cudaEvent_t ev_before, cudaEvent_t ev_after) {
+  int nl = 0;
+  // Every kernel of the step reads s = *counter + s_off; the counter is
+  // advanced once per chunk of steps.
+  if (has_ext && n_rec > 0) {
+    k_bextract<<<(n_rec + 127) / 128, 128, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (has_adj3d && n_v2u > 0) {
+    k_bv2u<<<n_v2u, 256, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  dim3 bs(32, 8, 1);
+  if (ev_before) cudaEventRecord(ev_before, s);
+  if (has_3d) k_bstep<false><<<n_step_tiles, bs, 0, s>>>(t, s_off);
+  else k_bstep<true><<<n_step_tiles, bs, 0, s>>>(t, s_off);
+  ++nl;
+  if (ev_after) cudaEventRecord(ev_after, s);
+  k_bhiggz<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
+  k_bhiggx<<<(n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
+  nl += 2;
+  if (has_3d && n_hy > 0) {
+    k_bhiggy<<<(n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (nlaunch) *nlaunch = nl;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_counter_add(int *counter, int add, cudaStream_t s) {
+  k_counter_add<<<1, 32, 0, s>>>(counter, add);
+  return cudaGetLastError();
+}
+
+}  // namespace swave

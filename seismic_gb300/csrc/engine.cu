@@ -16,6 +16,7 @@
 
 #include "../../include/swave.h"
 #include "engine.h"
+#include "batch.cuh"
 #include "swave_dev.cuh"
 
 using namespace swave;
@@ -345,224 +346,10 @@ int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int
 // ---------------------------------------------------------------------------
 
 int propagate_dev(sw_ctx *c, const sw_prop_desc &d, const DevIO &io) {
-  const sw_genpar &g = d.g;
-  int st = check_genpar(c, g);
-  if (st) return st;
-  if (d.tstep != 1 && d.tstep != -1) return fail(c, SW_BAD_PARAM, "tstep must be +-1");
-  const Geom G = make_geom(g);
-  const Coefs C = make_coefs(g);
-  const int nt = g.nt;
-  const int ntsnap = nt / g.snapi;
-  const size_t fbytes = (size_t)G.total() * sizeof(float);
-  const size_t nphys = (size_t)g.nz * g.nx * g.ny;
-  cudaStream_t s = c->stream;
-  cudaError_t e;
-
-  // Five wavefields (allocateUSpace + zeroUSpace, Propagator.f90:144-145).
-  float *f[5];
-  for (int q = 0; q < 5; ++q) {
-    f[q] = (float *)dbuf(c, "u" + std::to_string(q), fbytes, &st);
-    if (!f[q]) return st;
-    if ((e = cudaMemsetAsync(f[q], 0, fbytes, s)) != cudaSuccess) return cuda_fail(c, e, "memset");
-  }
-  float *tmp = nullptr;
-  const bool adj3d = !g.twoD && d.fd_scheme == SW_FD_ADJOINT;
-  if (adj3d) {
-    tmp = (float *)dbuf(c, "v2u", fbytes, &st);
-    if (!tmp) return st;
-    if ((e = cudaMemsetAsync(tmp, 0, fbytes, s)) != cudaSuccess) return cuda_fail(c, e, "memset");
-  }
-  // Higdon coefficients (Boundary.f90:17-63).
-  const long long n1 = G.nmax1 - G.nmin1 + 1, n2 = G.nmax2 - G.nmin2 + 1, n3 = G.nmax3 - G.nmin3 + 1;
-  float *gz = (float *)dbuf(c, "gz", 16 * n2 * n3 * sizeof(float), &st);
-  float *gx = (float *)dbuf(c, "gx", 16 * n1 * n3 * sizeof(float), &st);
-  float *gy = (float *)dbuf(c, "gy", 16 * n1 * n2 * sizeof(float), &st);
-  if (!gz || !gx || !gy) return st;
-  if ((e = launch_higdon_coeffs(G, io.vel_pad, g.dt, 1.f / g.dx, 1.f / g.dy, 1.f / g.dz, gz, gx,
-                                gy, s)) != cudaSuccess)
-    return cuda_fail(c, e, "higdon coeffs");
-  c->stats.launches_total++;
-
-  // Injection plan.
-  InjPlan inj;
-  if ((st = build_injection(c, g, G, d.injection, io.nsou, io.sou_coord, io.vel_phys_host, inj)))
-    return st;
-  int *d_off = nullptr;
-  InjEntry *d_ent = nullptr;
-  if (inj.on) {
-    d_off = (int *)dbuf(c, "inj_off", inj.off.size() * sizeof(int), &st);
-    d_ent = (InjEntry *)dbuf(c, "inj_ent", inj.ent.size() * sizeof(InjEntry), &st);
-    if (!d_off || !d_ent) return st;
-    cudaMemcpyAsync(d_off, inj.off.data(), inj.off.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-    if ((e = cudaMemcpyAsync(d_ent, inj.ent.data(), inj.ent.size() * sizeof(InjEntry),
-                             cudaMemcpyHostToDevice, s)) != cudaSuccess)
-      return cuda_fail(c, e, "upload injection plan");
-    // The host plan must outlive the async copies.
-    cudaStreamSynchronize(s);
-  }
-  // Extraction plan.
-  ExtPlan ext;
-  if ((st = build_extraction(c, g, G, d.extraction, io.nrec, io.rec_coord, ext))) return st;
-  int *d_ric = nullptr;
-  float *d_wz = nullptr, *d_wx = nullptr;
-  if (ext.on) {
-    d_ric = (int *)dbuf(c, "ext_ic", ext.ic.size() * sizeof(int), &st);
-    d_wz = (float *)dbuf(c, "ext_wz", ext.wz.size() * sizeof(float), &st);
-    d_wx = (float *)dbuf(c, "ext_wx", ext.wx.size() * sizeof(float), &st);
-    if (!d_ric || !d_wz || !d_wx) return st;
-    cudaMemcpyAsync(d_ric, ext.ic.data(), ext.ic.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_wz, ext.wz.data(), ext.wz.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_wx, ext.wx.data(), ext.wx.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaStreamSynchronize(s);
-  }
-  // Tapers for the imaging conditions (compute_taper, Taper.f90:14-28).
-  float *d_tx = nullptr, *d_ty = nullptr;
-  if (d.imaging != SW_IMG_NONE) {
-    std::vector<float> tx, ty;
-    compute_taper(g.nx, g.ny, tx, ty);
-    d_tx = (float *)dbuf(c, "taperx", tx.size() * sizeof(float), &st);
-    d_ty = (float *)dbuf(c, "tapery", ty.size() * sizeof(float), &st);
-    if (!d_tx || !d_ty) return st;
-    cudaMemcpyAsync(d_tx, tx.data(), tx.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_ty, ty.data(), ty.size() * sizeof(float), cudaMemcpyHostToDevice, s);
-    cudaStreamSynchronize(s);
-  }
-
-  StepArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.g = G;
-  a.c = C;
-  a.vel = io.vel_pad;
-  a.k12 = 12.f * (g.dt * g.dt);
-  a.div11 = 1.f / 11.f;
-  a.inj_on = inj.on;
-  a.bi0 = inj.bi0; a.bi1 = inj.bi1; a.bj0 = inj.bj0; a.bj1 = inj.bj1; a.bk0 = inj.bk0; a.bk1 = inj.bk1;
-  a.inj_off = d_off;
-  a.inj_ent = d_ent;
-  a.src_tr = io.sou_trace_dev;
-  a.nt = nt;
-  a.ref = io.ref_dev;
-  a.taperx = d_tx;
-  a.tapery = d_ty;
-  a.image = io.image_dev;
-  a.illum = io.illum_dev;
-  {
-    const float xs = g.dt * (float)g.snapi;
-    a.dt2snap = xs * xs;  // genpar%dt2 (compute_function_gradient.f90:237)
-  }
-  ExtArgs ea;
-  std::memset(&ea, 0, sizeof(ea));
-  ea.g = G;
-  ea.nrec = ext.nrec;
-  ea.nt = nt;
-  ea.half = g.lsinc / 2;
-  ea.mode = ext.mode;
-  ea.ic = d_ric;
-  ea.wz = d_wz;
-  ea.wx = d_wx;
-  ea.vel = io.vel_pad;
-  ea.tr = io.rec_trace_dev;
-  if (d.extraction == SW_EXT_LSRTM_SINC)
-    ea.vconst = g.twoD ? 1.f / (g.dz * g.dx) : 1.f / ((g.dz * g.dx) * g.dy);
-  else
-    ea.vconst = 1.f;
-  HigArgs ha;
-  ha.g = G;
-  ha.gz = gz;
-  ha.gx = gx;
-  ha.gy = gy;
-
-  // Rotating time levels (FDswaptime_pointer, FDswaptimes.f90:14-24).
-  int um1 = 0, u0 = 1, u1 = 2, u2 = 3, u3 = 4;
-  int wcounter = 0, mcounter = 0;
-  const long long npts = n1 * n2 * n3;
-  const int nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
-  int it = d.tmin;
-  for (int step = 0; step < nsteps; ++step, it += d.tstep) {
-    if (ext.on) {
-      ea.it = it;
-      ea.u2 = f[u2];
-      if ((e = launch_extract(ea, s)) != cudaSuccess) return cuda_fail(c, e, "extract");
-      c->stats.launches_total++;
-    }
-    a.u2 = f[u2]; a.u1 = f[u1]; a.u0 = f[u0]; a.um1 = f[um1]; a.u3 = f[u3];
-    a.lap_src = f[u2];
-    a.it = it;
-    a.snap_on = 0;
-    a.img = 0;
-    a.born_on = 0;
-    const bool snapstep = (it % g.snapi) == 0;
-    if (d.extract_wave && snapstep) {
-      ++wcounter;
-      if (wcounter <= ntsnap) {
-        a.snap_on = 1;
-        a.snap_out = io.wave_dev + (size_t)(wcounter - 1) * nphys;
-      }
-    }
-    if (d.imaging != SW_IMG_NONE && d.imaging != SW_IMG_BORN && d.tstep == -1 && snapstep) {
-      ++mcounter;
-      const int index = ntsnap - mcounter + 1;
-      if (index >= 1) {
-        a.img = d.imaging;
-        a.w0 = io.wave_dev + (size_t)(index - 1) * nphys;
-        a.wm1 = io.wave_dev + (size_t)(std::max(index - 1, 1) - 1) * nphys;
-        a.wp1 = io.wave_dev + (size_t)(std::min(index + 1, ntsnap) - 1) * nphys;
-      }
-    }
-    if (d.imaging == SW_IMG_BORN && d.tstep == 1 && snapstep) {
-      ++mcounter;
-      if (mcounter <= ntsnap) {
-        a.born_on = 1;
-        a.w0 = io.wave_dev + (size_t)(mcounter - 1) * nphys;
-      }
-    }
-    if (adj3d) {
-      if ((e = launch_v2u(G, io.vel_pad, f[u2], tmp, s)) != cudaSuccess) return cuda_fail(c, e, "v2u");
-      a.lap_src = tmp;
-      c->stats.launches_total++;
-    }
-    const bool timed = c->profiling;
-    if (timed) {
-      if (c->ev.size() < 2) {
-        c->ev.resize(2);
-        cudaEventCreate(&c->ev[0]);
-        cudaEventCreate(&c->ev[1]);
-      }
-      cudaEventRecord(c->ev[0], s);
-    }
-    if ((e = launch_step(a, g.twoD && d.fd_scheme == SW_FD_ADJOINT, s)) != cudaSuccess)
-      return cuda_fail(c, e, "step");
-    if (timed) {
-      cudaEventRecord(c->ev[1], s);
-      cudaEventSynchronize(c->ev[1]);
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
-      c->stats.step_kernel_ms += ms;
-      c->stats.step_kernel_timed++;
-      c->stats.step_bytes += (uint64_t)npts * 24ull;
-    }
-    c->stats.launches_total++;
-    c->stats.launches_step++;
-    c->stats.points_updated += (uint64_t)npts;
-    ha.u3 = f[u3];
-    ha.u2 = f[u2];
-    ha.u1 = f[u1];
-    int nl = 0;
-    if ((e = launch_higdon(ha, s, &nl)) != cudaSuccess) return cuda_fail(c, e, "higdon");
-    c->stats.launches_total += nl;
-    const int t = um1;
-    um1 = u0; u0 = u1; u1 = u2; u2 = u3; u3 = t;
-  }
-  if (io.final_u2_host) {
-    // Dense padded layout without the leading-dimension rounding.
-    e = cudaMemcpy2DAsync(io.final_u2_host, (size_t)G.n1p * sizeof(float), f[u2],
-                          (size_t)G.ld1 * sizeof(float), (size_t)G.n1p * sizeof(float),
-                          (size_t)G.n2p * G.n3p, cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return cuda_fail(c, e, "download u2");
-  }
-  e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(c, e, "propagate");
-  return SW_OK;
+  std::vector<PhaseShot> one(1);
+  one[0].d = d;
+  one[0].io = io;
+  return run_phases(c, one, c->run_opts);
 }
 
 // Uploads the physical velocity and pads it on the device.

@@ -13,6 +13,11 @@ struct DBuf {
   size_t cap = 0;
 };
 
+struct RunOpts {
+  int chunk = 16;       // steps per captured graph
+  bool use_graph = true;
+};
+
 struct sw_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -21,9 +26,12 @@ struct sw_ctx {
   std::vector<cudaEvent_t> ev;
   bool profiling = false;
   sw_stats stats{};
+  RunOpts run_opts;
 };
 
 namespace swave {
+
+using ::RunOpts;
 
 struct InjPlan {
   int on = 0;
@@ -56,6 +64,18 @@ struct DevIO {
   float *final_u2_host = nullptr;
 };
 
+// A shot's model window (ModelSpace%oxw, nxw, ...).
+struct Window {
+  float oxw, oyw, endx, endy;
+  int nxw, nyw;
+};
+
+// One shot of a propagation phase: its descriptor and device arrays.
+struct PhaseShot {
+  sw_prop_desc d;
+  DevIO io;
+};
+
 int fail(sw_ctx *c, int code, const char *fmt, ...);
 int cuda_fail(sw_ctx *c, cudaError_t e, const char *what);
 void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st);
@@ -64,6 +84,14 @@ Geom make_geom(const sw_genpar &g);
 Coefs make_coefs(const sw_genpar &g);
 void mksinc(float *sinc, int lsinc, float shift);
 void compute_taper(int nxw, int nyw, std::vector<float> &tx, std::vector<float> &ty);
+int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
+                    const float *sou_coord, const float *vel_phys, InjPlan &plan);
+int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nrec,
+                     const float *rec_coord, ExtPlan &plan);
+int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt);
+int compute_window(sw_ctx *c, const sw_genpar &g, float apx, float apy, const float *sou,
+                   int nrec, const float *rec, Window &w);
+void window_host(const sw_genpar &g, const Window &w, const float *big, std::vector<float> &small);
 int propagate_dev(sw_ctx *c, const sw_prop_desc &d, const DevIO &io);
 int upload_velocity(sw_ctx *c, const sw_genpar &g, const float *vel, const char *slot,
                     float **vel_pad);

@@ -228,48 +228,6 @@ inline int gsz(long long n) {
 // ---------------------------------------------------------------------------
 // compute_fct_gdt
 // ---------------------------------------------------------------------------
-namespace {
-
-struct Window {
-  float oxw, oyw, endx, endy;
-  int nxw, nyw;
-};
-
-// extract_coord_source_receiver_patch (ExtractPadModel.f90:19-85) and the
-// window size of copy_window_vel_gath (ExtractPadModel.f90:446-451).
-int shot_window(sw_ctx *c, const sw_fwi_desc &d, const sw_fwi_shot &s, Window &w) {
-  const sw_genpar &g = d.g;
-  if (s.nrec < 1 || !s.rec_coord || !s.dobs) return fail(c, SW_BAD_PARAM, "shot without receivers");
-  const float sx = s.sou_coord[1], sy = s.sou_coord[2];
-  float gx1 = s.rec_coord[1], gy1 = s.rec_coord[2], gxn = gx1, gyn = gy1;
-  for (int i = 1; i < s.nrec; ++i) {
-    gx1 = std::min(gx1, s.rec_coord[3 * i + 1]);
-    gxn = std::max(gxn, s.rec_coord[3 * i + 1]);
-    gy1 = std::min(gy1, s.rec_coord[3 * i + 2]);
-    gyn = std::max(gyn, s.rec_coord[3 * i + 2]);
-  }
-  const float minx = std::min(sx, gx1), miny = std::min(sy, gy1);
-  const float maxx = std::max(sx, gxn), maxy = std::max(sy, gyn);
-  const float mx1 = (gx1 + sx) / 2, mxn = (gxn + sx) / 2;
-  const float my1 = (gy1 + sy) / 2, myn = (gyn + sy) / 2;
-  const float cx = mx1 + std::fabs(mxn - mx1) / 2;
-  const float cy = my1 + std::fabs(myn - my1) / 2;
-  w.oxw = std::min(minx, cx - d.aperture_x / 2);
-  w.endx = std::max(maxx, cx + d.aperture_x / 2);
-  w.oyw = std::min(miny, cy - d.aperture_y / 2);
-  w.endy = std::max(maxy, cy + d.aperture_y / 2);
-  w.nxw = (int)lroundf((w.endx - w.oxw) / g.dx) + 1;
-  w.nyw = (int)lroundf((w.endy - w.oyw) / g.dy) + 1;
-  if (g.twoD) {
-    w.nyw = 1;
-    w.oyw = g.oy;
-  }
-  if (w.nxw < 4 || w.nyw < 1) return fail(c, SW_BAD_PARAM, "degenerate shot window");
-  return SW_OK;
-}
-
-}  // namespace
-
 int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const float *wavelet,
                    int nshot, const sw_fwi_shot *shots, const float *vpmask, double *f,
                    float *grad, float *illum) {
@@ -300,7 +258,9 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
   for (int is = 0; is < nshot; ++is) {
     const sw_fwi_shot &sh = shots[is];
     Window w;
-    if ((st = shot_window(c, d, sh, w))) return st;
+    if ((st = compute_window(c, G, d.aperture_x, d.aperture_y, sh.sou_coord, sh.nrec, sh.rec_coord, w)))
+      return st;
+    if (!sh.dobs) return fail(c, SW_BAD_PARAM, "shot %d without observed data", is);
     sw_genpar g = G;
     g.nx = w.nxw;
     g.ny = w.nyw;
@@ -319,10 +279,8 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     if ((e = launch_pad_velocity(Gw, vsmall, vpad, s)) != cudaSuccess) return cuda_fail(c, e, "pad");
     c->stats.launches_total += 2;
     // Host copy of the window velocity: the injection weights v^2 at the
-    // source node are part of the injection plan.
-    hv.resize(nw);
-    if ((st = download(c, hv.data(), vsmall, nw * sizeof(float)))) return st;
-    cudaStreamSynchronize(s);
+    // source and receiver nodes are part of the injection plans.
+    window_host(G, w, vel, hv);
     // AMOD_to_memory (to_disk_to_memory_AMOD.f90:27-82).
     DevIO a;
     a.vel_pad = vpad;

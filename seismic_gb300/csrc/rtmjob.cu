@@ -1,0 +1,406 @@
+// rtmjob.cu - multi-shot RTM: windows, batches admitted by HBM footprint,
+// forward + backward phases of a whole batch in the same launches, image
+// stacking and illumination normalisation.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/swave.h"
+#include "batch.cuh"
+#include "engine.h"
+
+using namespace swave;
+
+namespace swave {
+
+// extract_coord_source_receiver_patch (ExtractPadModel.f90:19-85) and the
+// window size of copy_window_vel_gath (ExtractPadModel.f90:446-451).
+int compute_window(sw_ctx *c, const sw_genpar &g, float apx, float apy, const float *sou,
+                   int nrec, const float *rec, Window &w) {
+  if (nrec < 1 || !rec) return fail(c, SW_BAD_PARAM, "shot without receivers");
+  const float sx = sou[1], sy = sou[2];
+  float gx1 = rec[1], gy1 = rec[2], gxn = gx1, gyn = gy1;
+  for (int i = 1; i < nrec; ++i) {
+    gx1 = std::min(gx1, rec[3 * i + 1]);
+    gxn = std::max(gxn, rec[3 * i + 1]);
+    gy1 = std::min(gy1, rec[3 * i + 2]);
+    gyn = std::max(gyn, rec[3 * i + 2]);
+  }
+  const float minx = std::min(sx, gx1), miny = std::min(sy, gy1);
+  const float maxx = std::max(sx, gxn), maxy = std::max(sy, gyn);
+  const float mx1 = (gx1 + sx) / 2, mxn = (gxn + sx) / 2;
+  const float my1 = (gy1 + sy) / 2, myn = (gyn + sy) / 2;
+  const float cx = mx1 + std::fabs(mxn - mx1) / 2;
+  const float cy = my1 + std::fabs(myn - my1) / 2;
+  w.oxw = std::min(minx, cx - apx / 2);
+  w.endx = std::max(maxx, cx + apx / 2);
+  w.oyw = std::min(miny, cy - apy / 2);
+  w.endy = std::max(maxy, cy + apy / 2);
+  w.nxw = (int)lroundf((w.endx - w.oxw) / g.dx) + 1;
+  w.nyw = (int)lroundf((w.endy - w.oyw) / g.dy) + 1;
+  if (g.twoD) {
+    w.nyw = 1;
+    w.oyw = g.oy;
+  }
+  if (w.nxw < 4 || w.nyw < 1) return fail(c, SW_BAD_PARAM, "degenerate shot window");
+  return SW_OK;
+}
+
+// mod_window_pad(adj=.true.) on the host copy of the model (the injection
+// plan needs v at the source nodes).
+void window_host(const sw_genpar &g, const Window &w, const float *big, std::vector<float> &small) {
+  small.resize((size_t)g.nz * w.nxw * w.nyw);
+  for (int j = 1; j <= w.nyw; ++j) {
+    const float cy = (float)(j - 1) * g.dy + w.oyw;
+    const int iy1 = std::min(g.ny, std::max(1, (int)lroundf((cy - g.oy) / g.dy) + 1));
+    for (int i = 1; i <= w.nxw; ++i) {
+      const float cx = (float)(i - 1) * g.dx + w.oxw;
+      const int ix1 = std::min(g.nx, std::max(1, (int)lroundf((cx - g.ox) / g.dx) + 1));
+      std::memcpy(&small[(size_t)g.nz * ((i - 1) + (size_t)w.nxw * (j - 1))],
+                  &big[(size_t)g.nz * ((ix1 - 1) + (size_t)g.nx * (iy1 - 1))],
+                  (size_t)g.nz * sizeof(float));
+    }
+  }
+}
+
+}  // namespace swave
+
+namespace {
+
+__global__ void k_illum_stats(long long n, const float *il, float *pmax, double *psum) {
+  __shared__ float smax[256];
+  __shared__ double ssum[256];
+  float m = -INFINITY;
+  double s = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float v = il[q];
+    m = fmaxf(m, v);
+    s = s + (double)v * (double)v;
+  }
+  smax[threadIdx.x] = m;
+  ssum[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      smax[threadIdx.x] = fmaxf(smax[threadIdx.x], smax[threadIdx.x + w]);
+      ssum[threadIdx.x] = ssum[threadIdx.x] + ssum[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pmax[blockIdx.x] = smax[0];
+    psum[blockIdx.x] = ssum[0];
+  }
+}
+
+// illu = (illu + maxval(illu)/10000)/sqrt(sum(dprod(illu,illu))/size(illu));
+// imag = imag/illu (compute_function_gradient.f90:452-453).
+__global__ void k_illum_normalise(long long n, int nb, const float *pmax, const double *psum,
+                                  const float *im, const float *il, float *out) {
+  __shared__ float m;
+  __shared__ double r;
+  if (threadIdx.x == 0) {
+    float mm = pmax[0];
+    double ss = 0.0;
+    for (int b = 0; b < nb; ++b) {
+      mm = fmaxf(mm, pmax[b]);
+      ss = ss + psum[b];
+    }
+    m = mm;
+    r = sqrt(ss / (double)n);
+  }
+  __syncthreads();
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const float v = (float)((double)(il[q] + m / 10000.f) / r);
+    out[q] = im[q] / v;
+  }
+}
+
+}  // namespace
+
+struct sw_rtm_job {
+  sw_ctx *c;
+  sw_genpar g;
+  float apx, apy;
+  std::vector<float> vel_host;
+  float *vel = nullptr;       // full model (device)
+  float *wavelet = nullptr;   // g.nt (device)
+  float *image = nullptr, *illum = nullptr;
+  struct Shot {
+    sw_shot s;
+    Window w;
+    std::vector<float> rec;   // host copy of coordinates
+    float *data = nullptr;    // device nrec*nt
+  };
+  std::vector<Shot> shots;
+  int max_batch = 64;
+  double mem_fraction = 0.85;
+  int last_batch = 0;
+  uint64_t points = 0;
+};
+
+static void job_free(sw_rtm_job *j) {
+  for (auto &s : j->shots)
+    if (s.data) cudaFree(s.data);
+  for (void *p : {(void *)j->vel, (void *)j->wavelet, (void *)j->image, (void *)j->illum})
+    if (p) cudaFree(p);
+}
+
+int sw_rtm_job_create(sw_ctx *c, const sw_genpar *model, float apx, float apy, const float *vel,
+                      const float *wavelet, int nshot, const sw_shot *shots, sw_rtm_job **out) {
+  if (!c || !model || !vel || !wavelet || nshot < 1 || !shots || !out) return SW_BAD_PARAM;
+  cudaSetDevice(c->device);
+  int st = check_genpar(c, *model);
+  if (st) return st;
+  sw_rtm_job *j = new sw_rtm_job();
+  j->c = c;
+  j->g = *model;
+  j->apx = apx;
+  j->apy = apy;
+  const size_t n = (size_t)model->nz * model->nx * model->ny;
+  j->vel_host.assign(vel, vel + n);
+  auto bail = [&](int code) {
+    job_free(j);
+    delete j;
+    return code;
+  };
+  cudaStream_t s = c->stream;
+  if (cudaMalloc(&j->vel, n * 4) != cudaSuccess || cudaMalloc(&j->image, n * 4) != cudaSuccess ||
+      cudaMalloc(&j->illum, n * 4) != cudaSuccess ||
+      cudaMalloc(&j->wavelet, (size_t)model->nt * 4) != cudaSuccess) {
+    cudaGetLastError();
+    return bail(fail(c, SW_OOM_ADMISSION, "RTM job model buffers do not fit"));
+  }
+  cudaMemcpyAsync(j->vel, vel, n * 4, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(j->wavelet, wavelet, (size_t)model->nt * 4, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(j->image, 0, n * 4, s);
+  cudaMemsetAsync(j->illum, 0, n * 4, s);
+  j->shots.resize(nshot);
+  for (int i = 0; i < nshot; ++i) {
+    auto &S = j->shots[i];
+    S.s = shots[i];
+    if (S.s.nt < 1 || S.s.nt > model->nt || !S.s.data)
+      return bail(fail(c, SW_BAD_PARAM, "shot %d: bad record length or data", i));
+    if ((st = compute_window(c, *model, apx, apy, S.s.sou_coord, S.s.nrec, S.s.rec_coord, S.w)))
+      return bail(st);
+    S.rec.assign(S.s.rec_coord, S.s.rec_coord + 3 * (size_t)S.s.nrec);
+    S.s.rec_coord = S.rec.data();
+    const size_t db = (size_t)S.s.nrec * S.s.nt * 4;
+    if (cudaMalloc(&S.data, db) != cudaSuccess) {
+      cudaGetLastError();
+      return bail(fail(c, SW_OOM_ADMISSION, "RTM job data of shot %d does not fit", i));
+    }
+    cudaMemcpyAsync(S.data, S.s.data, db, cudaMemcpyHostToDevice, s);
+    S.s.data = nullptr;
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(c, SW_CUDA_ERR, "job upload"));
+  *out = j;
+  return SW_OK;
+}
+
+int sw_rtm_job_set_batch(sw_rtm_job *j, int max_shots, double frac) {
+  if (!j || max_shots < 1 || !(frac > 0.0 && frac <= 1.0)) return SW_BAD_PARAM;
+  j->max_batch = max_shots;
+  j->mem_fraction = frac;
+  return SW_OK;
+}
+
+int sw_rtm_job_info(const sw_rtm_job *j, int *last_batch, uint64_t *points) {
+  if (!j) return SW_BAD_PARAM;
+  if (last_batch) *last_batch = j->last_batch;
+  if (points) *points = j->points;
+  return SW_OK;
+}
+
+int sw_rtm_job_reset(sw_rtm_job *j) {
+  if (!j) return SW_BAD_PARAM;
+  const size_t n = (size_t)j->g.nz * j->g.nx * j->g.ny;
+  cudaMemsetAsync(j->image, 0, n * 4, j->c->stream);
+  cudaMemsetAsync(j->illum, 0, n * 4, j->c->stream);
+  j->points = 0;
+  return cudaStreamSynchronize(j->c->stream) == cudaSuccess ? SW_OK : SW_CUDA_ERR;
+}
+
+int sw_rtm_job_destroy(sw_rtm_job *j) {
+  if (!j) return SW_OK;
+  cudaSetDevice(j->c->device);
+  cudaStreamSynchronize(j->c->stream);
+  job_free(j);
+  delete j;
+  return SW_OK;
+}
+
+namespace {
+
+sw_genpar shot_genpar(const sw_genpar &m, const Window &w, int nt) {
+  sw_genpar g = m;
+  g.nx = w.nxw;
+  g.ny = w.nyw;
+  g.ox = w.oxw;
+  g.oy = w.oyw;
+  g.nt = nt;
+  return g;
+}
+
+// Device bytes one shot needs while its batch runs.
+size_t shot_bytes(const sw_genpar &g) {
+  const Geom G = make_geom(g);
+  const size_t nw = (size_t)g.nz * g.nx * g.ny;
+  const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
+  return (size_t)G.total() * 4 * 7 + nw * 4 * (3 + ntsnap) + (1u << 20);
+}
+
+}  // namespace
+
+int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
+  if (!j || first < 0 || count < 1 || first + count > (int)j->shots.size()) return SW_BAD_PARAM;
+  sw_ctx *c = j->c;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int st = SW_OK;
+  const sw_genpar &M = j->g;
+  int next = first;
+  const int end = first + count;
+  while (next < end) {
+    // ---- admission by HBM footprint ----
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    // Buffers this context already holds for a previous batch are reusable.
+    size_t held = 0;
+    auto it = c->bufs.find("rtm_arena");
+    if (it != c->bufs.end()) held = it->second.cap;
+    const double budget = (double)(freeb + held) * j->mem_fraction;
+    std::vector<int> batch;
+    size_t need = 0;
+    while (next < end && (int)batch.size() < j->max_batch) {
+      const auto &S = j->shots[next];
+      const size_t b = shot_bytes(shot_genpar(M, S.w, S.s.nt));
+      if (!batch.empty() && (double)(need + b) > budget) break;
+      if (batch.empty() && (double)b > budget)
+        return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, b, budget);
+      need += b;
+      batch.push_back(next++);
+    }
+    j->last_batch = (int)batch.size();
+    // ---- per-shot device buffers carved from one arena ----
+    std::vector<size_t> offs;
+    size_t total = 0;
+    for (int id : batch) {
+      const auto &S = j->shots[id];
+      const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
+      const Geom G = make_geom(g);
+      const size_t nw = (size_t)g.nz * g.nx * g.ny;
+      const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
+      offs.push_back(total);
+      total += ((size_t)G.total() * 4 + 255) / 256 * 256;          // vel_pad
+      total += (nw * 4 + 255) / 256 * 256 * 3;                      // vsmall, image, illum
+      total += (nw * ntsnap * 4 + 255) / 256 * 256;                 // snapshots
+    }
+    char *arena = (char *)dbuf(c, "rtm_arena", total, &st);
+    if (!arena) return st;
+    std::vector<std::vector<float>> vhost(batch.size());
+    std::vector<PhaseShot> fwd(batch.size()), bwd(batch.size());
+    struct Bufs { float *vpad, *vsmall, *image, *illum, *wave; };
+    std::vector<Bufs> bufs(batch.size());
+    for (size_t q = 0; q < batch.size(); ++q) {
+      const auto &S = j->shots[batch[q]];
+      const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
+      const Geom G = make_geom(g);
+      const size_t nw = (size_t)g.nz * g.nx * g.ny;
+      const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
+      char *cur = arena + offs[q];
+      Bufs &B = bufs[q];
+      B.vpad = (float *)cur; cur += ((size_t)G.total() * 4 + 255) / 256 * 256;
+      B.vsmall = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+      B.image = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+      B.illum = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+      B.wave = (float *)cur;
+      // copy_window_vel_gath: window on the device, then model_pad.
+      if ((e = launch_window_vel(M.nz, M.nx, M.ny, M.ox, M.oy, M.dx, M.dy, S.w.nxw, S.w.nyw,
+                                 S.w.oxw, S.w.oyw, j->vel, B.vsmall, s)) != cudaSuccess)
+        return cuda_fail(c, e, "window vel");
+      if ((e = launch_pad_velocity(G, B.vsmall, B.vpad, s)) != cudaSuccess)
+        return cuda_fail(c, e, "pad vel");
+      cudaMemsetAsync(B.image, 0, nw * 4, s);
+      cudaMemsetAsync(B.illum, 0, nw * 4, s);
+      c->stats.launches_total += 2;
+      window_host(M, S.w, j->vel_host.data(), vhost[q]);
+      (void)ntsnap;
+      // Forward: Injection_sinc of the wavelet, Extraction_wavefield.
+      PhaseShot &F = fwd[q];
+      std::memset(&F.d, 0, sizeof(F.d));
+      F.d.g = g;
+      F.d.tmin = 1; F.d.tmax = g.nt; F.d.tstep = 1;
+      F.d.fd_scheme = SW_FD_FORWARD;
+      F.d.injection = SW_INJ_SINC;
+      F.d.extract_wave = 1;
+      F.io.vel_pad = B.vpad;
+      F.io.vel_phys_host = vhost[q].data();
+      F.io.nsou = 1;
+      F.io.sou_coord = S.s.sou_coord;
+      F.io.sou_trace_dev = j->wavelet;
+      F.io.wave_dev = B.wave;
+      // Backward: 2D adjoint (3D forward) stencil, Injection_sinc of the data,
+      // Imaging_condition_sourceonly_from_memory (to_disk_to_memory_RTM.f90:450-486).
+      PhaseShot &R = bwd[q];
+      std::memset(&R.d, 0, sizeof(R.d));
+      R.d.g = g;
+      R.d.tmin = g.nt; R.d.tmax = 1; R.d.tstep = -1;
+      R.d.fd_scheme = g.twoD ? SW_FD_ADJOINT : SW_FD_FORWARD;
+      R.d.injection = SW_INJ_SINC;
+      R.d.imaging = SW_IMG_RTM;
+      R.io.vel_pad = B.vpad;
+      R.io.vel_phys_host = vhost[q].data();
+      R.io.nsou = S.s.nrec;
+      R.io.sou_coord = S.rec.data();
+      R.io.sou_trace_dev = S.data;
+      R.io.wave_dev = B.wave;
+      R.io.image_dev = B.image;
+      R.io.illum_dev = B.illum;
+    }
+    const uint64_t p0 = c->stats.points_updated;
+    if ((st = run_phases(c, fwd, c->run_opts))) return st;
+    if ((st = run_phases(c, bwd, c->run_opts))) return st;
+    j->points += c->stats.points_updated - p0;
+    // mod_copy_image, shots in order.
+    for (size_t q = 0; q < batch.size(); ++q) {
+      const auto &S = j->shots[batch[q]];
+      if ((e = launch_copy_image(M.nz, M.nx, M.ny, M.ox, M.oy, M.dx, M.dy, S.w.nxw, S.w.nyw,
+                                 S.w.oxw, S.w.oyw, bufs[q].image, bufs[q].illum, j->image,
+                                 j->illum, s)) != cudaSuccess)
+        return cuda_fail(c, e, "copy image");
+      c->stats.launches_total++;
+    }
+  }
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "rtm job");
+  return SW_OK;
+}
+
+int sw_rtm_job_result(sw_rtm_job *j, float *image, float *illum, float *image_norm) {
+  if (!j) return SW_BAD_PARAM;
+  sw_ctx *c = j->c;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const long long n = (long long)j->g.nz * j->g.nx * j->g.ny;
+  int st = SW_OK;
+  if (image) cudaMemcpyAsync(image, j->image, n * 4, cudaMemcpyDeviceToHost, s);
+  if (illum) cudaMemcpyAsync(illum, j->illum, n * 4, cudaMemcpyDeviceToHost, s);
+  if (image_norm) {
+    const int nb = 296;
+    float *pmax = (float *)dbuf(c, "red_pmax", nb * sizeof(float), &st);
+    double *psum = (double *)dbuf(c, "red_psum", nb * sizeof(double), &st);
+    float *out = (float *)dbuf(c, "rtm_norm", n * 4, &st);
+    if (!pmax || !psum || !out) return st;
+    k_illum_stats<<<nb, 256, 0, s>>>(n, j->illum, pmax, psum);
+    k_illum_normalise<<<nb, 256, 0, s>>>(n, nb, pmax, psum, j->image, j->illum, out);
+    c->stats.launches_total += 2;
+    cudaMemcpyAsync(image_norm, out, n * 4, cudaMemcpyDeviceToHost, s);
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? SW_OK : cuda_fail(c, e, "rtm result");
+}

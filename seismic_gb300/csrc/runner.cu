@@ -1,0 +1,319 @@
+// runner.cu - runs one propagation phase for a batch of shots.
+//
+// Every shot of the batch gets its own five time levels, Higdon
+// coefficients, injection and extraction plans; the device descriptor
+// array (ShotDev) and prefix tables let one launch of each kernel cover the
+// whole batch.  The time loop is a CUDA graph of `chunk` steps captured
+// once and replayed; the step counter lives in device memory.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "batch.cuh"
+#include "engine.h"
+
+namespace swave {
+
+namespace {
+
+template <class T>
+T *carve(char *&cur, size_t n) {
+  T *p = reinterpret_cast<T *>(cur);
+  cur += (n * sizeof(T) + 255) / 256 * 256;
+  return p;
+}
+
+size_t rup(size_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+
+int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
+  const int nb = (int)shots.size();
+  if (nb == 0) return SW_OK;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int st = SW_OK;
+  std::vector<Geom> G(nb);
+  std::vector<InjPlan> inj(nb);
+  std::vector<ExtPlan> ext(nb);
+  std::vector<std::vector<float>> tx(nb), ty(nb);
+  bool has_3d = false, has_adj3d = false, has_ext = false;
+  // ---- host-side plans and arena sizes ----
+  size_t bytes = 0;
+  for (int b = 0; b < nb; ++b) {
+    const sw_prop_desc &d = shots[b].d;
+    const DevIO &io = shots[b].io;
+    if ((st = check_genpar(c, d.g))) return st;
+    if (d.tstep != 1 && d.tstep != -1) return fail(c, SW_BAD_PARAM, "tstep must be +-1");
+    if (b > 0 && (d.g.twoD != shots[0].d.g.twoD))
+      return fail(c, SW_BAD_PARAM, "a batch mixes 2D and 3D shots");
+    G[b] = make_geom(d.g);
+    has_3d = has_3d || !d.g.twoD;
+    has_adj3d = has_adj3d || (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT);
+    if ((st = build_injection(c, d.g, G[b], d.injection, io.nsou, io.sou_coord, io.vel_phys_host,
+                              inj[b])))
+      return st;
+    if ((st = build_extraction(c, d.g, G[b], d.extraction, io.nrec, io.rec_coord, ext[b])))
+      return st;
+    has_ext = has_ext || ext[b].on;
+    if (d.imaging != SW_IMG_NONE) compute_taper(d.g.nx, d.g.ny, tx[b], ty[b]);
+    const size_t fb = (size_t)G[b].total() * sizeof(float);
+    const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
+                    n3 = G[b].nmax3 - G[b].nmin3 + 1;
+    bytes += 5 * rup(fb);
+    if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT) bytes += rup(fb);
+    bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
+    bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry));
+    bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
+    bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
+  }
+  bytes += rup(nb * sizeof(ShotDev)) + 6 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
+  char *arena = (char *)dbuf(c, "batch_arena", bytes, &st);
+  if (!arena) return st;
+  char *cur = arena;
+  // ---- carve and fill ----
+  std::vector<ShotDev> hs(nb);
+  std::vector<int> step_tiles(nb + 1, 0), rec_start(nb + 1, 0), hz(nb + 1, 0), hx(nb + 1, 0),
+      hy(nb + 1, 0), v2b(nb + 1, 0);
+  int max_steps = 0;
+  for (int b = 0; b < nb; ++b) {
+    const sw_prop_desc &d = shots[b].d;
+    const DevIO &io = shots[b].io;
+    const sw_genpar &g = d.g;
+    ShotDev &S = hs[b];
+    std::memset(&S, 0, sizeof(S));
+    S.g = G[b];
+    S.c = make_coefs(g);
+    const size_t nf = (size_t)G[b].total();
+    for (int q = 0; q < 5; ++q) {
+      S.f[q] = carve<float>(cur, nf);
+      if ((e = cudaMemsetAsync(S.f[q], 0, nf * sizeof(float), s)) != cudaSuccess)
+        return cuda_fail(c, e, "zero fields");
+    }
+    S.adj2d = g.twoD && d.fd_scheme == SW_FD_ADJOINT;
+    S.adj3d = !g.twoD && d.fd_scheme == SW_FD_ADJOINT;
+    if (S.adj3d) {
+      S.v2u = carve<float>(cur, nf);
+      cudaMemsetAsync(S.v2u, 0, nf * sizeof(float), s);
+    }
+    S.vel = io.vel_pad;
+    const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
+                    n3 = G[b].nmax3 - G[b].nmin3 + 1;
+    float *gz = carve<float>(cur, 16 * n2 * n3), *gx = carve<float>(cur, 16 * n1 * n3),
+          *gy = carve<float>(cur, 16 * n1 * n2);
+    if ((e = launch_higdon_coeffs(G[b], io.vel_pad, g.dt, 1.f / g.dx, 1.f / g.dy, 1.f / g.dz, gz,
+                                  gx, gy, s)) != cudaSuccess)
+      return cuda_fail(c, e, "higdon coeffs");
+    c->stats.launches_total++;
+    S.gz = gz; S.gx = gx; S.gy = gy;
+    S.inj_on = inj[b].on;
+    if (inj[b].on) {
+      S.bi0 = inj[b].bi0; S.bi1 = inj[b].bi1; S.bj0 = inj[b].bj0; S.bj1 = inj[b].bj1;
+      S.bk0 = inj[b].bk0; S.bk1 = inj[b].bk1;
+      int *off = carve<int>(cur, inj[b].off.size());
+      InjEntry *ent = carve<InjEntry>(cur, inj[b].ent.size());
+      cudaMemcpyAsync(off, inj[b].off.data(), inj[b].off.size() * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(ent, inj[b].ent.data(), inj[b].ent.size() * sizeof(InjEntry),
+                      cudaMemcpyHostToDevice, s);
+      S.inj_off = off;
+      S.inj_ent = ent;
+      S.src_tr = io.sou_trace_dev;
+    }
+    S.ext_mode = ext[b].on ? ext[b].mode : 0;
+    S.nrec = ext[b].on ? ext[b].nrec : 0;
+    S.ext_half = g.lsinc / 2;
+    if (ext[b].on) {
+      int *ric = carve<int>(cur, ext[b].ic.size());
+      float *wz = carve<float>(cur, ext[b].wz.size()), *wx = carve<float>(cur, ext[b].wx.size());
+      cudaMemcpyAsync(ric, ext[b].ic.data(), ext[b].ic.size() * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(wz, ext[b].wz.data(), ext[b].wz.size() * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(wx, ext[b].wx.data(), ext[b].wx.size() * 4, cudaMemcpyHostToDevice, s);
+      S.ric = ric; S.wz = wz; S.wx = wx;
+      S.rec_tr = io.rec_trace_dev;
+      S.vconst = 1.f;
+      if (d.extraction == SW_EXT_LSRTM_SINC)
+        S.vconst = g.twoD ? 1.f / (g.dz * g.dx) : 1.f / ((g.dz * g.dx) * g.dy);
+    }
+    S.tmin = d.tmin;
+    S.tstep = d.tstep;
+    S.nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
+    S.nt = g.nt;
+    S.snapi = g.snapi;
+    S.ntsnap = g.nt / g.snapi;
+    S.extract_wave = d.extract_wave;
+    S.imaging = d.imaging;
+    S.wave = io.wave_dev;
+    S.image = io.image_dev;
+    S.illum = io.illum_dev;
+    S.ref = io.ref_dev;
+    if (d.imaging != SW_IMG_NONE) {
+      float *a = carve<float>(cur, tx[b].size() + 1), *bq = carve<float>(cur, ty[b].size() + 1);
+      cudaMemcpyAsync(a, tx[b].data(), tx[b].size() * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(bq, ty[b].data(), ty[b].size() * 4, cudaMemcpyHostToDevice, s);
+      S.taperx = a;
+      S.tapery = bq;
+    }
+    S.k12 = 12.f * (g.dt * g.dt);
+    S.div11 = 1.f / 11.f;
+    {
+      const float xs = g.dt * (float)g.snapi;
+      S.dt2snap = xs * xs;  // genpar%dt2 (compute_function_gradient.f90:237)
+    }
+    S.npts = n1 * n2 * n3;
+    if ((S.extract_wave || (S.imaging != SW_IMG_NONE)) && !S.wave)
+      return fail(c, SW_BAD_PARAM, "snapshot buffer missing");
+    if (S.imaging >= 1 && S.imaging <= 3 && (!S.image || !S.illum))
+      return fail(c, SW_BAD_PARAM, "image buffers missing");
+    if (S.imaging == SW_IMG_BORN && !S.ref) return fail(c, SW_BAD_PARAM, "reflectivity missing");
+    max_steps = std::max(max_steps, S.nsteps);
+    const int ntz = (int)((n1 + 31) / 32), ntx = (int)((n2 + 7) / 8);
+    step_tiles[b + 1] = step_tiles[b] + ntz * ntx * (int)n3;
+    rec_start[b + 1] = rec_start[b] + S.nrec;
+    hz[b + 1] = hz[b] + (int)(n2 * n3);
+    hx[b + 1] = hx[b] + (int)(n1 * n3);
+    hy[b + 1] = hy[b] + (g.twoD ? 0 : (int)(n1 * n2));
+    v2b[b + 1] = v2b[b] + (S.adj3d ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256) : 0);
+  }
+  ShotDev *dshots = carve<ShotDev>(cur, nb);
+  int *dtab[6];
+  std::vector<int> *htab[6] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b};
+  for (int q = 0; q < 6; ++q) {
+    dtab[q] = carve<int>(cur, nb + 1);
+    cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s);
+  }
+  int *counter = carve<int>(cur, 1);
+  cudaMemcpyAsync(dshots, hs.data(), nb * sizeof(ShotDev), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  if ((size_t)(cur - arena) > bytes) return fail(c, SW_CUDA_ERR, "arena overflow");
+  BatchTables t;
+  t.nshots = nb;
+  t.shots = dshots;
+  t.step_tiles = dtab[0];
+  t.rec_start = dtab[1];
+  t.hz_start = dtab[2];
+  t.hx_start = dtab[3];
+  t.hy_start = dtab[4];
+  t.v2u_blocks = dtab[5];
+  t.counter = counter;
+  // The host plans above must stay alive until the uploads complete.
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch setup");
+
+  const int n_tiles = step_tiles[nb], n_rec = rec_start[nb], n_hz = hz[nb], n_hx = hx[nb],
+            n_hy = hy[nb], n_v2u = v2b[nb];
+  long long npts_total = 0;
+  for (auto &S : hs) npts_total += S.npts;
+  // ---- time loop ----
+  const int chunk = std::max(1, std::min(opt.chunk, max_steps));
+  const int nchunks = (max_steps + chunk - 1) / chunk;
+  const bool prof = c->profiling;
+  if (prof && (int)c->ev.size() < 2 * chunk) {
+    const size_t old = c->ev.size();
+    c->ev.resize(2 * chunk);
+    for (size_t q = old; q < c->ev.size(); ++q) cudaEventCreate(&c->ev[q]);
+  }
+  auto record_chunk = [&](int nsteps_here) -> int {
+    int launched = 0;
+    for (int q = 0; q < nsteps_here; ++q) {
+      int nl = 0;
+      // In profiling mode events bracket the fused step kernel only.
+      if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
+                                 has_adj3d, s, &nl, prof ? c->ev[2 * q] : nullptr,
+                                 prof ? c->ev[2 * q + 1] : nullptr)) != cudaSuccess)
+        return -1;
+      launched += nl;
+    }
+    if ((e = launch_counter_add(counter, nsteps_here, s)) != cudaSuccess) return -1;
+    return launched + 1;
+  };
+  uint64_t launches = 0;
+  if (opt.use_graph && nchunks > 1) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+      return cuda_fail(c, e, "begin capture");
+    const int per = record_chunk(chunk);
+    cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    if (per < 0 || ec != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return cuda_fail(c, per < 0 ? e : ec, "capture step graph");
+    }
+    if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
+      cudaGraphDestroy(graph);
+      return cuda_fail(c, e, "instantiate step graph");
+    }
+    for (int q = 0; q < nchunks; ++q) {
+      if ((e = cudaGraphLaunch(exec, s)) != cudaSuccess) break;
+      launches += per;
+      if (prof) {
+        cudaEventSynchronize(c->ev[2 * chunk - 1]);
+        const int live = std::min(chunk, max_steps - q * chunk);
+        for (int k = 0; k < live; ++k) {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]);
+          c->stats.step_kernel_ms += ms;
+          c->stats.step_kernel_timed++;
+        }
+      }
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
+  } else {
+    for (int q = 0; q < max_steps; ++q) {
+      const int per = record_chunk(1);
+      if (per < 0) return cuda_fail(c, e, "step launch");
+      launches += per;
+      if (prof) {
+        cudaEventSynchronize(c->ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        c->stats.step_kernel_ms += ms;
+        c->stats.step_kernel_timed++;
+      }
+    }
+  }
+  // Point updates actually performed (inactive shots skip their tiles).
+  uint64_t upd = 0;
+  for (auto &S : hs) upd += (uint64_t)S.npts * (uint64_t)S.nsteps;
+  c->stats.points_updated += upd;
+  c->stats.launches_total += launches;
+  c->stats.launches_step += (uint64_t)max_steps;
+  if (prof) {
+    // Algorithmic bytes: 24 B per point update (u2, u1, u0, u_1, vel read,
+    // u3 written) plus, on snapshot steps, 4 B per physical point for a
+    // saved snapshot and the imaging traffic (RTM/LSRTM: snapshot read +
+    // image and illumination read-modify-write = 20 B; AFWI: two more
+    // snapshot reads = 28 B; Born source: snapshot + reflectivity = 8 B).
+    uint64_t extra = 0;
+    for (auto &S : hs) {
+      const uint64_t nph = (uint64_t)S.g.nz * S.g.nx * S.g.ny;
+      uint64_t nsnap = 0;
+      for (int q = 0; q < S.nsteps; ++q) {
+        const int it = S.tmin + q * S.tstep;
+        if (it % S.snapi == 0) ++nsnap;
+      }
+      nsnap = std::min<uint64_t>(nsnap, (uint64_t)S.ntsnap);
+      uint64_t per = S.extract_wave ? 4 : 0;
+      if (S.imaging == SW_IMG_RTM || S.imaging == SW_IMG_LSRTM) per += 20;
+      if (S.imaging == SW_IMG_AFWI) per += 28;
+      if (S.imaging == SW_IMG_BORN) per += 8;
+      extra += nsnap * nph * per;
+    }
+    c->stats.step_bytes += upd * 24ull + extra;
+  }
+  // ---- outputs ----
+  for (int b = 0; b < nb; ++b) {
+    if (!shots[b].io.final_u2_host) continue;
+    const int last = hs[b].nsteps;   // u2 after the last step = f[(last+3)%5]
+    const float *u2 = hs[b].f[(last + 3) % 5];
+    e = cudaMemcpy2DAsync(shots[b].io.final_u2_host, (size_t)G[b].n1p * sizeof(float), u2,
+                          (size_t)G[b].ld1 * sizeof(float), (size_t)G[b].n1p * sizeof(float),
+                          (size_t)G[b].n2p * G[b].n3p, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return cuda_fail(c, e, "download u2");
+  }
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch run");
+  return SW_OK;
+}
+
+}  // namespace swave

@@ -48,68 +48,12 @@ struct InjEntry {
   float v2r, wz, wx, wy;
 };
 
-// Arguments of the fused step kernel.
-struct StepArgs {
-  Geom g;
-  Coefs c;
-  const float *u2, *u1, *u0, *um1;
-  float *u3;
-  const float *vel;      // padded velocity
-  const float *lap_src;  // 3D adjoint: v^2*u2 (padded); else == u2
-  float k12;             // 12*dt^2
-  float div11;           // 1/11
-  // injection box [bi0..bi1]x[bj0..bj1]x[bk0..bk1] with dense CSR offsets
-  int inj_on;
-  int bi0, bi1, bj0, bj1, bk0, bk1;
-  const int *inj_off;
-  const InjEntry *inj_ent;
-  const float *src_tr;   // nsrc*nt, trace-major
-  int it, nt;
-  // Born secondary source: u3 += (((2*taper)*ref)*w)/vel
-  int born_on;
-  const float *ref;      // physical nz*nx*ny
-  const float *taperx, *tapery;
-  // snapshot of u2 into a dense nz*nx*ny slot
-  int snap_on;
-  float *snap_out;
-  // imaging on u2 (tstep = -1): 1 RTM, 2 LSRTM, 3 AFWI
-  int img;
-  const float *w0, *wm1, *wp1;
-  float *image, *illum;
-  float dt2snap;
-};
-
-// Arguments of the receiver-extraction kernel.
-struct ExtArgs {
-  Geom g;
-  int nrec, nt, it, half, mode;   // mode: sw_extraction
-  const int *ic;                  // 3*nrec Fortran indices
-  const float *wz, *wx;           // lsinc*nrec sinc weights
-  const float *u2, *vel;
-  float vconst;                   // LSRTM / afwi constant factor
-  float *tr;                      // nrec*nt
-};
-
-// Higdon coefficient arrays, coefficient-major for coalesced reads:
-// gz[c][k][j], gx[c][k][i], gy[c][j][i] with c = 0..15.
-struct HigArgs {
-  Geom g;
-  const float *gz, *gx, *gy;
-  float *u3;
-  const float *u2, *u1;
-};
-
 // Launchers (kernels.cu).
 cudaError_t launch_pad_velocity(const Geom &g, const float *vel_phys, float *vel_pad,
                                 cudaStream_t s);
 cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
                                  float dyi, float dzi, float *gz, float *gx, float *gy,
                                  cudaStream_t s);
-cudaError_t launch_step(const StepArgs &a, int adjoint2d, cudaStream_t s);
-cudaError_t launch_v2u(const Geom &g, const float *vel, const float *u2, float *out,
-                       cudaStream_t s);
-cudaError_t launch_higdon(const HigArgs &a, cudaStream_t s, int *nlaunch);
-cudaError_t launch_extract(const ExtArgs &a, cudaStream_t s);
 
 // FWI helpers (kernels.cu).
 cudaError_t launch_window_vel(int nz, int nx, int ny, float ox, float oy, float dx, float dy,
