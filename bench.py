@@ -255,14 +255,21 @@ def main():
     # Shots of this rank: rank r takes every ws-th shot of the survey.
     mine = shots[rank::ws]
     per_step = [mine[(k * B + q) % len(mine)] for k in range(nsteps) for q in range(B)]
-    # Observed data: modelled on each shot's window (untimed setup).
+    # Observed data: batched forward modelling on each shot's window (untimed).
     distinct = {}
     t0 = time.perf_counter()
+    uniq = []
     for s in per_step:
         key = float(s["sou"][1])
         if key not in distinct:
-            distinct[key] = model_data(ctx, g, vel, w, s)
-    log(f"[rank {rank}] modelled {len(distinct)} shots in {time.perf_counter() - t0:.1f}s")
+            distinct[key] = None
+            uniq.append(s)
+    mj = sw.RTMJob(ctx, g, vel, w, [{"sou": s["sou"], "rec": s["rec"], "nt": s["nt"]} for s in uniq])
+    mj.set_batch(B)
+    for s, d in zip(uniq, mj.model()):
+        distinct[float(s["sou"][1])] = d
+    mj.close()
+    log(f"[rank {rank}] modelled {len(uniq)} shots in {time.perf_counter() - t0:.1f}s")
     job_shots = [{"sou": s["sou"], "rec": s["rec"], "data": distinct[float(s["sou"][1])]}
                  for s in per_step]
     job = sw.RTMJob(ctx, g, vel, w, job_shots)

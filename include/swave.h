@@ -208,8 +208,15 @@ int sw_rtm_job_create(sw_ctx *ctx, const sw_genpar *model, float aperture_x,
 /* Admission: at most max_shots per batch and at most mem_fraction of the
  * free device memory (defaults 64 and 0.85). */
 int sw_rtm_job_set_batch(sw_rtm_job *job, int max_shots, double mem_fraction);
-/* Migrates shots [first, first+count) and adds them to the job's image. */
+/* Migrates shots [first, first+count) and adds them to the job's image.
+ * Every migrated shot needs observed data. */
 int sw_rtm_job_run(sw_rtm_job *job, int first, int count);
+/* Forward modelling of shots [first, first+count), batched like the RTM:
+ * Injection_sinc of the wavelet and Extraction_array_sinc at the receivers
+ * (progs/modeling/Acoustic_modeling.f90:115-123) on each shot's window.
+ * data[q] receives the nrec*nt traces of shot first+q.  Shots may have been
+ * created without observed data (sw_shot.data = NULL). */
+int sw_rtm_job_model(sw_rtm_job *job, int first, int count, float *const *data);
 /* Shots per batch used by the last run, and compute-domain point updates. */
 int sw_rtm_job_info(const sw_rtm_job *job, int *last_batch, uint64_t *points);
 /* image, illum: stacked nz*nx*ny sums; image_norm: image divided by the
@@ -263,6 +270,18 @@ int sw_lbfgs_step(sw_lbfgs *s, double *x, double f, const double *g,
                   double eps, double xtol, int *iflag, int *myinfo);
 /* Scalars of the last step: [iter, nfun, stp, gnorm, ys, yy, dginit, dg]. */
 int sw_lbfgs_diag(const sw_lbfgs *s, double *out8);
+
+/* ---- Tuning (no counterpart in the reference: launch shape knobs) -------- */
+typedef struct sw_tuning {
+  int step_kernel;   /* fused step: 0 = 32x8 point tiles, 1 = streaming, 2 = shared-memory tiles (2D; 3D uses streaming) */
+  int tile_z;        /* 2D streaming kernel: rows per CTA (32, 64 or 128)     */
+  int tile_x;        /* 2D streaming kernel: columns walked per CTA (>= 1)    */
+  int tile_y;        /* 3D streaming kernel: y planes marched per CTA (>= 1)  */
+  int graph_chunk;   /* time steps per captured CUDA graph (>= 1)             */
+  int use_graph;     /* 0: launch every step directly                         */
+} sw_tuning;
+int sw_ctx_set_tuning(sw_ctx *ctx, const sw_tuning *t);
+int sw_ctx_get_tuning(const sw_ctx *ctx, sw_tuning *t);
 
 /* ---- Instrumentation ----------------------------------------------------- */
 typedef struct sw_stats {

@@ -133,53 +133,71 @@ template <class T> static Coefs<T> make_coefs(const sw_genpar &g) {
 // ---------------------------------------------------------------------------
 
 // FD_2nd_2D_derivatives_scalar_forward_grid (FDderivatives.f90:715-743).
+// Column pointers keep the inner z loop vectorisable; the per-point
+// operation order is the Fortran one.
 template <class T>
 static void stencil2d_fwd(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
                           F3<T> &u3, const F3<T> &vel) {
+  const long L = u2.n1;
 #pragma omp parallel for schedule(static)
-  for (int j = b.nmin2; j <= b.nmax2; ++j)
-    for (int i = b.nmin1; i <= b.nmax1; ++i) {
-      T tz = c.c0z * u2(i, j, 1);
-      tz = tz + c.c1z * (u2(i + 1, j, 1) + u2(i - 1, j, 1));
-      tz = tz + c.c2z * (u2(i + 2, j, 1) + u2(i - 2, j, 1));
-      tz = tz + c.c3z * (u2(i + 3, j, 1) + u2(i - 3, j, 1));
-      tz = tz + c.c4z * (u2(i + 4, j, 1) + u2(i - 4, j, 1));
-      T tx = c.c0x * u2(i, j, 1);
-      tx = tx + c.c1x * (u2(i, j + 1, 1) + u2(i, j - 1, 1));
-      tx = tx + c.c2x * (u2(i, j + 2, 1) + u2(i, j - 2, 1));
-      tx = tx + c.c3x * (u2(i, j + 3, 1) + u2(i, j - 3, 1));
-      tx = tx + c.c4x * (u2(i, j + 4, 1) + u2(i, j - 4, 1));
-      const T v = vel(i, j, 1);
-      u3(i, j, 1) = (v * v) * (tx + tz);
+  for (int j = b.nmin2; j <= b.nmax2; ++j) {
+    const T *u = &u2.v[(size_t)(b.nmin1 - u2.lo1) + (size_t)u2.n1 * (size_t)(j - u2.lo2)];
+    const T *v = &vel.v[(size_t)(b.nmin1 - vel.lo1) + (size_t)vel.n1 * (size_t)(j - vel.lo2)];
+    T *o = &u3.v[(size_t)(b.nmin1 - u3.lo1) + (size_t)u3.n1 * (size_t)(j - u3.lo2)];
+    const int n = b.nmax1 - b.nmin1 + 1;
+#pragma omp simd
+    for (int q = 0; q < n; ++q) {
+      T tz = c.c0z * u[q];
+      tz = tz + c.c1z * (u[q + 1] + u[q - 1]);
+      tz = tz + c.c2z * (u[q + 2] + u[q - 2]);
+      tz = tz + c.c3z * (u[q + 3] + u[q - 3]);
+      tz = tz + c.c4z * (u[q + 4] + u[q - 4]);
+      T tx = c.c0x * u[q];
+      tx = tx + c.c1x * (u[q + L] + u[q - L]);
+      tx = tx + c.c2x * (u[q + 2 * L] + u[q - 2 * L]);
+      tx = tx + c.c3x * (u[q + 3 * L] + u[q - 3 * L]);
+      tx = tx + c.c4x * (u[q + 4 * L] + u[q - 4 * L]);
+      const T vv = v[q];
+      o[q] = (vv * vv) * (tx + tz);
     }
+  }
 }
 
 // FD_2nd_3D_derivatives_scalar_forward_grid (FDderivatives.f90:97-131).
 template <class T>
 static void stencil3d_fwd(const Coefs<T> &c, const Bounds &b, const F3<T> &u2,
                           F3<T> &u3, const F3<T> &vel) {
-#pragma omp parallel for schedule(static)
+  const long L = u2.n1, P = (long)u2.n1 * u2.n2;
+#pragma omp parallel for schedule(static) collapse(2)
   for (int k = b.nmin3; k <= b.nmax3; ++k)
-    for (int j = b.nmin2; j <= b.nmax2; ++j)
-      for (int i = b.nmin1; i <= b.nmax1; ++i) {
-        T tz = c.c0z * u2(i, j, k);
-        tz = tz + c.c1z * (u2(i + 1, j, k) + u2(i - 1, j, k));
-        tz = tz + c.c2z * (u2(i + 2, j, k) + u2(i - 2, j, k));
-        tz = tz + c.c3z * (u2(i + 3, j, k) + u2(i - 3, j, k));
-        tz = tz + c.c4z * (u2(i + 4, j, k) + u2(i - 4, j, k));
-        T tx = c.c0x * u2(i, j, k);
-        tx = tx + c.c1x * (u2(i, j + 1, k) + u2(i, j - 1, k));
-        tx = tx + c.c2x * (u2(i, j + 2, k) + u2(i, j - 2, k));
-        tx = tx + c.c3x * (u2(i, j + 3, k) + u2(i, j - 3, k));
-        tx = tx + c.c4x * (u2(i, j + 4, k) + u2(i, j - 4, k));
-        T ty = c.c0y * u2(i, j, k);
-        ty = ty + c.c1y * (u2(i, j, k + 1) + u2(i, j, k - 1));
-        ty = ty + c.c2y * (u2(i, j, k + 2) + u2(i, j, k - 2));
-        ty = ty + c.c3y * (u2(i, j, k + 3) + u2(i, j, k - 3));
-        ty = ty + c.c4y * (u2(i, j, k + 4) + u2(i, j, k - 4));
-        const T v = vel(i, j, k);
-        u3(i, j, k) = (v * v) * ((tx + tz) + ty);
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      const size_t off = (size_t)(b.nmin1 - u2.lo1) +
+                         (size_t)u2.n1 * ((size_t)(j - u2.lo2) + (size_t)u2.n2 * (size_t)(k - u2.lo3));
+      const T *u = &u2.v[off];
+      const T *v = &vel.v[off];
+      T *o = &u3.v[off];
+      const int n = b.nmax1 - b.nmin1 + 1;
+#pragma omp simd
+      for (int q = 0; q < n; ++q) {
+        T tz = c.c0z * u[q];
+        tz = tz + c.c1z * (u[q + 1] + u[q - 1]);
+        tz = tz + c.c2z * (u[q + 2] + u[q - 2]);
+        tz = tz + c.c3z * (u[q + 3] + u[q - 3]);
+        tz = tz + c.c4z * (u[q + 4] + u[q - 4]);
+        T tx = c.c0x * u[q];
+        tx = tx + c.c1x * (u[q + L] + u[q - L]);
+        tx = tx + c.c2x * (u[q + 2 * L] + u[q - 2 * L]);
+        tx = tx + c.c3x * (u[q + 3 * L] + u[q - 3 * L]);
+        tx = tx + c.c4x * (u[q + 4 * L] + u[q - 4 * L]);
+        T ty = c.c0y * u[q];
+        ty = ty + c.c1y * (u[q + P] + u[q - P]);
+        ty = ty + c.c2y * (u[q + 2 * P] + u[q - 2 * P]);
+        ty = ty + c.c3y * (u[q + 3 * P] + u[q - 3 * P]);
+        ty = ty + c.c4y * (u[q + 4 * P] + u[q - 4 * P]);
+        const T vv = v[q];
+        o[q] = (vv * vv) * ((tx + tz) + ty);
       }
+    }
 }
 
 // FD_2nd_2D_derivatives_scalar_adjoint_grid (FDderivatives.f90:847-891):
@@ -261,17 +279,24 @@ static void time_update(const Bounds &b, T dt, const F3<T> &u2, const F3<T> &u1,
   const T div11 = T(1.) / T(11);
   const T dt2 = dt * dt;
   const T k12 = T(12.) * dt2;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) collapse(2)
   for (int k = b.nmin3; k <= b.nmax3; ++k)
-    for (int j = b.nmin2; j <= b.nmax2; ++j)
-      for (int i = b.nmin1; i <= b.nmax1; ++i) {
-        T a = T(20.) * u2(i, j, k);
-        a = a - T(6.) * u1(i, j, k);
-        a = a - T(4.) * u0(i, j, k);
-        a = a + um1(i, j, k);
-        a = a + k12 * u3(i, j, k);
-        u3(i, j, k) = a * div11;
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      const size_t off = (size_t)(b.nmin1 - u2.lo1) +
+                         (size_t)u2.n1 * ((size_t)(j - u2.lo2) + (size_t)u2.n2 * (size_t)(k - u2.lo3));
+      const T *a2 = &u2.v[off], *a1 = &u1.v[off], *a0 = &u0.v[off], *am = &um1.v[off];
+      T *o = &u3.v[off];
+      const int n = b.nmax1 - b.nmin1 + 1;
+#pragma omp simd
+      for (int q = 0; q < n; ++q) {
+        T a = T(20.) * a2[q];
+        a = a - T(6.) * a1[q];
+        a = a - T(4.) * a0[q];
+        a = a + am[q];
+        a = a + k12 * o[q];
+        o[q] = a * div11;
       }
+    }
 }
 
 // ---------------------------------------------------------------------------

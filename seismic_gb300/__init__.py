@@ -73,6 +73,11 @@ class SwShot(C.Structure):
                 ("data", _fp), ("nt", C.c_int)]
 
 
+class SwTuning(C.Structure):
+    _fields_ = [("step_kernel", C.c_int), ("tile_z", C.c_int), ("tile_x", C.c_int),
+                ("tile_y", C.c_int), ("graph_chunk", C.c_int), ("use_graph", C.c_int)]
+
+
 class SwStats(C.Structure):
     _fields_ = [("launches_total", C.c_uint64), ("launches_step", C.c_uint64),
                 ("points_updated", C.c_uint64), ("step_kernel_ms", C.c_double),
@@ -104,10 +109,13 @@ _SIGS = {
                                     _fp, C.c_int, C.POINTER(SwShot), C.POINTER(C.c_void_p)]),
     "sw_rtm_job_set_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "sw_rtm_job_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "sw_rtm_job_model": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_fp)]),
     "sw_rtm_job_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "sw_rtm_job_result": (C.c_int, [C.c_void_p, _fp, _fp, _fp]),
     "sw_rtm_job_reset": (C.c_int, [C.c_void_p]),
     "sw_rtm_job_destroy": (C.c_int, [C.c_void_p]),
+    "sw_ctx_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(SwTuning)]),
+    "sw_ctx_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(SwTuning)]),
     "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
     "sw_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
@@ -213,6 +221,17 @@ class Context:
     def reset_stats(self):
         self._check(self.lib.sw_ctx_reset_stats(self.h))
 
+    def tuning(self) -> dict:
+        t = SwTuning()
+        self._check(self.lib.sw_ctx_get_tuning(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in SwTuning._fields_}
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = SwTuning(**cur)
+        self._check(self.lib.sw_ctx_set_tuning(self.h, C.byref(t)))
+
     def set_profiling(self, on: bool):
         self._check(self.lib.sw_ctx_set_profiling(self.h, int(bool(on))))
 
@@ -305,12 +324,13 @@ def make_shots(shots) -> tuple:
     arr = (SwShot * len(shots))()
     keep = []
     for i, s in enumerate(shots):
-        rc, d = _f32(s["rec"]), _f32(s["data"])
+        rc = _f32(s["rec"])
+        d = _f32(s["data"]) if s.get("data") is not None else None
         keep += [rc, d]
         arr[i].sou_coord[:] = [float(v) for v in s["sou"]]
         arr[i].nrec = rc.size // 3
         arr[i].rec_coord, arr[i].data = fptr(rc), fptr(d)
-        arr[i].nt = int(d.shape[-1]) if d.ndim == 2 else int(s["nt"])
+        arr[i].nt = int(d.shape[-1]) if d is not None and d.ndim == 2 else int(s["nt"])
     return arr, keep
 
 
@@ -328,6 +348,16 @@ class RTMJob:
                                              fptr(v), fptr(w), len(shots), arr, C.byref(h)))
         self.h = h
         self.nshot = len(shots)
+        self._nrec = [np.asarray(x["rec"]).size // 3 for x in shots]
+        self._nt = [int(arr[i].nt) for i in range(len(shots))]
+
+    def model(self, first: int = 0, count: int | None = None) -> list:
+        """Batched forward modelling of shots [first, first+count)."""
+        count = self.nshot - first if count is None else count
+        outs = [np.zeros((self._nrec[q], self._nt[q]), np.float32) for q in range(first, first + count)]
+        ptrs = (_fp * count)(*[fptr(o) for o in outs])
+        self.ctx._check(self.ctx.lib.sw_rtm_job_model(self.h, first, count, ptrs))
+        return outs
 
     def set_batch(self, max_shots: int, mem_fraction: float = 0.85):
         self.ctx._check(self.ctx.lib.sw_rtm_job_set_batch(self.h, max_shots, mem_fraction))

@@ -1,0 +1,130 @@
+"""Autotuner for the fused step kernel's launch shape and the graph chunk.
+
+Candidates are timed on a truncated copy of the real batch (same windows,
+same number of shots in flight, a few dozen time steps of both the forward
+and the backward phase); the fastest is cached per (device, padded-grid
+bucket, shots per batch) in a JSON file under the user's cache directory.
+Timing is injected so that the selection logic can be exercised without a
+GPU.
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+from typing import Callable, Iterable
+
+DEFAULT_CACHE = os.path.join(os.environ.get("XDG_CACHE_HOME", os.path.expanduser("~/.cache")),
+                             "seismic_gb300", "tuning.json")
+
+
+def candidates(two_d: bool = True) -> list[dict]:
+    out = []
+    for chunk in (16, 32):
+        out.append({"step_kernel": 0, "tile_z": 64, "tile_x": 64, "tile_y": 32,
+                    "graph_chunk": chunk, "use_graph": 1})
+        if two_d:
+            for tz in (32, 64, 128):
+                for tx in (32, 64, 128, 256):
+                    out.append({"step_kernel": 1, "tile_z": tz, "tile_x": tx, "tile_y": 32,
+                                "graph_chunk": chunk, "use_graph": 1})
+        else:
+            for ty in (8, 16, 32, 64):
+                out.append({"step_kernel": 1, "tile_z": 64, "tile_x": 64, "tile_y": ty,
+                            "graph_chunk": chunk, "use_graph": 1})
+    return out
+
+
+def bucket(n: int, step: int = 64) -> int:
+    return (n + step - 1) // step * step
+
+
+def cache_key(device: str, n1p: int, n2p: int, n3p: int, batch: int) -> str:
+    return f"{device}|{bucket(n1p)}x{bucket(n2p)}x{bucket(n3p, 8)}|b{batch}"
+
+
+def load_cache(path: str = DEFAULT_CACHE) -> dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def save_cache(cache: dict, path: str = DEFAULT_CACHE) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def select(cands: Iterable[dict], time_fn: Callable[[dict], float], repeats: int = 2) -> tuple[dict, list]:
+    """Returns the candidate with the smallest best-of-`repeats` time."""
+    results = []
+    for c in cands:
+        try:
+            t = min(time_fn(c) for _ in range(repeats))
+        except Exception as e:  # a candidate the device rejects is skipped
+            results.append((c, float("inf"), repr(e)))
+            continue
+        results.append((c, t, None))
+    ok = [r for r in results if r[1] != float("inf")]
+    if not ok:
+        raise RuntimeError("no tuning candidate ran: " + "; ".join(str(r[2]) for r in results))
+    best = min(ok, key=lambda r: r[1])
+    return best[0], results
+
+
+def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | None = None,
+             cache_path: str | None = DEFAULT_CACHE, device_name: str | None = None,
+             force: bool = False) -> dict:
+    """Tunes ctx for the RTM job of `shots` and applies the winner."""
+    import numpy as np
+
+    import seismic_gb300 as sw
+    batch = batch or len(shots)
+    sample = [{"sou": s["sou"], "rec": s["rec"],
+               "data": np.ascontiguousarray(np.asarray(s["data"])[:, :steps])} for s in shots[:batch]]
+    g = sw.SwGenpar.from_buffer_copy(model)
+    g.nt = steps
+    n1p = g.nz + 2 * g.ntaper + 8
+    widths = [int(np.ptp(np.asarray(s["rec"])[:, 1]) / g.dx) + 1 for s in sample]
+    n2p = max(widths) + 2 * g.ntaper + 8
+    n3p = 1 if g.twoD else g.ny + 2 * g.ntaper + 8
+    if device_name is None:
+        try:
+            import torch
+            device_name = torch.cuda.get_device_name(ctx_device(ctx))
+        except Exception:
+            device_name = "cuda"
+    key = cache_key(device_name, n1p, n2p, n3p, batch)
+    cache = load_cache(cache_path) if cache_path else {}
+    if key in cache and not force:
+        ctx.set_tuning(**cache[key]["tuning"])
+        return cache[key]
+    job = sw.RTMJob(ctx, g, vel, wavelet[:steps], sample)
+    job.set_batch(batch)
+
+    def time_fn(c):
+        ctx.set_tuning(**c)
+        job.run(0, len(sample))          # warm (graph capture, arena)
+        t0 = time.perf_counter()
+        job.run(0, len(sample))
+        return time.perf_counter() - t0
+
+    try:
+        best, results = select(candidates(bool(g.twoD)), time_fn)
+    finally:
+        job.close()
+    ctx.set_tuning(**best)
+    entry = {"tuning": best, "seconds": min(r[1] for r in results),
+             "tried": len(results), "steps": steps}
+    if cache_path:
+        cache[key] = entry
+        save_cache(cache, cache_path)
+    return entry
+
+
+def ctx_device(ctx) -> int:
+    return 0

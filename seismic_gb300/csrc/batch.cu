@@ -4,7 +4,12 @@
 // comes from a device counter so that the launches of all steps are
 // identical and graph-capturable.  The arithmetic restates the reference
 // loops in their evaluation order (file:line cited at each kernel).
+#include <algorithm>
+
 #include "batch.cuh"
+#include "stream2d.cuh"
+#include "stream3d.cuh"
+#include "tile2d.cuh"
 
 namespace swave {
 
@@ -364,14 +369,74 @@ __global__ void k_bhiggy(BatchTables t, int s_off) {
   }
 }
 
+// Streaming 2D step (stream2d.cuh); the shot's stencil variant is uniform
+// over the CTA.
+// Streaming 2D step (stream2d.cuh): one kernel per stencil variant; a CTA
+// whose shot uses the other variant exits at once.
+template <int TZ, bool ADJ>
+__global__ void __launch_bounds__(TZ, 1024 / TZ) k_bstep2d_s(BatchTables t, int s_off, int tx) {
+  const int b = find_shot(t.step_tiles, t.nshots, blockIdx.x);
+  if ((t.shots[b].adj2d != 0) != ADJ) return;
+  stream2d_body<TZ, ADJ>(t, s_off, b, blockIdx.x - t.step_tiles[b], tx);
+}
+
+template <int TZ>
+static void launch_stream2d(const BatchTables &t, int s_off, int n, const StepTile &tile,
+                            int has_fwd, int has_adj, cudaStream_t s, int *nl) {
+  if (has_fwd) {
+    k_bstep2d_s<TZ, false><<<n, TZ, 0, s>>>(t, s_off, tile.tx);
+    ++*nl;
+  }
+  if (has_adj) {
+    k_bstep2d_s<TZ, true><<<n, TZ, 0, s>>>(t, s_off, tile.tx);
+    ++*nl;
+  }
+}
+
+// Persistent pipelined 2D step (tile2d.cuh), one kernel per stencil variant.
+template <bool ADJ>
+__global__ void __launch_bounds__(256, 2) k_bstep2d_t(BatchTables t, int s_off, int n_tiles) {
+  tile2d_persistent<ADJ>(t, s_off, n_tiles);
+}
+
+template <bool ADJ>
+static cudaError_t launch_tile2d(const BatchTables &t, int s_off, int n_tiles, int nsm,
+                                 cudaStream_t s) {
+  // The shared-memory opt-in is a per-device function attribute.
+  static unsigned long long attr_set = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !(attr_set & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_bstep2d_t<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t2_smem_bytes<ADJ>());
+    if (e != cudaSuccess) return e;
+    if (dev < 64) attr_set |= 1ull << dev;
+  }
+  // Two resident CTAs per SM; more CTAs only when a CTA's tile list would
+  // overflow its shared-memory copy.
+  const int grid = std::max({1, std::min(n_tiles, 2 * nsm),
+                             (n_tiles + T2_MAX_TILES_PER_CTA - 1) / T2_MAX_TILES_PER_CTA});
+  k_bstep2d_t<ADJ><<<grid, 256, t2_smem_bytes<ADJ>(), s>>>(t, s_off, n_tiles);
+  return cudaGetLastError();
+}
+
+// Streaming 3D step (stream3d.cuh), one kernel per stencil variant.
+template <bool ADJ>
+__global__ void __launch_bounds__(256, 4) k_bstep3d_s(BatchTables t, int s_off, int ty) {
+  const int b = find_shot(t.step_tiles, t.nshots, blockIdx.x);
+  if ((t.shots[b].adj3d != 0) != ADJ) return;
+  stream3d_body<ADJ>(t, s_off, b, blockIdx.x - t.step_tiles[b], ty);
+}
+
 __global__ void k_counter_add(int *counter, int add) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *counter += add;
 }
 
 cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
                               int n_hz, int n_hx, int n_hy, int n_v2u, int has_ext, int has_3d,
-                              int has_adj3d, cudaStream_t s, int *nlaunch,
-                              cudaEvent_t ev_before, cudaEvent_t ev_after) {
+                              int has_adj3d, const StepTile &tile, cudaStream_t s,
+                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after) {
   int nl = 0;
   // Every kernel of the step reads s = *counter + s_off; the counter is
   // advanced once per chunk of steps.
@@ -379,16 +444,48 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     k_bextract<<<(n_rec + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   }
-  if (has_adj3d && n_v2u > 0) {
+  if (has_adj3d && n_v2u > 0 && !tile.stream3d) {
     k_bv2u<<<n_v2u, 256, 0, s>>>(t, s_off);
     ++nl;
   }
   dim3 bs(32, 8, 1);
-  if (ev_before) cudaEventRecord(ev_before, s);
-  if (has_3d) k_bstep<false><<<n_step_tiles, bs, 0, s>>>(t, s_off);
-  else k_bstep<true><<<n_step_tiles, bs, 0, s>>>(t, s_off);
-  ++nl;
-  if (ev_after) cudaEventRecord(ev_after, s);
+  // External record nodes: a plain record inside stream capture only adds a
+  // dependency and would never timestamp the event at graph replay.
+  if (ev_before) cudaEventRecordWithFlags(ev_before, s, cudaEventRecordExternal);
+  if (has_3d && tile.stream3d) {
+    dim3 b3(S3_BZ, S3_BY, 1);
+    if (tile.has_fwd3d) {
+      k_bstep3d_s<false><<<n_step_tiles, b3, 0, s>>>(t, s_off, tile.ty);
+      ++nl;
+    }
+    if (tile.has_adj3d) {
+      k_bstep3d_s<true><<<n_step_tiles, b3, 0, s>>>(t, s_off, tile.ty);
+      ++nl;
+    }
+  } else if (has_3d) {
+    k_bstep<false><<<n_step_tiles, bs, 0, s>>>(t, s_off);
+    ++nl;
+  } else if (tile.stream2d == 2) {
+    cudaError_t e = cudaSuccess;
+    if (tile.has_fwd2d) {
+      e = launch_tile2d<false>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e == cudaSuccess && tile.has_adj2d) {
+      e = launch_tile2d<true>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e != cudaSuccess) return e;
+  } else if (tile.stream2d) {
+    const int hf = tile.has_fwd2d, ha = tile.has_adj2d;
+    if (tile.tz == 128) launch_stream2d<128>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
+    else if (tile.tz == 32) launch_stream2d<32>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
+    else launch_stream2d<64>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
+  } else {
+    k_bstep<true><<<n_step_tiles, bs, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (ev_after) cudaEventRecordWithFlags(ev_after, s, cudaEventRecordExternal);
   k_bhiggz<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
   k_bhiggx<<<(n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
   nl += 2;

@@ -44,6 +44,19 @@ struct ShotDev {
   long long npts;         // compute-domain points
 };
 
+// Compact per-shot view used by the pipelined 2D kernel; the kernel keeps the
+// whole array in shared memory.
+struct T2Shot {
+  const float *f[5];
+  const float *vel;
+  float c0z, c1z, c2z, c3z, c4z, c0x, c1x, c2x, c3x, c4x, k12, div11;
+  int ld1, lo2, n2p, nmin1, nmax1, nmin2, nmax2, nz, nx;
+  int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
+};
+
+// Largest batch the pipelined 2D kernel accepts (its shot table is shared).
+constexpr int T2_MAX_SHOTS = 64;
+
 // Prefix tables of a batch (device resident).
 struct BatchTables {
   int nshots;
@@ -54,16 +67,44 @@ struct BatchTables {
   const int *hx_start;    // nshots+1: x-edge lines (n1*n3)
   const int *hy_start;    // nshots+1: y-edge lines (n1*n2, 3D)
   const int *v2u_blocks;  // nshots+1: blocks of the v^2*u2 pass
+  const T2Shot *t2shots;  // nshots compact views (pipelined 2D kernel)
+  const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
   int *counter;           // step counter s (0-based)
 };
 
 // Launches one full time step of the batch (extract, [v2u], fused step,
 // Higdon z/x/[y]) for step s = *counter + s_off.
+// Tile shape of the fused step kernel.  2D: stream2d = 1 selects the
+// streaming kernel with TZ = tz rows per CTA (32, 64 or 128) walking tx
+// columns; otherwise 32x8 point tiles.  3D: 32x8 point tiles per plane.
+struct StepTile {
+  int stream2d = 2;    // 2D: 0 point tiles, 1 streaming (stream2d.cuh), 2 tiled (tile2d.cuh)
+  int tz = 64;
+  int tx = 64;
+  int stream3d = 1;    // 3D: 2.5D streaming kernel (stream3d.cuh)
+  int ty = 32;         // 3D: y planes marched per CTA
+  int has_fwd2d = 1;   // set by the runner from the batch's stencil variants
+  int has_adj2d = 1;
+  int has_fwd3d = 1;
+  int has_adj3d = 1;
+  int nsm = 152;       // SMs of the device (persistent grids)
+};
+
+// Number of fused-step CTAs a shot needs with this tile shape.
+inline int step_ctas(const Geom &g, const StepTile &tile) {
+  const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  if (g.twoD && tile.stream2d == 2) return ((n1 + 63) / 64) * ((n2 + 31) / 32);
+  if (g.twoD && tile.stream2d) return ((n1 + tile.tz - 1) / tile.tz) * ((n2 + tile.tx - 1) / tile.tx);
+  if (!g.twoD && tile.stream3d)
+    return ((n1 + 31) / 32) * ((n2 + 15) / 16) * ((n3 + tile.ty - 1) / tile.ty);
+  return ((n1 + 31) / 32) * ((n2 + 7) / 8) * n3;
+}
+
 // ev_before / ev_after (may be null) bracket the fused step kernel.
 cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
                               int n_hz, int n_hx, int n_hy, int n_v2u, int has_ext, int has_3d,
-                              int has_adj3d, cudaStream_t s, int *nlaunch,
-                              cudaEvent_t ev_before, cudaEvent_t ev_after);
+                              int has_adj3d, const StepTile &tile, cudaStream_t s,
+                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after);
 cudaError_t launch_counter_add(int *counter, int add, cudaStream_t s);
 
 }  // namespace swave

@@ -67,6 +67,33 @@ int sw_ctx_reset_stats(sw_ctx *c) {
   std::memset(&c->stats, 0, sizeof(c->stats));
   return SW_OK;
 }
+int sw_ctx_set_tuning(sw_ctx *c, const sw_tuning *t) {
+  if (!c || !t) return SW_BAD_PARAM;
+  if (t->step_kernel < 0 || t->step_kernel > 2 || t->graph_chunk < 1 || t->tile_x < 1 ||
+      t->tile_y < 1 ||
+      (t->tile_z != 32 && t->tile_z != 64 && t->tile_z != 128))
+    return swave::fail(c, SW_BAD_PARAM, "invalid tuning");
+  c->run_opts.tile.stream2d = t->step_kernel;
+  c->run_opts.tile.stream3d = t->step_kernel != 0;
+  c->run_opts.tile.ty = t->tile_y;
+  c->run_opts.tile.tz = t->tile_z;
+  c->run_opts.tile.tx = t->tile_x;
+  c->run_opts.chunk = t->graph_chunk;
+  c->run_opts.use_graph = t->use_graph != 0;
+  return SW_OK;
+}
+
+int sw_ctx_get_tuning(const sw_ctx *c, sw_tuning *t) {
+  if (!c || !t) return SW_BAD_PARAM;
+  t->step_kernel = c->run_opts.tile.stream2d;
+  t->tile_z = c->run_opts.tile.tz;
+  t->tile_x = c->run_opts.tile.tx;
+  t->tile_y = c->run_opts.tile.ty;
+  t->graph_chunk = c->run_opts.chunk;
+  t->use_graph = c->run_opts.use_graph ? 1 : 0;
+  return SW_OK;
+}
+
 int sw_ctx_set_profiling(sw_ctx *c, int on) {
   if (!c) return SW_BAD_PARAM;
   c->profiling = on != 0;

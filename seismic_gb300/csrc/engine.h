@@ -13,9 +13,12 @@ struct DBuf {
   size_t cap = 0;
 };
 
+#include "batch.cuh"
+
 struct RunOpts {
   int chunk = 16;       // steps per captured graph
   bool use_graph = true;
+  swave::StepTile tile; // fused-step tile shape
 };
 
 struct sw_ctx {
@@ -77,6 +80,17 @@ struct PhaseShot {
 };
 
 int fail(sw_ctx *c, int code, const char *fmt, ...);
+
+#define SW_STR2(x) #x
+#define SW_STR(x) SW_STR2(x)
+// Returns SW_CUDA_ERR from the enclosing function (which has `sw_ctx *c`)
+// when a CUDA runtime call fails, naming the call site.
+#define SW_CK(call)                                                              \
+  do {                                                                           \
+    cudaError_t sw_e_ = (call);                                                  \
+    if (sw_e_ != cudaSuccess)                                                    \
+      return ::swave::cuda_fail(c, sw_e_, #call " @ " __FILE__ ":" SW_STR(__LINE__)); \
+  } while (0)
 int cuda_fail(sw_ctx *c, cudaError_t e, const char *what);
 void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st);
 int check_genpar(sw_ctx *c, const sw_genpar &g);

@@ -175,26 +175,29 @@ int sw_rtm_job_create(sw_ctx *c, const sw_genpar *model, float apx, float apy, c
     cudaGetLastError();
     return bail(fail(c, SW_OOM_ADMISSION, "RTM job model buffers do not fit"));
   }
-  cudaMemcpyAsync(j->vel, vel, n * 4, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(j->wavelet, wavelet, (size_t)model->nt * 4, cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(j->image, 0, n * 4, s);
-  cudaMemsetAsync(j->illum, 0, n * 4, s);
+  SW_CK(cudaMemcpyAsync(j->vel, vel, n * 4, cudaMemcpyHostToDevice, s));
+  SW_CK(cudaMemcpyAsync(j->wavelet, wavelet, (size_t)model->nt * 4, cudaMemcpyHostToDevice, s));
+  SW_CK(cudaMemsetAsync(j->image, 0, n * 4, s));
+  SW_CK(cudaMemsetAsync(j->illum, 0, n * 4, s));
   j->shots.resize(nshot);
   for (int i = 0; i < nshot; ++i) {
     auto &S = j->shots[i];
     S.s = shots[i];
-    if (S.s.nt < 1 || S.s.nt > model->nt || !S.s.data)
-      return bail(fail(c, SW_BAD_PARAM, "shot %d: bad record length or data", i));
+    if (S.s.nt < 1 || S.s.nt > model->nt)
+      return bail(fail(c, SW_BAD_PARAM, "shot %d: bad record length", i));
     if ((st = compute_window(c, *model, apx, apy, S.s.sou_coord, S.s.nrec, S.s.rec_coord, S.w)))
       return bail(st);
     S.rec.assign(S.s.rec_coord, S.s.rec_coord + 3 * (size_t)S.s.nrec);
     S.s.rec_coord = S.rec.data();
     const size_t db = (size_t)S.s.nrec * S.s.nt * 4;
-    if (cudaMalloc(&S.data, db) != cudaSuccess) {
-      cudaGetLastError();
-      return bail(fail(c, SW_OOM_ADMISSION, "RTM job data of shot %d does not fit", i));
+    if (S.s.data) {
+      if (cudaMalloc(&S.data, db) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(c, SW_OOM_ADMISSION, "RTM job data of shot %d does not fit", i));
+      }
+      if (cudaMemcpyAsync(S.data, S.s.data, db, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return bail(fail(c, SW_CUDA_ERR, "upload of shot %d data failed", i));
     }
-    cudaMemcpyAsync(S.data, S.s.data, db, cudaMemcpyHostToDevice, s);
     S.s.data = nullptr;
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return bail(fail(c, SW_CUDA_ERR, "job upload"));
@@ -218,9 +221,10 @@ int sw_rtm_job_info(const sw_rtm_job *j, int *last_batch, uint64_t *points) {
 
 int sw_rtm_job_reset(sw_rtm_job *j) {
   if (!j) return SW_BAD_PARAM;
+  sw_ctx *c = j->c;
   const size_t n = (size_t)j->g.nz * j->g.nx * j->g.ny;
-  cudaMemsetAsync(j->image, 0, n * 4, j->c->stream);
-  cudaMemsetAsync(j->illum, 0, n * 4, j->c->stream);
+  SW_CK(cudaMemsetAsync(j->image, 0, n * 4, j->c->stream));
+  SW_CK(cudaMemsetAsync(j->illum, 0, n * 4, j->c->stream));
   j->points = 0;
   return cudaStreamSynchronize(j->c->stream) == cudaSuccess ? SW_OK : SW_CUDA_ERR;
 }
@@ -246,12 +250,124 @@ sw_genpar shot_genpar(const sw_genpar &m, const Window &w, int nt) {
   return g;
 }
 
-// Device bytes one shot needs while its batch runs.
-size_t shot_bytes(const sw_genpar &g) {
-  const Geom G = make_geom(g);
-  const size_t nw = (size_t)g.nz * g.nx * g.ny;
-  const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
-  return (size_t)G.total() * 4 * 7 + nw * 4 * (3 + ntsnap) + (1u << 20);
+}  // namespace
+
+namespace {
+
+// Device buffers of one shot while its batch runs.
+struct ShotBufs {
+  float *vpad, *vsmall, *image, *illum, *wave, *traces;
+};
+
+// Admits shots [next, end) into a batch by HBM footprint, carves their
+// buffers from one arena, windows and pads their velocity.  `modeling`
+// batches need trace buffers and no snapshots.
+int prepare_batch(sw_rtm_job *j, int &next, int end, bool modeling, std::vector<int> &batch,
+                  std::vector<ShotBufs> &bufs, std::vector<std::vector<float>> &vhost) {
+  sw_ctx *c = j->c;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int st = SW_OK;
+  const sw_genpar &M = j->g;
+  auto need_of = [&](const sw_genpar &g, int nrec) -> size_t {
+    const Geom G = make_geom(g);
+    const size_t nw = (size_t)g.nz * g.nx * g.ny;
+    const size_t ntsnap = modeling ? 0 : (size_t)std::max(1, g.nt / g.snapi);
+    size_t t = ((size_t)G.total() * 4 + 255) / 256 * 256;        // vel_pad
+    t += (nw * 4 + 255) / 256 * 256 * 3;                          // vsmall, image, illum
+    t += (nw * ntsnap * 4 + 255) / 256 * 256;                     // snapshots
+    t += ((size_t)nrec * g.nt * 4 + 255) / 256 * 256;             // traces
+    return t;
+  };
+  size_t freeb = 0, totalb = 0;
+  SW_CK(cudaMemGetInfo(&freeb, &totalb));
+  size_t held = 0;
+  auto it = c->bufs.find("rtm_arena");
+  if (it != c->bufs.end()) held = it->second.cap;
+  // The fields and plans of run_phases need (7 padded grids per shot).
+  const double budget = (double)(freeb + held) * j->mem_fraction;
+  batch.clear();
+  size_t need = 0;
+  while (next < end && (int)batch.size() < j->max_batch) {
+    const auto &S = j->shots[next];
+    const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
+    const size_t bsz = need_of(g, modeling ? S.s.nrec : 0) + (size_t)make_geom(g).total() * 4 * 7;
+    if (!batch.empty() && (double)(need + bsz) > budget) break;
+    if (batch.empty() && (double)bsz > budget)
+      return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, bsz, budget);
+    need += bsz;
+    batch.push_back(next++);
+  }
+  j->last_batch = (int)batch.size();
+  std::vector<size_t> offs;
+  size_t total = 0;
+  for (int id : batch) {
+    const auto &S = j->shots[id];
+    offs.push_back(total);
+    total += need_of(shot_genpar(M, S.w, S.s.nt), modeling ? S.s.nrec : 0);
+  }
+  char *arena = (char *)dbuf(c, "rtm_arena", total, &st);
+  if (!arena) return st;
+  bufs.assign(batch.size(), ShotBufs{});
+  vhost.assign(batch.size(), {});
+  for (size_t q = 0; q < batch.size(); ++q) {
+    const auto &S = j->shots[batch[q]];
+    const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
+    const Geom G = make_geom(g);
+    const size_t nw = (size_t)g.nz * g.nx * g.ny;
+    const size_t ntsnap = modeling ? 0 : (size_t)std::max(1, g.nt / g.snapi);
+    char *cur = arena + offs[q];
+    ShotBufs &B = bufs[q];
+    B.vpad = (float *)cur; cur += ((size_t)G.total() * 4 + 255) / 256 * 256;
+    B.vsmall = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+    B.image = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+    B.illum = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
+    B.wave = (float *)cur; cur += (nw * ntsnap * 4 + 255) / 256 * 256;
+    B.traces = (float *)cur;
+    // copy_window_vel_gath: window on the device, then model_pad.
+    if ((e = launch_window_vel(M.nz, M.nx, M.ny, M.ox, M.oy, M.dx, M.dy, S.w.nxw, S.w.nyw,
+                               S.w.oxw, S.w.oyw, j->vel, B.vsmall, s)) != cudaSuccess)
+      return cuda_fail(c, e, "window vel");
+    if ((e = launch_pad_velocity(G, B.vsmall, B.vpad, s)) != cudaSuccess)
+      return cuda_fail(c, e, "pad vel");
+    c->stats.launches_total += 2;
+    if (modeling) {
+      SW_CK(cudaMemsetAsync(B.traces, 0, (size_t)S.s.nrec * g.nt * 4, s));
+    } else {
+      SW_CK(cudaMemsetAsync(B.image, 0, nw * 4, s));
+      SW_CK(cudaMemsetAsync(B.illum, 0, nw * 4, s));
+    }
+    window_host(M, S.w, j->vel_host.data(), vhost[q]);
+  }
+  return SW_OK;
+}
+
+// Forward phase of one shot: Injection_sinc of the wavelet; snapshots for
+// RTM, Extraction_array_sinc for modelling.
+PhaseShot forward_phase(sw_rtm_job *j, const sw_rtm_job::Shot &S, const ShotBufs &B,
+                        const std::vector<float> &vh, bool modeling) {
+  const sw_genpar g = shot_genpar(j->g, S.w, S.s.nt);
+  PhaseShot F;
+  std::memset(&F.d, 0, sizeof(F.d));
+  F.d.g = g;
+  F.d.tmin = 1; F.d.tmax = g.nt; F.d.tstep = 1;
+  F.d.fd_scheme = SW_FD_FORWARD;
+  F.d.injection = SW_INJ_SINC;
+  F.io.vel_pad = B.vpad;
+  F.io.vel_phys_host = vh.data();
+  F.io.nsou = 1;
+  F.io.sou_coord = S.s.sou_coord;
+  F.io.sou_trace_dev = j->wavelet;
+  if (modeling) {
+    F.d.extraction = SW_EXT_SINC;
+    F.io.nrec = S.s.nrec;
+    F.io.rec_coord = S.rec.data();
+    F.io.rec_trace_dev = B.traces;
+  } else {
+    F.d.extract_wave = 1;
+    F.io.wave_dev = B.wave;
+  }
+  return F;
 }
 
 }  // namespace
@@ -264,87 +380,21 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
   cudaError_t e;
   int st = SW_OK;
   const sw_genpar &M = j->g;
+  for (int q = first; q < first + count; ++q)
+    if (!j->shots[q].data) return fail(c, SW_BAD_PARAM, "shot %d has no observed data", q);
   int next = first;
   const int end = first + count;
+  std::vector<int> batch;
+  std::vector<ShotBufs> bufs;
+  std::vector<std::vector<float>> vhost;
   while (next < end) {
-    // ---- admission by HBM footprint ----
-    size_t freeb = 0, totalb = 0;
-    cudaMemGetInfo(&freeb, &totalb);
-    // Buffers this context already holds for a previous batch are reusable.
-    size_t held = 0;
-    auto it = c->bufs.find("rtm_arena");
-    if (it != c->bufs.end()) held = it->second.cap;
-    const double budget = (double)(freeb + held) * j->mem_fraction;
-    std::vector<int> batch;
-    size_t need = 0;
-    while (next < end && (int)batch.size() < j->max_batch) {
-      const auto &S = j->shots[next];
-      const size_t b = shot_bytes(shot_genpar(M, S.w, S.s.nt));
-      if (!batch.empty() && (double)(need + b) > budget) break;
-      if (batch.empty() && (double)b > budget)
-        return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, b, budget);
-      need += b;
-      batch.push_back(next++);
-    }
-    j->last_batch = (int)batch.size();
-    // ---- per-shot device buffers carved from one arena ----
-    std::vector<size_t> offs;
-    size_t total = 0;
-    for (int id : batch) {
-      const auto &S = j->shots[id];
-      const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
-      const Geom G = make_geom(g);
-      const size_t nw = (size_t)g.nz * g.nx * g.ny;
-      const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
-      offs.push_back(total);
-      total += ((size_t)G.total() * 4 + 255) / 256 * 256;          // vel_pad
-      total += (nw * 4 + 255) / 256 * 256 * 3;                      // vsmall, image, illum
-      total += (nw * ntsnap * 4 + 255) / 256 * 256;                 // snapshots
-    }
-    char *arena = (char *)dbuf(c, "rtm_arena", total, &st);
-    if (!arena) return st;
-    std::vector<std::vector<float>> vhost(batch.size());
+    if ((st = prepare_batch(j, next, end, false, batch, bufs, vhost))) return st;
     std::vector<PhaseShot> fwd(batch.size()), bwd(batch.size());
-    struct Bufs { float *vpad, *vsmall, *image, *illum, *wave; };
-    std::vector<Bufs> bufs(batch.size());
     for (size_t q = 0; q < batch.size(); ++q) {
       const auto &S = j->shots[batch[q]];
+      const ShotBufs &B = bufs[q];
       const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
-      const Geom G = make_geom(g);
-      const size_t nw = (size_t)g.nz * g.nx * g.ny;
-      const size_t ntsnap = (size_t)std::max(1, g.nt / g.snapi);
-      char *cur = arena + offs[q];
-      Bufs &B = bufs[q];
-      B.vpad = (float *)cur; cur += ((size_t)G.total() * 4 + 255) / 256 * 256;
-      B.vsmall = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
-      B.image = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
-      B.illum = (float *)cur; cur += (nw * 4 + 255) / 256 * 256;
-      B.wave = (float *)cur;
-      // copy_window_vel_gath: window on the device, then model_pad.
-      if ((e = launch_window_vel(M.nz, M.nx, M.ny, M.ox, M.oy, M.dx, M.dy, S.w.nxw, S.w.nyw,
-                                 S.w.oxw, S.w.oyw, j->vel, B.vsmall, s)) != cudaSuccess)
-        return cuda_fail(c, e, "window vel");
-      if ((e = launch_pad_velocity(G, B.vsmall, B.vpad, s)) != cudaSuccess)
-        return cuda_fail(c, e, "pad vel");
-      cudaMemsetAsync(B.image, 0, nw * 4, s);
-      cudaMemsetAsync(B.illum, 0, nw * 4, s);
-      c->stats.launches_total += 2;
-      window_host(M, S.w, j->vel_host.data(), vhost[q]);
-      (void)ntsnap;
-      // Forward: Injection_sinc of the wavelet, Extraction_wavefield.
-      PhaseShot &F = fwd[q];
-      std::memset(&F.d, 0, sizeof(F.d));
-      F.d.g = g;
-      F.d.tmin = 1; F.d.tmax = g.nt; F.d.tstep = 1;
-      F.d.fd_scheme = SW_FD_FORWARD;
-      F.d.injection = SW_INJ_SINC;
-      F.d.extract_wave = 1;
-      F.io.vel_pad = B.vpad;
-      F.io.vel_phys_host = vhost[q].data();
-      F.io.nsou = 1;
-      F.io.sou_coord = S.s.sou_coord;
-      F.io.sou_trace_dev = j->wavelet;
-      F.io.wave_dev = B.wave;
+      fwd[q] = forward_phase(j, S, B, vhost[q], false);
       // Backward: 2D adjoint (3D forward) stencil, Injection_sinc of the data,
       // Imaging_condition_sourceonly_from_memory (to_disk_to_memory_RTM.f90:450-486).
       PhaseShot &R = bwd[q];
@@ -381,6 +431,38 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
   return SW_OK;
 }
 
+int sw_rtm_job_model(sw_rtm_job *j, int first, int count, float *const *data) {
+  if (!j || !data || first < 0 || count < 1 || first + count > (int)j->shots.size())
+    return SW_BAD_PARAM;
+  sw_ctx *c = j->c;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  int st = SW_OK;
+  int next = first;
+  const int end = first + count;
+  std::vector<int> batch;
+  std::vector<ShotBufs> bufs;
+  std::vector<std::vector<float>> vhost;
+  while (next < end) {
+    if ((st = prepare_batch(j, next, end, true, batch, bufs, vhost))) return st;
+    std::vector<PhaseShot> fwd(batch.size());
+    for (size_t q = 0; q < batch.size(); ++q)
+      fwd[q] = forward_phase(j, j->shots[batch[q]], bufs[q], vhost[q], true);
+    const uint64_t p0 = c->stats.points_updated;
+    if ((st = run_phases(c, fwd, c->run_opts))) return st;
+    j->points += c->stats.points_updated - p0;
+    for (size_t q = 0; q < batch.size(); ++q) {
+      const auto &S = j->shots[batch[q]];
+      float *out = data[batch[q] - first];
+      if (!out) return fail(c, SW_BAD_PARAM, "null output for shot %d", batch[q]);
+      SW_CK(cudaMemcpyAsync(out, bufs[q].traces, (size_t)S.s.nrec * S.s.nt * 4,
+                            cudaMemcpyDeviceToHost, s));
+    }
+    SW_CK(cudaStreamSynchronize(s));
+  }
+  return SW_OK;
+}
+
 int sw_rtm_job_result(sw_rtm_job *j, float *image, float *illum, float *image_norm) {
   if (!j) return SW_BAD_PARAM;
   sw_ctx *c = j->c;
@@ -388,8 +470,8 @@ int sw_rtm_job_result(sw_rtm_job *j, float *image, float *illum, float *image_no
   cudaStream_t s = c->stream;
   const long long n = (long long)j->g.nz * j->g.nx * j->g.ny;
   int st = SW_OK;
-  if (image) cudaMemcpyAsync(image, j->image, n * 4, cudaMemcpyDeviceToHost, s);
-  if (illum) cudaMemcpyAsync(illum, j->illum, n * 4, cudaMemcpyDeviceToHost, s);
+  if (image) SW_CK(cudaMemcpyAsync(image, j->image, n * 4, cudaMemcpyDeviceToHost, s));
+  if (illum) SW_CK(cudaMemcpyAsync(illum, j->illum, n * 4, cudaMemcpyDeviceToHost, s));
   if (image_norm) {
     const int nb = 296;
     float *pmax = (float *)dbuf(c, "red_pmax", nb * sizeof(float), &st);
@@ -399,7 +481,7 @@ int sw_rtm_job_result(sw_rtm_job *j, float *image, float *illum, float *image_no
     k_illum_stats<<<nb, 256, 0, s>>>(n, j->illum, pmax, psum);
     k_illum_normalise<<<nb, 256, 0, s>>>(n, nb, pmax, psum, j->image, j->illum, out);
     c->stats.launches_total += 2;
-    cudaMemcpyAsync(image_norm, out, n * 4, cudaMemcpyDeviceToHost, s);
+    SW_CK(cudaMemcpyAsync(image_norm, out, n * 4, cudaMemcpyDeviceToHost, s));
   }
   cudaError_t e = cudaStreamSynchronize(s);
   return e == cudaSuccess ? SW_OK : cuda_fail(c, e, "rtm result");

@@ -39,6 +39,19 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   std::vector<ExtPlan> ext(nb);
   std::vector<std::vector<float>> tx(nb), ty(nb);
   bool has_3d = false, has_adj3d = false, has_ext = false;
+  // The pipelined 2D kernel keeps the batch's shot table in shared memory
+  // and packs tile coordinates into 12 bits each; larger batches or grids
+  // use the streaming kernel.
+  StepTile tile = opt.tile;
+  if (tile.stream2d == 2) {
+    bool fits = nb <= T2_MAX_SHOTS;
+    for (int b = 0; b < nb && fits; ++b) {
+      const Geom g = make_geom(shots[b].d.g);
+      fits = (g.nmax1 - g.nmin1 + 1) <= 64 * 4095 && (g.nmax2 - g.nmin2 + 1) <= 32 * 4095;
+    }
+    if (!fits) tile.stream2d = 1;
+  }
+  const bool t2 = tile.stream2d == 2 && shots[0].d.g.twoD;
   // ---- host-side plans and arena sizes ----
   size_t bytes = 0;
   for (int b = 0; b < nb; ++b) {
@@ -46,6 +59,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     const DevIO &io = shots[b].io;
     if ((st = check_genpar(c, d.g))) return st;
     if (d.tstep != 1 && d.tstep != -1) return fail(c, SW_BAD_PARAM, "tstep must be +-1");
+    if (make_geom(d.g).total() >= (1LL << 31))
+      return fail(c, SW_BAD_PARAM, "padded grid of shot %d exceeds 2^31 points", b);
     if (b > 0 && (d.g.twoD != shots[0].d.g.twoD))
       return fail(c, SW_BAD_PARAM, "a batch mixes 2D and 3D shots");
     G[b] = make_geom(d.g);
@@ -62,13 +77,18 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
                     n3 = G[b].nmax3 - G[b].nmin3 + 1;
     bytes += 5 * rup(fb);
-    if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT) bytes += rup(fb);
+    if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT && !tile.stream3d) bytes += rup(fb);
     bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
     bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry));
     bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
     bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
   }
   bytes += rup(nb * sizeof(ShotDev)) + 6 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
+  if (t2) {
+    size_t ntile = 0;
+    for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
+    bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int));
+  }
   char *arena = (char *)dbuf(c, "batch_arena", bytes, &st);
   if (!arena) return st;
   char *cur = arena;
@@ -93,9 +113,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     }
     S.adj2d = g.twoD && d.fd_scheme == SW_FD_ADJOINT;
     S.adj3d = !g.twoD && d.fd_scheme == SW_FD_ADJOINT;
-    if (S.adj3d) {
+    if (S.adj3d && !tile.stream3d) {
       S.v2u = carve<float>(cur, nf);
-      cudaMemsetAsync(S.v2u, 0, nf * sizeof(float), s);
+      SW_CK(cudaMemsetAsync(S.v2u, 0, nf * sizeof(float), s));
     }
     S.vel = io.vel_pad;
     const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
@@ -113,9 +133,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       S.bk0 = inj[b].bk0; S.bk1 = inj[b].bk1;
       int *off = carve<int>(cur, inj[b].off.size());
       InjEntry *ent = carve<InjEntry>(cur, inj[b].ent.size());
-      cudaMemcpyAsync(off, inj[b].off.data(), inj[b].off.size() * 4, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(ent, inj[b].ent.data(), inj[b].ent.size() * sizeof(InjEntry),
-                      cudaMemcpyHostToDevice, s);
+      SW_CK(cudaMemcpyAsync(off, inj[b].off.data(), inj[b].off.size() * 4, cudaMemcpyHostToDevice, s));
+      SW_CK(cudaMemcpyAsync(ent, inj[b].ent.data(), inj[b].ent.size() * sizeof(InjEntry),
+                      cudaMemcpyHostToDevice, s));
       S.inj_off = off;
       S.inj_ent = ent;
       S.src_tr = io.sou_trace_dev;
@@ -126,9 +146,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     if (ext[b].on) {
       int *ric = carve<int>(cur, ext[b].ic.size());
       float *wz = carve<float>(cur, ext[b].wz.size()), *wx = carve<float>(cur, ext[b].wx.size());
-      cudaMemcpyAsync(ric, ext[b].ic.data(), ext[b].ic.size() * 4, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(wz, ext[b].wz.data(), ext[b].wz.size() * 4, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(wx, ext[b].wx.data(), ext[b].wx.size() * 4, cudaMemcpyHostToDevice, s);
+      SW_CK(cudaMemcpyAsync(ric, ext[b].ic.data(), ext[b].ic.size() * 4, cudaMemcpyHostToDevice, s));
+      SW_CK(cudaMemcpyAsync(wz, ext[b].wz.data(), ext[b].wz.size() * 4, cudaMemcpyHostToDevice, s));
+      SW_CK(cudaMemcpyAsync(wx, ext[b].wx.data(), ext[b].wx.size() * 4, cudaMemcpyHostToDevice, s));
       S.ric = ric; S.wz = wz; S.wx = wx;
       S.rec_tr = io.rec_trace_dev;
       S.vconst = 1.f;
@@ -149,8 +169,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     S.ref = io.ref_dev;
     if (d.imaging != SW_IMG_NONE) {
       float *a = carve<float>(cur, tx[b].size() + 1), *bq = carve<float>(cur, ty[b].size() + 1);
-      cudaMemcpyAsync(a, tx[b].data(), tx[b].size() * 4, cudaMemcpyHostToDevice, s);
-      cudaMemcpyAsync(bq, ty[b].data(), ty[b].size() * 4, cudaMemcpyHostToDevice, s);
+      SW_CK(cudaMemcpyAsync(a, tx[b].data(), tx[b].size() * 4, cudaMemcpyHostToDevice, s));
+      SW_CK(cudaMemcpyAsync(bq, ty[b].data(), ty[b].size() * 4, cudaMemcpyHostToDevice, s));
       S.taperx = a;
       S.tapery = bq;
     }
@@ -167,24 +187,60 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       return fail(c, SW_BAD_PARAM, "image buffers missing");
     if (S.imaging == SW_IMG_BORN && !S.ref) return fail(c, SW_BAD_PARAM, "reflectivity missing");
     max_steps = std::max(max_steps, S.nsteps);
-    const int ntz = (int)((n1 + 31) / 32), ntx = (int)((n2 + 7) / 8);
-    step_tiles[b + 1] = step_tiles[b] + ntz * ntx * (int)n3;
+    step_tiles[b + 1] = step_tiles[b] + step_ctas(G[b], tile);
     rec_start[b + 1] = rec_start[b] + S.nrec;
     hz[b + 1] = hz[b] + (int)(n2 * n3);
     hx[b + 1] = hx[b] + (int)(n1 * n3);
     hy[b + 1] = hy[b] + (g.twoD ? 0 : (int)(n1 * n2));
-    v2b[b + 1] = v2b[b] + (S.adj3d ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256) : 0);
+    v2b[b + 1] = v2b[b] + ((S.adj3d && !tile.stream3d)
+                               ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256)
+                               : 0);
   }
   ShotDev *dshots = carve<ShotDev>(cur, nb);
   int *dtab[6];
   std::vector<int> *htab[6] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b};
   for (int q = 0; q < 6; ++q) {
     dtab[q] = carve<int>(cur, nb + 1);
-    cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s);
+    SW_CK(cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s));
   }
   int *counter = carve<int>(cur, 1);
-  cudaMemcpyAsync(dshots, hs.data(), nb * sizeof(ShotDev), cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(counter, 0, sizeof(int), s);
+  SW_CK(cudaMemcpyAsync(dshots, hs.data(), nb * sizeof(ShotDev), cudaMemcpyHostToDevice, s));
+  // Compact shot views and the shot-major tile table of the pipelined 2D
+  // kernel.
+  std::vector<T2Shot> h2(t2 ? nb : 0);
+  std::vector<int> htile;
+  T2Shot *d2 = nullptr;
+  int *dtile = nullptr;
+  if (t2) {
+    for (int b = 0; b < nb; ++b) {
+      const ShotDev &S = hs[b];
+      T2Shot &h = h2[b];
+      std::memset(&h, 0, sizeof(h));
+      for (int q = 0; q < 5; ++q) h.f[q] = S.f[q];
+      h.vel = S.vel;
+      h.c0z = S.c.c0z; h.c1z = S.c.c1z; h.c2z = S.c.c2z; h.c3z = S.c.c3z; h.c4z = S.c.c4z;
+      h.c0x = S.c.c0x; h.c1x = S.c.c1x; h.c2x = S.c.c2x; h.c3x = S.c.c3x; h.c4x = S.c.c4x;
+      h.k12 = S.k12; h.div11 = S.div11;
+      h.ld1 = S.g.ld1; h.lo2 = S.g.lo2; h.n2p = S.g.n2p;
+      h.nmin1 = S.g.nmin1; h.nmax1 = S.g.nmax1; h.nmin2 = S.g.nmin2; h.nmax2 = S.g.nmax2;
+      h.nz = S.g.nz; h.nx = S.g.nx;
+      h.nsteps = S.nsteps; h.tmin = S.tmin; h.tstep = S.tstep; h.snapi = S.snapi;
+      h.adj2d = S.adj2d; h.inj_on = S.inj_on;
+      h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
+      h.extract_wave = S.extract_wave; h.imaging = S.imaging;
+      const int n1t = (S.g.nmax1 - S.g.nmin1 + 1 + 63) / 64;
+      const int n2t = (S.g.nmax2 - S.g.nmin2 + 1 + 31) / 32;
+      for (int xi = 0; xi < n2t; ++xi)
+        for (int zi = 0; zi < n1t; ++zi) htile.push_back((b << 24) | (zi << 12) | xi);
+    }
+    if ((int)htile.size() != step_tiles[nb]) return fail(c, SW_CUDA_ERR, "tile table size");
+    d2 = carve<T2Shot>(cur, nb);
+    dtile = carve<int>(cur, htile.size());
+    SW_CK(cudaMemcpyAsync(d2, h2.data(), nb * sizeof(T2Shot), cudaMemcpyHostToDevice, s));
+    SW_CK(cudaMemcpyAsync(dtile, htile.data(), htile.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          s));
+  }
+  SW_CK(cudaMemsetAsync(counter, 0, sizeof(int), s));
   if ((size_t)(cur - arena) > bytes) return fail(c, SW_CUDA_ERR, "arena overflow");
   BatchTables t;
   t.nshots = nb;
@@ -195,12 +251,30 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.hx_start = dtab[3];
   t.hy_start = dtab[4];
   t.v2u_blocks = dtab[5];
+  t.t2shots = d2;
+  t.tile_tab = dtile;
   t.counter = counter;
   // The host plans above must stay alive until the uploads complete.
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch setup");
 
   const int n_tiles = step_tiles[nb], n_rec = rec_start[nb], n_hz = hz[nb], n_hx = hx[nb],
             n_hy = hy[nb], n_v2u = v2b[nb];
+  {
+    int dev = 0, nsm = 0;
+    SW_CK(cudaGetDevice(&dev));
+    SW_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    tile.nsm = nsm;
+  }
+  tile.has_fwd2d = tile.has_adj2d = tile.has_fwd3d = tile.has_adj3d = 0;
+  for (auto &S : hs) {
+    if (S.g.twoD) {
+      if (S.adj2d) tile.has_adj2d = 1;
+      else tile.has_fwd2d = 1;
+    } else {
+      if (S.adj3d) tile.has_adj3d = 1;
+      else tile.has_fwd3d = 1;
+    }
+  }
   long long npts_total = 0;
   for (auto &S : hs) npts_total += S.npts;
   // ---- time loop ----
@@ -210,7 +284,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   if (prof && (int)c->ev.size() < 2 * chunk) {
     const size_t old = c->ev.size();
     c->ev.resize(2 * chunk);
-    for (size_t q = old; q < c->ev.size(); ++q) cudaEventCreate(&c->ev[q]);
+    for (size_t q = old; q < c->ev.size(); ++q) SW_CK(cudaEventCreate(&c->ev[q]));
   }
   auto record_chunk = [&](int nsteps_here) -> int {
     int launched = 0;
@@ -218,7 +292,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       int nl = 0;
       // In profiling mode events bracket the fused step kernel only.
       if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
-                                 has_adj3d, s, &nl, prof ? c->ev[2 * q] : nullptr,
+                                 has_adj3d, tile, s, &nl, prof ? c->ev[2 * q] : nullptr,
                                  prof ? c->ev[2 * q + 1] : nullptr)) != cudaSuccess)
         return -1;
       launched += nl;
@@ -246,11 +320,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       if ((e = cudaGraphLaunch(exec, s)) != cudaSuccess) break;
       launches += per;
       if (prof) {
-        cudaEventSynchronize(c->ev[2 * chunk - 1]);
+        SW_CK(cudaEventSynchronize(c->ev[2 * chunk - 1]));
         const int live = std::min(chunk, max_steps - q * chunk);
         for (int k = 0; k < live; ++k) {
           float ms = 0.f;
-          cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]);
+          SW_CK(cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]));
           c->stats.step_kernel_ms += ms;
           c->stats.step_kernel_timed++;
         }
@@ -265,9 +339,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       if (per < 0) return cuda_fail(c, e, "step launch");
       launches += per;
       if (prof) {
-        cudaEventSynchronize(c->ev[1]);
+        SW_CK(cudaEventSynchronize(c->ev[1]));
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        SW_CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         c->stats.step_kernel_ms += ms;
         c->stats.step_kernel_timed++;
       }
