@@ -155,9 +155,11 @@ def measured_peak():
 # CPU baseline: the oracle (a restatement of the reference CPU path)
 # ---------------------------------------------------------------------------
 def cpu_sample(g, vel, w, shot, nsteps: int) -> dict:
-    """Times the oracle's RTM of one shot truncated to nsteps samples."""
+    """Times the oracle's RTM of one shot (its whole record when nsteps is 0,
+    else truncated to nsteps samples)."""
     import seismic_gb300 as sw
     from oracle import bind as oracle
+    nsteps = nsteps or shot["nt"]
     i0, nxw = window_of(shot)
     gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=nsteps, ntaper=NTAPER,
                         lsinc=7, snapi=SNAPI)
@@ -197,12 +199,13 @@ def run_reference(args):
         r = cpu_sample(g, vel, w, shots[k % len(shots)], nsteps)
         if k >= args.warmup:
             res.append(r)
+    nsteps = nsteps or "all"
     secs = sum(r["seconds"] for r in res)
     pts = sum(r["points"] for r in res)
     v = pts / secs / 1e9
     cores = cpu_threads()
     sample = (f"RTM (forward + backward, {nsteps} of the 8000-10667 time samples) of one "
-              f"{NZ}x(window) shot per step, {args.steps} steps")
+              f"{NZ}x(window) shot per step, {args.steps} steps, {secs:.1f} s")
     line = {
         "impl": "reference", "metric": "fd_gpts_per_s", "value": v, "unit": "Gpts/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
@@ -233,7 +236,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--shots-per-step", type=int, default=16)
-    ap.add_argument("--cpu-steps", type=int, default=240)
+    ap.add_argument("--cpu-steps", type=int, default=0,
+                    help="time samples of the CPU sample shot (0: its whole record)")
     ap.add_argument("--nt-cap", type=int, default=0, help="truncate records (debug)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -360,8 +364,8 @@ def main():
         r = cpu_sample(g, vel, w, per_step[0], args.cpu_steps)
         cpu = {"value": r["points"] / r["seconds"] / 1e9, "unit": "Gpts/s", "cores": cpu_threads(),
                "kind": "port",
-               "sample": f"oracle RTM of one shot window, {args.cpu_steps} of its time samples, "
-                         f"forward + backward ({r['seconds']:.1f} s)"}
+               "sample": f"oracle RTM of one shot window, {args.cpu_steps or per_step[0]['nt']} "
+                         f"time samples, forward + backward ({r['seconds']:.1f} s)"}
     if rank == 0:
         line = {
             "metric": "fd_gpts_per_s", "value": value, "unit": "Gpts/s", "n_gpus": ws,
@@ -371,7 +375,7 @@ def main():
             "config": workload_config(args, last_batch),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "peak_kind": peak_kind, "kernel": "k_bstep (fused stencil + time update)",
+                         "peak_kind": peak_kind, "kernel": "k_bstep2d_t (fused stencil + time update, pipelined 2D tiles)",
                          "avg_launch_ms": (st["step_kernel_ms"] / nl),
                          "launches_timed": st["step_kernel_timed"]},
             "cpu_baseline": cpu, "e2e": e2e_line, "clocks": clk,

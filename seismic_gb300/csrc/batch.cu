@@ -340,6 +340,94 @@ __global__ void k_bhiggx(BatchTables t, int s_off) {
   }
 }
 
+// Fused 2D edges: the z (top, bottom) and x (left, right) Higdon
+// recurrences of one step in one launch.  Each half line loads its 10 u2 and
+// u1 values, two u3 values and 8 coefficients first and then runs the 8-cell
+// recurrence in registers.  The reference applies all z lines and then all x
+// lines; only the x half lines of the 4 rows next to a z edge read or
+// overwrite cells the z half lines write (columns within 6 of an x edge),
+// so each corner is one warp that runs those 6 z half lines, synchronises
+// and then runs the 4 x half lines.  Every other half line is independent.
+__device__ __forceinline__ void higdon_half(const float *__restrict__ gc, long long cs,
+                                            const float *__restrict__ u1,
+                                            const float *__restrict__ u2, float *u3,
+                                            long long pstart, long long dst) {
+  float c[8], U2[10], U1[10];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) c[q] = gc[q * cs];
+#pragma unroll
+  for (int m = 0; m < 10; ++m) {
+    const long long pm = pstart - (long long)(m - 2) * dst;   // k = m - 2
+    U2[m] = u2[pm];
+    U1[m] = u1[pm];
+  }
+  float a = u3[pstart + dst], bq = u3[pstart + 2 * dst];
+  float out[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    float r = c[0] * a;
+    r = r + c[1] * bq;
+    r = r + c[2] * U2[k + 2];
+    r = r + c[3] * U2[k + 1];
+    r = r + c[4] * U2[k];
+    r = r + c[5] * U1[k + 2];
+    r = r + c[6] * U1[k + 1];
+    r = r + c[7] * U1[k];
+    out[k] = -r;
+    bq = a;
+    a = out[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) u3[pstart - (long long)k * dst] = out[k];
+}
+
+__global__ void __launch_bounds__(128) k_bedges2d(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.edge_start[t.nshots]) return;
+  const int b = find_shot(t.edge_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;   // uniform over the shot's warps
+  const Geom &g = S.g;
+  const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  const long long L = g.ld1;
+  const long long csz = n2, csx = n1;
+  // z half line of column j (bottom: the 8 coefficients after the top's).
+  auto zhalf = [&](int j, int bottom) {
+    const float *gc = S.gz + (j - g.nmin2) + (bottom ? 8 * csz : 0);
+    if (!bottom) higdon_half(gc, csz, u1, u2, u3, g.idx(g.nmin1 + 3, j, g.nmin3), 1);
+    else higdon_half(gc, csz, u1, u2, u3, g.idx(g.nmax1 - 3, j, g.nmin3), -1);
+  };
+  auto xhalf = [&](int i, int right) {
+    const float *gc = S.gx + (i - g.nmin1) + (right ? 8 * csx : 0);
+    if (!right) higdon_half(gc, csx, u1, u2, u3, g.idx(i, g.nmin2 + 3, g.nmin3), L);
+    else higdon_half(gc, csx, u1, u2, u3, g.idx(i, g.nmax2 - 3, g.nmin3), -L);
+  };
+  const int local = q - t.edge_start[b];
+  if (local < 128) {
+    const int w = local >> 5, lane = local & 31;
+    const int bottom = w & 1, right = w >> 1;
+    if (lane < 6) zhalf(right ? g.nmax2 - lane : g.nmin2 + lane, bottom);
+    __syncwarp();
+    if (lane < 4) xhalf(bottom ? g.nmax1 - lane : g.nmin1 + lane, right);
+    return;
+  }
+  int r = local - 128;
+  const int nz_rest = n2 - 12, nx_rest = n1 - 8;
+  if (r < 2 * nz_rest) {
+    const int bottom = r >= nz_rest;
+    zhalf(g.nmin2 + 6 + (bottom ? r - nz_rest : r), bottom);
+    return;
+  }
+  r -= 2 * nz_rest;
+  if (r < 2 * nx_rest) {
+    const int right = r >= nx_rest;
+    xhalf(g.nmin1 + 4 + (right ? r - nx_rest : r), right);
+  }
+}
+
 __global__ void k_bhiggy(BatchTables t, int s_off) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= t.hy_start[t.nshots]) return;
@@ -486,9 +574,14 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     ++nl;
   }
   if (ev_after) cudaEventRecordWithFlags(ev_after, s, cudaEventRecordExternal);
-  k_bhiggz<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
-  k_bhiggx<<<(n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
-  nl += 2;
+  if (!has_3d && tile.fused_edges) {
+    k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);
+    ++nl;
+  } else {
+    k_bhiggz<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
+    k_bhiggx<<<(n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
+    nl += 2;
+  }
   if (has_3d && n_hy > 0) {
     k_bhiggy<<<(n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;

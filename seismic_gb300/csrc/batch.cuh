@@ -69,6 +69,7 @@ struct BatchTables {
   const int *v2u_blocks;  // nshots+1: blocks of the v^2*u2 pass
   const T2Shot *t2shots;  // nshots compact views (pipelined 2D kernel)
   const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
+  const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
   int *counter;           // step counter s (0-based)
 };
 
@@ -88,7 +89,18 @@ struct StepTile {
   int has_fwd3d = 1;
   int has_adj3d = 1;
   int nsm = 152;       // SMs of the device (persistent grids)
+  int fused_edges = 0; // 2D: one launch for the z and x Higdon edges (set by the runner)
+  int n_edge = 0;      // threads of that launch
 };
+
+// Threads of the fused 2D edge kernel for one shot: four corner warps and
+// one thread per remaining half line, rounded to whole warps.  0 when the
+// compute domain is too small for the corner scheme (n1 or n2 below 16).
+inline int edge_threads_2d(const Geom &g) {
+  const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
+  if (n1 < 16 || n2 < 16) return 0;
+  return 128 + (2 * (n2 - 12) + 2 * (n1 - 8) + 31) / 32 * 32;
+}
 
 // Number of fused-step CTAs a shot needs with this tile shape.
 inline int step_ctas(const Geom &g, const StepTile &tile) {

@@ -83,7 +83,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
     bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
   }
-  bytes += rup(nb * sizeof(ShotDev)) + 6 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
+  bytes += rup(nb * sizeof(ShotDev)) + 7 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
   if (t2) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
@@ -95,7 +95,10 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // ---- carve and fill ----
   std::vector<ShotDev> hs(nb);
   std::vector<int> step_tiles(nb + 1, 0), rec_start(nb + 1, 0), hz(nb + 1, 0), hx(nb + 1, 0),
-      hy(nb + 1, 0), v2b(nb + 1, 0);
+      hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0);
+  // The fused 2D edge kernel needs n1, n2 >= 16 in every shot.
+  bool fused_edges = !has_3d;
+  for (int b = 0; b < nb && fused_edges; ++b) fused_edges = edge_threads_2d(G[b]) > 0;
   int max_steps = 0;
   for (int b = 0; b < nb; ++b) {
     const sw_prop_desc &d = shots[b].d;
@@ -192,14 +195,15 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     hz[b + 1] = hz[b] + (int)(n2 * n3);
     hx[b + 1] = hx[b] + (int)(n1 * n3);
     hy[b + 1] = hy[b] + (g.twoD ? 0 : (int)(n1 * n2));
+    edge[b + 1] = edge[b] + (fused_edges ? edge_threads_2d(G[b]) : 0);
     v2b[b + 1] = v2b[b] + ((S.adj3d && !tile.stream3d)
                                ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256)
                                : 0);
   }
   ShotDev *dshots = carve<ShotDev>(cur, nb);
-  int *dtab[6];
-  std::vector<int> *htab[6] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b};
-  for (int q = 0; q < 6; ++q) {
+  int *dtab[7];
+  std::vector<int> *htab[7] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b, &edge};
+  for (int q = 0; q < 7; ++q) {
     dtab[q] = carve<int>(cur, nb + 1);
     SW_CK(cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s));
   }
@@ -251,6 +255,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.hx_start = dtab[3];
   t.hy_start = dtab[4];
   t.v2u_blocks = dtab[5];
+  t.edge_start = dtab[6];
   t.t2shots = d2;
   t.tile_tab = dtile;
   t.counter = counter;
@@ -266,6 +271,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     tile.nsm = nsm;
   }
   tile.has_fwd2d = tile.has_adj2d = tile.has_fwd3d = tile.has_adj3d = 0;
+  tile.fused_edges = fused_edges ? 1 : 0;
+  tile.n_edge = edge[nb];
   for (auto &S : hs) {
     if (S.g.twoD) {
       if (S.adj2d) tile.has_adj2d = 1;
@@ -281,61 +288,84 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   const int chunk = std::max(1, std::min(opt.chunk, max_steps));
   const int nchunks = (max_steps + chunk - 1) / chunk;
   const bool prof = c->profiling;
-  if (prof && (int)c->ev.size() < 2 * chunk) {
+  // Profiling: events around every fused step kernel.  With the graph path
+  // two graphs record into two event sets, so the host reads the times of
+  // chunk q-1 while chunk q runs and the device never waits for the host.
+  const int nsets = (opt.use_graph && nchunks > 1) ? 2 : 1;
+  if (prof && (int)c->ev.size() < 2 * chunk * nsets) {
     const size_t old = c->ev.size();
-    c->ev.resize(2 * chunk);
+    c->ev.resize(2 * chunk * nsets);
     for (size_t q = old; q < c->ev.size(); ++q) SW_CK(cudaEventCreate(&c->ev[q]));
   }
-  auto record_chunk = [&](int nsteps_here) -> int {
+  auto record_chunk = [&](int nsteps_here, int set) -> int {
     int launched = 0;
+    cudaEvent_t *ev = prof ? c->ev.data() + 2 * chunk * set : nullptr;
     for (int q = 0; q < nsteps_here; ++q) {
       int nl = 0;
       // In profiling mode events bracket the fused step kernel only.
       if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
-                                 has_adj3d, tile, s, &nl, prof ? c->ev[2 * q] : nullptr,
-                                 prof ? c->ev[2 * q + 1] : nullptr)) != cudaSuccess)
+                                 has_adj3d, tile, s, &nl, prof ? ev[2 * q] : nullptr,
+                                 prof ? ev[2 * q + 1] : nullptr)) != cudaSuccess)
         return -1;
       launched += nl;
     }
     if ((e = launch_counter_add(counter, nsteps_here, s)) != cudaSuccess) return -1;
     return launched + 1;
   };
+  auto read_chunk = [&](int q) -> int {
+    const int set = q % nsets;
+    cudaEvent_t *ev = c->ev.data() + 2 * chunk * set;
+    const int live = std::min(chunk, max_steps - q * chunk);
+    SW_CK(cudaEventSynchronize(ev[2 * live - 1]));
+    for (int k = 0; k < live; ++k) {
+      float ms = 0.f;
+      SW_CK(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
+      c->stats.step_kernel_ms += ms;
+      c->stats.step_kernel_timed++;
+    }
+    return SW_OK;
+  };
   uint64_t launches = 0;
   if (opt.use_graph && nchunks > 1) {
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-      return cuda_fail(c, e, "begin capture");
-    const int per = record_chunk(chunk);
-    cudaError_t ec = cudaStreamEndCapture(s, &graph);
-    if (per < 0 || ec != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      return cuda_fail(c, per < 0 ? e : ec, "capture step graph");
-    }
-    if ((e = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) {
-      cudaGraphDestroy(graph);
-      return cuda_fail(c, e, "instantiate step graph");
-    }
-    for (int q = 0; q < nchunks; ++q) {
-      if ((e = cudaGraphLaunch(exec, s)) != cudaSuccess) break;
-      launches += per;
-      if (prof) {
-        SW_CK(cudaEventSynchronize(c->ev[2 * chunk - 1]));
-        const int live = std::min(chunk, max_steps - q * chunk);
-        for (int k = 0; k < live; ++k) {
-          float ms = 0.f;
-          SW_CK(cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]));
-          c->stats.step_kernel_ms += ms;
-          c->stats.step_kernel_timed++;
-        }
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    const int ngraph = prof ? 2 : 1;
+    int per = 0;
+    auto cleanup = [&]() {
+      for (int k = 0; k < 2; ++k) {
+        if (exec[k]) cudaGraphExecDestroy(exec[k]);
+        if (graph[k]) cudaGraphDestroy(graph[k]);
+      }
+    };
+    for (int k = 0; k < ngraph; ++k) {
+      if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(c, e, "begin capture");
+      }
+      per = record_chunk(chunk, k);
+      cudaError_t ec = cudaStreamEndCapture(s, &graph[k]);
+      if (per < 0 || ec != cudaSuccess) {
+        cleanup();
+        return cuda_fail(c, per < 0 ? e : ec, "capture step graph");
+      }
+      if ((e = cudaGraphInstantiate(&exec[k], graph[k], 0)) != cudaSuccess) {
+        cleanup();
+        return cuda_fail(c, e, "instantiate step graph");
       }
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
+    int rs = SW_OK;
+    for (int q = 0; q < nchunks; ++q) {
+      if ((e = cudaGraphLaunch(exec[q % ngraph], s)) != cudaSuccess) break;
+      launches += per;
+      if (prof && q > 0 && (rs = read_chunk(q - 1)) != SW_OK) break;
+    }
+    if (e == cudaSuccess && rs == SW_OK && prof) rs = read_chunk(nchunks - 1);
+    cleanup();
     if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
+    if (rs != SW_OK) return rs;
   } else {
     for (int q = 0; q < max_steps; ++q) {
-      const int per = record_chunk(1);
+      const int per = record_chunk(1, 0);
       if (per < 0) return cuda_fail(c, e, "step launch");
       launches += per;
       if (prof) {

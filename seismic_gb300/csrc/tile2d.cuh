@@ -10,13 +10,14 @@
 // The CTA's tile list and the batch's compact shot descriptors are copied
 // to shared memory once, so the loop issues no dependent global loads.  Each
 // thread computes 4 consecutive z rows in two columns from shared memory
-// with 128-bit reads and writes u3 with 128-bit stores.  Work only a few
-// tiles have (injection boxes, snapshot / imaging steps, clamped adjoint
-// edges) is decided once per tile.  The floating-point operation order is
-// the reference's (see batch.cu).
+// with 128-bit reads, packed FP32 pair arithmetic (f32x2.cuh) and 128-bit
+// stores of u3.  Work only a few tiles have (injection boxes, snapshot and
+// imaging steps) is decided once per tile.  The floating-point operation
+// order is the reference's (see batch.cu).
 #pragma once
 
 #include "batch.cuh"
+#include "f32x2.cuh"
 
 namespace swave {
 
@@ -91,56 +92,174 @@ __device__ __forceinline__ float f4get(const float4 &a, int e) {
   return e == 0 ? a.x : e == 1 ? a.y : e == 2 ? a.z : a.w;
 }
 
-// Injection, Born source, snapshot and imaging of one element (rare tiles;
-// reads the full shot descriptor from global memory).
-__device__ __noinline__ float t2_extras(const ShotDev &S, int it, bool snapstep, int i, int j,
-                                        float se, float u2c, float vc) {
-  const Geom &g = S.g;
-  if (S.inj_on && i >= S.bi0 && i <= S.bi1 && j >= S.bj0 && j <= S.bj1) {
-    const int bx = (i - S.bi0) + (S.bi1 - S.bi0 + 1) * (j - S.bj0);
-    const int e1 = S.inj_off[bx + 1];
-    for (int q = S.inj_off[bx]; q < e1; ++q) {
-      const InjEntry E = S.inj_ent[q];
-      const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
-      se = se + (((E.v2r * tr) * E.wz) * E.wx) * E.wy;   // Injection.f90:151-456,561-591
-    }
+// Injection into one element of the injection box (CSR list in source
+// order; Injection.f90:151-456,561-591).
+__device__ __noinline__ float t2_inject(const ShotDev &S, int it, int i, int j, float se) {
+  const int bx = (i - S.bi0) + (S.bi1 - S.bi0 + 1) * (j - S.bj0);
+  const int e1 = S.inj_off[bx + 1];
+  for (int q = S.inj_off[bx]; q < e1; ++q) {
+    const InjEntry E = S.inj_ent[q];
+    const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
+    se = se + (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
   }
-  if (snapstep && i >= 1 && i <= g.nz && j >= 1 && j <= g.nx) {
-    const long long nphys = (long long)g.nz * g.nx;
-    const long long pp = (long long)(i - 1) + (long long)g.nz * (j - 1);
-    const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
-    const int cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
-                                : S.tmin / S.snapi - (it - 1) / S.snapi;
-    // Injection_Born (Imaging.f90:747-788).
-    if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap)
-      se = se + (((2.0f * taper) * S.ref[pp]) * S.wave[(long long)(cnt - 1) * nphys + pp]) / vc;
-    // Extraction_wavefield (Extraction.f90:562-601).
-    if (S.extract_wave && cnt <= S.ntsnap) S.wave[(long long)(cnt - 1) * nphys + pp] = u2c;
-    if (S.imaging >= 1 && S.imaging <= 3 && S.tstep < 0) {
-      const int index = S.ntsnap - cnt + 1;
-      if (index >= 1) {
-        const float wsn = S.wave[(long long)(index - 1) * nphys + pp];
-        float im = S.image[pp];
-        if (S.imaging == 1) {
-          im = im + (u2c * wsn) * taper;                          // Imaging.f90:265
-        } else if (S.imaging == 2) {
-          im = im + (((2.0f * taper) * u2c) * wsn) / vc;          // Imaging.f90:735
-        } else {
-          const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
-          const float tt = ((S.wave[(long long)(im1 - 1) * nphys + pp] - 2.0f * wsn) +
-                            S.wave[(long long)(ip1 - 1) * nphys + pp]) /
-                           (S.dt2snap * ((vc * vc) * vc));
-          im = im + (u2c * tt) * taper;                           // Imaging.f90:410-411
-        }
-        S.image[pp] = im;
-        S.illum[pp] = S.illum[pp] + (wsn * wsn) * taper;
-      }
+  return se;
+}
+
+// Born source and AFWI imaging of one element on a snapshot step (the
+// imaging modes the vectorised t2_snap_col path does not cover).
+__device__ __noinline__ float t2_snap_generic(const ShotDev &S, int it, int i, int j, float se,
+                                              float u2c, float vc) {
+  const Geom &g = S.g;
+  if (i < 1 || i > g.nz || j < 1 || j > g.nx) return se;
+  const long long nphys = (long long)g.nz * g.nx;
+  const long long pp = (long long)(i - 1) + (long long)g.nz * (j - 1);
+  const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
+  const int cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
+                              : S.tmin / S.snapi - (it - 1) / S.snapi;
+  // Injection_Born (Imaging.f90:747-788).
+  if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap)
+    se = se + (((2.0f * taper) * S.ref[pp]) * S.wave[(long long)(cnt - 1) * nphys + pp]) / vc;
+  // Extraction_wavefield (Extraction.f90:562-601).
+  if (S.extract_wave && cnt <= S.ntsnap) S.wave[(long long)(cnt - 1) * nphys + pp] = u2c;
+  if (S.imaging == 3 && S.tstep < 0) {
+    const int index = S.ntsnap - cnt + 1;
+    if (index >= 1) {
+      const float wsn = S.wave[(long long)(index - 1) * nphys + pp];
+      const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
+      const float tt = ((S.wave[(long long)(im1 - 1) * nphys + pp] - 2.0f * wsn) +
+                        S.wave[(long long)(ip1 - 1) * nphys + pp]) /
+                       (S.dt2snap * ((vc * vc) * vc));
+      S.image[pp] = S.image[pp] + (u2c * tt) * taper;             // Imaging.f90:410-411
+      S.illum[pp] = S.illum[pp] + (wsn * wsn) * taper;
     }
   }
   return se;
 }
 
-// Computes one tile from a completed stage.
+__device__ __forceinline__ float4 lds4(const float *p) {
+  return *reinterpret_cast<const float4 *>(p);
+}
+
+// Constants of a shot used by the packed arithmetic.
+struct T2Pairs {
+  float cz[5], cx[5], k12;
+  P2 div11;
+};
+
+__device__ __forceinline__ T2Pairs t2_pairs(const T2Shot &h) {
+  T2Pairs c;
+  c.cz[0] = h.c0z; c.cz[1] = h.c1z; c.cz[2] = h.c2z; c.cz[3] = h.c3z; c.cz[4] = h.c4z;
+  c.cx[0] = h.c0x; c.cx[1] = h.c1x; c.cx[2] = h.c2x; c.cx[3] = h.c3x; c.cx[4] = h.c4x;
+  c.k12 = h.k12;
+  c.div11 = p2s(h.div11);
+  return c;
+}
+
+// Laplacian part of 4 consecutive rows of one column, away from the edges
+// of the compute domain, as two row pairs (rows 0,1 and 2,3).  col points at
+// row i0-4 of the staged u2 column, vcol (adjoint) at the same row of the
+// staged velocity, vcore (forward) at row i0 of the staged core velocity.
+// Per lane the operations are those of the scalar loops
+// (FDderivatives.f90:715-743 forward, 847-891 adjoint).
+template <bool ADJ>
+__device__ __forceinline__ void t2_col_fast(const T2Pairs &c, const float *col, const float *vcol,
+                                            const float *vcore, P2 sv[2], float4 &u2c) {
+  const float4 za = lds4(col), zb = lds4(col + 4), zc = lds4(col + 8);
+  u2c = zb;
+  P2 P[6] = {lo2(za), hi2(za), lo2(zb), hi2(zb), lo2(zc), hi2(zc)};
+  if (ADJ) {
+    const float4 va = lds4(vcol), vb = lds4(vcol + 4), vc = lds4(vcol + 8);
+    const P2 V[6] = {lo2(va), hi2(va), lo2(vb), hi2(vb), lo2(vc), hi2(vc)};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) P[k] = s_mul(p_mul(V[k], V[k]), P[k]);   // (v*v)*u
+  }
+  // Pairs of rows (2k+1, 2k+2) for the odd z offsets.
+  P2 Q[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) Q[k] = p2(P[k].y, P[k + 1].x);
+  P2 tzz[2], txx[2];
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    P2 a = s_mul(c.cz[0], P[2 + p]);
+    a = p_add(a, s_mul(c.cz[1], p_add(Q[2 + p], Q[1 + p])));
+    a = p_add(a, s_mul(c.cz[2], p_add(P[3 + p], P[1 + p])));
+    a = p_add(a, s_mul(c.cz[3], p_add(Q[3 + p], Q[p])));
+    a = p_add(a, s_mul(c.cz[4], p_add(P[4 + p], P[p])));
+    tzz[p] = a;
+    txx[p] = s_mul(c.cx[0], P[2 + p]);
+  }
+#pragma unroll
+  for (int l = 1; l <= 4; ++l) {
+    float4 rp = lds4(col + l * T2_SZ + 4), rm = lds4(col - l * T2_SZ + 4);
+    P2 rp0 = lo2(rp), rp1 = hi2(rp), rm0 = lo2(rm), rm1 = hi2(rm);
+    if (ADJ) {
+      const float4 vp = lds4(vcol + l * T2_SZ + 4), vm = lds4(vcol - l * T2_SZ + 4);
+      const P2 vp0 = lo2(vp), vp1 = hi2(vp), vm0 = lo2(vm), vm1 = hi2(vm);
+      rp0 = s_mul(p_mul(vp0, vp0), rp0);
+      rp1 = s_mul(p_mul(vp1, vp1), rp1);
+      rm0 = s_mul(p_mul(vm0, vm0), rm0);
+      rm1 = s_mul(p_mul(vm1, vm1), rm1);
+    }
+    txx[0] = p_add(txx[0], s_mul(c.cx[l], p_add(rp0, rm0)));
+    txx[1] = p_add(txx[1], s_mul(c.cx[l], p_add(rp1, rm1)));
+  }
+  if (ADJ) {
+    sv[0] = p_add(txx[0], tzz[0]);
+    sv[1] = p_add(txx[1], tzz[1]);
+  } else {
+    const float4 vv = lds4(vcore);
+    const P2 v0 = lo2(vv), v1 = hi2(vv);
+    sv[0] = p_mul(p_mul(v0, v0), p_add(txx[0], tzz[0]));
+    sv[1] = p_mul(p_mul(v1, v1), p_add(txx[1], tzz[1]));
+  }
+}
+
+// Snapshot saving and RTM / LSRTM imaging of one thread's 4 rows of one
+// column (the common snapshot-step work, kept out of the per-element
+// generic path).  cnt is the snapshot counter of the step; u2c the rows'
+// u2 values; vc4 their velocities (LSRTM only).  Same operations as
+// t2_extras: Extraction.f90:562-601, Imaging.f90:265 and 735.
+__device__ __forceinline__ void t2_snap_col(const ShotDev &S, int cnt, int i0, int j,
+                                            const float4 &u2c, const float4 &vc4) {
+  const int nz = S.g.nz;
+  if (j < 1 || j > S.g.nx) return;
+  const long long nphys = (long long)nz * S.g.nx;
+  const long long pc = (long long)nz * (j - 1) - 1;   // pp = pc + i
+  const float u[4] = {u2c.x, u2c.y, u2c.z, u2c.w};
+  if (S.extract_wave && cnt <= S.ntsnap) {
+    float *w = S.wave + (long long)(cnt - 1) * nphys + pc;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (i0 + q >= 1 && i0 + q <= nz) w[i0 + q] = u[q];
+  }
+  if ((S.imaging == 1 || S.imaging == 2) && S.tstep < 0) {
+    const int index = S.ntsnap - cnt + 1;
+    if (index < 1) return;
+    const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
+    const float *w = S.wave + (long long)(index - 1) * nphys + pc;
+    float *im = S.image + pc, *il = S.illum + pc;
+    const float v[4] = {vc4.x, vc4.y, vc4.z, vc4.w};
+    float wsn[4], imv[4], ilv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const bool ok = i0 + q >= 1 && i0 + q <= nz;
+      wsn[q] = ok ? w[i0 + q] : 0.f;
+      imv[q] = ok ? im[i0 + q] : 0.f;
+      ilv[q] = ok ? il[i0 + q] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (i0 + q < 1 || i0 + q > nz) continue;
+      if (S.imaging == 1) imv[q] = imv[q] + (u[q] * wsn[q]) * taper;
+      else imv[q] = imv[q] + (((2.0f * taper) * u[q]) * wsn[q]) / v[q];
+      im[i0 + q] = imv[q];
+      il[i0 + q] = ilv[q] + (wsn[q] * wsn[q]) * taper;
+    }
+  }
+}
+
+// Computes one tile from a completed stage.  Thread (tz, tx) owns rows
+// i0..i0+3 of columns x0+tx and x0+tx+16; both columns are computed together.
 template <bool ADJ>
 __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h, int b, int s,
                                            int e, const float *st) {
@@ -156,136 +275,89 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   const bool inj_tile = h.inj_on && !(zl < h.bi0 || z0 > h.bi1 || xl < h.bj0 || x0 > h.bj1);
   const bool snap_tile = snapstep && (h.extract_wave || h.imaging != 0) &&
                          !(zl < 1 || z0 > h.nz || xl < 1 || x0 > h.nx);
-  const bool clamp_free = !ADJ || (z0 - 4 >= h.nmin1 && zl + 4 <= h.nmax1 &&
-                                   x0 - 4 >= h.nmin2 && xl + 4 <= h.nmax2);
+  // Snapshot saving and RTM / LSRTM imaging take the vectorised path after
+  // the update; injection, Born source and AFWI imaging go element by
+  // element.
+  const bool snap_fast = snap_tile && h.imaging <= 2;
+  const bool snap_slow = snap_tile && !snap_fast;
+  const bool slow_extras = inj_tile || snap_slow;
   const float *su = st;
   const float *svel = st + T2_HALO;                       // adjoint only
   const float *core = st + (ADJ ? 2 : 1) * T2_HALO;
-  float *__restrict__ u3 = const_cast<float *>(h.f[(s + 4) % 5]);
-  const int L = h.ld1;
-  const int rbase = t2_tzi(e) * T2_Z;
+  const T2Pairs c = t2_pairs(h);
+  P2 sv[2][2];
+  float4 u2c[2];
+  // The adjoint reads v at every stencil point with indices clamped to the
+  // compute domain (FDderivatives.f90:863-878).  The padded velocity
+  // replicates the physical model's edge values outwards (k_pad_velocity)
+  // and the compute domain contains the physical one, so the padded value at
+  // any index equals the clamped lookup; no tile needs a special case.
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
     const int jl = tx + 16 * hh;
-    const int j = x0 + jl;
-    if (j > h.nmax2) break;
-    const int sc = jl + 4;                        // staged halo column
-    const float *col = su + sc * T2_SZ + 4 * tz;  // rows i0-4 .. i0+7 start here
-    float sv[4];
-    if (clamp_free) {
-      const float4 za = *reinterpret_cast<const float4 *>(col);
-      const float4 zb = *reinterpret_cast<const float4 *>(col + 4);
-      const float4 zc = *reinterpret_cast<const float4 *>(col + 8);
-      float zr[12] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w, zc.x, zc.y, zc.z, zc.w};
-      if (ADJ) {
-        const float *vcol = svel + sc * T2_SZ + 4 * tz;
-        const float4 va = *reinterpret_cast<const float4 *>(vcol);
-        const float4 vb = *reinterpret_cast<const float4 *>(vcol + 4);
-        const float4 vc4 = *reinterpret_cast<const float4 *>(vcol + 8);
-        const float vr[12] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w,
-                              vc4.x, vc4.y, vc4.z, vc4.w};
-        // w = (v*v)*u at every stencil point (FDderivatives.f90:847-891).
+    const int o = (jl + 4) * T2_SZ + 4 * tz;
+    t2_col_fast<ADJ>(c, su + o, svel + o, core + 3 * T2_CORE + jl * T2_Z + 4 * tz, sv[hh],
+                     u2c[hh]);
+  }
+  if (slow_extras) {
+    const ShotDev &S = t.shots[b];
+    const bool rows_inj = inj_tile && i0 + 3 >= h.bi0 && i0 <= h.bi1;
 #pragma unroll
-        for (int q = 0; q < 12; ++q) zr[q] = (vr[q] * vr[q]) * zr[q];
-      }
-      // FD_2nd_2D_derivatives_scalar_forward_grid (FDderivatives.f90:715-743).
-      float tzz[4], txx[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int m = 4 + q;
-        float a = h.c0z * zr[m];
-        a = a + h.c1z * (zr[m + 1] + zr[m - 1]);
-        a = a + h.c2z * (zr[m + 2] + zr[m - 2]);
-        a = a + h.c3z * (zr[m + 3] + zr[m - 3]);
-        a = a + h.c4z * (zr[m + 4] + zr[m - 4]);
-        tzz[q] = a;
-        txx[q] = h.c0x * zr[m];
-      }
-      const float cx[5] = {h.c0x, h.c1x, h.c2x, h.c3x, h.c4x};
-#pragma unroll
-      for (int l = 1; l <= 4; ++l) {
-        float4 rp = *reinterpret_cast<const float4 *>(col + l * T2_SZ + 4);
-        float4 rm = *reinterpret_cast<const float4 *>(col - l * T2_SZ + 4);
-        if (ADJ) {
-          const float *vcol = svel + sc * T2_SZ + 4 * tz + 4;
-          const float4 vp = *reinterpret_cast<const float4 *>(vcol + l * T2_SZ);
-          const float4 vm = *reinterpret_cast<const float4 *>(vcol - l * T2_SZ);
-          rp = make_float4((vp.x * vp.x) * rp.x, (vp.y * vp.y) * rp.y, (vp.z * vp.z) * rp.z,
-                           (vp.w * vp.w) * rp.w);
-          rm = make_float4((vm.x * vm.x) * rm.x, (vm.y * vm.y) * rm.y, (vm.z * vm.z) * rm.z,
-                           (vm.w * vm.w) * rm.w);
-        }
-        txx[0] = txx[0] + cx[l] * (rp.x + rm.x);
-        txx[1] = txx[1] + cx[l] * (rp.y + rm.y);
-        txx[2] = txx[2] + cx[l] * (rp.z + rm.z);
-        txx[3] = txx[3] + cx[l] * (rp.w + rm.w);
-      }
-      if (ADJ) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) sv[q] = txx[q] + tzz[q];
-      } else {
-        const float4 vv = *reinterpret_cast<const float4 *>(core + 3 * T2_CORE + jl * T2_Z + 4 * tz);
-        sv[0] = (vv.x * vv.x) * (txx[0] + tzz[0]);
-        sv[1] = (vv.y * vv.y) * (txx[1] + tzz[1]);
-        sv[2] = (vv.z * vv.z) * (txx[2] + tzz[2]);
-        sv[3] = (vv.w * vv.w) * (txx[3] + tzz[3]);
-      }
-    } else {
-      // Adjoint tile at an edge of the compute domain: vel indices clamped
-      // element by element (FDderivatives.f90:863-878).
-      auto U = [&](int zi, int xi) { return su[(xi - x0 + 4) * T2_SZ + (zi - z0 + 4)]; };
-      auto W = [&](int zi, int xi) {
-        const int zc = min(max(zi, h.nmin1), h.nmax1), xc = min(max(xi, h.nmin2), h.nmax2);
-        const float v = svel[(xc - x0 + 4) * T2_SZ + (zc - z0 + 4)];
-        return (v * v) * U(zi, xi);
-      };
+    for (int hh = 0; hh < 2; ++hh) {
+      const int jl = tx + 16 * hh, j = x0 + jl;
+      if (j > h.nmax2) continue;
+      const bool col_inj = rows_inj && j >= h.bj0 && j <= h.bj1;
+      if (!col_inj && !snap_slow) continue;
+      float r[4] = {sv[hh][0].x, sv[hh][0].y, sv[hh][1].x, sv[hh][1].y};
+      const float *cc = core + jl * T2_Z + 4 * tz;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int i = i0 + q;
-        float a = h.c0z * W(i, j);
-        a = a + h.c1z * (W(i + 1, j) + W(i - 1, j));
-        a = a + h.c2z * (W(i + 2, j) + W(i - 2, j));
-        a = a + h.c3z * (W(i + 3, j) + W(i - 3, j));
-        a = a + h.c4z * (W(i + 4, j) + W(i - 4, j));
-        float bx = h.c0x * W(i, j);
-        bx = bx + h.c1x * (W(i, j + 1) + W(i, j - 1));
-        bx = bx + h.c2x * (W(i, j + 2) + W(i, j - 2));
-        bx = bx + h.c3x * (W(i, j + 3) + W(i, j - 3));
-        bx = bx + h.c4x * (W(i, j + 4) + W(i, j - 4));
-        sv[q] = bx + a;
+        if (col_inj && i >= h.bi0 && i <= h.bi1) r[q] = t2_inject(S, it, i, j, r[q]);
+        if (snap_slow) {
+          const float vc = ADJ ? svel[(jl + 4) * T2_SZ + 4 * tz + 4 + q] : cc[3 * T2_CORE + q];
+          r[q] = t2_snap_generic(S, it, i, j, r[q], f4get(u2c[hh], q), vc);
+        }
       }
+      sv[hh][0] = p2(r[0], r[1]);
+      sv[hh][1] = p2(r[2], r[3]);
     }
-    const float4 u2c = *reinterpret_cast<const float4 *>(col + 4);
+  }
+  // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
+  float *__restrict__ u3 = const_cast<float *>(h.f[(s + 4) % 5]);
+  const int rbase = t2_tzi(e) * T2_Z;
+#pragma unroll
+  for (int hh = 0; hh < 2; ++hh) {
+    const int jl = tx + 16 * hh, j = x0 + jl;
     const float *cc = core + jl * T2_Z + 4 * tz;
-    if (inj_tile || snap_tile) {
-      const ShotDev &S = t.shots[b];
+    const float4 a1 = lds4(cc), a0 = lds4(cc + T2_CORE), am = lds4(cc + 2 * T2_CORE);
+    P2 o[2];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float vc = ADJ ? svel[(jl + 4) * T2_SZ + 4 * tz + 4 + q] : cc[3 * T2_CORE + q];
-        sv[q] = t2_extras(S, it, snap_tile, i0 + q, j, sv[q], f4get(u2c, q), vc);
-      }
+    for (int p = 0; p < 2; ++p) {
+      const P2 u = p ? hi2(u2c[hh]) : lo2(u2c[hh]);
+      P2 a = s_mul(20.0f, u);
+      a = p_sub(a, s_mul(6.0f, p ? hi2(a1) : lo2(a1)));
+      a = p_sub(a, s_mul(4.0f, p ? hi2(a0) : lo2(a0)));
+      a = p_add(a, p ? hi2(am) : lo2(am));
+      a = p_add(a, s_mul(c.k12, sv[hh][p]));
+      o[p] = p_mul(a, c.div11);
     }
-    // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
-    const float4 a1 = *reinterpret_cast<const float4 *>(cc);
-    const float4 a0 = *reinterpret_cast<const float4 *>(cc + T2_CORE);
-    const float4 am = *reinterpret_cast<const float4 *>(cc + 2 * T2_CORE);
-    float o[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      float a = 20.0f * f4get(u2c, q);
-      a = a - 6.0f * f4get(a1, q);
-      a = a - 4.0f * f4get(a0, q);
-      a = a + f4get(am, q);
-      a = a + h.k12 * sv[q];
-      o[q] = a * h.div11;
+    if (j > h.nmax2) continue;
+    if (snap_fast) {
+      const int cnt = h.tstep > 0 ? it / h.snapi - (h.tmin - 1) / h.snapi
+                                  : h.tmin / h.snapi - (it - 1) / h.snapi;
+      const float4 vc4 = ADJ ? lds4(svel + (jl + 4) * T2_SZ + 4 * tz + 4)
+                             : lds4(cc + 3 * T2_CORE);
+      t2_snap_col(t.shots[b], cnt, i0, j, u2c[hh], vc4);
     }
-    const int off = (rbase + 4 + 4 * tz) + L * (j - h.lo2);
+    const int off = (rbase + 4 + 4 * tz) + h.ld1 * (j - h.lo2);
     if (i0 + 3 <= h.nmax1) {
-      *reinterpret_cast<float4 *>(u3 + off) = make_float4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<float4 *>(u3 + off) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
     } else {
+      const float ov[4] = {o[0].x, o[0].y, o[1].x, o[1].y};
 #pragma unroll
       for (int q = 0; q < 4; ++q)
-        if (i0 + q <= h.nmax1) u3[off + q] = o[q];
+        if (i0 + q <= h.nmax1) u3[off + q] = ov[q];
     }
   }
 }
