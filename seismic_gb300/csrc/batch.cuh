@@ -9,6 +9,8 @@
 // replayed.
 #pragma once
 
+#include <cuda.h>
+
 #include "swave_dev.cuh"
 
 namespace swave {
@@ -57,6 +59,13 @@ struct T2Shot {
 // Largest batch the pipelined 2D kernel accepts (its shot table is shared).
 constexpr int T2_MAX_SHOTS = 64;
 
+// Tensor maps of one shot for the pipelined 2D kernel: [2*buf + box] with
+// buf 0..4 the time-level buffers and 5 the padded velocity, box 0 the
+// 72 x 40 halo tile and 1 the 64 x 32 core tile.
+struct T2Maps {
+  CUtensorMap m[12];
+};
+
 // Prefix tables of a batch (device resident).
 struct BatchTables {
   int nshots;
@@ -70,6 +79,8 @@ struct BatchTables {
   const T2Shot *t2shots;  // nshots compact views (pipelined 2D kernel)
   const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
   const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
+  const T2Maps *t2maps;   // nshots tensor-map sets (pipelined 2D kernel)
+  int *err;               // device error flags (bit 0: a bounded wait gave up)
   int *counter;           // step counter s (0-based)
 };
 

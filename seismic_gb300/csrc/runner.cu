@@ -10,12 +10,44 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "batch.cuh"
 #include "engine.h"
 
 namespace swave {
 
 namespace {
+
+// cuTensorMapEncodeTiled from the driver, looked up once.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2D FP32 tensor map over a padded field (ld1 rows x n2p columns) with a
+// box of bz rows x bx columns; out-of-range elements read as zero.
+bool encode_field_map(CUtensorMap *m, const float *base, const Geom &g, int bz, int bx) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)g.ld1, (cuuint64_t)g.n2p};
+  const cuuint64_t strides[1] = {(cuuint64_t)g.ld1 * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)bz, (cuuint32_t)bx};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 template <class T>
 T *carve(char *&cur, size_t n) {
@@ -87,8 +119,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   if (t2) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
-    bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int));
+    bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int)) + rup(nb * sizeof(T2Maps));
   }
+  bytes += rup(sizeof(int));   // error flags
   char *arena = (char *)dbuf(c, "batch_arena", bytes, &st);
   if (!arena) return st;
   char *cur = arena;
@@ -213,8 +246,10 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // kernel.
   std::vector<T2Shot> h2(t2 ? nb : 0);
   std::vector<int> htile;
+  std::vector<T2Maps> hmaps;
   T2Shot *d2 = nullptr;
   int *dtile = nullptr;
+  T2Maps *dmaps = nullptr;
   if (t2) {
     for (int b = 0; b < nb; ++b) {
       const ShotDev &S = hs[b];
@@ -238,13 +273,27 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         for (int zi = 0; zi < n1t; ++zi) htile.push_back((b << 24) | (zi << 12) | xi);
     }
     if ((int)htile.size() != step_tiles[nb]) return fail(c, SW_CUDA_ERR, "tile table size");
+    hmaps.resize(nb);
+    for (int b = 0; b < nb; ++b) {
+      const ShotDev &S = hs[b];
+      for (int q = 0; q < 6; ++q) {
+        const float *base = q < 5 ? S.f[q] : S.vel;
+        if (!encode_field_map(&hmaps[b].m[2 * q], base, S.g, 72, 40) ||
+            !encode_field_map(&hmaps[b].m[2 * q + 1], base, S.g, 64, 32))
+          return fail(c, SW_CUDA_ERR, "tensor map encoding failed (shot %d)", b);
+      }
+    }
     d2 = carve<T2Shot>(cur, nb);
     dtile = carve<int>(cur, htile.size());
+    dmaps = carve<T2Maps>(cur, nb);
+    SW_CK(cudaMemcpyAsync(dmaps, hmaps.data(), nb * sizeof(T2Maps), cudaMemcpyHostToDevice, s));
     SW_CK(cudaMemcpyAsync(d2, h2.data(), nb * sizeof(T2Shot), cudaMemcpyHostToDevice, s));
     SW_CK(cudaMemcpyAsync(dtile, htile.data(), htile.size() * sizeof(int), cudaMemcpyHostToDevice,
                           s));
   }
   SW_CK(cudaMemsetAsync(counter, 0, sizeof(int), s));
+  int *derr = carve<int>(cur, 1);
+  SW_CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
   if ((size_t)(cur - arena) > bytes) return fail(c, SW_CUDA_ERR, "arena overflow");
   BatchTables t;
   t.nshots = nb;
@@ -258,6 +307,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.edge_start = dtab[6];
   t.t2shots = d2;
   t.tile_tab = dtile;
+  t.t2maps = dmaps;
+  t.err = derr;
   t.counter = counter;
   // The host plans above must stay alive until the uploads complete.
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch setup");
@@ -416,7 +467,12 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                           (size_t)G[b].n2p * G[b].n3p, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "download u2");
   }
+  int herr = 0;
+  SW_CK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch run");
+  if (herr)
+    return fail(c, SW_CUDA_ERR, "step kernel gave up waiting for a tile copy (error flags %d)",
+                herr);
   return SW_OK;
 }
 

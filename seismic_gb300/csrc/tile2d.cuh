@@ -33,59 +33,90 @@ template <bool ADJ>
 __host__ __device__ constexpr int t2_stage_floats() {
   return ADJ ? 2 * T2_HALO + 3 * T2_CORE : T2_HALO + 4 * T2_CORE;
 }
-// Dynamic shared memory: two stages, the shot table and the tile list.
+// Per-step scalars of one shot, computed once per CTA and launch.
+struct T2Step {
+  int it;        // time sample of the step
+  int cnt;       // snapshot counter of the step
+  int live;      // the shot steps in this launch with this stencil variant
+  int snap;      // snapshot step with snapshot or imaging work
+};
+
+// Dynamic shared memory: two stages, the shot table, the per-step scalars,
+// the tile list and two mbarriers.
 template <bool ADJ>
 __host__ __device__ constexpr size_t t2_smem_bytes() {
   return 2 * sizeof(float) * t2_stage_floats<ADJ>() + sizeof(T2Shot) * T2_MAX_SHOTS +
-         sizeof(int) * (T2_MAX_TILES_PER_CTA + 4);
+         sizeof(T2Step) * T2_MAX_SHOTS + sizeof(int) * (T2_MAX_TILES_PER_CTA + 8) + 64;
 }
 
-__device__ __forceinline__ void cp_async16(float *smem, const float *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
 }
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
 }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for a phase of an mbarrier: false after T2_WAIT_LIMIT polls
+// (each poll may suspend the thread for a while), so a copy that never
+// completes ends the kernel with an error status instead of a hang.
+constexpr int T2_WAIT_LIMIT = 1 << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  for (int q = 0; q < T2_WAIT_LIMIT; ++q)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// 2D tensor copy global -> shared memory, completing on an mbarrier.
+__device__ __forceinline__ void tma_2d(float *dst, const CUtensorMap *map, int x, int y,
+                                       unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __device__ __forceinline__ int t2_b(int e) { return e >> 24; }
 __device__ __forceinline__ int t2_tzi(int e) { return (e >> 12) & 0xfff; }
 __device__ __forceinline__ int t2_txi(int e) { return e & 0xfff; }
 
-// Issues the cp.async copies of one tile into a stage.
+// Issues the tensor copies of one tile into a stage (one thread).  Tensor
+// map 2*buf+0 has the 72 x 40 halo box, 2*buf+1 the 64 x 32 core box; buf
+// 0..4 are the shot's time-level buffers, 5 its velocity.  Halo coordinates
+// start at row z0-4 and column x0-4 of the padded array (which starts 4
+// cells before the compute domain); elements outside the array read 0 and
+// only feed outputs that are never stored.
 template <bool ADJ>
-__device__ __forceinline__ void t2_issue(const T2Shot &h, int s, int e, float *st) {
-  const float *u2 = h.f[(s + 3) % 5];
-  const int L = h.ld1;
-  const int jmaxp = h.lo2 + h.n2p - 1;
-  const int rbase = t2_tzi(e) * T2_Z;   // row offset of z0-4 inside a column
-  const int x0 = h.nmin2 + t2_txi(e) * T2_X;
-  const int tid = threadIdx.x;
-  // Halo tiles: 40 columns x 18 float4.
-  for (int q = tid; q < T2_SX * (T2_SZ / 4); q += 256) {
-    const int col = q / (T2_SZ / 4), grp = q - col * (T2_SZ / 4);
-    const int j = min(x0 - 4 + col, jmaxp);
-    const int off = min(rbase + 4 * grp, L - 4) + L * (j - h.lo2);
-    cp_async16(st + col * T2_SZ + 4 * grp, u2 + off);
-    if (ADJ) cp_async16(st + T2_HALO + col * T2_SZ + 4 * grp, h.vel + off);
-  }
-  // Core tiles: 32 columns x 16 float4, rows z0..z0+63.
-  const float *c0 = h.f[(s + 2) % 5], *c1 = h.f[(s + 1) % 5], *c2 = h.f[s % 5];
+__device__ __forceinline__ void t2_issue(const T2Maps &M, int s, int e, float *st,
+                                         unsigned long long *bar) {
+  constexpr unsigned bytes = 4u * (unsigned)t2_stage_floats<ADJ>();
+  const int zi = t2_tzi(e) * T2_Z, xi = t2_txi(e) * T2_X;
+  mbar_expect_tx(bar, bytes);
+  tma_2d(st, &M.m[2 * ((s + 3) % 5)], zi, xi, bar);
+  if (ADJ) tma_2d(st + T2_HALO, &M.m[10], zi, xi, bar);
   float *cst = st + (ADJ ? 2 : 1) * T2_HALO;
-  for (int q = tid; q < T2_X * (T2_Z / 4); q += 256) {
-    const int col = q / (T2_Z / 4), grp = q - col * (T2_Z / 4);
-    const int j = min(x0 + col, jmaxp);
-    const int off = min(rbase + 4 + 4 * grp, L - 4) + L * (j - h.lo2);
-    float *d = cst + col * T2_Z + 4 * grp;
-    cp_async16(d, c0 + off);
-    cp_async16(d + T2_CORE, c1 + off);
-    cp_async16(d + 2 * T2_CORE, c2 + off);
-    if (!ADJ) cp_async16(d + 3 * T2_CORE, h.vel + off);
-  }
+  tma_2d(cst, &M.m[2 * ((s + 2) % 5) + 1], zi + 4, xi + 4, bar);
+  tma_2d(cst + T2_CORE, &M.m[2 * ((s + 1) % 5) + 1], zi + 4, xi + 4, bar);
+  tma_2d(cst + 2 * T2_CORE, &M.m[2 * (s % 5) + 1], zi + 4, xi + 4, bar);
+  if (!ADJ) tma_2d(cst + 3 * T2_CORE, &M.m[11], zi + 4, xi + 4, bar);
 }
 
 __device__ __forceinline__ float f4get(const float4 &a, int e) {
@@ -261,20 +292,19 @@ __device__ __forceinline__ void t2_snap_col(const ShotDev &S, int cnt, int i0, i
 // Computes one tile from a completed stage.  Thread (tz, tx) owns rows
 // i0..i0+3 of columns x0+tx and x0+tx+16; both columns are computed together.
 template <bool ADJ>
-__device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h, int b, int s,
-                                           int e, const float *st) {
+__device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h,
+                                           const T2Step &stp, int b, int s, int e,
+                                           const float *st) {
   const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
   const int tid = threadIdx.x;
   const int tz = tid & 15, tx = tid >> 4;
   const int i0 = z0 + 4 * tz;
   if (i0 > h.nmax1) return;
-  const int it = h.tmin + s * h.tstep;
-  const bool snapstep = (it % h.snapi) == 0;
+  const int it = stp.it;
   // Tile-level decisions.
   const int zl = z0 + T2_Z - 1, xl = x0 + T2_X - 1;
   const bool inj_tile = h.inj_on && !(zl < h.bi0 || z0 > h.bi1 || xl < h.bj0 || x0 > h.bj1);
-  const bool snap_tile = snapstep && (h.extract_wave || h.imaging != 0) &&
-                         !(zl < 1 || z0 > h.nz || xl < 1 || x0 > h.nx);
+  const bool snap_tile = stp.snap && !(zl < 1 || z0 > h.nz || xl < 1 || x0 > h.nx);
   // Snapshot saving and RTM / LSRTM imaging take the vectorised path after
   // the update; injection, Born source and AFWI imaging go element by
   // element.
@@ -344,8 +374,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
     }
     if (j > h.nmax2) continue;
     if (snap_fast) {
-      const int cnt = h.tstep > 0 ? it / h.snapi - (h.tmin - 1) / h.snapi
-                                  : h.tmin / h.snapi - (it - 1) / h.snapi;
+      const int cnt = stp.cnt;
       const float4 vc4 = ADJ ? lds4(svel + (jl + 4) * T2_SZ + 4 * tz + 4)
                              : lds4(cc + 3 * T2_CORE);
       t2_snap_col(t.shots[b], cnt, i0, j, u2c[hh], vc4);
@@ -364,12 +393,15 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
 
 template <bool ADJ>
 __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_off, int n_tiles) {
-  extern __shared__ __align__(16) float t2_smem[];
-  float *stage0 = t2_smem;
-  float *stage1 = t2_smem + t2_stage_floats<ADJ>();
+  extern __shared__ __align__(128) float t2_smem[];
+  constexpr int SF = t2_stage_floats<ADJ>();
   T2Shot *shots = reinterpret_cast<T2Shot *>(t2_smem + 2 * t2_stage_floats<ADJ>());
-  int *list = reinterpret_cast<int *>(shots + T2_MAX_SHOTS);
+  T2Step *steps = reinterpret_cast<T2Step *>(shots + T2_MAX_SHOTS);
+  int *list = reinterpret_cast<int *>(steps + T2_MAX_SHOTS);
   int *nlist = list + T2_MAX_TILES_PER_CTA;
+  int *abort_flag = nlist + 1;
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<char *>(t2_smem) + t2_smem_bytes<ADJ>() - 64);
   const int tid = threadIdx.x;
   const int s = *t.counter + s_off;
   // Shot table and this CTA's tile list into shared memory.
@@ -380,6 +412,23 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     for (int q = tid; q < nw; q += 256) dst[q] = src[q];
     for (int k = tid; blockIdx.x + k * gridDim.x < n_tiles && k < T2_MAX_TILES_PER_CTA; k += 256)
       list[k] = t.tile_tab[blockIdx.x + k * gridDim.x];
+    if (tid == 0) {
+      mbar_init(&full[0], 1);
+      mbar_init(&full[1], 1);
+      mbar_fence_init();
+      *abort_flag = 0;
+    }
+  }
+  __syncthreads();
+  if (tid < t.nshots) {
+    const T2Shot &h = shots[tid];
+    T2Step st;
+    st.live = s < h.nsteps && (h.adj2d != 0) == ADJ;
+    st.it = h.tmin + s * h.tstep;
+    st.snap = (st.it % h.snapi) == 0 && (h.extract_wave || h.imaging != 0);
+    st.cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
+                         : h.tmin / h.snapi - (st.it - 1) / h.snapi;
+    steps[tid] = st;
   }
   __syncthreads();
   if (tid == 0) {
@@ -387,28 +436,37 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     int n = 0;
     for (int k = 0; blockIdx.x + k * gridDim.x < n_tiles && k < T2_MAX_TILES_PER_CTA; ++k) {
       const int e = list[k];
-      const T2Shot &h = shots[t2_b(e)];
-      if (s < h.nsteps && (h.adj2d != 0) == ADJ) list[n++] = e;
+      if (steps[t2_b(e)].live) list[n++] = e;
     }
     *nlist = n;
+    if (n > 0) t2_issue<ADJ>(t.t2maps[t2_b(list[0])], s, list[0], t2_smem, &full[0]);
   }
   __syncthreads();
   const int n = *nlist;
-  if (n == 0) return;
-  t2_issue<ADJ>(shots[t2_b(list[0])], s, list[0], stage0);
-  cp_async_commit();
   for (int k = 0; k < n; ++k) {
-    float *cur = (k & 1) ? stage1 : stage0;
-    float *nxt = (k & 1) ? stage0 : stage1;
-    if (k + 1 < n) t2_issue<ADJ>(shots[t2_b(list[k + 1])], s, list[k + 1], nxt);
-    cp_async_commit();
-    cp_async_wait<1>();    // the current tile's group has landed
-    __syncthreads();
-    const int e = list[k];
-    t2_compute<ADJ>(t, shots[t2_b(e)], t2_b(e), s, e, cur);
-    __syncthreads();       // the stage is free for the tile after next
+    const int cur = k & 1;
+    // The other stage was released by the barrier that ended tile k-1.
+    if (tid == 0 && k + 1 < n)
+      t2_issue<ADJ>(t.t2maps[t2_b(list[k + 1])], s, list[k + 1], t2_smem + (cur ^ 1) * SF,
+                    &full[cur ^ 1]);
+    if (mbar_wait(&full[cur], (unsigned)((k >> 1) & 1))) {
+      const int e = list[k];
+      t2_compute<ADJ>(t, shots[t2_b(e)], steps[t2_b(e)], t2_b(e), s, e, t2_smem + cur * SF);
+    } else {
+      atomicOr(t.err, 1);
+      *abort_flag = 1;
+    }
+    __syncthreads();   // the stage is free for tile k+2
+    if (*abort_flag) {
+      // Wait (bounded) for the copies still in flight so that no tensor
+      // copy lands in the shared memory of a finished CTA.
+      if (tid == 0) {
+        mbar_wait(&full[cur], (unsigned)((k >> 1) & 1));
+        if (k + 1 < n) mbar_wait(&full[cur ^ 1], (unsigned)(((k + 1) >> 1) & 1));
+      }
+      break;
+    }
   }
-  cp_async_wait<0>();
 }
 
 }  // namespace swave
