@@ -26,7 +26,7 @@ constexpr int T2_SZ = T2_Z + 8;          // staged column length (with halo)
 constexpr int T2_SX = T2_X + 8;          // staged columns (with halo)
 constexpr int T2_HALO = T2_SX * T2_SZ;   // 2880 floats
 constexpr int T2_CORE = T2_X * T2_Z;     // 2048 floats
-constexpr int T2_MAX_TILES_PER_CTA = 512;
+constexpr int T2_MAX_TILES_PER_CTA = 384;
 
 // Floats of one pipeline stage.
 template <bool ADJ>
@@ -35,10 +35,23 @@ __host__ __device__ constexpr int t2_stage_floats() {
 }
 // Per-step scalars of one shot, computed once per CTA and launch.
 struct T2Step {
-  int it;        // time sample of the step
-  int cnt;       // snapshot counter of the step
-  int live;      // the shot steps in this launch with this stencil variant
-  int snap;      // snapshot step with snapshot or imaging work
+  int it;              // time sample of the step
+  int live;            // the shot steps in this launch with this stencil variant
+  int snap;            // snapshot step with snapshot or imaging work
+  int extract;         // save the snapshot this step
+  int img;             // RTM (1) or LSRTM (2) imaging this step, else 0
+  int pad_;
+  float *wsave;        // snapshot slot written this step
+  const float *wimg;   // snapshot slot read by the imaging
+  float *image, *illum;
+  const float *taperx; // null: no taper
+  float tapery0;
+};
+
+// One thread's imaging inputs for a tile (2 columns x 4 rows), loaded before
+// the tile's stage is waited for so that their latency overlaps the wait.
+struct T2Img {
+  float w[2][4], im[2][4], il[2][4];
 };
 
 // Dynamic shared memory: two stages, the shot table, the per-step scalars,
@@ -245,46 +258,75 @@ __device__ __forceinline__ void t2_col_fast(const T2Pairs &c, const float *col, 
   }
 }
 
-// Snapshot saving and RTM / LSRTM imaging of one thread's 4 rows of one
-// column (the common snapshot-step work, kept out of the per-element
-// generic path).  cnt is the snapshot counter of the step; u2c the rows'
-// u2 values; vc4 their velocities (LSRTM only).  Same operations as
-// t2_extras: Extraction.f90:562-601, Imaging.f90:265 and 735.
-__device__ __forceinline__ void t2_snap_col(const ShotDev &S, int cnt, int i0, int j,
-                                            const float4 &u2c, const float4 &vc4) {
-  const int nz = S.g.nz;
-  if (j < 1 || j > S.g.nx) return;
-  const long long nphys = (long long)nz * S.g.nx;
-  const long long pc = (long long)nz * (j - 1) - 1;   // pp = pc + i
-  const float u[4] = {u2c.x, u2c.y, u2c.z, u2c.w};
-  if (S.extract_wave && cnt <= S.ntsnap) {
-    float *w = S.wave + (long long)(cnt - 1) * nphys + pc;
+// Whether a tile overlaps the physical domain.
+__device__ __forceinline__ bool t2_phys_tile(const T2Shot &h, int e) {
+  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  return !(z0 + T2_Z - 1 < 1 || z0 > h.nz || x0 + T2_X - 1 < 1 || x0 > h.nx);
+}
+
+// Physical-domain tests of one thread's rows and columns.
+__device__ __forceinline__ bool t2_row_ok(const T2Shot &h, int i) { return i >= 1 && i <= h.nz; }
+__device__ __forceinline__ bool t2_col_ok(const T2Shot &h, int j) { return j >= 1 && j <= h.nx; }
+
+// Snapshot and imaging work use a row mapping of their own: thread (tz, tx)
+// handles rows z0+tz+16m (m = 0..3) of columns x0+tx and x0+tx+16, so that
+// every global load and store of a warp covers 16 consecutive floats of a
+// column.  Their inputs (u2 and the velocity) are read from the staged tile.
+
+// Loads the snapshot, image and illumination values of a thread's elements
+// for an imaging step (zeros outside the physical domain).
+__device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, int e, T2Img &P) {
+  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (i0 + q >= 1 && i0 + q <= nz) w[i0 + q] = u[q];
-  }
-  if ((S.imaging == 1 || S.imaging == 2) && S.tstep < 0) {
-    const int index = S.ntsnap - cnt + 1;
-    if (index < 1) return;
-    const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
-    const float *w = S.wave + (long long)(index - 1) * nphys + pc;
-    float *im = S.image + pc, *il = S.illum + pc;
-    const float v[4] = {vc4.x, vc4.y, vc4.z, vc4.w};
-    float wsn[4], imv[4], ilv[4];
+  for (int hh = 0; hh < 2; ++hh) {
+    const int j = x0 + tx + 16 * hh;
+    const long long pc = (long long)h.nz * (j - 1) - 1;   // pp = pc + i
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool ok = i0 + q >= 1 && i0 + q <= nz;
-      wsn[q] = ok ? w[i0 + q] : 0.f;
-      imv[q] = ok ? im[i0 + q] : 0.f;
-      ilv[q] = ok ? il[i0 + q] : 0.f;
+    for (int m = 0; m < 4; ++m) {
+      const int i = z0 + tz + 16 * m;
+      const bool ok = t2_col_ok(h, j) && t2_row_ok(h, i);
+      P.w[hh][m] = ok ? stp.wimg[pc + i] : 0.f;
+      P.im[hh][m] = ok ? stp.image[pc + i] : 0.f;
+      P.il[hh][m] = ok ? stp.illum[pc + i] : 0.f;
     }
+  }
+}
+
+// Snapshot saving (Extraction.f90:562-601) and RTM / LSRTM imaging
+// (Imaging.f90:265 and 735) of a thread's elements; su and svel are the
+// staged u2 and velocity halo tiles (svel only for the adjoint stencil, the
+// variant the imaging runs with).  The operations are those of the
+// element-by-element path.
+template <bool ADJ>
+__device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp, const T2Img &P,
+                                             int e, const float *su, const float *svel) {
+  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (i0 + q < 1 || i0 + q > nz) continue;
-      if (S.imaging == 1) imv[q] = imv[q] + (u[q] * wsn[q]) * taper;
-      else imv[q] = imv[q] + (((2.0f * taper) * u[q]) * wsn[q]) / v[q];
-      im[i0 + q] = imv[q];
-      il[i0 + q] = ilv[q] + (wsn[q] * wsn[q]) * taper;
+  for (int hh = 0; hh < 2; ++hh) {
+    const int jl = tx + 16 * hh, j = x0 + jl;
+    if (!t2_col_ok(h, j)) continue;
+    const long long pc = (long long)h.nz * (j - 1) - 1;
+    const float taper = stp.taperx ? stp.taperx[j - 1] * stp.tapery0 : 1.f;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const int r = tz + 16 * m, i = z0 + r;
+      if (!t2_row_ok(h, i)) continue;
+      const float u = su[(jl + 4) * T2_SZ + 4 + r];
+      if (stp.extract) stp.wsave[pc + i] = u;
+      if (stp.img) {
+        const float wsn = P.w[hh][m];
+        float im = P.im[hh][m];
+        if (stp.img == 1) {
+          im = im + (u * wsn) * taper;
+        } else {
+          const float v = ADJ ? svel[(jl + 4) * T2_SZ + 4 + r] : 1.f;
+          im = im + (((2.0f * taper) * u) * wsn) / v;
+        }
+        stp.image[pc + i] = im;
+        stp.illum[pc + i] = P.il[hh][m] + (wsn * wsn) * taper;
+      }
     }
   }
 }
@@ -304,7 +346,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   // Tile-level decisions.
   const int zl = z0 + T2_Z - 1, xl = x0 + T2_X - 1;
   const bool inj_tile = h.inj_on && !(zl < h.bi0 || z0 > h.bi1 || xl < h.bj0 || x0 > h.bj1);
-  const bool snap_tile = stp.snap && !(zl < 1 || z0 > h.nz || xl < 1 || x0 > h.nx);
+  const bool snap_tile = stp.snap && t2_phys_tile(h, e);
   // Snapshot saving and RTM / LSRTM imaging take the vectorised path after
   // the update; injection, Born source and AFWI imaging go element by
   // element.
@@ -373,12 +415,6 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
       o[p] = p_mul(a, c.div11);
     }
     if (j > h.nmax2) continue;
-    if (snap_fast) {
-      const int cnt = stp.cnt;
-      const float4 vc4 = ADJ ? lds4(svel + (jl + 4) * T2_SZ + 4 * tz + 4)
-                             : lds4(cc + 3 * T2_CORE);
-      t2_snap_col(t.shots[b], cnt, i0, j, u2c[hh], vc4);
-    }
     const int off = (rbase + 4 + 4 * tz) + h.ld1 * (j - h.lo2);
     if (i0 + 3 <= h.nmax1) {
       *reinterpret_cast<float4 *>(u3 + off) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
@@ -422,12 +458,25 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
   __syncthreads();
   if (tid < t.nshots) {
     const T2Shot &h = shots[tid];
+    const ShotDev &S = t.shots[tid];
     T2Step st;
     st.live = s < h.nsteps && (h.adj2d != 0) == ADJ;
     st.it = h.tmin + s * h.tstep;
     st.snap = (st.it % h.snapi) == 0 && (h.extract_wave || h.imaging != 0);
-    st.cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
-                         : h.tmin / h.snapi - (st.it - 1) / h.snapi;
+    const int cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
+                                : h.tmin / h.snapi - (st.it - 1) / h.snapi;
+    const long long nphys = (long long)h.nz * h.nx;
+    st.extract = st.snap && h.extract_wave && cnt <= S.ntsnap && h.imaging <= 2;
+    st.wsave = st.extract ? S.wave + (long long)(cnt - 1) * nphys : nullptr;
+    const int index = S.ntsnap - cnt + 1;
+    st.img = (st.snap && (h.imaging == 1 || h.imaging == 2) && h.tstep < 0 && index >= 1)
+                 ? h.imaging : 0;
+    st.wimg = st.img ? S.wave + (long long)(index - 1) * nphys : nullptr;
+    st.image = S.image;
+    st.illum = S.illum;
+    st.taperx = S.taperx;
+    st.tapery0 = S.taperx ? S.tapery[0] : 1.f;
+    st.pad_ = 0;
     steps[tid] = st;
   }
   __syncthreads();
@@ -449,9 +498,16 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     if (tid == 0 && k + 1 < n)
       t2_issue<ADJ>(t.t2maps[t2_b(list[k + 1])], s, list[k + 1], t2_smem + (cur ^ 1) * SF,
                     &full[cur ^ 1]);
+    const int e = list[k];
+    const T2Shot &h = shots[t2_b(e)];
+    const T2Step &stp = steps[t2_b(e)];
+    T2Img P;
+    if (stp.img && t2_phys_tile(h, e)) t2_img_load(h, stp, e, P);
     if (mbar_wait(&full[cur], (unsigned)((k >> 1) & 1))) {
-      const int e = list[k];
-      t2_compute<ADJ>(t, shots[t2_b(e)], steps[t2_b(e)], t2_b(e), s, e, t2_smem + cur * SF);
+      const float *st = t2_smem + cur * SF;
+      t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st);
+      if ((stp.extract || stp.img) && t2_phys_tile(h, e))
+        t2_snap_tile<ADJ>(h, stp, P, e, st, st + T2_HALO);
     } else {
       atomicOr(t.err, 1);
       *abort_flag = 1;
