@@ -487,6 +487,10 @@ __global__ void __launch_bounds__(256, 2) k_bstep2d_t(BatchTables t, int s_off, 
   tile2d_persistent<ADJ>(t, s_off, n_tiles);
 }
 
+// Two CTAs per SM: 228 KB of shared memory per SM, 1 KB reserved per CTA.
+static_assert(2 * (t2_smem_bytes<false>() + 1024) <= 228 * 1024, "tile kernel smem (fwd)");
+static_assert(2 * (t2_smem_bytes<true>() + 1024) <= 228 * 1024, "tile kernel smem (adj)");
+
 template <bool ADJ>
 static cudaError_t launch_tile2d(const BatchTables &t, int s_off, int n_tiles, int nsm,
                                  cudaStream_t s) {
@@ -574,7 +578,9 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     ++nl;
   }
   if (ev_after) cudaEventRecordWithFlags(ev_after, s, cudaEventRecordExternal);
-  if (!has_3d && tile.fused_edges) {
+  if (!has_3d && tile.stream2d == 2) {
+    // The pipelined 2D kernel applies the Higdon edges itself.
+  } else if (!has_3d && tile.fused_edges) {
     k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   } else {

@@ -51,10 +51,39 @@ struct ShotDev {
 struct T2Shot {
   const float *f[5];
   const float *vel;
+  const float *gz, *gx;   // Higdon coefficients (z and x edges)
   float c0z, c1z, c2z, c3z, c4z, c0x, c1x, c2x, c3x, c4x, k12, div11;
   int ld1, lo2, n2p, nmin1, nmax1, nmin2, nmax2, nz, nx;
   int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
+  int off1, off2;         // tile origin: nmin1 - off1, nmin2 - off2
+  int ntz, ntx;           // tiles along z and x
 };
+
+// Tile origin of the pipelined 2D kernel.  Tiles of 64 rows x 32 columns
+// start off1 rows before nmin1 and off2 columns before nmin2, chosen so that
+// the first and last tile along each axis own at least 6 rows (columns) of
+// the compute domain and stage the 4 padding cells beyond it: then every
+// Higdon edge line lies inside one tile and the tile can apply it.  off1 is
+// a multiple of 4 (tensor-copy row coordinates must be 16-byte aligned).
+// Returns false when the domain is too small (n1 or n2 below 16).
+inline bool t2_origin(int n1, int n2, int *off1, int *off2, int *ntz, int *ntx) {
+  if (n1 < 16 || n2 < 16) return false;
+  int a = -1, b = -1;
+  for (int o = 4; o <= 56 && a < 0; o += 4) {
+    const int nt = (n1 + o + 63) / 64, r = n1 + o - 64 * (nt - 1);
+    if (r >= 6 && r <= 60) a = o;
+  }
+  for (int o = 4; o <= 26 && b < 0; ++o) {
+    const int nt = (n2 + o + 31) / 32, r = n2 + o - 32 * (nt - 1);
+    if (r >= 6 && r <= 28) b = o;
+  }
+  if (a < 0 || b < 0) return false;
+  *off1 = a;
+  *off2 = b;
+  *ntz = (n1 + a + 63) / 64;
+  *ntx = (n2 + b + 31) / 32;
+  return true;
+}
 
 // Largest batch the pipelined 2D kernel accepts (its shot table is shared).
 constexpr int T2_MAX_SHOTS = 64;
@@ -116,7 +145,10 @@ inline int edge_threads_2d(const Geom &g) {
 // Number of fused-step CTAs a shot needs with this tile shape.
 inline int step_ctas(const Geom &g, const StepTile &tile) {
   const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
-  if (g.twoD && tile.stream2d == 2) return ((n1 + 63) / 64) * ((n2 + 31) / 32);
+  if (g.twoD && tile.stream2d == 2) {
+    int o1, o2, nz, nx;
+    return t2_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;
+  }
   if (g.twoD && tile.stream2d) return ((n1 + tile.tz - 1) / tile.tz) * ((n2 + tile.tx - 1) / tile.tx);
   if (!g.twoD && tile.stream3d)
     return ((n1 + 31) / 32) * ((n2 + 15) / 16) * ((n3 + tile.ty - 1) / tile.ty);

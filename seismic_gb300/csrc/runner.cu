@@ -72,14 +72,17 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   std::vector<std::vector<float>> tx(nb), ty(nb);
   bool has_3d = false, has_adj3d = false, has_ext = false;
   // The pipelined 2D kernel keeps the batch's shot table in shared memory
-  // and packs tile coordinates into 12 bits each; larger batches or grids
-  // use the streaming kernel.
+  // and packs tile coordinates into 12 bits each; larger batches, grids
+  // beyond that or domains below 16 cells use the streaming kernel.
   StepTile tile = opt.tile;
   if (tile.stream2d == 2) {
     bool fits = nb <= T2_MAX_SHOTS;
     for (int b = 0; b < nb && fits; ++b) {
       const Geom g = make_geom(shots[b].d.g);
-      fits = (g.nmax1 - g.nmin1 + 1) <= 64 * 4095 && (g.nmax2 - g.nmin2 + 1) <= 32 * 4095;
+      const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
+      int o1, o2, ntz, ntx;
+      fits = !g.twoD || (n1 <= 64 * 4000 && n2 <= 32 * 4000 &&
+                         t2_origin(n1, n2, &o1, &o2, &ntz, &ntx));
     }
     if (!fits) tile.stream2d = 1;
   }
@@ -267,8 +270,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.adj2d = S.adj2d; h.inj_on = S.inj_on;
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
-      const int n1t = (S.g.nmax1 - S.g.nmin1 + 1 + 63) / 64;
-      const int n2t = (S.g.nmax2 - S.g.nmin2 + 1 + 31) / 32;
+      h.gz = S.gz; h.gx = S.gx;
+      if (!t2_origin(S.g.nmax1 - S.g.nmin1 + 1, S.g.nmax2 - S.g.nmin2 + 1, &h.off1, &h.off2,
+                     &h.ntz, &h.ntx))
+        return fail(c, SW_CUDA_ERR, "tile origin");
+      const int n1t = h.ntz, n2t = h.ntx;
       for (int xi = 0; xi < n2t; ++xi)
         for (int zi = 0; zi < n1t; ++zi) htile.push_back((b << 24) | (zi << 12) | xi);
     }

@@ -110,18 +110,26 @@ __device__ __forceinline__ void tma_2d(float *dst, const CUtensorMap *map, int x
 __device__ __forceinline__ int t2_b(int e) { return e >> 24; }
 __device__ __forceinline__ int t2_tzi(int e) { return (e >> 12) & 0xfff; }
 __device__ __forceinline__ int t2_txi(int e) { return e & 0xfff; }
+// First row / column of a tile.
+__device__ __forceinline__ int t2_z0(const T2Shot &h, int e) {
+  return h.nmin1 - h.off1 + t2_tzi(e) * T2_Z;
+}
+__device__ __forceinline__ int t2_x0(const T2Shot &h, int e) {
+  return h.nmin2 - h.off2 + t2_txi(e) * T2_X;
+}
 
 // Issues the tensor copies of one tile into a stage (one thread).  Tensor
 // map 2*buf+0 has the 72 x 40 halo box, 2*buf+1 the 64 x 32 core box; buf
 // 0..4 are the shot's time-level buffers, 5 its velocity.  Halo coordinates
-// start at row z0-4 and column x0-4 of the padded array (which starts 4
-// cells before the compute domain); elements outside the array read 0 and
-// only feed outputs that are never stored.
+// are row z0-4 and column x0-4 relative to the padded array's origin (4
+// cells before the compute domain), so they may be negative for the first
+// tiles; elements outside the array read 0 and only feed outputs that are
+// never stored.  The row coordinate is a multiple of 4 (16 bytes).
 template <bool ADJ>
-__device__ __forceinline__ void t2_issue(const T2Maps &M, int s, int e, float *st,
-                                         unsigned long long *bar) {
+__device__ __forceinline__ void t2_issue(const T2Maps &M, const T2Shot &h, int s, int e,
+                                         float *st, unsigned long long *bar) {
   constexpr unsigned bytes = 4u * (unsigned)t2_stage_floats<ADJ>();
-  const int zi = t2_tzi(e) * T2_Z, xi = t2_txi(e) * T2_X;
+  const int zi = t2_tzi(e) * T2_Z - h.off1, xi = t2_txi(e) * T2_X - h.off2;
   mbar_expect_tx(bar, bytes);
   tma_2d(st, &M.m[2 * ((s + 3) % 5)], zi, xi, bar);
   if (ADJ) tma_2d(st + T2_HALO, &M.m[10], zi, xi, bar);
@@ -260,7 +268,7 @@ __device__ __forceinline__ void t2_col_fast(const T2Pairs &c, const float *col, 
 
 // Whether a tile overlaps the physical domain.
 __device__ __forceinline__ bool t2_phys_tile(const T2Shot &h, int e) {
-  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
   return !(z0 + T2_Z - 1 < 1 || z0 > h.nz || x0 + T2_X - 1 < 1 || x0 > h.nx);
 }
 
@@ -276,7 +284,7 @@ __device__ __forceinline__ bool t2_col_ok(const T2Shot &h, int j) { return j >= 
 // Loads the snapshot, image and illumination values of a thread's elements
 // for an imaging step (zeros outside the physical domain).
 __device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, int e, T2Img &P) {
-  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
   const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
@@ -301,7 +309,7 @@ __device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, 
 template <bool ADJ>
 __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp, const T2Img &P,
                                              int e, const float *su, const float *svel) {
-  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
   const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
@@ -337,11 +345,13 @@ template <bool ADJ>
 __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h,
                                            const T2Step &stp, int b, int s, int e,
                                            const float *st) {
-  const int z0 = h.nmin1 + t2_tzi(e) * T2_Z, x0 = h.nmin2 + t2_txi(e) * T2_X;
+  const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
   const int tid = threadIdx.x;
   const int tz = tid & 15, tx = tid >> 4;
   const int i0 = z0 + 4 * tz;
-  if (i0 > h.nmax1) return;
+  // Row groups outside the compute domain (the first tile starts off1, a
+  // multiple of 4, rows early) compute nothing.
+  if (i0 > h.nmax1 || i0 < h.nmin1) return;
   const int it = stp.it;
   // Tile-level decisions.
   const int zl = z0 + T2_Z - 1, xl = x0 + T2_X - 1;
@@ -377,7 +387,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
       const int jl = tx + 16 * hh, j = x0 + jl;
-      if (j > h.nmax2) continue;
+      if (j > h.nmax2 || j < h.nmin2) continue;
       const bool col_inj = rows_inj && j >= h.bj0 && j <= h.bj1;
       if (!col_inj && !snap_slow) continue;
       float r[4] = {sv[hh][0].x, sv[hh][0].y, sv[hh][1].x, sv[hh][1].y};
@@ -397,7 +407,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   }
   // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
   float *__restrict__ u3 = const_cast<float *>(h.f[(s + 4) % 5]);
-  const int rbase = t2_tzi(e) * T2_Z;
+  const int rbase = t2_tzi(e) * T2_Z - h.off1;   // row z0-4 relative to the padded origin
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
     const int jl = tx + 16 * hh, j = x0 + jl;
@@ -414,7 +424,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
       a = p_add(a, s_mul(c.k12, sv[hh][p]));
       o[p] = p_mul(a, c.div11);
     }
-    if (j > h.nmax2) continue;
+    if (j > h.nmax2 || j < h.nmin2) continue;
     const int off = (rbase + 4 + 4 * tz) + h.ld1 * (j - h.lo2);
     if (i0 + 3 <= h.nmax1) {
       *reinterpret_cast<float4 *>(u3 + off) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
@@ -423,6 +433,100 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
 #pragma unroll
       for (int q = 0; q < 4; ++q)
         if (i0 + q <= h.nmax1) u3[off + q] = ov[q];
+    }
+  }
+}
+
+// Higdon recurrence of one edge half line (Boundary_3d, Boundary.f90:89-184)
+// from gathered values: U2[m], U1[m] (m = 0..9) run from 2 cells inside the
+// innermost output to the outermost one; a and bq are u3 one and two cells
+// inside it.  out[k] (k = 0..7) from the innermost cell outwards.
+__device__ __forceinline__ void t2_higdon8(const float c[8], const float U2[10],
+                                           const float U1[10], float a, float bq,
+                                           float out[8]) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    float r = c[0] * a;
+    r = r + c[1] * bq;
+    r = r + c[2] * U2[k + 2];
+    r = r + c[3] * U2[k + 1];
+    r = r + c[4] * U2[k];
+    r = r + c[5] * U1[k + 2];
+    r = r + c[6] * U1[k + 1];
+    r = r + c[7] * U1[k];
+    out[k] = -r;
+    bq = a;
+    a = out[k];
+  }
+}
+
+// Higdon edges of a tile at the boundary of the compute domain, after its
+// interior values are stored: the z lines of its columns (top and / or
+// bottom), then the x lines of its rows (left and / or right), the order of
+// the reference (z before x).  Every value a line reads lies in this tile:
+// u2 in the staged halo, u1 in the staged core, u3 just stored by this CTA.
+template <bool ADJ>
+__device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const float *st) {
+  const int tzi = t2_tzi(e), txi = t2_txi(e);
+  const bool top = tzi == 0, bottom = tzi == h.ntz - 1;
+  const bool left = txi == 0, right = txi == h.ntx - 1;
+  if (!(top || bottom || left || right)) return;
+  const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
+  const float *su = st;                                   // u2, rows z0-4.., columns x0-4..
+  const float *cu1 = st + (ADJ ? 2 : 1) * T2_HALO;        // u1, rows z0.., columns x0..
+  float *u3 = const_cast<float *>(h.f[(s + 4) % 5]);
+  const long long L = h.ld1;
+  auto gidx = [&](int i, int j) {
+    return (long long)(i - (h.nmin1 - 4)) + L * (long long)(j - h.lo2);
+  };
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n1 = h.nmax1 - h.nmin1 + 1, n2 = h.nmax2 - h.nmin2 + 1;
+  __syncthreads();   // interior values of the tile are stored
+  if (top || bottom) {
+    // Warp 0: top z lines, warp 1: bottom z lines; lane = column.
+    const bool mine = (warp == 0 && top) || (warp == 1 && bottom);
+    const int j = x0 + lane;
+    if (mine && j >= h.nmin2 && j <= h.nmax2) {
+      const bool bot = warp == 1;
+      const int dir = bot ? -1 : 1;                       // towards the interior
+      const int p = bot ? h.nmax1 - 3 : h.nmin1 + 3;      // innermost output row
+      float c[8], U2[10], U1[10], out[8];
+      const float *gc = h.gz + (j - h.nmin2) + (bot ? 8 * n2 : 0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) c[q] = gc[q * n2];
+#pragma unroll
+      for (int m = 0; m < 10; ++m) {
+        const int i = p - (m - 2) * dir;
+        U2[m] = su[(lane + 4) * T2_SZ + (i - (z0 - 4))];
+        U1[m] = cu1[lane * T2_Z + (i - z0)];
+      }
+      t2_higdon8(c, U2, U1, u3[gidx(p + dir, j)], u3[gidx(p + 2 * dir, j)], out);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) u3[gidx(p - k * dir, j)] = out[k];
+    }
+  }
+  __syncthreads();   // z lines done before the x lines read the corners
+  if (left || right) {
+    // Threads 0..63: left x lines, 64..127: right x lines; one row each.
+    const bool rgt = tid >= 64;
+    const bool mine = tid < 128 && ((!rgt && left) || (rgt && right));
+    const int r = tid & 63, i = z0 + r;
+    if (mine && i >= h.nmin1 && i <= h.nmax1) {
+      const int dir = rgt ? -1 : 1;
+      const int p = rgt ? h.nmax2 - 3 : h.nmin2 + 3;      // innermost output column
+      float c[8], U2[10], U1[10], out[8];
+      const float *gc = h.gx + (i - h.nmin1) + (rgt ? 8 * n1 : 0);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) c[q] = gc[q * n1];
+#pragma unroll
+      for (int m = 0; m < 10; ++m) {
+        const int j = p - (m - 2) * dir;
+        U2[m] = su[(j - (x0 - 4)) * T2_SZ + (r + 4)];
+        U1[m] = cu1[(j - x0) * T2_Z + r];
+      }
+      t2_higdon8(c, U2, U1, u3[gidx(i, p + dir)], u3[gidx(i, p + 2 * dir)], out);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) u3[gidx(i, p - k * dir)] = out[k];
     }
   }
 }
@@ -488,7 +592,9 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       if (steps[t2_b(e)].live) list[n++] = e;
     }
     *nlist = n;
-    if (n > 0) t2_issue<ADJ>(t.t2maps[t2_b(list[0])], s, list[0], t2_smem, &full[0]);
+    if (n > 0)
+      t2_issue<ADJ>(t.t2maps[t2_b(list[0])], shots[t2_b(list[0])], s, list[0], t2_smem,
+                    &full[0]);
   }
   __syncthreads();
   const int n = *nlist;
@@ -496,21 +602,26 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     const int cur = k & 1;
     // The other stage was released by the barrier that ended tile k-1.
     if (tid == 0 && k + 1 < n)
-      t2_issue<ADJ>(t.t2maps[t2_b(list[k + 1])], s, list[k + 1], t2_smem + (cur ^ 1) * SF,
-                    &full[cur ^ 1]);
+      t2_issue<ADJ>(t.t2maps[t2_b(list[k + 1])], shots[t2_b(list[k + 1])], s, list[k + 1],
+                    t2_smem + (cur ^ 1) * SF, &full[cur ^ 1]);
     const int e = list[k];
     const T2Shot &h = shots[t2_b(e)];
     const T2Step &stp = steps[t2_b(e)];
     T2Img P;
     if (stp.img && t2_phys_tile(h, e)) t2_img_load(h, stp, e, P);
-    if (mbar_wait(&full[cur], (unsigned)((k >> 1) & 1))) {
+    // A wait that gives up records the error; the tile is still computed (on
+    // whatever the stage holds) so that every thread reaches the same
+    // barriers, and the loop ends after it.
+    if (!mbar_wait(&full[cur], (unsigned)((k >> 1) & 1))) {
+      atomicOr(t.err, 1);
+      *abort_flag = 1;
+    }
+    {
       const float *st = t2_smem + cur * SF;
       t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st);
       if ((stp.extract || stp.img) && t2_phys_tile(h, e))
         t2_snap_tile<ADJ>(h, stp, P, e, st, st + T2_HALO);
-    } else {
-      atomicOr(t.err, 1);
-      *abort_flag = 1;
+      t2_edges<ADJ>(h, s, e, st);
     }
     __syncthreads();   // the stage is free for tile k+2
     if (*abort_flag) {
