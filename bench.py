@@ -240,6 +240,8 @@ def main():
                     help="time samples of the CPU sample shot (0: its whole record)")
     ap.add_argument("--nt-cap", type=int, default=0, help="truncate records (debug)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="launch every time step directly (profiling runs: every launch timed)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -253,6 +255,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     ctx = sw.Context(local)
+    if args.no_graph:
+        ctx.set_tuning(use_graph=0)
     g, vel, w, shots = make_workload(args.nt_cap or None)
     B = args.shots_per_step
     nsteps = args.warmup + args.steps
@@ -297,6 +301,7 @@ def main():
     t_start = time.perf_counter()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
+    torch.cuda.nvtx.range_push("timed")
     points = 0
     for k in range(args.warmup, nsteps):
         job.run(k * B, B)
@@ -305,6 +310,7 @@ def main():
         im = torch.from_numpy(job.result(normalised=False)[0]).cuda()
         torch.distributed.all_reduce(im)
     ev1.record()
+    torch.cuda.nvtx.range_pop()
     barrier()
     elapsed = time.perf_counter() - t_start
     ev_ms = ev0.elapsed_time(ev1)
@@ -328,12 +334,15 @@ def main():
     kern_s = st["step_kernel_ms"] / 1e3
     nl = max(1, st["step_kernel_timed"])
     achieved = (st["step_bytes"] / nl) / (kern_s / nl) / 1e9 if kern_s > 0 else None
+    # DRAM traffic per launch: the ratio of ncu-measured DRAM bytes to
+    # algorithmic bytes over every fused-kernel launch of a smaller RTM batch
+    # (profiles/step_kernel_traffic.json) times this run's algorithmic bytes.
+    algo_per_launch = st["step_bytes"] / nl
     traffic = None
     prof_json = os.path.join(ROOT, "profiles", "step_kernel_traffic.json")
     if os.path.exists(prof_json):
         try:
-            pj = json.load(open(prof_json))
-            traffic = pj.get("bytes_per_point") and pj["bytes_per_point"] * (st["step_bytes"] / nl) / BYTES_PER_POINT
+            traffic = float(json.load(open(prof_json))["dram_per_algorithmic"]) * algo_per_launch
         except Exception:
             traffic = None
     # End to end through the public API with host buffers (one step's shots).
@@ -377,6 +386,7 @@ def main():
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "peak_kind": peak_kind, "kernel": "k_bstep2d_t (fused stencil + time update, pipelined 2D tiles)",
                          "avg_launch_ms": (st["step_kernel_ms"] / nl),
+                         "algorithmic_bytes_per_launch": algo_per_launch,
                          "launches_timed": st["step_kernel_timed"]},
             "cpu_baseline": cpu, "e2e": e2e_line, "clocks": clk,
             "gpu_launches": int(st["launches_total"]),

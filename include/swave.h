@@ -295,7 +295,9 @@ typedef struct sw_stats {
 } sw_stats;
 int sw_ctx_get_stats(const sw_ctx *ctx, sw_stats *out);
 int sw_ctx_reset_stats(sw_ctx *ctx);
-/* on=1: bracket every fused-kernel launch with CUDA events. */
+/* on=1: bracket fused-kernel launches with CUDA events: every launch when
+   the time loop runs without a CUDA graph, otherwise the launches of every
+   8th graph chunk (the event records cost a few microseconds each). */
 int sw_ctx_set_profiling(sw_ctx *ctx, int on);
 
 #ifdef __cplusplus

@@ -541,9 +541,23 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     ++nl;
   }
   dim3 bs(32, 8, 1);
-  // External record nodes: a plain record inside stream capture only adds a
-  // dependency and would never timestamp the event at graph replay.
-  if (ev_before) cudaEventRecordWithFlags(ev_before, s, cudaEventRecordExternal);
+  // Inside stream capture the records must be external nodes (a plain
+  // record only adds a dependency and would never timestamp the event at
+  // graph replay); outside capture a plain record is required.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (ev_before || ev_after) {
+    cudaError_t ec = cudaStreamIsCapturing(s, &cap);
+    if (ec != cudaSuccess) return ec;
+  }
+  auto record = [&](cudaEvent_t ev) {
+    return cap == cudaStreamCaptureStatusActive
+               ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+               : cudaEventRecord(ev, s);
+  };
+  if (ev_before) {
+    cudaError_t ec = record(ev_before);
+    if (ec != cudaSuccess) return ec;
+  }
   if (has_3d && tile.stream3d) {
     dim3 b3(S3_BZ, S3_BY, 1);
     if (tile.has_fwd3d) {
@@ -577,7 +591,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     k_bstep<true><<<n_step_tiles, bs, 0, s>>>(t, s_off);
     ++nl;
   }
-  if (ev_after) cudaEventRecordWithFlags(ev_after, s, cudaEventRecordExternal);
+  if (ev_after) {
+    cudaError_t ec = record(ev_after);
+    if (ec != cudaSuccess) return ec;
+  }
   if (!has_3d && tile.stream2d == 2) {
     // The pipelined 2D kernel applies the Higdon edges itself.
   } else if (!has_3d && tile.fused_edges) {

@@ -345,24 +345,49 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   const int chunk = std::max(1, std::min(opt.chunk, max_steps));
   const int nchunks = (max_steps + chunk - 1) / chunk;
   const bool prof = c->profiling;
-  // Profiling: events around every fused step kernel.  With the graph path
-  // two graphs record into two event sets, so the host reads the times of
-  // chunk q-1 while chunk q runs and the device never waits for the host.
-  const int nsets = (opt.use_graph && nchunks > 1) ? 2 : 1;
-  if (prof && (int)c->ev.size() < 2 * chunk * nsets) {
+  // Algorithmic bytes of the fused step kernel at step sidx: 24 B per point
+  // update (u2, u1, u0, u_1, vel read, u3 written) plus, on a shot's
+  // snapshot steps, per physical point 4 B for a saved snapshot and the
+  // imaging traffic (RTM/LSRTM: snapshot read + image and illumination
+  // read-modify-write = 20 B; AFWI: two more snapshot reads = 28 B; Born
+  // source: snapshot + reflectivity = 8 B).
+  auto step_bytes_at = [&](int sidx) -> uint64_t {
+    uint64_t by = 0;
+    for (auto &S : hs) {
+      if (sidx >= S.nsteps) continue;
+      by += (uint64_t)S.npts * 24ull;
+      const int it = S.tmin + sidx * S.tstep;
+      if (it % S.snapi != 0) continue;
+      const int cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
+                                  : S.tmin / S.snapi - (it - 1) / S.snapi;
+      const bool slot = S.tstep > 0 ? cnt <= S.ntsnap : S.ntsnap - cnt + 1 >= 1;
+      if (!slot) continue;
+      uint64_t per = S.extract_wave ? 4 : 0;
+      if (S.imaging == SW_IMG_RTM || S.imaging == SW_IMG_LSRTM) per += 20;
+      if (S.imaging == SW_IMG_AFWI) per += 28;
+      if (S.imaging == SW_IMG_BORN) per += 8;
+      by += (uint64_t)S.g.nz * S.g.nx * S.g.ny * per;
+    }
+    return by;
+  };
+  // Profiling: events around the fused step kernel of every
+  // kProfileEvery-th chunk of steps.  Those chunks replay a second graph
+  // that contains the event records; the host reads a profiled chunk's
+  // times after the next chunk is queued, so the device never waits.
+  constexpr int kProfileEvery = 8;
+  if (prof && (int)c->ev.size() < 2 * chunk) {
     const size_t old = c->ev.size();
-    c->ev.resize(2 * chunk * nsets);
+    c->ev.resize(2 * chunk);
     for (size_t q = old; q < c->ev.size(); ++q) SW_CK(cudaEventCreate(&c->ev[q]));
   }
-  auto record_chunk = [&](int nsteps_here, int set) -> int {
+  auto record_chunk = [&](int nsteps_here, bool with_events) -> int {
     int launched = 0;
-    cudaEvent_t *ev = prof ? c->ev.data() + 2 * chunk * set : nullptr;
     for (int q = 0; q < nsteps_here; ++q) {
       int nl = 0;
       // In profiling mode events bracket the fused step kernel only.
       if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
-                                 has_adj3d, tile, s, &nl, prof ? ev[2 * q] : nullptr,
-                                 prof ? ev[2 * q + 1] : nullptr)) != cudaSuccess)
+                                 has_adj3d, tile, s, &nl, with_events ? c->ev[2 * q] : nullptr,
+                                 with_events ? c->ev[2 * q + 1] : nullptr)) != cudaSuccess)
         return -1;
       launched += nl;
     }
@@ -370,15 +395,14 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     return launched + 1;
   };
   auto read_chunk = [&](int q) -> int {
-    const int set = q % nsets;
-    cudaEvent_t *ev = c->ev.data() + 2 * chunk * set;
     const int live = std::min(chunk, max_steps - q * chunk);
-    SW_CK(cudaEventSynchronize(ev[2 * live - 1]));
+    SW_CK(cudaEventSynchronize(c->ev[2 * live - 1]));
     for (int k = 0; k < live; ++k) {
       float ms = 0.f;
-      SW_CK(cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]));
+      SW_CK(cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]));
       c->stats.step_kernel_ms += ms;
       c->stats.step_kernel_timed++;
+      c->stats.step_bytes += step_bytes_at(q * chunk + k);
     }
     return SW_OK;
   };
@@ -386,7 +410,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   if (opt.use_graph && nchunks > 1) {
     cudaGraph_t graph[2] = {nullptr, nullptr};
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    const int ngraph = prof ? 2 : 1;
+    const int ngraph = prof ? 2 : 1;   // [0] plain, [1] with event records
     int per = 0;
     auto cleanup = [&]() {
       for (int k = 0; k < 2; ++k) {
@@ -399,7 +423,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         cleanup();
         return cuda_fail(c, e, "begin capture");
       }
-      per = record_chunk(chunk, k);
+      per = record_chunk(chunk, k == 1);
       cudaError_t ec = cudaStreamEndCapture(s, &graph[k]);
       if (per < 0 || ec != cudaSuccess) {
         cleanup();
@@ -410,19 +434,25 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         return cuda_fail(c, e, "instantiate step graph");
       }
     }
-    int rs = SW_OK;
+    int rs = SW_OK, pending = -1;
     for (int q = 0; q < nchunks; ++q) {
-      if ((e = cudaGraphLaunch(exec[q % ngraph], s)) != cudaSuccess) break;
+      const bool timed = prof && q % kProfileEvery == 0;
+      if ((e = cudaGraphLaunch(exec[timed ? 1 : 0], s)) != cudaSuccess) break;
       launches += per;
-      if (prof && q > 0 && (rs = read_chunk(q - 1)) != SW_OK) break;
+      if (pending >= 0) {
+        rs = read_chunk(pending);
+        pending = -1;
+        if (rs != SW_OK) break;
+      }
+      if (timed) pending = q;
     }
-    if (e == cudaSuccess && rs == SW_OK && prof) rs = read_chunk(nchunks - 1);
+    if (e == cudaSuccess && rs == SW_OK && pending >= 0) rs = read_chunk(pending);
     cleanup();
     if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
     if (rs != SW_OK) return rs;
   } else {
     for (int q = 0; q < max_steps; ++q) {
-      const int per = record_chunk(1, 0);
+      const int per = record_chunk(1, prof);
       if (per < 0) return cuda_fail(c, e, "step launch");
       launches += per;
       if (prof) {
@@ -431,6 +461,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         SW_CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         c->stats.step_kernel_ms += ms;
         c->stats.step_kernel_timed++;
+        c->stats.step_bytes += step_bytes_at(q);
       }
     }
   }
@@ -440,29 +471,6 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   c->stats.points_updated += upd;
   c->stats.launches_total += launches;
   c->stats.launches_step += (uint64_t)max_steps;
-  if (prof) {
-    // Algorithmic bytes: 24 B per point update (u2, u1, u0, u_1, vel read,
-    // u3 written) plus, on snapshot steps, 4 B per physical point for a
-    // saved snapshot and the imaging traffic (RTM/LSRTM: snapshot read +
-    // image and illumination read-modify-write = 20 B; AFWI: two more
-    // snapshot reads = 28 B; Born source: snapshot + reflectivity = 8 B).
-    uint64_t extra = 0;
-    for (auto &S : hs) {
-      const uint64_t nph = (uint64_t)S.g.nz * S.g.nx * S.g.ny;
-      uint64_t nsnap = 0;
-      for (int q = 0; q < S.nsteps; ++q) {
-        const int it = S.tmin + q * S.tstep;
-        if (it % S.snapi == 0) ++nsnap;
-      }
-      nsnap = std::min<uint64_t>(nsnap, (uint64_t)S.ntsnap);
-      uint64_t per = S.extract_wave ? 4 : 0;
-      if (S.imaging == SW_IMG_RTM || S.imaging == SW_IMG_LSRTM) per += 20;
-      if (S.imaging == SW_IMG_AFWI) per += 28;
-      if (S.imaging == SW_IMG_BORN) per += 8;
-      extra += nsnap * nph * per;
-    }
-    c->stats.step_bytes += upd * 24ull + extra;
-  }
   // ---- outputs ----
   for (int b = 0; b < nb; ++b) {
     if (!shots[b].io.final_u2_host) continue;
