@@ -283,6 +283,26 @@ typedef struct sw_tuning {
 int sw_ctx_set_tuning(sw_ctx *ctx, const sw_tuning *t);
 int sw_ctx_get_tuning(const sw_ctx *ctx, sw_tuning *t);
 
+/* ---- Modelling without device allocation --------------------------------- */
+/* No counterpart in the reference (its modelling allocates the wavefields of
+ * every shot it runs).  Same arguments, run and results as sw_modeling for
+ * a 2D model (host arrays in and out), for callers that cannot allocate
+ * device memory during the call: a process whose device memory is committed
+ * to its own pool (e.g. an RTM job's snapshot arena) or one that must not
+ * let cudaMalloc / cudaFree synchronise the device mid-run.  It allocates
+ * nothing: every device array lives in one file-scope scratch array of
+ * 32 MiB that each GPU loading the library holds until the process exits,
+ * which limits the padded grid to about 1.3 million points (6 float arrays
+ * of ld1 x (nx + 2*ntaper + 8) plus plans and traces).  Larger runs return
+ * SW_OOM_ADMISSION before any device work.  Runs on the current device's
+ * legacy default stream and returns when the traces are on the host.  The
+ * first call on a device looks the scratch array's device address up there
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (from several
+ * host threads at once) race on it.  3D models return SW_UNSUPPORTED. */
+int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const float *sou_coord,
+                        const float *wavelet, int nrec, const float *rec_coord, float *data);
+
 /* ---- Instrumentation ----------------------------------------------------- */
 typedef struct sw_stats {
   uint64_t launches_total;      /* kernels launched by this context          */

@@ -93,6 +93,7 @@ _SIGS = {
     "sw_vel_check": (C.c_int, [C.POINTER(SwGenpar), _fp, _fp, _fp]),
     "sw_propagate": (C.c_int, [C.c_void_p, C.POINTER(SwPropDesc), C.POINTER(SwPropIO)]),
     "sw_modeling": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp]),
+    "sw_modeling_noalloc": (C.c_int, [C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp]),
     "sw_rtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
     "sw_born": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
     "sw_lsrtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
@@ -440,6 +441,22 @@ def vel_check(g: SwGenpar, vel) -> tuple[int, float, float]:
     a, b = C.c_float(), C.c_float()
     code = lib.sw_vel_check(C.byref(g), fptr(v), C.byref(a), C.byref(b))
     return code, a.value, b.value
+
+
+def modeling_noalloc(g: SwGenpar, vel, sou_coord, wavelet, rec_coord) -> np.ndarray:
+    """sw_modeling_noalloc: 2D shot modelling on the current device that
+    allocates no device memory (results equal Context.modeling).  Raises
+    SwaveError with SW_OOM_ADMISSION when the run exceeds the library's fixed
+    32 MiB scratch array."""
+    lib = load_library()
+    vel, sc, w, rc = _f32(vel), _f32(sou_coord), _f32(wavelet), _f32(rec_coord)
+    nrec = rc.size // 3
+    data = np.zeros((nrec, g.nt), np.float32)
+    code = lib.sw_modeling_noalloc(C.byref(g), fptr(vel), fptr(sc), fptr(w), nrec, fptr(rc),
+                                   fptr(data))
+    if code != SW_OK:
+        raise SwaveError(code, "sw_modeling_noalloc")
+    return data
 
 
 def born_wavelet(w, dt: float) -> np.ndarray:
