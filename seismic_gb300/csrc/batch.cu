@@ -513,6 +513,35 @@ static cudaError_t launch_tile2d(const BatchTables &t, int s_off, int n_tiles, i
   return cudaGetLastError();
 }
 
+// Warp-specialised persistent 2D step (tile2d.cuh): one CTA per SM.
+static_assert(t2w_smem_bytes<false>() <= 227 * 1024, "ws tile kernel smem (fwd)");
+static_assert(t2w_smem_bytes<true>() <= 227 * 1024, "ws tile kernel smem (adj)");
+
+template <bool ADJ>
+__global__ void __launch_bounds__(T2W_THREADS, 1) k_bstep2d_w(BatchTables t, int s_off,
+                                                              int n_tiles) {
+  tile2d_ws<ADJ>(t, s_off, n_tiles);
+}
+
+template <bool ADJ>
+static cudaError_t launch_tile2d_ws(const BatchTables &t, int s_off, int n_tiles, int nsm,
+                                    cudaStream_t s) {
+  static unsigned long long attr_set = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !(attr_set & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_bstep2d_w<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t2w_smem_bytes<ADJ>());
+    if (e != cudaSuccess) return e;
+    if (dev < 64) attr_set |= 1ull << dev;
+  }
+  const int grid = std::max({1, std::min(n_tiles, nsm),
+                             (n_tiles + T2_MAX_TILES_PER_CTA - 1) / T2_MAX_TILES_PER_CTA});
+  k_bstep2d_w<ADJ><<<grid, T2W_THREADS, t2w_smem_bytes<ADJ>(), s>>>(t, s_off, n_tiles);
+  return cudaGetLastError();
+}
+
 // Streaming 3D step (stream3d.cuh), one kernel per stencil variant.
 template <bool ADJ>
 __global__ void __launch_bounds__(256, 4) k_bstep3d_s(BatchTables t, int s_off, int ty) {
@@ -571,6 +600,17 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   } else if (has_3d) {
     k_bstep<false><<<n_step_tiles, bs, 0, s>>>(t, s_off);
     ++nl;
+  } else if (tile.stream2d == 3) {
+    cudaError_t e = cudaSuccess;
+    if (tile.has_fwd2d) {
+      e = launch_tile2d_ws<false>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e == cudaSuccess && tile.has_adj2d) {
+      e = launch_tile2d_ws<true>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e != cudaSuccess) return e;
   } else if (tile.stream2d == 2) {
     cudaError_t e = cudaSuccess;
     if (tile.has_fwd2d) {
@@ -595,7 +635,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     cudaError_t ec = record(ev_after);
     if (ec != cudaSuccess) return ec;
   }
-  if (!has_3d && tile.stream2d == 2) {
+  if (!has_3d && (tile.stream2d == 2 || tile.stream2d == 3)) {
     // The pipelined 2D kernel applies the Higdon edges itself.
   } else if (!has_3d && tile.fused_edges) {
     k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);

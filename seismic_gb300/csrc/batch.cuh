@@ -119,7 +119,8 @@ struct BatchTables {
 // streaming kernel with TZ = tz rows per CTA (32, 64 or 128) walking tx
 // columns; otherwise 32x8 point tiles.  3D: 32x8 point tiles per plane.
 struct StepTile {
-  int stream2d = 2;    // 2D: 0 point tiles, 1 streaming (stream2d.cuh), 2 tiled (tile2d.cuh)
+  int stream2d = 2;    // 2D: 0 point tiles, 1 streaming (stream2d.cuh), 2 tiled, 3 tiled and
+                       // warp-specialised (tile2d.cuh)
   int tz = 64;
   int tx = 64;
   int stream3d = 1;    // 3D: 2.5D streaming kernel (stream3d.cuh)
@@ -145,7 +146,7 @@ inline int edge_threads_2d(const Geom &g) {
 // Number of fused-step CTAs a shot needs with this tile shape.
 inline int step_ctas(const Geom &g, const StepTile &tile) {
   const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
-  if (g.twoD && tile.stream2d == 2) {
+  if (g.twoD && (tile.stream2d == 2 || tile.stream2d == 3)) {
     int o1, o2, nz, nx;
     return t2_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;
   }

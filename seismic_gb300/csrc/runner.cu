@@ -75,7 +75,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // and packs tile coordinates into 12 bits each; larger batches, grids
   // beyond that or domains below 16 cells use the streaming kernel.
   StepTile tile = opt.tile;
-  if (tile.stream2d == 2) {
+  if (tile.stream2d == 2 || tile.stream2d == 3) {
     bool fits = nb <= T2_MAX_SHOTS;
     for (int b = 0; b < nb && fits; ++b) {
       const Geom g = make_geom(shots[b].d.g);
@@ -86,7 +86,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     }
     if (!fits) tile.stream2d = 1;
   }
-  const bool t2 = tile.stream2d == 2 && shots[0].d.g.twoD;
+  const bool t2 = (tile.stream2d == 2 || tile.stream2d == 3) && shots[0].d.g.twoD;
   // ---- host-side plans and arena sizes ----
   size_t bytes = 0;
   for (int b = 0; b < nb; ++b) {

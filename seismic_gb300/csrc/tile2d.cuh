@@ -207,65 +207,6 @@ __device__ __forceinline__ T2Pairs t2_pairs(const T2Shot &h) {
   return c;
 }
 
-// Laplacian part of 4 consecutive rows of one column, away from the edges
-// of the compute domain, as two row pairs (rows 0,1 and 2,3).  col points at
-// row i0-4 of the staged u2 column, vcol (adjoint) at the same row of the
-// staged velocity, vcore (forward) at row i0 of the staged core velocity.
-// Per lane the operations are those of the scalar loops
-// (FDderivatives.f90:715-743 forward, 847-891 adjoint).
-template <bool ADJ>
-__device__ __forceinline__ void t2_col_fast(const T2Pairs &c, const float *col, const float *vcol,
-                                            const float *vcore, P2 sv[2], float4 &u2c) {
-  const float4 za = lds4(col), zb = lds4(col + 4), zc = lds4(col + 8);
-  u2c = zb;
-  P2 P[6] = {lo2(za), hi2(za), lo2(zb), hi2(zb), lo2(zc), hi2(zc)};
-  if (ADJ) {
-    const float4 va = lds4(vcol), vb = lds4(vcol + 4), vc = lds4(vcol + 8);
-    const P2 V[6] = {lo2(va), hi2(va), lo2(vb), hi2(vb), lo2(vc), hi2(vc)};
-#pragma unroll
-    for (int k = 0; k < 6; ++k) P[k] = s_mul(p_mul(V[k], V[k]), P[k]);   // (v*v)*u
-  }
-  // Pairs of rows (2k+1, 2k+2) for the odd z offsets.
-  P2 Q[5];
-#pragma unroll
-  for (int k = 0; k < 5; ++k) Q[k] = p2(P[k].y, P[k + 1].x);
-  P2 tzz[2], txx[2];
-#pragma unroll
-  for (int p = 0; p < 2; ++p) {
-    P2 a = s_mul(c.cz[0], P[2 + p]);
-    a = p_add(a, s_mul(c.cz[1], p_add(Q[2 + p], Q[1 + p])));
-    a = p_add(a, s_mul(c.cz[2], p_add(P[3 + p], P[1 + p])));
-    a = p_add(a, s_mul(c.cz[3], p_add(Q[3 + p], Q[p])));
-    a = p_add(a, s_mul(c.cz[4], p_add(P[4 + p], P[p])));
-    tzz[p] = a;
-    txx[p] = s_mul(c.cx[0], P[2 + p]);
-  }
-#pragma unroll
-  for (int l = 1; l <= 4; ++l) {
-    float4 rp = lds4(col + l * T2_SZ + 4), rm = lds4(col - l * T2_SZ + 4);
-    P2 rp0 = lo2(rp), rp1 = hi2(rp), rm0 = lo2(rm), rm1 = hi2(rm);
-    if (ADJ) {
-      const float4 vp = lds4(vcol + l * T2_SZ + 4), vm = lds4(vcol - l * T2_SZ + 4);
-      const P2 vp0 = lo2(vp), vp1 = hi2(vp), vm0 = lo2(vm), vm1 = hi2(vm);
-      rp0 = s_mul(p_mul(vp0, vp0), rp0);
-      rp1 = s_mul(p_mul(vp1, vp1), rp1);
-      rm0 = s_mul(p_mul(vm0, vm0), rm0);
-      rm1 = s_mul(p_mul(vm1, vm1), rm1);
-    }
-    txx[0] = p_add(txx[0], s_mul(c.cx[l], p_add(rp0, rm0)));
-    txx[1] = p_add(txx[1], s_mul(c.cx[l], p_add(rp1, rm1)));
-  }
-  if (ADJ) {
-    sv[0] = p_add(txx[0], tzz[0]);
-    sv[1] = p_add(txx[1], tzz[1]);
-  } else {
-    const float4 vv = lds4(vcore);
-    const P2 v0 = lo2(vv), v1 = hi2(vv);
-    sv[0] = p_mul(p_mul(v0, v0), p_add(txx[0], tzz[0]));
-    sv[1] = p_mul(p_mul(v1, v1), p_add(txx[1], tzz[1]));
-  }
-}
-
 // Whether a tile overlaps the physical domain.
 __device__ __forceinline__ bool t2_phys_tile(const T2Shot &h, int e) {
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
@@ -283,9 +224,10 @@ __device__ __forceinline__ bool t2_col_ok(const T2Shot &h, int j) { return j >= 
 
 // Loads the snapshot, image and illumination values of a thread's elements
 // for an imaging step (zeros outside the physical domain).
-__device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, int e, T2Img &P) {
+__device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, int e, T2Img &P,
+                                            int tid) {
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
-  const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
+  const int tz = tid & 15, tx = tid >> 4;
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
     const int j = x0 + tx + 16 * hh;
@@ -308,9 +250,9 @@ __device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, 
 // element-by-element path.
 template <bool ADJ>
 __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp, const T2Img &P,
-                                             int e, const float *su, const float *svel) {
+                                             int e, const float *su, const float *svel, int tid) {
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
-  const int tz = threadIdx.x & 15, tx = threadIdx.x >> 4;
+  const int tz = tid & 15, tx = tid >> 4;
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
     const int jl = tx + 16 * hh, j = x0 + jl;
@@ -339,14 +281,89 @@ __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp,
   }
 }
 
+// Laplacian part of rows i0..i0+3 of two adjacent columns jl0, jl0+1 of a
+// tile, away from the edges of the compute domain, as row pairs.  The ten
+// columns jl0-4..jl0+5 at rows i0..i0+3 are read once and serve the x
+// derivatives of both columns.  col0 points at row i0 of column jl0 of the
+// staged u2 tile, vcol0 at the same place of the staged velocity halo
+// (adjoint), vcore0 at row i0 of column jl0 of the staged core velocity
+// (forward).  u2c receives the raw u2 values of the two columns.  Per lane
+// the operations are those of the scalar loops (FDderivatives.f90:715-743
+// forward, 847-891 adjoint).
+template <bool ADJ>
+__device__ __forceinline__ void t2_pair_fast(const T2Pairs &c, const float *col0,
+                                             const float *vcol0, const float *vcore0,
+                                             P2 sv[2][2], float4 u2c[2]) {
+  float4 N[10];
+#pragma unroll
+  for (int m = 0; m < 10; ++m) N[m] = lds4(col0 + (m - 4) * T2_SZ);
+  u2c[0] = N[4];
+  u2c[1] = N[5];
+  if (ADJ) {
+    // w = (v*v)*u at every stencil point (FDderivatives.f90:847-891).
+#pragma unroll
+    for (int m = 0; m < 10; ++m) {
+      const float4 v = lds4(vcol0 + (m - 4) * T2_SZ);
+      const P2 a = s_mul(p_mul(lo2(v), lo2(v)), lo2(N[m]));
+      const P2 b = s_mul(p_mul(hi2(v), hi2(v)), hi2(N[m]));
+      N[m] = make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+#pragma unroll
+  for (int cc = 0; cc < 2; ++cc) {
+    const float *col = col0 + cc * T2_SZ;
+    float4 za = lds4(col - 4), zc = lds4(col + 4);
+    if (ADJ) {
+      const float *vcol = vcol0 + cc * T2_SZ;
+      const float4 va = lds4(vcol - 4), vc = lds4(vcol + 4);
+      const P2 a0 = s_mul(p_mul(lo2(va), lo2(va)), lo2(za));
+      const P2 a1 = s_mul(p_mul(hi2(va), hi2(va)), hi2(za));
+      const P2 c0 = s_mul(p_mul(lo2(vc), lo2(vc)), lo2(zc));
+      const P2 c1 = s_mul(p_mul(hi2(vc), hi2(vc)), hi2(zc));
+      za = make_float4(a0.x, a0.y, a1.x, a1.y);
+      zc = make_float4(c0.x, c0.y, c1.x, c1.y);
+    }
+    const float4 zb = N[4 + cc];
+    const P2 P[6] = {lo2(za), hi2(za), lo2(zb), hi2(zb), lo2(zc), hi2(zc)};
+    // Pairs of rows (2k+1, 2k+2) for the odd z offsets.
+    P2 Q[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) Q[k] = p2(P[k].y, P[k + 1].x);
+    P2 tzz[2], txx[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+      P2 a = s_mul(c.cz[0], P[2 + p]);
+      a = p_add(a, s_mul(c.cz[1], p_add(Q[2 + p], Q[1 + p])));
+      a = p_add(a, s_mul(c.cz[2], p_add(P[3 + p], P[1 + p])));
+      a = p_add(a, s_mul(c.cz[3], p_add(Q[3 + p], Q[p])));
+      a = p_add(a, s_mul(c.cz[4], p_add(P[4 + p], P[p])));
+      tzz[p] = a;
+      txx[p] = s_mul(c.cx[0], P[2 + p]);
+    }
+#pragma unroll
+    for (int l = 1; l <= 4; ++l) {
+      const float4 rp = N[4 + cc + l], rm = N[4 + cc - l];
+      txx[0] = p_add(txx[0], s_mul(c.cx[l], p_add(lo2(rp), lo2(rm))));
+      txx[1] = p_add(txx[1], s_mul(c.cx[l], p_add(hi2(rp), hi2(rm))));
+    }
+    if (ADJ) {
+      sv[cc][0] = p_add(txx[0], tzz[0]);
+      sv[cc][1] = p_add(txx[1], tzz[1]);
+    } else {
+      const float4 vv = lds4(vcore0 + cc * T2_Z);
+      sv[cc][0] = p_mul(p_mul(lo2(vv), lo2(vv)), p_add(txx[0], tzz[0]));
+      sv[cc][1] = p_mul(p_mul(hi2(vv), hi2(vv)), p_add(txx[1], tzz[1]));
+    }
+  }
+}
+
 // Computes one tile from a completed stage.  Thread (tz, tx) owns rows
-// i0..i0+3 of columns x0+tx and x0+tx+16; both columns are computed together.
+// i0..i0+3 of the adjacent columns x0+2tx and x0+2tx+1.
 template <bool ADJ>
 __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h,
                                            const T2Step &stp, int b, int s, int e,
-                                           const float *st) {
+                                           const float *st, int tid) {
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
-  const int tid = threadIdx.x;
   const int tz = tid & 15, tx = tid >> 4;
   const int i0 = z0 + 4 * tz;
   // Row groups outside the compute domain (the first tile starts off1, a
@@ -374,19 +391,16 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   // replicates the physical model's edge values outwards (k_pad_velocity)
   // and the compute domain contains the physical one, so the padded value at
   // any index equals the clamped lookup; no tile needs a special case.
-#pragma unroll
-  for (int hh = 0; hh < 2; ++hh) {
-    const int jl = tx + 16 * hh;
-    const int o = (jl + 4) * T2_SZ + 4 * tz;
-    t2_col_fast<ADJ>(c, su + o, svel + o, core + 3 * T2_CORE + jl * T2_Z + 4 * tz, sv[hh],
-                     u2c[hh]);
+  {
+    const int o = (2 * tx + 4) * T2_SZ + 4 * tz + 4;
+    t2_pair_fast<ADJ>(c, su + o, svel + o, core + 3 * T2_CORE + 2 * tx * T2_Z + 4 * tz, sv, u2c);
   }
   if (slow_extras) {
     const ShotDev &S = t.shots[b];
     const bool rows_inj = inj_tile && i0 + 3 >= h.bi0 && i0 <= h.bi1;
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
-      const int jl = tx + 16 * hh, j = x0 + jl;
+      const int jl = 2 * tx + hh, j = x0 + jl;
       if (j > h.nmax2 || j < h.nmin2) continue;
       const bool col_inj = rows_inj && j >= h.bj0 && j <= h.bj1;
       if (!col_inj && !snap_slow) continue;
@@ -410,7 +424,7 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   const int rbase = t2_tzi(e) * T2_Z - h.off1;   // row z0-4 relative to the padded origin
 #pragma unroll
   for (int hh = 0; hh < 2; ++hh) {
-    const int jl = tx + 16 * hh, j = x0 + jl;
+    const int jl = 2 * tx + hh, j = x0 + jl;
     const float *cc = core + jl * T2_Z + 4 * tz;
     const float4 a1 = lds4(cc), a0 = lds4(cc + T2_CORE), am = lds4(cc + 2 * T2_CORE);
     P2 o[2];
@@ -435,6 +449,13 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
         if (i0 + q <= h.nmax1) u3[off + q] = ov[q];
     }
   }
+}
+
+// Barrier of the threads that compute a tile: the whole CTA (bar 0) or one
+// 256-thread consumer group (named barrier bar).
+__device__ __forceinline__ void t2_bar(int bar) {
+  if (bar == 0) __syncthreads();
+  else asm volatile("bar.sync %0, 256;" ::"r"(bar) : "memory");
 }
 
 // Higdon recurrence of one edge half line (Boundary_3d, Boundary.f90:89-184)
@@ -466,7 +487,8 @@ __device__ __forceinline__ void t2_higdon8(const float c[8], const float U2[10],
 // the reference (z before x).  Every value a line reads lies in this tile:
 // u2 in the staged halo, u1 in the staged core, u3 just stored by this CTA.
 template <bool ADJ>
-__device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const float *st) {
+__device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const float *st, int tid,
+                                         int bar) {
   const int tzi = t2_tzi(e), txi = t2_txi(e);
   const bool top = tzi == 0, bottom = tzi == h.ntz - 1;
   const bool left = txi == 0, right = txi == h.ntx - 1;
@@ -479,9 +501,9 @@ __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const fl
   auto gidx = [&](int i, int j) {
     return (long long)(i - (h.nmin1 - 4)) + L * (long long)(j - h.lo2);
   };
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int warp = tid >> 5, lane = tid & 31;
   const int n1 = h.nmax1 - h.nmin1 + 1, n2 = h.nmax2 - h.nmin2 + 1;
-  __syncthreads();   // interior values of the tile are stored
+  t2_bar(bar);   // interior values of the tile are stored
   if (top || bottom) {
     // Warp 0: top z lines, warp 1: bottom z lines; lane = column.
     const bool mine = (warp == 0 && top) || (warp == 1 && bottom);
@@ -505,7 +527,7 @@ __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const fl
       for (int k = 0; k < 8; ++k) u3[gidx(p - k * dir, j)] = out[k];
     }
   }
-  __syncthreads();   // z lines done before the x lines read the corners
+  t2_bar(bar);   // z lines done before the x lines read the corners
   if (left || right) {
     // Threads 0..63: left x lines, 64..127: right x lines; one row each.
     const bool rgt = tid >= 64;
@@ -529,6 +551,31 @@ __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const fl
       for (int k = 0; k < 8; ++k) u3[gidx(i, p - k * dir)] = out[k];
     }
   }
+}
+
+// Per-step scalars of shot b for step s of this launch.
+template <bool ADJ>
+__device__ __forceinline__ T2Step t2_step_of(const BatchTables &t, const T2Shot &h, int b, int s) {
+  const ShotDev &S = t.shots[b];
+  T2Step st;
+  st.live = s < h.nsteps && (h.adj2d != 0) == ADJ;
+  st.it = h.tmin + s * h.tstep;
+  st.snap = (st.it % h.snapi) == 0 && (h.extract_wave || h.imaging != 0);
+  const int cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
+                              : h.tmin / h.snapi - (st.it - 1) / h.snapi;
+  const long long nphys = (long long)h.nz * h.nx;
+  st.extract = st.snap && h.extract_wave && cnt <= S.ntsnap && h.imaging <= 2;
+  st.wsave = st.extract ? S.wave + (long long)(cnt - 1) * nphys : nullptr;
+  const int index = S.ntsnap - cnt + 1;
+  st.img = (st.snap && (h.imaging == 1 || h.imaging == 2) && h.tstep < 0 && index >= 1)
+               ? h.imaging : 0;
+  st.wimg = st.img ? S.wave + (long long)(index - 1) * nphys : nullptr;
+  st.image = S.image;
+  st.illum = S.illum;
+  st.taperx = S.taperx;
+  st.tapery0 = S.taperx ? S.tapery[0] : 1.f;
+  st.pad_ = 0;
+  return st;
 }
 
 template <bool ADJ>
@@ -560,29 +607,7 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     }
   }
   __syncthreads();
-  if (tid < t.nshots) {
-    const T2Shot &h = shots[tid];
-    const ShotDev &S = t.shots[tid];
-    T2Step st;
-    st.live = s < h.nsteps && (h.adj2d != 0) == ADJ;
-    st.it = h.tmin + s * h.tstep;
-    st.snap = (st.it % h.snapi) == 0 && (h.extract_wave || h.imaging != 0);
-    const int cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
-                                : h.tmin / h.snapi - (st.it - 1) / h.snapi;
-    const long long nphys = (long long)h.nz * h.nx;
-    st.extract = st.snap && h.extract_wave && cnt <= S.ntsnap && h.imaging <= 2;
-    st.wsave = st.extract ? S.wave + (long long)(cnt - 1) * nphys : nullptr;
-    const int index = S.ntsnap - cnt + 1;
-    st.img = (st.snap && (h.imaging == 1 || h.imaging == 2) && h.tstep < 0 && index >= 1)
-                 ? h.imaging : 0;
-    st.wimg = st.img ? S.wave + (long long)(index - 1) * nphys : nullptr;
-    st.image = S.image;
-    st.illum = S.illum;
-    st.taperx = S.taperx;
-    st.tapery0 = S.taperx ? S.tapery[0] : 1.f;
-    st.pad_ = 0;
-    steps[tid] = st;
-  }
+  if (tid < t.nshots) steps[tid] = t2_step_of<ADJ>(t, shots[tid], tid, s);
   __syncthreads();
   if (tid == 0) {
     // Keep the tiles of shots that are live this step and use this variant.
@@ -608,7 +633,7 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     const T2Shot &h = shots[t2_b(e)];
     const T2Step &stp = steps[t2_b(e)];
     T2Img P;
-    if (stp.img && t2_phys_tile(h, e)) t2_img_load(h, stp, e, P);
+    if (stp.img && t2_phys_tile(h, e)) t2_img_load(h, stp, e, P, tid);
     // A wait that gives up records the error; the tile is still computed (on
     // whatever the stage holds) so that every thread reaches the same
     // barriers, and the loop ends after it.
@@ -618,10 +643,10 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     }
     {
       const float *st = t2_smem + cur * SF;
-      t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st);
+      t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st, tid);
       if ((stp.extract || stp.img) && t2_phys_tile(h, e))
-        t2_snap_tile<ADJ>(h, stp, P, e, st, st + T2_HALO);
-      t2_edges<ADJ>(h, s, e, st);
+        t2_snap_tile<ADJ>(h, stp, P, e, st, st + T2_HALO, tid);
+      t2_edges<ADJ>(h, s, e, st, tid, 0);
     }
     __syncthreads();   // the stage is free for tile k+2
     if (*abort_flag) {
@@ -633,6 +658,122 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       }
       break;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised variant: one CTA per SM with a producer warp and two
+// consumer groups of 8 warps.  Four stages; tile k of the CTA's list goes
+// to stage k % 4 and consumer group k % 2, so each group computes while the
+// producer keeps up to three further tiles in flight.  Stages are handed
+// back through "empty" mbarriers (one arrival per consumer warp) instead of
+// CTA-wide barriers; the groups synchronise internally with named barriers.
+// ---------------------------------------------------------------------------
+constexpr int T2W_STAGES = 4;
+constexpr int T2W_THREADS = 544;   // 2 x 256 consumers + 1 producer warp
+
+template <bool ADJ>
+__host__ __device__ constexpr size_t t2w_smem_bytes() {
+  return T2W_STAGES * sizeof(float) * t2_stage_floats<ADJ>() + sizeof(T2Shot) * T2_MAX_SHOTS +
+         sizeof(T2Step) * T2_MAX_SHOTS + sizeof(int) * (T2_MAX_TILES_PER_CTA + 8) +
+         2 * T2W_STAGES * 8;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <bool ADJ>
+__device__ __forceinline__ void tile2d_ws(const BatchTables &t, int s_off, int n_tiles) {
+  extern __shared__ __align__(128) float t2_smem[];
+  constexpr int SF = t2_stage_floats<ADJ>();
+  T2Shot *shots = reinterpret_cast<T2Shot *>(t2_smem + T2W_STAGES * SF);
+  T2Step *steps = reinterpret_cast<T2Step *>(shots + T2_MAX_SHOTS);
+  int *list = reinterpret_cast<int *>(steps + T2_MAX_SHOTS);
+  int *nlist = list + T2_MAX_TILES_PER_CTA;
+  volatile int *abort_flag = nlist + 1;
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<char *>(t2_smem) + t2w_smem_bytes<ADJ>() - 2 * T2W_STAGES * 8);
+  unsigned long long *empty = full + T2W_STAGES;
+  const int tid = threadIdx.x;
+  const int s = *t.counter + s_off;
+  {
+    const int *src = reinterpret_cast<const int *>(t.t2shots);
+    int *dst = reinterpret_cast<int *>(shots);
+    const int nw = t.nshots * (int)(sizeof(T2Shot) / sizeof(int));
+    for (int q = tid; q < nw; q += T2W_THREADS) dst[q] = src[q];
+    for (int k = tid; blockIdx.x + k * gridDim.x < n_tiles && k < T2_MAX_TILES_PER_CTA;
+         k += T2W_THREADS)
+      list[k] = t.tile_tab[blockIdx.x + k * gridDim.x];
+    if (tid == 0) {
+      for (int q = 0; q < T2W_STAGES; ++q) {
+        mbar_init(&full[q], 1);
+        mbar_init(&empty[q], 8);
+      }
+      mbar_fence_init();
+      *abort_flag = 0;
+    }
+  }
+  __syncthreads();
+  if (tid < t.nshots) steps[tid] = t2_step_of<ADJ>(t, shots[tid], tid, s);
+  __syncthreads();
+  if (tid == 0) {
+    int n = 0;
+    for (int k = 0; blockIdx.x + k * gridDim.x < n_tiles && k < T2_MAX_TILES_PER_CTA; ++k) {
+      const int e = list[k];
+      if (steps[t2_b(e)].live) list[n++] = e;
+    }
+    *nlist = n;
+  }
+  __syncthreads();
+  const int n = *nlist;
+  const int warp = tid >> 5;
+  if (warp == 16) {
+    // Producer: one thread issues every tile once its stage is free.
+    if ((tid & 31) == 0) {
+      int k = 0;
+      for (; k < n && !*abort_flag; ++k) {
+        const int st = k % T2W_STAGES, use = k / T2W_STAGES;
+        if (use > 0 && !mbar_wait(&empty[st], (unsigned)((use - 1) & 1))) {
+          atomicOr(t.err, 1);
+          *abort_flag = 1;
+          break;
+        }
+        const int e = list[k];
+        t2_issue<ADJ>(t.t2maps[t2_b(e)], shots[t2_b(e)], s, e, t2_smem + st * SF, &full[st]);
+      }
+      // After an abort, wait (bounded) for the latest copy issued into each
+      // stage, so that none lands after the CTA has finished.
+      if (*abort_flag) {
+        for (int q = (k > T2W_STAGES ? k - T2W_STAGES : 0); q < k; ++q)
+          mbar_wait(&full[q % T2W_STAGES], (unsigned)((q / T2W_STAGES) & 1));
+      }
+    }
+    return;
+  }
+  // Consumers never leave the loop early, so every thread of a group reaches
+  // the group's named barriers; after an abort the waits are skipped and
+  // the remaining tiles are run through (their results are discarded with
+  // the error status).
+  const int g = warp >> 3, gtid = tid & 255;
+  for (int k = g; k < n; k += 2) {
+    const int st = k % T2W_STAGES;
+    const int e = list[k];
+    const T2Shot &h = shots[t2_b(e)];
+    const T2Step &stp = steps[t2_b(e)];
+    T2Img P;
+    if (stp.img && t2_phys_tile(h, e)) t2_img_load(h, stp, e, P, gtid);
+    if (!*abort_flag && !mbar_wait(&full[st], (unsigned)((k / T2W_STAGES) & 1))) {
+      atomicOr(t.err, 1);
+      *abort_flag = 1;
+    }
+    const float *stg = t2_smem + st * SF;
+    t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, stg, gtid);
+    if ((stp.extract || stp.img) && t2_phys_tile(h, e))
+      t2_snap_tile<ADJ>(h, stp, P, e, stg, stg + T2_HALO, gtid);
+    t2_edges<ADJ>(h, s, e, stg, gtid, 1 + g);
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&empty[st]);
   }
 }
 
