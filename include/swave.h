@@ -243,6 +243,14 @@ typedef struct sw_fwi_desc {
   float illu_pow;           /* invparam%illupow (default 1)               */
   int smooth_rect1, smooth_rect2, smooth_rect3;  /* triangle2 half-widths  */
   int smooth_doz, smooth_dox, smooth_doy;
+  /* Snapshot memory (no counterpart in the reference, which keeps every
+   * snapshot in RAM or on disk, 3DRTM.f90:77-109):
+   *   0      store all ntsnap snapshots of a shot in HBM;
+   *   K > 0  keep the forward state (4 padded fields) every K snapshots and
+   *          recompute K + 2 snapshots at a time during the backward pass:
+   *          memory (ntsnap/K) x 4 padded fields + (K + 2) snapshots, one
+   *          extra forward propagation; results identical to store-all. */
+  int checkpoint_snaps;
 } sw_fwi_desc;
 
 /* compute_fct_gdt (compute_function_gradient.f90:208-350): for every shot

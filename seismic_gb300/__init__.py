@@ -65,7 +65,7 @@ class SwFwiDesc(C.Structure):
     _fields_ = [("g", SwGenpar), ("aperture_x", C.c_float), ("aperture_y", C.c_float),
                 ("illu_pow", C.c_float), ("smooth_rect1", C.c_int), ("smooth_rect2", C.c_int),
                 ("smooth_rect3", C.c_int), ("smooth_doz", C.c_int), ("smooth_dox", C.c_int),
-                ("smooth_doy", C.c_int)]
+                ("smooth_doy", C.c_int), ("checkpoint_snaps", C.c_int)]
 
 
 class SwShot(C.Structure):

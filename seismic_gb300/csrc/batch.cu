@@ -28,8 +28,8 @@ __device__ __forceinline__ int find_shot(const int *start, int n, int idx) {
 // Extraction_wavefield (Extraction.f90:574-575) and the imaging conditions
 // (Imaging.f90:242-244, 760-762).
 __device__ __forceinline__ int snap_count(const ShotDev &S, int it) {
-  if (S.tstep > 0) return it / S.snapi - (S.tmin - 1) / S.snapi;
-  return S.tmin / S.snapi - (it - 1) / S.snapi;
+  if (S.tstep > 0) return it / S.snapi - (S.tcnt - 1) / S.snapi;
+  return S.tcnt / S.snapi - (it - 1) / S.snapi;
 }
 
 __device__ __forceinline__ float lap_axis(const float *__restrict__ u, long long p, long long s,

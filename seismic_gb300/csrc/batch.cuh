@@ -37,6 +37,7 @@ struct ShotDev {
   float *rec_tr;          // nrec*nt
   // time axis of this phase
   int tmin, tstep, nsteps, nt, snapi, ntsnap;
+  int tcnt;               // first time sample of the whole phase (snapshot counting)
   int extract_wave, imaging, adj2d, adj3d;
   float *wave;            // ntsnap*nz*nx*ny snapshots
   float *image, *illum;
@@ -55,6 +56,7 @@ struct T2Shot {
   float c0z, c1z, c2z, c3z, c4z, c0x, c1x, c2x, c3x, c4x, k12, div11;
   int ld1, lo2, n2p, nmin1, nmax1, nmin2, nmax2, nz, nx;
   int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
+  int tcnt;
   int off1, off2;         // tile origin: nmin1 - off1, nmin2 - off2
   int ntz, ntx;           // tiles along z and x
 };

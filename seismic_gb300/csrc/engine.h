@@ -65,6 +65,13 @@ struct DevIO {
   float *illum_dev = nullptr;
   const float *ref_dev = nullptr;
   float *final_u2_host = nullptr;
+  // Checkpointed phases: the phase starts from init_state instead of zero
+  // fields and leaves its final state in save_state (device arrays of 4
+  // padded fields: u_1, u0, u1, u2).  tcnt, when non-zero, is the first
+  // time sample of the whole phase, which snapshot counting refers to.
+  const float *init_state = nullptr;
+  float *save_state = nullptr;
+  int tcnt = 0;
 };
 
 // A shot's model window (ModelSpace%oxw, nxw, ...).

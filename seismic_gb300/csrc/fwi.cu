@@ -292,8 +292,6 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     a.rec_coord = sh.rec_coord;
     if ((st = upload(c, "rec_tr", nullptr, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
     a.rec_trace_dev = (float *)p;
-    if ((st = upload(c, "wave", nullptr, nw * std::max(ntsnap, 1) * sizeof(float), &p))) return st;
-    a.wave_dev = (float *)p;
     sw_prop_desc fd;
     std::memset(&fd, 0, sizeof(fd));
     fd.g = g;
@@ -301,8 +299,34 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     fd.fd_scheme = SW_FD_FORWARD;
     fd.injection = SW_INJ_SINC;
     fd.extraction = SW_EXT_SIMPLE_AFWI;
-    fd.extract_wave = 1;
-    if ((st = propagate_dev(c, fd, a))) return st;
+    // Checkpointed snapshots: K snapshots per segment (K >= 2).
+    const int K = d.checkpoint_snaps > 0 ? std::max(d.checkpoint_snaps, 2) : 0;
+    const bool ckpt = K > 0 && ntsnap > K;
+    const int nseg = ckpt ? (ntsnap + K - 1) / K : 1;
+    const size_t nf = (size_t)Gw.total();
+    float *dck = nullptr, *dseg = nullptr, *dadj = nullptr;
+    if (!ckpt) {
+      if ((st = upload(c, "wave", nullptr, nw * std::max(ntsnap, 1) * sizeof(float), &p))) return st;
+      a.wave_dev = (float *)p;
+      fd.extract_wave = 1;
+      if ((st = propagate_dev(c, fd, a))) return st;
+    } else {
+      // Forward in segments; the state after step (jK-1)*snapi, j = 1..nseg-1,
+      // is kept as checkpoint j (4 padded fields).
+      dck = (float *)dbuf(c, "fwi_ckpt", (size_t)(nseg - 1) * 4 * nf * sizeof(float), &st);
+      dseg = (float *)dbuf(c, "fwi_seg", (size_t)(K + 2) * nw * sizeof(float), &st);
+      dadj = (float *)dbuf(c, "fwi_adj_state", 4 * nf * sizeof(float), &st);
+      if (!dck || !dseg || !dadj) return st;
+      for (int j = 0; j < nseg; ++j) {
+        fd.tmin = j == 0 ? 1 : (j * K - 1) * g.snapi + 1;
+        fd.tmax = j == nseg - 1 ? nt : ((j + 1) * K - 1) * g.snapi;
+        DevIO aj = a;
+        aj.tcnt = 1;
+        aj.init_state = j > 0 ? dck + (size_t)(j - 1) * 4 * nf : nullptr;
+        aj.save_state = j < nseg - 1 ? dck + (size_t)j * 4 * nf : nullptr;
+        if ((st = propagate_dev(c, fd, aj))) return st;
+      }
+    }
     // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40).
     float *ddobs = nullptr, *dmute = nullptr, *dres = nullptr;
     if ((st = upload(c, "dobs", sh.dobs, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
@@ -343,7 +367,39 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     bd.fd_scheme = SW_FD_FORWARD;
     bd.injection = SW_INJ_SIMPLE;
     bd.imaging = SW_IMG_AFWI;
-    if ((st = propagate_dev(c, bd, b))) return st;
+    if (!ckpt) {
+      if ((st = propagate_dev(c, bd, b))) return st;
+    } else {
+      // Segments from the last to the first: recompute snapshots
+      // max(jK,1)..min((j+1)K+1, ntsnap) from checkpoint j into the segment
+      // buffer (slot = snapshot - jK), then run the backward steps whose
+      // imaging reads them; the adjoint state carries over between segments.
+      // The wave pointer is offset so that the kernels' global snapshot
+      // numbers land in the segment buffer.
+      sw_prop_desc rd = fd;
+      rd.extraction = SW_EXT_NONE;
+      rd.extract_wave = 1;
+      for (int j = nseg - 1; j >= 0; --j) {
+        float *wbase = dseg - (ptrdiff_t)(j * K - 1) * (ptrdiff_t)nw;
+        rd.tmin = j == 0 ? 1 : (j * K - 1) * g.snapi + 1;
+        rd.tmax = std::min(((j + 1) * K + 1) * g.snapi, nt);
+        DevIO rj = a;
+        rj.nrec = 0;
+        rj.rec_trace_dev = nullptr;
+        rj.wave_dev = wbase;
+        rj.tcnt = 1;
+        rj.init_state = j > 0 ? dck + (size_t)(j - 1) * 4 * nf : nullptr;
+        if ((st = propagate_dev(c, rd, rj))) return st;
+        bd.tmin = j == nseg - 1 ? nt : (j + 1) * K * g.snapi;
+        bd.tmax = j == 0 ? 1 : j * K * g.snapi + 1;
+        DevIO bj = b;
+        bj.wave_dev = wbase;
+        bj.tcnt = nt;
+        bj.init_state = j == nseg - 1 ? nullptr : dadj;
+        bj.save_state = j > 0 ? dadj : nullptr;
+        if ((st = propagate_dev(c, bd, bj))) return st;
+      }
+    }
     // mod_copy_image (ExtractPadModel.f90:662-697), shots in order.
     if ((e = launch_copy_image(G.nz, G.nx, G.ny, G.ox, G.oy, G.dx, G.dy, w.nxw, w.nyw, w.oxw,
                                w.oyw, b.image_dev, b.illum_dev, dgrad, dill, s)) != cudaSuccess)

@@ -158,6 +158,7 @@ extern "C" int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const f
   S.rec_tr = rec;
   S.vconst = 1.f;
   S.tmin = 1;
+  S.tcnt = 1;
   S.tstep = 1;
   S.nsteps = nt;
   S.nt = nt;

@@ -147,8 +147,14 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     const size_t nf = (size_t)G[b].total();
     for (int q = 0; q < 5; ++q) {
       S.f[q] = carve<float>(cur, nf);
-      if ((e = cudaMemsetAsync(S.f[q], 0, nf * sizeof(float), s)) != cudaSuccess)
-        return cuda_fail(c, e, "zero fields");
+      // Level L at step 0 is buffer L: a checkpointed phase resumes from the
+      // saved u_1, u0, u1, u2; u3 (and every level otherwise) starts at 0.
+      if (io.init_state && q < 4)
+        e = cudaMemcpyAsync(S.f[q], io.init_state + (size_t)q * nf, nf * sizeof(float),
+                            cudaMemcpyDeviceToDevice, s);
+      else
+        e = cudaMemsetAsync(S.f[q], 0, nf * sizeof(float), s);
+      if (e != cudaSuccess) return cuda_fail(c, e, "initial fields");
     }
     S.adj2d = g.twoD && d.fd_scheme == SW_FD_ADJOINT;
     S.adj3d = !g.twoD && d.fd_scheme == SW_FD_ADJOINT;
@@ -195,6 +201,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         S.vconst = g.twoD ? 1.f / (g.dz * g.dx) : 1.f / ((g.dz * g.dx) * g.dy);
     }
     S.tmin = d.tmin;
+    S.tcnt = io.tcnt ? io.tcnt : d.tmin;
     S.tstep = d.tstep;
     S.nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
     S.nt = g.nt;
@@ -267,6 +274,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.nmin1 = S.g.nmin1; h.nmax1 = S.g.nmax1; h.nmin2 = S.g.nmin2; h.nmax2 = S.g.nmax2;
       h.nz = S.g.nz; h.nx = S.g.nx;
       h.nsteps = S.nsteps; h.tmin = S.tmin; h.tstep = S.tstep; h.snapi = S.snapi;
+      h.tcnt = S.tcnt;
       h.adj2d = S.adj2d; h.inj_on = S.inj_on;
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
@@ -358,8 +366,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       by += (uint64_t)S.npts * 24ull;
       const int it = S.tmin + sidx * S.tstep;
       if (it % S.snapi != 0) continue;
-      const int cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
-                                  : S.tmin / S.snapi - (it - 1) / S.snapi;
+      const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
+                                  : S.tcnt / S.snapi - (it - 1) / S.snapi;
       const bool slot = S.tstep > 0 ? cnt <= S.ntsnap : S.ntsnap - cnt + 1 >= 1;
       if (!slot) continue;
       uint64_t per = S.extract_wave ? 4 : 0;
@@ -472,6 +480,16 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   c->stats.launches_total += launches;
   c->stats.launches_step += (uint64_t)max_steps;
   // ---- outputs ----
+  for (int b = 0; b < nb; ++b) {
+    if (!shots[b].io.save_state) continue;
+    // Level L after the last step is buffer (L + nsteps) mod 5.
+    const size_t nf = (size_t)G[b].total();
+    for (int q = 0; q < 4; ++q) {
+      e = cudaMemcpyAsync(shots[b].io.save_state + (size_t)q * nf, hs[b].f[(q + hs[b].nsteps) % 5],
+                          nf * sizeof(float), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_fail(c, e, "save state");
+    }
+  }
   for (int b = 0; b < nb; ++b) {
     if (!shots[b].io.final_u2_host) continue;
     const int last = hs[b].nsteps;   // u2 after the last step = f[(last+3)%5]

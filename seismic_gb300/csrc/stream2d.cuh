@@ -182,8 +182,8 @@ __device__ __forceinline__ void stream2d_body(const BatchTables &t, int s_off, i
       if (phys && snapstep) {
         pp = (long long)(i - 1) + (long long)g.nz * (j - 1);
         if (S.taperx) taper = S.taperx[j - 1] * S.tapery[0];
-        cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
-                          : S.tmin / S.snapi - (it - 1) / S.snapi;
+        cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
+                          : S.tcnt / S.snapi - (it - 1) / S.snapi;
         // Injection_Born (Imaging.f90:747-788).
         if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap) {
           const float vc = ADJ ? vel[p] : c_v;

@@ -150,8 +150,8 @@ __device__ __forceinline__ void stream3d_body(const BatchTables &t, int s_off, i
       if (phys && snapstep) {
         pp = g.pidx(i, j, k);
         if (S.taperx) taper = S.taperx[j - 1] * S.tapery[k - 1];
-        cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
-                          : S.tmin / S.snapi - (it - 1) / S.snapi;
+        cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
+                          : S.tcnt / S.snapi - (it - 1) / S.snapi;
         if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap)
           sv = sv + (((2.0f * taper) * S.ref[pp]) * S.wave[(long long)(cnt - 1) * nphys + pp]) / vel[p];
       }

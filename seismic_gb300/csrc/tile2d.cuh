@@ -166,8 +166,8 @@ __device__ __noinline__ float t2_snap_generic(const ShotDev &S, int it, int i, i
   const long long nphys = (long long)g.nz * g.nx;
   const long long pp = (long long)(i - 1) + (long long)g.nz * (j - 1);
   const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
-  const int cnt = S.tstep > 0 ? it / S.snapi - (S.tmin - 1) / S.snapi
-                              : S.tmin / S.snapi - (it - 1) / S.snapi;
+  const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
+                              : S.tcnt / S.snapi - (it - 1) / S.snapi;
   // Injection_Born (Imaging.f90:747-788).
   if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap)
     se = se + (((2.0f * taper) * S.ref[pp]) * S.wave[(long long)(cnt - 1) * nphys + pp]) / vc;
@@ -561,8 +561,8 @@ __device__ __forceinline__ T2Step t2_step_of(const BatchTables &t, const T2Shot 
   st.live = s < h.nsteps && (h.adj2d != 0) == ADJ;
   st.it = h.tmin + s * h.tstep;
   st.snap = (st.it % h.snapi) == 0 && (h.extract_wave || h.imaging != 0);
-  const int cnt = h.tstep > 0 ? st.it / h.snapi - (h.tmin - 1) / h.snapi
-                              : h.tmin / h.snapi - (st.it - 1) / h.snapi;
+  const int cnt = h.tstep > 0 ? st.it / h.snapi - (h.tcnt - 1) / h.snapi
+                              : h.tcnt / h.snapi - (st.it - 1) / h.snapi;
   const long long nphys = (long long)h.nz * h.nx;
   st.extract = st.snap && h.extract_wave && cnt <= S.ntsnap && h.imaging <= 2;
   st.wsave = st.extract ? S.wave + (long long)(cnt - 1) * nphys : nullptr;

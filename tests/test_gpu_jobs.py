@@ -100,6 +100,30 @@ def test_fwi_fct_gdt_matches_oracle(ctx, oracle):
     assert rel_l2(illum, rillum) < 1e-6
 
 
+@pytest.mark.parametrize("K", [2, 3, 7])
+def test_fwi_checkpointed_equals_store_all(ctx, K):
+    """Checkpointed snapshots (state every K snapshots, K + 2 recomputed at a
+    time in the backward pass) give the store-all misfit and gradient bit for
+    bit: the recomputed forward steps repeat the same operations."""
+    d, vel, w, shots, mask = _fwi_case()
+    d.checkpoint_snaps = 0
+    f0, g0, il0 = ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    ctx.reset_stats()
+    d.checkpoint_snaps = K
+    f1, g1, il1 = ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    pts_ck = ctx.stats()["points_updated"]
+    assert f1 == f0
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(il1, il0)
+    # One extra forward propagation; each segment recomputes K + 2 snapshot
+    # intervals, so the recomputation is about (K + 2) / K forward runs.
+    ctx.reset_stats()
+    d.checkpoint_snaps = 0
+    ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    pts_all = ctx.stats()["points_updated"]
+    assert 1.4 * pts_all < pts_ck <= (1.0 + (K + 2) / (2.0 * K) + 0.02) * pts_all
+
+
 def test_lbfgs_device_matches_oracle(ctx, oracle):
     """A few LBFGS iterations on a bound-constrained quadratic."""
     n = 5000
