@@ -1,0 +1,132 @@
+"""Self-pinning checks of the oracle that the reference's own tests do not
+provide: an FP64 dot-product test of the stencil / adjoint-stencil pair,
+finite-difference checks of the FWI gradient along seeded smooth directions,
+and the instability of reconstructing the forward wavefield backwards in
+time from boundary strips (why snapshots are stored or recomputed from
+checkpoints instead)."""
+import numpy as np
+import pytest
+
+import seismic_gb300 as sw
+from seismic_gb300 import synth
+
+
+def _padded(g):
+    return sw.padded_shape(g)
+
+
+def test_stencil_adjoint_dot_product_fp64(oracle):
+    """<A x, y> = <x, A^T y> for A = v^2 Lap (FDderivatives.f90:715-743) and
+    A^T = Lap(v^2 .) (FDderivatives.f90:847-891), with x, y supported away
+    from the domain edges (where the adjoint clamps the velocity index)."""
+    g = sw.make_genpar(48, 56, 1, dz=10.0, dx=12.0, ntaper=6)
+    rng = np.random.default_rng(33)
+    vel = rng.uniform(1500.0, 4000.0, (g.nx, g.nz))
+    shp = _padded(g)                      # (1, n2p, n1p)
+    x = np.zeros(shp)
+    y = np.zeros(shp)
+    core = (0, slice(20, shp[1] - 20), slice(20, shp[2] - 20))
+    x[core] = rng.standard_normal(x[core].shape)
+    y[core] = rng.standard_normal(y[core].shape)
+    ax = oracle.stencil_f64(g, vel, x)
+    aty = oracle.stencil_f64(g, vel, y, adjoint=True)
+    lhs = float(np.sum(ax * y))
+    rhs = float(np.sum(x * aty))
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), abs(rhs))
+
+
+def _fwi_setup(snapi=1):
+    nz, nx, d, dt, nt = 40, 70, 10.0, 1.5e-3, 400
+    z = np.arange(nz)[None, :] * d
+    x = np.arange(nx)[:, None] * d
+    blob = np.exp(-((x - 350.0) ** 2 + (z - 200.0) ** 2) / (2 * 60.0 ** 2))
+    vtrue = (1800 + 0.8 * z + 150 * blob).astype(np.float32)
+    v0 = (1800 + 0.8 * z + 0 * x).astype(np.float32)
+    g = sw.make_genpar(nz, nx, 1, dz=d, dx=d, dt=dt, nt=nt, ntaper=10, lsinc=7, snapi=snapi,
+                       fmax=30.0)
+    w = synth.ricker(12.0, dt, nt)
+    desc = sw.SwFwiDesc()
+    desc.g = g
+    desc.aperture_x, desc.aperture_y, desc.illu_pow = 0.0, 0.0, 0.0   # no illumination scaling
+    desc.smooth_rect1 = desc.smooth_rect2 = desc.smooth_rect3 = 1
+    desc.smooth_doz = desc.smooth_dox = desc.smooth_doy = 0          # no smoothing
+    shots = []
+    for sx in (205.0, 455.0):
+        rec = np.zeros((60, 3), np.float32)
+        rec[:, 0] = 12.0
+        rec[:, 1] = np.linspace(20.0, 670.0, 60)
+        shots.append({"sou": np.array([21.0, sx, 0.0], np.float32), "rec": rec,
+                      "dobs": np.zeros((60, nt), np.float32),
+                      "resid": np.zeros((60, nt), np.float32)})
+    return desc, vtrue, v0, w, shots
+
+
+def test_fwi_gradient_along_smooth_directions(oracle):
+    """Finite differences of the misfit along 8 seeded smooth directions
+    against <g, dm> from compute_fct_gdt (compute_function_gradient.f90:
+    208-350, AFWI imaging Imaging.f90:371-422).  The reference's gradient is
+    a descent direction (l_bfgs negates it, Inversion.f90:118-125) from an
+    approximate adjoint, so the check is on correlation and sign: the
+    directional derivatives correlate at > 0.85 with minus the FD values."""
+    from scipy.ndimage import gaussian_filter
+    desc, vtrue, v0, w, shots = _fwi_setup()
+    oracle.fwi_fct_gdt(desc, vtrue, w, shots)           # data of the true model
+    for s in shots:
+        s["dobs"] = -s.pop("resid")                     # resid = dobs - dmod with dobs = 0
+    f0, g0, _ = oracle.fwi_fct_gdt(desc, v0, w, shots)
+    assert f0 > 0 and np.abs(g0).max() > 0
+    rng = np.random.default_rng(8)
+    an, fd = [], []
+    for _ in range(8):
+        dm = gaussian_filter(rng.standard_normal(v0.shape), 4.0)
+        dm /= np.abs(dm).max()
+        fp, _, _ = oracle.fwi_fct_gdt(desc, (v0 + dm).astype(np.float32), w, shots)
+        fm, _, _ = oracle.fwi_fct_gdt(desc, (v0 - dm).astype(np.float32), w, shots)
+        fd.append((fp - fm) / 2.0)
+        an.append(float(np.dot(g0.astype(np.float64).ravel(), dm.ravel())))
+    an, fd = np.array(an), np.array(fd)
+    assert np.corrcoef(an, -fd)[0, 1] > 0.85
+    assert np.dot(an, fd) < 0
+
+
+def test_backward_reconstruction_from_strips_diverges():
+    """Running the 5-level scheme backwards (solving its update for u_-1, the
+    reconstruction a boundary-strip method needs) amplifies rounding errors
+    by the inverse parasitic roots, 1/0.224 = 4.5 per step: a 1e-15
+    perturbation exceeds 1 within about 25 steps.  The reconstruction is
+    infeasible for this scheme; snapshots are stored or recomputed from
+    checkpoints instead."""
+    n, d, v, dt = 96, 10.0, 2000.0, 1e-3
+    c = np.array([-205 / 72, 8 / 5, -1 / 5, 8 / 315, -1 / 560]) / d ** 2
+
+    def lap(u):
+        out = 2 * c[0] * u
+        for k in range(1, 5):
+            out += c[k] * (np.roll(u, k, 0) + np.roll(u, -k, 0) + np.roll(u, k, 1) +
+                           np.roll(u, -k, 1))
+        return out
+
+    k12 = 12 * dt * dt
+    x = np.arange(n) * d
+    X, Z = np.meshgrid(x, x, indexing="ij")
+    u = [np.exp(-((X - 480) ** 2 + (Z - 480) ** 2) / (2 * 60.0 ** 2)) * a
+         for a in (0.97, 0.98, 0.99, 1.0)]               # u_-1, u0, u1, u2
+    for _ in range(200):                                  # forward, FDderivatives.f90:960-982
+        u3 = (20 * u[3] - 6 * u[2] - 4 * u[1] + u[0] + k12 * v * v * lap(u[3])) / 11
+        u = u[1:] + [u3]
+    rng = np.random.default_rng(0)
+    p = [a + 1e-15 * rng.standard_normal(a.shape) for a in u]
+    e0 = max(np.abs(a - b).max() for a, b in zip(p, u))
+    steps = 0
+    while steps < 60:
+        # Backwards: u_-1 = 11 u3 - 20 u2 + 6 u1 + 4 u0 - 12 dt^2 v^2 Lap u2
+        um1 = 11 * p[3] - 20 * p[2] + 6 * p[1] + 4 * p[0] - k12 * v * v * lap(p[2])
+        ref = 11 * u[3] - 20 * u[2] + 6 * u[1] + 4 * u[0] - k12 * v * v * lap(u[2])
+        p = [um1] + p[:3]
+        u = [ref] + u[:3]
+        steps += 1
+        if np.abs(p[0] - u[0]).max() > 1.0:
+            break
+    assert steps <= 30
+    growth = (np.abs(p[0] - u[0]).max() / e0) ** (1.0 / steps)
+    assert growth > 3.0
