@@ -293,6 +293,27 @@ typedef struct sw_tuning {
 int sw_ctx_set_tuning(sw_ctx *ctx, const sw_tuning *t);
 int sw_ctx_get_tuning(const sw_ctx *ctx, sw_tuning *t);
 
+/* ---- Convolutional gradient preconditioner (N4) --------------------------- */
+/* No counterpart in the reference.  A stack of nlayers 3x3 convolutions
+ * (zero padding, ReLU between layers, channels[0..nlayers], each 1..16,
+ * the last 1) mapping planar FP32 input channels of an nz x nx image
+ * (z fastest) to one output channel.  BF16 weights and activations on the
+ * tcgen05 tensor cores with FP32 accumulation; FP32 master weights and
+ * Adam state.  Weights are packed per layer as w[co][tap][ci] (tap =
+ * 3 * (dx + 1) + (dz + 1)) followed by b[co]. */
+typedef struct sw_cnn sw_cnn;
+int sw_cnn_create(sw_ctx *ctx, int nlayers, const int *channels, uint64_t seed, sw_cnn **out);
+int sw_cnn_destroy(sw_cnn *net);
+int sw_cnn_num_weights(const sw_cnn *net);
+int sw_cnn_get_weights(const sw_cnn *net, float *w);
+int sw_cnn_set_weights(sw_cnn *net, const float *w);
+/* in: channels[0] x nz x nx (planar), out: nz x nx. */
+int sw_cnn_forward(sw_cnn *net, int nz, int nx, const float *in, float *out);
+/* One Adam step (lr; beta 0.9 / 0.999) on the mean over nbatch images of
+ * 0.5 * mean((out - target)^2); *loss receives that mean loss. */
+int sw_cnn_train_step(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
+                      const float *target, float lr, double *loss);
+
 /* ---- Modelling without device allocation --------------------------------- */
 /* No counterpart in the reference (its modelling allocates the wavefields of
  * every shot it runs).  Same arguments, run and results as sw_modeling for

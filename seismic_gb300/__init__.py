@@ -94,6 +94,15 @@ _SIGS = {
     "sw_propagate": (C.c_int, [C.c_void_p, C.POINTER(SwPropDesc), C.POINTER(SwPropIO)]),
     "sw_modeling": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp]),
     "sw_modeling_noalloc": (C.c_int, [C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp]),
+    "sw_cnn_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_uint64,
+                                C.POINTER(C.c_void_p)]),
+    "sw_cnn_destroy": (C.c_int, [C.c_void_p]),
+    "sw_cnn_num_weights": (C.c_int, [C.c_void_p]),
+    "sw_cnn_get_weights": (C.c_int, [C.c_void_p, _fp]),
+    "sw_cnn_set_weights": (C.c_int, [C.c_void_p, _fp]),
+    "sw_cnn_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp, _fp]),
+    "sw_cnn_train_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, C.c_float,
+                                    C.POINTER(C.c_double)]),
     "sw_rtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
     "sw_born": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
     "sw_lsrtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
@@ -441,6 +450,54 @@ def vel_check(g: SwGenpar, vel) -> tuple[int, float, float]:
     a, b = C.c_float(), C.c_float()
     code = lib.sw_vel_check(C.byref(g), fptr(v), C.byref(a), C.byref(b))
     return code, a.value, b.value
+
+
+class CNN:
+    """sw_cnn_*: the convolutional gradient preconditioner on the tensor cores."""
+
+    def __init__(self, ctx: "Context", channels=(2, 16, 16, 16, 1), seed: int = 0):
+        self.ctx = ctx
+        self.channels = list(channels)
+        ch = (C.c_int * len(channels))(*channels)
+        h = C.c_void_p()
+        ctx._check(ctx.lib.sw_cnn_create(ctx.h, len(channels) - 1, ch, seed, C.byref(h)))
+        self.h = h
+
+    @property
+    def num_weights(self) -> int:
+        return self.ctx.lib.sw_cnn_num_weights(self.h)
+
+    def get_weights(self) -> np.ndarray:
+        w = np.zeros(self.num_weights, np.float32)
+        self.ctx._check(self.ctx.lib.sw_cnn_get_weights(self.h, fptr(w)))
+        return w
+
+    def set_weights(self, w) -> None:
+        w = _f32(w)
+        assert w.size == self.num_weights
+        self.ctx._check(self.ctx.lib.sw_cnn_set_weights(self.h, fptr(w)))
+
+    def forward(self, x) -> np.ndarray:
+        """x: (channels[0], nx, nz) planar image stack (z fastest)."""
+        x = _f32(x)
+        c, nx, nz = x.shape
+        out = np.zeros((nx, nz), np.float32)
+        self.ctx._check(self.ctx.lib.sw_cnn_forward(self.h, nz, nx, fptr(x), fptr(out)))
+        return out
+
+    def train_step(self, x, target, lr: float = 1e-3) -> float:
+        """x: (batch, channels[0], nx, nz); target: (batch, nx, nz)."""
+        x, t = _f32(x), _f32(target)
+        b, c, nx, nz = x.shape
+        loss = C.c_double()
+        self.ctx._check(self.ctx.lib.sw_cnn_train_step(self.h, b, nz, nx, fptr(x), fptr(t),
+                                                       float(lr), C.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.sw_cnn_destroy(self.h)
+            self.h = None
 
 
 def modeling_noalloc(g: SwGenpar, vel, sou_coord, wavelet, rec_coord) -> np.ndarray:
