@@ -240,11 +240,15 @@ def main():
                     help="time samples of the CPU sample shot (0: its whole record)")
     ap.add_argument("--nt-cap", type=int, default=0, help="truncate records (debug)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precond-study", action="store_true",
+                    help="run the learned-preconditioner FWI study instead of the RTM bench")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every time step directly (profiling runs: every launch timed)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.precond_study:
+        return run_precond_study()
 
     import torch
 
@@ -397,6 +401,23 @@ def main():
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_precond_study() -> int:
+    """Learned-preconditioned vs plain L-BFGS FWI on seeded 60 x 180 models
+    (network trained on plain runs over 12 other seeds); one JSON line."""
+    import seismic_gb300 as sw
+    from seismic_gb300 import precond
+    ctx = sw.Context(0)
+    r = precond.run_study(ctx, train_seeds=tuple(range(1000, 1012)), test_seeds=(4, 5, 6),
+                          epochs=400, f0=5.0, smooth_m=120.0,
+                          learned_kw={"max_learned": 3, "c1": 0.1})
+    for row in r["tests"]:
+        row.pop("plain_curve")
+        row.pop("learned_curve")
+    print(json.dumps({"study": "learned vs plain L-BFGS FWI", **r}), flush=True)
+    ctx.close()
     return 0
 
 
