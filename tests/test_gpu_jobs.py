@@ -190,3 +190,29 @@ def test_batched_modeling_matches_oracle(ctx, oracle):
         ref = oracle.modeling(gw, vel[i0:i0 + nxw], s["sou"], w[: d.shape[1]], s["rec"])
         assert np.abs(ref).max() > 0
         np.testing.assert_array_equal(d, ref)
+
+
+def test_autotuner_on_device(oracle, tmp_path):
+    """tune_rtm times every candidate on a truncated copy of the batch, caches
+    the winner per device / grid bucket / batch size and applies it; the
+    tuned job still matches the oracle bit for bit."""
+    from seismic_gb300 import autotune
+    g, vel, w, shots = _survey(nshot=3, seed=9)
+    c = sw.Context(0)
+    try:
+        path = str(tmp_path / "tuning.json")
+        entry = autotune.tune_rtm(c, g, vel, w, shots, steps=32, cache_path=path)
+        assert entry["tuning"] in autotune.candidates(True)
+        assert entry["tried"] == len(autotune.candidates(True))
+        again = autotune.tune_rtm(c, g, vel, w, shots, steps=32, cache_path=path)
+        assert again["tuning"] == entry["tuning"]       # served from the cache
+        assert c.tuning()["step_kernel"] == entry["tuning"]["step_kernel"]
+        job = sw.RTMJob(c, g, vel, w, shots)
+        job.set_batch(3)
+        job.run()
+        im, il, _ = job.result()
+        job.close()
+    finally:
+        c.close()
+    rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
+    np.testing.assert_array_equal(im, rim)
