@@ -10,6 +10,7 @@
 #include "stream2d.cuh"
 #include "stream3d.cuh"
 #include "tile2d.cuh"
+#include "tile3d.cuh"
 
 namespace swave {
 
@@ -542,6 +543,34 @@ static cudaError_t launch_tile2d_ws(const BatchTables &t, int s_off, int n_tiles
   return cudaGetLastError();
 }
 
+// TMA-pipelined persistent 3D step (tile3d.cuh), one kernel per variant.
+static_assert(2 * (t3_smem_bytes<false>() + 1024) <= 228 * 1024, "3D tile kernel smem (fwd)");
+static_assert(2 * (t3_smem_bytes<true>() + 1024) <= 228 * 1024, "3D tile kernel smem (adj)");
+
+template <bool ADJ>
+__global__ void __launch_bounds__(256, 2) k_bstep3d_t(BatchTables t, int s_off, int n_units) {
+  tile3d_persistent<ADJ>(t, s_off, n_units);
+}
+
+template <bool ADJ>
+static cudaError_t launch_tile3d(const BatchTables &t, int s_off, int n_units, int nsm,
+                                 cudaStream_t s) {
+  static unsigned long long attr_set = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !(attr_set & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_bstep3d_t<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)t3_smem_bytes<ADJ>());
+    if (e != cudaSuccess) return e;
+    if (dev < 64) attr_set |= 1ull << dev;
+  }
+  const int grid = std::max({1, std::min(n_units, 2 * nsm),
+                             (n_units + T3_MAX_UNITS_PER_CTA - 1) / T3_MAX_UNITS_PER_CTA});
+  k_bstep3d_t<ADJ><<<grid, 256, t3_smem_bytes<ADJ>(), s>>>(t, s_off, n_units);
+  return cudaGetLastError();
+}
+
 // Streaming 3D step (stream3d.cuh), one kernel per stencil variant.
 template <bool ADJ>
 __global__ void __launch_bounds__(256, 4) k_bstep3d_s(BatchTables t, int s_off, int ty) {
@@ -587,7 +616,18 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     cudaError_t ec = record(ev_before);
     if (ec != cudaSuccess) return ec;
   }
-  if (has_3d && tile.stream3d) {
+  if (has_3d && tile.stream3d == 2) {
+    cudaError_t e = cudaSuccess;
+    if (tile.has_fwd3d) {
+      e = launch_tile3d<false>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e == cudaSuccess && tile.has_adj3d) {
+      e = launch_tile3d<true>(t, s_off, n_step_tiles, tile.nsm, s);
+      ++nl;
+    }
+    if (e != cudaSuccess) return e;
+  } else if (has_3d && tile.stream3d) {
     dim3 b3(S3_BZ, S3_BY, 1);
     if (tile.has_fwd3d) {
       k_bstep3d_s<false><<<n_step_tiles, b3, 0, s>>>(t, s_off, tile.ty);

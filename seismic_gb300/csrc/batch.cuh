@@ -38,6 +38,7 @@ struct ShotDev {
   // time axis of this phase
   int tmin, tstep, nsteps, nt, snapi, ntsnap;
   int tcnt;               // first time sample of the whole phase (snapshot counting)
+  int t3_ty;              // planes per work unit of the pipelined 3D kernel
   int extract_wave, imaging, adj2d, adj3d;
   float *wave;            // ntsnap*nz*nx*ny snapshots
   float *image, *illum;
@@ -97,6 +98,13 @@ struct T2Maps {
   CUtensorMap m[12];
 };
 
+// Tensor maps of one shot for the pipelined 3D kernel (rank 3, one plane per
+// box): [2*buf + box], box 0 the 40 x 40 plane tile with halo, 1 the
+// 32 x 32 core tile.
+struct T3Maps {
+  CUtensorMap m[12];
+};
+
 // Prefix tables of a batch (device resident).
 struct BatchTables {
   int nshots;
@@ -111,6 +119,7 @@ struct BatchTables {
   const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
   const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
   const T2Maps *t2maps;   // nshots tensor-map sets (pipelined 2D kernel)
+  const T3Maps *t3maps;   // nshots tensor-map sets (pipelined 3D kernel)
   int *err;               // device error flags (bit 0: a bounded wait gave up)
   int *counter;           // step counter s (0-based)
 };
@@ -125,7 +134,7 @@ struct StepTile {
                        // warp-specialised (tile2d.cuh)
   int tz = 64;
   int tx = 64;
-  int stream3d = 1;    // 3D: 2.5D streaming kernel (stream3d.cuh)
+  int stream3d = 2;    // 3D: 1 2.5D streaming kernel (stream3d.cuh), 2 TMA-pipelined (tile3d.cuh)
   int ty = 32;         // 3D: y planes marched per CTA
   int has_fwd2d = 1;   // set by the runner from the batch's stencil variants
   int has_adj2d = 1;
@@ -153,6 +162,8 @@ inline int step_ctas(const Geom &g, const StepTile &tile) {
     return t2_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;
   }
   if (g.twoD && tile.stream2d) return ((n1 + tile.tz - 1) / tile.tz) * ((n2 + tile.tx - 1) / tile.tx);
+  if (!g.twoD && tile.stream3d == 2)
+    return ((n1 + 31) / 32) * ((n2 + 31) / 32) * ((n3 + tile.ty - 1) / tile.ty);
   if (!g.twoD && tile.stream3d)
     return ((n1 + 31) / 32) * ((n2 + 15) / 16) * ((n3 + tile.ty - 1) / tile.ty);
   return ((n1 + 31) / 32) * ((n2 + 7) / 8) * n3;

@@ -74,7 +74,7 @@ int sw_ctx_set_tuning(sw_ctx *c, const sw_tuning *t) {
       (t->tile_z != 32 && t->tile_z != 64 && t->tile_z != 128))
     return swave::fail(c, SW_BAD_PARAM, "invalid tuning");
   c->run_opts.tile.stream2d = t->step_kernel;
-  c->run_opts.tile.stream3d = t->step_kernel != 0;
+  c->run_opts.tile.stream3d = t->step_kernel == 0 ? 0 : t->step_kernel == 1 ? 1 : 2;
   c->run_opts.tile.ty = t->tile_y;
   c->run_opts.tile.tz = t->tile_z;
   c->run_opts.tile.tx = t->tile_x;

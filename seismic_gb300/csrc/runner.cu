@@ -58,6 +58,21 @@ T *carve(char *&cur, size_t n) {
 
 size_t rup(size_t b) { return (b + 255) / 256 * 256; }
 
+// 3D FP32 tensor map over a padded field (ld1 x n2p x n3p) with a box of
+// bz rows x bx columns x 1 plane.
+bool encode_field_map3(CUtensorMap *m, const float *base, const Geom &g, int bz, int bx) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)g.ld1, (cuuint64_t)g.n2p, (cuuint64_t)g.n3p};
+  const cuuint64_t strides[2] = {(cuuint64_t)g.ld1 * sizeof(float),
+                                 (cuuint64_t)g.ld1 * g.n2p * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)bz, (cuuint32_t)bx, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
@@ -87,6 +102,18 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     if (!fits) tile.stream2d = 1;
   }
   const bool t2 = (tile.stream2d == 2 || tile.stream2d == 3) && shots[0].d.g.twoD;
+  // The pipelined 3D kernel packs (shot, z tile, x tile, y unit) into 7/8/8/8
+  // bits; larger batches or grids use the streaming kernel.
+  if (!shots[0].d.g.twoD && tile.stream3d == 2) {
+    bool fits = nb < 128 && tile.ty >= 1;
+    for (int b = 0; b < nb && fits; ++b) {
+      const Geom g = make_geom(shots[b].d.g);
+      fits = (g.nmax1 - g.nmin1 + 32) / 32 <= 256 && (g.nmax2 - g.nmin2 + 32) / 32 <= 256 &&
+             (g.nmax3 - g.nmin3 + tile.ty) / tile.ty <= 256;
+    }
+    if (!fits) tile.stream3d = 1;
+  }
+  const bool t3 = !shots[0].d.g.twoD && tile.stream3d == 2;
   // ---- host-side plans and arena sizes ----
   size_t bytes = 0;
   for (int b = 0; b < nb; ++b) {
@@ -123,6 +150,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
     bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int)) + rup(nb * sizeof(T2Maps));
+  }
+  if (t3) {
+    size_t ntile = 0;
+    for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
+    bytes += rup(ntile * sizeof(int)) + rup(nb * sizeof(T3Maps));
   }
   bytes += rup(sizeof(int));   // error flags
   char *arena = (char *)dbuf(c, "batch_arena", bytes, &st);
@@ -202,6 +234,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     }
     S.tmin = d.tmin;
     S.tcnt = io.tcnt ? io.tcnt : d.tmin;
+    S.t3_ty = tile.ty;
     S.tstep = d.tstep;
     S.nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
     S.nt = g.nt;
@@ -305,6 +338,35 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     SW_CK(cudaMemcpyAsync(dtile, htile.data(), htile.size() * sizeof(int), cudaMemcpyHostToDevice,
                           s));
   }
+  std::vector<T3Maps> hmaps3;
+  T3Maps *dmaps3 = nullptr;
+  if (t3) {
+    for (int b = 0; b < nb; ++b) {
+      const Geom &g = G[b];
+      const int n1t = (g.nmax1 - g.nmin1 + 32) / 32, n2t = (g.nmax2 - g.nmin2 + 32) / 32;
+      const int n3t = (g.nmax3 - g.nmin3 + tile.ty) / tile.ty;
+      for (int ky = 0; ky < n3t; ++ky)
+        for (int xi = 0; xi < n2t; ++xi)
+          for (int zi = 0; zi < n1t; ++zi)
+            htile.push_back((b << 24) | (zi << 16) | (xi << 8) | ky);
+    }
+    if ((int)htile.size() != step_tiles[nb]) return fail(c, SW_CUDA_ERR, "unit table size");
+    hmaps3.resize(nb);
+    for (int b = 0; b < nb; ++b) {
+      const ShotDev &S = hs[b];
+      for (int q = 0; q < 6; ++q) {
+        const float *base = q < 5 ? S.f[q] : S.vel;
+        if (!encode_field_map3(&hmaps3[b].m[2 * q], base, S.g, 40, 40) ||
+            !encode_field_map3(&hmaps3[b].m[2 * q + 1], base, S.g, 32, 32))
+          return fail(c, SW_CUDA_ERR, "tensor map encoding failed (shot %d)", b);
+      }
+    }
+    dtile = carve<int>(cur, htile.size());
+    dmaps3 = carve<T3Maps>(cur, nb);
+    SW_CK(cudaMemcpyAsync(dmaps3, hmaps3.data(), nb * sizeof(T3Maps), cudaMemcpyHostToDevice, s));
+    SW_CK(cudaMemcpyAsync(dtile, htile.data(), htile.size() * sizeof(int), cudaMemcpyHostToDevice,
+                          s));
+  }
   SW_CK(cudaMemsetAsync(counter, 0, sizeof(int), s));
   int *derr = carve<int>(cur, 1);
   SW_CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
@@ -322,6 +384,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.t2shots = d2;
   t.tile_tab = dtile;
   t.t2maps = dmaps;
+  t.t3maps = dmaps3;
   t.err = derr;
   t.counter = counter;
   // The host plans above must stay alive until the uploads complete.
