@@ -204,41 +204,17 @@ __global__ void k_bv2u(BatchTables t, int s_off) {
 // Sinc gather of one receiver in the loop order of Extraction_1trace_sinc_xy
 // (Extraction.f90:511-560) / _xyz (Extraction.f90:276-337).  H is the
 // half-width when known at compile time (lsinc = 7), else -1.
-template <int H>
-__device__ __forceinline__ float sinc_gather(const ShotDev &S, const Geom &g,
-                                             const float *__restrict__ u2, int r, int i0, int j0,
-                                             int k0, float v, float tr) {
-  const int h = H > 0 ? H : S.ext_half;
-  const int ls = 2 * h + 1;
-  const float *wz = S.wz + (long long)r * ls, *wx = S.wx + (long long)r * ls;
-  if (g.twoD) {
-#pragma unroll
-    for (int jj = -h; jj <= h; ++jj) {
-      const long long pj = g.idx(i0, j0 + jj, 1);
-#pragma unroll
-      for (int ii = -h; ii <= h; ++ii) tr = tr + ((v * u2[pj + ii]) * wz[h + ii]) * wx[h + jj];
-    }
-  } else {
-    for (int kq = -h; kq <= h; ++kq)
-#pragma unroll
-      for (int jj = -h; jj <= h; ++jj) {
-        const long long pj = g.idx(i0, j0 + jj, k0 + kq);
-#pragma unroll
-        for (int ii = -h; ii <= h; ++ii)
-          tr = tr + (((v * u2[pj + ii]) * wz[h + ii]) * wx[h + jj]) * wx[h + kq];
-      }
-  }
-  return tr;
-}
-
 // ---------------------------------------------------------------------------
 // Receiver extraction (Extraction.f90:71-135, 217-247, 276-337, 511-560):
-// one thread per receiver, the sinc sum in the reference loop order.
+// one warp per receiver.  The lanes form the lsinc^2 (3D: lsinc^3) products
+// of a sinc gather 32 at a time, and lane 0 adds them to the trace sample
+// one by one in the reference's loop order (z fastest, then x, then y).
 // ---------------------------------------------------------------------------
 __global__ void k_bextract(BatchTables t, int s_off) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   const int ntot = t.rec_start[t.nshots];
-  if (q >= ntot) return;
+  if (q >= ntot) return;   // uniform per warp
   const int b = find_shot(t.rec_start, t.nshots, q);
   const ShotDev &S = t.shots[b];
   const int s = *t.counter + s_off;
@@ -249,9 +225,8 @@ __global__ void k_bextract(BatchTables t, int s_off) {
   const float *__restrict__ u2 = S.f[(s + 3) % 5];
   const int i0 = S.ric[3 * r], j0 = S.ric[3 * r + 1], k0 = g.twoD ? 1 : S.ric[3 * r + 2];
   float *trp = S.rec_tr + (long long)r * S.nt + (it - 1);
-  float tr = *trp;
   if (S.ext_mode == 2) {  // Extraction_array_simple_afwi_noomp
-    *trp = tr + u2[g.idx(i0, j0, k0)];
+    if (lane == 0) *trp = *trp + u2[g.idx(i0, j0, k0)];
     return;
   }
   float v;
@@ -261,94 +236,41 @@ __global__ void k_bextract(BatchTables t, int s_off) {
   } else {
     v = S.vconst;
   }
-  if (S.ext_half == 3) tr = sinc_gather<3>(S, g, u2, r, i0, j0, k0, v, tr);
-  else tr = sinc_gather<-1>(S, g, u2, r, i0, j0, k0, v, tr);
-  *trp = tr;
+  const int h = S.ext_half, ls = 2 * h + 1;
+  const int ntap = g.twoD ? ls * ls : ls * ls * ls;
+  const float *wz = S.wz + (long long)r * ls, *wx = S.wx + (long long)r * ls;
+  float tr = lane == 0 ? *trp : 0.f;
+  for (int c0 = 0; c0 < ntap; c0 += 32) {
+    const int tp = c0 + lane;
+    float prod = 0.f;
+    if (tp < ntap) {
+      const int ii = tp % ls, rest = tp / ls;
+      const int jj = rest % ls, kq = rest / ls;
+      const long long p = g.idx(i0 - h + ii, j0 - h + jj, g.twoD ? 1 : k0 - h + kq);
+      prod = ((v * u2[p]) * wz[ii]) * wx[jj];
+      if (!g.twoD) prod = prod * wx[kq];     // the y weights are the x column
+    }
+    const int nlane = min(32, ntap - c0);
+    for (int l = 0; l < nlane; ++l) {
+      const float pl = __shfl_sync(0xffffffffu, prod, l);
+      tr = tr + pl;
+    }
+  }
+  if (lane == 0) *trp = tr;
 }
 
 // ---------------------------------------------------------------------------
 // Higdon recurrences (Boundary_3d, Boundary.f90:89-184; Higdon_factor,
-// Boundary.f90:366-447).  One thread per line normal to the edge.
+// Boundary.f90:366-447) for the kernels that do not apply them in the tile.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float hsum(const float *__restrict__ gc, long long cs, float a, float b,
-                                      float cc, float d, float e, float f, float gg, float h) {
-  float r = gc[0] * a;
-  r = r + gc[cs] * b;
-  r = r + gc[2 * cs] * cc;
-  r = r + gc[3 * cs] * d;
-  r = r + gc[4 * cs] * e;
-  r = r + gc[5 * cs] * f;
-  r = r + gc[6 * cs] * gg;
-  r = r + gc[7 * cs] * h;
-  return -r;
-}
 
-__global__ void k_bhiggz(BatchTables t, int s_off) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= t.hz_start[t.nshots]) return;
-  const int b = find_shot(t.hz_start, t.nshots, q);
-  const ShotDev &S = t.shots[b];
-  const int s = *t.counter + s_off;
-  if (s >= S.nsteps) return;
-  const Geom &g = S.g;
-  const int n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
-  const long long l = q - t.hz_start[b];
-  const long long cs = (long long)n2 * n3;
-  const int j = g.nmin2 + (int)(l % n2), k = g.nmin3 + (int)(l / n2);
-  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
-  float *u3 = S.f[(s + 4) % 5];
-  const float *gc = S.gz + l;
-  const long long p0 = g.idx(0, j, k);
-  for (int i = g.nmin1 + 3; i >= g.nmin1 - 4; --i) {
-    const long long p = p0 + i;
-    u3[p] = hsum(gc, cs, u3[p + 1], u3[p + 2], u2[p], u2[p + 1], u2[p + 2], u1[p], u1[p + 1],
-                 u1[p + 2]);
-  }
-  gc += 8 * cs;
-  for (int i = g.nmax1 - 3; i <= g.nmax1 + 4; ++i) {
-    const long long p = p0 + i;
-    u3[p] = hsum(gc, cs, u3[p - 1], u3[p - 2], u2[p], u2[p - 1], u2[p - 2], u1[p], u1[p - 1],
-                 u1[p - 2]);
-  }
-}
-
-__global__ void k_bhiggx(BatchTables t, int s_off) {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= t.hx_start[t.nshots]) return;
-  const int b = find_shot(t.hx_start, t.nshots, q);
-  const ShotDev &S = t.shots[b];
-  const int s = *t.counter + s_off;
-  if (s >= S.nsteps) return;
-  const Geom &g = S.g;
-  const int n1 = g.nmax1 - g.nmin1 + 1, n3 = g.nmax3 - g.nmin3 + 1;
-  const long long l = q - t.hx_start[b];
-  const long long cs = (long long)n1 * n3;
-  const int i = g.nmin1 + (int)(l % n1), k = g.nmin3 + (int)(l / n1);
-  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
-  float *u3 = S.f[(s + 4) % 5];
-  const long long L = g.ld1;
-  const float *gc = S.gx + l;
-  for (int j = g.nmin2 + 3; j >= g.nmin2 - 4; --j) {
-    const long long p = g.idx(i, j, k);
-    u3[p] = hsum(gc, cs, u3[p + L], u3[p + 2 * L], u2[p], u2[p + L], u2[p + 2 * L], u1[p],
-                 u1[p + L], u1[p + 2 * L]);
-  }
-  gc += 8 * cs;
-  for (int j = g.nmax2 - 3; j <= g.nmax2 + 4; ++j) {
-    const long long p = g.idx(i, j, k);
-    u3[p] = hsum(gc, cs, u3[p - L], u3[p - 2 * L], u2[p], u2[p - L], u2[p - 2 * L], u1[p],
-                 u1[p - L], u1[p - 2 * L]);
-  }
-}
-
-// Fused 2D edges: the z (top, bottom) and x (left, right) Higdon
-// recurrences of one step in one launch.  Each half line loads its 10 u2 and
-// u1 values, two u3 values and 8 coefficients first and then runs the 8-cell
-// recurrence in registers.  The reference applies all z lines and then all x
-// lines; only the x half lines of the 4 rows next to a z edge read or
-// overwrite cells the z half lines write (columns within 6 of an x edge),
-// so each corner is one warp that runs those 6 z half lines, synchronises
-// and then runs the 4 x half lines.  Every other half line is independent.
+// One half line of the Higdon recurrence with all inputs loaded first:
+// the 10 u2 and u1 values from 2 cells inside the innermost output to the
+// outermost one, the two u3 values inside it and the 8 coefficients; then
+// the 8 outputs in order in registers:
+//   u3(i) = -(g1 u3(i+d) + g2 u3(i+2d) + g3 u2(i) + g4 u2(i+d) + g5 u2(i+2d)
+//            + g6 u1(i) + g7 u1(i+d) + g8 u1(i+2d))
+// summed left to right, d the step towards the interior.
 __device__ __forceinline__ void higdon_half(const float *__restrict__ gc, long long cs,
                                             const float *__restrict__ u1,
                                             const float *__restrict__ u2, float *u3,
@@ -382,6 +304,14 @@ __device__ __forceinline__ void higdon_half(const float *__restrict__ gc, long l
   for (int k = 0; k < 8; ++k) u3[pstart - (long long)k * dst] = out[k];
 }
 
+// Fused 2D edges: the z (top, bottom) and x (left, right) Higdon
+// recurrences of one step in one launch.  Each half line loads its 10 u2 and
+// u1 values, two u3 values and 8 coefficients first and then runs the 8-cell
+// recurrence in registers.  The reference applies all z lines and then all x
+// lines; only the x half lines of the 4 rows next to a z edge read or
+// overwrite cells the z half lines write (columns within 6 of an x edge),
+// so each corner is one warp that runs those 6 z half lines, synchronises
+// and then runs the 4 x half lines.  Every other half line is independent.
 __global__ void __launch_bounds__(128) k_bedges2d(BatchTables t, int s_off) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= t.edge_start[t.nshots]) return;
@@ -429,33 +359,63 @@ __global__ void __launch_bounds__(128) k_bedges2d(BatchTables t, int s_off) {
   }
 }
 
+// One thread per half line (line = q / 2, half = q % 2: the near and the far
+// edge are independent); z lines (n2*n3 per shot), x lines (n1*n3), y lines
+// (n1*n2, 3D only), launched in that order like the reference's loops.
+__global__ void k_bhiggz(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((q >> 1) >= t.hz_start[t.nshots]) return;
+  const int b = find_shot(t.hz_start, t.nshots, q >> 1);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  const long long l = (q >> 1) - t.hz_start[b];
+  const long long cs = (long long)n2 * n3;
+  const int j = g.nmin2 + (int)(l % n2), k = g.nmin3 + (int)(l / n2);
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  if ((q & 1) == 0) higdon_half(S.gz + l, cs, u1, u2, u3, g.idx(g.nmin1 + 3, j, k), 1);
+  else higdon_half(S.gz + l + 8 * cs, cs, u1, u2, u3, g.idx(g.nmax1 - 3, j, k), -1);
+}
+
+__global__ void k_bhiggx(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((q >> 1) >= t.hx_start[t.nshots]) return;
+  const int b = find_shot(t.hx_start, t.nshots, q >> 1);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n1 = g.nmax1 - g.nmin1 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  const long long l = (q >> 1) - t.hx_start[b];
+  const long long cs = (long long)n1 * n3;
+  const int i = g.nmin1 + (int)(l % n1), k = g.nmin3 + (int)(l / n1);
+  const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
+  float *u3 = S.f[(s + 4) % 5];
+  const long long L = g.ld1;
+  if ((q & 1) == 0) higdon_half(S.gx + l, cs, u1, u2, u3, g.idx(i, g.nmin2 + 3, k), L);
+  else higdon_half(S.gx + l + 8 * cs, cs, u1, u2, u3, g.idx(i, g.nmax2 - 3, k), -L);
+}
+
 __global__ void k_bhiggy(BatchTables t, int s_off) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= t.hy_start[t.nshots]) return;
-  const int b = find_shot(t.hy_start, t.nshots, q);
+  if ((q >> 1) >= t.hy_start[t.nshots]) return;
+  const int b = find_shot(t.hy_start, t.nshots, q >> 1);
   const ShotDev &S = t.shots[b];
   const int s = *t.counter + s_off;
   if (s >= S.nsteps || S.g.nbound == 0) return;
   const Geom &g = S.g;
   const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1;
-  const long long l = q - t.hy_start[b];
+  const long long l = (q >> 1) - t.hy_start[b];
   const long long cs = (long long)n1 * n2;
   const int i = g.nmin1 + (int)(l % n1), j = g.nmin2 + (int)(l / n1);
   const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
   float *u3 = S.f[(s + 4) % 5];
   const long long P = g.plane();
-  const float *gc = S.gy + l;
-  for (int k = g.nmin3 + 3; k >= g.nmin3 - 4; --k) {
-    const long long p = g.idx(i, j, k);
-    u3[p] = hsum(gc, cs, u3[p + P], u3[p + 2 * P], u2[p], u2[p + P], u2[p + 2 * P], u1[p],
-                 u1[p + P], u1[p + 2 * P]);
-  }
-  gc += 8 * cs;
-  for (int k = g.nmax3 - 3; k <= g.nmax3 + 4; ++k) {
-    const long long p = g.idx(i, j, k);
-    u3[p] = hsum(gc, cs, u3[p - P], u3[p - 2 * P], u2[p], u2[p - P], u2[p - 2 * P], u1[p],
-                 u1[p - P], u1[p - 2 * P]);
-  }
+  if ((q & 1) == 0) higdon_half(S.gy + l, cs, u1, u2, u3, g.idx(i, j, g.nmin3 + 3), P);
+  else higdon_half(S.gy + l + 8 * cs, cs, u1, u2, u3, g.idx(i, j, g.nmax3 - 3), -P);
 }
 
 // Streaming 2D step (stream2d.cuh); the shot's stencil variant is uniform
@@ -591,7 +551,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   // Every kernel of the step reads s = *counter + s_off; the counter is
   // advanced once per chunk of steps.
   if (has_ext && n_rec > 0) {
-    k_bextract<<<(n_rec + 127) / 128, 128, 0, s>>>(t, s_off);
+    k_bextract<<<(n_rec + 3) / 4, 128, 0, s>>>(t, s_off);
     ++nl;
   }
   if (has_adj3d && n_v2u > 0 && !tile.stream3d) {
@@ -681,12 +641,12 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   } else {
-    k_bhiggz<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
-    k_bhiggx<<<(n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
+    k_bhiggz<<<(2 * n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
+    k_bhiggx<<<(2 * n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
     nl += 2;
   }
   if (has_3d && n_hy > 0) {
-    k_bhiggy<<<(n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
+    k_bhiggy<<<(2 * n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   }
   if (nlaunch) *nlaunch = nl;

@@ -65,7 +65,6 @@ __device__ __forceinline__ void stream3d_body(const BatchTables &t, int s_off, i
   const float *__restrict__ u2 = S.f[(s + 3) % 5];
   float *__restrict__ u3 = S.f[(s + 4) % 5];
   const float *__restrict__ vel = S.vel;
-  const int L = g.ld1;
   const int P = (int)g.plane();
   const Coefs c = S.c;
   const float k12 = S.k12, div11 = S.div11;
