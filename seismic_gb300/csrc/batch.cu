@@ -543,15 +543,37 @@ __global__ void k_counter_add(int *counter, int add) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *counter += add;
 }
 
+// Injection terms of the step, one thread per (shot, entry):
+// term = (((v2r * trace(it)) * wz) * wx) * wy (Injection.f90:151-456,
+// 561-591); the step kernel adds a cell's terms in entry order.
+__global__ void k_bterms(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.term_start[t.nshots]) return;
+  const int b = find_shot(t.term_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const int k = q - t.term_start[b];
+  const int it = S.tmin + s * S.tstep;
+  const InjEntry E = S.inj_ent[k];
+  const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
+  S.inj_term[k] = (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
+}
+
 cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
                               int n_hz, int n_hx, int n_hy, int n_v2u, int has_ext, int has_3d,
                               int has_adj3d, const StepTile &tile, cudaStream_t s,
-                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after) {
+                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after,
+                              int n_term) {
   int nl = 0;
   // Every kernel of the step reads s = *counter + s_off; the counter is
   // advanced once per chunk of steps.
   if (has_ext && n_rec > 0) {
     k_bextract<<<(n_rec + 3) / 4, 128, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (n_term > 0) {
+    k_bterms<<<(n_term + 255) / 256, 256, 0, s>>>(t, s_off);
     ++nl;
   }
   if (has_adj3d && n_v2u > 0 && !tile.stream3d) {

@@ -28,6 +28,7 @@ struct ShotDev {
   int bi0, bi1, bj0, bj1, bk0, bk1;
   const int *inj_off;
   const InjEntry *inj_ent;
+  float *inj_term;        // per entry: its contribution at the current step
   const float *src_tr;    // nsrc*nt
   // extraction
   int ext_mode, nrec, ext_half;
@@ -58,6 +59,7 @@ struct T2Shot {
   int ld1, lo2, n2p, nmin1, nmax1, nmin2, nmax2, nz, nx;
   int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
   int tcnt;
+  int inj_direct;         // 1: form injection terms in the tile (few entries)
   int off1, off2;         // tile origin: nmin1 - off1, nmin2 - off2
   int ntz, ntx;           // tiles along z and x
 };
@@ -118,6 +120,7 @@ struct BatchTables {
   const T2Shot *t2shots;  // nshots compact views (pipelined 2D kernel)
   const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
   const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
+  const int *term_start;  // nshots+1: injection entries (per-step term kernel)
   const T2Maps *t2maps;   // nshots tensor-map sets (pipelined 2D kernel)
   const T3Maps *t3maps;   // nshots tensor-map sets (pipelined 3D kernel)
   int *err;               // device error flags (bit 0: a bounded wait gave up)
@@ -173,7 +176,8 @@ inline int step_ctas(const Geom &g, const StepTile &tile) {
 cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
                               int n_hz, int n_hx, int n_hy, int n_v2u, int has_ext, int has_3d,
                               int has_adj3d, const StepTile &tile, cudaStream_t s,
-                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after);
+                              int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after,
+                              int n_term = 0);
 cudaError_t launch_counter_add(int *counter, int add, cudaStream_t s);
 
 }  // namespace swave

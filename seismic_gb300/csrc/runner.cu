@@ -58,6 +58,9 @@ T *carve(char *&cur, size_t n) {
 
 size_t rup(size_t b) { return (b + 255) / 256 * 256; }
 
+// Injection entries from which a shot's terms are formed by k_bterms.
+constexpr size_t kTermKernelMin = 2048;
+
 // 3D FP32 tensor map over a padded field (ld1 x n2p x n3p) with a box of
 // bz rows x bx columns x 1 plane.
 bool encode_field_map3(CUtensorMap *m, const float *base, const Geom &g, int bz, int bx) {
@@ -141,11 +144,12 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     bytes += 5 * rup(fb);
     if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT && !tile.stream3d) bytes += rup(fb);
     bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
-    bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry));
+    bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry)) +
+             rup(inj[b].ent.size() * sizeof(float));
     bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
     bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
   }
-  bytes += rup(nb * sizeof(ShotDev)) + 7 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
+  bytes += rup(nb * sizeof(ShotDev)) + 8 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
   if (t2) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
@@ -163,7 +167,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // ---- carve and fill ----
   std::vector<ShotDev> hs(nb);
   std::vector<int> step_tiles(nb + 1, 0), rec_start(nb + 1, 0), hz(nb + 1, 0), hx(nb + 1, 0),
-      hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0);
+      hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0), term(nb + 1, 0);
   // The fused 2D edge kernel needs n1, n2 >= 16 in every shot.
   bool fused_edges = !has_3d;
   for (int b = 0; b < nb && fused_edges; ++b) fused_edges = edge_threads_2d(G[b]) > 0;
@@ -215,6 +219,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                       cudaMemcpyHostToDevice, s));
       S.inj_off = off;
       S.inj_ent = ent;
+      S.inj_term = carve<float>(cur, inj[b].ent.size());
       S.src_tr = io.sou_trace_dev;
     }
     S.ext_mode = ext[b].on ? ext[b].mode : 0;
@@ -272,14 +277,19 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     hx[b + 1] = hx[b] + (int)(n1 * n3);
     hy[b + 1] = hy[b] + (g.twoD ? 0 : (int)(n1 * n2));
     edge[b + 1] = edge[b] + (fused_edges ? edge_threads_2d(G[b]) : 0);
+    // The pipelined 2D kernel adds injection terms computed per step by
+    // k_bterms when a shot has many entries (receiver-side injection);
+    // a few source entries are formed in the tile.
+    term[b + 1] = term[b] + (t2 && inj[b].on && inj[b].ent.size() >= kTermKernelMin
+                                 ? (int)inj[b].ent.size() : 0);
     v2b[b + 1] = v2b[b] + ((S.adj3d && !tile.stream3d)
                                ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256)
                                : 0);
   }
   ShotDev *dshots = carve<ShotDev>(cur, nb);
-  int *dtab[7];
-  std::vector<int> *htab[7] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b, &edge};
-  for (int q = 0; q < 7; ++q) {
+  int *dtab[8];
+  std::vector<int> *htab[8] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b, &edge, &term};
+  for (int q = 0; q < 8; ++q) {
     dtab[q] = carve<int>(cur, nb + 1);
     SW_CK(cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s));
   }
@@ -309,6 +319,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.nsteps = S.nsteps; h.tmin = S.tmin; h.tstep = S.tstep; h.snapi = S.snapi;
       h.tcnt = S.tcnt;
       h.adj2d = S.adj2d; h.inj_on = S.inj_on;
+      h.inj_direct = S.inj_on && inj[b].ent.size() < kTermKernelMin;
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
       h.gz = S.gz; h.gx = S.gx;
@@ -381,6 +392,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.hy_start = dtab[4];
   t.v2u_blocks = dtab[5];
   t.edge_start = dtab[6];
+  t.term_start = dtab[7];
   t.t2shots = d2;
   t.tile_tab = dtile;
   t.t2maps = dmaps;
@@ -390,6 +402,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // The host plans above must stay alive until the uploads complete.
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch setup");
 
+  const int n_term = term[nb];
   const int n_tiles = step_tiles[nb], n_rec = rec_start[nb], n_hz = hz[nb], n_hx = hx[nb],
             n_hy = hy[nb], n_v2u = v2b[nb];
   {
@@ -458,7 +471,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       // In profiling mode events bracket the fused step kernel only.
       if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
                                  has_adj3d, tile, s, &nl, with_events ? c->ev[2 * q] : nullptr,
-                                 with_events ? c->ev[2 * q + 1] : nullptr)) != cudaSuccess)
+                                 with_events ? c->ev[2 * q + 1] : nullptr, n_term)) != cudaSuccess)
         return -1;
       launched += nl;
     }

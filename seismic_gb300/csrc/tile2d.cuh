@@ -26,7 +26,7 @@ constexpr int T2_SZ = T2_Z + 8;          // staged column length (with halo)
 constexpr int T2_SX = T2_X + 8;          // staged columns (with halo)
 constexpr int T2_HALO = T2_SX * T2_SZ;   // 2880 floats
 constexpr int T2_CORE = T2_X * T2_Z;     // 2048 floats
-constexpr int T2_MAX_TILES_PER_CTA = 384;
+constexpr int T2_MAX_TILES_PER_CTA = 320;
 
 // Floats of one pipeline stage.
 template <bool ADJ>
@@ -142,19 +142,6 @@ __device__ __forceinline__ void t2_issue(const T2Maps &M, const T2Shot &h, int s
 
 __device__ __forceinline__ float f4get(const float4 &a, int e) {
   return e == 0 ? a.x : e == 1 ? a.y : e == 2 ? a.z : a.w;
-}
-
-// Injection into one element of the injection box (CSR list in source
-// order; Injection.f90:151-456,561-591).
-__device__ __noinline__ float t2_inject(const ShotDev &S, int it, int i, int j, float se) {
-  const int bx = (i - S.bi0) + (S.bi1 - S.bi0 + 1) * (j - S.bj0);
-  const int e1 = S.inj_off[bx + 1];
-  for (int q = S.inj_off[bx]; q < e1; ++q) {
-    const InjEntry E = S.inj_ent[q];
-    const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
-    se = se + (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
-  }
-  return se;
 }
 
 // Born source and AFWI imaging of one element on a snapshot step (the
@@ -398,25 +385,71 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   if (slow_extras) {
     const ShotDev &S = t.shots[b];
     const bool rows_inj = inj_tile && i0 + 3 >= h.bi0 && i0 <= h.bi1;
+    if (rows_inj) {
+      // Injection (Injection.f90:151-456,561-591): every cell adds the
+      // step's terms of its entries (k_bterms) in entry order.  The offsets
+      // and the first 4 terms of all 8 cells are loaded before any sum.
+      int beg[2][4], end[2][4];
 #pragma unroll
-    for (int hh = 0; hh < 2; ++hh) {
-      const int jl = 2 * tx + hh, j = x0 + jl;
-      if (j > h.nmax2 || j < h.nmin2) continue;
-      const bool col_inj = rows_inj && j >= h.bj0 && j <= h.bj1;
-      if (!col_inj && !snap_slow) continue;
-      float r[4] = {sv[hh][0].x, sv[hh][0].y, sv[hh][1].x, sv[hh][1].y};
-      const float *cc = core + jl * T2_Z + 4 * tz;
+      for (int hh = 0; hh < 2; ++hh) {
+        const int j = x0 + 2 * tx + hh;
+        const bool cin = j >= h.bj0 && j <= h.bj1 && j >= h.nmin2 && j <= h.nmax2;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = i0 + q;
-        if (col_inj && i >= h.bi0 && i <= h.bi1) r[q] = t2_inject(S, it, i, j, r[q]);
-        if (snap_slow) {
-          const float vc = ADJ ? svel[(jl + 4) * T2_SZ + 4 * tz + 4 + q] : cc[3 * T2_CORE + q];
-          r[q] = t2_snap_generic(S, it, i, j, r[q], f4get(u2c[hh], q), vc);
+        for (int q = 0; q < 4; ++q) {
+          const int i = i0 + q;
+          beg[hh][q] = end[hh][q] = 0;
+          if (cin && i >= h.bi0 && i <= h.bi1) {
+            const int bx = (i - h.bi0) + (h.bi1 - h.bi0 + 1) * (j - h.bj0);
+            beg[hh][q] = S.inj_off[bx];
+            end[hh][q] = S.inj_off[bx + 1];
+          }
         }
       }
-      sv[hh][0] = p2(r[0], r[1]);
-      sv[hh][1] = p2(r[2], r[3]);
+      // Term of entry k: precomputed, or formed here for a shot with few
+      // entries (its source), the same operations as k_bterms.
+      auto term = [&](int k) {
+        if (!h.inj_direct) return S.inj_term[k];
+        const InjEntry E = S.inj_ent[k];
+        const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
+        return (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
+      };
+      float tv[2][4][4];
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            tv[hh][q][m] = beg[hh][q] + m < end[hh][q] ? term(beg[hh][q] + m) : 0.f;
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        float r[4] = {sv[hh][0].x, sv[hh][0].y, sv[hh][1].x, sv[hh][1].y};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+#pragma unroll
+          for (int m = 0; m < 4; ++m)
+            if (beg[hh][q] + m < end[hh][q]) r[q] = r[q] + tv[hh][q][m];
+          for (int k = beg[hh][q] + 4; k < end[hh][q]; ++k) r[q] = r[q] + term(k);
+        }
+        sv[hh][0] = p2(r[0], r[1]);
+        sv[hh][1] = p2(r[2], r[3]);
+      }
+    }
+    if (snap_slow) {
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int jl = 2 * tx + hh, j = x0 + jl;
+        if (j > h.nmax2 || j < h.nmin2) continue;
+        float r[4] = {sv[hh][0].x, sv[hh][0].y, sv[hh][1].x, sv[hh][1].y};
+        const float *cc = core + jl * T2_Z + 4 * tz;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float vc = ADJ ? svel[(jl + 4) * T2_SZ + 4 * tz + 4 + q] : cc[3 * T2_CORE + q];
+          r[q] = t2_snap_generic(S, it, i0 + q, j, r[q], f4get(u2c[hh], q), vc);
+        }
+        sv[hh][0] = p2(r[0], r[1]);
+        sv[hh][1] = p2(r[2], r[3]);
+      }
     }
   }
   // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
