@@ -346,6 +346,12 @@ typedef struct sw_stats {
 } sw_stats;
 int sw_ctx_get_stats(const sw_ctx *ctx, sw_stats *out);
 int sw_ctx_reset_stats(sw_ctx *ctx);
+/* Boundary of every propagation on this context: 0 = the reference's
+ * Higdon absorbing boundary (default), 1 = rigid (no Higdon recurrence,
+ * zero halo; no counterpart in the reference).  With 1 the Born
+ * (sw_born) and LSRTM (sw_lsrtm) operators are an exact adjoint pair: the
+ * Higdon boundary is what makes the reference's pair approximate. */
+int sw_ctx_set_boundary(sw_ctx *ctx, int mode);
 /* on=1: bracket fused-kernel launches with CUDA events: every launch when
    the time loop runs without a CUDA graph, otherwise the launches of every
    8th graph chunk (the event records cost a few microseconds each). */

@@ -188,6 +188,8 @@ def fwi_fct_gdt(desc, vel, wavelet, shots, vpmask=None):
         arr[i].rec_coord, arr[i].dobs = prc, pdo
         if s.get("mute") is not None:
             mu, pmu = _f(s["mute"]); keep.append(mu); arr[i].mute = pmu
+        if s.get("resid") is not None:   # float32 (nrec, nt) array filled in place
+            arr[i].resid = s["resid"].ctypes.data_as(_fp)
     g = desc.g
     n = g.nz * g.nx * g.ny
     grad, illum = np.zeros(n, np.float32), np.zeros(n, np.float32)
@@ -211,6 +213,14 @@ def rtm_job(model, vel, wavelet, shots, aperture_x=0.0, aperture_y=0.0):
                             C.cast(arr, C.c_void_p), im.ctypes.data_as(_fp),
                             il.ctypes.data_as(_fp), nm.ctypes.data_as(_fp)), "rtm_job")
     return im, il, nm
+
+
+def set_rigid(on: bool) -> None:
+    """Skip the Higdon boundary in every propagation (exact-adjoint mode)."""
+    lib = load()
+    lib.oracle_set_rigid.argtypes = [C.c_int]
+    lib.oracle_set_rigid.restype = None
+    lib.oracle_set_rigid(int(bool(on)))
 
 
 def stencil_f64(g, vel, u2, adjoint=False):

@@ -106,6 +106,8 @@ int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2,
                      int rect3, int doz, int dox, int doy);
 
 /* One stencil application on a padded FP64 field (analytic tests). */
+/* 1: skip the Higdon boundary in every propagation (rigid halo). */
+void oracle_set_rigid(int on);
 int oracle_stencil_f64(const sw_genpar *g, int adjoint, const double *vel,
                        const double *u2, double *u3);
 

@@ -538,6 +538,11 @@ static void compute_taper(int nxw, int nyw, std::vector<T> &tx, std::vector<T> &
 }
 
 // ---------------------------------------------------------------------------
+// Rigid-boundary switch (no counterpart in the reference): the Higdon
+// recurrence is skipped, so the halo stays zero.  With it the Born / LSRTM
+// pair is an exact adjoint pair (the Higdon boundary is not self-adjoint).
+static int g_rigid = 0;
+
 // propagator_acoustic (libs/libwave/Propagator.f90:27-270)
 // ---------------------------------------------------------------------------
 template <class T> struct IO {
@@ -770,7 +775,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
     }
     // TimeDer (Propagator.f90:218), Higdon (Propagator.f90:222-228).
     time_update(b, (T)g.dt, *u2, *u1, *u0, *um1, *u3);
-    boundary(hig, b, *u1, *u2, *u3);
+    if (!g_rigid) boundary(hig, b, *u1, *u2, *u3);
     // FDswaptime_pointer (FDswaptimes.f90:14-24).
     F3<T> *t = um1;
     um1 = u0; u0 = u1; u1 = u2; u2 = u3; u3 = t;
@@ -1537,6 +1542,8 @@ L172:
 // C entry points
 // ---------------------------------------------------------------------------
 extern "C" {
+
+void oracle_set_rigid(int on) { g_rigid = on != 0; }
 
 int oracle_propagate_f32(const sw_prop_desc *d, const sw_prop_io *io) {
   IO<float> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,

@@ -128,6 +128,7 @@ _SIGS = {
     "sw_ctx_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(SwTuning)]),
     "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
+    "sw_ctx_set_boundary": (C.c_int, [C.c_void_p, C.c_int]),
     "sw_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
 }
 
@@ -241,6 +242,10 @@ class Context:
         cur.update(kw)
         t = SwTuning(**cur)
         self._check(self.lib.sw_ctx_set_tuning(self.h, C.byref(t)))
+
+    def set_boundary(self, mode: int):
+        """0: Higdon absorbing boundary (reference); 1: rigid (exact-adjoint mode)."""
+        self._check(self.lib.sw_ctx_set_boundary(self.h, int(mode)))
 
     def set_profiling(self, on: bool):
         self._check(self.lib.sw_ctx_set_profiling(self.h, int(bool(on))))

@@ -657,7 +657,9 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     cudaError_t ec = record(ev_after);
     if (ec != cudaSuccess) return ec;
   }
-  if (!has_3d && (tile.stream2d == 2 || tile.stream2d == 3)) {
+  if (tile.rigid) {
+    // Exact-adjoint mode: no absorbing boundary, the halo stays zero.
+  } else if (!has_3d && (tile.stream2d == 2 || tile.stream2d == 3)) {
     // The pipelined 2D kernel applies the Higdon edges itself.
   } else if (!has_3d && tile.fused_edges) {
     k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);
@@ -667,7 +669,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     k_bhiggx<<<(2 * n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
     nl += 2;
   }
-  if (has_3d && n_hy > 0) {
+  if (has_3d && n_hy > 0 && !tile.rigid) {
     k_bhiggy<<<(2 * n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   }

@@ -60,6 +60,7 @@ struct T2Shot {
   int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
   int tcnt;
   int inj_direct;         // 1: form injection terms in the tile (few entries)
+  int rigid;              // 1: no Higdon edges (exact-adjoint mode)
   int off1, off2;         // tile origin: nmin1 - off1, nmin2 - off2
   int ntz, ntx;           // tiles along z and x
 };
@@ -146,6 +147,7 @@ struct StepTile {
   int nsm = 152;       // SMs of the device (persistent grids)
   int fused_edges = 0; // 2D: one launch for the z and x Higdon edges (set by the runner)
   int n_edge = 0;      // threads of that launch
+  int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
 };
 
 // Threads of the fused 2D edge kernel for one shot: four corner warps and

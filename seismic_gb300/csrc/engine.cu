@@ -94,6 +94,12 @@ int sw_ctx_get_tuning(const sw_ctx *c, sw_tuning *t) {
   return SW_OK;
 }
 
+int sw_ctx_set_boundary(sw_ctx *c, int mode) {
+  if (!c || mode < 0 || mode > 1) return SW_BAD_PARAM;
+  c->run_opts.rigid = mode == 1;
+  return SW_OK;
+}
+
 int sw_ctx_set_profiling(sw_ctx *c, int on) {
   if (!c) return SW_BAD_PARAM;
   c->profiling = on != 0;

@@ -18,6 +18,7 @@ struct DBuf {
 struct RunOpts {
   int chunk = 16;       // steps per captured graph
   bool use_graph = true;
+  bool rigid = false;   // skip the Higdon boundary (exact-adjoint mode)
   swave::StepTile tile; // fused-step tile shape
 };
 

@@ -320,6 +320,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.tcnt = S.tcnt;
       h.adj2d = S.adj2d; h.inj_on = S.inj_on;
       h.inj_direct = S.inj_on && inj[b].ent.size() < kTermKernelMin;
+      h.rigid = opt.rigid ? 1 : 0;
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
       h.gz = S.gz; h.gx = S.gx;
@@ -413,6 +414,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   }
   tile.has_fwd2d = tile.has_adj2d = tile.has_fwd3d = tile.has_adj3d = 0;
   tile.fused_edges = fused_edges ? 1 : 0;
+  tile.rigid = opt.rigid ? 1 : 0;
   tile.n_edge = edge[nb];
   for (auto &S : hs) {
     if (S.g.twoD) {

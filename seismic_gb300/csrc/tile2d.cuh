@@ -522,6 +522,7 @@ __device__ __forceinline__ void t2_higdon8(const float c[8], const float U2[10],
 template <bool ADJ>
 __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const float *st, int tid,
                                          int bar) {
+  if (h.rigid) return;   // exact-adjoint mode: no absorbing boundary
   const int tzi = t2_tzi(e), txi = t2_txi(e);
   const bool top = tzi == 0, bottom = tzi == h.ntz - 1;
   const bool left = txi == 0, right = txi == h.ntx - 1;

@@ -155,3 +155,36 @@ def test_linearity_scaling(ctx):
     a = ctx.modeling(g, vel, sou, w, rec)
     b = ctx.modeling(g, vel, sou, 2 * w, rec)
     assert rel_l2(b, 2 * a) < 1e-6
+
+
+@pytest.mark.parametrize("three_d", [False, True])
+def test_born_lsrtm_dot_test_rigid(oracle, three_d):
+    """Exact-adjoint mode (sw_ctx_set_boundary(ctx, 1)): the GPU Born and
+    LSRTM operators pass the dot-product test to 1e-5 in FP32 and match the
+    oracle's rigid-boundary runs bit for bit."""
+    from tests.cases import case2d, case3d
+    if three_d:
+        g, vel, sou, rec, w = case3d(nt=100, snapi=2)
+    else:
+        g, vel, sou, rec, w = case2d(nz=50, nx=70, nt=400, seed=2, snapi=4)
+    rng = np.random.default_rng(35)
+    m = rng.standard_normal(vel.shape).astype(np.float32)
+    d = rng.standard_normal((rec.shape[0], g.nt)).astype(np.float32)
+    c = sw.Context(0)
+    try:
+        c.set_boundary(1)
+        lm = c.born(g, vel, m, sou, w, rec)
+        ltd, _ = c.lsrtm(g, vel, sou, w, rec, d)
+    finally:
+        c.close()
+    a = float(np.sum(lm.astype(np.float64) * d))
+    b = float(np.sum(m.ravel().astype(np.float64) * ltd.ravel()))
+    assert abs(a - b) <= 1e-5 * max(abs(a), abs(b))
+    oracle.set_rigid(True)
+    try:
+        rlm = oracle.born(g, vel, m, sou, w, rec)
+        rltd, _ = oracle.lsrtm(g, vel, sou, w, rec, d)
+    finally:
+        oracle.set_rigid(False)
+    np.testing.assert_array_equal(lm, rlm)
+    np.testing.assert_array_equal(ltd, rltd)

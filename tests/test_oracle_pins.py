@@ -147,3 +147,27 @@ def test_born_lsrtm_pair_is_approximate(oracle):
     b = float(np.sum(m.ravel() * ltd.ravel()))
     rel = abs(a - b) / max(abs(a), abs(b))
     assert 0.01 < rel < 0.06
+
+
+@pytest.mark.parametrize("three_d", [False, True])
+def test_born_lsrtm_exact_pair_with_rigid_boundary(oracle, three_d):
+    """Without the Higdon recurrence (rigid, zero halo) the reference's Born
+    and LSRTM operators are an exact adjoint pair: the FP64 dot test closes
+    to rounding."""
+    from tests.cases import case2d, case3d
+    if three_d:
+        g, vel, sou, rec, w = case3d(nt=100, snapi=2)
+    else:
+        g, vel, sou, rec, w = case2d(nz=50, nx=70, nt=400, seed=2, snapi=4)
+    rng = np.random.default_rng(34)
+    m = rng.standard_normal(vel.shape)
+    d = rng.standard_normal((rec.shape[0], g.nt))
+    oracle.set_rigid(True)
+    try:
+        lm = oracle.born(g, vel, m, sou, w, rec, f64=True)
+        ltd, _ = oracle.lsrtm(g, vel, sou, w, rec, d, f64=True)
+    finally:
+        oracle.set_rigid(False)
+    a = float(np.sum(lm * d))
+    b = float(np.sum(m.ravel() * ltd.ravel()))
+    assert abs(a - b) <= 1e-12 * max(abs(a), abs(b))
