@@ -46,6 +46,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "oracle_modeling_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp],
         "oracle_modeling_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp],
         "oracle_rtm_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp],
+        "oracle_rtm_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp],
         "oracle_born_f32": [g, _fp, _fp, _fp, _fp, C.c_int, _fp, _fp],
         "oracle_born_f64": [g, _dp, _dp, _dp, _dp, C.c_int, _dp, _dp],
         "oracle_lsrtm_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp],
@@ -110,10 +111,16 @@ def modeling(g, vel, sou, wavelet, rec, final_u2=False, f64=False):
     return (data, fu) if final_u2 else data
 
 
-def rtm(g, vel, sou, wavelet, rec, data):
+def rtm(g, vel, sou, wavelet, rec, data, f64=False):
     lib = load()
-    v, pv = _f(vel); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec); d, pd = _f(data)
     n = g.nz * g.nx * g.ny
+    if f64:
+        v, pv = _d(vel); s, ps = _d(sou); w, pw = _d(wavelet); r, pr = _d(rec); d, pd = _d(data)
+        im, il = np.zeros(n), np.zeros(n)
+        _chk(lib.oracle_rtm_f64(C.byref(g), pv, ps, pw, r.size // 3, pr, pd,
+                                im.ctypes.data_as(_dp), il.ctypes.data_as(_dp)), "rtm")
+        return im, il
+    v, pv = _f(vel); s, ps = _f(sou); w, pw = _f(wavelet); r, pr = _f(rec); d, pd = _f(data)
     im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
     _chk(lib.oracle_rtm_f32(C.byref(g), pv, ps, pw, r.size // 3, pr, pd, im.ctypes.data_as(_fp),
                             il.ctypes.data_as(_fp)), "rtm")

@@ -62,6 +62,9 @@ int oracle_rtm_f32(const sw_genpar *g, const float *vel,
                    const float *sou_coord, const float *wavelet, int nrec,
                    const float *rec_coord, const float *data, float *image,
                    float *illum);
+int oracle_rtm_f64(const sw_genpar *g, const double *vel, const double *sou_coord,
+                   const double *wavelet, int nrec, const double *rec_coord,
+                   const double *data, double *image, double *illum);
 int oracle_born_f32(const sw_genpar *g, const float *vel, const float *ref,
                     const float *sou_coord, const float *wavelet, int nrec,
                     const float *rec_coord, float *data);

@@ -1573,6 +1573,12 @@ int oracle_rtm_f32(const sw_genpar *g, const float *vel, const float *sou_coord,
   return rtm_like<float>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, image,
                          illum, false);
 }
+int oracle_rtm_f64(const sw_genpar *g, const double *vel, const double *sou_coord,
+                   const double *wavelet, int nrec, const double *rec_coord,
+                   const double *data, double *image, double *illum) {
+  return rtm_like<double>(*g, vel, sou_coord, wavelet, nrec, rec_coord, data, image,
+                          illum, false);
+}
 int oracle_born_f32(const sw_genpar *g, const float *vel, const float *ref,
                     const float *sou_coord, const float *wavelet, int nrec,
                     const float *rec_coord, float *data) {
