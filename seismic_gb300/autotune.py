@@ -1,9 +1,13 @@
-"""Autotuner for the fused step kernel's launch shape and the graph chunk.
+"""Autotuner for the fused step kernel's launch shape, the graph chunk and
+the number of shots per launch.
 
 Candidates are timed on a truncated copy of the real batch (same windows,
 same number of shots in flight, a few dozen time steps of both the forward
 and the backward phase); the fastest is cached per (device, padded-grid
 bucket, shots per batch) in a JSON file under the user's cache directory.
+With `batch="auto"` the shots per launch are chosen first (each candidate
+batch size runs the same sample of shots, in as many launches as it needs,
+with the current launch shape), then the launch shape at that batch size.
 Timing is injected so that the selection logic can be exercised without a
 GPU.
 """
@@ -80,14 +84,101 @@ def select(cands: Iterable[dict], time_fn: Callable[[dict], float], repeats: int
     return best[0], results
 
 
-def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | None = None,
-             cache_path: str | None = DEFAULT_CACHE, device_name: str | None = None,
-             force: bool = False) -> dict:
-    """Tunes ctx for the RTM job of `shots` and applies the winner."""
+BATCH_CANDIDATES = (1, 2, 4, 8, 16, 32, 64)
+
+
+def batch_candidates(nshots: int, cands: Iterable[int] = BATCH_CANDIDATES) -> list[int]:
+    """Batch sizes worth timing for a survey of `nshots` shots: those below
+    the shot count, plus the shot count itself when it is below the largest
+    candidate (a batch larger than the survey runs the same launch)."""
+    out = sorted({b for b in cands if b < nshots} | ({nshots} if nshots <= max(cands) else set()))
+    return out or [1]
+
+
+def select_batch(batches: Iterable[int], time_fn: Callable[[int], float],
+                 repeats: int = 2) -> tuple[int, list]:
+    """The batch size whose run of the same shot sample is fastest (ties go
+    to the smaller batch, which holds less memory)."""
+    best, res = select([{"batch": b} for b in sorted(batches)], lambda c: time_fn(c["batch"]),
+                       repeats)
+    return best["batch"], res
+
+
+def _sample(shots, count, steps):
+    import numpy as np
+    return [{"sou": shots[i % len(shots)]["sou"], "rec": shots[i % len(shots)]["rec"],
+             "data": np.ascontiguousarray(np.asarray(shots[i % len(shots)]["data"])[:, :steps])}
+            for i in range(count)]
+
+
+def _device_name(ctx, device_name):
+    if device_name is not None:
+        return device_name
+    try:
+        import torch
+        return torch.cuda.get_device_name(ctx_device(ctx))
+    except Exception:
+        return "cuda"
+
+
+def tune_batch(ctx, model, vel, wavelet, shots, steps: int = 48,
+               cands: Iterable[int] = BATCH_CANDIDATES, cache_path: str | None = DEFAULT_CACHE,
+               device_name: str | None = None, force: bool = False) -> dict:
+    """Chooses the shots per launch for the RTM job of `shots` with ctx's
+    current launch shape.  Every candidate runs the same sample (the largest
+    candidate's worth of shots, cycling through `shots`), so the times
+    compare whole-sample throughput."""
     import numpy as np
 
     import seismic_gb300 as sw
-    batch = batch or len(shots)
+    batches = batch_candidates(len(shots), cands)
+    sample = _sample(shots, max(batches), steps)
+    g = sw.SwGenpar.from_buffer_copy(model)
+    g.nt = steps
+    n1p = g.nz + 2 * g.ntaper + 8
+    widths = [int(np.ptp(np.asarray(s["rec"])[:, 1]) / g.dx) + 1 for s in sample]
+    n2p = max(widths) + 2 * g.ntaper + 8
+    n3p = 1 if g.twoD else g.ny + 2 * g.ntaper + 8
+    key = cache_key(_device_name(ctx, device_name), n1p, n2p, n3p, len(shots)) + "|batch"
+    cache = load_cache(cache_path) if cache_path else {}
+    if key in cache and not force:
+        return cache[key]
+    job = sw.RTMJob(ctx, g, vel, wavelet[:steps], sample)
+
+    def time_fn(b):
+        job.set_batch(b)
+        job.run(0, len(sample))          # warm (graph capture, arena)
+        t0 = time.perf_counter()
+        job.run(0, len(sample))
+        return time.perf_counter() - t0
+
+    try:
+        best, results = select_batch(batches, time_fn)
+    finally:
+        job.close()
+    entry = {"batch": best, "seconds": {str(r[0]["batch"]): r[1] for r in results},
+             "shots_timed": len(sample), "steps": steps}
+    if cache_path:
+        cache[key] = entry
+        save_cache(cache, cache_path)
+    return entry
+
+
+def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | str | None = None,
+             cache_path: str | None = DEFAULT_CACHE, device_name: str | None = None,
+             force: bool = False) -> dict:
+    """Tunes ctx for the RTM job of `shots` and applies the winner.  `batch`
+    is the shots per launch (default: all of `shots`); "auto" chooses it
+    first (tune_batch) and returns it in the entry's "batch"."""
+    import numpy as np
+
+    import seismic_gb300 as sw
+    chosen = None
+    if batch == "auto":
+        chosen = tune_batch(ctx, model, vel, wavelet, shots, steps=steps, cache_path=cache_path,
+                            device_name=device_name, force=force)
+        batch = chosen["batch"]
+    batch = min(batch or len(shots), len(shots))
     sample = [{"sou": s["sou"], "rec": s["rec"],
                "data": np.ascontiguousarray(np.asarray(s["data"])[:, :steps])} for s in shots[:batch]]
     g = sw.SwGenpar.from_buffer_copy(model)
@@ -96,17 +187,11 @@ def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | None
     widths = [int(np.ptp(np.asarray(s["rec"])[:, 1]) / g.dx) + 1 for s in sample]
     n2p = max(widths) + 2 * g.ntaper + 8
     n3p = 1 if g.twoD else g.ny + 2 * g.ntaper + 8
-    if device_name is None:
-        try:
-            import torch
-            device_name = torch.cuda.get_device_name(ctx_device(ctx))
-        except Exception:
-            device_name = "cuda"
-    key = cache_key(device_name, n1p, n2p, n3p, batch)
+    key = cache_key(_device_name(ctx, device_name), n1p, n2p, n3p, batch)
     cache = load_cache(cache_path) if cache_path else {}
     if key in cache and not force:
         ctx.set_tuning(**cache[key]["tuning"])
-        return cache[key]
+        return dict(cache[key], batch=batch) if chosen else cache[key]
     job = sw.RTMJob(ctx, g, vel, wavelet[:steps], sample)
     job.set_batch(batch)
 
@@ -127,7 +212,7 @@ def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | None
     if cache_path:
         cache[key] = entry
         save_cache(cache, cache_path)
-    return entry
+    return dict(entry, batch=batch) if chosen else entry
 
 
 def ctx_device(ctx) -> int:

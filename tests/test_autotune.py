@@ -41,3 +41,19 @@ def test_cache_roundtrip(tmp_path):
     autotune.save_cache({k: {"tuning": {"tile_z": 64}}}, p)
     assert autotune.load_cache(p)[k]["tuning"]["tile_z"] == 64
     assert autotune.load_cache(os.path.join(tmp_path, "missing.json")) == {}
+
+
+def test_batch_candidates_cover_the_survey():
+    assert autotune.batch_candidates(3) == [1, 2, 3]
+    assert autotune.batch_candidates(16) == [1, 2, 4, 8, 16]
+    assert autotune.batch_candidates(100) == [1, 2, 4, 8, 16, 32, 64]
+    assert autotune.batch_candidates(1) == [1]
+
+
+def test_select_batch_prefers_throughput_then_smaller():
+    # Whole-sample seconds: launch overhead falls with batch size until the
+    # device is full, then flattens.
+    secs = {1: 8.0, 2: 4.1, 4: 2.2, 8: 1.5, 16: 1.5, 32: 1.7}
+    b, res = autotune.select_batch(secs, lambda b: secs[b])
+    assert b == 8
+    assert len(res) == len(secs)

@@ -216,3 +216,29 @@ def test_autotuner_on_device(oracle, tmp_path):
         c.close()
     rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
     np.testing.assert_array_equal(im, rim)
+
+
+def test_autotuner_chooses_shots_per_launch(oracle, tmp_path):
+    """tune_rtm(batch="auto") times each batch size on the same shot sample,
+    then the launch shape at the chosen size; the job run with both stays
+    bit-exact with the oracle."""
+    from seismic_gb300 import autotune
+    g, vel, w, shots = _survey(nshot=5, seed=13)
+    c = sw.Context(0)
+    try:
+        path = str(tmp_path / "tuning.json")
+        entry = autotune.tune_rtm(c, g, vel, w, shots, steps=24, batch="auto", cache_path=path)
+        assert entry["batch"] in autotune.batch_candidates(len(shots))
+        cached = autotune.load_cache(path)
+        times = next(v for k, v in cached.items() if k.endswith("|batch"))["seconds"]
+        assert set(times) == {str(b) for b in autotune.batch_candidates(len(shots))}
+        job = sw.RTMJob(c, g, vel, w, shots)
+        job.set_batch(entry["batch"])
+        job.run()
+        im, il, _ = job.result()
+        job.close()
+    finally:
+        c.close()
+    rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
+    np.testing.assert_array_equal(im, rim)
+    np.testing.assert_array_equal(il, ril)
