@@ -296,9 +296,8 @@ def main():
     for k in range(args.warmup):
         job.run(k * B, B)
     barrier()
-    # Timed region: inputs resident in HBM; events bracket the fused kernel.
+    # Timed region: inputs resident in HBM, no per-kernel events.
     ctx.reset_stats()
-    ctx.set_profiling(True)
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
@@ -319,9 +318,16 @@ def main():
     elapsed = time.perf_counter() - t_start
     ev_ms = ev0.elapsed_time(ev1)
     clk = clocks.stop()
+    launches_timed_region = int(ctx.stats()["launches_total"])
+    last_batch, _ = job.info()
+    # Roofline pass: one more step with CUDA events bracketing the fused step
+    # kernel (every 8th graph chunk), outside the timed region.
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    job.run(args.warmup * B, B)
+    torch.cuda.synchronize()
     ctx.set_profiling(False)
     st = ctx.stats()
-    last_batch, _ = job.info()
     secs = elapsed
     if ws > 1:
         t = torch.tensor([secs], device="cuda")
@@ -333,7 +339,7 @@ def main():
     else:
         points_all = float(points)
     value = points_all / secs / 1e9
-    # Roofline of the fused step kernel (CUDA events around every launch).
+    # Roofline of the fused step kernel from the roofline pass's events.
     peak, peak_kind = measured_peak()
     kern_s = st["step_kernel_ms"] / 1e3
     nl = max(1, st["step_kernel_timed"])
@@ -393,7 +399,7 @@ def main():
                          "algorithmic_bytes_per_launch": algo_per_launch,
                          "launches_timed": st["step_kernel_timed"]},
             "cpu_baseline": cpu, "e2e": e2e_line, "clocks": clk,
-            "gpu_launches": int(st["launches_total"]),
+            "gpu_launches": launches_timed_region,
             "timed_event_ms": ev_ms,
         }
         print(json.dumps(line), flush=True)

@@ -226,6 +226,28 @@ int sw_rtm_job_result(sw_rtm_job *job, float *image, float *illum, float *image_
 int sw_rtm_job_reset(sw_rtm_job *job);
 int sw_rtm_job_destroy(sw_rtm_job *job);
 
+/* ---- Shot windows (host only; no context) --------------------------------
+ * The source/receiver patch widened by the aperture
+ * (extract_coord_source_receiver_patch, ExtractPadModel.f90:19-85) and its
+ * grid size (read_window_vel, ExtractPadModel.f90:176-182): nxw =
+ * nint((endx - oxw)/dx) + 1, and likewise in y (nyw = 1, oyw = oy in 2D).
+ * The window's genpar is the model's with nx = nxw, ny = nyw, ox = oxw,
+ * oy = oyw. */
+typedef struct sw_window {
+  float oxw, oyw, endx, endy;
+  int nxw, nyw;
+} sw_window;
+int sw_shot_window(const sw_genpar *model, float aperture_x, float aperture_y,
+                   const float *sou_coord, int nrec, const float *rec_coord, sw_window *out);
+/* small (nz*nxw*nyw) = the model columns nearest each window column, clamped
+ * to the model (mod_window_pad adj=.true., ExtractPadModel.f90:517-531). */
+int sw_window_extract(const sw_genpar *model, const sw_window *w, const float *big, float *small);
+/* big (nz*nx*ny) += the window columns that fall inside the model
+ * (mod_window_pad adj=.false. and mod_copy_image_to_disk,
+ * ExtractPadModel.f90:532-546,551-590). */
+int sw_window_scatter_add(const sw_genpar *model, const sw_window *w, const float *small,
+                          float *big);
+
 /* ---- FWI objective / gradient (progs/afwi/compute_function_gradient.f90) */
 
 typedef struct sw_fwi_shot {

@@ -68,6 +68,11 @@ class SwFwiDesc(C.Structure):
                 ("smooth_doy", C.c_int), ("checkpoint_snaps", C.c_int)]
 
 
+class SwWindow(C.Structure):
+    _fields_ = [("oxw", C.c_float), ("oyw", C.c_float), ("endx", C.c_float),
+                ("endy", C.c_float), ("nxw", C.c_int), ("nyw", C.c_int)]
+
+
 class SwShot(C.Structure):
     _fields_ = [("sou_coord", C.c_float * 3), ("nrec", C.c_int), ("rec_coord", _fp),
                 ("data", _fp), ("nt", C.c_int)]
@@ -129,6 +134,10 @@ _SIGS = {
     "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
     "sw_ctx_set_boundary": (C.c_int, [C.c_void_p, C.c_int]),
+    "sw_shot_window": (C.c_int, [C.POINTER(SwGenpar), C.c_float, C.c_float, _fp, C.c_int, _fp,
+                                 C.POINTER(SwWindow)]),
+    "sw_window_extract": (C.c_int, [C.POINTER(SwGenpar), C.POINTER(SwWindow), _fp, _fp]),
+    "sw_window_scatter_add": (C.c_int, [C.POINTER(SwGenpar), C.POINTER(SwWindow), _fp, _fp]),
     "sw_ctx_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
 }
 
@@ -455,6 +464,42 @@ def vel_check(g: SwGenpar, vel) -> tuple[int, float, float]:
     a, b = C.c_float(), C.c_float()
     code = lib.sw_vel_check(C.byref(g), fptr(v), C.byref(a), C.byref(b))
     return code, a.value, b.value
+
+
+def shot_window(model: SwGenpar, aperture_x: float, aperture_y: float, sou_coord,
+                rec_coord) -> tuple[SwWindow, SwGenpar]:
+    """The shot's window (sw_shot_window) and the window's genpar."""
+    lib = load_library()
+    s, r = _f32(sou_coord), _f32(rec_coord)
+    w = SwWindow()
+    code = lib.sw_shot_window(C.byref(model), aperture_x, aperture_y, fptr(s), r.size // 3,
+                              fptr(r), C.byref(w))
+    if code != SW_OK:
+        raise SwaveError(code, "sw_shot_window")
+    g = SwGenpar.from_buffer_copy(model)
+    g.nx, g.ny, g.ox, g.oy = w.nxw, w.nyw, w.oxw, w.oyw
+    return w, g
+
+
+def window_extract(model: SwGenpar, w: SwWindow, big) -> np.ndarray:
+    lib = load_library()
+    b = _f32(big)
+    out = np.zeros((w.nyw, w.nxw, model.nz), np.float32)
+    code = lib.sw_window_extract(C.byref(model), C.byref(w), fptr(b), fptr(out))
+    if code != SW_OK:
+        raise SwaveError(code, "sw_window_extract")
+    return out if not model.twoD else out[0]
+
+
+def window_scatter_add(model: SwGenpar, w: SwWindow, small, big: np.ndarray) -> np.ndarray:
+    """big += the window columns inside the model (in place; big float32)."""
+    lib = load_library()
+    s = _f32(small)
+    assert big.dtype == np.float32 and big.flags.c_contiguous
+    code = lib.sw_window_scatter_add(C.byref(model), C.byref(w), fptr(s), fptr(big))
+    if code != SW_OK:
+        raise SwaveError(code, "sw_window_scatter_add")
+    return big
 
 
 class CNN:

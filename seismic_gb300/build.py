@@ -73,6 +73,44 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+CLI_DIR = os.path.join(PKG, "cli")
+BINDIR = os.path.join(LIBDIR, "bin")
+# Program name (as the reference names it) -> its source in cli/.
+CLI_PROGRAMS = {
+    "Acoustic_modeling_sep.x": "acoustic_modeling_sep.c",
+    "3DRTM.x": "rtm3d.c",
+    "3DBORNMOD.x": "bornmod3d.c",
+}
+
+
+def build_cli(force: bool = False) -> dict[str, str]:
+    """Compiles the SEP command-line programs against libswave.so (host C;
+    the library is found next to them through the run path)."""
+    build_library()
+    os.makedirs(BINDIR, exist_ok=True)
+    common = [os.path.join(CLI_DIR, f) for f in ("sep.c", "swcli.c")]
+    deps = common + [os.path.join(CLI_DIR, f) for f in ("sep.h", "swcli.h")] + [
+        os.path.join(ROOT, "include", "swave.h"), LIB]
+    cc = shutil.which("gcc") or "gcc"
+    jobs, out = [], {}
+    for exe, src in CLI_PROGRAMS.items():
+        target = os.path.join(BINDIR, exe)
+        out[exe] = target
+        s = os.path.join(CLI_DIR, src)
+        if force or _stale(target, [s] + deps):
+            jobs.append([cc, "-O2", "-std=c11", "-Wall", "-Wextra", "-Wno-unused-parameter",
+                         "-I", os.path.join(ROOT, "include"), "-o", target, s, *common,
+                         "-L", LIBDIR, "-lswave", "-Wl,-rpath,$ORIGIN/..", "-lm"])
+    sep_lib = os.path.join(LIBDIR, "libswsep.so")
+    if force or _stale(sep_lib, common + deps[2:4]):
+        jobs.append([cc, "-O2", "-std=c11", "-Wall", "-fPIC", "-shared", "-o", sep_lib,
+                     common[0]])
+    with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(_run, jobs))
+    out["libswsep.so"] = sep_lib
+    return out
+
+
 def build_oracle(force: bool = False) -> str:
     """Compiles the CPU restatement used by the tests and the CPU baseline."""
     src = os.path.join(ORACLE_DIR, "swave_oracle.cpp")
@@ -88,4 +126,5 @@ def build_oracle(force: bool = False) -> str:
 if __name__ == "__main__":
     force = "--force" in sys.argv
     build_library(force=force, verbose=True)
+    build_cli(force=force)
     build_oracle(force=force)

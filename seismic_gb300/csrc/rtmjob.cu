@@ -65,7 +65,69 @@ void window_host(const sw_genpar &g, const Window &w, const float *big, std::vec
   }
 }
 
+// mod_window_pad(adj=.false.) / mod_copy_image_to_disk
+// (ExtractPadModel.f90:532-546,551-590): window columns that fall inside the
+// model are added to the model column of the nearest node.
+void window_scatter_add_host(const sw_genpar &g, const Window &w, const float *small, float *big) {
+  for (int j = 1; j <= w.nyw; ++j) {
+    const float cy = (float)(j - 1) * g.dy + w.oyw;
+    const int iy = (int)lroundf((cy - g.oy) / g.dy) + 1;
+    if (iy < 1 || iy > g.ny) continue;
+    for (int i = 1; i <= w.nxw; ++i) {
+      const float cx = (float)(i - 1) * g.dx + w.oxw;
+      const int ix = (int)lroundf((cx - g.ox) / g.dx) + 1;
+      if (ix < 1 || ix > g.nx) continue;
+      float *dst = &big[(size_t)g.nz * ((ix - 1) + (size_t)g.nx * (iy - 1))];
+      const float *src = &small[(size_t)g.nz * ((i - 1) + (size_t)w.nxw * (j - 1))];
+      for (int k = 0; k < g.nz; ++k) dst[k] = dst[k] + src[k];
+    }
+  }
+}
+
 }  // namespace swave
+
+// ---- C-ABI window helpers (host only) --------------------------------------
+int sw_shot_window(const sw_genpar *model, float aperture_x, float aperture_y,
+                   const float *sou_coord, int nrec, const float *rec_coord, sw_window *out) {
+  if (!model || !sou_coord || !rec_coord || !out) return SW_BAD_PARAM;
+  Window w;
+  const int st = compute_window(nullptr, *model, aperture_x, aperture_y, sou_coord, nrec,
+                                rec_coord, w);
+  if (st) return st;
+  out->oxw = w.oxw;
+  out->oyw = w.oyw;
+  out->endx = w.endx;
+  out->endy = w.endy;
+  out->nxw = w.nxw;
+  out->nyw = w.nyw;
+  return SW_OK;
+}
+
+static Window to_window(const sw_window *w) {
+  Window v;
+  v.oxw = w->oxw;
+  v.oyw = w->oyw;
+  v.endx = w->endx;
+  v.endy = w->endy;
+  v.nxw = w->nxw;
+  v.nyw = w->nyw;
+  return v;
+}
+
+int sw_window_extract(const sw_genpar *model, const sw_window *w, const float *big, float *small) {
+  if (!model || !w || !big || !small || w->nxw < 1 || w->nyw < 1) return SW_BAD_PARAM;
+  std::vector<float> tmp;
+  window_host(*model, to_window(w), big, tmp);
+  std::memcpy(small, tmp.data(), tmp.size() * sizeof(float));
+  return SW_OK;
+}
+
+int sw_window_scatter_add(const sw_genpar *model, const sw_window *w, const float *small,
+                          float *big) {
+  if (!model || !w || !big || !small || w->nxw < 1 || w->nyw < 1) return SW_BAD_PARAM;
+  window_scatter_add_host(*model, to_window(w), small, big);
+  return SW_OK;
+}
 
 namespace {
 

@@ -66,3 +66,28 @@ def test_born_wavelet_matches_oracle(lib, oracle):
     oracle.load().oracle_born_wavelet(b.ctypes.data_as(C.POINTER(C.c_float)), b.size, 5e-4)
     np.testing.assert_array_equal(a, b)
     assert a[0] == 0 and a[-1] == 0
+
+
+def test_window_helpers_match_the_oracle_job_windowing(lib):
+    """sw_shot_window / sw_window_extract / sw_window_scatter_add: the
+    extract_coord_source_receiver_patch window, nearest-column extraction
+    clamped to the model, and the in-model scatter-add (host only)."""
+    g = sw.make_genpar(12, 50, 1, dz=10.0, dx=10.0, ox=100.0)
+    rec = np.zeros((5, 3), np.float32)
+    rec[:, 1] = [150.0, 200.0, 260.0, 300.0, 333.0]
+    sou = np.array([5.0, 120.0, 0.0], np.float32)
+    w, gw = sw.shot_window(g, 400.0, 0.0, sou, rec)
+    # centre = midpoint range [135, 226.5] -> 180.75; window [-19.25, 380.75]
+    assert w.oxw == np.float32(-19.25) and w.endx == np.float32(380.75)
+    assert w.nxw == 41 and gw.nx == 41 and gw.ox == w.oxw
+    big = np.arange(50 * 12, dtype=np.float32).reshape(50, 12)
+    small = sw.window_extract(g, w, big)
+    ix = np.clip(np.rint((w.oxw + 10.0 * np.arange(41) - 100.0) / 10.0).astype(int), 0, 49)
+    np.testing.assert_array_equal(small, big[ix])
+    acc = np.zeros_like(big)
+    sw.window_scatter_add(g, w, np.ones_like(small), acc)
+    inside = np.rint((w.oxw + 10.0 * np.arange(41) - 100.0) / 10.0).astype(int)
+    inside = inside[(inside >= 0) & (inside < 50)]
+    expect = np.zeros(50, np.float32)
+    np.add.at(expect, inside, 1.0)
+    np.testing.assert_array_equal(acc[:, 0], expect)
