@@ -80,6 +80,7 @@ CLI_PROGRAMS = {
     "Acoustic_modeling_sep.x": "acoustic_modeling_sep.c",
     "3DRTM.x": "rtm3d.c",
     "3DBORNMOD.x": "bornmod3d.c",
+    "2DAFWI.x": "afwi2d.c",
 }
 
 

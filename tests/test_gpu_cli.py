@@ -131,3 +131,98 @@ def test_born_program(built, oracle, tmp_path, three_d):
     rd = oracle.born(g, vel[win], ref[win], sou, sw.born_wavelet(w, g.dt), rec)
     assert np.abs(rd).max() > 0
     np.testing.assert_array_equal(data, rd)
+
+
+def _survey_files(tmp_path, nt=140):
+    """Three gathers on an 80-column 2D model; coordfile rows in gather
+    order (the source changes between gathers)."""
+    nz = 36
+    vel = model2d(nz, 80, D, seed=8)
+    rows, gathers = [], []
+    for sx in (250.0, 400.0, 520.0):
+        rx = np.arange(sx - 120.0, sx + 121.0, 20.0)
+        gathers.append((sx, rx))
+        for x in rx:
+            rows.append([sx, x, 0.0, 0.0, 20.3, 12.3])
+    keys = np.array(rows, np.float32)
+    w = synth.ricker(12.0, DT, nt).astype(np.float32)
+    sep.write(str(tmp_path / "vel.H"), vel, {"d1": D, "d2": D, "o1": 0.0, "o2": 0.0})
+    sep.write(str(tmp_path / "w.H"), w, {"d1": DT, "o1": 0.0})
+    sep.write(str(tmp_path / "keys.H"), keys)
+    params = dict(stdin=tmp_path / "w.H", vel=tmp_path / "vel.H", coordfile=tmp_path / "keys.H",
+                  keysx=1, keygx=2, keysy=3, keygy=4, keyselev=5, keygelev=6,
+                  aperture_x=200, aperture_y=0, twoD=1, snapi=4, ntaper=10, fmax=30)
+    return params, vel, w, gathers
+
+
+def _gather_geometry(vel, sx, rx, nt, apx=200.0):
+    """Window of one gather: centre sx (receivers symmetric about it),
+    window [min(sx-120, sx-apx/2), max(sx+120, sx+apx/2)]."""
+    lo = min(rx.min(), sx - apx / 2)
+    hi = max(rx.max(), sx + apx / 2)
+    i0, nxw = int(round(lo / D)), int(round((hi - lo) / D)) + 1
+    g = sw.make_genpar(vel.shape[1], nxw, 1, dz=D, dx=D, ox=lo, dt=DT, nt=nt, ntaper=10,
+                       lsinc=7, snapi=4, fmax=30.0)
+    rec = np.stack([np.full(rx.size, 12.3), rx, np.zeros_like(rx)], 1).astype(np.float32)
+    return g, i0, nxw, rec
+
+
+def test_afwi_program_task_mod(built, oracle, tmp_path):
+    params, vel, w, gathers = _survey_files(tmp_path)
+    nt = w.size
+    params.update(Task="MOD", data=tmp_path / "d.H")
+    _run(built, "2DAFWI.x", params)
+    data, h = sep.read(str(tmp_path / "d.H"))
+    ntot = sum(rx.size for _, rx in gathers)
+    assert data.shape == (ntot, nt) and int(h["n2"]) == ntot
+    row = 0
+    for sx, rx in gathers:
+        g, i0, nxw, rec = _gather_geometry(vel, sx, rx, nt)
+        d = sw.SwPropDesc()
+        d.g = g
+        d.tmin, d.tmax, d.tstep = 1, nt, 1
+        d.fd_scheme, d.injection, d.extraction = sw.FD_FORWARD, sw.INJ_SINC, sw.EXT_SIMPLE_AFWI
+        ref = np.zeros((rx.size, nt), np.float32)
+        oracle.propagate(d, vel[i0:i0 + nxw], np.array([20.3, sx, 0.0], np.float32), w, rec, ref)
+        assert np.abs(ref).max() > 0
+        np.testing.assert_array_equal(data[row:row + rx.size], ref)
+        row += rx.size
+
+
+def test_afwi_program_task_mig(built, oracle, tmp_path):
+    params, vel, w, gathers = _survey_files(tmp_path, nt=120)
+    nt = w.size
+    ntot = sum(rx.size for _, rx in gathers)
+    obs = (np.random.default_rng(9).standard_normal((ntot, nt)) * 1e-2).astype(np.float32)
+    params.update(Task="MIG", traces=_traces(tmp_path, "t.H", obs), image=tmp_path / "im.H")
+    _run(built, "2DAFWI.x", params)
+    img, _ = sep.read(str(tmp_path / "im.H"))
+    im = np.zeros_like(vel)
+    il = np.zeros_like(vel)
+    row = 0
+    for sx, rx in gathers:
+        g, i0, nxw, rec = _gather_geometry(vel, sx, rx, nt)
+        vs = vel[i0:i0 + nxw]
+        sou = np.array([20.3, sx, 0.0], np.float32)
+        d = sw.SwPropDesc()
+        d.g = g
+        d.tmin, d.tmax, d.tstep = 1, nt, 1
+        d.fd_scheme, d.injection, d.extract_wave = sw.FD_FORWARD, sw.INJ_SINC, 1
+        wave = np.zeros((nt // g.snapi) * vs.size, np.float32)
+        oracle.propagate(d, vs, sou, w, wave=wave)
+        b = sw.SwPropDesc()
+        b.g = g
+        b.tmin, b.tmax, b.tstep = nt, 1, -1
+        b.fd_scheme, b.injection, b.imaging = sw.FD_FORWARD, sw.INJ_SIMPLE, sw.IMG_AFWI
+        ims, ils = np.zeros(vs.size, np.float32), np.zeros(vs.size, np.float32)
+        oracle.propagate(b, vs, rec, obs[row:row + rx.size], wave=wave, image=ims, illum=ils)
+        im[i0:i0 + nxw] += ims.reshape(vs.shape)
+        il[i0:i0 + nxw] += ils.reshape(vs.shape)
+        row += rx.size
+    r = np.sqrt(np.sum(il.astype(np.float64) ** 2) / il.size)
+    norm = ((il + np.float32(il.max() / np.float32(10000))).astype(np.float64) / r).astype(np.float32)
+    expect = im / norm
+    assert np.abs(expect).max() > 0
+    # The stacking order is the same (gather order); the FP64 RMS sum runs in
+    # index order on both sides.
+    np.testing.assert_allclose(img, expect, rtol=1e-6, atol=1e-6 * np.abs(expect).max())
