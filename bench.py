@@ -355,10 +355,12 @@ def main():
             traffic = float(json.load(open(prof_json))["dram_per_algorithmic"]) * algo_per_launch
         except Exception:
             traffic = None
-    # End to end through the public API with host buffers (one step's shots).
+    # End to end through the public API with host buffers: the timed steps'
+    # shots again, through a new job (model, wavelet and traces copied from
+    # pinned host memory, the images read back).
     e2e_line = None
     if rank == 0:
-        sel = job_shots[args.warmup * B:(args.warmup + 1) * B]
+        sel = job_shots[args.warmup * B:nsteps * B]
         pin = lambda a: _pinned(torch, a)
         hshots = [{"sou": s["sou"], "rec": s["rec"], "data": pin(s["data"])} for s in sel]
         hvel = pin(vel)
@@ -372,11 +374,12 @@ def main():
         j2.close()
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
-        pts_e2e = sum(shot_points(s) for s in per_step[args.warmup * B:(args.warmup + 1) * B])
+        pts_e2e = sum(shot_points(s) for s in per_step[args.warmup * B:nsteps * B])
         h2d = hvel.nbytes + hw.nbytes + sum(s["data"].nbytes + s["rec"].nbytes for s in hshots)
         d2h = im.nbytes + il.nbytes + nm.nbytes
-        e2e_line = {"value": pts_e2e / e2e_s / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h)}
+        e2e_line = {"value": pts_e2e / e2e_s / 1e9, "unit": "Gpts/s",
+                    "h2d_bytes_per_step": int(h2d) // args.steps,
+                    "d2h_bytes_per_step": int(d2h) // args.steps}
     # CPU baseline (rank 0, N=1 only): a bounded sample of the same workload.
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
