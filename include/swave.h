@@ -122,6 +122,13 @@ typedef struct sw_prop_io {
   const float *ref;         /* nz*nx*ny reflectivity for SW_IMG_BORN       */
   float *final_u2;          /* optional: padded u2 after the last step,
                                (nz+2nt+8)*(nx+2nt+8)*(ny>1?ny+2nt+8:1)    */
+  const float *rho;         /* nz*nx*ny density (withRho), or NULL: the
+                               variable-density operator
+                               FD_{2D,3D}_derivatives_acoustic_forward_grid
+                               (FDderivatives.f90:263-382,588-657) with
+                               sinc- and nearest-node injection scaled by
+                               v^2*rho (Injection.f90:170-190); requires
+                               fd_scheme = SW_FD_FORWARD                   */
 } sw_prop_io;
 
 typedef struct sw_ctx sw_ctx;

@@ -27,7 +27,8 @@ def _types():
 class OrPropIO64(C.Structure):
     _fields_ = [("vel", _dp), ("nsou", C.c_int), ("sou_coord", _dp), ("sou_trace", _dp),
                 ("nrec", C.c_int), ("rec_coord", _dp), ("rec_trace", _dp), ("wave", _dp),
-                ("image", _dp), ("illum", _dp), ("ref", _dp), ("final_u2", _dp)]
+                ("image", _dp), ("illum", _dp), ("ref", _dp), ("final_u2", _dp),
+                ("rho", _dp)]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -56,6 +57,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
         "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],
         "oracle_stencil_f64": [g, C.c_int, _dp, _dp, _dp],
+        "oracle_stencil_rho_f64": [g, _dp, _dp, _dp, _dp],
         "oracle_triangle2": [_fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                              C.c_int, C.c_int],
         "oracle_lbfgs_step": [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
@@ -160,7 +162,7 @@ def born(g, vel, ref, sou, wavelet, rec, f64=False):
 
 
 def propagate(desc, vel, sou_coord=None, sou_trace=None, rec_coord=None, rec_trace=None,
-              wave=None, image=None, illum=None, ref=None, final_u2=None):
+              wave=None, image=None, illum=None, ref=None, final_u2=None, rho=None):
     lib = load()
     _, _, IO, _, _ = _types()
     io = IO()
@@ -179,6 +181,8 @@ def propagate(desc, vel, sou_coord=None, sou_trace=None, rec_coord=None, rec_tra
             setattr(io, name, arr.ctypes.data_as(_fp))
     if ref is not None:
         a, io.ref = _f(ref); keep.append(a)
+    if rho is not None:
+        a, io.rho = _f(rho); keep.append(a)
     _chk(lib.oracle_propagate_f32(C.byref(desc), C.byref(io)), "propagate")
 
 
@@ -238,6 +242,18 @@ def stencil_f64(g, vel, u2, adjoint=False):
     out = np.zeros_like(a)
     _chk(lib.oracle_stencil_f64(C.byref(g), int(adjoint), pv, pa, out.ctypes.data_as(_dp)),
          "stencil")
+    return out
+
+
+def stencil_rho_f64(g, vel, rho, u2):
+    """Applies the variable-density operator once to a padded field u2."""
+    lib = load()
+    v, pv = _d(vel)
+    r, pr = _d(rho)
+    a, pa = _d(u2)
+    out = np.zeros_like(a)
+    _chk(lib.oracle_stencil_rho_f64(C.byref(g), pv, pr, pa, out.ctypes.data_as(_dp)),
+         "stencil_rho")
     return out
 
 

@@ -43,6 +43,7 @@ typedef struct or_prop_io64 {
   double *illum;
   const double *ref;
   double *final_u2;
+  const double *rho;
 } or_prop_io64;
 
 /* propagator_acoustic (libs/libwave/Propagator.f90:27-270). */
@@ -113,6 +114,10 @@ int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2,
 void oracle_set_rigid(int on);
 int oracle_stencil_f64(const sw_genpar *g, int adjoint, const double *vel,
                        const double *u2, double *u3);
+/* One application of the variable-density operator v^2*rho*div(grad(u2)/rho2)
+ * (FDderivatives.f90:263-382,588-657) to a padded field, FP64. */
+int oracle_stencil_rho_f64(const sw_genpar *g, const double *vel, const double *rho,
+                           const double *u2, double *u3);
 
 /* mksinc (libs/libwave/Interpolate.f90:15-42). */
 void oracle_mksinc(float *sinc, int lsinc, float shift);

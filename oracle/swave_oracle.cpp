@@ -468,6 +468,170 @@ template <class T> static void mksinc(T *sinc, int lsinc, T shift) {
   for (int n = 1; n <= lsinc; ++n) sinc[n - 1] = sinc[n - 1] / fsum;
 }
 
+// ---------------------------------------------------------------------------
+// Variable density (genpar%withRho)
+// ---------------------------------------------------------------------------
+
+// FD_acoustic_rho_init_coefs (FDcoefs.f90:12-23) scaled by
+// FD_types_assign_scaled_coefs with coefpower = 1 (FDtypes.f90:50-80).
+template <class T> static Coefs<T> make_rho_coefs(const sw_genpar &g) {
+  const T c0 = T(0.), c1 = T(1225.) / T(1024.), c2 = T(-1225.) / (T(1024.) * T(15.)),
+          c3 = T(1225.) / (T(1024.) * T(125.)), c4 = T(-1225.) / (T(1024.) * T(1715.));
+  const T dxi = T(1.) / (T)g.dx, dyi = T(1.) / (T)g.dy, dzi = T(1.) / (T)g.dz;
+  Coefs<T> c;
+  c.c0x = c0 * dxi; c.c1x = c1 * dxi; c.c2x = c2 * dxi; c.c3x = c3 * dxi; c.c4x = c4 * dxi;
+  c.c0y = c0 * dyi; c.c1y = c1 * dyi; c.c2y = c2 * dyi; c.c3y = c3 * dyi; c.c4y = c4 * dyi;
+  c.c0z = c0 * dzi; c.c1z = c1 * dzi; c.c2z = c2 * dzi; c.c3z = c3 * dzi; c.c4z = c4 * dzi;
+  return c;
+}
+
+// Interpolate (Interpolate.f90:44-130): rho2 = rho shifted half a cell along
+// z, then x, then (3D) y by a 9-point sinc, each line extended by its end
+// values.
+template <class T>
+static void rho_interpolate(const Bounds &b, const F3<T> &rho, F3<T> &rho2) {
+  const int lsinc = 9, h = lsinc / 2;
+  T sinc[9];
+  mksinc<T>(sinc, lsinc, T(0.5));
+  rho2 = rho;
+  const int lo1 = b.nmin1 - 4, hi1 = b.nmax1 + 4, lo2 = b.nmin2 - 4, hi2 = b.nmax2 + 4;
+  const int lo3 = b.nmin3 - b.nbound, hi3 = b.nmax3 + b.nbound;
+  std::vector<T> tr;
+  // One line: tr[q - lo + lsinc] holds sample q, q in lo-lsinc..hi+lsinc.
+  auto filter = [&](int lo, int hi, auto get, auto put) {
+    tr.assign((size_t)(hi - lo + 1 + 2 * lsinc), T(0));
+    for (int q = lo; q <= hi; ++q) tr[(size_t)(q - lo + lsinc)] = get(q);
+    for (int q = lo - lsinc; q <= lo - 1; ++q) tr[(size_t)(q - lo + lsinc)] = get(lo);
+    for (int q = hi + 1; q <= hi + lsinc; ++q) tr[(size_t)(q - lo + lsinc)] = get(hi);
+    for (int q = lo; q <= hi; ++q) {
+      T f = T(0.);
+      for (int l = -h; l <= h; ++l) f = f + sinc[h + l] * tr[(size_t)(q + l - lo + lsinc)];
+      put(q, f);
+    }
+  };
+  for (int k = lo3; k <= hi3; ++k)
+    for (int j = lo2; j <= hi2; ++j)
+      filter(lo1, hi1, [&](int i) { return rho(i, j, k); },
+             [&](int i, T f) { rho2(i, j, k) = f; });
+  for (int k = lo3; k <= hi3; ++k)
+    for (int i = lo1; i <= hi1; ++i)
+      filter(lo2, hi2, [&](int j) { return rho2(i, j, k); },
+             [&](int j, T f) { rho2(i, j, k) = f; });
+  if (hi3 > 1)
+    for (int j = lo2; j <= hi2; ++j)
+      for (int i = lo1; i <= hi1; ++i)
+        filter(lo3, hi3, [&](int k) { return rho2(i, j, k); },
+               [&](int k, T f) { rho2(i, j, k) = f; });
+}
+
+// FD_2D_derivatives_acoustic_forward_grid (FDderivatives.f90:588-657) and
+// FD_3D_derivatives_acoustic_forward_grid (FDderivatives.f90:263-382): the
+// staggered gradient of u2 scaled by delp = 1/rho2 (with first-order
+// differences in the three padding cells beyond each face), then its
+// staggered divergence times v^2*rho.  The gradient arrays persist over the
+// steps of a propagation; the cells the reference never writes (the fourth
+// padding cell, read by the divergence at the domain's first cell) stay zero.
+template <class T> struct RhoState {
+  F3<T> rho, delp, sz, sx, sy;
+  Coefs<T> c;
+  T dzi, dxi, dyi;
+};
+
+template <class T>
+static void rho_state_init(RhoState<T> &r, const sw_genpar &g, const Bounds &b, const T *rho_in) {
+  r.rho.init(b);
+  model_pad(rho_in, r.rho, b, g.nz, g.nx, g.ny, g.twoD != 0);
+  F3<T> rho2;
+  rho_interpolate(b, r.rho, rho2);
+  r.delp = rho2;
+  for (auto &v : r.delp.v) v = T(1.) / v;
+  r.sz.init(b);
+  r.sx.init(b);
+  if (!g.twoD) r.sy.init(b);
+  r.c = make_rho_coefs<T>(g);
+  r.dzi = T(1.) / (T)g.dz;
+  r.dxi = T(1.) / (T)g.dx;
+  r.dyi = T(1.) / (T)g.dy;
+}
+
+template <class T>
+static void stencil_rho(RhoState<T> &r, const Bounds &b, bool twoD, const F3<T> &u2, F3<T> &u3,
+                        const F3<T> &vel) {
+  const Coefs<T> &c = r.c;
+  F3<T> &sz = r.sz, &sx = r.sx, &sy = r.sy;
+  const F3<T> &dp = r.delp;
+  const int k0 = twoD ? 1 : b.nmin3, k1 = twoD ? 1 : b.nmax3;
+  for (int k = k0; k <= k1; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        const T d = dp(i, j, k);
+        T a = c.c1z * (u2(i + 1, j, k) - u2(i, j, k));
+        a = a + c.c2z * (u2(i + 2, j, k) - u2(i - 1, j, k));
+        a = a + c.c3z * (u2(i + 3, j, k) - u2(i - 2, j, k));
+        a = a + c.c4z * (u2(i + 4, j, k) - u2(i - 3, j, k));
+        sz(i, j, k) = a * d;
+        a = c.c1x * (u2(i, j + 1, k) - u2(i, j, k));
+        a = a + c.c2x * (u2(i, j + 2, k) - u2(i, j - 1, k));
+        a = a + c.c3x * (u2(i, j + 3, k) - u2(i, j - 2, k));
+        a = a + c.c4x * (u2(i, j + 4, k) - u2(i, j - 3, k));
+        sx(i, j, k) = a * d;
+        if (!twoD) {
+          a = c.c1y * (u2(i, j, k + 1) - u2(i, j, k));
+          a = a + c.c2y * (u2(i, j, k + 2) - u2(i, j, k - 1));
+          a = a + c.c3y * (u2(i, j, k + 3) - u2(i, j, k - 2));
+          a = a + c.c4y * (u2(i, j, k + 4) - u2(i, j, k - 3));
+          sy(i, j, k) = a * d;
+        }
+      }
+  // First-order gradient in the padding cells, scaled by delp of the
+  // adjacent domain face.
+  auto pad = [&](int i, int j, int k, T d) {
+    sz(i, j, k) = (r.dzi * (u2(i + 1, j, k) - u2(i, j, k))) * d;
+    sx(i, j, k) = (r.dxi * (u2(i, j + 1, k) - u2(i, j, k))) * d;
+    if (!twoD) sy(i, j, k) = (r.dyi * (u2(i, j, k + 1) - u2(i, j, k))) * d;
+  };
+  for (int k = k0; k <= k1; ++k) {
+    for (int j = b.nmin2; j <= b.nmax2; ++j) {
+      for (int i = b.nmin1 - 1; i >= b.nmin1 - 3; --i) pad(i, j, k, dp(b.nmin1, j, k));
+      for (int i = b.nmax1 + 1; i <= b.nmax1 + 3; ++i) pad(i, j, k, dp(b.nmax1, j, k));
+    }
+    for (int j = b.nmin2 - 1; j >= b.nmin2 - 3; --j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) pad(i, j, k, dp(i, b.nmin2, k));
+    for (int j = b.nmax2 + 1; j <= b.nmax2 + 3; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) pad(i, j, k, dp(i, b.nmax2, k));
+  }
+  if (!twoD) {
+    for (int k = b.nmin3 - 1; k >= b.nmin3 - 3; --k)
+      for (int j = b.nmin2; j <= b.nmax2; ++j)
+        for (int i = b.nmin1; i <= b.nmax1; ++i) pad(i, j, k, dp(i, j, b.nmin3));
+    for (int k = b.nmax3 + 1; k <= b.nmax3 + 3; ++k)
+      for (int j = b.nmin2; j <= b.nmax2; ++j)
+        for (int i = b.nmin1; i <= b.nmax1; ++i) pad(i, j, k, dp(i, j, b.nmax3));
+  }
+  for (int k = k0; k <= k1; ++k)
+    for (int j = b.nmin2; j <= b.nmax2; ++j)
+      for (int i = b.nmin1; i <= b.nmax1; ++i) {
+        T tz = c.c1z * (sz(i, j, k) - sz(i - 1, j, k));
+        tz = tz + c.c2z * (sz(i + 1, j, k) - sz(i - 2, j, k));
+        tz = tz + c.c3z * (sz(i + 2, j, k) - sz(i - 3, j, k));
+        tz = tz + c.c4z * (sz(i + 3, j, k) - sz(i - 4, j, k));
+        T tx = c.c1x * (sx(i, j, k) - sx(i, j - 1, k));
+        tx = tx + c.c2x * (sx(i, j + 1, k) - sx(i, j - 2, k));
+        tx = tx + c.c3x * (sx(i, j + 2, k) - sx(i, j - 3, k));
+        tx = tx + c.c4x * (sx(i, j + 3, k) - sx(i, j - 4, k));
+        const T v = vel(i, j, k);
+        if (twoD) {
+          u3(i, j, k) = ((v * v) * r.rho(i, j, k)) * (tx + tz);
+        } else {
+          T ty = c.c1y * (sy(i, j, k) - sy(i, j, k - 1));
+          ty = ty + c.c2y * (sy(i, j, k + 1) - sy(i, j, k - 2));
+          ty = ty + c.c3y * (sy(i, j, k + 2) - sy(i, j, k - 3));
+          ty = ty + c.c4y * (sy(i, j, k + 3) - sy(i, j, k - 4));
+          u3(i, j, k) = ((v * v) * r.rho(i, j, k)) * ((tx + ty) + tz);
+        }
+      }
+}
+
 // find_i_d (libs/libwave/ModelSpaceTypes.f90:144-151).
 template <class T>
 static void find_i_d(int &ielev, T &delev, T elev, T orig, T delta) {
@@ -558,6 +722,7 @@ template <class T> struct IO {
   T *illum;
   const T *ref;
   T *final_u2;
+  const T *rho;   // unpadded density (withRho), or null
 };
 
 static int check_genpar(const sw_genpar &g) {
@@ -590,6 +755,13 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
   F3<T> *um1 = &ua, *u0 = &ub, *u1 = &uc, *u2 = &ud, *u3 = &ue;
 
   const Coefs<T> c = make_coefs<T>(g);
+  RhoState<T> rs;
+  if (io.rho) {
+    // The variable-density drivers run the forward-grid operator in both
+    // directions (to_disk_to_memory_RTM.f90:388-398,455-465).
+    if (d.fd_scheme != SW_FD_FORWARD) return SW_UNSUPPORTED;
+    rho_state_init(rs, g, b, io.rho);
+  }
   Higdon<T> hig;
   higdon_init(hig, b, vel, (T)g.dt, g);
 
@@ -710,7 +882,9 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
     }
     // Boundary_set_free_surface_grid: no-op for surf_type = 0.
     // FD_scheme(u2 -> u3) (Propagator.f90:202).
-    if (d.fd_scheme == SW_FD_FORWARD) {
+    if (io.rho) {
+      stencil_rho(rs, b, g.twoD != 0, *u2, *u3, vel);
+    } else if (d.fd_scheme == SW_FD_FORWARD) {
       if (g.twoD) stencil2d_fwd(c, b, *u2, *u3, vel);
       else stencil3d_fwd(c, b, *u2, *u3, vel);
     } else {
@@ -725,16 +899,17 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
         const int k1 = g.twoD ? 1 : p.ic[2];
         if (d.injection == SW_INJ_SIMPLE) {
           // Injection_simple_noomp + Injection_source_simple_xyz
-          // (Injection.f90:63-104,561-591).
+          // (Injection.f90:63-104,561-591); v^2*rho with density.
           const T vv = vel(p.ic[0], p.ic[1], k1);
-          const T v2r = vv * vv;
+          const T v2r = io.rho ? (vv * vv) * rs.rho(p.ic[0], p.ic[1], k1) : vv * vv;
           (*u3)(p.ic[0], p.ic[1], k1) = (*u3)(p.ic[0], p.ic[1], k1) + v2r * tr;
           continue;
         }
         T v2r;
         if (d.injection == SW_INJ_SINC) {
+          // Injection_sinc (Injection.f90:170-190): v^2, times rho with density.
           const T vv = vel(p.ic[0], p.ic[1], k1);
-          v2r = vv * vv;
+          v2r = io.rho ? (vv * vv) * rs.rho(p.ic[0], p.ic[1], k1) : vv * vv;
         } else {
           v2r = g.twoD ? inv_d2 : inv_d3;   // Injection.f90:258-270
         }
@@ -1547,13 +1722,13 @@ void oracle_set_rigid(int on) { g_rigid = on != 0; }
 
 int oracle_propagate_f32(const sw_prop_desc *d, const sw_prop_io *io) {
   IO<float> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
-              io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2};
+              io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho};
   return propagate<float>(*d, o);
 }
 
 int oracle_propagate_f64(const sw_prop_desc *d, const or_prop_io64 *io) {
   IO<double> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
-               io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2};
+               io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho};
   return propagate<double>(*d, o);
 }
 
@@ -1664,6 +1839,23 @@ int oracle_stencil_f64(const sw_genpar *g, int adjoint, const double *vel,
     if (g->twoD) stencil2d_adj(c, b, a, o, v);
     else { t.init(b); stencil3d_adj(c, b, a, o, v, t); }
   }
+  std::memcpy(u3, o.v.data(), o.v.size() * sizeof(double));
+  return SW_OK;
+}
+
+int oracle_stencil_rho_f64(const sw_genpar *g, const double *vel, const double *rho,
+                           const double *u2, double *u3) {
+  int st = check_genpar(*g);
+  if (st) return st;
+  const Bounds b = make_bounds(*g);
+  F3<double> v, a, o;
+  v.init(b); a.init(b); o.init(b);
+  model_pad(vel, v, b, g->nz, g->nx, g->ny, g->twoD != 0);
+  std::memcpy(a.v.data(), u2, a.v.size() * sizeof(double));
+  std::memcpy(o.v.data(), u3, o.v.size() * sizeof(double));
+  RhoState<double> rs;
+  rho_state_init(rs, *g, b, rho);
+  stencil_rho(rs, b, g->twoD != 0, a, o, v);
   std::memcpy(u3, o.v.data(), o.v.size() * sizeof(double));
   return SW_OK;
 }

@@ -53,7 +53,8 @@ _dp = C.POINTER(C.c_double)
 class SwPropIO(C.Structure):
     _fields_ = [("vel", _fp), ("nsou", C.c_int), ("sou_coord", _fp), ("sou_trace", _fp),
                 ("nrec", C.c_int), ("rec_coord", _fp), ("rec_trace", _fp), ("wave", _fp),
-                ("image", _fp), ("illum", _fp), ("ref", _fp), ("final_u2", _fp)]
+                ("image", _fp), ("illum", _fp), ("ref", _fp), ("final_u2", _fp),
+                ("rho", _fp)]
 
 
 class SwFwiShot(C.Structure):
@@ -261,7 +262,8 @@ class Context:
 
     # -- propagator_acoustic ----------------------------------------------
     def propagate(self, desc: SwPropDesc, vel, sou_coord=None, sou_trace=None, rec_coord=None,
-                  rec_trace=None, wave=None, image=None, illum=None, ref=None, final_u2=None):
+                  rec_trace=None, wave=None, image=None, illum=None, ref=None, final_u2=None,
+                  rho=None):
         """sw_propagate; array arguments are modified in place like the reference."""
         io = SwPropIO()
         vel = _f32(vel)
@@ -281,6 +283,10 @@ class Context:
             keep.append(ref)
         io.ref = fptr(ref)
         io.final_u2 = fptr(final_u2)
+        if rho is not None:
+            rho = _f32(rho)
+            keep.append(rho)
+        io.rho = fptr(rho)
         self._check(self.lib.sw_propagate(self.h, C.byref(desc), C.byref(io)))
 
     # -- drivers -----------------------------------------------------------
