@@ -189,6 +189,11 @@ int sw_lsrtm(sw_ctx *ctx, const sw_genpar *g, const float *vel,
  * centred 2nd difference / dt^2. */
 int sw_born_wavelet(float *wavelet, int nt, float dt);
 
+/* readsou's withRho preprocessing (ReadSouVelRho.f90:328-343): in place,
+ * w'(t) = w(t + dt/2) by an lsinc-point sinc (staggered grid), edge taps
+ * dropped and the weights renormalised.  Host only. */
+int sw_rho_wavelet(float *wavelet, int nt, int lsinc);
+
 /* ---- Multi-shot RTM job (3DRTM.f90 per shot + compute_mig's stacking) ---
  * Shots of uneven aperture and record length are windowed out of one model
  * (extract_coord_source_receiver_patch + copy_window_vel_gath,

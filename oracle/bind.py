@@ -53,6 +53,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "oracle_lsrtm_f32": [g, _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp],
         "oracle_lsrtm_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp],
         "oracle_born_wavelet": [_fp, C.c_int, C.c_float],
+        "oracle_rho_wavelet": [_fp, C.c_int, C.c_int],
         "oracle_vel_check": [g, _fp, _fp, _fp],
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
         "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],

@@ -80,6 +80,7 @@ int oracle_lsrtm_f64(const sw_genpar *g, const double *vel,
                      const double *sou_coord, const double *wavelet, int nrec,
                      const double *rec_coord, const double *data,
                      double *image, double *illum);
+int oracle_rho_wavelet(float *w, int nt, int lsinc);
 int oracle_born_wavelet(float *wavelet, int nt, float dt);
 int oracle_vel_check(const sw_genpar *g, const float *vel, float *courant,
                      float *samplerate);

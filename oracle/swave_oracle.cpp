@@ -1778,6 +1778,22 @@ int oracle_lsrtm_f64(const sw_genpar *g, const double *vel, const double *sou_co
 }
 
 // readsou Born/LSRTM branch (ReadSouVelRho.f90:318-326).
+// readsou withRho branch (ReadSouVelRho.f90:328-343).
+int oracle_rho_wavelet(float *w, int nt, int lsinc) {
+  std::vector<float> sinc(lsinc), tr(w, w + nt);
+  mksinc<float>(sinc.data(), lsinc, 0.5f);
+  const int h = lsinc / 2;
+  for (int it = 1; it <= nt; ++it) {
+    float fscale = 1.f, fdum = 0.f;
+    for (int l = -h; l <= h; ++l) {
+      if (it + l >= 1 && it + l <= nt) fdum = fdum + sinc[h + l] * tr[it + l - 1];
+      else fscale = fscale - sinc[h + l];
+    }
+    w[it - 1] = fdum / fscale;
+  }
+  return SW_OK;
+}
+
 int oracle_born_wavelet(float *w, int nt, float dt) {
   if (nt < 1) return SW_BAD_PARAM;
   std::vector<float> tr(w, w + nt);

@@ -135,6 +135,7 @@ _SIGS = {
     "sw_ctx_get_stats": (C.c_int, [C.c_void_p, C.POINTER(SwStats)]),
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
     "sw_ctx_set_boundary": (C.c_int, [C.c_void_p, C.c_int]),
+    "sw_rho_wavelet": (C.c_int, [_fp, C.c_int, C.c_int]),
     "sw_shot_window": (C.c_int, [C.POINTER(SwGenpar), C.c_float, C.c_float, _fp, C.c_int, _fp,
                                  C.POINTER(SwWindow)]),
     "sw_window_extract": (C.c_int, [C.POINTER(SwGenpar), C.POINTER(SwWindow), _fp, _fp]),
@@ -570,6 +571,16 @@ def modeling_noalloc(g: SwGenpar, vel, sou_coord, wavelet, rec_coord) -> np.ndar
     if code != SW_OK:
         raise SwaveError(code, "sw_modeling_noalloc")
     return data
+
+
+def rho_wavelet(w, lsinc: int = 7) -> np.ndarray:
+    """readsou's half-sample shift of the wavelet for the density path."""
+    lib = load_library()
+    w = _f32(w).copy()
+    code = lib.sw_rho_wavelet(fptr(w), w.size, lsinc)
+    if code != SW_OK:
+        raise SwaveError(code, "sw_rho_wavelet")
+    return w
 
 
 def born_wavelet(w, dt: float) -> np.ndarray:

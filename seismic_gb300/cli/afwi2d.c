@@ -50,6 +50,7 @@ int main(int argc, char **argv) {
   if (!sep_exist("vel")) cli_fail("need velocity file");
   cli_par p;
   cli_read_params(&p);
+  if (p.withRho) cli_fail("Rho not implemented in this version");
   const int mod = !strcmp(p.task, "MOD") || !strcmp(p.task, "mod");
   const int mig = !strcmp(p.task, "MIG") || !strcmp(p.task, "mig");
   if (!mod && !mig)

@@ -16,6 +16,7 @@ int main(int argc, char **argv) {
   if (!sep_exist("data")) cli_fail("need dat file for output");
   cli_par p;
   cli_read_params(&p);
+  if (p.withRho) cli_fail("withRho=1: Born modelling has no variable-density path in swave");
   p.Born = 1;
   float *wavelet = cli_read_source(&p);
   int ntr = 0;

@@ -6,7 +6,9 @@
  * (mod_copy_image_to_disk); image= receives the image, then the
  * illumination (n3 = 2 in 2D, n4 = 2 in 3D).  Snapshots stay in device
  * memory: maxsize= and the wave_fwd disk path of the reference are not
- * used. */
+ * used.  withRho=1 with rho= runs RTM_to_memory's variable-density branch:
+ * the forward-grid density operator in both passes
+ * (to_disk_to_memory_RTM.f90:388-398,455-465). */
 #include <stdlib.h>
 #include <string.h>
 
@@ -23,7 +25,9 @@ int main(int argc, char **argv) {
   float *traces = cli_read_traces(p.g.nt, &ntr);
   float sou[3];
   float *rec = cli_read_coords(ntr, sou);
+  if (p.withRho && p.LSRTM) cli_fail("withRho=1 with LSRTM=1 is not built in swave");
   float *vel = cli_read_model(&p, "vel");
+  float *rho = p.withRho ? cli_read_model(&p, "rho") : NULL;
   if (!sep_exist("image")) cli_fail("need image file for output");
   sw_window w;
   sw_genpar gw;
@@ -40,7 +44,46 @@ int main(int argc, char **argv) {
   if (!vsmall || !ims || !ils || !im || !il) cli_fail("out of host memory");
   if (sw_window_extract(&p.g, &w, vel, vsmall) != SW_OK) cli_fail("window extract");
   sw_ctx *ctx = cli_context();
-  if (p.LSRTM)
+  if (rho) {
+    float *rs = (float *)malloc(nw * 4);
+    const int ntsnap = gw.nt / gw.snapi;
+    float *wave = (float *)malloc(nw * (size_t)(ntsnap > 0 ? ntsnap : 1) * 4);
+    if (!rs || !wave) cli_fail("out of host memory");
+    if (sw_window_extract(&p.g, &w, rho, rs) != SW_OK) cli_fail("window extract");
+    sw_prop_desc d;
+    memset(&d, 0, sizeof(d));
+    d.g = gw;
+    d.tmin = 1;
+    d.tmax = gw.nt;
+    d.tstep = 1;
+    d.fd_scheme = SW_FD_FORWARD;
+    d.injection = SW_INJ_SINC;
+    d.extract_wave = 1;
+    sw_prop_io io;
+    memset(&io, 0, sizeof(io));
+    io.vel = vsmall;
+    io.rho = rs;
+    io.nsou = 1;
+    io.sou_coord = sou;
+    io.sou_trace = wavelet;
+    io.wave = wave;
+    cli_check(ctx, sw_propagate(ctx, &d, &io), "forward propagation (withRho)");
+    d.tmin = gw.nt;
+    d.tmax = 1;
+    d.tstep = -1;
+    d.extract_wave = 0;
+    d.imaging = SW_IMG_RTM;
+    memset(ims, 0, nw * 4);
+    memset(ils, 0, nw * 4);
+    io.nsou = ntr;
+    io.sou_coord = rec;
+    io.sou_trace = traces;
+    io.image = ims;
+    io.illum = ils;
+    cli_check(ctx, sw_propagate(ctx, &d, &io), "backward propagation (withRho)");
+    free(wave);
+    free(rs);
+  } else if (p.LSRTM)
     cli_check(ctx, sw_lsrtm(ctx, &gw, vsmall, sou, wavelet, ntr, rec, traces, ims, ils),
               "sw_lsrtm");
   else
@@ -54,6 +97,7 @@ int main(int argc, char **argv) {
   free(ils);
   free(im);
   free(il);
+  free(rho);
   free(vel);
   free(rec);
   free(traces);

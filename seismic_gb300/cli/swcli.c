@@ -60,7 +60,6 @@ void cli_read_params(cli_par *p) {
   sep_par_str("Task", p->task, sizeof(p->task));
   if (p->LSRTM) par_bool("CHEAPLSRTM", &p->CHEAPLSRTM, 0);
   par_bool("write_forward_wavefield", &p->WriteFwdWvfld, 0);
-  if (p->withRho) cli_fail("withRho=1: the variable-density path is not built in swave");
   if (g->rec_type || g->shot_type || g->surf_type)
     cli_fail("rec_type/shot_type/surf_type > 0: mirror and free-surface modes are not built in "
              "swave");
@@ -88,6 +87,7 @@ float *cli_read_source(cli_par *p) {
   p->g.nt = nt;
   p->g.dt = dt;
   if (p->Born || p->LSRTM) sw_born_wavelet(w, nt, dt);
+  if (p->withRho) sw_rho_wavelet(w, nt, p->g.lsinc);
   return w;
 }
 

@@ -20,13 +20,15 @@ void cli_fail(const char *fmt, ...);
 /* read_3D_params (libs/libwave/ReadParam.f90:15-84): fmax 30, ntaper 20,
  * snapi 4, lsinc 7, num_threads 4, maxsize 16, rec/shot/surf_type 0, twoD,
  * withRho, LSRTM, Born false, verb true, Task MOD.  Options of the
- * reference that this build does not implement (withRho, non-zero
- * rec/shot/surf_type, CHEAPLSRTM) stop the program with an error. */
+ * reference that this build does not implement (non-zero
+ * rec/shot/surf_type, CHEAPLSRTM) stop the program with an error; programs
+ * without a variable-density path reject withRho themselves. */
 void cli_read_params(cli_par *p);
 
 /* readsou (ReadSouVelRho.f90:298-344): the wavelet from the "in" dataset
  * (n1 = nt, d1 = dt, o1 = t0); with Born or LSRTM it is replaced by its
- * centred second difference / dt^2.  Returns the nt samples (malloc). */
+ * centred second difference / dt^2, with withRho it is then moved half a
+ * sample (sw_rho_wavelet).  Returns the nt samples (malloc). */
 float *cli_read_source(cli_par *p);
 
 /* readtraces (ReadSouVelRho.f90:59-88): n2 traces of n1 = nt samples from

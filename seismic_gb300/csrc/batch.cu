@@ -75,7 +75,34 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
   const long long L = g.ld1;
   const Coefs &c = S.c;
   float sv;
-  if (TWO_D && S.adj2d) {
+  if (S.rho_on) {
+    // Divergence of the staggered gradient times v^2*rho
+    // (FDderivatives.f90:371-380 3D, 642-655 2D).
+    const Coefs &r = S.cr;
+    const float *__restrict__ sz = S.sz;
+    const float *__restrict__ sx = S.sx;
+    float tz = r.c1z * (sz[p] - sz[p - 1]);
+    tz = tz + r.c2z * (sz[p + 1] - sz[p - 2]);
+    tz = tz + r.c3z * (sz[p + 2] - sz[p - 3]);
+    tz = tz + r.c4z * (sz[p + 3] - sz[p - 4]);
+    float tx = r.c1x * (sx[p] - sx[p - L]);
+    tx = tx + r.c2x * (sx[p + L] - sx[p - 2 * L]);
+    tx = tx + r.c3x * (sx[p + 2 * L] - sx[p - 3 * L]);
+    tx = tx + r.c4x * (sx[p + 3 * L] - sx[p - 4 * L]);
+    const float vv = S.vel[p];
+    const float vr = (vv * vv) * S.rho[p];
+    if (TWO_D) {
+      sv = vr * (tx + tz);
+    } else {
+      const long long P = g.plane();
+      const float *__restrict__ sy = S.sy;
+      float ty = r.c1y * (sy[p] - sy[p - P]);
+      ty = ty + r.c2y * (sy[p + P] - sy[p - 2 * P]);
+      ty = ty + r.c3y * (sy[p + 2 * P] - sy[p - 3 * P]);
+      ty = ty + r.c4y * (sy[p + 3 * P] - sy[p - 4 * P]);
+      sv = vr * ((tx + ty) + tz);
+    }
+  } else if (TWO_D && S.adj2d) {
     // FD_2nd_2D_derivatives_scalar_adjoint_grid (FDderivatives.f90:847-891):
     // vel indices clamped to the compute domain.
     const float *__restrict__ v = S.vel;
@@ -198,6 +225,72 @@ __global__ void k_bv2u(BatchTables t, int s_off) {
        q += (long long)nb * blockDim.x) {
     const float v = S.vel[q];
     S.v2u[q] = (v * v) * u2[q];
+  }
+}
+
+// Staggered gradient of u2 scaled by delp = 1/rho2 for the variable-density
+// operator (FDderivatives.f90:277-336 3D, 601-640 2D): the 8th-order
+// difference at half cells inside the compute domain, a first-order
+// difference scaled by delp of the adjacent face in the three padding cells
+// beyond each face.  Only the cells the divergence reads are written; the
+// fourth padding cell, which the reference reads but never writes, stays at
+// its initial zero.
+__global__ void k_brho_grad(BatchTables t, int s_off) {
+  const int b = find_shot(t.v2u_blocks, t.nshots, blockIdx.x);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (!S.rho_on || s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const float *__restrict__ u = S.f[(s + 3) % 5];
+  const float *__restrict__ dp = S.delp;
+  const Coefs &c = S.cr;
+  const long long n = (long long)g.n1p * g.n2p * g.n3p;
+  const long long L = g.ld1, P = g.plane();
+  const int nb = t.v2u_blocks[b + 1] - t.v2u_blocks[b];
+  for (long long q = (long long)(blockIdx.x - t.v2u_blocks[b]) * blockDim.x + threadIdx.x; q < n;
+       q += (long long)nb * blockDim.x) {
+    const int i = g.lo1 + (int)(q % g.n1p);
+    const long long rr = q / g.n1p;
+    const int j = g.lo2 + (int)(rr % g.n2p), k = g.lo3 + (int)(rr / g.n2p);
+    const bool iin = i >= g.nmin1 && i <= g.nmax1, jin = j >= g.nmin2 && j <= g.nmax2;
+    const bool kin = g.twoD || (k >= g.nmin3 && k <= g.nmax3);
+    const long long p = g.idx(i, j, k);
+    if (jin && kin) {
+      if (iin) {
+        float a = c.c1z * (u[p + 1] - u[p]);
+        a = a + c.c2z * (u[p + 2] - u[p - 1]);
+        a = a + c.c3z * (u[p + 3] - u[p - 2]);
+        a = a + c.c4z * (u[p + 4] - u[p - 3]);
+        S.sz[p] = a * dp[p];
+      } else if (i >= g.nmin1 - 3 && i <= g.nmax1 + 3) {
+        const int ie = i < g.nmin1 ? g.nmin1 : g.nmax1;
+        S.sz[p] = (S.dzi * (u[p + 1] - u[p])) * dp[g.idx(ie, j, k)];
+      }
+    }
+    if (iin && kin) {
+      if (jin) {
+        float a = c.c1x * (u[p + L] - u[p]);
+        a = a + c.c2x * (u[p + 2 * L] - u[p - L]);
+        a = a + c.c3x * (u[p + 3 * L] - u[p - 2 * L]);
+        a = a + c.c4x * (u[p + 4 * L] - u[p - 3 * L]);
+        S.sx[p] = a * dp[p];
+      } else if (j >= g.nmin2 - 3 && j <= g.nmax2 + 3) {
+        const int je = j < g.nmin2 ? g.nmin2 : g.nmax2;
+        S.sx[p] = (S.dxi * (u[p + L] - u[p])) * dp[g.idx(i, je, k)];
+      }
+    }
+    if (!g.twoD && iin && jin) {
+      if (kin) {
+        float a = c.c1y * (u[p + P] - u[p]);
+        a = a + c.c2y * (u[p + 2 * P] - u[p - P]);
+        a = a + c.c3y * (u[p + 3 * P] - u[p - 2 * P]);
+        a = a + c.c4y * (u[p + 4 * P] - u[p - 3 * P]);
+        S.sy[p] = a * dp[p];
+      } else if (k >= g.nmin3 - 3 && k <= g.nmax3 + 3) {
+        const int ke = k < g.nmin3 ? g.nmin3 : g.nmax3;
+        S.sy[p] = (S.dyi * (u[p + P] - u[p])) * dp[g.idx(i, j, ke)];
+      }
+    }
   }
 }
 
@@ -578,6 +671,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   }
   if (has_adj3d && n_v2u > 0 && !tile.stream3d) {
     k_bv2u<<<n_v2u, 256, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (tile.has_rho && n_v2u > 0) {
+    k_brho_grad<<<n_v2u, 256, 0, s>>>(t, s_off);
     ++nl;
   }
   dim3 bs(32, 8, 1);

@@ -47,6 +47,13 @@ struct ShotDev {
   const float *taperx, *tapery;
   float k12, div11, dt2snap;
   long long npts;         // compute-domain points
+  // Variable density (withRho): padded rho, delp = 1/rho2 and the staggered
+  // gradient arrays (sy in 3D), with the rho-operator coefficients.
+  int rho_on;
+  const float *rho, *delp;
+  float *sz, *sx, *sy;
+  Coefs cr;
+  float dzi, dxi, dyi;
 };
 
 // Compact per-shot view used by the pipelined 2D kernel; the kernel keeps the
@@ -148,6 +155,7 @@ struct StepTile {
   int fused_edges = 0; // 2D: one launch for the z and x Higdon edges (set by the runner)
   int n_edge = 0;      // threads of that launch
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
+  int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
 };
 
 // Threads of the fused 2D edge kernel for one shot: four corner warps and

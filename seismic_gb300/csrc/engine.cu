@@ -200,6 +200,17 @@ Coefs make_coefs(const sw_genpar &g) {
   return c;
 }
 
+Coefs make_rho_coefs(const sw_genpar &g) {
+  const float c0 = 0.f, c1 = 1225.f / 1024.f, c2 = -1225.f / (1024.f * 15.f),
+              c3 = 1225.f / (1024.f * 125.f), c4 = -1225.f / (1024.f * 1715.f);
+  const float dxi = 1.f / g.dx, dyi = 1.f / g.dy, dzi = 1.f / g.dz;
+  Coefs c;
+  c.c0x = c0 * dxi; c.c1x = c1 * dxi; c.c2x = c2 * dxi; c.c3x = c3 * dxi; c.c4x = c4 * dxi;
+  c.c0y = c0 * dyi; c.c1y = c1 * dyi; c.c2y = c2 * dyi; c.c3y = c3 * dyi; c.c4y = c4 * dyi;
+  c.c0z = c0 * dzi; c.c1z = c1 * dzi; c.c2z = c2 * dzi; c.c3z = c3 * dzi; c.c4z = c4 * dzi;
+  return c;
+}
+
 // mksinc (Interpolate.f90:15-42), evaluated once per trace.
 void mksinc(float *sinc, int lsinc, float shift) {
   const float pi = 3.141592654f;
@@ -267,7 +278,8 @@ static inline float host_vel(const sw_genpar &g, const float *vp, int i, int j, 
 // Builds the injection plan: a box covering every contribution and, per box
 // cell, the contributions in source order.
 int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
-                    const float *sou_coord, const float *vel_phys, InjPlan &plan) {
+                    const float *sou_coord, const float *vel_phys, InjPlan &plan,
+                    const float *rho_phys) {
   plan.on = 0;
   if (mode == SW_INJ_NONE || nsou <= 0) return SW_OK;
   std::vector<int> ic;
@@ -304,8 +316,10 @@ int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int 
     if (mode == SW_INJ_LSRTM_SINC) {
       v2r = g.twoD ? inv_d2 : inv_d3;
     } else {
+      // Injection_sinc / Injection_simple: v**2, times rho with density
+      // (Injection.f90:170-190).
       const float vv = host_vel(g, vel_phys, i0, j0, k0);
-      v2r = vv * vv;
+      v2r = rho_phys ? (vv * vv) * host_vel(g, rho_phys, i0, j0, k0) : vv * vv;
     }
     auto cell = [&](int i, int j, int k) {
       return (int)((i - bi0) + (long long)(bi1 - bi0 + 1) * ((j - bj0) + (long long)(bj1 - bj0 + 1) * (k - bk0)));
@@ -402,6 +416,27 @@ int upload_velocity(sw_ctx *c, const sw_genpar &g, const float *vel, const char 
   return SW_OK;
 }
 
+int prepare_rho(sw_ctx *c, const sw_genpar &g, const float *rho_host, const char *slot,
+                const float **rho_pad, const float **delp) {
+  int st = SW_OK;
+  float *pad = nullptr;
+  if ((st = upload_velocity(c, g, rho_host, slot, &pad))) return st;
+  const Geom G = make_geom(g);
+  const size_t nf = (size_t)G.total();
+  float *a = (float *)dbuf(c, std::string(slot) + "_delp", nf * sizeof(float), &st);
+  float *b = (float *)dbuf(c, std::string(slot) + "_tmp", nf * sizeof(float), &st);
+  if (!a || !b) return st;
+  float sinc[9];
+  mksinc(sinc, 9, 0.5f);
+  int nl = 0;
+  cudaError_t e = launch_rho_delp(G, pad, a, b, sinc, c->stream, &nl);
+  if (e != cudaSuccess) return cuda_fail(c, e, "rho interpolation");
+  c->stats.launches_total += nl;
+  *rho_pad = pad;
+  *delp = a;
+  return SW_OK;
+}
+
 int upload(sw_ctx *c, const char *slot, const void *h, size_t bytes, void **d) {
   int st = SW_OK;
   void *p = dbuf(c, slot, bytes, &st);
@@ -461,6 +496,14 @@ int sw_propagate(sw_ctx *c, const sw_prop_desc *d, const sw_prop_io *io) {
   DevIO dio;
   if ((st = upload_velocity(c, g, io->vel, "vel", &dio.vel_pad))) return st;
   dio.vel_phys_host = io->vel;
+  if (io->rho) {
+    // The variable-density drivers use the forward-grid operator in both
+    // directions (to_disk_to_memory_RTM.f90:388-398,455-465).
+    if (d->fd_scheme != SW_FD_FORWARD)
+      return fail(c, SW_UNSUPPORTED, "the variable-density operator has no adjoint-grid form");
+    if ((st = prepare_rho(c, g, io->rho, "rho", &dio.rho_pad, &dio.delp))) return st;
+    dio.rho_phys_host = io->rho;
+  }
   dio.nsou = d->injection != SW_INJ_NONE ? io->nsou : 0;
   dio.sou_coord = io->sou_coord;
   void *p = nullptr;
@@ -640,6 +683,25 @@ int sw_born(sw_ctx *c, const sw_genpar *g, const float *vel, const float *ref,
     return SW_BAD_PARAM;
   return two_pass(c, *g, vel, ref, sou_coord, wavelet, nrec, rec_coord, nullptr, data, nullptr,
                   nullptr, 2);
+}
+
+int sw_rho_wavelet(float *w, int nt, int lsinc) {
+  if (!w || nt < 1 || lsinc < 3 || (lsinc % 2) == 0) return SW_BAD_PARAM;
+  // readsou, withRho branch (ReadSouVelRho.f90:328-343): w'(t) = w(t + dt/2)
+  // by an lsinc-point sinc; taps outside the trace are dropped and the
+  // remaining weights renormalised.
+  std::vector<float> sinc(lsinc), tr(w, w + nt);
+  mksinc(sinc.data(), lsinc, 0.5f);
+  const int h = lsinc / 2;
+  for (int it = 1; it <= nt; ++it) {
+    float fscale = 1.f, fdum = 0.f;
+    for (int l = -h; l <= h; ++l) {
+      if (it + l >= 1 && it + l <= nt) fdum = fdum + sinc[h + l] * tr[it + l - 1];
+      else fscale = fscale - sinc[h + l];
+    }
+    w[it - 1] = fdum / fscale;
+  }
+  return SW_OK;
 }
 
 int sw_born_wavelet(float *w, int nt, float dt) {

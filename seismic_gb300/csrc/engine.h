@@ -73,6 +73,11 @@ struct DevIO {
   const float *init_state = nullptr;
   float *save_state = nullptr;
   int tcnt = 0;
+  // Variable density: padded rho, delp = 1/rho2 (device) and the unpadded
+  // rho on the host (injection weights v^2*rho).
+  const float *rho_pad = nullptr;
+  const float *delp = nullptr;
+  const float *rho_phys_host = nullptr;
 };
 
 // A shot's model window (ModelSpace%oxw, nxw, ...).
@@ -104,10 +109,18 @@ void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st);
 int check_genpar(sw_ctx *c, const sw_genpar &g);
 Geom make_geom(const sw_genpar &g);
 Coefs make_coefs(const sw_genpar &g);
+// FD_acoustic_rho_init_coefs (FDcoefs.f90:12-23), coefpower = 1.
+Coefs make_rho_coefs(const sw_genpar &g);
+// Pads rho on the device like the velocity and forms delp = 1/rho2 with the
+// half-cell sinc interpolation of Interpolate.f90:44-130 (slots "<slot>" and
+// "<slot>_delp" of the context arena).
+int prepare_rho(sw_ctx *c, const sw_genpar &g, const float *rho_host, const char *slot,
+                const float **rho_pad, const float **delp);
 void mksinc(float *sinc, int lsinc, float shift);
 void compute_taper(int nxw, int nyw, std::vector<float> &tx, std::vector<float> &ty);
 int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
-                    const float *sou_coord, const float *vel_phys, InjPlan &plan);
+                    const float *sou_coord, const float *vel_phys, InjPlan &plan,
+                    const float *rho_phys = nullptr);
 int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nrec,
                      const float *rec_coord, ExtPlan &plan);
 int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt);

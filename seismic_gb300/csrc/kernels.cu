@@ -159,6 +159,71 @@ cudaError_t launch_pad_velocity(const Geom &g, const float *vel_phys, float *vel
   return cudaGetLastError();
 }
 
+// One pass of Interpolate (Interpolate.f90:63-126) along `axis` (0 z, 1 x,
+// 2 y): every line of the padded array is filtered by the 9-point half-cell
+// sinc, its end values extended past both ends; one thread per line, taps
+// added in order from -4 to +4.  recip stores 1/f (delp = 1/rho2,
+// FDderivatives.f90:393,581) instead of f.
+struct Sinc9 {
+  float s[9];
+};
+
+__global__ void k_sinc9_lines(Geom g, int axis, Sinc9 w, const float *__restrict__ src,
+                              float *__restrict__ dst, int recip) {
+  const long long nl = axis == 0 ? (long long)g.n2p * g.n3p
+                                 : axis == 1 ? (long long)g.n1p * g.n3p
+                                             : (long long)g.n1p * g.n2p;
+  for (long long L = blockIdx.x * (long long)blockDim.x + threadIdx.x; L < nl;
+       L += (long long)gridDim.x * blockDim.x) {
+    long long base, stride;
+    int len;
+    if (axis == 0) {
+      base = g.idx(g.lo1, g.lo2 + (int)(L % g.n2p), g.lo3 + (int)(L / g.n2p));
+      len = g.n1p;
+      stride = 1;
+    } else if (axis == 1) {
+      base = g.idx(g.lo1 + (int)(L % g.n1p), g.lo2, g.lo3 + (int)(L / g.n1p));
+      len = g.n2p;
+      stride = g.ld1;
+    } else {
+      base = g.idx(g.lo1 + (int)(L % g.n1p), g.lo2 + (int)(L / g.n1p), g.lo3);
+      len = g.n3p;
+      stride = g.plane();
+    }
+    for (int q = 0; q < len; ++q) {
+      float f = 0.f;
+#pragma unroll
+      for (int l = -4; l <= 4; ++l) {
+        const int qq = min(max(q + l, 0), len - 1);
+        f = f + w.s[4 + l] * src[base + (long long)qq * stride];
+      }
+      dst[base + (long long)q * stride] = recip ? 1.f / f : f;
+    }
+  }
+}
+
+cudaError_t launch_rho_delp(const Geom &g, const float *rho_pad, float *delp, float *tmp,
+                            const float *sinc9, cudaStream_t s, int *nlaunch) {
+  Sinc9 w;
+  for (int q = 0; q < 9; ++q) w.s[q] = sinc9[q];
+  auto go = [&](int axis, const float *a, float *b, int recip) {
+    const long long nl = axis == 0 ? (long long)g.n2p * g.n3p
+                                   : axis == 1 ? (long long)g.n1p * g.n3p
+                                               : (long long)g.n1p * g.n2p;
+    k_sinc9_lines<<<nblocks(nl, 128), 128, 0, s>>>(g, axis, w, a, b, recip);
+    ++*nlaunch;
+  };
+  if (g.n3p > 1) {
+    go(0, rho_pad, delp, 0);
+    go(1, delp, tmp, 0);
+    go(2, tmp, delp, 1);
+  } else {
+    go(0, rho_pad, tmp, 0);
+    go(1, tmp, delp, 1);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
                                  float dyi, float dzi, float *gz, float *gx, float *gy,
                                  cudaStream_t s) {

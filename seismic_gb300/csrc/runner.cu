@@ -93,6 +93,15 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // and packs tile coordinates into 12 bits each; larger batches, grids
   // beyond that or domains below 16 cells use the streaming kernel.
   StepTile tile = opt.tile;
+  // The variable-density operator runs on the point-tile step kernel after a
+  // gradient pass (k_brho_grad).
+  tile.has_rho = 0;
+  for (int b = 0; b < nb; ++b)
+    if (shots[b].io.rho_pad) tile.has_rho = 1;
+  if (tile.has_rho) {
+    tile.stream2d = 0;
+    tile.stream3d = 0;
+  }
   if (tile.stream2d == 2 || tile.stream2d == 3) {
     bool fits = nb <= T2_MAX_SHOTS;
     for (int b = 0; b < nb && fits; ++b) {
@@ -131,8 +140,10 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     G[b] = make_geom(d.g);
     has_3d = has_3d || !d.g.twoD;
     has_adj3d = has_adj3d || (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT);
+    if (io.rho_pad && d.fd_scheme != SW_FD_FORWARD)
+      return fail(c, SW_UNSUPPORTED, "the variable-density operator has no adjoint-grid form");
     if ((st = build_injection(c, d.g, G[b], d.injection, io.nsou, io.sou_coord, io.vel_phys_host,
-                              inj[b])))
+                              inj[b], io.rho_pad ? io.rho_phys_host : nullptr)))
       return st;
     if ((st = build_extraction(c, d.g, G[b], d.extraction, io.nrec, io.rec_coord, ext[b])))
       return st;
@@ -143,6 +154,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                     n3 = G[b].nmax3 - G[b].nmin3 + 1;
     bytes += 5 * rup(fb);
     if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT && !tile.stream3d) bytes += rup(fb);
+    if (io.rho_pad) bytes += (d.g.twoD ? 2 : 3) * rup(fb);
     bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
     bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry)) +
              rup(inj[b].ent.size() * sizeof(float));
@@ -199,6 +211,24 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       SW_CK(cudaMemsetAsync(S.v2u, 0, nf * sizeof(float), s));
     }
     S.vel = io.vel_pad;
+    if (io.rho_pad) {
+      if (!io.delp || !io.rho_phys_host) return fail(c, SW_BAD_PARAM, "density arrays missing");
+      S.rho_on = 1;
+      S.rho = io.rho_pad;
+      S.delp = io.delp;
+      S.cr = make_rho_coefs(g);
+      S.dzi = 1.f / g.dz;
+      S.dxi = 1.f / g.dx;
+      S.dyi = 1.f / g.dy;
+      S.sz = carve<float>(cur, nf);
+      S.sx = carve<float>(cur, nf);
+      SW_CK(cudaMemsetAsync(S.sz, 0, nf * sizeof(float), s));
+      SW_CK(cudaMemsetAsync(S.sx, 0, nf * sizeof(float), s));
+      if (!g.twoD) {
+        S.sy = carve<float>(cur, nf);
+        SW_CK(cudaMemsetAsync(S.sy, 0, nf * sizeof(float), s));
+      }
+    }
     const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
                     n3 = G[b].nmax3 - G[b].nmin3 + 1;
     float *gz = carve<float>(cur, 16 * n2 * n3), *gx = carve<float>(cur, 16 * n1 * n3),
@@ -282,7 +312,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     // a few source entries are formed in the tile.
     term[b + 1] = term[b] + (t2 && inj[b].on && inj[b].ent.size() >= kTermKernelMin
                                  ? (int)inj[b].ent.size() : 0);
-    v2b[b + 1] = v2b[b] + ((S.adj3d && !tile.stream3d)
+    v2b[b + 1] = v2b[b] + (((S.adj3d && !tile.stream3d) || S.rho_on)
                                ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256)
                                : 0);
   }

@@ -54,6 +54,10 @@ cudaError_t launch_pad_velocity(const Geom &g, const float *vel_phys, float *vel
 cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
                                  float dyi, float dzi, float *gz, float *gx, float *gy,
                                  cudaStream_t s);
+// delp = 1/rho2 from the padded rho (Interpolate.f90:44-130); tmp is a
+// scratch array of the same size; sinc9 = mksinc(9, 0.5).
+cudaError_t launch_rho_delp(const Geom &g, const float *rho_pad, float *delp, float *tmp,
+                            const float *sinc9, cudaStream_t s, int *nlaunch);
 
 // FWI helpers (kernels.cu).
 cudaError_t launch_window_vel(int nz, int nx, int ny, float ox, float oy, float dx, float dy,

@@ -91,3 +91,19 @@ def test_window_helpers_match_the_oracle_job_windowing(lib):
     expect = np.zeros(50, np.float32)
     np.add.at(expect, inside, 1.0)
     np.testing.assert_array_equal(acc[:, 0], expect)
+
+
+def test_rho_wavelet_matches_oracle_and_shifts_half_a_sample(lib, oracle):
+    """sw_rho_wavelet (readsou withRho, ReadSouVelRho.f90:328-343): the
+    same floats as the oracle; the result samples the wavelet half a step
+    later, w'(t) = w(t + dt/2), so its energy centre moves half a sample
+    earlier."""
+    from seismic_gb300 import synth
+    w = synth.ricker(15.0, 1e-3, 400).astype(np.float32)
+    a = sw.rho_wavelet(w, 7)
+    b = w.copy()
+    oracle.load().oracle_rho_wavelet(b.ctypes.data_as(C.POINTER(C.c_float)), b.size, 7)
+    np.testing.assert_array_equal(a, b)
+    t = np.arange(400)
+    peak = lambda x: np.sum(t * x ** 2) / np.sum(x ** 2)
+    assert abs((peak(a) - peak(w)) + 0.5) < 0.02

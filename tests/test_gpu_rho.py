@@ -1,0 +1,113 @@
+"""The variable-density path on the GPU (withRho: the staggered
+FD_{2D,3D}_derivatives_acoustic_forward_grid operator, v^2*rho injection)
+against the oracle, bit for bit, through sw_propagate and the SEP modelling
+program."""
+import subprocess
+
+import numpy as np
+import pytest
+
+import seismic_gb300 as sw
+from seismic_gb300 import sep
+from tests.cases import case2d, case3d
+
+pytestmark = pytest.mark.gpu
+
+
+def _rho(shape, seed):
+    rng = np.random.default_rng(seed)
+    z = np.arange(shape[-1])[None, :] * 10.0
+    base = 1.8 + 0.0008 * z
+    return np.ascontiguousarray(base + 0.15 * rng.random(shape), np.float32)
+
+
+def _desc(g, fwd=True, **kw):
+    d = sw.SwPropDesc()
+    d.g = g
+    d.tmin, d.tmax, d.tstep = (1, g.nt, 1) if fwd else (g.nt, 1, -1)
+    d.fd_scheme = sw.FD_FORWARD
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("three_d", [False, True])
+def test_rho_modeling_bitexact(ctx, oracle, three_d):
+    g, vel, sou, rec, w = case3d(nt=100) if three_d else case2d(nt=300)
+    rho = _rho(vel.shape, 3)
+    w = sw.rho_wavelet(w, g.lsinc)
+    d = _desc(g, injection=sw.INJ_SINC, extraction=sw.EXT_SINC)
+    a = np.zeros((rec.shape[0], g.nt), np.float32)
+    b = np.zeros_like(a)
+    ctx.propagate(d, vel, sou, w, rec, a, rho=rho)
+    oracle.propagate(d, vel, sou, w, rec, b, rho=rho)
+    assert np.abs(b).max() > 0
+    np.testing.assert_array_equal(a, b)
+    # The density matters: the same run without it differs.
+    c = np.zeros_like(a)
+    ctx.propagate(d, vel, sou, w, rec, c)
+    assert np.abs(c - a).max() > 1e-3 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("three_d", [False, True])
+def test_rho_rtm_bitexact(ctx, oracle, three_d):
+    """RTM_to_memory's withRho branch: forward with snapshots and the
+    backward pass both on the forward-grid density operator."""
+    g, vel, sou, rec, w = case3d(nt=80) if three_d else case2d(nt=200)
+    rho = _rho(vel.shape, 4)
+    data = (np.random.default_rng(5).standard_normal((rec.shape[0], g.nt)) * 1e-2).astype(np.float32)
+    n = vel.size
+    out = {}
+    for name, api in (("gpu", ctx), ("oracle", oracle)):
+        wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+        api.propagate(_desc(g, injection=sw.INJ_SINC, extract_wave=1), vel, sou, w, wave=wave,
+                      rho=rho)
+        im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        api.propagate(_desc(g, False, injection=sw.INJ_SINC, imaging=sw.IMG_RTM), vel, rec, data,
+                      wave=wave, image=im, illum=il, rho=rho)
+        out[name] = (im, il)
+    assert np.abs(out["oracle"][0]).max() > 0
+    np.testing.assert_array_equal(out["gpu"][0], out["oracle"][0])
+    np.testing.assert_array_equal(out["gpu"][1], out["oracle"][1])
+
+
+def test_rho_rejects_the_adjoint_grid(ctx):
+    g, vel, sou, rec, w = case2d(nt=50)
+    d = _desc(g, injection=sw.INJ_SINC)
+    d.fd_scheme = sw.FD_ADJOINT
+    with pytest.raises(sw.SwaveError):
+        ctx.propagate(d, vel, sou, w, rho=np.ones_like(vel))
+
+
+def test_modeling_program_with_density(oracle, tmp_path):
+    from seismic_gb300.build import build_cli
+    built = build_cli()
+    g, vel, sou, rec, w = case2d(nz=40, nx=60, nt=200)
+    rho = _rho(vel.shape, 6)
+    ax = {"d1": 10.0, "d2": 10.0, "o1": 0.0, "o2": 0.0}
+    sep.write(str(tmp_path / "vel.H"), vel, ax)
+    sep.write(str(tmp_path / "rho.H"), rho, ax)
+    sep.write(str(tmp_path / "w.H"), w, {"d1": g.dt, "o1": 0.0})
+    ntr = rec.shape[0]
+    keys = np.zeros((ntr, 6), np.float32)
+    keys[:, 0], keys[:, 1], keys[:, 4], keys[:, 5] = sou[1], rec[:, 1], sou[0], rec[:, 0]
+    sep.write(str(tmp_path / "k.H"), keys)
+    sep.write(str(tmp_path / "t.H"), np.zeros((ntr, g.nt), np.float32), {"d1": g.dt})
+    # aperture 1000 m: the window is the whole model (clamped extraction of
+    # the columns beyond it repeats the edge columns).
+    params = dict(stdin=tmp_path / "w.H", vel=tmp_path / "vel.H", rho=tmp_path / "rho.H",
+                  withRho=1, traces=tmp_path / "t.H", coordfile=tmp_path / "k.H", keysx=1,
+                  keygx=2, keysy=3, keygy=4, keyselev=5, keygelev=6, aperture_x=0, twoD=1,
+                  ntaper=g.ntaper, snapi=g.snapi, data=tmp_path / "d.H")
+    r = subprocess.run(sep.command(built["Acoustic_modeling_sep.x"], **params),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    data, _ = sep.read(str(tmp_path / "d.H"))
+    wv, gw = sw.shot_window(g, 0.0, 0.0, sou, rec)
+    vs = sw.window_extract(g, wv, vel)
+    rs = sw.window_extract(g, wv, rho)
+    d = _desc(gw, injection=sw.INJ_SINC, extraction=sw.EXT_SINC)
+    ref = np.zeros((ntr, g.nt), np.float32)
+    oracle.propagate(d, vs, sou, sw.rho_wavelet(w, g.lsinc), rec, ref, rho=rs)
+    assert np.abs(ref).max() > 0
+    np.testing.assert_array_equal(data, ref)

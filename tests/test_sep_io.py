@@ -176,7 +176,9 @@ def test_programs_reject_inconsistent_or_unbuilt_options(built, tmp_path):
     assert rc == 1 and "nt traces and sources are different" in err
     p = _write_shot(tmp_path)
     rc, err = _run(built, "3DRTM.x", **p, withRho=1, image=tmp_path / "i.H")
-    assert rc == 1 and "variable-density" in err
+    assert rc == 1 and "need rho file" in err
+    rc, err = _run(built, "3DRTM.x", **p, withRho=1, LSRTM=1, image=tmp_path / "i.H")
+    assert rc == 1 and "withRho=1 with LSRTM=1" in err
     rc, err = _run(built, "3DRTM.x", **p, surf_type=1, image=tmp_path / "i.H")
     assert rc == 1 and "free-surface" in err
     rc, err = _run(built, "3DBORNMOD.x", **p)
