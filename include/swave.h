@@ -189,6 +189,26 @@ int sw_lsrtm(sw_ctx *ctx, const sw_genpar *g, const float *vel,
  * centred 2nd difference / dt^2. */
 int sw_born_wavelet(float *wavelet, int nt, float dt);
 
+/* bandpass (libs/libwave/Bandpass.f90:89-149, filters of bandpass.c): ntr
+ * traces of nt samples (trace-major, in place) padded by 10 samples of
+ * cosine-squared ramps at each end, then a Butterworth low-cut (flo Hz,
+ * nplo poles) and high-cut (fhi Hz, nphi poles); phase 0 = zero phase
+ * (each filter with half the poles, run forward and backward), 1 = minimum
+ * phase.  The low-cut is skipped for flo*dt <= 1e-6; flo*dt < 1e-4 together
+ * with fhi*dt > 0.4999 is refused.  Runs on the GPU, one thread per trace. */
+int sw_bandpass(sw_ctx *ctx, int ntr, int nt, float dt, float flo, float fhi, int nplo,
+                int nphi, int phase, float *traces);
+
+/* MuteParam_compute_mask (libs/libwave/Mute.f90:50-95, 172-219): the mute
+ * mask of nrec traces of nt samples (first sample at time ot), top mute at
+ * sqrt(t0^2 + ((hx+hy)/v0)^2) with a sin^2 ramp of tramp seconds before it,
+ * bottom mute at sqrt(t1^2 + ((hx+hy)/v1)^2) with a cos^2 ramp after it
+ * (hx, hy: receiver minus source x and y).  mask is nrec*nt.  Host only;
+ * defaults of the reference: v0 1500, v1 10000, t0 0, t1 40, tramp 0.5. */
+int sw_mute_mask(int nrec, int nt, float dt, float ot, const float *sou_coord,
+                 const float *rec_coord, float v0, float v1, float t0, float t1, float tramp,
+                 float *mask);
+
 /* readsou's withRho preprocessing (ReadSouVelRho.f90:328-343): in place,
  * w'(t) = w(t + dt/2) by an lsinc-point sinc (staggered grid), edge taps
  * dropped and the weights renormalised.  Host only. */

@@ -54,6 +54,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         "oracle_lsrtm_f64": [g, _dp, _dp, _dp, C.c_int, _dp, _dp, _dp, _dp],
         "oracle_born_wavelet": [_fp, C.c_int, C.c_float],
         "oracle_rho_wavelet": [_fp, C.c_int, C.c_int],
+        "oracle_mute_mask": [C.c_int, C.c_int, C.c_float, C.c_float, _fp, _fp, C.c_float,
+                             C.c_float, C.c_float, C.c_float, C.c_float, _fp],
+        "oracle_bandpass": [_fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int,
+                            C.c_int, C.c_int],
         "oracle_vel_check": [g, _fp, _fp, _fp],
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
         "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],
@@ -256,6 +260,16 @@ def stencil_rho_f64(g, vel, rho, u2):
     _chk(lib.oracle_stencil_rho_f64(C.byref(g), pv, pr, pa, out.ctypes.data_as(_dp)),
          "stencil_rho")
     return out
+
+
+def bandpass(traces, dt, flo=0.0, fhi=20.0, nplo=14, nphi=14, phase=0):
+    """bandpass of a (ntr, nt) array (returns a filtered float32 copy)."""
+    lib = load()
+    t = np.ascontiguousarray(traces, np.float32).copy()
+    ntr, nt = t.shape
+    _chk(lib.oracle_bandpass(t.ctypes.data_as(_fp), ntr, nt, dt, flo, fhi, nplo, nphi, phase),
+         "bandpass")
+    return t
 
 
 def mksinc(lsinc: int, shift: float) -> np.ndarray:

@@ -80,6 +80,12 @@ int oracle_lsrtm_f64(const sw_genpar *g, const double *vel,
                      const double *sou_coord, const double *wavelet, int nrec,
                      const double *rec_coord, const double *data,
                      double *image, double *illum);
+/* bandpass (Bandpass.f90:89-149, bandpass.c), in place over trace-major data. */
+int oracle_bandpass(float *traces, int ntr, int nt, float dt, float flo, float fhi, int nplo,
+                    int nphi, int phase);
+int oracle_mute_mask(int nrec, int nt, float dt, float ot, const float *sou,
+                     const float *rec, float v0, float v1, float t0, float t1, float tramp,
+                     float *mask);
 int oracle_rho_wavelet(float *w, int nt, int lsinc);
 int oracle_born_wavelet(float *wavelet, int nt, float dt);
 int oracle_vel_check(const sw_genpar *g, const float *vel, float *courant,

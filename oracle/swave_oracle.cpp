@@ -1778,6 +1778,181 @@ int oracle_lsrtm_f64(const sw_genpar *g, const double *vel, const double *sou_co
 }
 
 // readsou Born/LSRTM branch (ReadSouVelRho.f90:318-326).
+// ---------------------------------------------------------------------------
+// Band-pass (libs/libwave/Bandpass.f90:89-149 and the Butterworth filters of
+// libs/libwave/bandpass.c), restated with the reference's work arrays: data,
+// newdata and tempdata zeroed per trace, the filters writing samples 2..n-1,
+// every section copying newdata back in full.  The float/double mix of the C
+// coefficient formulas is kept.  The Fortran copies data(npad+1:nt) into an
+// nt-sample trace, a non-conforming assignment; it is taken as the nt samples
+// from npad+1 on (the unpadded trace).
+// ---------------------------------------------------------------------------
+namespace {
+const double kPiD = 3.1415926535897932384626433832795028841971693;
+
+struct BpCoef {
+  int ns;
+  std::vector<float> c;   // 5 per section
+};
+
+BpCoef bp_highcut(float fhi, int nphi, int phase) {
+  int nodd = nphi % 2;
+  if (phase == 0) {
+    if (nodd != 0) nphi = (nphi + 1) / 2;
+    else nphi = nphi / 2;
+    nodd = nphi % 2;
+  }
+  BpCoef r;
+  r.ns = (nphi + 1) / 2;
+  r.c.assign(5 * r.ns, 0.f);
+  float a = (float)(2.0 * tan(kPiD * fhi));
+  float aa = a * a;
+  float aap4 = (float)(aa + 4.0);
+  float dtheta = (float)(kPiD / nphi);
+  float theta0 = nodd != 0 ? 0.0f : (float)(dtheta / 2.0);
+  if (nodd != 0) {
+    r.c[0] = (float)(a / (a + 2.0));
+    r.c[1] = r.c[0];
+    r.c[2] = 0.0f;
+    r.c[3] = (float)((a - 2.0) / (a + 2.0));
+    r.c[4] = 0.0f;
+  }
+  for (int j = nodd; j < r.ns; ++j) {
+    double c = 4.0 * a * cos((double)(theta0 + j * dtheta));
+    r.c[5 * j + 0] = (float)(aa / (aap4 + c));
+    r.c[5 * j + 1] = (float)(2.0 * r.c[5 * j + 0]);
+    r.c[5 * j + 2] = r.c[5 * j + 0];
+    r.c[5 * j + 3] = (float)((2.0 * aa - 8.0) / (aap4 + c));
+    r.c[5 * j + 4] = (float)((aap4 - c) / (aap4 + c));
+  }
+  return r;
+}
+
+BpCoef bp_lowcut(float flo, int nplo, int phase) {
+  int nodd = nplo % 2;
+  if (phase == 0) {
+    if (nodd != 0) nplo = (nplo + 1) / 2;
+    else nplo = nplo / 2;
+    nodd = nplo % 2;
+  }
+  BpCoef r;
+  r.ns = (nplo + 1) / 2;
+  r.c.assign(5 * r.ns, 0.f);
+  float fno2 = 0.25f;
+  float a = (float)(2. * sin(kPiD * fno2) / cos(kPiD * fno2));
+  float aa = a * a;
+  float aap4 = aa + 4;
+  float e = (float)(-cos(kPiD * (flo + fno2)) / cos(kPiD * (flo - fno2)));
+  float ee = e * e;
+  float dtheta = (float)(kPiD / nplo);
+  float theta0 = nodd != 0 ? 0.0f : dtheta / 2;
+  if (nodd != 0) {
+    float b1 = a / (a + 2);
+    float b2 = (a - 2) / (a + 2);
+    float den = (float)(1.0 - b2 * e);
+    r.c[0] = (float)(b1 * (1. - e) / den);
+    r.c[1] = -r.c[0];
+    r.c[2] = 0.f;
+    r.c[3] = (e - b2) / den;
+    r.c[4] = 0.f;
+  }
+  for (int j = nodd; j < r.ns; ++j) {
+    double c = 4. * a * cos((double)(theta0 + j * dtheta));
+    float b1 = (float)(aa / (aap4 + c));
+    float b2 = (float)((2. * aa - 8.) / (aap4 + c));
+    float b3 = (float)((aap4 - c) / (aap4 + c));
+    float den = (float)(1. - b2 * e + b3 * ee);
+    r.c[5 * j + 0] = (float)(b1 * (1. - e) * (1. - e) / den);
+    r.c[5 * j + 1] = (float)(-2. * r.c[5 * j + 0]);
+    r.c[5 * j + 2] = r.c[5 * j + 0];
+    r.c[5 * j + 3] = (float)((2. * e * (1. + b3) - b2 * (1. + ee)) / den);
+    r.c[5 * j + 4] = (ee - b2 * e + b3) / den;
+  }
+  return r;
+}
+
+void bp_run(const BpCoef &k, int phase, int n1, float *data, float *newdata, float *tempdata) {
+  for (int s = 0; s < k.ns; ++s) {
+    const float *b = &k.c[5 * s];
+    for (int i1 = 2; i1 < n1; ++i1)
+      newdata[i1] = b[0] * data[i1] + b[1] * data[i1 - 1] + b[2] * data[i1 - 2] -
+                    b[3] * newdata[i1 - 1] - b[4] * newdata[i1 - 2];
+    for (int i1 = 0; i1 < n1; ++i1) data[i1] = newdata[i1];
+  }
+  if (phase == 0) {
+    for (int i1 = 2; i1 < n1; ++i1) tempdata[i1] = data[n1 + 1 - i1];
+    for (int s = 0; s < k.ns; ++s) {
+      const float *b = &k.c[5 * s];
+      for (int i1 = 2; i1 < n1; ++i1)
+        newdata[i1] = b[0] * tempdata[i1] + b[1] * tempdata[i1 - 1] + b[2] * tempdata[i1 - 2] -
+                      b[3] * newdata[i1 - 1] - b[4] * newdata[i1 - 2];
+      for (int i1 = 0; i1 < n1; ++i1) tempdata[i1] = newdata[i1];
+    }
+    for (int i1 = 2; i1 < n1; ++i1) data[i1] = tempdata[n1 + 1 - i1];
+  }
+}
+}  // namespace
+
+int oracle_bandpass(float *traces, int ntr, int nt, float dt, float flo, float fhi, int nplo,
+                    int nphi, int phase) {
+  const float pi = 3.1415926535f;
+  const float flo_tmp = flo * dt, fhi_tmp = fhi * dt;
+  const int npad = 10, n1pad = nt + 2 * npad;
+  if (flo_tmp < 0.0001f && fhi_tmp > 0.4999f) return SW_BAD_PARAM;
+  std::vector<float> data(n1pad), newdata(n1pad), tempdata(n1pad);
+  for (int i = 0; i < ntr; ++i) {
+    float *in = traces + (size_t)i * nt;
+    std::fill(data.begin(), data.end(), 0.f);
+    std::fill(newdata.begin(), newdata.end(), 0.f);
+    std::fill(tempdata.begin(), tempdata.end(), 0.f);
+    for (int q = 0; q < nt; ++q) data[npad + q] = in[q];
+    for (int j = 1; j <= npad; ++j) {
+      const float s1 = sinf((j - 1) * pi / (2 * (npad - 1)));
+      const float s2 = sinf((npad - j) * pi / (2 * (npad - 1)));
+      data[j - 1] = in[0] * (s1 * s1);
+      data[n1pad - npad + j - 1] = in[nt - 1] * (s2 * s2);
+    }
+    if (flo_tmp > 0.000001f) bp_run(bp_lowcut(flo_tmp, nplo, phase), phase, n1pad, data.data(),
+                                     newdata.data(), tempdata.data());
+    if (fhi_tmp < 4.999999f) bp_run(bp_highcut(fhi_tmp, nphi, phase), phase, n1pad, data.data(),
+                                    newdata.data(), tempdata.data());
+    for (int q = 0; q < nt; ++q) in[q] = data[npad + q];
+  }
+  return SW_OK;
+}
+
+// compute_top_mute / compute_bottom_mute (libs/libwave/Mute.f90:172-219) and
+// their product (MuteParam_compute_mask, Mute.f90:50-95).  Array sections
+// that would start before sample 1 start at sample 1.
+int oracle_mute_mask(int nrec, int nt, float dt, float ot, const float *sou,
+                     const float *rec, float v0, float v1, float t0, float t1, float tramp,
+                     float *mask) {
+  const float pi = 3.1415926535f;
+  std::vector<float> top(nt + 1), bot(nt + 1);
+  for (int r = 0; r < nrec; ++r) {
+    const float hx = rec[3 * r + 1] - sou[1], hy = rec[3 * r + 2] - sou[2];
+    int nramp = (int)(tramp / dt + 1.5f);
+    float tmute = sqrtf(t0 * t0 + ((hx + hy) / v0) * ((hx + hy) / v0));
+    int it = (int)((tmute - ot) / dt + 1.5f);
+    for (int i = 1; i <= nt; ++i) top[i] = 0.f;
+    for (int i = std::max(1, it - nramp); i <= std::min(nt, it); ++i) {
+      const float sv = sinf((i - it + nramp) * pi / (2 * nramp));
+      top[i] = sv * sv;
+    }
+    for (int i = std::max(1, it + 1); i <= nt; ++i) top[i] = 1.f;
+    tmute = sqrtf(t1 * t1 + ((hx + hy) / v1) * ((hx + hy) / v1));
+    it = (int)((tmute - ot) / dt + 1.5f);
+    for (int i = 1; i <= nt; ++i) bot[i] = 1.f;
+    for (int i = std::max(1, it + 1); i <= std::min(nt, it + 1 + nramp); ++i) {
+      const float cv = cosf((i - it - 1) * pi / (2 * nramp));
+      bot[i] = cv * cv;
+    }
+    for (int i = std::max(1, it + 1 + nramp); i <= nt; ++i) bot[i] = 0.f;
+    for (int i = 1; i <= nt; ++i) mask[(size_t)r * nt + i - 1] = top[i] * bot[i];
+  }
+  return SW_OK;
+}
+
 // readsou withRho branch (ReadSouVelRho.f90:328-343).
 int oracle_rho_wavelet(float *w, int nt, int lsinc) {
   std::vector<float> sinc(lsinc), tr(w, w + nt);

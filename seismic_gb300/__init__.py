@@ -136,6 +136,10 @@ _SIGS = {
     "sw_ctx_reset_stats": (C.c_int, [C.c_void_p]),
     "sw_ctx_set_boundary": (C.c_int, [C.c_void_p, C.c_int]),
     "sw_rho_wavelet": (C.c_int, [_fp, C.c_int, C.c_int]),
+    "sw_bandpass": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                              C.c_int, C.c_int, C.c_int, _fp]),
+    "sw_mute_mask": (C.c_int, [C.c_int, C.c_int, C.c_float, C.c_float, _fp, _fp, C.c_float,
+                               C.c_float, C.c_float, C.c_float, C.c_float, _fp]),
     "sw_shot_window": (C.c_int, [C.POINTER(SwGenpar), C.c_float, C.c_float, _fp, C.c_int, _fp,
                                  C.POINTER(SwWindow)]),
     "sw_window_extract": (C.c_int, [C.POINTER(SwGenpar), C.POINTER(SwWindow), _fp, _fp]),
@@ -289,6 +293,15 @@ class Context:
             keep.append(rho)
         io.rho = fptr(rho)
         self._check(self.lib.sw_propagate(self.h, C.byref(desc), C.byref(io)))
+
+    def bandpass(self, traces, dt: float, flo: float = 0.0, fhi: float = 20.0, nplo: int = 14,
+                 nphi: int = 14, phase: int = 0) -> np.ndarray:
+        """sw_bandpass of a (ntr, nt) array; returns the filtered copy."""
+        t = _f32(traces).copy()
+        ntr, nt = t.shape
+        self._check(self.lib.sw_bandpass(self.h, ntr, nt, dt, flo, fhi, nplo, nphi, phase,
+                                         fptr(t)))
+        return t
 
     # -- drivers -----------------------------------------------------------
     def modeling(self, g: SwGenpar, vel, sou_coord, wavelet, rec_coord, final_u2=False):
@@ -571,6 +584,20 @@ def modeling_noalloc(g: SwGenpar, vel, sou_coord, wavelet, rec_coord) -> np.ndar
     if code != SW_OK:
         raise SwaveError(code, "sw_modeling_noalloc")
     return data
+
+
+def mute_mask(nt: int, dt: float, sou_coord, rec_coord, ot: float = 0.0, v0: float = 1500.0,
+              v1: float = 10000.0, t0: float = 0.0, t1: float = 40.0,
+              tramp: float = 0.5) -> np.ndarray:
+    """sw_mute_mask: (nrec, nt) mute mask of one gather (reference defaults)."""
+    lib = load_library()
+    s, r = _f32(sou_coord), _f32(rec_coord)
+    m = np.zeros((r.size // 3, nt), np.float32)
+    code = lib.sw_mute_mask(r.size // 3, nt, dt, ot, fptr(s), fptr(r), v0, v1, t0, t1, tramp,
+                            fptr(m))
+    if code != SW_OK:
+        raise SwaveError(code, "sw_mute_mask")
+    return m
 
 
 def rho_wavelet(w, lsinc: int = 7) -> np.ndarray:

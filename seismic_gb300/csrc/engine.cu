@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/swave.h"
+#include "butterworth.h"
 #include "engine.h"
 #include "batch.cuh"
 #include "swave_dev.cuh"
@@ -683,6 +684,89 @@ int sw_born(sw_ctx *c, const sw_genpar *g, const float *vel, const float *ref,
     return SW_BAD_PARAM;
   return two_pass(c, *g, vel, ref, sou_coord, wavelet, nrec, rec_coord, nullptr, data, nullptr,
                   nullptr, 2);
+}
+
+int sw_bandpass(sw_ctx *c, int ntr, int nt, float dt, float flo, float fhi, int nplo,
+                int nphi, int phase, float *traces) {
+  if (!c || !traces || ntr < 1 || nt < 2 || !(dt > 0.f) || nplo < 1 || nphi < 1 ||
+      nplo > 2 * swave_bp::kMaxSections || nphi > 2 * swave_bp::kMaxSections)
+    return SW_BAD_PARAM;
+  cudaSetDevice(c->device);
+  // bandpass (Bandpass.f90:89-149): cutoffs in cycles per sample; a
+  // low-cut below 1e-6 or a high-cut at or above 4.999999 is skipped, and a
+  // filter that passes everything is refused.
+  const float flo_t = flo * dt, fhi_t = fhi * dt;
+  if (flo_t < 0.0001f && fhi_t > 0.4999f)
+    return fail(c, SW_BAD_PARAM, "band-pass needs flo or fhi inside the band");
+  swave_bp::Sections lo, hi;
+  if (flo_t > 0.000001f) lo = swave_bp::lowcut_sections(flo_t, nplo, phase);
+  if (fhi_t < 4.999999f) hi = swave_bp::highcut_sections(fhi_t, nphi, phase);
+  const int npad = 10, n = nt + 2 * npad;
+  std::vector<float> hostc(5 * (lo.n + hi.n) + 2 * npad);
+  std::memcpy(hostc.data(), lo.c, sizeof(float) * 5 * lo.n);
+  std::memcpy(hostc.data() + 5 * lo.n, hi.c, sizeof(float) * 5 * hi.n);
+  swave_bp::end_tapers(npad, hostc.data() + 5 * (lo.n + hi.n),
+                       hostc.data() + 5 * (lo.n + hi.n) + npad);
+  int st = SW_OK;
+  void *p = nullptr;
+  if ((st = upload(c, "bp_coef", hostc.data(), hostc.size() * sizeof(float), &p))) return st;
+  const float *dc = (const float *)p;
+  const size_t nb = (size_t)ntr * nt * sizeof(float);
+  if ((st = upload(c, "bp_in", traces, nb, &p))) return st;
+  const float *din = (const float *)p;
+  float *dout = (float *)dbuf(c, "bp_out", nb, &st);
+  float *D = (float *)dbuf(c, "bp_d", (size_t)n * ntr * sizeof(float), &st);
+  float *T = (float *)dbuf(c, "bp_t", (size_t)n * ntr * sizeof(float), &st);
+  if (!dout || !D || !T) return st;
+  cudaError_t e = launch_bandpass(ntr, nt, npad, phase, lo.n, dc, hi.n, dc + 5 * lo.n,
+                                  dc + 5 * (lo.n + hi.n), dc + 5 * (lo.n + hi.n) + npad, din,
+                                  dout, D, T, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "band-pass");
+  c->stats.launches_total++;
+  if ((st = download(c, traces, dout, nb))) return st;
+  if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(c, e, "band-pass");
+  return SW_OK;
+}
+
+int sw_mute_mask(int nrec, int nt, float dt, float ot, const float *sou_coord,
+                 const float *rec_coord, float v0, float v1, float t0, float t1, float tramp,
+                 float *mask) {
+  if (nrec < 0 || nt < 1 || !(dt > 0.f) || !sou_coord || (nrec > 0 && (!rec_coord || !mask)))
+    return SW_BAD_PARAM;
+  // MuteParam_compute_mask (Mute.f90:50-95) with compute_top_mute and
+  // compute_bottom_mute (Mute.f90:172-219): a sin^2 ramp up to the top mute
+  // time, a cos^2 ramp down after the bottom one, both at the offset
+  // (hx + hy) over their velocity; the mask is their product.
+  const float pi = 3.1415926535f;
+  const int nramp = (int)(tramp / dt + 1.5f);
+  for (int r = 0; r < nrec; ++r) {
+    const float hx = rec_coord[3 * r + 1] - sou_coord[1];
+    const float hy = rec_coord[3 * r + 2] - sou_coord[2];
+    float *m = mask + (size_t)r * nt;
+    // top: 0, ramp over samples it-nramp..it, then 1
+    const float ht = (hx + hy) / v0;
+    const float tt = std::sqrt(t0 * t0 + ht * ht);
+    const int it = (int)((tt - ot) / dt + 1.5f);
+    // bottom: 1, ramp over samples ib+1..ib+1+nramp, then 0
+    const float hb = (hx + hy) / v1;
+    const float tb = std::sqrt(t1 * t1 + hb * hb);
+    const int ib = (int)((tb - ot) / dt + 1.5f);
+    for (int i = 1; i <= nt; ++i) {
+      float top = i > it ? 1.f : 0.f;
+      if (i >= std::max(1, it - nramp) && i <= std::min(nt, it)) {
+        const float sv = std::sin((float)(i - it + nramp) * pi / (float)(2 * nramp));
+        top = sv * sv;
+      }
+      float bot = 1.f;
+      if (i >= std::max(1, ib + 1) && i <= std::min(nt, ib + 1 + nramp)) {
+        const float cv = std::cos((float)(i - ib - 1) * pi / (float)(2 * nramp));
+        bot = cv * cv;
+      }
+      if (i >= ib + 1 + nramp) bot = 0.f;   // mute(it+1+nramp:) = 0 comes last
+      m[i - 1] = top * bot;
+    }
+  }
+  return SW_OK;
 }
 
 int sw_rho_wavelet(float *w, int nt, int lsinc) {

@@ -224,6 +224,77 @@ cudaError_t launch_rho_delp(const Geom &g, const float *rho_pad, float *delp, fl
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Band-pass of traces (Bandpass.f90:89-149 with the filters of bandpass.c):
+// one thread per trace.  The trace is padded by npad samples at each end with
+// cosine-squared ramps from its end values, run through the low-cut and then
+// the high-cut cascade of second-order sections (forward, and for a
+// zero-phase filter again over the reversed samples 2..n-2), and its middle
+// nt samples are returned.  The work arrays are sample-major (sample i of
+// trace t at i*ntr + t) so that a warp's accesses coalesce.  Each section is
+// run in place: the old input samples and the new output samples it still
+// needs are carried in registers.  The first two outputs of every section
+// stay zero, as the reference's never-written work samples do.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bp_sections(float *X, int n, int ntr, int t, int ns,
+                                            const float *__restrict__ c) {
+  for (int q = 0; q < ns; ++q) {
+    const float c0 = c[5 * q], c1 = c[5 * q + 1], c2 = c[5 * q + 2], c3 = c[5 * q + 3],
+                c4 = c[5 * q + 4];
+    float xm2 = X[t], xm1 = X[(size_t)ntr + t], nm2 = 0.f, nm1 = 0.f;
+    for (int i = 2; i < n; ++i) {
+      const float xc = X[(size_t)i * ntr + t];
+      const float v = (((c0 * xc + c1 * xm1) + c2 * xm2) - c3 * nm1) - c4 * nm2;
+      X[(size_t)i * ntr + t] = v;
+      xm2 = xm1;
+      xm1 = xc;
+      nm2 = nm1;
+      nm1 = v;
+    }
+    X[t] = 0.f;
+    X[(size_t)ntr + t] = 0.f;
+  }
+}
+
+__device__ __forceinline__ void bp_filter(float *D, float *T, int n, int ntr, int t, int ns,
+                                          const float *__restrict__ c, int phase) {
+  bp_sections(D, n, ntr, t, ns, c);
+  if (phase == 0) {
+    T[t] = 0.f;
+    T[(size_t)ntr + t] = 0.f;
+    for (int i = 2; i < n; ++i) T[(size_t)i * ntr + t] = D[(size_t)(n + 1 - i) * ntr + t];
+    bp_sections(T, n, ntr, t, ns, c);
+    for (int i = 2; i < n; ++i) D[(size_t)i * ntr + t] = T[(size_t)(n + 1 - i) * ntr + t];
+  }
+}
+
+__global__ void k_bandpass(int ntr, int nt, int npad, int phase, int nlo, const float *clo,
+                           int nhi, const float *chi, const float *lead, const float *trail,
+                           const float *__restrict__ in, float *__restrict__ out, float *D,
+                           float *T) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntr) return;
+  const int n = nt + 2 * npad;
+  const float *tr = in + (size_t)t * nt;
+  for (int i = 0; i < nt; ++i) D[(size_t)(npad + i) * ntr + t] = tr[i];
+  for (int j = 0; j < npad; ++j) {
+    D[(size_t)j * ntr + t] = tr[0] * lead[j];
+    D[(size_t)(n - npad + j) * ntr + t] = tr[nt - 1] * trail[j];
+  }
+  if (nlo > 0) bp_filter(D, T, n, ntr, t, nlo, clo, phase);
+  if (nhi > 0) bp_filter(D, T, n, ntr, t, nhi, chi, phase);
+  float *o = out + (size_t)t * nt;
+  for (int i = 0; i < nt; ++i) o[i] = D[(size_t)(npad + i) * ntr + t];
+}
+
+cudaError_t launch_bandpass(int ntr, int nt, int npad, int phase, int nlo, const float *clo,
+                            int nhi, const float *chi, const float *lead, const float *trail,
+                            const float *in, float *out, float *D, float *T, cudaStream_t s) {
+  k_bandpass<<<(ntr + 127) / 128, 128, 0, s>>>(ntr, nt, npad, phase, nlo, clo, nhi, chi, lead,
+                                                trail, in, out, D, T);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
                                  float dyi, float dzi, float *gz, float *gx, float *gy,
                                  cudaStream_t s) {

@@ -54,6 +54,12 @@ cudaError_t launch_pad_velocity(const Geom &g, const float *vel_phys, float *vel
 cudaError_t launch_higdon_coeffs(const Geom &g, const float *vel_pad, float dt, float dxi,
                                  float dyi, float dzi, float *gz, float *gx, float *gy,
                                  cudaStream_t s);
+// Band-pass of ntr traces of nt samples (in/out trace-major, D and T work
+// arrays of (nt + 2*npad)*ntr floats); clo/chi: nlo/nhi sections of 5
+// coefficients (device).
+cudaError_t launch_bandpass(int ntr, int nt, int npad, int phase, int nlo, const float *clo,
+                            int nhi, const float *chi, const float *lead, const float *trail,
+                            const float *in, float *out, float *D, float *T, cudaStream_t s);
 // delp = 1/rho2 from the padded rho (Interpolate.f90:44-130); tmp is a
 // scratch array of the same size; sinc9 = mksinc(9, 0.5).
 cudaError_t launch_rho_delp(const Geom &g, const float *rho_pad, float *delp, float *tmp,

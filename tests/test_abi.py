@@ -107,3 +107,24 @@ def test_rho_wavelet_matches_oracle_and_shifts_half_a_sample(lib, oracle):
     t = np.arange(400)
     peak = lambda x: np.sum(t * x ** 2) / np.sum(x ** 2)
     assert abs((peak(a) - peak(w)) + 0.5) < 0.02
+
+
+def test_mute_mask_matches_oracle(lib, oracle):
+    """sw_mute_mask (MuteParam_compute_mask, Mute.f90:50-95,172-219)."""
+    nt, dt, ot = 600, 4e-3, 0.0
+    sou = np.array([10.0, 1000.0, 0.0], np.float32)
+    rec = np.zeros((40, 3), np.float32)
+    rec[:, 1] = np.linspace(200.0, 2600.0, 40)
+    args = (1500.0, 2500.0, 0.1, 1.6, 0.3)
+    a = np.zeros((40, nt), np.float32)
+    assert lib.sw_mute_mask(40, nt, C.c_float(dt), C.c_float(ot), sw.fptr(sou), sw.fptr(rec),
+                            *[C.c_float(x) for x in args], sw.fptr(a)) == sw.SW_OK
+    b = np.zeros_like(a)
+    oracle.load().oracle_mute_mask(40, nt, dt, ot, sou.ctypes.data_as(C.POINTER(C.c_float)),
+                                   rec.ctypes.data_as(C.POINTER(C.c_float)), *args,
+                                   b.ctypes.data_as(C.POINTER(C.c_float)))
+    np.testing.assert_array_equal(a, b)
+    assert a.min() == 0.0 and a.max() == 1.0
+    # the top mute moves later with offset
+    first = [(np.argmax(row > 0.5)) for row in a]
+    assert first[0] > first[20] and first[-1] > first[20]
