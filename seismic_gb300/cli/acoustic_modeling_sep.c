@@ -25,7 +25,7 @@ int main(int argc, char **argv) {
   cli_read_params(&p);
   float *wavelet = cli_read_source(&p);
   int ntr = 0;
-  float *traces = cli_read_traces(p.g.nt, &ntr);
+  float *traces = cli_read_traces(p.g.nt, &ntr, NULL);
   float sou[3];
   float *rec = cli_read_coords(ntr, sou);
   float *vel = cli_read_model(&p, "vel");

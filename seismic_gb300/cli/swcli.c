@@ -91,7 +91,7 @@ float *cli_read_source(cli_par *p) {
   return w;
 }
 
-float *cli_read_traces(int nt, int *ntr) {
+float *cli_read_traces(int nt, int *ntr, float *ot) {
   if (!sep_exist("traces")) cli_fail("need traces file");
   sep_file *f = sep_open_in("traces");
   if (!f) cli_fail("%s", sep_error());
@@ -99,6 +99,10 @@ float *cli_read_traces(int nt, int *ntr) {
   if (sep_hdr_int(f, "n1", &n1) != 1) cli_fail("traces header needs n1");
   if (sep_hdr_int(f, "n2", &n2) != 1 || n2 < 1) cli_fail("traces header needs n2");
   if (n1 != nt) cli_fail("nt traces and sources are different, exit now");
+  if (ot) {
+    *ot = 0.f;
+    sep_hdr_float(f, "o1", ot);
+  }
   float *t = (float *)xmalloc((size_t)n1 * n2 * 4);
   if (sep_read(f, t, (size_t)n1 * n2)) cli_fail("%s", sep_error());
   sep_close(f);

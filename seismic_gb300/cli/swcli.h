@@ -32,8 +32,9 @@ void cli_read_params(cli_par *p);
 float *cli_read_source(cli_par *p);
 
 /* readtraces (ReadSouVelRho.f90:59-88): n2 traces of n1 = nt samples from
- * the "traces" dataset.  Returns them (malloc, ntr*nt) and sets *ntr. */
-float *cli_read_traces(int nt, int *ntr);
+ * the "traces" dataset.  Returns them (malloc, ntr*nt), sets *ntr and, when
+ * ot is not NULL, the first sample's time (o1). */
+float *cli_read_traces(int nt, int *ntr, float *ot);
 
 /* readcoords (ReadSouVelRho.f90:90-137): coordfile rows of n1 keys, one per
  * trace; keygelev/keygx/keygy give the receiver (z, x, y), the last row's

@@ -226,3 +226,117 @@ def test_afwi_program_task_mig(built, oracle, tmp_path):
     # The stacking order is the same (gather order); the FP64 RMS sum runs in
     # index order on both sides.
     np.testing.assert_allclose(img, expect, rtol=1e-6, atol=1e-6 * np.abs(expect).max())
+
+
+def _inv_survey(tmp_path, built, nt=300):
+    """True model with a slow blob, three gathers; observed data from the
+    program's own Task=MOD; a smooth starting model."""
+    nz, nx, d = 40, 90, 10.0
+    z = np.arange(nz)[None, :] * d
+    x = np.arange(nx)[:, None] * d
+    vtrue = (1800 + 1.5 * z - 180 * np.exp(-((x - 450) ** 2 + (z - 220) ** 2) / 60.0 ** 2))
+    v0 = (1800 + 1.5 * z + 0 * x)
+    rows = []
+    for sx in (200.0, 450.0, 700.0):
+        for gx in np.arange(sx - 150.0, sx + 151.0, 20.0):
+            rows.append([sx, gx, 0.0, 0.0, 20.5, 12.0])
+    keys = np.array(rows, np.float32)
+    w = synth.ricker(8.0, 2e-3, nt).astype(np.float32)
+    ax = {"d1": d, "d2": d, "o1": 0.0, "o2": 0.0}
+    sep.write(str(tmp_path / "vtrue.H"), vtrue.astype(np.float32), ax)
+    sep.write(str(tmp_path / "v0.H"), v0.astype(np.float32), ax)
+    sep.write(str(tmp_path / "w.H"), w, {"d1": 2e-3, "o1": 0.0})
+    sep.write(str(tmp_path / "keys.H"), keys)
+    common = dict(stdin=tmp_path / "w.H", coordfile=tmp_path / "keys.H", keysx=1, keygx=2,
+                  keysy=3, keygy=4, keyselev=5, keygelev=6, aperture_x=100, twoD=1, snapi=4,
+                  ntaper=10, fmax=20)
+    _run(built, "2DAFWI.x", dict(common, vel=tmp_path / "vtrue.H", Task="MOD",
+                                 data=tmp_path / "obs.H"))
+    return common, v0.astype(np.float32), w, keys
+
+
+def test_afwi_program_task_inv(built, tmp_path):
+    """Task=INV against the same l_bfgs loop written here over the Python
+    API (band-pass, mute masks, smoothing radii, sw_fwi_fct_gdt, device
+    L-BFGS): the final model and the misfit history agree bit for bit, and
+    the misfit falls."""
+    common, v0, w, keys = _inv_survey(tmp_path, built)
+    obs, _ = sep.read(str(tmp_path / "obs.H"))
+    niter = 3
+    _run(built, "2DAFWI.x", dict(common, vel=tmp_path / "v0.H", Task="INV",
+                                 traces=tmp_path / "obs.H", niter=niter, vpmin=1500,
+                                 vpmax=2600, inv=tmp_path / "inv.H",
+                                 function=tmp_path / "f.H", model=tmp_path / "m.H"))
+    inv, h = sep.read(str(tmp_path / "inv.H"))
+    fun, _ = sep.read(str(tmp_path / "f.H"))
+    models, hm = sep.read(str(tmp_path / "m.H"))
+    assert int(h["n1"]) == 40 and int(h["n2"]) == 90
+    # -- the same loop over the Python API ------------------------------
+    nt, dt = w.size, 2e-3
+    g = sw.make_genpar(40, 90, 1, dz=10.0, dx=10.0, dt=dt, nt=nt, ntaper=10, lsinc=7, snapi=4,
+                       fmax=20.0)
+    c = sw.Context(0)
+    try:
+        wb = c.bandpass(w[None, :], dt)[0]
+        ob = c.bandpass(obs, dt)
+        desc = sw.SwFwiDesc()
+        desc.g = g
+        desc.aperture_x, desc.aperture_y, desc.illu_pow = 100.0, 0.0, 1.0
+        velref = np.float32((v0.max() - v0.min()) / np.float32(2) + v0.min())
+        freqref = np.float32(0.0 + (20.0 - 0.0) / 2)
+        wave = np.float32(0.5) * velref / freqref
+        r = int((wave / np.float32(10.0) + np.float32(1.5)) / np.float32(2))
+        desc.smooth_rect1, desc.smooth_rect2, desc.smooth_rect3 = r, r, int((0 + 1.5) / 2)
+        desc.smooth_doz = desc.smooth_dox = int(not wave <= 10.0)
+        desc.smooth_doy = 0
+        shots, row = [], 0
+        for sx in (200.0, 450.0, 700.0):
+            sel = keys[:, 0] == sx
+            rec = np.stack([keys[sel, 5], keys[sel, 1], keys[sel, 3]], 1).astype(np.float32)
+            sou = np.array([20.5, sx, 0.0], np.float32)
+            shots.append({"sou": sou, "rec": rec, "dobs": ob[row:row + rec.shape[0]],
+                          "mute": sw.mute_mask(nt, dt, sou, rec)})
+            row += rec.shape[0]
+        n = v0.size
+        x = v0.ravel().copy()
+        vpinit = x.astype(np.float64)
+        lb = sw.LBFGS(c, n, 5, 1500.0, 2600.0, xinit=vpinit)
+        eval_, it, count, cont, found = 0, 0, 0, True, False
+        xsave = vpinit.copy()
+        fhist = []
+        while cont and not found:
+            fd, grad, _ = c.fwi_fct_gdt(desc, x.reshape(v0.shape), wb, shots)
+            grad = grad.ravel()
+            if eval_ == 0:
+                mx = np.float32(x.max())
+                g0 = mx / (np.float32(100) * np.float32(np.abs(grad).max()))
+                f0 = float(mx * mx) / abs(fd)
+                fhist.append(np.float32(f0 * fd))
+            grad = (g0 * grad).astype(np.float32)
+            fd = f0 * fd
+            xd = x.astype(np.float64)
+            xdsave = xd.copy()
+            iflag, info = lb.step(xd, fd, -grad.astype(np.float64))
+            x = xd.astype(np.float32)
+            if info == 1:
+                xdsave = np.minimum(2600.0, np.maximum(1500.0, xdsave))
+                xsave = xdsave
+                it += 1
+                count += 1
+                found = count >= niter
+                fhist.append(np.float32(fd))
+            if iflag <= 0:
+                cont = False
+            eval_ += 1
+            if eval_ >= 3 * niter:
+                cont = False
+        lb.close()
+    finally:
+        c.close()
+    if not cont:
+        x = xsave.astype(np.float32)
+    x = np.minimum(np.float32(2600), np.maximum(np.float32(1500), x))
+    np.testing.assert_array_equal(fun, np.array(fhist, np.float32))
+    np.testing.assert_array_equal(inv.ravel(), x)
+    assert models.shape[0] == it
+    assert fun[-1] < 0.9 * fun[0]

@@ -193,8 +193,8 @@ def test_programs_reject_inconsistent_or_unbuilt_options(built, tmp_path):
 def test_afwi_program_rejects_inv_and_trace_count(built, tmp_path):
     p = _write_shot(tmp_path)
     p.pop("data")
-    rc, err = _run(built, "2DAFWI.x", **p, Task="INV")
-    assert rc == 1 and "only MOD and MIG" in err
+    rc, err = _run(built, "2DAFWI.x", **p, Task="FOO")
+    assert rc == 1 and "expected MOD, MIG or INV" in err
     sep.write(str(tmp_path / "t3.H"), np.zeros((3, 50), np.float32), {"d1": 0.001})
     rc, err = _run(built, "2DAFWI.x", **dict(p, traces=tmp_path / "t3.H"), Task="MIG",
                    image=tmp_path / "i.H")
