@@ -37,7 +37,15 @@ struct Bounds {
 
 static Bounds make_bounds(const sw_genpar &g) {
   Bounds b;
-  b.nmin1 = -g.ntaper + 1;
+  // Mirror sources extend the top padding to hold the mirrored footprint;
+  // a free surface replaces the top taper by lsinc cells
+  // (ExtractPadModel.f90:228-234).
+  if (g.shot_type > 0 || g.surf_type > 0) {
+    if (g.shot_type > 0) b.nmin1 = -(g.ntaper + g.lsinc / 2 + 2) + 1;
+    if (g.surf_type > 0) b.nmin1 = -g.lsinc + 1;
+  } else {
+    b.nmin1 = -g.ntaper + 1;
+  }
   b.nmax1 = g.nz + g.ntaper;
   b.nmin2 = -g.ntaper + 1;
   b.nmax2 = g.nx + g.ntaper;
@@ -385,17 +393,20 @@ static inline T higdon_sum(const T *g, T u3p1, T u3p2, T u2p0, T u2p1, T u2p2,
 // Boundary_3d (Boundary.f90:89-184) for surf_type = 0 (nz0 = nmin1).
 template <class T>
 static void boundary(Higdon<T> &h, const Bounds &b, const F3<T> &u1,
-                     const F3<T> &u2, F3<T> &u3) {
+                     const F3<T> &u2, F3<T> &u3, bool surf = false) {
   const int nst = 3;
-  const int nz0 = b.nmin1;
+  // With a free surface the top is not absorbing and the side lines start
+  // at row 1 (Boundary.f90:104-108,123-128).
+  const int nz0 = surf ? 1 : b.nmin1;
 #pragma omp parallel for schedule(static)
   for (int k = b.nmin3; k <= b.nmax3; ++k) {
     for (int j = b.nmin2; j <= b.nmax2; ++j) {
       const T *g = h.Gz(j, k);
-      for (int i = nz0 + nst; i >= b.nmin1 - 4; --i)
-        u3(i, j, k) = higdon_sum(g, u3(i + 1, j, k), u3(i + 2, j, k), u2(i, j, k),
-                                 u2(i + 1, j, k), u2(i + 2, j, k), u1(i, j, k),
-                                 u1(i + 1, j, k), u1(i + 2, j, k));
+      if (!surf)
+        for (int i = nz0 + nst; i >= b.nmin1 - 4; --i)
+          u3(i, j, k) = higdon_sum(g, u3(i + 1, j, k), u3(i + 2, j, k), u2(i, j, k),
+                                   u2(i + 1, j, k), u2(i + 2, j, k), u1(i, j, k),
+                                   u1(i + 1, j, k), u1(i + 2, j, k));
       for (int i = b.nmax1 - nst; i <= b.nmax1 + 4; ++i)
         u3(i, j, k) = higdon_sum(g + 8, u3(i - 1, j, k), u3(i - 2, j, k), u2(i, j, k),
                                  u2(i - 1, j, k), u2(i - 2, j, k), u1(i, j, k),
@@ -651,7 +662,7 @@ template <class T> struct Pos {
 template <class T>
 static bool make_positions(const sw_genpar &g, const Bounds &b, int n,
                            const T *coord, std::vector<Pos<T>> &out,
-                           bool need_sinc) {
+                           bool need_sinc, bool mirror = false) {
   out.resize(n);
   const T om[3] = {(T)g.oz, (T)g.ox, (T)(g.twoD ? 0.f : g.oy)};
   const T de[3] = {(T)g.dz, (T)g.dx, (T)(g.twoD ? 1.f : g.dy)};
@@ -662,6 +673,8 @@ static bool make_positions(const sw_genpar &g, const Bounds &b, int n,
     if (g.twoD && p.ic[2] != 1) return false;
     const int hw = need_sinc ? half : 0;
     if (p.ic[0] - hw < b.nmin1 - 4 || p.ic[0] + hw > b.nmax1 + 4) return false;
+    // The mirrored footprint (rows -ic-hw..-ic+hw) must lie in the array too.
+    if (mirror && (-p.ic[0] - hw < b.nmin1 - 4 || -p.ic[0] + hw > b.nmax1 + 4)) return false;
     if (p.ic[1] - hw < b.nmin2 - 4 || p.ic[1] + hw > b.nmax2 + 4) return false;
     if (!g.twoD && (p.ic[2] - hw < b.nmin3 - 4 || p.ic[2] + hw > b.nmax3 + 4)) return false;
     if (need_sinc) {
@@ -726,7 +739,7 @@ template <class T> struct IO {
 };
 
 static int check_genpar(const sw_genpar &g) {
-  if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0) return SW_UNSUPPORTED;
+  if (g.surf_type < 0 || g.shot_type < 0 || g.rec_type < 0) return SW_BAD_PARAM;
   if (g.nz < 1 || g.nx < 1 || g.ny < 1 || g.nt < 1 || g.ntaper < 1 || g.snapi < 1)
     return SW_BAD_PARAM;
   if (g.lsinc < 3 || (g.lsinc % 2) == 0) return SW_BAD_PARAM;
@@ -769,10 +782,25 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
   const bool inj_sinc = d.injection == SW_INJ_SINC || d.injection == SW_INJ_LSRTM_SINC;
   const bool ext_sinc = d.extraction == SW_EXT_SINC || d.extraction == SW_EXT_LSRTM_SINC ||
                         d.extraction == SW_EXT_SINC_AFWI;
+  // Mirror sources / receivers (Injection.f90:160-164, Extraction.f90:38-50):
+  // the injected side of a backward propagation (tmax = 1) follows rec_type.
+  const bool inj_mirror = (d.tmax == 1 ? g.rec_type : g.shot_type) != 0;
+  const bool ext_mirror = g.rec_type != 0;
+  const bool surf = g.surf_type != 0;
   if (d.injection != SW_INJ_NONE && io.nsou > 0)
-    if (!make_positions<T>(g, b, io.nsou, io.sou_coord, spos, inj_sinc)) return SW_BAD_PARAM;
+    if (!make_positions<T>(g, b, io.nsou, io.sou_coord, spos, inj_sinc, inj_mirror))
+      return SW_BAD_PARAM;
   if (d.extraction != SW_EXT_NONE && io.nrec > 0)
-    if (!make_positions<T>(g, b, io.nrec, io.rec_coord, rpos, ext_sinc)) return SW_BAD_PARAM;
+    if (!make_positions<T>(g, b, io.nrec, io.rec_coord, rpos, ext_sinc, ext_mirror))
+      return SW_BAD_PARAM;
+  // Flat surface at elevation 0 (drivers allocate elev%elev = 0):
+  // find_i_d (ModelSpaceTypes.f90:144-151) gives its row and offset.
+  int ielev = 1;
+  T delev = T(0);
+  if (surf) find_i_d<T>(ielev, delev, T(0), (T)g.oz, (T)g.dz);
+  const int irow0 = surf ? std::max(ielev, 1) : 1;   // first row kept in snapshots and images
+  std::vector<T> fs_sinc(g.lsinc), fs_interp(g.lsinc);
+  if (surf && delev != T(0)) mksinc<T>(fs_sinc.data(), g.lsinc, delev / (T)g.dz);
 
   std::vector<T> taperx, tapery;
   if (d.imaging != SW_IMG_NONE) compute_taper<T>(nx, ny, taperx, tapery);
@@ -804,7 +832,9 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
         T &tr = io.rec_trace[(size_t)r * nt + (it - 1)];
         if (d.extraction == SW_EXT_SIMPLE_AFWI) {
           // Extraction_array_simple_afwi_noomp (Extraction.f90:71-107).
-          tr = tr + (*u2)(p.ic[0], p.ic[1], g.twoD ? 1 : p.ic[2]);
+          const int k1 = g.twoD ? 1 : p.ic[2];
+          if (ext_mirror) tr = tr + ((*u2)(p.ic[0], p.ic[1], k1) - (*u2)(-p.ic[0], p.ic[1], k1));
+          else tr = tr + (*u2)(p.ic[0], p.ic[1], k1);
           continue;
         }
         T v;
@@ -821,18 +851,23 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
         } else {
           v = T(1.);                       // Extraction.f90:137-162
         }
+        // The mirror receiver takes u at the cell reflected through row 0
+        // (Extraction.f90:549-555, 324-333).
+        auto uval = [&](int i, int j, int k) -> T {
+          return ext_mirror ? (*u2)(i, j, k) - (*u2)(-i, j, k) : (*u2)(i, j, k);
+        };
         if (g.twoD) {
           // Extraction_1trace_sinc_xy (Extraction.f90:511-560).
           for (int j = -half; j <= half; ++j)
             for (int i = -half; i <= half; ++i)
-              tr = tr + ((v * (*u2)(i + p.ic[0], j + p.ic[1], 1)) * p.sz[half + i]) * p.sx[half + j];
+              tr = tr + ((v * uval(i + p.ic[0], j + p.ic[1], 1)) * p.sz[half + i]) * p.sx[half + j];
         } else {
           // Extraction_1trace_sinc_xyz (Extraction.f90:276-337); the y
           // weight is the x sinc column (sinc(maxy+1+k,2)).
           for (int k = -half; k <= half; ++k)
             for (int j = -half; j <= half; ++j)
               for (int i = -half; i <= half; ++i)
-                tr = tr + (((v * (*u2)(i + p.ic[0], j + p.ic[1], k + p.ic[2])) * p.sz[half + i]) *
+                tr = tr + (((v * uval(i + p.ic[0], j + p.ic[1], k + p.ic[2])) * p.sz[half + i]) *
                            p.sx[half + j]) * p.sx[half + k];
         }
       }
@@ -841,9 +876,11 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
     if (d.extract_wave && (it % g.snapi) == 0) {
       ++wcounter;
       if (wcounter <= ntsnap) {
+        // With a free surface the rows above it are stored as zero
+        // (Extraction.f90:580-592).
         for (int k = 1; k <= ny; ++k)
           for (int j = 1; j <= nx; ++j)
-            for (int i = 1; i <= nz; ++i) W(i, j, k, wcounter) = (*u2)(i, j, k);
+            for (int i = 1; i <= nz; ++i) W(i, j, k, wcounter) = i >= irow0 ? (*u2)(i, j, k) : T(0);
       }
     }
     // ImagingCondition(u2) for tstep = -1 (Propagator.f90:192-194).
@@ -857,7 +894,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
         for (int k = 1; k <= ny; ++k)
           for (int j = 1; j <= nx; ++j) {
             const T taper = taperx[j - 1] * tapery[k - 1];
-            for (int i = 1; i <= nz; ++i) {
+            for (int i = irow0; i <= nz; ++i) {
               const T u = (*u2)(i, j, k);
               const T w = W(i, j, k, index);
               T &im = M(io.image, i, j, k);
@@ -880,7 +917,30 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
           }
       }
     }
-    // Boundary_set_free_surface_grid: no-op for surf_type = 0.
+    // Boundary_set_free_surface_grid (Boundary.f90:1609-1658, called at
+    // Propagator.f90:198): zero above the surface, then the mirror image of
+    // the rows below it with the opposite sign (on the grid, or through a
+    // sinc when the surface lies between rows).
+    if (surf) {
+      const int h = g.lsinc / 2;
+      for (int k = b.nmin3; k <= b.nmax3; ++k)
+        for (int j = b.nmin2; j <= b.nmax2; ++j) {
+          for (int i = b.nmin1; i <= ielev - 1; ++i) (*u2)(i, j, k) = T(0);
+          if (delev == T(0)) {
+            for (int i = 0; i <= 2; ++i) (*u2)(ielev - 2 - i, j, k) = -(*u2)(ielev + i, j, k);
+          } else {
+            for (int i = -h; i <= h; ++i) {
+              T f = T(0);
+              for (int l = -h; l <= h; ++l) f = f + (*u2)(ielev + l + i, j, k) * fs_sinc[h + l];
+              fs_interp[h + i] = f;
+            }
+            for (int i = 2; i <= h + 1; ++i)
+              for (int l = -h; l <= i - 1; ++l)
+                (*u2)(ielev - i + l, j, k) =
+                    (*u2)(ielev - i + l, j, k) - fs_interp[h + i - 1] * fs_sinc[h + l];
+          }
+        }
+    }
     // FD_scheme(u2 -> u3) (Propagator.f90:202).
     if (io.rho) {
       stencil_rho(rs, b, g.twoD != 0, *u2, *u3, vel);
@@ -903,6 +963,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
           const T vv = vel(p.ic[0], p.ic[1], k1);
           const T v2r = io.rho ? (vv * vv) * rs.rho(p.ic[0], p.ic[1], k1) : vv * vv;
           (*u3)(p.ic[0], p.ic[1], k1) = (*u3)(p.ic[0], p.ic[1], k1) + v2r * tr;
+          if (inj_mirror) (*u3)(-p.ic[0], p.ic[1], k1) = (*u3)(-p.ic[0], p.ic[1], k1) - v2r * tr;
           continue;
         }
         T v2r;
@@ -920,6 +981,12 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
             for (int i = -half; i <= half; ++i) {
               T &u = (*u3)(i + p.ic[0], j + p.ic[1], 1);
               u = u + (a * p.sz[half + i]) * p.sx[half + j];
+              if (inj_mirror) {
+                // The mirror source: reflected row, reflected z weight
+                // (Injection.f90:440-449).
+                T &m = (*u3)(i - p.ic[0], j + p.ic[1], 1);
+                m = m - (a * p.sz[half - i]) * p.sx[half + j];
+              }
             }
         } else {
           // Injection_source_sinc_xyz (Injection.f90:274-338), x sinc on y.
@@ -928,6 +995,10 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
               for (int i = -half; i <= half; ++i) {
                 T &u = (*u3)(i + p.ic[0], j + p.ic[1], k + p.ic[2]);
                 u = u + ((a * p.sz[half + i]) * p.sx[half + j]) * p.sx[half + k];
+                if (inj_mirror) {
+                  T &m = (*u3)(i - p.ic[0], j + p.ic[1], k + p.ic[2]);
+                  m = m - ((a * p.sz[half - i]) * p.sx[half + j]) * p.sx[half + k];
+                }
               }
         }
       }
@@ -940,7 +1011,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
         for (int k = 1; k <= ny; ++k)
           for (int j = 1; j <= nx; ++j) {
             const T taper = taperx[j - 1] * tapery[k - 1];
-            for (int i = 1; i <= nz; ++i) {
+            for (int i = irow0; i <= nz; ++i) {
               T &u = (*u3)(i, j, k);
               const T rf = io.ref[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * (k - 1))];
               u = u + (((T(2) * taper) * rf) * W(i, j, k, mcounter)) / vel(i, j, k);
@@ -950,7 +1021,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
     }
     // TimeDer (Propagator.f90:218), Higdon (Propagator.f90:222-228).
     time_update(b, (T)g.dt, *u2, *u1, *u0, *um1, *u3);
-    if (!g_rigid) boundary(hig, b, *u1, *u2, *u3);
+    if (!g_rigid) boundary(hig, b, *u1, *u2, *u3, surf);
     // FDswaptime_pointer (FDswaptimes.f90:14-24).
     F3<T> *t = um1;
     um1 = u0; u0 = u1; u1 = u2; u2 = u3; u3 = t;

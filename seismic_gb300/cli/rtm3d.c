@@ -8,7 +8,9 @@
  * memory: maxsize= and the wave_fwd disk path of the reference are not
  * used.  withRho=1 with rho= runs RTM_to_memory's variable-density branch:
  * the forward-grid density operator in both passes
- * (to_disk_to_memory_RTM.f90:388-398,455-465). */
+ * (to_disk_to_memory_RTM.f90:388-398,455-465).  LSRTM=1 CHEAPLSRTM=1 runs
+ * CHEAP_LSRTM_to_memory (to_disk_to_memory_RTM.f90:581-668): the LSRTM
+ * backward pass on the forward-grid stencil instead of the adjoint one. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -44,12 +46,15 @@ int main(int argc, char **argv) {
   if (!vsmall || !ims || !ils || !im || !il) cli_fail("out of host memory");
   if (sw_window_extract(&p.g, &w, vel, vsmall) != SW_OK) cli_fail("window extract");
   sw_ctx *ctx = cli_context();
-  if (rho) {
-    float *rs = (float *)malloc(nw * 4);
+  if (rho || p.CHEAPLSRTM) {
+    float *rs = NULL;
     const int ntsnap = gw.nt / gw.snapi;
     float *wave = (float *)malloc(nw * (size_t)(ntsnap > 0 ? ntsnap : 1) * 4);
-    if (!rs || !wave) cli_fail("out of host memory");
-    if (sw_window_extract(&p.g, &w, rho, rs) != SW_OK) cli_fail("window extract");
+    if (!wave) cli_fail("out of host memory");
+    if (rho) {
+      rs = (float *)malloc(nw * 4);
+      if (!rs || sw_window_extract(&p.g, &w, rho, rs) != SW_OK) cli_fail("window extract");
+    }
     sw_prop_desc d;
     memset(&d, 0, sizeof(d));
     d.g = gw;
@@ -67,12 +72,13 @@ int main(int argc, char **argv) {
     io.sou_coord = sou;
     io.sou_trace = wavelet;
     io.wave = wave;
-    cli_check(ctx, sw_propagate(ctx, &d, &io), "forward propagation (withRho)");
+    cli_check(ctx, sw_propagate(ctx, &d, &io), "forward propagation");
     d.tmin = gw.nt;
     d.tmax = 1;
     d.tstep = -1;
     d.extract_wave = 0;
-    d.imaging = SW_IMG_RTM;
+    d.imaging = p.CHEAPLSRTM ? SW_IMG_LSRTM : SW_IMG_RTM;
+    d.injection = p.CHEAPLSRTM ? SW_INJ_LSRTM_SINC : SW_INJ_SINC;
     memset(ims, 0, nw * 4);
     memset(ils, 0, nw * 4);
     io.nsou = ntr;
@@ -80,7 +86,7 @@ int main(int argc, char **argv) {
     io.sou_trace = traces;
     io.image = ims;
     io.illum = ils;
-    cli_check(ctx, sw_propagate(ctx, &d, &io), "backward propagation (withRho)");
+    cli_check(ctx, sw_propagate(ctx, &d, &io), "backward propagation");
     free(wave);
     free(rs);
   } else if (p.LSRTM)

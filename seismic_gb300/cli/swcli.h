@@ -21,7 +21,7 @@ void cli_fail(const char *fmt, ...);
  * snapi 4, lsinc 7, num_threads 4, maxsize 16, rec/shot/surf_type 0, twoD,
  * withRho, LSRTM, Born false, verb true, Task MOD.  Options of the
  * reference that this build does not implement (non-zero
- * rec/shot/surf_type, CHEAPLSRTM) stop the program with an error; programs
+ * rec/shot/surf_type) stop the program with an error; programs
  * without a variable-density path reject withRho themselves. */
 void cli_read_params(cli_par *p);
 

@@ -124,21 +124,26 @@ int cuda_fail(sw_ctx *c, cudaError_t e, const char *what) {
 }
 
 // Grow-only named device buffers owned by the context.
-void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st) {
+void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st, size_t slack) {
   if (bytes == 0) bytes = 16;
   DBuf &b = c->bufs[name];
   if (b.cap < bytes) {
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.cap = 0;
-    cudaError_t e = cudaMalloc(&b.p, bytes);
+    cudaError_t e = cudaMalloc(&b.p, bytes + slack);
+    if (e == cudaErrorMemoryAllocation && slack > 0) {
+      cudaGetLastError();
+      slack = 0;
+      e = cudaMalloc(&b.p, bytes);
+    }
     if (e != cudaSuccess) {
       cudaGetLastError();
       *st = fail(c, e == cudaErrorMemoryAllocation ? SW_OOM_ADMISSION : SW_CUDA_ERR,
                  "cudaMalloc(%s, %zu bytes): %s", name.c_str(), bytes, cudaGetErrorString(e));
       return nullptr;
     }
-    b.cap = bytes;
+    b.cap = bytes + slack;
   }
   return b.p;
 }

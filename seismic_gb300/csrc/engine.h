@@ -105,7 +105,9 @@ int fail(sw_ctx *c, int code, const char *fmt, ...);
       return ::swave::cuda_fail(c, sw_e_, #call " @ " __FILE__ ":" SW_STR(__LINE__)); \
   } while (0)
 int cuda_fail(sw_ctx *c, cudaError_t e, const char *what);
-void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st);
+// Grow-only named device buffer of the context; a growth allocates
+// bytes + slack.
+void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st, size_t slack = 0);
 int check_genpar(sw_ctx *c, const sw_genpar &g);
 Geom make_geom(const sw_genpar &g);
 Coefs make_coefs(const sw_genpar &g);

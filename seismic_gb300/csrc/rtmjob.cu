@@ -368,7 +368,26 @@ int prepare_batch(sw_rtm_job *j, int &next, int end, bool modeling, std::vector<
     offs.push_back(total);
     total += need_of(shot_genpar(M, S.w, S.s.nt), modeling ? S.s.nrec : 0);
   }
-  char *arena = (char *)dbuf(c, "rtm_arena", total, &st);
+  // Growing the arena frees and reallocates it (tens of milliseconds at
+  // these sizes); when it must grow, size it for the largest batch of
+  // max_batch consecutive shots of the job (within the budget), so that it
+  // grows at most once per job.
+  size_t reserve = total;
+  if (held < total) {
+    const int ns = (int)j->shots.size();
+    std::vector<size_t> need_i(ns);
+    for (int q = 0; q < ns; ++q) {
+      const auto &S = j->shots[q];
+      need_i[q] = need_of(shot_genpar(M, S.w, S.s.nt), modeling ? S.s.nrec : 0);
+    }
+    size_t window = 0;
+    for (int q = 0; q < ns; ++q) {
+      window += need_i[q];
+      if (q >= j->max_batch) window -= need_i[q - j->max_batch];
+      reserve = std::max(reserve, std::min(window, (size_t)budget));
+    }
+  }
+  char *arena = (char *)dbuf(c, "rtm_arena", reserve, &st);
   if (!arena) return st;
   bufs.assign(batch.size(), ShotBufs{});
   vhost.assign(batch.size(), {});

@@ -173,7 +173,9 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     bytes += rup(ntile * sizeof(int)) + rup(nb * sizeof(T3Maps));
   }
   bytes += rup(sizeof(int));   // error flags
-  char *arena = (char *)dbuf(c, "batch_arena", bytes, &st);
+  // A quarter of headroom when the arena grows: batches of slightly larger
+  // windows then reuse it instead of reallocating.
+  char *arena = (char *)dbuf(c, "batch_arena", bytes, &st, bytes / 4);
   if (!arena) return st;
   char *cur = arena;
   // ---- carve and fill ----

@@ -231,10 +231,11 @@ __device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, 
 }
 
 // Snapshot saving (Extraction.f90:562-601) and RTM / LSRTM imaging
-// (Imaging.f90:265 and 735) of a thread's elements; su and svel are the
-// staged u2 and velocity halo tiles (svel only for the adjoint stencil, the
-// variant the imaging runs with).  The operations are those of the
-// element-by-element path.
+// (Imaging.f90:265 and 735) of a thread's elements; su is the staged u2 halo
+// tile and svel the staged velocity: the halo tile for the adjoint stencil,
+// the core tile (column stride T2_Z) for the forward one (the backward pass
+// of CHEAP_LSRTM images on the forward grid).  The operations are those of
+// the element-by-element path.
 template <bool ADJ>
 __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp, const T2Img &P,
                                              int e, const float *su, const float *svel, int tid) {
@@ -258,7 +259,7 @@ __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp,
         if (stp.img == 1) {
           im = im + (u * wsn) * taper;
         } else {
-          const float v = ADJ ? svel[(jl + 4) * T2_SZ + 4 + r] : 1.f;
+          const float v = ADJ ? svel[(jl + 4) * T2_SZ + 4 + r] : svel[jl * T2_Z + r];
           im = im + (((2.0f * taper) * u) * wsn) / v;
         }
         stp.image[pc + i] = im;
@@ -679,7 +680,8 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       const float *st = t2_smem + cur * SF;
       t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st, tid);
       if ((stp.extract || stp.img) && t2_phys_tile(h, e))
-        t2_snap_tile<ADJ>(h, stp, P, e, st, st + T2_HALO, tid);
+        t2_snap_tile<ADJ>(h, stp, P, e, st, ADJ ? st + T2_HALO : st + T2_HALO + 3 * T2_CORE,
+                          tid);
       t2_edges<ADJ>(h, s, e, st, tid, 0);
     }
     __syncthreads();   // the stage is free for tile k+2
@@ -804,7 +806,8 @@ __device__ __forceinline__ void tile2d_ws(const BatchTables &t, int s_off, int n
     const float *stg = t2_smem + st * SF;
     t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, stg, gtid);
     if ((stp.extract || stp.img) && t2_phys_tile(h, e))
-      t2_snap_tile<ADJ>(h, stp, P, e, stg, stg + T2_HALO, gtid);
+      t2_snap_tile<ADJ>(h, stp, P, e, stg,
+                        ADJ ? stg + T2_HALO : stg + T2_HALO + 3 * T2_CORE, gtid);
     t2_edges<ADJ>(h, s, e, stg, gtid, 1 + g);
     __syncwarp();
     if ((tid & 31) == 0) mbar_arrive(&empty[st]);

@@ -90,18 +90,41 @@ def test_modeling_program(built, oracle, tmp_path, three_d):
     np.testing.assert_array_equal(data, ref)
 
 
+def _cheap_lsrtm(oracle, g, vel, sou, w, rec, d):
+    """CHEAP_LSRTM_to_memory: the LSRTM backward pass on the forward grid."""
+    n = vel.size
+    wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+    f = sw.SwPropDesc()
+    f.g = g
+    f.tmin, f.tmax, f.tstep = 1, g.nt, 1
+    f.fd_scheme, f.injection, f.extract_wave = sw.FD_FORWARD, sw.INJ_SINC, 1
+    oracle.propagate(f, vel, sou, w, wave=wave)
+    b = sw.SwPropDesc()
+    b.g = g
+    b.tmin, b.tmax, b.tstep = g.nt, 1, -1
+    b.fd_scheme, b.injection, b.imaging = sw.FD_FORWARD, sw.INJ_LSRTM_SINC, sw.IMG_LSRTM
+    im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    oracle.propagate(b, vel, rec, d, wave=wave, image=im, illum=il)
+    return im, il
+
+
 @pytest.mark.parametrize("three_d", [False, True])
-@pytest.mark.parametrize("lsrtm", [False, True])
-def test_rtm_program(built, oracle, tmp_path, three_d, lsrtm):
+@pytest.mark.parametrize("mode", ["rtm", "lsrtm", "cheap"])
+def test_rtm_program(built, oracle, tmp_path, three_d, mode):
     params, g, vel, win, sou, rec, w, ntr = _case(tmp_path, three_d, nt=120)
     d = (np.random.default_rng(3).standard_normal((ntr, g.nt)) * 1e-2).astype(np.float32)
     params.update(traces=_traces(tmp_path, "t.H", d), image=tmp_path / "im.H")
-    if lsrtm:
+    if mode != "rtm":
         params.update(LSRTM=1)
+    if mode == "cheap":
+        params.update(CHEAPLSRTM=1)
     _run(built, "3DRTM.x", params)
     out, h = sep.read(str(tmp_path / "im.H"))
-    if lsrtm:
+    if mode == "lsrtm":
         rim, ril = oracle.lsrtm(g, vel[win], sou, sw.born_wavelet(w, g.dt), rec, d)
+    elif mode == "cheap":
+        rim, ril = _cheap_lsrtm(oracle, g, np.ascontiguousarray(vel[win]), sou,
+                                sw.born_wavelet(w, g.dt), rec, d)
     else:
         rim, ril = oracle.rtm(g, vel[win], sou, w, rec, d)
     im_full = np.zeros_like(vel)
@@ -228,7 +251,7 @@ def test_afwi_program_task_mig(built, oracle, tmp_path):
     np.testing.assert_allclose(img, expect, rtol=1e-6, atol=1e-6 * np.abs(expect).max())
 
 
-def _inv_survey(tmp_path, built, nt=300):
+def _inv_survey(tmp_path, built, nt=400):
     """True model with a slow blob, three gathers; observed data from the
     program's own Task=MOD; a smooth starting model."""
     nz, nx, d = 40, 90, 10.0
@@ -241,11 +264,11 @@ def _inv_survey(tmp_path, built, nt=300):
         for gx in np.arange(sx - 150.0, sx + 151.0, 20.0):
             rows.append([sx, gx, 0.0, 0.0, 20.5, 12.0])
     keys = np.array(rows, np.float32)
-    w = synth.ricker(8.0, 2e-3, nt).astype(np.float32)
+    w = synth.ricker(8.0, 1.5e-3, nt).astype(np.float32)
     ax = {"d1": d, "d2": d, "o1": 0.0, "o2": 0.0}
     sep.write(str(tmp_path / "vtrue.H"), vtrue.astype(np.float32), ax)
     sep.write(str(tmp_path / "v0.H"), v0.astype(np.float32), ax)
-    sep.write(str(tmp_path / "w.H"), w, {"d1": 2e-3, "o1": 0.0})
+    sep.write(str(tmp_path / "w.H"), w, {"d1": 1.5e-3, "o1": 0.0})
     sep.write(str(tmp_path / "keys.H"), keys)
     common = dict(stdin=tmp_path / "w.H", coordfile=tmp_path / "keys.H", keysx=1, keygx=2,
                   keysy=3, keygy=4, keyselev=5, keygelev=6, aperture_x=100, twoD=1, snapi=4,
@@ -272,7 +295,7 @@ def test_afwi_program_task_inv(built, tmp_path):
     models, hm = sep.read(str(tmp_path / "m.H"))
     assert int(h["n1"]) == 40 and int(h["n2"]) == 90
     # -- the same loop over the Python API ------------------------------
-    nt, dt = w.size, 2e-3
+    nt, dt = w.size, 1.5e-3
     g = sw.make_genpar(40, 90, 1, dz=10.0, dx=10.0, dt=dt, nt=nt, ntaper=10, lsinc=7, snapi=4,
                        fmax=20.0)
     c = sw.Context(0)

@@ -188,3 +188,32 @@ def test_born_lsrtm_dot_test_rigid(oracle, three_d):
         oracle.set_rigid(False)
     np.testing.assert_array_equal(lm, rlm)
     np.testing.assert_array_equal(ltd, rltd)
+
+
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
+@pytest.mark.parametrize("fd", [sw.FD_FORWARD, sw.FD_ADJOINT])
+@pytest.mark.parametrize("imaging", [sw.IMG_RTM, sw.IMG_LSRTM, sw.IMG_AFWI])
+def test_backward_imaging_every_grid_and_kernel(oracle, kernel, fd, imaging):
+    """Every imaging condition on either stencil grid (the CHEAP_LSRTM
+    backward pass images on the forward grid) with every 2D step kernel."""
+    g, vel, sou, rec, w = case2d(nt=120)
+    ntsnap = g.nt // g.snapi
+    rng = np.random.default_rng(7)
+    wave = rng.standard_normal(ntsnap * g.nz * g.nx).astype(np.float32)
+    adj = rng.standard_normal((rec.shape[0], g.nt)).astype(np.float32)
+    inj = sw.INJ_SIMPLE if imaging == sw.IMG_AFWI else (
+        sw.INJ_LSRTM_SINC if imaging == sw.IMG_LSRTM else sw.INJ_SINC)
+    d = _desc(g, False, fd_scheme=fd, injection=inj, imaging=imaging)
+    n = g.nz * g.nx
+    a_im, a_il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    b_im, b_il = a_im.copy(), a_il.copy()
+    c = sw.Context(0)
+    try:
+        c.set_tuning(step_kernel=kernel)
+        c.propagate(d, vel, rec, adj, wave=wave.copy(), image=a_im, illum=a_il)
+    finally:
+        c.close()
+    oracle.propagate(d, vel, rec, adj, wave=wave.copy(), image=b_im, illum=b_il)
+    assert np.abs(b_im).max() > 0
+    np.testing.assert_array_equal(a_im, b_im)
+    np.testing.assert_array_equal(a_il, b_il)
