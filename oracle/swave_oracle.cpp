@@ -662,7 +662,7 @@ template <class T> struct Pos {
 template <class T>
 static bool make_positions(const sw_genpar &g, const Bounds &b, int n,
                            const T *coord, std::vector<Pos<T>> &out,
-                           bool need_sinc, bool mirror = false) {
+                           bool need_sinc, bool mirror = false, bool mirror_in_domain = false) {
   out.resize(n);
   const T om[3] = {(T)g.oz, (T)g.ox, (T)(g.twoD ? 0.f : g.oy)};
   const T de[3] = {(T)g.dz, (T)g.dx, (T)(g.twoD ? 1.f : g.dy)};
@@ -674,7 +674,11 @@ static bool make_positions(const sw_genpar &g, const Bounds &b, int n,
     const int hw = need_sinc ? half : 0;
     if (p.ic[0] - hw < b.nmin1 - 4 || p.ic[0] + hw > b.nmax1 + 4) return false;
     // The mirrored footprint (rows -ic-hw..-ic+hw) must lie in the array too.
-    if (mirror && (-p.ic[0] - hw < b.nmin1 - 4 || -p.ic[0] + hw > b.nmax1 + 4)) return false;
+    // A mirror source must also lie in the compute domain (an injection
+    // into the padding cells would be overwritten by the boundary update).
+    const int mlo = mirror_in_domain ? b.nmin1 : b.nmin1 - 4;
+    const int mhi = mirror_in_domain ? b.nmax1 : b.nmax1 + 4;
+    if (mirror && (-p.ic[0] - hw < mlo || -p.ic[0] + hw > mhi)) return false;
     if (p.ic[1] - hw < b.nmin2 - 4 || p.ic[1] + hw > b.nmax2 + 4) return false;
     if (!g.twoD && (p.ic[2] - hw < b.nmin3 - 4 || p.ic[2] + hw > b.nmax3 + 4)) return false;
     if (need_sinc) {
@@ -788,7 +792,7 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
   const bool ext_mirror = g.rec_type != 0;
   const bool surf = g.surf_type != 0;
   if (d.injection != SW_INJ_NONE && io.nsou > 0)
-    if (!make_positions<T>(g, b, io.nsou, io.sou_coord, spos, inj_sinc, inj_mirror))
+    if (!make_positions<T>(g, b, io.nsou, io.sou_coord, spos, inj_sinc, inj_mirror, true))
       return SW_BAD_PARAM;
   if (d.extraction != SW_EXT_NONE && io.nrec > 0)
     if (!make_positions<T>(g, b, io.nrec, io.rec_coord, rpos, ext_sinc, ext_mirror))
@@ -799,6 +803,8 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
   T delev = T(0);
   if (surf) find_i_d<T>(ielev, delev, T(0), (T)g.oz, (T)g.dz);
   const int irow0 = surf ? std::max(ielev, 1) : 1;   // first row kept in snapshots and images
+  if (surf && (ielev - 2 * (g.lsinc / 2) - 1 < b.nmin1 - 4 || ielev + 2 * (g.lsinc / 2) > b.nmax1 + 4))
+    return SW_BAD_PARAM;
   std::vector<T> fs_sinc(g.lsinc), fs_interp(g.lsinc);
   if (surf && delev != T(0)) mksinc<T>(fs_sinc.data(), g.lsinc, delev / (T)g.dz);
 

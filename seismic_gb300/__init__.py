@@ -205,8 +205,14 @@ def make_genpar(nz, nx, ny=1, dz=10.0, dx=10.0, dy=1.0, oz=0.0, ox=0.0, oy=0.0, 
 
 
 def padded_shape(g: SwGenpar) -> tuple[int, int, int]:
-    """(n3p, n2p, n1p) of the padded arrays u(nmin1-4:nmax1+4, ...)."""
-    n1p = g.nz + 2 * g.ntaper + 8
+    """(n3p, n2p, n1p) of the padded arrays u(nmin1-4:nmax1+4, ...); the top
+    padding follows shot_type and surf_type (ExtractPadModel.f90:228-234)."""
+    nmin1 = -g.ntaper + 1
+    if g.shot_type > 0:
+        nmin1 = -(g.ntaper + g.lsinc // 2 + 2) + 1
+    if g.surf_type > 0:
+        nmin1 = -g.lsinc + 1
+    n1p = (g.nz + g.ntaper + 4) - (nmin1 - 4) + 1
     n2p = g.nx + 2 * g.ntaper + 8
     n3p = 1 if g.twoD else g.ny + 2 * g.ntaper + 8
     return (n3p, n2p, n1p)

@@ -60,9 +60,6 @@ void cli_read_params(cli_par *p) {
   sep_par_str("Task", p->task, sizeof(p->task));
   if (p->LSRTM) par_bool("CHEAPLSRTM", &p->CHEAPLSRTM, 0);
   par_bool("write_forward_wavefield", &p->WriteFwdWvfld, 0);
-  if (g->rec_type || g->shot_type || g->surf_type)
-    cli_fail("rec_type/shot_type/surf_type > 0: mirror and free-surface modes are not built in "
-             "swave");
   if (p->verbose) {
     fprintf(stderr, "INFO: task=%s fmax=%g ntaper=%d snapi=%d aperture_x=%g aperture_y=%g\n",
             p->task, (double)g->fmax, g->ntaper, g->snapi, (double)p->aperture_x,

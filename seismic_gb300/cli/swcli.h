@@ -19,10 +19,8 @@ void cli_fail(const char *fmt, ...);
 
 /* read_3D_params (libs/libwave/ReadParam.f90:15-84): fmax 30, ntaper 20,
  * snapi 4, lsinc 7, num_threads 4, maxsize 16, rec/shot/surf_type 0, twoD,
- * withRho, LSRTM, Born false, verb true, Task MOD.  Options of the
- * reference that this build does not implement (non-zero
- * rec/shot/surf_type) stop the program with an error; programs
- * without a variable-density path reject withRho themselves. */
+ * withRho, LSRTM, Born false, verb true, Task MOD.  Programs without a
+ * variable-density path reject withRho themselves. */
 void cli_read_params(cli_par *p);
 
 /* readsou (ReadSouVelRho.f90:298-344): the wavelet from the "in" dataset

@@ -161,6 +161,9 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
     }
   }
   const bool phys = i >= 1 && i <= g.nz && j >= 1 && j <= g.nx && k >= 1 && k <= g.ny;
+  // Under a free surface the rows above it are stored as zero and take no
+  // imaging or Born source (Extraction.f90:580-592, Imaging.f90:248-258).
+  const bool below = i >= S.irow0;
   const bool snapstep = (it % S.snapi) == 0;
   int cnt = 0;
   long long pp = 0;
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
   }
   const long long nphys = (long long)g.nz * g.nx * g.ny;
   // Injection_Born (Imaging.f90:747-788), tstep = +1 only.
-  if (S.imaging == 4 && S.tstep > 0 && phys && snapstep && cnt <= S.ntsnap) {
+  if (S.imaging == 4 && S.tstep > 0 && phys && below && snapstep && cnt <= S.ntsnap) {
     const float *w0 = S.wave + (long long)(cnt - 1) * nphys;
     sv = sv + (((2.0f * taper) * S.ref[pp]) * w0[pp]) / S.vel[p];
   }
@@ -186,9 +189,10 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
   u3[p] = a * S.div11;
   if (phys && snapstep) {
     // Extraction_wavefield (Extraction.f90:562-601).
-    if (S.extract_wave && cnt <= S.ntsnap) S.wave[(long long)(cnt - 1) * nphys + pp] = u2c;
+    if (S.extract_wave && cnt <= S.ntsnap)
+      S.wave[(long long)(cnt - 1) * nphys + pp] = below ? u2c : 0.f;
     // Imaging conditions on u2 before the step, tstep = -1 (Propagator.f90:192-194).
-    if (S.imaging >= 1 && S.imaging <= 3 && S.tstep < 0) {
+    if (S.imaging >= 1 && S.imaging <= 3 && S.tstep < 0 && below) {
       const int index = S.ntsnap - cnt + 1;
       if (index >= 1) {
         const float w = S.wave[(long long)(index - 1) * nphys + pp];
@@ -319,7 +323,10 @@ __global__ void k_bextract(BatchTables t, int s_off) {
   const int i0 = S.ric[3 * r], j0 = S.ric[3 * r + 1], k0 = g.twoD ? 1 : S.ric[3 * r + 2];
   float *trp = S.rec_tr + (long long)r * S.nt + (it - 1);
   if (S.ext_mode == 2) {  // Extraction_array_simple_afwi_noomp
-    if (lane == 0) *trp = *trp + u2[g.idx(i0, j0, k0)];
+    if (lane == 0) {
+      if (S.ext_mirror) *trp = *trp + (u2[g.idx(i0, j0, k0)] - u2[g.idx(-i0, j0, k0)]);
+      else *trp = *trp + u2[g.idx(i0, j0, k0)];
+    }
     return;
   }
   float v;
@@ -339,8 +346,12 @@ __global__ void k_bextract(BatchTables t, int s_off) {
     if (tp < ntap) {
       const int ii = tp % ls, rest = tp / ls;
       const int jj = rest % ls, kq = rest / ls;
-      const long long p = g.idx(i0 - h + ii, j0 - h + jj, g.twoD ? 1 : k0 - h + kq);
-      prod = ((v * u2[p]) * wz[ii]) * wx[jj];
+      const int kc = g.twoD ? 1 : k0 - h + kq;
+      const long long p = g.idx(i0 - h + ii, j0 - h + jj, kc);
+      // A mirror receiver takes u minus u at the row reflected through row 0
+      // (Extraction.f90:549-555, 324-333).
+      const float uv = S.ext_mirror ? u2[p] - u2[g.idx(h - ii - i0, j0 - h + jj, kc)] : u2[p];
+      prod = ((v * uv) * wz[ii]) * wx[jj];
       if (!g.twoD) prod = prod * wx[kq];     // the y weights are the x column
     }
     const int nlane = min(32, ntap - c0);
@@ -455,6 +466,43 @@ __global__ void __launch_bounds__(128) k_bedges2d(BatchTables t, int s_off) {
 // One thread per half line (line = q / 2, half = q % 2: the near and the far
 // edge are independent); z lines (n2*n3 per shot), x lines (n1*n3), y lines
 // (n1*n2, 3D only), launched in that order like the reference's loops.
+// Boundary_set_free_surface_grid (Boundary.f90:1609-1658) on u2 of the
+// step, one thread per (x, y) column of a shot with a free surface: zero the
+// rows above the surface row ielev, then write the mirror image of the rows
+// below it with the opposite sign, on the grid (the surface on a row) or
+// through the sinc weights fs_sinc (the surface between rows).
+__global__ void k_bfree(BatchTables t, int s_off) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= t.hz_start[t.nshots]) return;
+  const int b = find_shot(t.hz_start, t.nshots, q);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (!S.surf || s >= S.nsteps) return;
+  const Geom &g = S.g;
+  const int n2 = g.nmax2 - g.nmin2 + 1;
+  const long long l = q - t.hz_start[b];
+  const int j = g.nmin2 + (int)(l % n2), k = g.nmin3 + (int)(l / n2);
+  float *u2 = S.f[(s + 3) % 5];
+  const int ie = S.ielev;
+  for (int i = g.nmin1; i <= ie - 1; ++i) u2[g.idx(i, j, k)] = 0.f;
+  if (S.fs_grid) {
+    for (int i = 0; i <= 2; ++i) u2[g.idx(ie - 2 - i, j, k)] = -u2[g.idx(ie + i, j, k)];
+    return;
+  }
+  const int h = S.ext_half;
+  float ui[15];
+  for (int i = -h; i <= h; ++i) {
+    float f = 0.f;
+    for (int l2 = -h; l2 <= h; ++l2) f = f + u2[g.idx(ie + l2 + i, j, k)] * S.fs_sinc[h + l2];
+    ui[h + i] = f;
+  }
+  for (int i = 2; i <= h + 1; ++i)
+    for (int l2 = -h; l2 <= i - 1; ++l2) {
+      const long long p = g.idx(ie - i + l2, j, k);
+      u2[p] = u2[p] - ui[h + i - 1] * S.fs_sinc[h + l2];
+    }
+}
+
 __global__ void k_bhiggz(BatchTables t, int s_off) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if ((q >> 1) >= t.hz_start[t.nshots]) return;
@@ -469,6 +517,7 @@ __global__ void k_bhiggz(BatchTables t, int s_off) {
   const int j = g.nmin2 + (int)(l % n2), k = g.nmin3 + (int)(l / n2);
   const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
   float *u3 = S.f[(s + 4) % 5];
+  if ((q & 1) == 0 && S.surf) return;   // a free surface: the top does not absorb
   if ((q & 1) == 0) higdon_half(S.gz + l, cs, u1, u2, u3, g.idx(g.nmin1 + 3, j, k), 1);
   else higdon_half(S.gz + l + 8 * cs, cs, u1, u2, u3, g.idx(g.nmax1 - 3, j, k), -1);
 }
@@ -485,6 +534,7 @@ __global__ void k_bhiggx(BatchTables t, int s_off) {
   const long long l = (q >> 1) - t.hx_start[b];
   const long long cs = (long long)n1 * n3;
   const int i = g.nmin1 + (int)(l % n1), k = g.nmin3 + (int)(l / n1);
+  if (S.surf && i < 1) return;   // side lines from row 1 under a free surface
   const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
   float *u3 = S.f[(s + 4) % 5];
   const long long L = g.ld1;
@@ -504,6 +554,7 @@ __global__ void k_bhiggy(BatchTables t, int s_off) {
   const long long l = (q >> 1) - t.hy_start[b];
   const long long cs = (long long)n1 * n2;
   const int i = g.nmin1 + (int)(l % n1), j = g.nmin2 + (int)(l / n1);
+  if (S.surf && i < 1) return;   // side lines from row 1 under a free surface
   const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
   float *u3 = S.f[(s + 4) % 5];
   const long long P = g.plane();
@@ -671,6 +722,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   }
   if (has_adj3d && n_v2u > 0 && !tile.stream3d) {
     k_bv2u<<<n_v2u, 256, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (tile.has_surf && n_hz > 0) {
+    k_bfree<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   }
   if (tile.has_rho && n_v2u > 0) {

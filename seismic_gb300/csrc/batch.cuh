@@ -54,6 +54,11 @@ struct ShotDev {
   float *sz, *sx, *sy;
   Coefs cr;
   float dzi, dxi, dyi;
+  // Mirror receivers (rec_type > 0) and the free surface (surf_type > 0):
+  // the surface row ielev, its grid (1) or sinc (0) mirror with the weights
+  // fs_sinc, and irow0, the first row kept in snapshots and images.
+  int ext_mirror, surf, ielev, fs_grid, irow0;
+  float fs_sinc[15];
 };
 
 // Compact per-shot view used by the pipelined 2D kernel; the kernel keeps the
@@ -156,6 +161,7 @@ struct StepTile {
   int n_edge = 0;      // threads of that launch
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
   int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
+  int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)
 };
 
 // Threads of the fused 2D edge kernel for one shot: four corner warps and

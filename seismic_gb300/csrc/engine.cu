@@ -149,8 +149,8 @@ void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st, size_t sla
 }
 
 int check_genpar(sw_ctx *c, const sw_genpar &g) {
-  if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0)
-    return fail(c, SW_UNSUPPORTED, "surf_type/shot_type/rec_type != 0 is not built");
+  if (g.surf_type < 0 || g.shot_type < 0 || g.rec_type < 0)
+    return fail(c, SW_BAD_PARAM, "negative surf_type/shot_type/rec_type");
   if (g.nz < 1 || g.nx < 1 || g.ny < 1 || g.nt < 1 || g.ntaper < 4 || g.snapi < 1)
     return fail(c, SW_BAD_PARAM, "bad sizes nz=%d nx=%d ny=%d nt=%d ntaper=%d snapi=%d", g.nz,
                 g.nx, g.ny, g.nt, g.ntaper, g.snapi);
@@ -165,7 +165,14 @@ int check_genpar(sw_ctx *c, const sw_genpar &g) {
 // FDbounds for shot_type = surf_type = 0 (ReadSouVelRho.f90:456-470).
 Geom make_geom(const sw_genpar &g) {
   Geom G;
-  G.nmin1 = -g.ntaper + 1;
+  // Mirror sources extend the top padding; a free surface replaces the top
+  // taper by lsinc cells (ExtractPadModel.f90:228-234).
+  if (g.shot_type > 0 || g.surf_type > 0) {
+    if (g.shot_type > 0) G.nmin1 = -(g.ntaper + g.lsinc / 2 + 2) + 1;
+    if (g.surf_type > 0) G.nmin1 = -g.lsinc + 1;
+  } else {
+    G.nmin1 = -g.ntaper + 1;
+  }
   G.nmax1 = g.nz + g.ntaper;
   G.nmin2 = -g.ntaper + 1;
   G.nmax2 = g.nx + g.ntaper;
@@ -285,7 +292,7 @@ static inline float host_vel(const sw_genpar &g, const float *vp, int i, int j, 
 // cell, the contributions in source order.
 int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
                     const float *sou_coord, const float *vel_phys, InjPlan &plan,
-                    const float *rho_phys) {
+                    const float *rho_phys, bool mirror) {
   plan.on = 0;
   if (mode == SW_INJ_NONE || nsou <= 0) return SW_OK;
   std::vector<int> ic;
@@ -304,6 +311,12 @@ int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int 
     if (i - h < G.nmin1 || i + h > G.nmax1 || j - h < G.nmin2 || j + h > G.nmax2 ||
         k - hk < G.nmin3 || k + hk > G.nmax3)
       return fail(c, SW_BAD_PARAM, "source %d footprint leaves the compute domain", r);
+    if (mirror) {
+      // The mirror source sits at row -i (Injection.f90:440-449).
+      if (-i - h < G.nmin1 || -i + h > G.nmax1)
+        return fail(c, SW_BAD_PARAM, "mirror of source %d leaves the compute domain", r);
+      bi0 = std::min(bi0, -i - h); bi1 = std::max(bi1, -i + h);
+    }
     bi0 = std::min(bi0, i - h); bi1 = std::max(bi1, i + h);
     bj0 = std::min(bj0, j - h); bj1 = std::max(bj1, j + h);
     bk0 = std::min(bk0, k - hk); bk1 = std::max(bk1, k + hk);
@@ -311,7 +324,7 @@ int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int 
   const long long nb = (long long)(bi1 - bi0 + 1) * (bj1 - bj0 + 1) * (bk1 - bk0 + 1);
   struct Tmp { int cell; InjEntry e; };
   std::vector<Tmp> all;
-  const long long per = sinc ? (long long)ls * ls * (g.twoD ? 1 : ls) : 1;
+  const long long per = (sinc ? (long long)ls * ls * (g.twoD ? 1 : ls) : 1) * (mirror ? 2 : 1);
   all.reserve((size_t)(per * nsou));
   std::vector<float> sz(ls), sx(ls), sy(ls);
   const float inv_d2 = 1.f / (g.dz * g.dx);
@@ -330,23 +343,33 @@ int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int 
     auto cell = [&](int i, int j, int k) {
       return (int)((i - bi0) + (long long)(bi1 - bi0 + 1) * ((j - bj0) + (long long)(bj1 - bj0 + 1) * (k - bk0)));
     };
+    // A mirror entry subtracts the term of the reflected row with the
+    // reflected z weight; it carries -v2r, which negates the product exactly.
     if (!sinc) {
       all.push_back({cell(i0, j0, k0), {r, v2r, 1.f, 1.f, 1.f}});
+      if (mirror) all.push_back({cell(-i0, j0, k0), {r, -v2r, 1.f, 1.f, 1.f}});
       continue;
     }
     mksinc(sz.data(), ls, dc[3 * r] / de[0]);
     mksinc(sx.data(), ls, dc[3 * r + 1] / de[1]);
     if (g.twoD) {
       for (int j = -h; j <= h; ++j)
-        for (int i = -h; i <= h; ++i)
+        for (int i = -h; i <= h; ++i) {
           all.push_back({cell(i0 + i, j0 + j, 1), {r, v2r, sz[h + i], sx[h + j], 1.f}});
+          if (mirror)
+            all.push_back({cell(i - i0, j0 + j, 1), {r, -v2r, sz[h - i], sx[h + j], 1.f}});
+        }
     } else {
       // Injection_source_sinc_xyz weights y with the x sinc column
       // (Injection.f90:314).
       for (int k = -h; k <= h; ++k)
         for (int j = -h; j <= h; ++j)
-          for (int i = -h; i <= h; ++i)
+          for (int i = -h; i <= h; ++i) {
             all.push_back({cell(i0 + i, j0 + j, k0 + k), {r, v2r, sz[h + i], sx[h + j], sx[h + k]}});
+            if (mirror)
+              all.push_back(
+                  {cell(i - i0, j0 + j, k0 + k), {r, -v2r, sz[h - i], sx[h + j], sx[h + k]}});
+          }
     }
   }
   // Stable counting sort by cell keeps source order inside a cell.
@@ -364,7 +387,7 @@ int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int 
 }
 
 int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nrec,
-                     const float *rec_coord, ExtPlan &plan) {
+                     const float *rec_coord, ExtPlan &plan, bool mirror) {
   plan.on = 0;
   if (mode == SW_EXT_NONE || nrec <= 0) return SW_OK;
   std::vector<float> dc;
@@ -383,6 +406,8 @@ int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int
     if (i - hh < G.lo1 || i + hh > G.nmax1 + 4 || j - hh < G.lo2 || j + hh > G.nmax2 + 4 ||
         kk - hk < G.lo3 || kk + hk > G.nmax3 + G.nbound)
       return fail(c, SW_BAD_PARAM, "receiver %d footprint leaves the padded grid", r);
+    if (mirror && (-i - hh < G.lo1 || -i + hh > G.nmax1 + 4))
+      return fail(c, SW_BAD_PARAM, "mirror of receiver %d leaves the padded grid", r);
     if (sinc) {
       mksinc(&plan.wz[(size_t)r * ls], ls, dc[3 * r] / de[0]);
       mksinc(&plan.wx[(size_t)r * ls], ls, dc[3 * r + 1] / de[1]);
@@ -391,6 +416,7 @@ int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int
   plan.on = 1;
   plan.mode = mode;
   plan.nrec = nrec;
+  plan.mirror = mirror ? 1 : 0;
   return SW_OK;
 }
 

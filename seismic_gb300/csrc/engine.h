@@ -46,6 +46,7 @@ struct InjPlan {
 
 struct ExtPlan {
   int on = 0, mode = 0, nrec = 0;
+  int mirror = 0;   // rec_type > 0: u(row) - u(-row)
   std::vector<int> ic;
   std::vector<float> wz, wx;
 };
@@ -122,9 +123,9 @@ void mksinc(float *sinc, int lsinc, float shift);
 void compute_taper(int nxw, int nyw, std::vector<float> &tx, std::vector<float> &ty);
 int build_injection(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nsou,
                     const float *sou_coord, const float *vel_phys, InjPlan &plan,
-                    const float *rho_phys = nullptr);
+                    const float *rho_phys = nullptr, bool mirror = false);
 int build_extraction(sw_ctx *c, const sw_genpar &g, const Geom &G, int mode, int nrec,
-                     const float *rec_coord, ExtPlan &plan);
+                     const float *rec_coord, ExtPlan &plan, bool mirror = false);
 int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt);
 int compute_window(sw_ctx *c, const sw_genpar &g, float apx, float apy, const float *sou,
                    int nrec, const float *rec, Window &w);

@@ -95,10 +95,18 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   StepTile tile = opt.tile;
   // The variable-density operator runs on the point-tile step kernel after a
   // gradient pass (k_brho_grad).
+  // So do the free surface (k_bfree before the step) and mirror sources and
+  // receivers.
   tile.has_rho = 0;
-  for (int b = 0; b < nb; ++b)
+  tile.has_surf = 0;
+  bool special = false;
+  for (int b = 0; b < nb; ++b) {
+    const sw_genpar &g = shots[b].d.g;
     if (shots[b].io.rho_pad) tile.has_rho = 1;
-  if (tile.has_rho) {
+    if (g.surf_type != 0) tile.has_surf = 1;
+    if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0) special = true;
+  }
+  if (tile.has_rho || special) {
     tile.stream2d = 0;
     tile.stream3d = 0;
   }
@@ -142,10 +150,14 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     has_adj3d = has_adj3d || (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT);
     if (io.rho_pad && d.fd_scheme != SW_FD_FORWARD)
       return fail(c, SW_UNSUPPORTED, "the variable-density operator has no adjoint-grid form");
+    // The injected side of a backward propagation (tmax = 1) follows
+    // rec_type, a forward one shot_type (Injection.f90:160-164).
+    const bool inj_mirror = (d.tmax == 1 ? d.g.rec_type : d.g.shot_type) != 0;
     if ((st = build_injection(c, d.g, G[b], d.injection, io.nsou, io.sou_coord, io.vel_phys_host,
-                              inj[b], io.rho_pad ? io.rho_phys_host : nullptr)))
+                              inj[b], io.rho_pad ? io.rho_phys_host : nullptr, inj_mirror)))
       return st;
-    if ((st = build_extraction(c, d.g, G[b], d.extraction, io.nrec, io.rec_coord, ext[b])))
+    if ((st = build_extraction(c, d.g, G[b], d.extraction, io.nrec, io.rec_coord, ext[b],
+                               d.g.rec_type != 0)))
       return st;
     has_ext = has_ext || ext[b].on;
     if (d.imaging != SW_IMG_NONE) compute_taper(d.g.nx, d.g.ny, tx[b], ty[b]);
@@ -183,7 +195,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   std::vector<int> step_tiles(nb + 1, 0), rec_start(nb + 1, 0), hz(nb + 1, 0), hx(nb + 1, 0),
       hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0), term(nb + 1, 0);
   // The fused 2D edge kernel needs n1, n2 >= 16 in every shot.
-  bool fused_edges = !has_3d;
+  bool fused_edges = !has_3d && !tile.has_surf;
   for (int b = 0; b < nb && fused_edges; ++b) fused_edges = edge_threads_2d(G[b]) > 0;
   int max_steps = 0;
   for (int b = 0; b < nb; ++b) {
@@ -255,6 +267,21 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       S.src_tr = io.sou_trace_dev;
     }
     S.ext_mode = ext[b].on ? ext[b].mode : 0;
+    S.ext_mirror = ext[b].on ? ext[b].mirror : 0;
+    S.irow0 = 1;
+    if (g.surf_type != 0) {
+      // Flat surface at elevation 0 (the drivers' elev%elev = 0): find_i_d
+      // (ModelSpaceTypes.f90:144-151) gives its row and offset.
+      S.surf = 1;
+      S.ielev = (int)lroundf((0.f - g.oz) / g.dz) + 1;
+      const float delev = 0.f - (g.oz + (float)(S.ielev - 1) * g.dz);
+      S.fs_grid = delev == 0.f;
+      if (!S.fs_grid) mksinc(S.fs_sinc, g.lsinc, delev / g.dz);
+      S.irow0 = std::max(S.ielev, 1);
+      const int h = g.lsinc / 2;
+      if (S.ielev - 2 * h - 1 < G[b].lo1 || S.ielev + 2 * h > G[b].nmax1 + 4)
+        return fail(c, SW_BAD_PARAM, "free surface row %d leaves the padded grid", S.ielev);
+    }
     S.nrec = ext[b].on ? ext[b].nrec : 0;
     S.ext_half = g.lsinc / 2;
     if (ext[b].on) {

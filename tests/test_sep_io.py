@@ -179,8 +179,6 @@ def test_programs_reject_inconsistent_or_unbuilt_options(built, tmp_path):
     assert rc == 1 and "need rho file" in err
     rc, err = _run(built, "3DRTM.x", **p, withRho=1, LSRTM=1, image=tmp_path / "i.H")
     assert rc == 1 and "withRho=1 with LSRTM=1" in err
-    rc, err = _run(built, "3DRTM.x", **p, surf_type=1, image=tmp_path / "i.H")
-    assert rc == 1 and "free-surface" in err
     rc, err = _run(built, "3DBORNMOD.x", **p)
     assert rc == 1 and "need reflectivity file" in err
     far = dict(p, aperture_x=100)                     # every key 5000 m: off the model
