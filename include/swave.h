@@ -41,7 +41,7 @@ typedef enum sw_status {
   SW_TIMEOUT = 3,        /* a bounded device-side wait ran out              */
   SW_NUMERIC = 4,        /* NaN / Inf detected                              */
   SW_CUDA_ERR = 5,       /* a CUDA runtime call failed                      */
-  SW_UNSUPPORTED = 6     /* option not built (mirror / free surface / rho)  */
+  SW_UNSUPPORTED = 6     /* option not built (an adjoint grid with rho, ...) */
 } sw_status;
 
 /* Subset of GeneralParam (libs/libwave/GeneralParamTypes.f90:9-48) that the
