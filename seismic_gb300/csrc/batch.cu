@@ -614,7 +614,21 @@ static cudaError_t launch_tile2d(const BatchTables &t, int s_off, int n_tiles, i
   // overflow its shared-memory copy.
   const int grid = std::max({1, std::min(n_tiles, 2 * nsm),
                              (n_tiles + T2_MAX_TILES_PER_CTA - 1) / T2_MAX_TILES_PER_CTA});
-  k_bstep2d_t<ADJ><<<grid, 256, t2_smem_bytes<ADJ>(), s>>>(t, s_off, n_tiles);
+  // Programmatic dependent launch: the CTAs of this step start (shot tables
+  // into shared memory, barriers) as the previous kernel's CTAs retire, and
+  // wait in the kernel before touching its results.
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = t2_smem_bytes<ADJ>();
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, k_bstep2d_t<ADJ>, t, s_off, n_tiles);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
@@ -691,6 +705,9 @@ __global__ void k_counter_add(int *counter, int add) {
 // term = (((v2r * trace(it)) * wz) * wx) * wy (Injection.f90:151-456,
 // 561-591); the step kernel adds a cell's terms in entry order.
 __global__ void k_bterms(BatchTables t, int s_off) {
+  // The previous step kernel still reads the terms this kernel overwrites.
+  pdl_wait();
+  pdl_launch_dependents();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= t.term_start[t.nshots]) return;
   const int b = find_shot(t.term_start, t.nshots, q);
@@ -717,7 +734,17 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     ++nl;
   }
   if (n_term > 0) {
-    k_bterms<<<(n_term + 255) / 256, 256, 0, s>>>(t, s_off);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((n_term + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_bterms, t, s_off);
+    if (e != cudaSuccess) return e;
     ++nl;
   }
   if (has_adj3d && n_v2u > 0 && !tile.stream3d) {

@@ -65,6 +65,14 @@ __host__ __device__ constexpr size_t t2_smem_bytes() {
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
+// Programmatic dependent launch: wait for the grids this one depends on to
+// complete (and their writes to be visible); allow the next grid in the
+// stream to start its own prologue.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
                : "memory");
@@ -625,8 +633,9 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
   unsigned long long *full = reinterpret_cast<unsigned long long *>(
       reinterpret_cast<char *>(t2_smem) + t2_smem_bytes<ADJ>() - 64);
   const int tid = threadIdx.x;
-  const int s = *t.counter + s_off;
-  // Shot table and this CTA's tile list into shared memory.
+  // Shot table and this CTA's tile list into shared memory: constant over
+  // the run, so this overlaps the end of the previous step's kernel (the
+  // launch allows programmatic dependent launch).
   {
     const int *src = reinterpret_cast<const int *>(t.t2shots);
     int *dst = reinterpret_cast<int *>(shots);
@@ -641,6 +650,11 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       *abort_flag = 0;
     }
   }
+  // Everything after this reads what the previous kernels of the step
+  // sequence wrote (fields, injection terms, the step counter).
+  pdl_wait();
+  pdl_launch_dependents();
+  const int s = *t.counter + s_off;
   __syncthreads();
   if (tid < t.nshots) steps[tid] = t2_step_of<ADJ>(t, shots[tid], tid, s);
   __syncthreads();

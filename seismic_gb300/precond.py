@@ -266,11 +266,25 @@ def run_study(ctx, train_seeds=tuple(range(1000, 1016)), test_seeds=(4, 5, 6), e
             hp = plain_fwi(ctx, sv, target=0.0, max_evals=max_evals)
             tgt = min(hp.misfit)
             ep = 1 + int(np.argmax(np.array(hp.misfit) <= tgt))
-            hl = learned_fwi(ctx, sv, net, scale, target=tgt, max_evals=max_evals,
+            # The learned run goes the full max_evals so that both curves can
+            # be read at every misfit level.
+            hl = learned_fwi(ctx, sv, net, scale, target=0.0, max_evals=max_evals,
                              **(learned_kw or {}))
             reached = min(hl.misfit) <= tgt
             el = (1 + int(np.argmax(np.array(hl.misfit) <= tgt))) if reached else None
+
+            def evals_to(curve, level):
+                c = np.array(curve)
+                return 1 + int(np.argmax(c <= level)) if (c <= level).any() else None
+
+            levels = []
+            for lv in (0.5, 0.3, 0.2, 0.1, 0.05, 0.02, 0.01):
+                a, b = evals_to(hp.misfit, lv), evals_to(hl.misfit, lv)
+                levels.append({"rel_misfit": lv, "plain_solves": 2 * nshot * a if a else None,
+                               "learned_solves": 2 * nshot * b if b else None,
+                               "ratio": (a / b) if (a and b) else None})
             rows.append({
+                "solves_to_level": levels,
                 "seed": sd, "target_rel_misfit": tgt,
                 "plain_solves": 2 * nshot * ep,
                 "learned_solves": (2 * nshot * el) if el else None,

@@ -135,10 +135,10 @@ def test_bad_params_are_rejected(ctx):
         ctx.modeling(g, vel, sou, w, rec)
     assert e.value.code == sw.SW_BAD_PARAM
     g, vel, sou, rec, w = case2d(nt=10)
-    g.surf_type = 1
+    g.surf_type = -1
     with pytest.raises(sw.SwaveError) as e:
         ctx.modeling(g, vel, sou, w, rec)
-    assert e.value.code == sw.SW_UNSUPPORTED
+    assert e.value.code == sw.SW_BAD_PARAM
     g, vel, sou, rec, w = case2d(nt=10)
     bad = sou.copy()
     bad[1] = -1000.0   # footprint outside the compute domain
