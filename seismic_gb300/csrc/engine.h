@@ -20,6 +20,10 @@ struct RunOpts {
   bool use_graph = true;
   bool rigid = false;   // skip the Higdon boundary (exact-adjoint mode)
   swave::StepTile tile; // fused-step tile shape
+  // Return once the phase is queued: the kernels record errors in the
+  // context's "run_err" flag, which the caller zeroes before and reads after
+  // its phases (no profiling, no host outputs).
+  bool async_end = false;
 };
 
 struct sw_ctx {

@@ -468,6 +468,15 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
   std::vector<int> batch;
   std::vector<ShotBufs> bufs;
   std::vector<std::vector<float>> vhost;
+  // The phases are queued without waiting for each other: the host builds
+  // the next phase's plans (the backward pass's receiver injection plan is
+  // the large one) while the device runs the previous phase.  Errors of the
+  // step kernels collect in the run_err flag, read once at the end.
+  RunOpts opts = c->run_opts;
+  opts.async_end = true;
+  int *rerr = (int *)dbuf(c, "run_err", sizeof(int), &st);
+  if (!rerr) return st;
+  SW_CK(cudaMemsetAsync(rerr, 0, sizeof(int), s));
   while (next < end) {
     if ((st = prepare_batch(j, next, end, false, batch, bufs, vhost))) return st;
     std::vector<PhaseShot> fwd(batch.size()), bwd(batch.size());
@@ -495,8 +504,8 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
       R.io.illum_dev = B.illum;
     }
     const uint64_t p0 = c->stats.points_updated;
-    if ((st = run_phases(c, fwd, c->run_opts))) return st;
-    if ((st = run_phases(c, bwd, c->run_opts))) return st;
+    if ((st = run_phases(c, fwd, opts))) return st;
+    if ((st = run_phases(c, bwd, opts))) return st;
     j->points += c->stats.points_updated - p0;
     // mod_copy_image, shots in order.
     for (size_t q = 0; q < batch.size(); ++q) {
@@ -508,7 +517,12 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
       c->stats.launches_total++;
     }
   }
+  int herr = 0;
+  SW_CK(cudaMemcpyAsync(&herr, rerr, sizeof(int), cudaMemcpyDeviceToHost, s));
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "rtm job");
+  if (herr)
+    return fail(c, SW_CUDA_ERR, "step kernel gave up waiting for a tile copy (error flags %d)",
+                herr);
   return SW_OK;
 }
 

@@ -439,8 +439,18 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                           s));
   }
   SW_CK(cudaMemsetAsync(counter, 0, sizeof(int), s));
+  // A queued (asynchronous) phase records its errors in the context's
+  // run_err flag, which outlives it; a synchronous one in the arena.
+  bool async = opt.async_end && !c->profiling;
+  for (int b = 0; b < nb && async; ++b)
+    if (shots[b].io.final_u2_host || shots[b].io.save_state) async = false;
   int *derr = carve<int>(cur, 1);
-  SW_CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+  if (async) {
+    derr = (int *)dbuf(c, "run_err", sizeof(int), &st);
+    if (!derr) return st;
+  } else {
+    SW_CK(cudaMemsetAsync(derr, 0, sizeof(int), s));
+  }
   if ((size_t)(cur - arena) > bytes) return fail(c, SW_CUDA_ERR, "arena overflow");
   BatchTables t;
   t.nshots = nb;
@@ -459,8 +469,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.t3maps = dmaps3;
   t.err = derr;
   t.counter = counter;
-  // The host plans above must stay alive until the uploads complete.
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch setup");
+  // The host plans above must stay alive until the uploads complete.  Copies
+  // from pageable memory are staged before cudaMemcpyAsync returns, so a
+  // queued phase need not wait here (the previous phase keeps running).
+  if (!async && (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_fail(c, e, "batch setup");
 
   const int n_term = term[nb];
   const int n_tiles = step_tiles[nb], n_rec = rec_start[nb], n_hz = hz[nb], n_hx = hx[nb],
@@ -636,6 +649,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                           (size_t)G[b].n2p * G[b].n3p, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) return cuda_fail(c, e, "download u2");
   }
+  if (async) return SW_OK;
   int herr = 0;
   SW_CK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch run");
