@@ -115,15 +115,6 @@ __device__ __forceinline__ void tma_2d(float *dst, const CUtensorMap *map, int x
       : "memory");
 }
 
-// L2 prefetch of a tensor box (no shared-memory destination, no barrier):
-// the later tensor copy of the same box then reads L2.
-__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap *map, int x, int y) {
-  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
-                   reinterpret_cast<unsigned long long>(map)),
-               "r"(x), "r"(y)
-               : "memory");
-}
-
 __device__ __forceinline__ int t2_b(int e) { return e >> 24; }
 __device__ __forceinline__ int t2_tzi(int e) { return (e >> 12) & 0xfff; }
 __device__ __forceinline__ int t2_txi(int e) { return e & 0xfff; }
@@ -155,19 +146,6 @@ __device__ __forceinline__ void t2_issue(const T2Maps &M, const T2Shot &h, int s
   tma_2d(cst + T2_CORE, &M.m[2 * ((s + 1) % 5) + 1], zi + 4, xi + 4, bar);
   tma_2d(cst + 2 * T2_CORE, &M.m[2 * (s % 5) + 1], zi + 4, xi + 4, bar);
   if (!ADJ) tma_2d(cst + 3 * T2_CORE, &M.m[11], zi + 4, xi + 4, bar);
-}
-
-// The boxes of t2_issue, prefetched into L2 two tiles ahead of the compute
-// so that each CTA keeps two tiles of DRAM reads in flight.
-template <bool ADJ>
-__device__ __forceinline__ void t2_prefetch(const T2Maps &M, const T2Shot &h, int s, int e) {
-  const int zi = t2_tzi(e) * T2_Z - h.off1, xi = t2_txi(e) * T2_X - h.off2;
-  tma_prefetch_2d(&M.m[2 * ((s + 3) % 5)], zi, xi);
-  if (ADJ) tma_prefetch_2d(&M.m[10], zi, xi);
-  tma_prefetch_2d(&M.m[2 * ((s + 2) % 5) + 1], zi + 4, xi + 4);
-  tma_prefetch_2d(&M.m[2 * ((s + 1) % 5) + 1], zi + 4, xi + 4);
-  tma_prefetch_2d(&M.m[2 * (s % 5) + 1], zi + 4, xi + 4);
-  if (!ADJ) tma_prefetch_2d(&M.m[11], zi + 4, xi + 4);
 }
 
 __device__ __forceinline__ float f4get(const float4 &a, int e) {
@@ -700,8 +678,6 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     if (tid == 0 && k + 1 < n)
       t2_issue<ADJ>(t.t2maps[t2_b(list[k + 1])], shots[t2_b(list[k + 1])], s, list[k + 1],
                     t2_smem + (cur ^ 1) * SF, &full[cur ^ 1]);
-    if (tid == 0 && k + 2 < n)
-      t2_prefetch<ADJ>(t.t2maps[t2_b(list[k + 2])], shots[t2_b(list[k + 2])], s, list[k + 2]);
     const int e = list[k];
     const T2Shot &h = shots[t2_b(e)];
     const T2Step &stp = steps[t2_b(e)];
