@@ -305,7 +305,20 @@ typedef struct sw_fwi_desc {
    *          memory (ntsnap/K) x 4 padded fields + (K + 2) snapshots, one
    *          extra forward propagation; results identical to store-all. */
   int checkpoint_snaps;
+  /* Data norm of the misfit and its adjoint source (invparam%dat_nrm_type,
+   * Inversion_types.f90:61-68; fct_compute / gdt_compute,
+   * libs/libinv/Norm.f90:12-141): SW_NRM_L2 (also 0), SW_NRM_L1,
+   * SW_NRM_HUBER, SW_NRM_CAUCHY, SW_NRM_HYPERBOLIC.  dat_thresh is
+   * data_threshold; when it is 0 the threshold of a shot is max|r| of the
+   * first of its traces whose muted residual r is not all zero
+   * (Norm.f90:37-40 resets the caller's threshold, which the following
+   * traces of the gather then use). */
+  int dat_nrm_type;
+  float dat_thresh;
 } sw_fwi_desc;
+
+enum { SW_NRM_L1 = 1, SW_NRM_L2 = 2, SW_NRM_CAUCHY = 3, SW_NRM_HYPERBOLIC = 4,
+       SW_NRM_HUBER = 12 };
 
 /* compute_fct_gdt (compute_function_gradient.f90:208-350): for every shot
  * window + pad the model, AMOD (forward, nearest-node extraction,

@@ -60,6 +60,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                             C.c_int, C.c_int],
         "oracle_vel_check": [g, _fp, _fp, _fp],
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
+        "oracle_data_norm": [C.c_int, C.c_float, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _dp],
         "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],
         "oracle_stencil_f64": [g, C.c_int, _dp, _dp, _dp],
         "oracle_stencil_rho_f64": [g, _dp, _dp, _dp, _dp],
@@ -215,6 +216,22 @@ def fwi_fct_gdt(desc, vel, wavelet, shots, vpmask=None):
     _chk(lib.oracle_fwi_fct_gdt(C.byref(desc), pv, pw, len(shots), arr, pm, C.byref(f),
                                 grad.ctypes.data_as(_fp), illum.ctypes.data_as(_fp)), "fwi")
     return f.value, grad, illum
+
+
+def data_norm(ntype, thresh, dobs, dmod, mute=None):
+    """Compute_OF_RES_ADJ of one gather: returns (misfit, adjoint source,
+    residual) for (nrec, nt) float32 traces."""
+    lib = load()
+    dobs = np.ascontiguousarray(dobs, np.float32)
+    adj = np.array(dmod, np.float32, copy=True, order="C")
+    res = np.zeros_like(adj)
+    nrec, nt = adj.shape
+    mu, pmu = (_f(mute) if mute is not None else (None, None))
+    f = C.c_double()
+    _chk(lib.oracle_data_norm(int(ntype), float(thresh), nrec, nt, dobs.ctypes.data_as(_fp), pmu,
+                              adj.ctypes.data_as(_fp), res.ctypes.data_as(_fp), C.byref(f)),
+         "data_norm")
+    return f.value, adj, res
 
 
 def rtm_job(model, vel, wavelet, shots, aperture_x=0.0, aperture_y=0.0):

@@ -97,6 +97,13 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel,
                        const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum);
 
+/* Compute_OF_RES_ADJ of one gather (Objective_Function_Residual_Adjsource.f90:
+ * 17-40 with libs/libinv/Norm.f90): dmod holds the nrec*nt modelled traces
+ * and receives the adjoint source; resid (optional) the muted residual;
+ * *f the gather's misfit.  ntype is SW_NRM_* (0 = L2). */
+int oracle_data_norm(int ntype, float thresh, int nrec, int nt, const float *dobs,
+                     const float *mute, float *dmod, float *resid, double *f);
+
 /* Multi-shot RTM stacking, same meaning as sw_rtm_job_* run over all shots. */
 int oracle_rtm_job(const sw_genpar *model, float apx, float apy, const float *vel,
                    const float *wavelet, int nshot, const sw_shot *shots, float *image,

@@ -1335,12 +1335,99 @@ static int rtm_job(const sw_genpar &M, float apx, float apy, const float *vel,
   return SW_OK;
 }
 
+// fct_compute (libs/libinv/Norm.f90:12-81) of one trace rd[0..n): L2 as an
+// FP64 sum of FP64 products, the other norms as FP32 sums in sample order
+// (sum() of a real array).  thresh is the caller's threshold: when it is 0
+// the thresholded norms set it to max|rd| (Norm.f90:37-40), and the caller
+// keeps that value for its next traces.
+static double norm_fct(int ntype, const float *rd, int n, float &thresh) {
+  if (ntype == SW_NRM_L2) {
+    double s = 0.;
+    for (int t = 0; t < n; ++t) s = s + (double)rd[t] * (double)rd[t];
+    return s / 2;
+  }
+  if (ntype == SW_NRM_L1) {
+    float s = 0.f;
+    for (int t = 0; t < n; ++t) s = s + std::fabs(rd[t]);
+    return (double)s;
+  }
+  if (thresh == 0.f) {
+    float mx = 0.f;
+    for (int t = 0; t < n; ++t) mx = std::fmax(mx, std::fabs(rd[t]));
+    thresh = mx;
+  }
+  const float g = thresh;
+  float s = 0.f;
+  for (int t = 0; t < n; ++t) {
+    float v;
+    if (ntype == SW_NRM_HUBER) {
+      const float a = std::fabs(rd[t]);
+      v = a > g ? a - g / 2.0f : rd[t] * rd[t] / (2.0f * g);
+    } else if (ntype == SW_NRM_CAUCHY) {
+      const float q = rd[t] / g;
+      v = std::log(1.0f + q * q) / 2.0f;
+    } else {
+      v = std::sqrt(g * g + rd[t] * rd[t]) - g;
+    }
+    s = s + v;
+  }
+  return (double)s;
+}
+
+// gdt_compute (libs/libinv/Norm.f90:83-141): the adjoint source of one
+// trace, in place, with the threshold fct_compute left.
+static void norm_gdt(int ntype, float *rd, int n, float g) {
+  for (int t = 0; t < n; ++t) {
+    const float e = rd[t];
+    switch (ntype) {
+      case SW_NRM_L2: break;
+      case SW_NRM_L1: rd[t] = e < 0.f ? -1.f : (e > 0.f ? 1.f : 0.f); break;
+      case SW_NRM_HUBER: rd[t] = std::fmax(-1.0f, std::fmin(1.0f, e / g)); break;
+      case SW_NRM_CAUCHY: rd[t] = e / (g * g + e * e); break;
+      default: rd[t] = (e / g) / std::sqrt(1.0f + e * e / (g * g)); break;
+    }
+  }
+}
+
+// Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40) of
+// one gather: dmod (modelled traces in, adjoint source out), the residual
+// m*(dobs - dmod) into resid when given; every trace's misfit is added to
+// the running total f in trace order.  The threshold starts from
+// data_threshold for every gather.
+static void residual_gather(int ntype, float thresh0, int nrec, int nt, const float *dobs,
+                            const float *mute, float *dmod, float *resid, double &f) {
+  float thresh = thresh0;
+  for (int r = 0; r < nrec; ++r) {
+    float *dm = &dmod[(size_t)r * nt];
+    const float *dob = &dobs[(size_t)r * nt];
+    const float *mu = mute ? &mute[(size_t)r * nt] : nullptr;
+    for (int t = 0; t < nt; ++t) {
+      const float m = mu ? mu[t] : 1.f;
+      dm[t] = m * (dob[t] - dm[t]);
+    }
+    f = f + norm_fct(ntype, dm, nt, thresh);
+    if (resid) std::memcpy(&resid[(size_t)r * nt], dm, sizeof(float) * nt);
+    for (int t = 0; t < nt; ++t) {
+      const float m = mu ? mu[t] : 1.f;
+      dm[t] = m * dm[t];
+    }
+    norm_gdt(ntype, dm, nt, thresh);
+  }
+}
+
+static bool known_norm(int ntype) {
+  return ntype == SW_NRM_L1 || ntype == SW_NRM_L2 || ntype == SW_NRM_HUBER ||
+         ntype == SW_NRM_CAUCHY || ntype == SW_NRM_HYPERBOLIC;
+}
+
 static int fwi_fct_gdt(const sw_fwi_desc &d, const float *vel, const float *wavelet,
                        int nshot, const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum_out) {
   const sw_genpar &G = d.g;
   const size_t nfull = (size_t)G.nz * G.nx * G.ny;
   const int nt = G.nt;
+  const int ntype = d.dat_nrm_type == 0 ? SW_NRM_L2 : d.dat_nrm_type;
+  if (!known_norm(ntype)) return SW_BAD_PARAM;
   std::vector<float> gradacc(nfull, 0.f), illacc(nfull, 0.f);
   double fsum = 0.;
   long ntotaltraces = 0;
@@ -1373,25 +1460,7 @@ static int fwi_fct_gdt(const sw_fwi_desc &d, const float *vel, const float *wave
     io.wave = wave.data();
     st = propagate<float>(a, io);
     if (st) return st;
-    // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40),
-    // L2 norm (libs/libinv/Norm.f90:26-28,95-97).
-    for (int r = 0; r < s.nrec; ++r) {
-      float *dm = &dmod[(size_t)r * nt];
-      const float *dob = &s.dobs[(size_t)r * nt];
-      const float *mu = s.mute ? &s.mute[(size_t)r * nt] : nullptr;
-      double ssum = 0.;
-      for (int t = 0; t < nt; ++t) {
-        const float m = mu ? mu[t] : 1.f;
-        dm[t] = m * (dob[t] - dm[t]);
-        ssum = ssum + (double)dm[t] * (double)dm[t];
-      }
-      fsum = fsum + ssum / 2;
-      if (s.resid) std::memcpy(&s.resid[(size_t)r * nt], dm, sizeof(float) * nt);
-      for (int t = 0; t < nt; ++t) {
-        const float m = mu ? mu[t] : 1.f;
-        dm[t] = m * dm[t];
-      }
-    }
+    residual_gather(ntype, d.dat_thresh, s.nrec, nt, s.dobs, s.mute, dmod.data(), s.resid, fsum);
     ntotaltraces += s.nrec;
     // AGRAD_to_memory (progs/afwi/to_disk_to_memory_AGRAD.f90:27-79).
     std::vector<float> ims(nw, 0.f), ils(nw, 0.f);
@@ -2079,6 +2148,15 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel, const float *wave
                        int nshot, const sw_fwi_shot *shots, const float *vpmask,
                        double *f, float *grad, float *illum) {
   return fwi_fct_gdt(*d, vel, wavelet, nshot, shots, vpmask, f, grad, illum);
+}
+
+int oracle_data_norm(int ntype, float thresh, int nrec, int nt, const float *dobs,
+                     const float *mute, float *dmod, float *resid, double *f) {
+  if (ntype == 0) ntype = SW_NRM_L2;
+  if (!known_norm(ntype) || nrec < 0 || nt < 0 || !f) return SW_BAD_PARAM;
+  *f = 0.;
+  residual_gather(ntype, thresh, nrec, nt, dobs, mute, dmod, resid, *f);
+  return SW_OK;
 }
 
 int oracle_rtm_job(const sw_genpar *model, float apx, float apy, const float *vel,

@@ -28,6 +28,8 @@ FD_FORWARD, FD_ADJOINT = 0, 1
 INJ_NONE, INJ_SINC, INJ_SIMPLE, INJ_LSRTM_SINC = 0, 1, 2, 3
 EXT_NONE, EXT_SINC, EXT_SIMPLE_AFWI, EXT_LSRTM_SINC, EXT_SINC_AFWI = 0, 1, 2, 3, 4
 IMG_NONE, IMG_RTM, IMG_LSRTM, IMG_AFWI, IMG_BORN = 0, 1, 2, 3, 4
+# Data norms (invparam%dat_nrm_type).
+NRM_L1, NRM_L2, NRM_CAUCHY, NRM_HYPERBOLIC, NRM_HUBER = 1, 2, 3, 4, 12
 
 
 class SwGenpar(C.Structure):
@@ -66,7 +68,8 @@ class SwFwiDesc(C.Structure):
     _fields_ = [("g", SwGenpar), ("aperture_x", C.c_float), ("aperture_y", C.c_float),
                 ("illu_pow", C.c_float), ("smooth_rect1", C.c_int), ("smooth_rect2", C.c_int),
                 ("smooth_rect3", C.c_int), ("smooth_doz", C.c_int), ("smooth_dox", C.c_int),
-                ("smooth_doy", C.c_int), ("checkpoint_snaps", C.c_int)]
+                ("smooth_doy", C.c_int), ("checkpoint_snaps", C.c_int),
+                ("dat_nrm_type", C.c_int), ("dat_thresh", C.c_float)]
 
 
 class SwWindow(C.Structure):

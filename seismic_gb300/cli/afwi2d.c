@@ -23,8 +23,9 @@
  *     illu_pow, vpmask=).  inv= receives the final model after Freeze and
  *     ApplyMask; model=, gradient=, function= and residual= (when given)
  *     receive every iteration's model, gradient, scaled misfit and residual
- *     traces.  Only data_nrm_type=L2norm is built; wantreg/wantlog (sparse
- *     regularisation) are not.
+ *     traces.  data_nrm_type (L2norm, L1norm, Huber, Cauchy) and
+ *     data_threshold select the data norm; wantreg/wantlog (sparse
+ *     regularisation) are not built.
  */
 #include <math.h>
 #include <stdio.h>
@@ -132,7 +133,14 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
   sep_par_float("illu_pow", &illu_pow);
   sep_par_str("data_nrm_type", nrm, sizeof(nrm));
   if (wantreg || wantlog) cli_fail("wantreg/wantlog: sparse regularisation is not built in swave");
-  if (strncmp(nrm, "L2nor", 5) != 0) cli_fail("data_nrm_type=%s: only L2norm is built", nrm);
+  float dat_thresh = 0.f;
+  sep_par_float("data_threshold", &dat_thresh);
+  int nrm_type = 0;
+  if (strncmp(nrm, "Cauch", 5) == 0) nrm_type = SW_NRM_CAUCHY;
+  if (strncmp(nrm, "Huber", 5) == 0) nrm_type = SW_NRM_HUBER;
+  if (strncmp(nrm, "L1nor", 5) == 0) nrm_type = SW_NRM_L1;
+  if (strncmp(nrm, "L2nor", 5) == 0) nrm_type = SW_NRM_L2;
+  if (!nrm_type) cli_fail("data_nrm_type=%s is not L2norm, L1norm, Huber or Cauchy", nrm);
   /* Init_BandPassParam + BandpassSouTraces (Bandpass.f90:26-87). */
   float fhi = 20.f, flo = 0.f;
   int nphi = 14, nplo = 14, phase = 0;
@@ -173,6 +181,8 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
   desc.smooth_doy = !(wavey <= g->dy || wavey == 0.f);
   desc.checkpoint_snaps = 0;
   sep_par_int("checkpoint_snaps", &desc.checkpoint_snaps);
+  desc.dat_nrm_type = nrm_type;
+  desc.dat_thresh = dat_thresh;
   /* Init_Inversion_Array (Inversion_types.f90:106-134). */
   double *vpinit = (double *)malloc(n * sizeof(double));
   float *vpmask = (float *)malloc(n * 4);

@@ -237,6 +237,10 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
   const sw_genpar &G = d.g;
   int st = check_genpar(c, G);
   if (st) return st;
+  const int ntype = d.dat_nrm_type == 0 ? SW_NRM_L2 : d.dat_nrm_type;
+  if (ntype != SW_NRM_L1 && ntype != SW_NRM_L2 && ntype != SW_NRM_HUBER &&
+      ntype != SW_NRM_CAUCHY && ntype != SW_NRM_HYPERBOLIC)
+    return fail(c, SW_BAD_PARAM, "dat_nrm_type %d is not a data norm", d.dat_nrm_type);
   cudaStream_t s = c->stream;
   cudaError_t e;
   const long long nfull = (long long)G.nz * G.nx * G.ny;
@@ -341,10 +345,19 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     }
     double *dpart = (double *)dbuf(c, "fpart", (size_t)sh.nrec * sizeof(double), &st);
     if (!dpart) return st;
-    if ((e = launch_residual(sh.nrec, nt, ddobs, dmute, a.rec_trace_dev, dres, dpart, s)) !=
-        cudaSuccess)
-      return cuda_fail(c, e, "residual");
-    c->stats.launches_total++;
+    if (ntype == SW_NRM_L2) {
+      if ((e = launch_residual(sh.nrec, nt, ddobs, dmute, a.rec_trace_dev, dres, dpart, s)) !=
+          cudaSuccess)
+        return cuda_fail(c, e, "residual");
+      c->stats.launches_total++;
+    } else {
+      float *dmax = (float *)dbuf(c, "fmaxabs", (size_t)sh.nrec * sizeof(float), &st);
+      if (!dmax) return st;
+      if ((e = launch_residual_nrm(ntype, d.dat_thresh, sh.nrec, nt, ddobs, dmute,
+                                   a.rec_trace_dev, dres, dpart, dmax, s)) != cudaSuccess)
+        return cuda_fail(c, e, "residual");
+      c->stats.launches_total += (ntype != SW_NRM_L1 && d.dat_thresh == 0.f) ? 2 : 1;
+    }
     part.resize(sh.nrec);
     if ((st = download(c, part.data(), dpart, (size_t)sh.nrec * sizeof(double)))) return st;
     if (sh.resid && (st = download(c, sh.resid, dres, (size_t)sh.nrec * nt * sizeof(float)))) return st;

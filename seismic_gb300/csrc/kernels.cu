@@ -3,6 +3,7 @@
 // Each kernel restates one reference loop nest with the same floating-point
 // operation order; the comments give the reference file:line.  Paths are
 // relative to the reference project root.
+#include "../../include/swave.h"
 #include "swave_dev.cuh"
 
 namespace swave {
@@ -140,6 +141,80 @@ __global__ void k_residual(int nrec, int nt, const float *__restrict__ dobs,
     dmod[o + t] = m * d;
   }
   partial[r] = ssum / 2;
+}
+
+// max|m*(dobs - dmod)| of every trace: the threshold fct_compute takes when
+// data_threshold is 0 (Norm.f90:37-40).
+__global__ void k_trace_maxabs(int nrec, int nt, const float *__restrict__ dobs,
+                               const float *__restrict__ mute, const float *__restrict__ dmod,
+                               float *maxabs) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  const long long o = (long long)r * nt;
+  float mx = 0.0f;
+  for (int t = 0; t < nt; ++t) {
+    const float m = mute ? mute[o + t] : 1.0f;
+    mx = fmaxf(mx, fabsf(m * (dobs[o + t] - dmod[o + t])));
+  }
+  maxabs[r] = mx;
+}
+
+// Compute_OF_RES_ADJ for the L1, Huber, Cauchy and hyperbolic norms
+// (Objective_Function_Residual_Adjsource.f90:32-38 with fct_compute and
+// gdt_compute, libs/libinv/Norm.f90:12-141): one thread per trace, the
+// trace's misfit summed in FP32 in sample order like the reference's
+// sum() of a real array.  Trace r's threshold is thresh0, or, when that is
+// 0, max|r| of the first trace k <= r whose maximum is not 0 (the caller's
+// threshold is reset by the first such trace and kept by the following
+// ones); with no such trace it stays 0, as in the reference.
+__global__ void k_residual_nrm(int ntype, int nrec, int nt, const float *__restrict__ dobs,
+                               const float *__restrict__ mute, float *dmod, float *resid,
+                               double *partial, float thresh0, const float *__restrict__ maxabs) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  float g = thresh0;
+  if (g == 0.0f && maxabs) {
+    for (int k = 0; k <= r; ++k)
+      if (maxabs[k] != 0.0f) {
+        g = maxabs[k];
+        break;
+      }
+  }
+  const long long o = (long long)r * nt;
+  float fs = 0.0f;
+  for (int t = 0; t < nt; ++t) {
+    const float m = mute ? mute[o + t] : 1.0f;
+    const float d = m * (dobs[o + t] - dmod[o + t]);
+    if (resid) resid[o + t] = d;
+    const float e = m * d;
+    float v, a;
+    switch (ntype) {
+      case SW_NRM_L1:
+        v = fabsf(d);
+        a = e < 0.0f ? -1.0f : (e > 0.0f ? 1.0f : 0.0f);
+        break;
+      case SW_NRM_HUBER: {
+        const float ad = fabsf(d);
+        v = ad > g ? ad - g / 2.0f : d * d / (2.0f * g);
+        a = fmaxf(-1.0f, fminf(1.0f, e / g));
+        break;
+      }
+      case SW_NRM_CAUCHY: {
+        const float q = d / g;
+        v = logf(1.0f + q * q) / 2.0f;
+        a = e / (g * g + e * e);
+        break;
+      }
+      default: {  // SW_NRM_HYPERBOLIC
+        v = sqrtf(g * g + d * d) - g;
+        a = (e / g) / sqrtf(1.0f + e * e / (g * g));
+        break;
+      }
+    }
+    fs = fs + v;
+    dmod[o + t] = a;
+  }
+  partial[r] = (double)fs;
 }
 
 // ---------------------------------------------------------------------------
@@ -326,6 +401,17 @@ cudaError_t launch_copy_image(int nz, int nx, int ny, float ox, float oy, float 
 cudaError_t launch_residual(int nrec, int nt, const float *dobs, const float *mute, float *dmod,
                             float *resid, double *partial, cudaStream_t s) {
   k_residual<<<(nrec + 127) / 128, 128, 0, s>>>(nrec, nt, dobs, mute, dmod, resid, partial);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_residual_nrm(int ntype, float thresh, int nrec, int nt, const float *dobs,
+                                const float *mute, float *dmod, float *resid, double *partial,
+                                float *maxabs, cudaStream_t s) {
+  const bool need_max = ntype != SW_NRM_L1 && thresh == 0.0f;
+  if (need_max)
+    k_trace_maxabs<<<(nrec + 127) / 128, 128, 0, s>>>(nrec, nt, dobs, mute, dmod, maxabs);
+  k_residual_nrm<<<(nrec + 127) / 128, 128, 0, s>>>(ntype, nrec, nt, dobs, mute, dmod, resid,
+                                                    partial, thresh, need_max ? maxabs : nullptr);
   return cudaGetLastError();
 }
 

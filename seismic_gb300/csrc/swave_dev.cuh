@@ -74,5 +74,11 @@ cudaError_t launch_copy_image(int nz, int nx, int ny, float ox, float oy, float 
                               const float *ils, float *image, float *illum, cudaStream_t s);
 cudaError_t launch_residual(int nrec, int nt, const float *dobs, const float *mute,
                             float *dmod, float *resid, double *partial, cudaStream_t s);
+// The L1 / Huber / Cauchy / hyperbolic residual (SW_NRM_*); maxabs holds
+// nrec floats of scratch.  Launches 2 kernels when a threshold is searched
+// for, else 1.
+cudaError_t launch_residual_nrm(int ntype, float thresh, int nrec, int nt, const float *dobs,
+                                const float *mute, float *dmod, float *resid, double *partial,
+                                float *maxabs, cudaStream_t s);
 
 }  // namespace swave

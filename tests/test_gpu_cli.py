@@ -278,18 +278,21 @@ def _inv_survey(tmp_path, built, nt=400):
     return common, v0.astype(np.float32), w, keys
 
 
-def test_afwi_program_task_inv(built, tmp_path):
+@pytest.mark.parametrize("nrm", [("L2norm", 0.0), ("Huber", 0.0), ("L1norm", 0.0)])
+def test_afwi_program_task_inv(built, tmp_path, nrm):
     """Task=INV against the same l_bfgs loop written here over the Python
     API (band-pass, mute masks, smoothing radii, sw_fwi_fct_gdt, device
     L-BFGS): the final model and the misfit history agree bit for bit, and
-    the misfit falls."""
+    the misfit falls; with the L2, Huber and L1 data norms."""
     common, v0, w, keys = _inv_survey(tmp_path, built)
     obs, _ = sep.read(str(tmp_path / "obs.H"))
     niter = 3
+    nrm_name, thresh = nrm
     _run(built, "2DAFWI.x", dict(common, vel=tmp_path / "v0.H", Task="INV",
                                  traces=tmp_path / "obs.H", niter=niter, vpmin=1500,
                                  vpmax=2600, inv=tmp_path / "inv.H",
-                                 function=tmp_path / "f.H", model=tmp_path / "m.H"))
+                                 function=tmp_path / "f.H", model=tmp_path / "m.H",
+                                 data_nrm_type=nrm_name, data_threshold=thresh))
     inv, h = sep.read(str(tmp_path / "inv.H"))
     fun, _ = sep.read(str(tmp_path / "f.H"))
     models, hm = sep.read(str(tmp_path / "m.H"))
@@ -312,6 +315,9 @@ def test_afwi_program_task_inv(built, tmp_path):
         desc.smooth_rect1, desc.smooth_rect2, desc.smooth_rect3 = r, r, int((0 + 1.5) / 2)
         desc.smooth_doz = desc.smooth_dox = int(not wave <= 10.0)
         desc.smooth_doy = 0
+        desc.dat_nrm_type = {"L2norm": sw.NRM_L2, "Huber": sw.NRM_HUBER,
+                             "L1norm": sw.NRM_L1}[nrm_name]
+        desc.dat_thresh = thresh
         shots, row = [], 0
         for sx in (200.0, 450.0, 700.0):
             sel = keys[:, 0] == sx

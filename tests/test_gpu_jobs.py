@@ -100,6 +100,38 @@ def test_fwi_fct_gdt_matches_oracle(ctx, oracle):
     assert rel_l2(illum, rillum) < 1e-6
 
 
+@pytest.mark.parametrize("ntype", [sw.NRM_L1, sw.NRM_HUBER, sw.NRM_CAUCHY, sw.NRM_HYPERBOLIC])
+@pytest.mark.parametrize("thresh", [0.0, 0.01])
+def test_fwi_data_norms_match_oracle(ctx, oracle, ntype, thresh):
+    """The L1, Huber, Cauchy and hyperbolic misfits and adjoint sources
+    (Norm.f90) with data_threshold 0 (each gather's threshold from its first
+    live trace) and a fixed one: residuals bit-exact, misfit bit-exact except
+    Cauchy, whose FP32 log is CUDA's logf against the C library's (1e-6)."""
+    d, vel, w, shots, mask = _fwi_case()
+    d.dat_nrm_type, d.dat_thresh = ntype, thresh
+    f, grad, illum, gres = ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask, want_resid=True)
+    for s in shots:
+        s["resid"] = np.zeros(s["dobs"].shape, np.float32)
+    rf, rgrad, rillum = oracle.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    for s, r in zip(shots, gres):
+        np.testing.assert_array_equal(r, s["resid"])
+    assert rf > 0
+    if ntype == sw.NRM_CAUCHY:
+        assert abs(f - rf) <= 1e-6 * rf
+    else:
+        assert f == rf
+    assert rel_l2(grad, rgrad) < 1e-6
+    assert rel_l2(illum, rillum) < 1e-6
+
+
+def test_fwi_bad_norm_is_refused(ctx):
+    d, vel, w, shots, mask = _fwi_case()
+    d.dat_nrm_type = 5
+    with pytest.raises(sw.SwaveError) as e:
+        ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    assert e.value.code == sw.SW_BAD_PARAM
+
+
 @pytest.mark.parametrize("K", [2, 3, 7])
 def test_fwi_checkpointed_equals_store_all(ctx, K):
     """Checkpointed snapshots (state every K snapshots, K + 2 recomputed at a
