@@ -330,6 +330,50 @@ int sw_fwi_fct_gdt(sw_ctx *ctx, const sw_fwi_desc *d, const float *vel,
                    const float *wavelet, int nshot, const sw_fwi_shot *shots,
                    const float *vpmask, double *f, float *grad, float *illum);
 
+/* ---- Model regularisation of 2DAFWI (compute_fct_gdt_reg,
+ * progs/afwi/compute_function_gradient.f90:98-206) ----------------------
+ * wantreg: SparseRegularization_apply (libs/libwave/Sparse_regularization.
+ * f90:238-327): the model, padded by edge replication (sparse_taperz/x/y),
+ * is differenced by the helix filters 1 - Z^lag (lag 1 along z, nz+2*taperz
+ * along x; derivdy applies the x filter a second time, as the reference's
+ * helicon2_mod_lop does), weighted by Z_weights, and its norm
+ * (model_nrm_type, reg_threshold) and gradient are formed; log_z_plus keeps
+ * only the positive z differences.  wantlog: LogisticRegularization_apply
+ * (:329-397): the z difference where it is <= 0 under hinge_nrm_type and
+ * hin_threshold.  Both terms are divided by nz*nx*ny, weighted by eps and
+ * eps_log (computed at evaluation 0 from ratio / ratio_log when
+ * compute_eps / compute_eps_log) and added to f and subtracted from grad;
+ * grad is then multiplied by vpmask (always, also without
+ * regularisation).  Norms are taken, as in the reference, over the first
+ * nz*nx samples of the model and the first (nz+2*taperz)*(nx+2*taperx) of
+ * the padded differences. */
+typedef struct sw_reg_desc {
+  int nz, nx, ny;
+  int wantreg, wantlog;
+  int derivdx, derivdy, derivdz, log_z_plus;
+  int ntaperz, ntaperx, ntapery;  /* sparse_taperz/x/y (10, 10, 0); y is 0 in 2D */
+  int mod_nrm_type, hin_nrm_type; /* SW_NRM_*; model_nrm_type, hinge_nrm_type */
+  int compute_eps, compute_eps_log;
+  float ratio, ratio_log;         /* ratio (10), ratio_logistic (10)           */
+  const float *zweight;           /* Z_weights (nz*nx*ny) or NULL              */
+} sw_reg_desc;
+
+/* What compute_fct_gdt_reg keeps between evaluations: eps and eps_log
+ * (parameters eps / eps_log, default 1, or the computed values), and the
+ * norm thresholds, which fct_compute sets to max|.| when they are 0 and
+ * which then stay set. */
+typedef struct sw_reg_state {
+  float eps, eps_log;
+  float mod_thresh, hin_thresh;
+} sw_reg_state;
+
+/* f and grad hold compute_fct_gdt's misfit and gradient (nz*nx*ny) on entry
+ * and compute_fct_gdt_reg's on return; eval is invparam%eval (0 on the first
+ * evaluation).  vel is the current model, vpmask the inversion mask (NULL =
+ * ones). */
+int sw_fwi_regularize(sw_ctx *ctx, const sw_reg_desc *d, sw_reg_state *state, int eval,
+                      const float *vel, const float *vpmask, double *f, float *grad);
+
 /* ---- L-BFGS (libs/libinv/lbfgs.f:49-558, FP64 on the device) ----------
  * Reverse communication exactly like LBFGS(): the caller evaluates f and g
  * at x whenever *iflag returns 1, and calls again. */

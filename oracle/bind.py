@@ -60,6 +60,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                             C.c_int, C.c_int],
         "oracle_vel_check": [g, _fp, _fp, _fp],
         "oracle_fwi_fct_gdt": [C.POINTER(FD), _fp, _fp, C.c_int, C.POINTER(FS), _fp, _dp, _fp, _fp],
+        "oracle_fwi_regularize": [C.c_void_p, C.c_void_p, C.c_int, _fp, _fp, _dp, _fp],
         "oracle_data_norm": [C.c_int, C.c_float, C.c_int, C.c_int, _fp, _fp, _fp, _fp, _dp],
         "oracle_rtm_job": [g, C.c_float, C.c_float, _fp, _fp, C.c_int, C.c_void_p, _fp, _fp, _fp],
         "oracle_stencil_f64": [g, C.c_int, _dp, _dp, _dp],
@@ -216,6 +217,24 @@ def fwi_fct_gdt(desc, vel, wavelet, shots, vpmask=None):
     _chk(lib.oracle_fwi_fct_gdt(C.byref(desc), pv, pw, len(shots), arr, pm, C.byref(f),
                                 grad.ctypes.data_as(_fp), illum.ctypes.data_as(_fp)), "fwi")
     return f.value, grad, illum
+
+
+def fwi_regularize(desc, state, eval_, vel, f, grad, vpmask=None, zweight=None):
+    """compute_fct_gdt_reg's terms on the CPU; desc/state are the
+    seismic_gb300 SwRegDesc/SwRegState (state updated in place)."""
+    lib = load()
+    v, pv = _f(vel)
+    g = np.array(grad, np.float32, copy=True).ravel()
+    m, pm = (_f(vpmask) if vpmask is not None else (None, None))
+    zw, pz = (_f(zweight) if zweight is not None else (None, None))
+    desc.zweight = pz
+    fd = C.c_double(f)
+    try:
+        _chk(lib.oracle_fwi_regularize(C.byref(desc), C.byref(state), int(eval_), pv, pm,
+                                       C.byref(fd), g.ctypes.data_as(_fp)), "fwi_regularize")
+    finally:
+        desc.zweight = None
+    return fd.value, g
 
 
 def data_norm(ntype, thresh, dobs, dmod, mute=None):

@@ -104,6 +104,11 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel,
 int oracle_data_norm(int ntype, float thresh, int nrec, int nt, const float *dobs,
                      const float *mute, float *dmod, float *resid, double *f);
 
+/* compute_fct_gdt_reg's regularisation terms, same meaning as
+ * sw_fwi_regularize. */
+int oracle_fwi_regularize(const sw_reg_desc *d, sw_reg_state *state, int eval, const float *vel,
+                          const float *vpmask, double *f, float *grad);
+
 /* Multi-shot RTM stacking, same meaning as sw_rtm_job_* run over all shots. */
 int oracle_rtm_job(const sw_genpar *model, float apx, float apy, const float *vel,
                    const float *wavelet, int nshot, const sw_shot *shots, float *image,

@@ -2150,6 +2150,159 @@ int oracle_fwi_fct_gdt(const sw_fwi_desc *d, const float *vel, const float *wave
   return fwi_fct_gdt(*d, vel, wavelet, nshot, shots, vpmask, f, grad, illum);
 }
 
+// ---------------------------------------------------------------------------
+// Model regularisation of 2DAFWI (compute_fct_gdt_reg,
+// progs/afwi/compute_function_gradient.f90:98-206).
+// ---------------------------------------------------------------------------
+struct RegGrid {
+  int nz, nx, ny, tz, tx, ty;
+  size_t nzt() const { return (size_t)nz + 2 * tz; }
+  size_t nxt() const { return (size_t)nx + 2 * tx; }
+  size_t nyt() const { return (size_t)ny + 2 * ty; }
+  size_t ntap() const { return nzt() * nxt() * nyt(); }
+  size_t n() const { return (size_t)nz * nx * ny; }
+  // Index of model sample (iz, ix, iy) in the padded array.
+  size_t tap(int iz, int ix, int iy) const {
+    return (size_t)(iz + tz) + nzt() * ((size_t)(ix + tx) + nxt() * (size_t)(iy + ty));
+  }
+};
+
+// SparseRegularization_add_taper, forw (Sparse_regularization.f90:399-437):
+// the interior is the model, the pads repeat the edge samples (z first, then
+// x, then y, which is the clamped index on every axis).
+static void reg_pad(const RegGrid &R, const float *a, float *tap) {
+  for (size_t k = 0; k < R.nyt(); ++k)
+    for (size_t j = 0; j < R.nxt(); ++j)
+      for (size_t i = 0; i < R.nzt(); ++i) {
+        const int iz = std::min(std::max((int)i - R.tz, 0), R.nz - 1);
+        const int ix = std::min(std::max((int)j - R.tx, 0), R.nx - 1);
+        const int iy = std::min(std::max((int)k - R.ty, 0), R.ny - 1);
+        tap[i + R.nzt() * (j + R.nxt() * k)] = a[iz + (size_t)R.nz * (ix + (size_t)R.nx * iy)];
+      }
+}
+
+// helicon_mod_lop (libs/libflt/helicon.f90:25-60) with the filters that
+// SparseRegularization_filter_init builds (Sparse_regularization.f90:
+// 166-213): createhelix of the GEE helix library (not in the reference
+// tree) gives, for a 2-point box along one axis with the "1" at its first
+// point, a single lag (1 along z, nzt along x, nzt*nxt along y), and flt is
+// set to -1.  The output is cleared (adjnull), the zero lag added, then the
+// lag term, over the whole padded array as one line (the helix).
+static void helix_fwd(const float *xx, float *yy, size_t n, size_t lag) {
+  for (size_t i = 0; i < n; ++i) yy[i] = 0.f + xx[i];
+  for (size_t iy = lag; iy < n; ++iy) yy[iy] = yy[iy] + xx[iy - lag] * -1.f;
+}
+static void helix_adj(float *xx, const float *yy, size_t n, size_t lag) {
+  for (size_t i = 0; i < n; ++i) xx[i] = 0.f + yy[i];
+  for (size_t iy = lag; iy < n; ++iy) xx[iy - lag] = xx[iy - lag] + yy[iy] * -1.f;
+}
+
+// SparseRegularization_Compute_f_g (Sparse_regularization.f90:258-327) and,
+// with logistic set, LogisticRegularization_Compute_f_g (:329-397).
+static void reg_compute_f_g(const RegGrid &R, const float *zweight, const float *vel,
+                            size_t lag, bool hinge, bool logistic, int ntype, float &thresh,
+                            double &f, float *g) {
+  const size_t nt = R.ntap(), n = R.n();
+  std::vector<float> zwt(nt, 1.f), mask(nt, logistic ? 0.f : 1.f), rm(nt), rt(nt), gtmp(n, 0.f);
+  if (zweight) reg_pad(R, zweight, zwt.data());
+  reg_pad(R, vel, rt.data());
+  helix_fwd(rt.data(), rm.data(), nt, lag);
+  if (logistic) {
+    for (size_t i = 0; i < nt; ++i) mask[i] = rm[i] <= 0.f ? 1.f : 0.f;
+    for (size_t i = 0; i < nt; ++i) rm[i] = rm[i] * mask[i] * zwt[i];
+  } else {
+    if (hinge)
+      for (size_t i = 0; i < nt; ++i) mask[i] = rm[i] <= 0.f ? 0.f : 1.f;
+    for (size_t i = 0; i < nt; ++i) rm[i] = rm[i] * zwt[i] * mask[i];
+  }
+  for (int iy = 0; iy < R.ny; ++iy)
+    for (int ix = 0; ix < R.nx; ++ix)
+      for (int iz = 0; iz < R.nz; ++iz) {
+        const size_t k = iz + (size_t)R.nz * (ix + (size_t)R.nx * iy);
+        gtmp[k] = gtmp[k] + rm[R.tap(iz, ix, iy)];
+      }
+  f = f + norm_fct(ntype, gtmp.data(), R.nz * R.nx, thresh);
+  norm_gdt(ntype, rm.data(), (int)(R.nzt() * R.nxt()), thresh);
+  for (size_t i = 0; i < nt; ++i)
+    rm[i] = logistic ? mask[i] * rm[i] * zwt[i] : rm[i] * zwt[i] * mask[i];
+  helix_adj(rt.data(), rm.data(), nt, lag);
+  for (int iy = 0; iy < R.ny; ++iy)
+    for (int ix = 0; ix < R.nx; ++ix)
+      for (int iz = 0; iz < R.nz; ++iz) {
+        const size_t k = iz + (size_t)R.nz * (ix + (size_t)R.nx * iy);
+        g[k] = g[k] + (0.f + rt[R.tap(iz, ix, iy)]);
+      }
+}
+
+static int fwi_regularize(const sw_reg_desc &d, sw_reg_state &st, int eval, const float *vel,
+                          const float *vpmask, double &f, float *grad) {
+  if (d.nz < 1 || d.nx < 1 || d.ny < 1 || d.ntaperz < 0 || d.ntaperx < 0 || d.ntapery < 0)
+    return SW_BAD_PARAM;
+  const int mtype = d.mod_nrm_type == 0 ? SW_NRM_L2 : d.mod_nrm_type;
+  const int htype = d.hin_nrm_type == 0 ? SW_NRM_L2 : d.hin_nrm_type;
+  if ((d.wantreg && !known_norm(mtype)) || (d.wantlog && !known_norm(htype))) return SW_BAD_PARAM;
+  // Init_SparseRegularization (Sparse_regularization.f90:81-93): no y pad in 2D.
+  const RegGrid R{d.nz, d.nx, d.ny, d.ntaperz, d.ntaperx, d.ny != 1 ? d.ntapery : 0};
+  const size_t n = R.n();
+  const double scaling = (double)d.nx * d.ny * d.nz;
+  double ftmp = 0., ftmp1 = 0.;
+  std::vector<float> gtmp(n);
+  if (d.compute_eps && eval == 0) st.eps = 0.f;
+  if (d.compute_eps_log && eval == 0) st.eps_log = 0.f;
+  if (d.wantreg) {
+    // SparseRegularization_apply (:238-256): x, then z, then y (the x filter).
+    std::fill(gtmp.begin(), gtmp.end(), 0.f);
+    const size_t lx = R.nzt();
+    if (d.derivdx)
+      reg_compute_f_g(R, d.zweight, vel, lx, false, false, mtype, st.mod_thresh, ftmp, gtmp.data());
+    if (d.derivdz)
+      reg_compute_f_g(R, d.zweight, vel, 1, d.log_z_plus != 0, false, mtype, st.mod_thresh, ftmp,
+                      gtmp.data());
+    if (d.ny != 1 && d.derivdy)
+      reg_compute_f_g(R, d.zweight, vel, lx, false, false, mtype, st.mod_thresh, ftmp, gtmp.data());
+    ftmp = ftmp / scaling;
+    for (size_t i = 0; i < n; ++i) gtmp[i] = gtmp[i] / (float)scaling;
+    if (d.compute_eps && eval == 0) {
+      if (d.ratio == 0.f)
+        st.eps = 0.f;
+      else if (ftmp != 0.)
+        st.eps = (float)std::fabs(f / ((double)d.ratio * ftmp));
+      else
+        return SW_NUMERIC;
+    }
+    for (size_t i = 0; i < n; ++i) grad[i] = grad[i] - gtmp[i] * st.eps;
+  } else {
+    st.eps = 0.f;
+  }
+  if (d.wantlog) {
+    std::fill(gtmp.begin(), gtmp.end(), 0.f);
+    reg_compute_f_g(R, d.zweight, vel, 1, false, true, htype, st.hin_thresh, ftmp1, gtmp.data());
+    ftmp1 = ftmp1 / scaling;
+    for (size_t i = 0; i < n; ++i) gtmp[i] = gtmp[i] / (float)scaling;
+    if (d.compute_eps_log && eval == 0) {
+      if (d.ratio_log == 0.f)
+        st.eps_log = 0.f;
+      else if (ftmp1 == 0.)
+        st.eps_log = (float)std::fabs(f / ((double)d.ratio_log * ftmp));
+      else
+        st.eps_log = (float)std::fabs(f / ((double)d.ratio_log * ftmp1));
+    }
+    for (size_t i = 0; i < n; ++i) grad[i] = grad[i] - gtmp[i] * st.eps_log;
+  } else {
+    st.eps_log = 0.f;
+  }
+  if (vpmask)
+    for (size_t i = 0; i < n; ++i) grad[i] = grad[i] * vpmask[i];
+  f = f + ftmp * (double)st.eps + ftmp1 * (double)st.eps_log;
+  return SW_OK;
+}
+
+int oracle_fwi_regularize(const sw_reg_desc *d, sw_reg_state *state, int eval, const float *vel,
+                          const float *vpmask, double *f, float *grad) {
+  if (!d || !state || !vel || !f || !grad) return SW_BAD_PARAM;
+  return fwi_regularize(*d, *state, eval, vel, vpmask, *f, grad);
+}
+
 int oracle_data_norm(int ntype, float thresh, int nrec, int nt, const float *dobs,
                      const float *mute, float *dmod, float *resid, double *f) {
   if (ntype == 0) ntype = SW_NRM_L2;

@@ -72,6 +72,39 @@ class SwFwiDesc(C.Structure):
                 ("dat_nrm_type", C.c_int), ("dat_thresh", C.c_float)]
 
 
+class SwRegDesc(C.Structure):
+    """sw_reg_desc: the SparseRegParam fields of compute_fct_gdt_reg."""
+    _fields_ = [("nz", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("wantreg", C.c_int),
+                ("wantlog", C.c_int), ("derivdx", C.c_int), ("derivdy", C.c_int),
+                ("derivdz", C.c_int), ("log_z_plus", C.c_int), ("ntaperz", C.c_int),
+                ("ntaperx", C.c_int), ("ntapery", C.c_int), ("mod_nrm_type", C.c_int),
+                ("hin_nrm_type", C.c_int), ("compute_eps", C.c_int), ("compute_eps_log", C.c_int),
+                ("ratio", C.c_float), ("ratio_log", C.c_float), ("zweight", _fp)]
+
+
+class SwRegState(C.Structure):
+    _fields_ = [("eps", C.c_float), ("eps_log", C.c_float), ("mod_thresh", C.c_float),
+                ("hin_thresh", C.c_float)]
+
+
+def reg_desc(nz, nx, ny=1, wantreg=False, wantlog=False, derivdx=False, derivdy=False,
+             derivdz=False, log_z_plus=False, taperz=10, taperx=10, tapery=0,
+             model_nrm_type=NRM_CAUCHY, hinge_nrm_type=NRM_L2, compute_eps=False,
+             compute_eps_log=False, ratio=10.0, ratio_log=10.0):
+    """A sw_reg_desc with Init_SparseRegularization's defaults
+    (Sparse_regularization.f90:51-79)."""
+    d = SwRegDesc()
+    d.nz, d.nx, d.ny = nz, nx, ny
+    d.wantreg, d.wantlog = int(wantreg), int(wantlog)
+    d.derivdx, d.derivdy, d.derivdz, d.log_z_plus = map(int, (derivdx, derivdy, derivdz,
+                                                             log_z_plus))
+    d.ntaperz, d.ntaperx, d.ntapery = taperz, taperx, tapery
+    d.mod_nrm_type, d.hin_nrm_type = model_nrm_type, hinge_nrm_type
+    d.compute_eps, d.compute_eps_log = int(compute_eps), int(compute_eps_log)
+    d.ratio, d.ratio_log = ratio, ratio_log
+    return d
+
+
 class SwWindow(C.Structure):
     _fields_ = [("oxw", C.c_float), ("oyw", C.c_float), ("endx", C.c_float),
                 ("endy", C.c_float), ("nxw", C.c_int), ("nyw", C.c_int)]
@@ -118,6 +151,8 @@ _SIGS = {
     "sw_born_wavelet": (C.c_int, [_fp, C.c_int, C.c_float]),
     "sw_fwi_fct_gdt": (C.c_int, [C.c_void_p, C.POINTER(SwFwiDesc), _fp, _fp, C.c_int,
                                  C.POINTER(SwFwiShot), _fp, _dp, _fp, _fp]),
+    "sw_fwi_regularize": (C.c_int, [C.c_void_p, C.POINTER(SwRegDesc), C.POINTER(SwRegState),
+                                    C.c_int, _fp, _fp, _dp, _fp]),
     "sw_lbfgs_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, _fp,
                                   C.c_int, C.c_int, _dp, C.POINTER(C.c_void_p)]),
     "sw_lbfgs_destroy": (C.c_int, [C.c_void_p]),
@@ -370,6 +405,24 @@ class Context:
         self._check(self.lib.sw_fwi_fct_gdt(self.h, C.byref(desc), fptr(vel), fptr(w), len(shots),
                                             arr, fptr(m), C.byref(f), fptr(grad), fptr(illum)))
         return (f.value, grad, illum, resids) if want_resid else (f.value, grad, illum)
+
+    def fwi_regularize(self, desc: SwRegDesc, state: SwRegState, eval_, vel, f, grad,
+                       vpmask=None, zweight=None):
+        """compute_fct_gdt_reg's terms: returns (f, grad) after the sparse and
+        logistic regularisation and the mask; state is updated in place."""
+        vel = _f32(vel)
+        g = np.array(grad, np.float32, copy=True).ravel()
+        m = _f32(vpmask) if vpmask is not None else None
+        zw = _f32(zweight) if zweight is not None else None
+        desc.zweight = fptr(zw)
+        fd = C.c_double(f)
+        try:
+            self._check(self.lib.sw_fwi_regularize(self.h, C.byref(desc), C.byref(state),
+                                                   int(eval_), fptr(vel), fptr(m), C.byref(fd),
+                                                   fptr(g)))
+        finally:
+            desc.zweight = None
+        return fd.value, g
 
 
 def make_shots(shots) -> tuple:

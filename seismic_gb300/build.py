@@ -21,7 +21,7 @@ LIB = os.path.join(LIBDIR, "libswave.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 
-CUDA_SOURCES = ["kernels.cu", "batch.cu", "runner.cu", "engine.cu", "rtmjob.cu", "fwi.cu", "noalloc.cu", "cnn.cu"]
+CUDA_SOURCES = ["kernels.cu", "batch.cu", "runner.cu", "engine.cu", "rtmjob.cu", "fwi.cu", "noalloc.cu", "cnn.cu", "regularize.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",

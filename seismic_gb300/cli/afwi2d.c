@@ -24,8 +24,11 @@
  *     ApplyMask; model=, gradient=, function= and residual= (when given)
  *     receive every iteration's model, gradient, scaled misfit and residual
  *     traces.  data_nrm_type (L2norm, L1norm, Huber, Cauchy) and
- *     data_threshold select the data norm; wantreg/wantlog (sparse
- *     regularisation) are not built.
+ *     data_threshold select the data norm; wantreg / wantlog add the sparse
+ *     and logistic model regularisation of compute_fct_gdt_reg
+ *     (sw_fwi_regularize: derivdx/dy/dz, log_z_plus, model_nrm_type,
+ *     hinge_nrm_type, eps/ratio, eps_log/ratio_logistic, reg_threshold,
+ *     hin_threshold, sparse_taperx/y/z, Z_weights=).
  */
 #include <math.h>
 #include <stdio.h>
@@ -132,7 +135,6 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
   sep_par_bool("wantlog", &wantlog);
   sep_par_float("illu_pow", &illu_pow);
   sep_par_str("data_nrm_type", nrm, sizeof(nrm));
-  if (wantreg || wantlog) cli_fail("wantreg/wantlog: sparse regularisation is not built in swave");
   float dat_thresh = 0.f;
   sep_par_float("data_threshold", &dat_thresh);
   int nrm_type = 0;
@@ -141,6 +143,68 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
   if (strncmp(nrm, "L1nor", 5) == 0) nrm_type = SW_NRM_L1;
   if (strncmp(nrm, "L2nor", 5) == 0) nrm_type = SW_NRM_L2;
   if (!nrm_type) cli_fail("data_nrm_type=%s is not L2norm, L1norm, Huber or Cauchy", nrm);
+  /* Init_SparseRegularization (Sparse_regularization.f90:51-143), read only
+   * with wantreg or wantlog as in 2DAFWI.f90:80-84. */
+  sw_reg_desc rd;
+  sw_reg_state rs;
+  memset(&rd, 0, sizeof(rd));
+  memset(&rs, 0, sizeof(rs));
+  rd.nz = g->nz;
+  rd.nx = g->nx;
+  rd.ny = g->ny;
+  rd.wantreg = wantreg;
+  rd.wantlog = wantlog;
+  float *zweight = NULL;
+  if (wantreg || wantlog) {
+    char mn[32] = "Cauchy", hn[32] = "L2norm";
+    sep_par_bool("compute_eps", &rd.compute_eps);
+    sep_par_bool("compute_eps_log", &rd.compute_eps_log);
+    sep_par_bool("derivdx", &rd.derivdx);
+    sep_par_bool("derivdy", &rd.derivdy);
+    sep_par_bool("derivdz", &rd.derivdz);
+    sep_par_bool("log_z_plus", &rd.log_z_plus);
+    sep_par_str("model_nrm_type", mn, sizeof(mn));
+    sep_par_str("hinge_nrm_type", hn, sizeof(hn));
+    rd.ratio = 10.f;
+    rd.ratio_log = 10.f;
+    rs.eps = 1.f;
+    rs.eps_log = 1.f;
+    if (rd.compute_eps) sep_par_float("ratio", &rd.ratio);
+    else sep_par_float("eps", &rs.eps);
+    if (rd.compute_eps_log) sep_par_float("ratio_logistic", &rd.ratio_log);
+    else sep_par_float("eps_log", &rs.eps_log);
+    sep_par_float("reg_threshold", &rs.mod_thresh);
+    sep_par_float("hin_threshold", &rs.hin_thresh);
+    rd.ntaperx = 10;
+    rd.ntapery = 0;
+    rd.ntaperz = 10;
+    sep_par_int("sparse_taperx", &rd.ntaperx);
+    sep_par_int("sparse_tapery", &rd.ntapery);
+    sep_par_int("sparse_taperz", &rd.ntaperz);
+    const char *names[2] = {mn, hn};
+    int *types[2] = {&rd.mod_nrm_type, &rd.hin_nrm_type};
+    for (int k = 0; k < 2; ++k) {
+      if (strncmp(names[k], "Cauch", 5) == 0) *types[k] = SW_NRM_CAUCHY;
+      if (strncmp(names[k], "Huber", 5) == 0) *types[k] = SW_NRM_HUBER;
+      if (strncmp(names[k], "L1nor", 5) == 0) *types[k] = SW_NRM_L1;
+      if (strncmp(names[k], "L2nor", 5) == 0) *types[k] = SW_NRM_L2;
+      if (!*types[k]) cli_fail("%s is not L2norm, L1norm, Huber or Cauchy", names[k]);
+    }
+    /* Init_SparseRegularization_Array (:145-164). */
+    if (sep_exist("Z_weights")) {
+      sep_file *f = sep_open_in("Z_weights");
+      if (!f) cli_fail("%s", sep_error());
+      int n1 = 0, n2 = 0;
+      sep_hdr_int(f, "n1", &n1);
+      sep_hdr_int(f, "n2", &n2);
+      if (n1 != g->nz) cli_fail("Error: n1 and nz mask/vel different, exit now");
+      if (n2 != g->nx) cli_fail("Error: n2 and nx mask/vel different, exit now");
+      zweight = (float *)malloc(n * 4);
+      if (!zweight || sep_read(f, zweight, n)) cli_fail("Z_weights: %s", sep_error());
+      sep_close(f);
+      rd.zweight = zweight;
+    }
+  }
   /* Init_BandPassParam + BandpassSouTraces (Bandpass.f90:26-87). */
   float fhi = 20.f, flo = 0.f;
   int nphi = 14, nplo = 14, phase = 0;
@@ -245,6 +309,8 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
     double fd = 0.0;
     cli_check(ctx, sw_fwi_fct_gdt(ctx, &desc, x, wavelet, ng, shots, vpmask, &fd, grad, illum),
               "sw_fwi_fct_gdt");
+    cli_check(ctx, sw_fwi_regularize(ctx, &rd, &rs, eval, x, vpmask, &fd, grad),
+              "sw_fwi_regularize");
     if (eval == 0) {
       float mx = x[0];
       for (size_t i = 1; i < n; ++i) mx = x[i] > mx ? x[i] : mx;
@@ -340,6 +406,7 @@ static int run_inversion(sw_ctx *ctx, cli_par *p, float *wavelet, float *vel, fl
   free(xdsave);
   free(vpinit);
   free(vpmask);
+  free(zweight);
   free(mute);
   free(resid);
   free(shots);

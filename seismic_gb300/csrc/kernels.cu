@@ -4,6 +4,7 @@
 // operation order; the comments give the reference file:line.  Paths are
 // relative to the reference project root.
 #include "../../include/swave.h"
+#include "norms.cuh"
 #include "swave_dev.cuh"
 
 namespace swave {
@@ -186,33 +187,8 @@ __global__ void k_residual_nrm(int ntype, int nrec, int nt, const float *__restr
     const float m = mute ? mute[o + t] : 1.0f;
     const float d = m * (dobs[o + t] - dmod[o + t]);
     if (resid) resid[o + t] = d;
-    const float e = m * d;
-    float v, a;
-    switch (ntype) {
-      case SW_NRM_L1:
-        v = fabsf(d);
-        a = e < 0.0f ? -1.0f : (e > 0.0f ? 1.0f : 0.0f);
-        break;
-      case SW_NRM_HUBER: {
-        const float ad = fabsf(d);
-        v = ad > g ? ad - g / 2.0f : d * d / (2.0f * g);
-        a = fmaxf(-1.0f, fminf(1.0f, e / g));
-        break;
-      }
-      case SW_NRM_CAUCHY: {
-        const float q = d / g;
-        v = logf(1.0f + q * q) / 2.0f;
-        a = e / (g * g + e * e);
-        break;
-      }
-      default: {  // SW_NRM_HYPERBOLIC
-        v = sqrtf(g * g + d * d) - g;
-        a = (e / g) / sqrtf(1.0f + e * e / (g * g));
-        break;
-      }
-    }
-    fs = fs + v;
-    dmod[o + t] = a;
+    fs = fs + nrm_term(ntype, d, g);
+    dmod[o + t] = nrm_gdt(ntype, m * d, g);
   }
   partial[r] = (double)fs;
 }

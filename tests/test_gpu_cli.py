@@ -278,21 +278,38 @@ def _inv_survey(tmp_path, built, nt=400):
     return common, v0.astype(np.float32), w, keys
 
 
-@pytest.mark.parametrize("nrm", [("L2norm", 0.0), ("Huber", 0.0), ("L1norm", 0.0)])
+_REG = dict(wantreg=1, derivdx=1, derivdz=1, log_z_plus=1, model_nrm_type="Huber",
+            compute_eps=1, ratio=5.0, wantlog=1, hinge_nrm_type="L2norm", compute_eps_log=1,
+            ratio_logistic=20.0, sparse_taperx=6, sparse_taperz=4)
+_NRM = {"L2norm": sw.NRM_L2, "Huber": sw.NRM_HUBER, "L1norm": sw.NRM_L1}
+
+
+@pytest.mark.parametrize("nrm", [("L2norm", 0.0, None), ("Huber", 0.0, None),
+                                 ("L1norm", 0.0, None), ("L2norm", 0.0, _REG)],
+                         ids=["l2", "huber", "l1", "l2-regularised"])
 def test_afwi_program_task_inv(built, tmp_path, nrm):
     """Task=INV against the same l_bfgs loop written here over the Python
-    API (band-pass, mute masks, smoothing radii, sw_fwi_fct_gdt, device
-    L-BFGS): the final model and the misfit history agree bit for bit, and
-    the misfit falls; with the L2, Huber and L1 data norms."""
+    API (band-pass, mute masks, smoothing radii, sw_fwi_fct_gdt,
+    sw_fwi_regularize, device L-BFGS): the final model and the misfit history
+    agree bit for bit, and the misfit falls; with the L2, Huber and L1 data
+    norms and with the sparse + logistic model regularisation."""
     common, v0, w, keys = _inv_survey(tmp_path, built)
     obs, _ = sep.read(str(tmp_path / "obs.H"))
     niter = 3
-    nrm_name, thresh = nrm
+    nrm_name, thresh, reg = nrm
     _run(built, "2DAFWI.x", dict(common, vel=tmp_path / "v0.H", Task="INV",
                                  traces=tmp_path / "obs.H", niter=niter, vpmin=1500,
                                  vpmax=2600, inv=tmp_path / "inv.H",
                                  function=tmp_path / "f.H", model=tmp_path / "m.H",
-                                 data_nrm_type=nrm_name, data_threshold=thresh))
+                                 data_nrm_type=nrm_name, data_threshold=thresh, **(reg or {})))
+    if reg:
+        rdesc = sw.reg_desc(40, 90, wantreg=True, wantlog=True, derivdx=True, derivdz=True,
+                            log_z_plus=True, taperz=4, taperx=6, model_nrm_type=sw.NRM_HUBER,
+                            hinge_nrm_type=sw.NRM_L2, compute_eps=True, ratio=5.0,
+                            compute_eps_log=True, ratio_log=20.0)
+    else:
+        rdesc = sw.reg_desc(40, 90)
+    rstate = sw.SwRegState(1.0, 1.0, 0.0, 0.0)
     inv, h = sep.read(str(tmp_path / "inv.H"))
     fun, _ = sep.read(str(tmp_path / "f.H"))
     models, hm = sep.read(str(tmp_path / "m.H"))
@@ -315,8 +332,7 @@ def test_afwi_program_task_inv(built, tmp_path, nrm):
         desc.smooth_rect1, desc.smooth_rect2, desc.smooth_rect3 = r, r, int((0 + 1.5) / 2)
         desc.smooth_doz = desc.smooth_dox = int(not wave <= 10.0)
         desc.smooth_doy = 0
-        desc.dat_nrm_type = {"L2norm": sw.NRM_L2, "Huber": sw.NRM_HUBER,
-                             "L1norm": sw.NRM_L1}[nrm_name]
+        desc.dat_nrm_type = _NRM[nrm_name]
         desc.dat_thresh = thresh
         shots, row = [], 0
         for sx in (200.0, 450.0, 700.0):
@@ -335,7 +351,7 @@ def test_afwi_program_task_inv(built, tmp_path, nrm):
         fhist = []
         while cont and not found:
             fd, grad, _ = c.fwi_fct_gdt(desc, x.reshape(v0.shape), wb, shots)
-            grad = grad.ravel()
+            fd, grad = c.fwi_regularize(rdesc, rstate, eval_, x, fd, grad.ravel())
             if eval_ == 0:
                 mx = np.float32(x.max())
                 g0 = mx / (np.float32(100) * np.float32(np.abs(grad).max()))
