@@ -3,8 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (seismic_gb300/) links,
  * loads or calls this code; only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / --impl reference legs of bench.py use it, as the checker
- * and as the timed CPU baseline.
+ * cpu_baseline / --impl reference legs of bench.py use it, as the result
+ * the GPU path is compared against and as the timed CPU baseline.
  *
  * Parity status: UNPINNED.  The reference is Fortran (ifort + SEPlib) and
  * cannot be compiled in this environment, and its tree holds no golden

@@ -1,6 +1,6 @@
 // swave_oracle.cpp - CPU restatement of the reference acoustic path.
 //
-// TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for the CUDA engine
+// TEST INFRASTRUCTURE ONLY (see oracle.h): what the CUDA engine is compared with
 // and the timed CPU baseline.  Parity status: UNPINNED (no compilable
 // reference, no golden vectors in the reference tree).
 //
