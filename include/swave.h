@@ -89,7 +89,10 @@ typedef enum sw_imaging {
   SW_IMG_RTM = 1,    /* Imaging_condition_sourceonly_from_memory (Imaging.f90:228) */
   SW_IMG_LSRTM = 2,  /* Imaging_condition_LSRTM_sourceonly_...   (Imaging.f90:698) */
   SW_IMG_AFWI = 3,   /* Imaging_condition_AFWI_from_memory       (Imaging.f90:371) */
-  SW_IMG_BORN = 4    /* Injection_Born                           (Imaging.f90:747) */
+  SW_IMG_BORN = 4,   /* Injection_Born                           (Imaging.f90:747) */
+  SW_IMG_AFWI_RHO = 5 /* Imaging_condition_AFWI_RHOVP_from_memory (Imaging.f90:424):
+                         the velocity gradient into image, the density
+                         gradient into image2; needs rho (withRho)    */
 } sw_imaging;
 
 /* One propagation = one call of propagator_acoustic. */
@@ -129,6 +132,8 @@ typedef struct sw_prop_io {
                                sinc- and nearest-node injection scaled by
                                v^2*rho (Injection.f90:170-190); requires
                                fd_scheme = SW_FD_FORWARD                   */
+  float *image2;            /* nz*nx*ny second accumulator of
+                               SW_IMG_AFWI_RHO (imagesmall_nparam(:,:,:,2)) */
 } sw_prop_io;
 
 typedef struct sw_ctx sw_ctx;

@@ -28,7 +28,7 @@ class OrPropIO64(C.Structure):
     _fields_ = [("vel", _dp), ("nsou", C.c_int), ("sou_coord", _dp), ("sou_trace", _dp),
                 ("nrec", C.c_int), ("rec_coord", _dp), ("rec_trace", _dp), ("wave", _dp),
                 ("image", _dp), ("illum", _dp), ("ref", _dp), ("final_u2", _dp),
-                ("rho", _dp)]
+                ("rho", _dp), ("image2", _dp)]
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -169,7 +169,8 @@ def born(g, vel, ref, sou, wavelet, rec, f64=False):
 
 
 def propagate(desc, vel, sou_coord=None, sou_trace=None, rec_coord=None, rec_trace=None,
-              wave=None, image=None, illum=None, ref=None, final_u2=None, rho=None):
+              wave=None, image=None, illum=None, ref=None, final_u2=None, rho=None,
+              image2=None):
     lib = load()
     _, _, IO, _, _ = _types()
     io = IO()
@@ -182,7 +183,8 @@ def propagate(desc, vel, sou_coord=None, sou_trace=None, rec_coord=None, rec_tra
         a, io.rec_coord = _f(rec_coord); keep.append(a)
         io.nrec = a.size // 3
         io.rec_trace = rec_trace.ctypes.data_as(_fp)
-    for name, arr in (("wave", wave), ("image", image), ("illum", illum), ("final_u2", final_u2)):
+    for name, arr in (("wave", wave), ("image", image), ("illum", illum), ("final_u2", final_u2),
+                      ("image2", image2)):
         if arr is not None:
             assert arr.dtype == np.float32 and arr.flags["C_CONTIGUOUS"]
             setattr(io, name, arr.ctypes.data_as(_fp))

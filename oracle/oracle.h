@@ -44,6 +44,7 @@ typedef struct or_prop_io64 {
   const double *ref;
   double *final_u2;
   const double *rho;
+  double *image2;
 } or_prop_io64;
 
 /* propagator_acoustic (libs/libwave/Propagator.f90:27-270). */

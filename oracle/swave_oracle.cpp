@@ -740,6 +740,7 @@ template <class T> struct IO {
   const T *ref;
   T *final_u2;
   const T *rho;   // unpadded density (withRho), or null
+  T *image2;      // SW_IMG_AFWI_RHO: the density gradient
 };
 
 static int check_genpar(const sw_genpar &g) {
@@ -758,6 +759,8 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
   int st = check_genpar(g);
   if (st) return st;
   if (d.tstep != 1 && d.tstep != -1) return SW_BAD_PARAM;
+  if (d.imaging < SW_IMG_NONE || d.imaging > SW_IMG_AFWI_RHO) return SW_BAD_PARAM;
+  if (d.imaging == SW_IMG_AFWI_RHO && (!io.rho || !io.image2)) return SW_BAD_PARAM;
   const Bounds b = make_bounds(g);
   const int nt = g.nt;
   const int ntsnap = nt / g.snapi;
@@ -905,7 +908,26 @@ template <class T> static int propagate(const sw_prop_desc &d, const IO<T> &io) 
               const T w = W(i, j, k, index);
               T &im = M(io.image, i, j, k);
               T &il = M(io.illum, i, j, k);
-              if (d.imaging == SW_IMG_RTM) {
+              if (d.imaging == SW_IMG_AFWI_RHO) {
+                // Imaging_condition_AFWI_RHOVP_from_memory (Imaging.f90:424-511).
+                const int dk = ny == 1 ? 0 : 1;
+                const int ip = std::min(nz, i + 1), jp = std::min(j + 1, nx), kp = std::min(k + dk, ny);
+                const int im_ = ip - 1, jm = jp - 1, km = kp - dk;
+                const T dzi = T(1) / (T)g.dz, dxi = T(1) / (T)g.dx, dyi = T(1) / (T)g.dy;
+                const T dti2 = T(1) / dt2snap;
+                T tmp = dzi * ((*u2)(ip, jm, km) - (*u2)(im_, jm, km)) * dzi *
+                        (W(ip, jm, km, index) - W(im_, jm, km, index));
+                tmp = tmp + dxi * ((*u2)(im_, jp, km) - (*u2)(im_, jm, km)) * dxi *
+                                (W(im_, jp, km, index) - W(im_, jm, km, index));
+                tmp = tmp + dyi * ((*u2)(im_, jm, kp) - (*u2)(im_, jm, km)) * dyi *
+                                (W(im_, jm, kp, index) - W(im_, jm, km, index));
+                const T tmp1 = u * dti2 * ((W(i, j, k, im1) - T(2) * w) + W(i, j, k, ip1));
+                const T v = vel(i, j, k);
+                const T r = io.rho[(size_t)(i - 1) + (size_t)nz * ((j - 1) + (size_t)nx * (k - 1))];
+                im = im + ((T(2) * tmp1) * taper) / (((v * v) * v) * r);
+                T &im2 = M(io.image2, i, j, k);
+                im2 = im2 + (tmp * taper) / (r * r) + (tmp1 * taper) / ((r * r) * (v * v));
+              } else if (d.imaging == SW_IMG_RTM) {
                 // Imaging.f90:265-266
                 im = im + (u * w) * taper;
               } else if (d.imaging == SW_IMG_LSRTM) {
@@ -1868,13 +1890,15 @@ void oracle_set_rigid(int on) { g_rigid = on != 0; }
 
 int oracle_propagate_f32(const sw_prop_desc *d, const sw_prop_io *io) {
   IO<float> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
-              io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho};
+              io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho,
+              io->image2};
   return propagate<float>(*d, o);
 }
 
 int oracle_propagate_f64(const sw_prop_desc *d, const or_prop_io64 *io) {
   IO<double> o{io->vel, io->nsou, io->sou_coord, io->sou_trace, io->nrec, io->rec_coord,
-               io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho};
+               io->rec_trace, io->wave, io->image, io->illum, io->ref, io->final_u2, io->rho,
+               io->image2};
   return propagate<double>(*d, o);
 }
 

@@ -27,7 +27,7 @@ STATUS_NAMES = {0: "SW_OK", 1: "SW_BAD_PARAM", 2: "SW_OOM_ADMISSION", 3: "SW_TIM
 FD_FORWARD, FD_ADJOINT = 0, 1
 INJ_NONE, INJ_SINC, INJ_SIMPLE, INJ_LSRTM_SINC = 0, 1, 2, 3
 EXT_NONE, EXT_SINC, EXT_SIMPLE_AFWI, EXT_LSRTM_SINC, EXT_SINC_AFWI = 0, 1, 2, 3, 4
-IMG_NONE, IMG_RTM, IMG_LSRTM, IMG_AFWI, IMG_BORN = 0, 1, 2, 3, 4
+IMG_NONE, IMG_RTM, IMG_LSRTM, IMG_AFWI, IMG_BORN, IMG_AFWI_RHO = 0, 1, 2, 3, 4, 5
 # Data norms (invparam%dat_nrm_type).
 NRM_L1, NRM_L2, NRM_CAUCHY, NRM_HYPERBOLIC, NRM_HUBER = 1, 2, 3, 4, 12
 
@@ -56,7 +56,7 @@ class SwPropIO(C.Structure):
     _fields_ = [("vel", _fp), ("nsou", C.c_int), ("sou_coord", _fp), ("sou_trace", _fp),
                 ("nrec", C.c_int), ("rec_coord", _fp), ("rec_trace", _fp), ("wave", _fp),
                 ("image", _fp), ("illum", _fp), ("ref", _fp), ("final_u2", _fp),
-                ("rho", _fp)]
+                ("rho", _fp), ("image2", _fp)]
 
 
 class SwFwiShot(C.Structure):
@@ -312,7 +312,7 @@ class Context:
     # -- propagator_acoustic ----------------------------------------------
     def propagate(self, desc: SwPropDesc, vel, sou_coord=None, sou_trace=None, rec_coord=None,
                   rec_trace=None, wave=None, image=None, illum=None, ref=None, final_u2=None,
-                  rho=None):
+                  rho=None, image2=None):
         """sw_propagate; array arguments are modified in place like the reference."""
         io = SwPropIO()
         vel = _f32(vel)
@@ -336,6 +336,7 @@ class Context:
             rho = _f32(rho)
             keep.append(rho)
         io.rho = fptr(rho)
+        io.image2 = fptr(image2)
         self._check(self.lib.sw_propagate(self.h, C.byref(desc), C.byref(io)))
 
     def bandpass(self, traces, dt: float, flo: float = 0.0, fhi: float = 20.0, nplo: int = 14,

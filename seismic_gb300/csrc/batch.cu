@@ -213,6 +213,36 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
         S.illum[pp] = S.illum[pp] + (w * w) * taper;
       }
     }
+    // Imaging_condition_AFWI_RHOVP_from_memory (Imaging.f90:424-511): forward
+    // differences of u2 and of the snapshot (backward ones on the last row
+    // and column; none along y in 2D), the second time difference of the
+    // snapshots, and the velocity and density gradients.
+    if (S.imaging == 5 && S.tstep < 0 && below) {   // SW_IMG_AFWI_RHO
+      const int index = S.ntsnap - cnt + 1;
+      if (index >= 1) {
+        const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
+        const float *wi = S.wave + (long long)(index - 1) * nphys;
+        const int dk = g.ny == 1 ? 0 : 1;
+        const int ip = min(g.nz, i + 1), jp = min(j + 1, g.nx), kp = min(k + dk, g.ny);
+        const int im = ip - 1, jm = jp - 1, km = kp - dk;
+        const float dzi = S.dzi, dxi = S.dxi, dyi = S.dyi;   // 1/delta (rho setup)
+        const float dti2 = 1.0f / S.dt2snap;
+        auto U = [&](int a, int b2, int c2) { return u2[g.idx(a, b2, c2)]; };
+        auto Wv = [&](int a, int b2, int c2) { return wi[g.pidx(a, b2, c2)]; };
+        float tmp = dzi * (U(ip, jm, km) - U(im, jm, km)) * dzi * (Wv(ip, jm, km) - Wv(im, jm, km));
+        tmp = tmp + dxi * (U(im, jp, km) - U(im, jm, km)) * dxi * (Wv(im, jp, km) - Wv(im, jm, km));
+        tmp = tmp + dyi * (U(im, jm, kp) - U(im, jm, km)) * dyi * (Wv(im, jm, kp) - Wv(im, jm, km));
+        const float w = wi[pp];
+        const float tmp1 = u2c * dti2 *
+                           ((S.wave[(long long)(im1 - 1) * nphys + pp] - 2.0f * w) +
+                            S.wave[(long long)(ip1 - 1) * nphys + pp]);
+        const float vv = S.vel[p], rr = S.rho[p];
+        S.image[pp] = S.image[pp] + ((2.0f * tmp1) * taper) / (((vv * vv) * vv) * rr);
+        S.image2[pp] = S.image2[pp] + (tmp * taper) / (rr * rr) +
+                       (tmp1 * taper) / ((rr * rr) * (vv * vv));
+        S.illum[pp] = S.illum[pp] + (w * w) * taper;
+      }
+    }
   }
 }
 

@@ -43,6 +43,7 @@ struct ShotDev {
   int extract_wave, imaging, adj2d, adj3d;
   float *wave;            // ntsnap*nz*nx*ny snapshots
   float *image, *illum;
+  float *image2;          // SW_IMG_AFWI_RHO: the density gradient
   const float *ref;
   const float *taperx, *tapery;
   float k12, div11, dt2snap;

@@ -565,6 +565,14 @@ int sw_propagate(sw_ctx *c, const sw_prop_desc *d, const sw_prop_io *io) {
     if ((st = upload(c, "illum", io->illum, nphys * sizeof(float), &p))) return st;
     dio.illum_dev = (float *)p;
   }
+  if (d->imaging == SW_IMG_AFWI_RHO) {
+    // Only the variable-density AFWI driver calls it (to_disk_to_memory_AFWI.f90:
+    // 375-381,397-403).
+    if (!io->rho || !io->image2)
+      return fail(c, SW_BAD_PARAM, "SW_IMG_AFWI_RHO needs rho and image2");
+    if ((st = upload(c, "image2", io->image2, nphys * sizeof(float), &p))) return st;
+    dio.image2_dev = (float *)p;
+  }
   if (d->imaging == SW_IMG_BORN) {
     if (!io->ref) return fail(c, SW_BAD_PARAM, "ref required");
     if ((st = upload(c, "ref", io->ref, nphys * sizeof(float), &p))) return st;
@@ -581,6 +589,9 @@ int sw_propagate(sw_ctx *c, const sw_prop_desc *d, const sw_prop_io *io) {
     if ((st = download(c, io->image, dio.image_dev, nphys * sizeof(float)))) return st;
     if ((st = download(c, io->illum, dio.illum_dev, nphys * sizeof(float)))) return st;
   }
+  if (dio.image2_dev &&
+      (st = download(c, io->image2, dio.image2_dev, nphys * sizeof(float))))
+    return st;
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "sw_propagate");
   return SW_OK;

@@ -68,6 +68,7 @@ struct DevIO {
   float *rec_trace_dev = nullptr;
   float *wave_dev = nullptr;
   float *image_dev = nullptr;
+  float *image2_dev = nullptr;   // SW_IMG_AFWI_RHO: the density gradient
   float *illum_dev = nullptr;
   const float *ref_dev = nullptr;
   float *final_u2_host = nullptr;

@@ -309,6 +309,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     S.wave = io.wave_dev;
     S.image = io.image_dev;
     S.illum = io.illum_dev;
+    S.image2 = io.image2_dev;
     S.ref = io.ref_dev;
     if (d.imaging != SW_IMG_NONE) {
       float *a = carve<float>(cur, tx[b].size() + 1), *bq = carve<float>(cur, ty[b].size() + 1);
@@ -326,8 +327,13 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     S.npts = n1 * n2 * n3;
     if ((S.extract_wave || (S.imaging != SW_IMG_NONE)) && !S.wave)
       return fail(c, SW_BAD_PARAM, "snapshot buffer missing");
-    if (S.imaging >= 1 && S.imaging <= 3 && (!S.image || !S.illum))
+    if (S.imaging < SW_IMG_NONE || S.imaging > SW_IMG_AFWI_RHO)
+      return fail(c, SW_BAD_PARAM, "imaging %d", S.imaging);
+    if (((S.imaging >= 1 && S.imaging <= 3) || S.imaging == SW_IMG_AFWI_RHO) &&
+        (!S.image || !S.illum))
       return fail(c, SW_BAD_PARAM, "image buffers missing");
+    if (S.imaging == SW_IMG_AFWI_RHO && (!S.image2 || !S.rho_on))
+      return fail(c, SW_BAD_PARAM, "SW_IMG_AFWI_RHO needs rho and image2");
     if (S.imaging == SW_IMG_BORN && !S.ref) return fail(c, SW_BAD_PARAM, "reflectivity missing");
     max_steps = std::max(max_steps, S.nsteps);
     step_tiles[b + 1] = step_tiles[b] + step_ctas(G[b], tile);
@@ -523,6 +529,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       uint64_t per = S.extract_wave ? 4 : 0;
       if (S.imaging == SW_IMG_RTM || S.imaging == SW_IMG_LSRTM) per += 20;
       if (S.imaging == SW_IMG_AFWI) per += 28;
+      if (S.imaging == SW_IMG_AFWI_RHO) per += 36;
       if (S.imaging == SW_IMG_BORN) per += 8;
       by += (uint64_t)S.g.nz * S.g.nx * S.g.ny * per;
     }

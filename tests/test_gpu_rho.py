@@ -71,6 +71,42 @@ def test_rho_rtm_bitexact(ctx, oracle, three_d):
     np.testing.assert_array_equal(out["gpu"][1], out["oracle"][1])
 
 
+@pytest.mark.parametrize("three_d", [False, True])
+def test_rho_afwi_imaging_bitexact(ctx, oracle, three_d):
+    """AFWI_to_memory's withRho branch: the backward pass on the density
+    operator with Imaging_condition_AFWI_RHOVP_from_memory, whose velocity
+    and density gradients (image, image2) and illumination equal the
+    oracle's bit for bit."""
+    g, vel, sou, rec, w = case3d(nt=80) if three_d else case2d(nt=200)
+    rho = _rho(vel.shape, 7)
+    data = (np.random.default_rng(8).standard_normal((rec.shape[0], g.nt)) * 1e-2).astype(np.float32)
+    n = vel.size
+    out = {}
+    for name, api in (("gpu", ctx), ("oracle", oracle)):
+        wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+        api.propagate(_desc(g, injection=sw.INJ_SINC, extract_wave=1), vel, sou, w, wave=wave,
+                      rho=rho)
+        im, im2, il = (np.zeros(n, np.float32) for _ in range(3))
+        api.propagate(_desc(g, False, injection=sw.INJ_SINC, imaging=sw.IMG_AFWI_RHO), vel, rec,
+                      data, wave=wave, image=im, illum=il, rho=rho, image2=im2)
+        out[name] = (im, im2, il)
+    for a, b in zip(out["gpu"], out["oracle"]):
+        assert np.abs(b).max() > 0
+        np.testing.assert_array_equal(a, b)
+
+
+def test_rho_afwi_imaging_needs_density(ctx):
+    g, vel, sou, rec, w = case2d(nt=40)
+    n = vel.size
+    wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+    im, im2, il = (np.zeros(n, np.float32) for _ in range(3))
+    d = _desc(g, False, injection=sw.INJ_SINC, imaging=sw.IMG_AFWI_RHO)
+    with pytest.raises(sw.SwaveError) as e:
+        ctx.propagate(d, vel, rec, np.zeros((rec.shape[0], g.nt), np.float32), wave=wave,
+                      image=im, illum=il, image2=im2)
+    assert e.value.code == sw.SW_BAD_PARAM
+
+
 def test_rho_rejects_the_adjoint_grid(ctx):
     g, vel, sou, rec, w = case2d(nt=50)
     d = _desc(g, injection=sw.INJ_SINC)

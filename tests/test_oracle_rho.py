@@ -79,3 +79,42 @@ def test_constant_density_scales_the_data(oracle):
     assert np.linalg.norm(b - 2.5 * a) / np.linalg.norm(b) < 2e-5
     rel = np.linalg.norm(a - out["none"]) / np.linalg.norm(out["none"])
     assert rel < 2e-3, rel     # 3.6e-4 measured
+
+
+def _afwi_rho_run(oracle, g, vel, sou, w, rec, data, rho, imaging):
+    n = vel.size
+    wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+    d = sw.SwPropDesc()
+    d.g, d.tmin, d.tmax, d.tstep = g, 1, g.nt, 1
+    d.fd_scheme, d.injection, d.extract_wave = sw.FD_FORWARD, sw.INJ_SINC, 1
+    oracle.propagate(d, vel, sou, w, wave=wave, rho=rho)
+    b = sw.SwPropDesc()
+    b.g, b.tmin, b.tmax, b.tstep = g, g.nt, 1, -1
+    b.fd_scheme, b.injection, b.imaging = sw.FD_FORWARD, sw.INJ_SINC, imaging
+    im, im2, il = (np.zeros(n, np.float32) for _ in range(3))
+    oracle.propagate(b, vel, rec, data, wave=wave, image=im, illum=il, rho=rho,
+                     image2=im2 if imaging == sw.IMG_AFWI_RHO else None)
+    return im, im2, il
+
+
+def test_afwi_rho_imaging_pins(oracle):
+    """Imaging_condition_AFWI_RHOVP_from_memory (Imaging.f90:424-511): its
+    illumination is the AFWI one; with a constant density c its velocity
+    gradient is 2/c times the AFWI image (Imaging.f90:410-411) up to
+    rounding; both gradients are linear in the receiver data.  The density
+    2 makes the velocity gradient equal the AFWI image."""
+    from tests.cases import case2d
+    g, vel, sou, rec, w = case2d(nt=160)
+    data = (np.random.default_rng(3).standard_normal((rec.shape[0], g.nt)) * 1e-2).astype(np.float32)
+    rho = np.full(vel.shape, 2.0, np.float32)
+    im, im2, il = _afwi_rho_run(oracle, g, vel, sou, w, rec, data, rho, sw.IMG_AFWI_RHO)
+    ia, _, ila = _afwi_rho_run(oracle, g, vel, sou, w, rec, data, rho, sw.IMG_AFWI)
+    np.testing.assert_array_equal(il, ila)
+    assert np.abs(im).max() > 0 and np.abs(im2).max() > 0
+    assert np.linalg.norm(im - ia) <= 1e-5 * np.linalg.norm(ia)
+    im_2, im2_2, _ = _afwi_rho_run(oracle, g, vel, sou, w, rec, 2 * data, rho, sw.IMG_AFWI_RHO)
+    # Exact up to subnormal intermediate values at the wavefront edges.
+    assert np.abs(im_2 - 2 * im).max() <= 1e-6 * np.abs(im).max()
+    assert np.abs(im2_2 - 2 * im2).max() <= 1e-6 * np.abs(im2).max()
+    with pytest.raises(RuntimeError):
+        _afwi_rho_run(oracle, g, vel, sou, w, rec, data, None, sw.IMG_AFWI_RHO)
