@@ -10,7 +10,6 @@
 
 int main(int argc, char **argv) {
   if (sep_init(argc, argv)) cli_fail("%s", sep_error());
-  if (sep_exist("vel2")) cli_fail("vel2= (a second velocity) is not built in swave");
   if (!sep_exist("vel")) cli_fail("need velocity file");
   if (!sep_exist("ref")) cli_fail("need reflectivity file");
   if (!sep_exist("data")) cli_fail("need dat file for output");

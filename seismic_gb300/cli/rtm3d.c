@@ -10,7 +10,11 @@
  * the forward-grid density operator in both passes
  * (to_disk_to_memory_RTM.f90:388-398,455-465).  LSRTM=1 CHEAPLSRTM=1 runs
  * CHEAP_LSRTM_to_memory (to_disk_to_memory_RTM.f90:581-668): the LSRTM
- * backward pass on the forward-grid stencil instead of the adjoint one. */
+ * backward pass on the forward-grid stencil instead of the adjoint one.
+ * vel2= replaces the velocity of the backward pass and of its imaging
+ * condition (mod%vel=mod%vel2, to_disk_to_memory_RTM.f90:438-439,550-551,
+ * 637-638); the passes then run as two sw_propagate calls with the
+ * procedures sw_rtm / sw_lsrtm use. */
 #include <stdlib.h>
 #include <string.h>
 
@@ -19,7 +23,6 @@
 int main(int argc, char **argv) {
   if (sep_init(argc, argv)) cli_fail("%s", sep_error());
   if (!sep_exist("vel")) cli_fail("need vel file");
-  if (sep_exist("vel2")) cli_fail("vel2= (a second velocity) is not built in swave");
   cli_par p;
   cli_read_params(&p);
   float *wavelet = cli_read_source(&p);
@@ -30,6 +33,7 @@ int main(int argc, char **argv) {
   if (p.withRho && p.LSRTM) cli_fail("withRho=1 with LSRTM=1 is not built in swave");
   float *vel = cli_read_model(&p, "vel");
   float *rho = p.withRho ? cli_read_model(&p, "rho") : NULL;
+  float *vel2 = sep_exist("vel2") ? cli_read_model(&p, "vel2") : NULL;
   if (!sep_exist("image")) cli_fail("need image file for output");
   sw_window w;
   sw_genpar gw;
@@ -46,14 +50,19 @@ int main(int argc, char **argv) {
   if (!vsmall || !ims || !ils || !im || !il) cli_fail("out of host memory");
   if (sw_window_extract(&p.g, &w, vel, vsmall) != SW_OK) cli_fail("window extract");
   sw_ctx *ctx = cli_context();
-  if (rho || p.CHEAPLSRTM) {
-    float *rs = NULL;
+  if (rho || p.CHEAPLSRTM || vel2) {
+    float *rs = NULL, *vsmall2 = NULL;
     const int ntsnap = gw.nt / gw.snapi;
     float *wave = (float *)malloc(nw * (size_t)(ntsnap > 0 ? ntsnap : 1) * 4);
     if (!wave) cli_fail("out of host memory");
     if (rho) {
       rs = (float *)malloc(nw * 4);
       if (!rs || sw_window_extract(&p.g, &w, rho, rs) != SW_OK) cli_fail("window extract");
+    }
+    if (vel2) {
+      vsmall2 = (float *)malloc(nw * 4);
+      if (!vsmall2 || sw_window_extract(&p.g, &w, vel2, vsmall2) != SW_OK)
+        cli_fail("window extract");
     }
     sw_prop_desc d;
     memset(&d, 0, sizeof(d));
@@ -77,8 +86,15 @@ int main(int argc, char **argv) {
     d.tmax = 1;
     d.tstep = -1;
     d.extract_wave = 0;
-    d.imaging = p.CHEAPLSRTM ? SW_IMG_LSRTM : SW_IMG_RTM;
-    d.injection = p.CHEAPLSRTM ? SW_INJ_LSRTM_SINC : SW_INJ_SINC;
+    d.imaging = p.LSRTM ? SW_IMG_LSRTM : SW_IMG_RTM;
+    d.injection = p.LSRTM ? SW_INJ_LSRTM_SINC : SW_INJ_SINC;
+    /* The backward stencil of RTM_to_memory / LSRTM_to_memory: the adjoint
+     * grid (RTM in 3D: the forward grid); the forward grid with rho or
+     * CHEAP_LSRTM. */
+    if (rho || p.CHEAPLSRTM) d.fd_scheme = SW_FD_FORWARD;
+    else if (p.LSRTM) d.fd_scheme = SW_FD_ADJOINT;
+    else d.fd_scheme = gw.twoD ? SW_FD_ADJOINT : SW_FD_FORWARD;
+    if (vsmall2) io.vel = vsmall2;
     memset(ims, 0, nw * 4);
     memset(ils, 0, nw * 4);
     io.nsou = ntr;
@@ -89,6 +105,7 @@ int main(int argc, char **argv) {
     cli_check(ctx, sw_propagate(ctx, &d, &io), "backward propagation");
     free(wave);
     free(rs);
+    free(vsmall2);
   } else if (p.LSRTM)
     cli_check(ctx, sw_lsrtm(ctx, &gw, vsmall, sou, wavelet, ntr, rec, traces, ims, ils),
               "sw_lsrtm");
@@ -104,6 +121,7 @@ int main(int argc, char **argv) {
   free(im);
   free(il);
   free(rho);
+  free(vel2);
   free(vel);
   free(rec);
   free(traces);

@@ -139,6 +139,55 @@ def test_rtm_program(built, oracle, tmp_path, three_d, mode):
 
 
 @pytest.mark.parametrize("three_d", [False, True])
+@pytest.mark.parametrize("lsrtm", [False, True])
+def test_rtm_program_second_velocity(built, oracle, tmp_path, three_d, lsrtm):
+    """vel2=: the backward pass and its imaging condition run on the second
+    velocity (mod%vel=mod%vel2, to_disk_to_memory_RTM.f90:438-439,550-551);
+    the forward pass keeps vel."""
+    params, g, vel, win, sou, rec, w, ntr = _case(tmp_path, three_d, nt=120)
+    vel2 = (vel * np.float32(1.04)).astype(np.float32)
+    axes = {"d1": D, "d2": D, "o1": 0.0, "o2": 0.0}
+    if three_d:
+        axes.update({"d3": D, "o3": 0.0})
+    sep.write(str(tmp_path / "vel2.H"), vel2, axes)
+    d = (np.random.default_rng(3).standard_normal((ntr, g.nt)) * 1e-2).astype(np.float32)
+    params.update(traces=_traces(tmp_path, "t.H", d), image=tmp_path / "im.H",
+                  vel2=tmp_path / "vel2.H")
+    if lsrtm:
+        params.update(LSRTM=1)
+    _run(built, "3DRTM.x", params)
+    out, _ = sep.read(str(tmp_path / "im.H"))
+    v1, v2 = np.ascontiguousarray(vel[win]), np.ascontiguousarray(vel2[win])
+    wl = sw.born_wavelet(w, g.dt) if lsrtm else w
+    n = v1.size
+    wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+    f = sw.SwPropDesc()
+    f.g = g
+    f.tmin, f.tmax, f.tstep = 1, g.nt, 1
+    f.fd_scheme, f.injection, f.extract_wave = sw.FD_FORWARD, sw.INJ_SINC, 1
+    oracle.propagate(f, v1, sou, wl, wave=wave)
+    b = sw.SwPropDesc()
+    b.g = g
+    b.tmin, b.tmax, b.tstep = g.nt, 1, -1
+    if lsrtm:
+        b.fd_scheme, b.injection, b.imaging = sw.FD_ADJOINT, sw.INJ_LSRTM_SINC, sw.IMG_LSRTM
+    else:
+        b.fd_scheme = sw.FD_FORWARD if three_d else sw.FD_ADJOINT
+        b.injection, b.imaging = sw.INJ_SINC, sw.IMG_RTM
+    im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    oracle.propagate(b, v2, rec, d, wave=wave, image=im, illum=il)
+    im_full, il_full = np.zeros_like(vel), np.zeros_like(vel)
+    im_full[win] = im.reshape(v1.shape)
+    il_full[win] = il.reshape(v1.shape)
+    assert np.abs(im).max() > 0
+    np.testing.assert_array_equal(out[0], im_full)
+    np.testing.assert_array_equal(out[1], il_full)
+    # The second velocity matters.
+    ref = oracle.lsrtm(g, v1, sou, wl, rec, d) if lsrtm else oracle.rtm(g, v1, sou, w, rec, d)
+    assert np.abs(ref[0] - im).max() > 1e-3 * np.abs(im).max()
+
+
+@pytest.mark.parametrize("three_d", [False, True])
 def test_born_program(built, oracle, tmp_path, three_d):
     params, g, vel, win, sou, rec, w, ntr = _case(tmp_path, three_d, nt=120)
     rng = np.random.default_rng(6)
