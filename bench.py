@@ -49,26 +49,16 @@ def log(*a):
 # Workload
 # ---------------------------------------------------------------------------
 def make_workload(nt_cap: int | None = None):
-    from seismic_gb300 import make_genpar, synth
-    vel = synth.layered_faulted(NZ, NX, D, seed=2)          # (nx, nz) = Fortran (nz, nx)
-    shots = synth.rtm_shots(NX, D, NSHOT_SURVEY, SPACING, seed=2, dt=DT)
-    if nt_cap:
-        for s in shots:
-            s["nt"] = min(s["nt"], nt_cap)
-    ntmax = max(s["nt"] for s in shots)
-    g = make_genpar(NZ, NX, 1, dz=D, dx=D, dt=DT, nt=ntmax, ntaper=NTAPER, lsinc=7,
-                    snapi=SNAPI, fmax=50.0)
-    w = synth.ricker(F0, DT, ntmax)
-    return g, vel, w, shots
+    """The 240-shot survey (seismic_gb300.synth.config2): full-model genpar,
+    vel (nx, nz) = Fortran (nz, nx), wavelet, shots."""
+    from seismic_gb300 import synth
+    return synth.config2(nt_cap)
 
 
 def window_of(shot):
     """Columns [i0, i0+nxw) of the shot window (aperture 0: source + spread)."""
-    lo = min(shot["lo"], float(shot["sou"][1]))
-    hi = max(shot["hi"], float(shot["sou"][1]))
-    i0 = int(round(lo / D))
-    nxw = int(round((hi - lo) / D)) + 1
-    return i0, nxw
+    from seismic_gb300 import synth
+    return synth.config2_window(shot)
 
 
 def model_data(ctx, g, vel, w, shot):
@@ -156,7 +146,8 @@ def measured_peak():
 # ---------------------------------------------------------------------------
 def cpu_sample(g, vel, w, shot, nsteps: int) -> dict:
     """Times the oracle's RTM of one shot (its whole record when nsteps is 0,
-    else truncated to nsteps samples)."""
+    else truncated to nsteps samples) on random data (the reference arm:
+    the time does not depend on the data values)."""
     import seismic_gb300 as sw
     from oracle import bind as oracle
     nsteps = nsteps or shot["nt"]
@@ -171,6 +162,47 @@ def cpu_sample(g, vel, w, shot, nsteps: int) -> dict:
     dt = time.perf_counter() - t0
     pts = (NZ + 2 * NTAPER) * (nxw + 2 * NTAPER) * nsteps * 2
     return {"seconds": dt, "points": pts}
+
+
+def cpu_parity_sample(ctx, g, vel, w, shots) -> tuple[dict, dict]:
+    """The CPU baseline and the parity check of the benchmarked workload:
+    the oracle's stacked RTM (RTM_to_memory per shot window + mod_copy_image)
+    of `shots` with the very data the GPU migrated, timed on the host cores,
+    against the same shots migrated together in one batch on the GPU; and
+    the oracle's modelling of the first shot against the GPU-modelled data."""
+    import seismic_gb300 as sw
+    from oracle import bind as oracle
+    oracle.load()
+    job = sw.RTMJob(ctx, g, vel, w, shots)
+    job.set_batch(len(shots))
+    job.run()
+    im, il = job.result(normalised=False)
+    job.close()
+    t0 = time.perf_counter()
+    rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
+    secs = time.perf_counter() - t0
+    pts = sum(shot_points({"lo": s["lo"], "hi": s["hi"], "sou": s["sou"],
+                           "nt": s["data"].shape[1]}) for s in shots)
+    s0 = shots[0]
+    i0, nxw = window_of(s0)
+    nt0 = s0["data"].shape[1]
+    gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=nt0, ntaper=NTAPER,
+                        lsinc=7, snapi=SNAPI)
+    rdata = oracle.modeling(gw, vel[i0:i0 + nxw], s0["sou"], w[:nt0], s0["rec"])
+
+    def rel(a, b):
+        den = float(np.linalg.norm(b.astype(np.float64)))
+        return float(np.linalg.norm((a.astype(np.float64) - b)) / (den or 1.0))
+
+    parity = {"shots": [float(s["sou"][1]) for s in shots],
+              "windows": [window_of(s)[1] for s in shots],
+              "records": [int(s["data"].shape[1]) for s in shots],
+              "batch": len(shots),
+              "image_rel_l2": rel(im, rim), "illum_rel_l2": rel(il, ril),
+              "data_rel_l2": rel(s0["data"], rdata),
+              "bitexact": bool(np.array_equal(im, rim) and np.array_equal(il, ril)
+                               and np.array_equal(s0["data"], rdata))}
+    return {"seconds": secs, "points": pts}, parity
 
 
 def cpu_threads() -> int:
@@ -384,14 +416,20 @@ def main():
         e2e_line = {"value": pts_e2e / e2e_s / 1e9, "unit": "Gpts/s",
                     "h2d_bytes_per_step": int(h2d) // args.steps,
                     "d2h_bytes_per_step": int(d2h) // args.steps}
-    # CPU baseline (rank 0, N=1 only): a bounded sample of the same workload.
-    cpu = None
+    # CPU baseline (rank 0, N=1 only): the oracle's RTM of the first two
+    # shots of the first timed batch with the same data, which also checks
+    # the GPU's image of those shots.
+    cpu, parity = None, None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        r = cpu_sample(g, vel, w, per_step[0], args.cpu_steps)
+        k0 = args.warmup * B
+        psh = [dict(job_shots[k0 + q], lo=per_step[k0 + q]["lo"], hi=per_step[k0 + q]["hi"])
+               for q in range(min(2, B))]
+        r, parity = cpu_parity_sample(ctx, g, vel, w, psh)
         cpu = {"value": r["points"] / r["seconds"] / 1e9, "unit": "Gpts/s", "cores": cpu_threads(),
                "kind": "port",
-               "sample": f"oracle RTM of one shot window, {args.cpu_steps or per_step[0]['nt']} "
-                         f"time samples, forward + backward ({r['seconds']:.1f} s)"}
+               "sample": f"oracle stacked RTM (forward + backward, whole records) of {len(psh)} "
+                         f"shots of the first timed batch with the GPU's data "
+                         f"({r['seconds']:.1f} s)"}
     if rank == 0:
         line = {
             "metric": "fd_gpts_per_s", "value": value, "unit": "Gpts/s", "n_gpus": ws,
@@ -405,7 +443,7 @@ def main():
                          "avg_launch_ms": (st["step_kernel_ms"] / nl),
                          "algorithmic_bytes_per_launch": algo_per_launch,
                          "launches_timed": st["step_kernel_timed"]},
-            "cpu_baseline": cpu, "e2e": e2e_line, "clocks": clk,
+            "cpu_baseline": cpu, "parity": parity, "e2e": e2e_line, "clocks": clk,
             "gpu_launches": launches_timed_region,
             "timed_event_ms": ev_ms,
         }

@@ -58,7 +58,11 @@ typedef struct sw_genpar {
   int ntaper;      /* padding cells per side (ReadParam.f90:19, default 20) */
   int lsinc;       /* sinc length (ReadParam.f90:24, default 7)             */
   int snapi;       /* snapshot decimation (ReadParam.f90:20, default 4)     */
-  int surf_type, shot_type, rec_type;   /* only 0 is built                 */
+  int surf_type, shot_type, rec_type;   /* 0: none; surf_type 1 / 2: sinc free
+                      surface on a row / between rows (Boundary.f90:1609-1658);
+                      shot_type, rec_type 1: mirror sources / receivers
+                      (Injection.f90:274-338, Extraction.f90:276-337); all
+                      entry points but sw_modeling_noalloc (0 only)          */
   float fmax;      /* used by vel_check only                                */
 } sw_genpar;
 
@@ -446,7 +450,10 @@ int sw_cnn_train_step(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
  * first call on a device looks the scratch array's device address up there
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * All calls share the array: calls that overlap on the GPU (from several
- * host threads at once) race on it.  3D models return SW_UNSUPPORTED. */
+ * host threads at once) race on it.  Do not cudaDeviceReset a device this
+ * entry point has run on (the cached address would go stale).  3D models
+ * and surf_type / shot_type / rec_type other than 0 return SW_UNSUPPORTED;
+ * a bounded device wait that gave up returns SW_TIMEOUT. */
 int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const float *sou_coord,
                         const float *wavelet, int nrec, const float *rec_coord, float *data);
 

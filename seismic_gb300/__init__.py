@@ -637,7 +637,8 @@ def modeling_noalloc(g: SwGenpar, vel, sou_coord, wavelet, rec_coord) -> np.ndar
     """sw_modeling_noalloc: 2D shot modelling on the current device that
     allocates no device memory (results equal Context.modeling).  Raises
     SwaveError with SW_OOM_ADMISSION when the run exceeds the library's fixed
-    32 MiB scratch array."""
+    32 MiB scratch array, and with SW_UNSUPPORTED for a free surface or
+    mirror sources / receivers (surf_type, shot_type, rec_type other than 0)."""
     lib = load_library()
     vel, sc, w, rc = _f32(vel), _f32(sou_coord), _f32(wavelet), _f32(rec_coord)
     nrec = rc.size // 3

@@ -13,7 +13,13 @@
 //
 // The first call on a device looks up the array's device address there with
 // cudaGetSymbolAddress (a host-side name is not a device address); make
-// that first call before any stream capture.  All calls share the array and
+// that first call before any stream capture.  The lookup is guarded by a
+// mutex, so first calls from several host threads are safe.  The cached
+// address belongs to the device's primary context: after cudaDeviceReset
+// the module is loaded again, possibly elsewhere, so do not reset a device
+// on which this entry point has run.  Only the reference's default
+// geometry is built: surf_type, shot_type and rec_type must be 0 (the free
+// surface and mirror modes return SW_UNSUPPORTED).  All calls share the array and
 // it keeps the last call's contents: the time levels, the receiver traces,
 // the step counter and the error flags are cleared at the start of each
 // call.  Calls that overlap on the GPU (from several host threads, or
@@ -24,6 +30,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "../../include/swave.h"
@@ -38,8 +45,10 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-// Device address of the scratch array on each device (set up once).
+// Device address of the scratch array on each device (set up once, under
+// g_scratch_mu).
 unsigned char *g_scratch_ptr[kMaxDevices] = {};
+std::mutex g_scratch_mu;
 
 size_t rup256(size_t b) { return (b + 255) / 256 * 256; }
 
@@ -65,6 +74,9 @@ extern "C" int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const f
   if (!g || !vel || !sou_coord || !wavelet || !data || nrec < 0 || (nrec > 0 && !rec_coord))
     return SW_BAD_PARAM;
   if (!g->twoD || g->ny != 1) return SW_UNSUPPORTED;
+  // The free surface and the mirror sources / receivers need the surface
+  // plan and the mirror injection entries; this entry point builds neither.
+  if (g->surf_type != 0 || g->shot_type != 0 || g->rec_type != 0) return SW_UNSUPPORTED;
   int st = check_genpar(nullptr, *g);
   if (st) return st;
   const Geom G = make_geom(*g);
@@ -93,13 +105,18 @@ extern "C" int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const f
   // Once per device: the scratch array's device address.
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SW_CUDA_ERR;
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SW_CUDA_ERR;
-    g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SW_CUDA_ERR;
+      g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    base = g_scratch_ptr[dev];
   }
   cudaStream_t s = 0;   // legacy default stream
-  Carver cv{g_scratch_ptr[dev]};
+  Carver cv{base};
   float *vphys = cv.take<float>(nphys);
   float *vpad = cv.take<float>(nf);
   ShotDev S;
@@ -207,6 +224,10 @@ extern "C" int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const f
   if (nrec > 0 &&
       !ck(cudaMemcpyAsync(data, rec, (size_t)nrec * nt * 4, cudaMemcpyDeviceToHost, s)))
     return SW_CUDA_ERR;
-  if (!ck(cudaStreamSynchronize(s))) return SW_CUDA_ERR;
-  return SW_OK;
+  // The step kernels record a bounded wait that gave up in the error flag.
+  int herr = 0;
+  if (!ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+      !ck(cudaStreamSynchronize(s)))
+    return SW_CUDA_ERR;
+  return herr ? SW_TIMEOUT : SW_OK;
 }

@@ -521,7 +521,7 @@ int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
   SW_CK(cudaMemcpyAsync(&herr, rerr, sizeof(int), cudaMemcpyDeviceToHost, s));
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "rtm job");
   if (herr)
-    return fail(c, SW_CUDA_ERR, "step kernel gave up waiting for a tile copy (error flags %d)",
+    return fail(c, SW_TIMEOUT, "step kernel gave up waiting for a tile copy (error flags %d)",
                 herr);
   return SW_OK;
 }

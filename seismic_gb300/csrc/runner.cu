@@ -661,7 +661,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   SW_CK(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, s));
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "batch run");
   if (herr)
-    return fail(c, SW_CUDA_ERR, "step kernel gave up waiting for a tile copy (error flags %d)",
+    return fail(c, SW_TIMEOUT, "step kernel gave up waiting for a tile copy (error flags %d)",
                 herr);
   return SW_OK;
 }

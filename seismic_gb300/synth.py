@@ -14,6 +14,12 @@ value ranges of the benchmark configurations instead:
   generator of the batched RTM, Born and FWI configurations).
 * ``rtm_shots``: 37.5 m shot spacing, per-shot split-spread aperture of
   3-6 km and record length of 3-4 s.
+* ``config2``: the batched-RTM survey, 751 x 2301 at 4 m, dt 0.375 ms (the
+  scheme's Courant limit rules out 0.4 ms at 4700 m/s), 240 shots, 20 Hz
+  Ricker, generator seed 2.
+* ``config3``: the Born / FWI-gradient grid, 1201 x 3401 at 6.25 m, dt
+  0.5 ms, background = the layered-faulted generator (seed 3) smoothed by a
+  150 m Gaussian, reflectivity = 1 % density spikes N(0, 0.05) relative.
 """
 from __future__ import annotations
 
@@ -126,3 +132,65 @@ def rtm_shots(nx: int, d: float, nshot: int, spacing: float, seed: int, dt: floa
         shots.append({"sou": np.array([0.0, sx, 0.0], np.float32), "rec": rec, "nt": nt,
                       "lo": lo, "hi": max(hi, rx[-1])})
     return shots
+
+
+# Batched-RTM survey (751 x 2301 at 4 m).
+CONFIG2 = {"nz": 751, "nx": 2301, "d": 4.0, "dt": 3.75e-4, "snapi": 4, "ntaper": 20,
+           "f0": 20.0, "nshot": 240, "spacing": 37.5, "seed": 2}
+
+
+def config2(nt_cap: int | None = None) -> tuple:
+    """(genpar of the full model, vel (nx, nz), wavelet, shots): the 240-shot
+    survey with per-shot apertures of 3-6 km and records of 3-4 s; genpar.nt
+    is the longest record.  nt_cap truncates every record."""
+    from . import make_genpar
+    c = CONFIG2
+    vel = layered_faulted(c["nz"], c["nx"], c["d"], seed=c["seed"])
+    shots = rtm_shots(c["nx"], c["d"], c["nshot"], c["spacing"], seed=c["seed"], dt=c["dt"])
+    if nt_cap:
+        for s in shots:
+            s["nt"] = min(s["nt"], nt_cap)
+    ntmax = max(s["nt"] for s in shots)
+    g = make_genpar(c["nz"], c["nx"], 1, dz=c["d"], dx=c["d"], dt=c["dt"], nt=ntmax,
+                    ntaper=c["ntaper"], lsinc=7, snapi=c["snapi"], fmax=50.0)
+    return g, vel, ricker(c["f0"], c["dt"], ntmax), shots
+
+
+def config2_window(shot: dict) -> tuple[int, int]:
+    """Columns [i0, i0 + nxw) of a config-2 shot's window (aperture 0: the
+    source and its receiver spread)."""
+    d = CONFIG2["d"]
+    lo = min(shot["lo"], float(shot["sou"][1]))
+    hi = max(shot["hi"], float(shot["sou"][1]))
+    return int(round(lo / d)), int(round((hi - lo) / d)) + 1
+
+
+# Born / FWI-gradient grid (1201 x 3401 at 6.25 m).
+CONFIG3 = {"nz": 1201, "nx": 3401, "d": 6.25, "dt": 5e-4, "nt": 10000, "snapi": 4,
+           "ntaper": 20, "f0": 15.0, "nshot": 120, "seed": 3}
+
+
+def config3(nt: int | None = None, rec_step: int = 2) -> dict:
+    """Smoothed background, sparse reflectivity and the 120 surface shots
+    (full-width spread, a receiver every rec_step columns at depth index 2).
+    Arrays are (nx, nz) C order = Fortran (nz, nx)."""
+    from . import make_genpar
+    c = CONFIG3
+    nz, nx, d = c["nz"], c["nx"], c["d"]
+    nt = nt or c["nt"]
+    raw = layered_faulted(nz, nx, d, seed=c["seed"])
+    vel = smooth(raw, d, 150.0)
+    rng = np.random.default_rng(c["seed"])
+    spikes = rng.random(vel.shape) < 0.01
+    ref = np.where(spikes, rng.normal(0.0, 0.05, vel.shape), 0.0).astype(np.float32)
+    g = make_genpar(nz, nx, 1, dz=d, dx=d, dt=c["dt"], nt=nt, ntaper=c["ntaper"], lsinc=7,
+                    snapi=c["snapi"], fmax=30.0)
+    xmax = (nx - 1) * d
+    sx = np.linspace(0.05 * xmax, 0.95 * xmax, c["nshot"])
+    rx = np.arange(0, nx, rec_step) * d
+    rec = np.zeros((rx.size, 3), np.float32)
+    rec[:, 0] = d
+    rec[:, 1] = rx
+    shots = [np.array([2 * d, x, 0.0], np.float32) for x in sx]
+    return {"g": g, "vel": vel, "ref": ref, "rec": rec, "shots": shots,
+            "wavelet": ricker(c["f0"], c["dt"], nt)}

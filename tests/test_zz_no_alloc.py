@@ -36,3 +36,15 @@ def test_modeling_noalloc_rejects_oversize(ctx):
     with pytest.raises(sw.SwaveError) as ei:
         sw.modeling_noalloc(big, vbig, sou, w, rec)
     assert ei.value.code == sw.SW_OOM_ADMISSION
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("field", ["surf_type", "shot_type", "rec_type"])
+def test_modeling_noalloc_rejects_surface_and_mirror_modes(ctx, field):
+    # The free surface and the mirror modes are built on the allocating
+    # entry points only; this one refuses them instead of ignoring them.
+    g, vel, sou, rec, w = case2d(nz=60, nx=80, nt=8, seed=0)
+    setattr(g, field, 1)
+    with pytest.raises(sw.SwaveError) as ei:
+        sw.modeling_noalloc(g, vel, sou, w, rec)
+    assert ei.value.code == sw.SW_UNSUPPORTED
