@@ -61,15 +61,6 @@ def window_of(shot):
     return synth.config2_window(shot)
 
 
-def model_data(ctx, g, vel, w, shot):
-    """Observed data of one shot: forward modelling on its window."""
-    import seismic_gb300 as sw
-    i0, nxw = window_of(shot)
-    gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=shot["nt"], ntaper=NTAPER,
-                        lsinc=7, snapi=SNAPI)
-    return ctx.modeling(gw, vel[i0:i0 + nxw], shot["sou"], w[: shot["nt"]], shot["rec"])
-
-
 def shot_points(shot, forward_and_back=True):
     i0, nxw = window_of(shot)
     n1 = NZ + 2 * NTAPER
@@ -181,8 +172,7 @@ def cpu_parity_sample(ctx, g, vel, w, shots) -> tuple[dict, dict]:
     t0 = time.perf_counter()
     rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
     secs = time.perf_counter() - t0
-    pts = sum(shot_points({"lo": s["lo"], "hi": s["hi"], "sou": s["sou"],
-                           "nt": s["data"].shape[1]}) for s in shots)
+    pts = sum(shot_points(dict(s, nt=s["data"].shape[1])) for s in shots)
     s0 = shots[0]
     i0, nxw = window_of(s0)
     nt0 = s0["data"].shape[1]
@@ -422,8 +412,7 @@ def main():
     cpu, parity = None, None
     if rank == 0 and ws == 1 and not args.no_cpu:
         k0 = args.warmup * B
-        psh = [dict(job_shots[k0 + q], lo=per_step[k0 + q]["lo"], hi=per_step[k0 + q]["hi"])
-               for q in range(min(2, B))]
+        psh = job_shots[k0:k0 + min(2, B)]
         r, parity = cpu_parity_sample(ctx, g, vel, w, psh)
         cpu = {"value": r["points"] / r["seconds"] / 1e9, "unit": "Gpts/s", "cores": cpu_threads(),
                "kind": "port",

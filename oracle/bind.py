@@ -356,3 +356,94 @@ class LBFGS:
             self.lib.oracle_lbfgs_destroy(self.h)
         except Exception:
             pass
+
+
+def mute_mask(nt, dt, sou, rec, ot=0.0, v0=1500.0, v1=10000.0, t0=0.0, t1=40.0, tramp=0.5):
+    """MuteParam_compute_mask (Mute.f90:50-95,172-219) of one gather."""
+    lib = load()
+    s, ps = _f(sou)
+    r, pr = _f(rec)
+    m = np.zeros((r.size // 3, nt), np.float32)
+    _chk(lib.oracle_mute_mask(r.size // 3, nt, C.c_float(dt), C.c_float(ot), ps, pr,
+                              C.c_float(v0), C.c_float(v1), C.c_float(t0), C.c_float(t1),
+                              C.c_float(tramp), m.ctypes.data_as(_fp)), "mute_mask")
+    return m
+
+
+def freeze_x(x, xmin, xmax, mask, soft, xinit):
+    """FREEZE_X (libs/libinv/lbfgs.f:1-40) on an FP64 vector, in place:
+    TYPE (soft) clips every entry to [xmin, xmax]; otherwise entries whose
+    mask is neither 0 nor 2 are clipped and the others reset to xinit."""
+    if soft:
+        np.maximum(xmin, x, out=x)
+        np.minimum(xmax, x, out=x)
+        return x
+    m = np.asarray(mask, np.float32).ravel()
+    free = (m != 0) & (m != 2)
+    x[free] = np.minimum(xmax, np.maximum(xmin, x[free]))
+    x[~free] = np.asarray(xinit, np.float64).ravel()[~free]
+    return x
+
+
+def l_bfgs(fctgdt, x, niter, neval, xmin, xmax, vpmask=None, const_type=2, freeze_soft=True,
+           vpinit=None, msave=5):
+    """l_bfgs (libs/libwave/Inversion.f90:29-189) over the oracle's LBFGS
+    (lbfgs.f restated in swave_oracle.cpp).
+
+    fctgdt(x, eval) -> (f: float (FP64), g: float32 array): the objective
+    and gradient at the FP32 model x on evaluation `eval` (invparam%eval).
+    At evaluation 0 the scalings g0 = max(x) / (100 max|g|) (FP32) and
+    f0 = max(x)^2 / |f| (FP64) are fixed and then applied to every
+    evaluation (Inversion.f90:118-125: f and g are scaled differently, a
+    quirk kept as is); LBFGS receives the scaled f and minus the scaled g
+    (gd = -dble(g), :130).  After each completed iteration the saved model
+    goes through FREEZE_X when const_type = 2 (:140).  The loop ends after
+    niter iterations, neval evaluations or when LBFGS returns iflag <= 0;
+    in the last two cases the model of the last completed iteration is
+    returned (:177-182).
+
+    Returns (x, history) with history the values the reference writes to
+    its 'function' file: f0*f at evaluation 0, then the scaled f of every
+    completed iteration; plus the saved models of the iterations.
+    """
+    x = np.ascontiguousarray(x, np.float32).ravel().copy()
+    n = x.size
+    mask = np.ones(n, np.float32) if vpmask is None else np.ascontiguousarray(vpmask, np.float32).ravel()
+    vpinit = x.astype(np.float64) if vpinit is None else np.ascontiguousarray(vpinit, np.float64).ravel()
+    lb = LBFGS(n, msave, float(xmin), float(xmax), mask=mask, bound_type=const_type,
+               freeze_soft=freeze_soft, xinit=vpinit)
+    xsave = x.astype(np.float64)
+    eval_, count, cont, found = 0, 0, True, False
+    g0, f0 = np.float32(0), 0.0
+    history, models = [], []
+    while cont and not found:
+        fd, g = fctgdt(x, eval_)
+        g = np.asarray(g, np.float32).ravel()
+        if eval_ == 0:
+            mx = np.float32(x.max())
+            g0 = np.float32(mx / (np.float32(100) * np.float32(np.abs(g).max())))
+            f0 = float(np.float64(mx * mx)) / abs(fd)
+            history.append(np.float32(f0 * fd))
+        g = (g0 * g).astype(np.float32)
+        fd = f0 * fd
+        xd = x.astype(np.float64)
+        gd = -g.astype(np.float64)
+        xdsave = xd.copy()
+        iflag, myinfo = lb.step(xd, fd, gd, eps=1.0e-20, xtol=np.finfo(np.float64).eps)
+        x = xd.astype(np.float32)
+        if myinfo == 1:
+            if const_type == 2:
+                freeze_x(xdsave, float(xmin), float(xmax), mask, freeze_soft, vpinit)
+            xsave = xdsave
+            count += 1
+            found = count >= niter
+            models.append(xdsave.astype(np.float32))
+            history.append(np.float32(fd))
+        if iflag <= 0:
+            cont = False
+        eval_ += 1
+        if eval_ >= neval:
+            cont = False
+    if not cont:
+        x = xsave.astype(np.float32)
+    return x, np.array(history, np.float32), models

@@ -157,11 +157,14 @@ def config2(nt_cap: int | None = None) -> tuple:
 
 
 def config2_window(shot: dict) -> tuple[int, int]:
-    """Columns [i0, i0 + nxw) of a config-2 shot's window (aperture 0: the
-    source and its receiver spread)."""
+    """Columns [i0, i0 + nxw) of a config-2 shot's window with aperture 0:
+    the patch spanned by the source and its receivers
+    (extract_coord_source_receiver_patch, ExtractPadModel.f90:19-85).  The
+    receivers of these shots bracket the source and sit on grid columns."""
     d = CONFIG2["d"]
-    lo = min(shot["lo"], float(shot["sou"][1]))
-    hi = max(shot["hi"], float(shot["sou"][1]))
+    rx = np.asarray(shot["rec"])[:, 1]
+    lo = min(float(rx.min()), float(shot["sou"][1]))
+    hi = max(float(rx.max()), float(shot["sou"][1]))
     return int(round(lo / d)), int(round((hi - lo) / d)) + 1
 
 

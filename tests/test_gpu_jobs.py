@@ -274,3 +274,36 @@ def test_autotuner_chooses_shots_per_launch(oracle, tmp_path):
     rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
     np.testing.assert_array_equal(im, rim)
     np.testing.assert_array_equal(il, ril)
+
+
+def test_fwi_gradient_fd_check_on_device(oracle):
+    """The device's raw FWI gradient against centred finite differences of
+    the device's misfit along the 8 seeded smooth directions of the oracle's
+    check (rigid boundary, illu_pow 0, no smoothing, snapi 1, 6 Hz; see
+    tests/test_oracle_pins.py:fd_gradient_check), to the same bound, and the
+    device's raw gradient against the oracle's."""
+    from tests.test_oracle_pins import check_fd, fd_gradient_check
+    c = sw.Context(0)
+    try:
+        c.set_boundary(1)
+
+        def fct_gdt(desc, vel, w, shots):
+            want = all("resid" in s for s in shots)
+            out = c.fwi_fct_gdt(desc, vel, w, shots, want_resid=want)
+            if want:
+                for s, r in zip(shots, out[3]):
+                    s["resid"][...] = r
+            return out[0], out[1]
+
+        an, fd = fd_gradient_check(fct_gdt)
+    finally:
+        c.close()
+    check_fd(an, fd)
+    oracle.set_rigid(True)
+    try:
+        ran, rfd = fd_gradient_check(
+            lambda desc, vel, w, shots: oracle.fwi_fct_gdt(desc, vel, w, shots)[:2])
+    finally:
+        oracle.set_rigid(False)
+    np.testing.assert_array_equal(fd, rfd)       # FP64 misfits summed in the same order
+    assert rel_l2(an, ran) < 1e-6

@@ -61,32 +61,71 @@ def _fwi_setup(snapi=1):
     return desc, vtrue, v0, w, shots
 
 
-def test_fwi_gradient_along_smooth_directions(oracle):
-    """Finite differences of the misfit along 8 seeded smooth directions
-    against <g, dm> from compute_fct_gdt (compute_function_gradient.f90:
-    208-350, AFWI imaging Imaging.f90:371-422).  The reference's gradient is
-    a descent direction (l_bfgs negates it, Inversion.f90:118-125) from an
-    approximate adjoint, so the check is on correlation and sign: the
-    directional derivatives correlate at > 0.85 with minus the FD values."""
+def fd_gradient_check(fct_gdt):
+    """Centred finite differences (h = 2 m/s) of the misfit along 8 seeded
+    smooth directions against <g, dm> for the raw gradient of
+    compute_fct_gdt (compute_function_gradient.f90:208-350, AFWI imaging
+    Imaging.f90:371-422): illu_pow = 0, no smoothing, no mask, snapi = 1, a
+    6 Hz Ricker, rigid boundary (set by the caller).  The directions vanish
+    in the 8 rows next to the sources and receivers, where the imaging
+    condition's d2s/dt2 / v^3 carries the source term that the derivative of
+    the discrete misfit does not have.  The reference's gradient is minus the
+    derivative (l_bfgs hands -g to LBFGS, Inversion.f90:130).
+    fct_gdt(desc, vel, w, shots) -> (f, grad); returns (an, -fd)."""
     from scipy.ndimage import gaussian_filter
     desc, vtrue, v0, w, shots = _fwi_setup()
-    oracle.fwi_fct_gdt(desc, vtrue, w, shots)           # data of the true model
+    w = synth.ricker(6.0, desc.g.dt, desc.g.nt)
+    fct_gdt(desc, vtrue, w, shots)                      # data of the true model
     for s in shots:
         s["dobs"] = -s.pop("resid")                     # resid = dobs - dmod with dobs = 0
-    f0, g0, _ = oracle.fwi_fct_gdt(desc, v0, w, shots)
+    f0, g0 = fct_gdt(desc, v0, w, shots)
     assert f0 > 0 and np.abs(g0).max() > 0
+    taper = np.clip((np.arange(v0.shape[1]) - 8) / 5.0, 0.0, 1.0)[None, :]
     rng = np.random.default_rng(8)
     an, fd = [], []
+    h = 2.0
     for _ in range(8):
-        dm = gaussian_filter(rng.standard_normal(v0.shape), 4.0)
+        dm = gaussian_filter(rng.standard_normal(v0.shape), 4.0) * taper
         dm /= np.abs(dm).max()
-        fp, _, _ = oracle.fwi_fct_gdt(desc, (v0 + dm).astype(np.float32), w, shots)
-        fm, _, _ = oracle.fwi_fct_gdt(desc, (v0 - dm).astype(np.float32), w, shots)
-        fd.append((fp - fm) / 2.0)
+        fp, _ = fct_gdt(desc, (v0 + h * dm).astype(np.float32), w, shots)
+        fm, _ = fct_gdt(desc, (v0 - h * dm).astype(np.float32), w, shots)
+        fd.append(-(fp - fm) / (2.0 * h))
         an.append(float(np.dot(g0.astype(np.float64).ravel(), dm.ravel())))
-    an, fd = np.array(an), np.array(fd)
-    assert np.corrcoef(an, -fd)[0, 1] > 0.85
-    assert np.dot(an, fd) < 0
+    return np.array(an), np.array(fd)
+
+
+# Achieved on the oracle (and, bit for bit the same misfits, on the GPU): the
+# 8 directional derivatives agree with the centred differences to 8.4 %
+# relative L2 over the 8 directions, the least-squares scale is 0.995.  The
+# gap is the reference's: its imaging condition is the continuous adjoint
+# state's, with data taken from u2 before the step and sources injected
+# after it (Propagator.f90:177,209), a phase lag that grows with frequency
+# (29 % at 12 Hz on the same model).
+FD_REL_L2 = 0.12
+FD_SCALE = (0.9, 1.1)
+
+
+def check_fd(an, fd):
+    rel = float(np.linalg.norm(an - fd) / np.linalg.norm(fd))
+    scale = float(np.dot(an, fd) / np.dot(an, an))
+    assert rel < FD_REL_L2, (rel, an, fd)
+    assert FD_SCALE[0] < scale < FD_SCALE[1], (scale, an, fd)
+    return rel, scale
+
+
+def test_fwi_gradient_along_smooth_directions(oracle):
+    """The raw FWI gradient against centred finite differences of the misfit
+    (see fd_gradient_check) on the oracle with the rigid boundary: a sign or
+    scale error in the AFWI imaging term fails the 12 % / [0.9, 1.1] bound."""
+    def fct_gdt(desc, vel, w, shots):
+        f, g, _ = oracle.fwi_fct_gdt(desc, vel, w, shots)
+        return f, g
+    oracle.set_rigid(True)
+    try:
+        an, fd = fd_gradient_check(fct_gdt)
+    finally:
+        oracle.set_rigid(False)
+    check_fd(an, fd)
 
 
 def test_backward_reconstruction_from_strips_diverges():
