@@ -73,6 +73,12 @@ __device__ __forceinline__ void pdl_launch_dependents() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Orders this thread's generic-proxy shared-memory writes before later
+// tensor copies (async proxy) into the same memory.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
                : "memory");
@@ -286,16 +292,24 @@ __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp,
 // (forward).  u2c receives the raw u2 values of the two columns.  Per lane
 // the operations are those of the scalar loops (FDderivatives.f90:715-743
 // forward, 847-891 adjoint).
-template <bool ADJ>
+template <bool ADJ, bool PRE = false>
 __device__ __forceinline__ void t2_pair_fast(const T2Pairs &c, const float *col0,
                                              const float *vcol0, const float *vcore0,
                                              P2 sv[2][2], float4 u2c[2]) {
   float4 N[10];
+  if (PRE) {
+    // vcol0 points at the staged w = (v*v)*u of the tile (t2_premul).
+    u2c[0] = lds4(col0);
+    u2c[1] = lds4(col0 + T2_SZ);
 #pragma unroll
-  for (int m = 0; m < 10; ++m) N[m] = lds4(col0 + (m - 4) * T2_SZ);
-  u2c[0] = N[4];
-  u2c[1] = N[5];
-  if (ADJ) {
+    for (int m = 0; m < 10; ++m) N[m] = lds4(vcol0 + (m - 4) * T2_SZ);
+  } else {
+#pragma unroll
+    for (int m = 0; m < 10; ++m) N[m] = lds4(col0 + (m - 4) * T2_SZ);
+    u2c[0] = N[4];
+    u2c[1] = N[5];
+  }
+  if (ADJ && !PRE) {
     // w = (v*v)*u at every stencil point (FDderivatives.f90:847-891).
 #pragma unroll
     for (int m = 0; m < 10; ++m) {
@@ -308,8 +322,16 @@ __device__ __forceinline__ void t2_pair_fast(const T2Pairs &c, const float *col0
 #pragma unroll
   for (int cc = 0; cc < 2; ++cc) {
     const float *col = col0 + cc * T2_SZ;
-    float4 za = lds4(col - 4), zc = lds4(col + 4);
-    if (ADJ) {
+    float4 za, zc;
+    if (PRE) {
+      const float *wcol = vcol0 + cc * T2_SZ;
+      za = lds4(wcol - 4);
+      zc = lds4(wcol + 4);
+    } else {
+      za = lds4(col - 4);
+      zc = lds4(col + 4);
+    }
+    if (ADJ && !PRE) {
       const float *vcol = vcol0 + cc * T2_SZ;
       const float4 va = lds4(vcol - 4), vc = lds4(vcol + 4);
       const P2 a0 = s_mul(p_mul(lo2(va), lo2(va)), lo2(za));
@@ -353,12 +375,35 @@ __device__ __forceinline__ void t2_pair_fast(const T2Pairs &c, const float *col0
   }
 }
 
+// The adjoint stencil's w = (v*v)*u (FDderivatives.f90:847-891) over the
+// whole staged u2 halo tile, written over the staged velocity halo: every
+// staged value is squared and multiplied once per tile instead of once per
+// stencil point that reads it.  Same operations, same roundings.  The
+// caller synchronises before the tile is computed.
+__device__ __forceinline__ void t2_premul(float *st, int tid, int nthreads) {
+  const float4 *u = reinterpret_cast<const float4 *>(st);
+  float4 *vw = reinterpret_cast<float4 *>(st + T2_HALO);
+  for (int q = tid; q < T2_HALO / 4; q += nthreads) {
+    const float4 v = vw[q], x = u[q];
+    const P2 a = s_mul(p_mul(lo2(v), lo2(v)), lo2(x));
+    const P2 b = s_mul(p_mul(hi2(v), hi2(v)), hi2(x));
+    vw[q] = make_float4(a.x, a.y, b.x, b.y);
+  }
+}
+
+// Whether an adjoint tile reads the staged velocity itself (LSRTM imaging,
+// and the element-by-element snapshot work: AFWI imaging and the Born
+// source); the others take the pre-multiplied w (t2_premul).
+__device__ __forceinline__ bool t2_needs_vel(const T2Shot &h, const T2Step &stp, int e) {
+  return stp.img == 2 || (stp.snap && h.imaging > 2 && t2_phys_tile(h, e));
+}
+
 // Computes one tile from a completed stage.  Thread (tz, tx) owns rows
 // i0..i0+3 of the adjacent columns x0+2tx and x0+2tx+1.
 template <bool ADJ>
 __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h,
                                            const T2Step &stp, int b, int s, int e,
-                                           const float *st, int tid) {
+                                           const float *st, int tid, bool pre) {
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
   const int tz = tid & 15, tx = tid >> 4;
   const int i0 = z0 + 4 * tz;
@@ -389,7 +434,11 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   // any index equals the clamped lookup; no tile needs a special case.
   {
     const int o = (2 * tx + 4) * T2_SZ + 4 * tz + 4;
-    t2_pair_fast<ADJ>(c, su + o, svel + o, core + 3 * T2_CORE + 2 * tx * T2_Z + 4 * tz, sv, u2c);
+    if (ADJ && pre)
+      t2_pair_fast<ADJ, true>(c, su + o, svel + o, nullptr, sv, u2c);
+    else
+      t2_pair_fast<ADJ, false>(c, su + o, svel + o, core + 3 * T2_CORE + 2 * tx * T2_Z + 4 * tz,
+                               sv, u2c);
   }
   if (slow_extras) {
     const ShotDev &S = t.shots[b];
@@ -691,12 +740,20 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       *abort_flag = 1;
     }
     {
-      const float *st = t2_smem + cur * SF;
-      t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st, tid);
+      float *st = t2_smem + cur * SF;
+      const bool pre = ADJ && !t2_needs_vel(h, stp, e);
+      if (pre) {
+        t2_premul(st, tid, 256);
+        __syncthreads();
+      }
+      t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, st, tid, pre);
       if ((stp.extract || stp.img) && t2_phys_tile(h, e))
         t2_snap_tile<ADJ>(h, stp, P, e, st, ADJ ? st + T2_HALO : st + T2_HALO + 3 * T2_CORE,
                           tid);
       t2_edges<ADJ>(h, s, e, st, tid, 0);
+      // The stage was written (t2_premul): order that before the tensor
+      // copies of tile k+2 overwrite it.
+      if (pre) fence_proxy_async_smem();
     }
     __syncthreads();   // the stage is free for tile k+2
     if (*abort_flag) {
@@ -817,12 +874,18 @@ __device__ __forceinline__ void tile2d_ws(const BatchTables &t, int s_off, int n
       atomicOr(t.err, 1);
       *abort_flag = 1;
     }
-    const float *stg = t2_smem + st * SF;
-    t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, stg, gtid);
+    float *stg = t2_smem + st * SF;
+    const bool pre = ADJ && !t2_needs_vel(h, stp, e);
+    if (pre) {
+      t2_premul(stg, gtid, 256);
+      t2_bar(1 + g);
+    }
+    t2_compute<ADJ>(t, h, stp, t2_b(e), s, e, stg, gtid, pre);
     if ((stp.extract || stp.img) && t2_phys_tile(h, e))
       t2_snap_tile<ADJ>(h, stp, P, e, stg,
                         ADJ ? stg + T2_HALO : stg + T2_HALO + 3 * T2_CORE, gtid);
     t2_edges<ADJ>(h, s, e, stg, gtid, 1 + g);
+    if (pre) fence_proxy_async_smem();
     __syncwarp();
     if ((tid & 31) == 0) mbar_arrive(&empty[st]);
   }
