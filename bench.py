@@ -266,6 +266,9 @@ def main():
                     help="run the learned-preconditioner FWI study instead of the RTM bench")
     ap.add_argument("--model3d", action="store_true",
                     help="time 3D modelling of one shot instead of the 2D RTM bench")
+    ap.add_argument("--revolve-study", action="store_true",
+                    help="FWI gradient memory modes on the 1201 x 3401 grid: store-all against "
+                         "binomial checkpointing with 32/64/128 state slots")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every time step directly (profiling runs: every launch timed)")
     args = ap.parse_args()
@@ -275,6 +278,8 @@ def main():
         return run_precond_study()
     if args.model3d:
         return run_model3d(args)
+    if args.revolve_study:
+        return run_revolve_study(args)
 
     import torch
 
@@ -508,6 +513,72 @@ def run_model3d(args) -> int:
         "clocks": clk, "gpu_launches": int(st["launches_total"]),
     }
     print(json.dumps(line))
+    return 0
+
+
+def run_revolve_study(args) -> int:
+    """FWI gradient of one shot on the 1201 x 3401 grid at 6.25 m (dt 0.5 ms,
+    10000 steps unless --nt-cap): store-all snapshots in HBM against the
+    binomial checkpoint schedule with 32, 64 and 128 state slots (segments
+    of 10 snapshots).  Per mode: device memory of the snapshot store, forward
+    and backward time steps (recompute factor = forward steps / nt), wall
+    time per gradient, and whether misfit and gradient equal store-all's bit
+    for bit.  One JSON line."""
+    import torch
+
+    import seismic_gb300 as sw
+    from seismic_gb300 import synth
+    torch.cuda.set_device(0)
+    ctx = sw.Context(0)
+    c3 = synth.config3(nt=args.nt_cap or None)
+    g, vb, ref, rec = c3["g"], c3["vel"], c3["ref"], c3["rec"]
+    w = c3["wavelet"]
+    nt = g.nt
+    vtrue = (vb * (1.0 + ref)).astype(np.float32)
+    sou = c3["shots"][len(c3["shots"]) // 2]
+    desc = sw.SwFwiDesc()
+    desc.g = g
+    desc.aperture_x, desc.aperture_y, desc.illu_pow = 1e5, 0.0, 1.0
+    desc.smooth_rect1 = desc.smooth_rect2 = desc.smooth_rect3 = 1
+    shot = {"sou": sou, "rec": rec, "dobs": np.zeros((rec.shape[0], nt), np.float32)}
+    _, _, _, res = ctx.fwi_fct_gdt(desc, vtrue, w, [shot], want_resid=True)
+    shot["dobs"] = -res[0]                       # data of the true model
+    nw = g.nz * g.nx
+    pad = (g.nz + 2 * g.ntaper + 8) * (g.nx + 2 * g.ntaper + 8)
+    ntsnap = nt // g.snapi
+    K = 10
+    rows, base = [], None
+    for slots in (None, 32, 64, 128):
+        desc.checkpoint_snaps = 0 if slots is None else K
+        desc.revolve_slots = 0 if slots is None else slots
+        ctx.fwi_fct_gdt(desc, vb, w, [shot])     # warm-up (arena, graphs)
+        ctx.reset_stats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        f, grad, _ = ctx.fwi_fct_gdt(desc, vb, w, [shot])
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        st = ctx.stats()
+        if slots is None:
+            mem = ntsnap * nw * 4
+            base = (f, grad)
+        else:
+            mem = (slots + 1) * 4 * pad * 4 + (K + 2) * nw * 4
+        rows.append({"mode": "store-all" if slots is None else f"revolve-{slots}",
+                     "snapshot_store_gb": mem / 1e9,
+                     "steps_forward": int(st["steps_forward"]),
+                     "steps_backward": int(st["steps_backward"]),
+                     "recompute_factor": st["steps_forward"] / nt,
+                     "segment_advances": int(st["ckpt_advances"]),
+                     "seconds_per_gradient": secs,
+                     "gpts_per_s": st["points_updated"] / secs / 1e9,
+                     "bitexact_vs_store_all": bool(f == base[0] and np.array_equal(grad, base[1]))})
+        log(json.dumps(rows[-1]))
+    print(json.dumps({"study": "FWI gradient memory modes", "grid": [g.nz, g.nx],
+                      "spacing_m": g.dx, "dt_s": g.dt, "nt": nt, "snapi": g.snapi,
+                      "segment_snapshots": K, "receivers": int(rec.shape[0]), "rows": rows}),
+          flush=True)
+    ctx.close()
     return 0
 
 

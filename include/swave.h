@@ -324,6 +324,14 @@ typedef struct sw_fwi_desc {
    * traces of the gather then use). */
   int dat_nrm_type;
   float dat_thresh;
+  /* Binomial checkpointing (revolve; no counterpart in the reference): with
+   * checkpoint_snaps = K > 0 and revolve_slots = s > 0 the forward states
+   * at segment boundaries are kept in s slots (+ one work slot) chosen by
+   * the binomial schedule over the ntsnap/K segments instead of all of
+   * them: memory (s + 1) x 4 padded fields + (K + 2) snapshots, segment
+   * advances = the minimum for s + 1 checkpoints (the zero initial state
+   * is the first); results identical to store-all.  0 = every boundary. */
+  int revolve_slots;
 } sw_fwi_desc;
 
 enum { SW_NRM_L1 = 1, SW_NRM_L2 = 2, SW_NRM_CAUCHY = 3, SW_NRM_HYPERBOLIC = 4,
@@ -466,6 +474,9 @@ typedef struct sw_stats {
                                    (only while profiling is on)              */
   uint64_t step_kernel_timed;   /* number of timed fused-kernel launches     */
   uint64_t step_bytes;          /* algorithmic bytes of those launches       */
+  uint64_t steps_forward;       /* time steps of forward (tstep = +1) runs    */
+  uint64_t steps_backward;      /* time steps of backward (tstep = -1) runs   */
+  uint64_t ckpt_advances;       /* checkpoint-segment advances of FWI runs    */
 } sw_stats;
 int sw_ctx_get_stats(const sw_ctx *ctx, sw_stats *out);
 int sw_ctx_reset_stats(sw_ctx *ctx);

@@ -69,7 +69,8 @@ class SwFwiDesc(C.Structure):
                 ("illu_pow", C.c_float), ("smooth_rect1", C.c_int), ("smooth_rect2", C.c_int),
                 ("smooth_rect3", C.c_int), ("smooth_doz", C.c_int), ("smooth_dox", C.c_int),
                 ("smooth_doy", C.c_int), ("checkpoint_snaps", C.c_int),
-                ("dat_nrm_type", C.c_int), ("dat_thresh", C.c_float)]
+                ("dat_nrm_type", C.c_int), ("dat_thresh", C.c_float),
+                ("revolve_slots", C.c_int)]
 
 
 class SwRegDesc(C.Structure):
@@ -123,7 +124,9 @@ class SwTuning(C.Structure):
 class SwStats(C.Structure):
     _fields_ = [("launches_total", C.c_uint64), ("launches_step", C.c_uint64),
                 ("points_updated", C.c_uint64), ("step_kernel_ms", C.c_double),
-                ("step_kernel_timed", C.c_uint64), ("step_bytes", C.c_uint64)]
+                ("step_kernel_timed", C.c_uint64), ("step_bytes", C.c_uint64),
+                ("steps_forward", C.c_uint64), ("steps_backward", C.c_uint64),
+                ("ckpt_advances", C.c_uint64)]
 
 
 # Every symbol of include/swave.h with its signature.

@@ -223,7 +223,77 @@ inline int gsz(long long n) {
   return (int)std::max(1LL, std::min(b, 152LL * 8));
 }
 
+// ---------------------------------------------------------------------------
+// Binomial checkpoint schedule (revolve) over checkpoint segments.
+// Reversing l segments whose first state is available, with s free state
+// slots, takes at least t(l, s + 1) segment advances (Griewank 1992:
+// t(l, c) = r l - beta(c + 1, r - 1) with beta(c, r) = (c + r)! / (c! r!) and
+// r the smallest integer with beta(c, r) >= l).  The schedule attains it by
+// splitting at the m minimising m + t(l - m, s - 1) + t(m, s): advance m
+// segments, keep that state in a slot, reverse the last l - m segments with
+// one slot less, release the slot, reverse the first m.  Without a free
+// slot every segment is reached from the first state through a work slot.
+// ---------------------------------------------------------------------------
+double binom_beta(int c, long long r) {
+  if (r < 0) return 0.0;
+  double b = 1.0;
+  for (long long i = 1; i <= r; ++i) b = b * (double)(c + i) / (double)i;
+  return b;
+}
+
+long long revolve_advances(long long l, int s) {
+  if (l <= 1) return 0;
+  const int c = s + 1;
+  long long r = 0;
+  double b = 1.0;   // beta(c, r)
+  while (b < (double)l) {
+    ++r;
+    b = b * (double)(c + r) / (double)r;
+  }
+  return r * l - (long long)std::llround(binom_beta(c + 1, r - 1));
+}
+
+struct CkOp {
+  int process;   // 0: advance S_a -> S_b from slot src into slot dst; 1: segment a from src
+  int a, b, src, dst;
+};
+
+void revolve_schedule(int a, int b, int src, std::vector<int> &freel, int work,
+                      std::vector<CkOp> &ops) {
+  const int l = b - a;
+  if (l == 1) {
+    ops.push_back({1, a, a + 1, src, -1});
+    return;
+  }
+  const int s = (int)freel.size();
+  if (s == 0) {
+    for (int k = b - 1; k > a; --k) {
+      ops.push_back({0, a, k, src, work});
+      ops.push_back({1, k, k + 1, work, -1});
+    }
+    ops.push_back({1, a, a + 1, src, -1});
+    return;
+  }
+  long long best = -1;
+  int bm = 1;
+  for (int m = 1; m < l; ++m) {
+    const long long cost = m + revolve_advances(l - m, s - 1) + revolve_advances(m, s);
+    if (best < 0 || cost < best) {
+      best = cost;
+      bm = m;
+    }
+  }
+  const int slot = freel.back();
+  freel.pop_back();
+  ops.push_back({0, a, a + bm, src, slot});
+  revolve_schedule(a + bm, b, slot, freel, work, ops);
+  freel.push_back(slot);
+  revolve_schedule(a, a + bm, src, freel, work, ops);
+}
+
 }  // namespace
+
+long long sw_revolve_advances_internal(long long l, int s) { return revolve_advances(l, s); }
 
 // ---------------------------------------------------------------------------
 // compute_fct_gdt
@@ -307,6 +377,10 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     const int K = d.checkpoint_snaps > 0 ? std::max(d.checkpoint_snaps, 2) : 0;
     const bool ckpt = K > 0 && ntsnap > K;
     const int nseg = ckpt ? (ntsnap + K - 1) / K : 1;
+    // Binomial schedule: nslot state slots (+ one work slot) instead of one
+    // per segment boundary; the forward runs happen inside the schedule.
+    const int nslot = ckpt && d.revolve_slots > 0 ? std::min(d.revolve_slots, nseg - 1) : 0;
+    const bool revolve = nslot > 0;
     const size_t nf = (size_t)Gw.total();
     float *dck = nullptr, *dseg = nullptr, *dadj = nullptr;
     if (!ckpt) {
@@ -314,6 +388,11 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
       a.wave_dev = (float *)p;
       fd.extract_wave = 1;
       if ((st = propagate_dev(c, fd, a))) return st;
+    } else if (revolve) {
+      dck = (float *)dbuf(c, "fwi_ckpt", (size_t)(nslot + 1) * 4 * nf * sizeof(float), &st);
+      dseg = (float *)dbuf(c, "fwi_seg", (size_t)(K + 2) * nw * sizeof(float), &st);
+      dadj = (float *)dbuf(c, "fwi_adj_state", 4 * nf * sizeof(float), &st);
+      if (!dck || !dseg || !dadj) return st;
     } else {
       // Forward in segments; the state after step (jK-1)*snapi, j = 1..nseg-1,
       // is kept as checkpoint j (4 padded fields).
@@ -330,8 +409,12 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
         aj.save_state = j < nseg - 1 ? dck + (size_t)j * 4 * nf : nullptr;
         if ((st = propagate_dev(c, fd, aj))) return st;
       }
+      c->stats.ckpt_advances += (uint64_t)(nseg - 1);
     }
-    // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40).
+    // Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40);
+    // with the binomial schedule it runs once the first pass has reached
+    // the end of the record.
+    auto residual = [&]() -> int {
     float *ddobs = nullptr, *dmute = nullptr, *dres = nullptr;
     if ((st = upload(c, "dobs", sh.dobs, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
     ddobs = (float *)p;
@@ -361,6 +444,9 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     part.resize(sh.nrec);
     if ((st = download(c, part.data(), dpart, (size_t)sh.nrec * sizeof(double)))) return st;
     if (sh.resid && (st = download(c, sh.resid, dres, (size_t)sh.nrec * nt * sizeof(float)))) return st;
+    return SW_OK;
+    };
+    if (!revolve && (st = residual())) return st;
     // AGRAD_to_memory (to_disk_to_memory_AGRAD.f90:27-79).
     DevIO b;
     b.vel_pad = vpad;
@@ -390,19 +476,29 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
       // The wave pointer is offset so that the kernels' global snapshot
       // numbers land in the segment buffer.
       sw_prop_desc rd = fd;
-      rd.extraction = SW_EXT_NONE;
       rd.extract_wave = 1;
-      for (int j = nseg - 1; j >= 0; --j) {
+      // The forward steps already run (their data are extracted once).
+      int frontier = 0;
+      // Segment j: recompute its K + 2 snapshots from its first state, then
+      // the backward steps whose imaging reads them.
+      auto segment = [&](int j, const float *state) -> int {
         float *wbase = dseg - (ptrdiff_t)(j * K - 1) * (ptrdiff_t)nw;
         rd.tmin = j == 0 ? 1 : (j * K - 1) * g.snapi + 1;
         rd.tmax = std::min(((j + 1) * K + 1) * g.snapi, nt);
+        const bool first = revolve && rd.tmin == frontier + 1;
         DevIO rj = a;
-        rj.nrec = 0;
-        rj.rec_trace_dev = nullptr;
+        rd.extraction = first ? fd.extraction : SW_EXT_NONE;
+        if (!first) {
+          rj.nrec = 0;
+          rj.rec_trace_dev = nullptr;
+        }
         rj.wave_dev = wbase;
         rj.tcnt = 1;
-        rj.init_state = j > 0 ? dck + (size_t)(j - 1) * 4 * nf : nullptr;
-        if ((st = propagate_dev(c, rd, rj))) return st;
+        rj.init_state = state;
+        int q;
+        if ((q = propagate_dev(c, rd, rj))) return q;
+        frontier = std::max(frontier, rd.tmax);
+        if (first && (q = residual())) return q;
         bd.tmin = j == nseg - 1 ? nt : (j + 1) * K * g.snapi;
         bd.tmax = j == 0 ? 1 : j * K * g.snapi + 1;
         DevIO bj = b;
@@ -410,7 +506,43 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
         bj.tcnt = nt;
         bj.init_state = j == nseg - 1 ? nullptr : dadj;
         bj.save_state = j > 0 ? dadj : nullptr;
-        if ((st = propagate_dev(c, bd, bj))) return st;
+        return propagate_dev(c, bd, bj);
+      };
+      if (!revolve) {
+        for (int j = nseg - 1; j >= 0; --j)
+          if ((st = segment(j, j > 0 ? dck + (size_t)(j - 1) * 4 * nf : nullptr))) return st;
+      } else {
+        std::vector<int> freel(nslot);
+        for (int q = 0; q < nslot; ++q) freel[q] = q;
+        std::vector<CkOp> ops;
+        revolve_schedule(0, nseg, -1, freel, nslot, ops);
+        auto slot = [&](int q) { return q < 0 ? nullptr : dck + (size_t)q * 4 * nf; };
+        for (const CkOp &op : ops) {
+          if (op.process) {
+            if ((st = segment(op.a, slot(op.src)))) return st;
+            continue;
+          }
+          // Advance S_a -> S_b (the state after step (bK - 1) snapi); the
+          // first pass over these steps extracts the data.
+          fd.tmin = op.a == 0 ? 1 : (op.a * K - 1) * g.snapi + 1;
+          fd.tmax = (op.b * K - 1) * g.snapi;
+          const bool first = fd.tmin == frontier + 1;
+          if (!first && fd.tmax > frontier)
+            return fail(c, SW_BAD_PARAM, "checkpoint schedule runs past the first pass");
+          DevIO aj = a;
+          sw_prop_desc fa = fd;
+          if (!first) {
+            fa.extraction = SW_EXT_NONE;
+            aj.nrec = 0;
+            aj.rec_trace_dev = nullptr;
+          }
+          aj.tcnt = 1;
+          aj.init_state = slot(op.src);
+          aj.save_state = slot(op.dst);
+          if ((st = propagate_dev(c, fa, aj))) return st;
+          frontier = std::max(frontier, fd.tmax);
+          c->stats.ckpt_advances += (uint64_t)(op.b - op.a);
+        }
       }
     }
     // mod_copy_image (ExtractPadModel.f90:662-697), shots in order.

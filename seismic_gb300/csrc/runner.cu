@@ -634,6 +634,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   uint64_t upd = 0;
   for (auto &S : hs) upd += (uint64_t)S.npts * (uint64_t)S.nsteps;
   c->stats.points_updated += upd;
+  for (auto &S : hs) (S.tstep > 0 ? c->stats.steps_forward : c->stats.steps_backward) += S.nsteps;
   c->stats.launches_total += launches;
   c->stats.launches_step += (uint64_t)max_steps;
   // ---- outputs ----

@@ -156,6 +156,55 @@ def test_fwi_checkpointed_equals_store_all(ctx, K):
     assert 1.4 * pts_all < pts_ck <= (1.0 + (K + 2) / (2.0 * K) + 0.02) * pts_all
 
 
+def _binomial_advances(l, s):
+    """t(l, c) with c = s + 1 checkpoints (Griewank 1992): the fewest
+    segment advances that reverse l segments."""
+    from math import comb
+    if l <= 1:
+        return 0
+    c = s + 1
+    r = 0
+    while comb(c + r, c) < l:
+        r += 1
+    return r * l - (comb(c + 1 + r - 1, c + 1) if r >= 1 else 0)
+
+
+@pytest.mark.parametrize("K,slots", [(2, 1), (2, 2), (2, 3), (3, 1), (2, 100)])
+def test_fwi_revolve_equals_store_all(ctx, K, slots):
+    """The binomial (revolve) schedule over checkpoint segments gives the
+    store-all misfit and gradient bit for bit, with the number of segment
+    advances the binomial formula gives for slots + 1 checkpoints (the zero
+    initial state is the first), and no more forward steps than the
+    uniform scheme needs when slots cover every segment boundary."""
+    d, vel, w, shots, mask = _fwi_case()
+    d.checkpoint_snaps = 0
+    d.revolve_slots = 0
+    f0, g0, il0 = ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    d.checkpoint_snaps = K
+    d.revolve_slots = slots
+    ctx.reset_stats()
+    f1, g1, il1 = ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    st = ctx.stats()
+    assert f1 == f0
+    np.testing.assert_array_equal(g1, g0)
+    np.testing.assert_array_equal(il1, il0)
+    ntsnap = d.g.nt // d.g.snapi
+    nseg = (ntsnap + K - 1) // K
+    s_eff = min(slots, nseg - 1)
+    assert st["ckpt_advances"] == len(shots) * _binomial_advances(nseg, s_eff)
+    d.revolve_slots = 0
+    ctx.reset_stats()
+    ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    uni = ctx.stats()
+    assert uni["ckpt_advances"] == len(shots) * (nseg - 1)
+    assert st["steps_backward"] == uni["steps_backward"]
+    if s_eff == nseg - 1:
+        assert st["steps_forward"] <= uni["steps_forward"]
+    else:
+        assert st["steps_forward"] > uni["steps_forward"]
+    d.checkpoint_snaps = 0
+
+
 def test_lbfgs_device_matches_oracle(ctx, oracle):
     """A few LBFGS iterations on a bound-constrained quadratic."""
     n = 5000
