@@ -296,7 +296,8 @@ def main():
     B = args.shots_per_step
     nsteps = args.warmup + args.steps
     # Shots of this rank: rank r takes every ws-th shot of the survey.
-    mine = shots[rank::ws]
+    from seismic_gb300 import dist as sdist
+    mine = [shots[i] for i in sdist.shard(len(shots), rank, ws)]
     per_step = [mine[(k * B + q) % len(mine)] for k in range(nsteps) for q in range(B)]
     # Observed data: batched forward modelling on each shot's window (untimed).
     distinct = {}
@@ -341,8 +342,8 @@ def main():
         job.run(k * B, B)
         points += sum(shot_points(s) for s in per_step[k * B:(k + 1) * B])
     if ws > 1:
-        im = torch.from_numpy(job.result(normalised=False)[0]).cuda()
-        torch.distributed.all_reduce(im)
+        # The exchange step: one sum of the stacked images over the ranks.
+        sdist.allreduce_sum([job.result(normalised=False)[0]], device="cuda")
     ev1.record()
     torch.cuda.nvtx.range_pop()
     barrier()
@@ -361,12 +362,8 @@ def main():
     st = ctx.stats()
     secs = elapsed
     if ws > 1:
-        t = torch.tensor([secs], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        secs = float(t.item())
-        p = torch.tensor([float(points)], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(p)
-        points_all = float(p.item())
+        secs = sdist.allreduce_max(secs, device="cuda")
+        points_all = float(sdist.allreduce_sum([np.array([float(points)])], device="cuda")[0][0])
     else:
         points_all = float(points)
     value = points_all / secs / 1e9

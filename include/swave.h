@@ -39,7 +39,8 @@ typedef enum sw_status {
   SW_BAD_PARAM = 1,      /* invalid sizes, vel_check failure, bad coords    */
   SW_OOM_ADMISSION = 2,  /* the work does not fit the device memory budget  */
   SW_TIMEOUT = 3,        /* a bounded device-side wait ran out              */
-  SW_NUMERIC = 4,        /* NaN / Inf detected                              */
+  SW_NUMERIC = 4,        /* NaN / Inf in the FWI misfit or gradient; eps of
+                            the regularisation not computable               */
   SW_CUDA_ERR = 5,       /* a CUDA runtime call failed                      */
   SW_UNSUPPORTED = 6     /* option not built (an adjoint grid with rho, ...) */
 } sw_status;
@@ -342,7 +343,8 @@ enum { SW_NRM_L1 = 1, SW_NRM_L2 = 2, SW_NRM_CAUCHY = 3, SW_NRM_HYPERBOLIC = 4,
  * snapshots), residual/misfit (FP64), AGRAD (backward with the AFWI imaging
  * condition), scatter-add into the full grid; then scaling, illumination
  * normalisation, mask, triangle smoothing, mask.  vel/grad/illum/mask are
- * nz*nx*ny.  *f receives the FP64 misfit. */
+ * nz*nx*ny.  *f receives the FP64 misfit.  A misfit or gradient that is not
+ * finite returns SW_NUMERIC (the outputs then hold what was computed). */
 int sw_fwi_fct_gdt(sw_ctx *ctx, const sw_fwi_desc *d, const float *vel,
                    const float *wavelet, int nshot, const sw_fwi_shot *shots,
                    const float *vpmask, double *f, float *grad, float *illum);

@@ -602,6 +602,12 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
   if (illum && (st = download(c, illum, dill, nfull * sizeof(float)))) return st;
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(c, e, "fwi");
   *f = fsum / scaling;
+  // A NaN or Inf anywhere (data, model, an unstable propagation) reaches
+  // the FP64 misfit or the gradient; report it instead of returning it.
+  if (!std::isfinite(*f)) return fail(c, SW_NUMERIC, "misfit is not finite (%g)", *f);
+  for (long long q = 0; q < nfull; ++q)
+    if (!std::isfinite(grad[q]))
+      return fail(c, SW_NUMERIC, "gradient is not finite at model index %lld", q);
   return SW_OK;
 }
 

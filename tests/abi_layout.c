@@ -1,0 +1,74 @@
+/* Prints the layout of every struct of include/swave.h: one line per struct
+ * ("struct <name> <sizeof>") followed by one line per field in declaration
+ * order ("field <name> <offsetof> <sizeof>").  Built and run by
+ * tests/test_abi_layout.py, which compares it with the ctypes mirror
+ * (seismic_gb300/__init__.py) and the Fortran bind(C) types
+ * (include/swave_iface.f90). */
+#include <stddef.h>
+#include <stdio.h>
+
+#include "swave.h"
+
+#define S(T) printf("struct %s %zu\n", #T, sizeof(T))
+#define F(T, f) printf("field %s %zu %zu\n", #f, offsetof(T, f), sizeof(((T *)0)->f))
+
+int main(void) {
+  S(sw_genpar);
+  F(sw_genpar, twoD); F(sw_genpar, nz); F(sw_genpar, nx); F(sw_genpar, ny);
+  F(sw_genpar, dz); F(sw_genpar, dx); F(sw_genpar, dy);
+  F(sw_genpar, oz); F(sw_genpar, ox); F(sw_genpar, oy); F(sw_genpar, dt);
+  F(sw_genpar, nt); F(sw_genpar, ntaper); F(sw_genpar, lsinc); F(sw_genpar, snapi);
+  F(sw_genpar, surf_type); F(sw_genpar, shot_type); F(sw_genpar, rec_type); F(sw_genpar, fmax);
+
+  S(sw_prop_desc);
+  F(sw_prop_desc, g); F(sw_prop_desc, tmin); F(sw_prop_desc, tmax); F(sw_prop_desc, tstep);
+  F(sw_prop_desc, fd_scheme); F(sw_prop_desc, injection); F(sw_prop_desc, extraction);
+  F(sw_prop_desc, extract_wave); F(sw_prop_desc, imaging);
+
+  S(sw_prop_io);
+  F(sw_prop_io, vel); F(sw_prop_io, nsou); F(sw_prop_io, sou_coord); F(sw_prop_io, sou_trace);
+  F(sw_prop_io, nrec); F(sw_prop_io, rec_coord); F(sw_prop_io, rec_trace); F(sw_prop_io, wave);
+  F(sw_prop_io, image); F(sw_prop_io, illum); F(sw_prop_io, ref); F(sw_prop_io, final_u2);
+  F(sw_prop_io, rho); F(sw_prop_io, image2);
+
+  S(sw_shot);
+  F(sw_shot, sou_coord); F(sw_shot, nrec); F(sw_shot, rec_coord); F(sw_shot, data);
+  F(sw_shot, nt);
+
+  S(sw_window);
+  F(sw_window, oxw); F(sw_window, oyw); F(sw_window, endx); F(sw_window, endy);
+  F(sw_window, nxw); F(sw_window, nyw);
+
+  S(sw_fwi_shot);
+  F(sw_fwi_shot, sou_coord); F(sw_fwi_shot, nrec); F(sw_fwi_shot, rec_coord);
+  F(sw_fwi_shot, dobs); F(sw_fwi_shot, mute); F(sw_fwi_shot, resid);
+
+  S(sw_fwi_desc);
+  F(sw_fwi_desc, g); F(sw_fwi_desc, aperture_x); F(sw_fwi_desc, aperture_y);
+  F(sw_fwi_desc, illu_pow); F(sw_fwi_desc, smooth_rect1); F(sw_fwi_desc, smooth_rect2);
+  F(sw_fwi_desc, smooth_rect3); F(sw_fwi_desc, smooth_doz); F(sw_fwi_desc, smooth_dox);
+  F(sw_fwi_desc, smooth_doy); F(sw_fwi_desc, checkpoint_snaps); F(sw_fwi_desc, dat_nrm_type);
+  F(sw_fwi_desc, dat_thresh); F(sw_fwi_desc, revolve_slots);
+
+  S(sw_reg_desc);
+  F(sw_reg_desc, nz); F(sw_reg_desc, nx); F(sw_reg_desc, ny); F(sw_reg_desc, wantreg);
+  F(sw_reg_desc, wantlog); F(sw_reg_desc, derivdx); F(sw_reg_desc, derivdy);
+  F(sw_reg_desc, derivdz); F(sw_reg_desc, log_z_plus); F(sw_reg_desc, ntaperz);
+  F(sw_reg_desc, ntaperx); F(sw_reg_desc, ntapery); F(sw_reg_desc, mod_nrm_type);
+  F(sw_reg_desc, hin_nrm_type); F(sw_reg_desc, compute_eps); F(sw_reg_desc, compute_eps_log);
+  F(sw_reg_desc, ratio); F(sw_reg_desc, ratio_log); F(sw_reg_desc, zweight);
+
+  S(sw_reg_state);
+  F(sw_reg_state, eps); F(sw_reg_state, eps_log); F(sw_reg_state, mod_thresh);
+  F(sw_reg_state, hin_thresh);
+
+  S(sw_tuning);
+  F(sw_tuning, step_kernel); F(sw_tuning, tile_z); F(sw_tuning, tile_x); F(sw_tuning, tile_y);
+  F(sw_tuning, graph_chunk); F(sw_tuning, use_graph);
+
+  S(sw_stats);
+  F(sw_stats, launches_total); F(sw_stats, launches_step); F(sw_stats, points_updated);
+  F(sw_stats, step_kernel_ms); F(sw_stats, step_kernel_timed); F(sw_stats, step_bytes);
+  F(sw_stats, steps_forward); F(sw_stats, steps_backward); F(sw_stats, ckpt_advances);
+  return 0;
+}

@@ -356,3 +356,14 @@ def test_fwi_gradient_fd_check_on_device(oracle):
         oracle.set_rigid(False)
     np.testing.assert_array_equal(fd, rfd)       # FP64 misfits summed in the same order
     assert rel_l2(an, ran) < 1e-6
+
+
+def test_fwi_non_finite_data_is_reported(ctx):
+    """A NaN in the observed data reaches the FP64 misfit: sw_fwi_fct_gdt
+    returns SW_NUMERIC instead of a NaN misfit."""
+    d, vel, w, shots, mask = _fwi_case()
+    shots[1]["dobs"] = shots[1]["dobs"].copy()
+    shots[1]["dobs"][3, 17] = np.nan
+    with pytest.raises(sw.SwaveError) as e:
+        ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
+    assert e.value.code == sw.SW_NUMERIC
