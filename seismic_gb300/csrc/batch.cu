@@ -10,6 +10,7 @@
 #include "stream2d.cuh"
 #include "stream3d.cuh"
 #include "tile2d.cuh"
+#include "tile2d2.cuh"
 #include "tile3d.cuh"
 
 namespace swave {
@@ -349,7 +350,7 @@ __global__ void k_bextract(BatchTables t, int s_off) {
   const int r = q - t.rec_start[b];
   const int it = S.tmin + s * S.tstep;
   const Geom &g = S.g;
-  const float *__restrict__ u2 = S.f[(s + 3) % 5];
+  const float *__restrict__ u2 = S.f[(s + 3) % S.nbuf];
   const int i0 = S.ric[3 * r], j0 = S.ric[3 * r + 1], k0 = g.twoD ? 1 : S.ric[3 * r + 2];
   float *trp = S.rec_tr + (long long)r * S.nt + (it - 1);
   if (S.ext_mode == 2) {  // Extraction_array_simple_afwi_noomp
@@ -744,6 +745,46 @@ static cudaError_t launch_tile2d(const BatchTables &t, int s_off, int n_tiles, i
   return cudaGetLastError();
 }
 
+// Two-step persistent 2D kernel (tile2d2.cuh): one CTA of 512 threads per SM.
+template <bool ADJ>
+__global__ void __launch_bounds__(TF_THREADS, 1) k_bstep2d_f(BatchTables t, int s_off,
+                                                            int n_tiles) {
+  tile2d_fused<ADJ>(t, s_off, n_tiles);
+}
+
+static_assert(tf_smem_bytes<false>() + 1024 <= 228 * 1024, "two-step kernel smem (fwd)");
+static_assert(tf_smem_bytes<true>() + 1024 <= 228 * 1024, "two-step kernel smem (adj)");
+
+template <bool ADJ>
+static cudaError_t launch_tile2d_f(const BatchTables &t, int s_off, int n_tiles, int nsm,
+                                   cudaStream_t s) {
+  static unsigned long long attr_set = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !(attr_set & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_bstep2d_f<ADJ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tf_smem_bytes<ADJ>());
+    if (e != cudaSuccess) return e;
+    if (dev < 64) attr_set |= 1ull << dev;
+  }
+  const int grid = std::max({1, std::min(n_tiles, nsm),
+                             (n_tiles + TF_MAX_TILES_PER_CTA - 1) / TF_MAX_TILES_PER_CTA});
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(TF_THREADS);
+  cfg.dynamicSmemBytes = tf_smem_bytes<ADJ>();
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, k_bstep2d_f<ADJ>, t, s_off, n_tiles);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
 // Warp-specialised persistent 2D step (tile2d.cuh): one CTA per SM.
 static_assert(t2w_smem_bytes<false>() <= 227 * 1024, "ws tile kernel smem (fwd)");
 static_assert(t2w_smem_bytes<true>() <= 227 * 1024, "ws tile kernel smem (adj)");
@@ -816,7 +857,9 @@ __global__ void k_counter_add(int *counter, int add) {
 // Injection terms of the step, one thread per (shot, entry):
 // term = (((v2r * trace(it)) * wz) * wx) * wy (Injection.f90:151-456,
 // 561-591); the step kernel adds a cell's terms in entry order.
-__global__ void k_bterms(BatchTables t, int s_off) {
+// sub = 1 forms the terms of the second step of a two-step launch (step
+// s_off - 1 + 1 of the counter) into the second block of inj_term.
+__global__ void k_bterms(BatchTables t, int s_off, int sub) {
   // The previous step kernel still reads the terms this kernel overwrites.
   pdl_wait();
   pdl_launch_dependents();
@@ -830,7 +873,7 @@ __global__ void k_bterms(BatchTables t, int s_off) {
   const int it = S.tmin + s * S.tstep;
   const InjEntry E = S.inj_ent[k];
   const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
-  S.inj_term[k] = (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
+  S.inj_term[(long long)sub * S.inj_nterm + k] = (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
 }
 
 cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
@@ -855,7 +898,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, k_bterms, t, s_off);
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_bterms, t, s_off, 0);
     if (e != cudaSuccess) return e;
     ++nl;
   }
@@ -962,6 +1005,69 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   }
   if (has_3d && n_hy > 0 && !tile.rigid) {
     k_bhiggy<<<(2 * n_hy + 127) / 128, 128, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  if (nlaunch) *nlaunch = nl;
+  return cudaGetLastError();
+}
+
+// Two time steps s = *counter + s_off and s + 1 of a 2D batch in one
+// launch of the two-step tile kernel: receiver extraction of step s, the
+// injection terms of both steps, the fused kernel (stencils, time updates,
+// injection, snapshots, imaging and Higdon edges of both steps), then the
+// extraction of step s + 1 from the level the launch wrote.
+cudaError_t launch_batch_step2(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
+                               int has_ext, const StepTile &tile, cudaStream_t s, int *nlaunch,
+                               cudaEvent_t ev_before, cudaEvent_t ev_after, int n_term) {
+  int nl = 0;
+  if (has_ext && n_rec > 0) {
+    k_bextract<<<(n_rec + 3) / 4, 128, 0, s>>>(t, s_off);
+    ++nl;
+  }
+  for (int sub = 0; sub < 2 && n_term > 0; ++sub) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((n_term + 255) / 256);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_bterms, t, s_off + sub, sub);
+    if (e != cudaSuccess) return e;
+    ++nl;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (ev_before || ev_after) {
+    cudaError_t ec = cudaStreamIsCapturing(s, &cap);
+    if (ec != cudaSuccess) return ec;
+  }
+  auto record = [&](cudaEvent_t ev) {
+    return cap == cudaStreamCaptureStatusActive
+               ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+               : cudaEventRecord(ev, s);
+  };
+  if (ev_before) {
+    cudaError_t ec = record(ev_before);
+    if (ec != cudaSuccess) return ec;
+  }
+  cudaError_t e = cudaSuccess;
+  if (tile.has_fwd2d) {
+    e = launch_tile2d_f<false>(t, s_off, n_step_tiles, tile.nsm, s);
+    ++nl;
+  }
+  if (e == cudaSuccess && tile.has_adj2d) {
+    e = launch_tile2d_f<true>(t, s_off, n_step_tiles, tile.nsm, s);
+    ++nl;
+  }
+  if (e != cudaSuccess) return e;
+  if (ev_after) {
+    cudaError_t ec = record(ev_after);
+    if (ec != cudaSuccess) return ec;
+  }
+  if (has_ext && n_rec > 0) {
+    k_bextract<<<(n_rec + 3) / 4, 128, 0, s>>>(t, s_off + 1);
     ++nl;
   }
   if (nlaunch) *nlaunch = nl;

@@ -19,7 +19,10 @@ namespace swave {
 struct ShotDev {
   Geom g;
   Coefs c;
-  float *f[5];            // five time levels, rotated by the step counter
+  float *f[6];            // time levels, rotated by the step counter: level L of
+                          // step s in f[(s + L) % nbuf]
+  int nbuf;               // 5, or 6 when two steps run per launch (the second
+                          // step's output must not overwrite the first's input)
   const float *vel;       // padded velocity
   float *v2u;             // 3D adjoint: v^2*u2 scratch (else null)
   const float *gz, *gx, *gy;
@@ -29,6 +32,9 @@ struct ShotDev {
   const int *inj_off;
   const InjEntry *inj_ent;
   float *inj_term;        // per entry: its contribution at the current step
+                          // (two-step launches: a second block of inj_nterm
+                          // entries for the step after it)
+  int inj_nterm;
   const float *src_tr;    // nsrc*nt
   // extraction
   int ext_mode, nrec, ext_half;
@@ -65,7 +71,8 @@ struct ShotDev {
 // Compact per-shot view used by the pipelined 2D kernel; the kernel keeps the
 // whole array in shared memory.
 struct T2Shot {
-  const float *f[5];
+  const float *f[5];      // (the two-step kernel reads all six levels and their
+                          // count from the ShotDev)
   const float *vel;
   const float *gz, *gx;   // Higdon coefficients (z and x edges)
   float c0z, c1z, c2z, c3z, c4z, c0x, c1x, c2x, c3x, c4x, k12, div11;
@@ -106,6 +113,8 @@ inline bool t2_origin(int n1, int n2, int *off1, int *off2, int *ntz, int *ntx) 
 
 // Largest batch the pipelined 2D kernel accepts (its shot table is shared).
 constexpr int T2_MAX_SHOTS = 64;
+// Largest batch of the two-step 2D kernel (tile2d2.cuh).
+constexpr int TF_MAX_SHOTS = 32;
 
 // Tensor maps of one shot for the pipelined 2D kernel: [2*buf + box] with
 // buf 0..4 the time-level buffers and 5 the padded velocity, box 0 the
@@ -113,6 +122,42 @@ constexpr int T2_MAX_SHOTS = 64;
 struct T2Maps {
   CUtensorMap m[12];
 };
+
+// Tensor maps of one shot for the two-step 2D kernel (tile2d2.cuh):
+// [2*buf + box] for the six time-level buffers, box 0 the 80 x 80 tile with
+// an 8-cell halo, box 1 the 72 x 72 tile with a 4-cell halo; [12] the
+// velocity's 72 x 72 box, [13] its 80 x 80 box.
+struct T2FMaps {
+  CUtensorMap m[14];
+};
+
+// Tile origin of the two-step 2D kernel: 64 x 64 tiles starting off1 rows /
+// off2 columns before the compute domain (off1 a multiple of 4).  The first
+// and last tile along each axis own 8..60 rows (columns) of the compute
+// domain, so that each holds its 8-cell Higdon edge zone and the 4 padding
+// cells beyond in its core, and no other tile's 4-cell extended region
+// reaches an edge zone.  A single tile along an axis holds both.
+inline bool tf_origin_axis(int n, bool aligned, int *off, int *nt) {
+  for (int o = 4; o <= 56; o += aligned ? 4 : 1) {
+    const int k = (n + o + 4 + 63) / 64;
+    if (k == 1) {
+      *off = o;
+      *nt = 1;
+      return true;
+    }
+    const int first = 64 - o, last = n - (64 * (k - 1) - o);
+    if (first >= 8 && last >= 8 && last <= 60) {
+      *off = o;
+      *nt = k;
+      return true;
+    }
+  }
+  return false;
+}
+inline bool tf_origin(int n1, int n2, int *off1, int *off2, int *ntz, int *ntx) {
+  if (n1 < 16 || n2 < 16) return false;
+  return tf_origin_axis(n1, true, off1, ntz) && tf_origin_axis(n2, false, off2, ntx);
+}
 
 // Tensor maps of one shot for the pipelined 3D kernel (rank 3, one plane per
 // box): [2*buf + box], box 0 the 40 x 40 plane tile with halo, 1 the
@@ -136,6 +181,7 @@ struct BatchTables {
   const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
   const int *term_start;  // nshots+1: injection entries (per-step term kernel)
   const T2Maps *t2maps;   // nshots tensor-map sets (pipelined 2D kernel)
+  const T2FMaps *tfmaps;  // nshots tensor-map sets (two-step 2D kernel)
   const T3Maps *t3maps;   // nshots tensor-map sets (pipelined 3D kernel)
   int *err;               // device error flags (bit 0: a bounded wait gave up)
   int *counter;           // step counter s (0-based)
@@ -163,6 +209,7 @@ struct StepTile {
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
   int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
   int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)
+  int fuse2 = 0;       // 2D tiles: two time steps per launch (tile2d2.cuh)
 };
 
 // Threads of the fused 2D edge kernel for one shot: four corner warps and
@@ -177,6 +224,10 @@ inline int edge_threads_2d(const Geom &g) {
 // Number of fused-step CTAs a shot needs with this tile shape.
 inline int step_ctas(const Geom &g, const StepTile &tile) {
   const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  if (g.twoD && tile.fuse2) {
+    int o1, o2, nz, nx;
+    return tf_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;
+  }
   if (g.twoD && (tile.stream2d == 2 || tile.stream2d == 3)) {
     int o1, o2, nz, nx;
     return t2_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;
@@ -195,6 +246,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
                               int has_adj3d, const StepTile &tile, cudaStream_t s,
                               int *nlaunch, cudaEvent_t ev_before, cudaEvent_t ev_after,
                               int n_term = 0);
+// Two steps per launch (StepTile::fuse2): steps s = *counter + s_off and s + 1.
+cudaError_t launch_batch_step2(const BatchTables &t, int s_off, int n_step_tiles, int n_rec,
+                               int has_ext, const StepTile &tile, cudaStream_t s, int *nlaunch,
+                               cudaEvent_t ev_before, cudaEvent_t ev_after, int n_term);
 cudaError_t launch_counter_add(int *counter, int add, cudaStream_t s);
 
 }  // namespace swave

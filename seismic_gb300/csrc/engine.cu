@@ -70,7 +70,7 @@ int sw_ctx_reset_stats(sw_ctx *c) {
 }
 int sw_ctx_set_tuning(sw_ctx *c, const sw_tuning *t) {
   if (!c || !t) return SW_BAD_PARAM;
-  if (t->step_kernel < 0 || t->step_kernel > 3 || t->graph_chunk < 1 || t->tile_x < 1 ||
+  if (t->step_kernel < 0 || t->step_kernel > 4 || t->graph_chunk < 1 || t->tile_x < 1 ||
       t->tile_y < 1 ||
       (t->tile_z != 32 && t->tile_z != 64 && t->tile_z != 128))
     return swave::fail(c, SW_BAD_PARAM, "invalid tuning");

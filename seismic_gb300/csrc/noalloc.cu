@@ -121,6 +121,7 @@ extern "C" int sw_modeling_noalloc(const sw_genpar *g, const float *vel, const f
   float *vpad = cv.take<float>(nf);
   ShotDev S;
   std::memset(&S, 0, sizeof(S));
+  S.nbuf = 5;   // one step per launch: five rotating time levels
   for (int q = 0; q < 5; ++q) S.f[q] = cv.take<float>(nf);
   float *gz = cv.take<float>(16 * n2), *gx = cv.take<float>(16 * n1);
   int *ioff = cv.take<int>(inj.off.size());

@@ -110,7 +110,25 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     tile.stream2d = 0;
     tile.stream3d = 0;
   }
-  if (tile.stream2d == 2 || tile.stream2d == 3) {
+  // Two time steps per launch (tile2d2.cuh) for 2D batches of up to
+  // TF_MAX_SHOTS shots whose imaging reads only the staged fields (none,
+  // RTM, LSRTM); other batches take the single-step tile kernel.
+  tile.fuse2 = 0;
+  if (tile.stream2d == 4) {
+    bool ok = shots[0].d.g.twoD && nb <= TF_MAX_SHOTS;
+    for (int b = 0; b < nb && ok; ++b) {
+      const sw_prop_desc &d = shots[b].d;
+      const Geom g = make_geom(d.g);
+      int o1, o2, ntz, ntx;
+      ok = d.g.twoD &&
+           (d.imaging == SW_IMG_NONE || d.imaging == SW_IMG_RTM || d.imaging == SW_IMG_LSRTM) &&
+           g.nmax1 - g.nmin1 + 1 <= 64 * 4000 && g.nmax2 - g.nmin2 + 1 <= 64 * 4000 &&
+           tf_origin(g.nmax1 - g.nmin1 + 1, g.nmax2 - g.nmin2 + 1, &o1, &o2, &ntz, &ntx);
+    }
+    tile.stream2d = 2;
+    tile.fuse2 = ok ? 1 : 0;
+  }
+  if ((tile.stream2d == 2 || tile.stream2d == 3) && !tile.fuse2) {
     bool fits = nb <= T2_MAX_SHOTS;
     for (int b = 0; b < nb && fits; ++b) {
       const Geom g = make_geom(shots[b].d.g);
@@ -164,12 +182,12 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     const size_t fb = (size_t)G[b].total() * sizeof(float);
     const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
                     n3 = G[b].nmax3 - G[b].nmin3 + 1;
-    bytes += 5 * rup(fb);
+    bytes += (tile.fuse2 ? 6 : 5) * rup(fb);
     if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT && !tile.stream3d) bytes += rup(fb);
     if (io.rho_pad) bytes += (d.g.twoD ? 2 : 3) * rup(fb);
     bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
     bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry)) +
-             rup(inj[b].ent.size() * sizeof(float));
+             rup((tile.fuse2 ? 2 : 1) * inj[b].ent.size() * sizeof(float));
     bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
     bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
   }
@@ -177,7 +195,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   if (t2) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
-    bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int)) + rup(nb * sizeof(T2Maps));
+    bytes += rup(nb * sizeof(T2Shot)) + rup(ntile * sizeof(int)) +
+             (tile.fuse2 ? rup(nb * sizeof(T2FMaps)) : rup(nb * sizeof(T2Maps)));
   }
   if (t3) {
     size_t ntile = 0;
@@ -207,7 +226,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     S.g = G[b];
     S.c = make_coefs(g);
     const size_t nf = (size_t)G[b].total();
-    for (int q = 0; q < 5; ++q) {
+    S.nbuf = tile.fuse2 ? 6 : 5;
+    for (int q = 0; q < S.nbuf; ++q) {
       S.f[q] = carve<float>(cur, nf);
       // Level L at step 0 is buffer L: a checkpointed phase resumes from the
       // saved u_1, u0, u1, u2; u3 (and every level otherwise) starts at 0.
@@ -263,7 +283,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                       cudaMemcpyHostToDevice, s));
       S.inj_off = off;
       S.inj_ent = ent;
-      S.inj_term = carve<float>(cur, inj[b].ent.size());
+      S.inj_nterm = (int)inj[b].ent.size();
+      S.inj_term = carve<float>(cur, (tile.fuse2 ? 2 : 1) * inj[b].ent.size());
       S.src_tr = io.sou_trace_dev;
     }
     S.ext_mode = ext[b].on ? ext[b].mode : 0;
@@ -365,9 +386,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   std::vector<T2Shot> h2(t2 ? nb : 0);
   std::vector<int> htile;
   std::vector<T2Maps> hmaps;
+  std::vector<T2FMaps> hfmaps;
   T2Shot *d2 = nullptr;
   int *dtile = nullptr;
   T2Maps *dmaps = nullptr;
+  T2FMaps *dfmaps = nullptr;
   if (t2) {
     for (int b = 0; b < nb; ++b) {
       const ShotDev &S = hs[b];
@@ -389,28 +412,52 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
       h.gz = S.gz; h.gx = S.gx;
-      if (!t2_origin(S.g.nmax1 - S.g.nmin1 + 1, S.g.nmax2 - S.g.nmin2 + 1, &h.off1, &h.off2,
-                     &h.ntz, &h.ntx))
-        return fail(c, SW_CUDA_ERR, "tile origin");
+      const bool org = tile.fuse2 ? tf_origin(S.g.nmax1 - S.g.nmin1 + 1, S.g.nmax2 - S.g.nmin2 + 1,
+                                              &h.off1, &h.off2, &h.ntz, &h.ntx)
+                                  : t2_origin(S.g.nmax1 - S.g.nmin1 + 1, S.g.nmax2 - S.g.nmin2 + 1,
+                                              &h.off1, &h.off2, &h.ntz, &h.ntx);
+      if (!org) return fail(c, SW_CUDA_ERR, "tile origin");
       const int n1t = h.ntz, n2t = h.ntx;
       for (int xi = 0; xi < n2t; ++xi)
         for (int zi = 0; zi < n1t; ++zi) htile.push_back((b << 24) | (zi << 12) | xi);
     }
     if ((int)htile.size() != step_tiles[nb]) return fail(c, SW_CUDA_ERR, "tile table size");
-    hmaps.resize(nb);
-    for (int b = 0; b < nb; ++b) {
-      const ShotDev &S = hs[b];
-      for (int q = 0; q < 6; ++q) {
-        const float *base = q < 5 ? S.f[q] : S.vel;
-        if (!encode_field_map(&hmaps[b].m[2 * q], base, S.g, 72, 40) ||
-            !encode_field_map(&hmaps[b].m[2 * q + 1], base, S.g, 64, 32))
-          return fail(c, SW_CUDA_ERR, "tensor map encoding failed (shot %d)", b);
+    if (tile.fuse2) {
+      // Six level buffers with the 80 x 80 and 72 x 72 boxes, then the
+      // velocity's 72 x 72 and 80 x 80 boxes.
+      hfmaps.resize(nb);
+      for (int b = 0; b < nb; ++b) {
+        const ShotDev &S = hs[b];
+        bool ok = true;
+        for (int q = 0; q < 6 && ok; ++q)
+          ok = encode_field_map(&hfmaps[b].m[2 * q], S.f[q], S.g, 80, 80) &&
+               encode_field_map(&hfmaps[b].m[2 * q + 1], S.f[q], S.g, 72, 72);
+        ok = ok && encode_field_map(&hfmaps[b].m[12], S.vel, S.g, 72, 72) &&
+             encode_field_map(&hfmaps[b].m[13], S.vel, S.g, 80, 80);
+        if (!ok) return fail(c, SW_CUDA_ERR, "tensor map encoding failed (shot %d)", b);
+      }
+    } else {
+      hmaps.resize(nb);
+      for (int b = 0; b < nb; ++b) {
+        const ShotDev &S = hs[b];
+        for (int q = 0; q < 6; ++q) {
+          const float *base = q < 5 ? S.f[q] : S.vel;
+          if (!encode_field_map(&hmaps[b].m[2 * q], base, S.g, 72, 40) ||
+              !encode_field_map(&hmaps[b].m[2 * q + 1], base, S.g, 64, 32))
+            return fail(c, SW_CUDA_ERR, "tensor map encoding failed (shot %d)", b);
+        }
       }
     }
     d2 = carve<T2Shot>(cur, nb);
     dtile = carve<int>(cur, htile.size());
-    dmaps = carve<T2Maps>(cur, nb);
-    SW_CK(cudaMemcpyAsync(dmaps, hmaps.data(), nb * sizeof(T2Maps), cudaMemcpyHostToDevice, s));
+    if (tile.fuse2) {
+      dfmaps = carve<T2FMaps>(cur, nb);
+      SW_CK(cudaMemcpyAsync(dfmaps, hfmaps.data(), nb * sizeof(T2FMaps), cudaMemcpyHostToDevice,
+                            s));
+    } else {
+      dmaps = carve<T2Maps>(cur, nb);
+      SW_CK(cudaMemcpyAsync(dmaps, hmaps.data(), nb * sizeof(T2Maps), cudaMemcpyHostToDevice, s));
+    }
     SW_CK(cudaMemcpyAsync(d2, h2.data(), nb * sizeof(T2Shot), cudaMemcpyHostToDevice, s));
     SW_CK(cudaMemcpyAsync(dtile, htile.data(), htile.size() * sizeof(int), cudaMemcpyHostToDevice,
                           s));
@@ -472,6 +519,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.t2shots = d2;
   t.tile_tab = dtile;
   t.t2maps = dmaps;
+  t.tfmaps = dfmaps;
   t.t3maps = dmaps3;
   t.err = derr;
   t.counter = counter;
@@ -506,7 +554,11 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   long long npts_total = 0;
   for (auto &S : hs) npts_total += S.npts;
   // ---- time loop ----
-  const int chunk = std::max(1, std::min(opt.chunk, max_steps));
+  // Two-step launches cover steps q and q + 1 of a chunk: chunks of an even
+  // number of steps (steps past a shot's last one are skipped by the kernels).
+  const int stride = tile.fuse2 ? 2 : 1;
+  int chunk = std::max(1, std::min(opt.chunk, max_steps));
+  if (chunk % stride) chunk += stride - chunk % stride;
   const int nchunks = (max_steps + chunk - 1) / chunk;
   const bool prof = c->profiling;
   // Algorithmic bytes of the fused step kernel at step sidx: 24 B per point
@@ -535,6 +587,15 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     }
     return by;
   };
+  // Two-step launch at steps sidx, sidx + 1: 28 B per point that takes both
+  // steps (u2, u1, u0, u_1, vel read, two levels written), 24 B for one,
+  // plus each step's snapshot and imaging traffic.
+  auto step_bytes2_at = [&](int sidx) -> uint64_t {
+    uint64_t by = step_bytes_at(sidx) + step_bytes_at(sidx + 1);
+    for (auto &S : hs)
+      if (sidx + 1 < S.nsteps) by -= (uint64_t)S.npts * 20ull;
+    return by;
+  };
   // Profiling: events around the fused step kernel of every
   // kProfileEvery-th chunk of steps.  Those chunks replay a second graph
   // that contains the event records; the host reads a profiled chunk's
@@ -547,27 +608,33 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   }
   auto record_chunk = [&](int nsteps_here, bool with_events) -> int {
     int launched = 0;
-    for (int q = 0; q < nsteps_here; ++q) {
+    for (int q = 0; q < nsteps_here; q += stride) {
       int nl = 0;
+      const int k = q / stride;   // launch of the chunk
       // In profiling mode events bracket the fused step kernel only.
-      if ((e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
-                                 has_adj3d, tile, s, &nl, with_events ? c->ev[2 * q] : nullptr,
-                                 with_events ? c->ev[2 * q + 1] : nullptr, n_term)) != cudaSuccess)
-        return -1;
+      cudaEvent_t e0 = with_events ? c->ev[2 * k] : nullptr;
+      cudaEvent_t e1 = with_events ? c->ev[2 * k + 1] : nullptr;
+      if (tile.fuse2)
+        e = launch_batch_step2(t, q, n_tiles, n_rec, has_ext, tile, s, &nl, e0, e1, n_term);
+      else
+        e = launch_batch_step(t, q, n_tiles, n_rec, n_hz, n_hx, n_hy, n_v2u, has_ext, has_3d,
+                              has_adj3d, tile, s, &nl, e0, e1, n_term);
+      if (e != cudaSuccess) return -1;
       launched += nl;
     }
     if ((e = launch_counter_add(counter, nsteps_here, s)) != cudaSuccess) return -1;
     return launched + 1;
   };
   auto read_chunk = [&](int q) -> int {
-    const int live = std::min(chunk, max_steps - q * chunk);
+    const int live = (std::min(chunk, max_steps - q * chunk) + stride - 1) / stride;
     SW_CK(cudaEventSynchronize(c->ev[2 * live - 1]));
     for (int k = 0; k < live; ++k) {
       float ms = 0.f;
       SW_CK(cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]));
       c->stats.step_kernel_ms += ms;
       c->stats.step_kernel_timed++;
-      c->stats.step_bytes += step_bytes_at(q * chunk + k);
+      c->stats.step_bytes += tile.fuse2 ? step_bytes2_at(q * chunk + 2 * k)
+                                        : step_bytes_at(q * chunk + k);
     }
     return SW_OK;
   };
@@ -616,8 +683,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     if (e != cudaSuccess) return cuda_fail(c, e, "graph launch");
     if (rs != SW_OK) return rs;
   } else {
-    for (int q = 0; q < max_steps; ++q) {
-      const int per = record_chunk(1, prof);
+    for (int q = 0; q < max_steps; q += stride) {
+      const int per = record_chunk(stride, prof);
       if (per < 0) return cuda_fail(c, e, "step launch");
       launches += per;
       if (prof) {
@@ -626,7 +693,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
         SW_CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         c->stats.step_kernel_ms += ms;
         c->stats.step_kernel_timed++;
-        c->stats.step_bytes += step_bytes_at(q);
+        c->stats.step_bytes += tile.fuse2 ? step_bytes2_at(q) : step_bytes_at(q);
       }
     }
   }
@@ -640,18 +707,19 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // ---- outputs ----
   for (int b = 0; b < nb; ++b) {
     if (!shots[b].io.save_state) continue;
-    // Level L after the last step is buffer (L + nsteps) mod 5.
+    // Level L after the last step is buffer (L + nsteps) mod nbuf.
     const size_t nf = (size_t)G[b].total();
     for (int q = 0; q < 4; ++q) {
-      e = cudaMemcpyAsync(shots[b].io.save_state + (size_t)q * nf, hs[b].f[(q + hs[b].nsteps) % 5],
+      e = cudaMemcpyAsync(shots[b].io.save_state + (size_t)q * nf,
+                          hs[b].f[(q + hs[b].nsteps) % hs[b].nbuf],
                           nf * sizeof(float), cudaMemcpyDeviceToDevice, s);
       if (e != cudaSuccess) return cuda_fail(c, e, "save state");
     }
   }
   for (int b = 0; b < nb; ++b) {
     if (!shots[b].io.final_u2_host) continue;
-    const int last = hs[b].nsteps;   // u2 after the last step = f[(last+3)%5]
-    const float *u2 = hs[b].f[(last + 3) % 5];
+    const int last = hs[b].nsteps;   // u2 after the last step = f[(last+3)%nbuf]
+    const float *u2 = hs[b].f[(last + 3) % hs[b].nbuf];
     e = cudaMemcpy2DAsync(shots[b].io.final_u2_host, (size_t)G[b].n1p * sizeof(float), u2,
                           (size_t)G[b].ld1 * sizeof(float), (size_t)G[b].n1p * sizeof(float),
                           (size_t)G[b].n2p * G[b].n3p, cudaMemcpyDeviceToHost, s);

@@ -52,7 +52,7 @@ def test_rtm_job_matches_oracle(ctx, oracle, max_batch):
     assert rel_l2(nm, rnm) < 1e-6
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 4])
 def test_rtm_job_every_step_kernel(oracle, kernel):
     """The batched RTM (forward with snapshots, backward with injection and
     imaging) is bit-exact with every 2D step kernel: point tiles, streaming,

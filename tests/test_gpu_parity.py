@@ -190,7 +190,7 @@ def test_born_lsrtm_dot_test_rigid(oracle, three_d):
     np.testing.assert_array_equal(ltd, rltd)
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("fd", [sw.FD_FORWARD, sw.FD_ADJOINT])
 @pytest.mark.parametrize("imaging", [sw.IMG_RTM, sw.IMG_LSRTM, sw.IMG_AFWI])
 def test_backward_imaging_every_grid_and_kernel(oracle, kernel, fd, imaging):
@@ -217,3 +217,31 @@ def test_backward_imaging_every_grid_and_kernel(oracle, kernel, fd, imaging):
     assert np.abs(b_im).max() > 0
     np.testing.assert_array_equal(a_im, b_im)
     np.testing.assert_array_equal(a_il, b_il)
+
+
+@pytest.mark.parametrize("nt", [400, 401])
+@pytest.mark.parametrize("rigid", [0, 1])
+@pytest.mark.parametrize("shape", [(60, 80), (45, 130), (130, 45), (30, 36)])
+def test_modeling_two_step_kernel(oracle, nt, rigid, shape):
+    """The two-step tile kernel (step_kernel 4: steps s and s + 1 in one
+    launch, step A over the tile grown by 4 cells, Higdon edges of both
+    steps in the tile): traces and the final wavefield bit-exact with the
+    oracle, for an even and an odd number of steps, with the Higdon and the
+    rigid boundary, on grids with one and several tiles along each axis."""
+    nz, nx = shape
+    g, vel, sou, rec, w = case2d(nz=nz, nx=nx, nt=nt)
+    c = sw.Context(0)
+    try:
+        c.set_tuning(step_kernel=4)
+        c.set_boundary(rigid)
+        data, fu = c.modeling(g, vel, sou, w, rec, final_u2=True)
+    finally:
+        c.close()
+    oracle.set_rigid(bool(rigid))
+    try:
+        ref, rfu = oracle.modeling(g, vel, sou, w, rec, final_u2=True)
+    finally:
+        oracle.set_rigid(False)
+    assert np.abs(ref).max() > 0
+    np.testing.assert_array_equal(data, ref)
+    np.testing.assert_array_equal(fu, rfu)
