@@ -28,8 +28,9 @@ def candidates(two_d: bool = True) -> list[dict]:
         out.append({"step_kernel": 0, "tile_z": 64, "tile_x": 64, "tile_y": 32,
                     "graph_chunk": chunk, "use_graph": 1})
         if two_d:
-            # TMA-staged tiles: 2 CTAs per SM (2) and warp-specialised (3).
-            for k in (2, 3):
+            # TMA-staged tiles: 2 CTAs per SM (2), warp-specialised (3) and
+            # two steps per launch (4).
+            for k in (2, 3, 4):
                 out.append({"step_kernel": k, "tile_z": 64, "tile_x": 64, "tile_y": 32,
                             "graph_chunk": chunk, "use_graph": 1})
             for tz in (32, 64, 128):
