@@ -412,8 +412,8 @@ int sw_lbfgs_diag(const sw_lbfgs *s, double *out8);
 /* ---- Tuning (no counterpart in the reference: launch shape knobs) -------- */
 typedef struct sw_tuning {
   int step_kernel;   /* fused step: 0 = 32x8 point tiles, 1 = streaming, 2 = TMA-staged
-                        tiles, 2 CTAs per SM, 3 = TMA-staged tiles, warp-specialised,
-                        4 (default) = two time steps per launch on 64x64 TMA tiles
+                        tiles, 2 CTAs per SM (default), 3 = TMA-staged tiles,
+                        warp-specialised, 4 = two time steps per launch on 64x64 TMA tiles
                         for 2D batches of up to 32 shots without AFWI / Born
                         imaging (others run 2); 3D uses streaming for 1 and the
                         TMA plane pipeline for 2-4 */

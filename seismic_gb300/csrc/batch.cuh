@@ -193,7 +193,7 @@ struct BatchTables {
 // streaming kernel with TZ = tz rows per CTA (32, 64 or 128) walking tx
 // columns; otherwise 32x8 point tiles.  3D: 32x8 point tiles per plane.
 struct StepTile {
-  int stream2d = 4;    // 2D: 0 point tiles, 1 streaming (stream2d.cuh), 2 tiled, 3 tiled and
+  int stream2d = 2;    // 2D: 0 point tiles, 1 streaming (stream2d.cuh), 2 tiled, 3 tiled and
                        // warp-specialised (tile2d.cuh), 4 two steps per launch where the
                        // batch allows it (tile2d2.cuh), else 2
   int tz = 64;
