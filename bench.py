@@ -178,6 +178,7 @@ def cpu_parity_sample(ctx, g, vel, w, shots) -> tuple[dict, dict]:
     nt0 = s0["data"].shape[1]
     gw = sw.make_genpar(NZ, nxw, 1, dz=D, dx=D, ox=i0 * D, dt=DT, nt=nt0, ntaper=NTAPER,
                         lsinc=7, snapi=SNAPI)
+    gw.surf_type, gw.shot_type, gw.rec_type = g.surf_type, g.shot_type, g.rec_type
     rdata = oracle.modeling(gw, vel[i0:i0 + nxw], s0["sou"], w[:nt0], s0["rec"])
 
     def rel(a, b):
@@ -243,7 +244,10 @@ def run_reference(args):
 
 
 def workload_config(args, batch):
-    return {"workload": "batched 2D shot RTM with illumination-normalised stacking",
+    surf = bool(getattr(args, "surf", False))
+    return {"workload": "batched 2D shot RTM with illumination-normalised stacking" +
+                        (", free surface and mirror receivers" if surf else ""),
+            "surf_type": 1 if surf else 0, "rec_type": 1 if surf else 0,
             "grid": [NZ, NX], "spacing_m": D, "dt_s": DT, "ntaper": NTAPER, "snapi": SNAPI,
             "record_s": [3.0, 4.0], "aperture_m": [3000, 6000], "shot_spacing_m": SPACING,
             "survey_shots": NSHOT_SURVEY, "shots_per_step": batch, "ricker_hz": F0,
@@ -266,6 +270,9 @@ def main():
                     help="run the learned-preconditioner FWI study instead of the RTM bench")
     ap.add_argument("--model3d", action="store_true",
                     help="time 3D modelling of one shot instead of the 2D RTM bench")
+    ap.add_argument("--surf", action="store_true",
+                    help="the same RTM with a free surface (surf_type 1) and mirror receivers "
+                         "(rec_type 1)")
     ap.add_argument("--revolve-study", action="store_true",
                     help="FWI gradient memory modes on the 1201 x 3401 grid: store-all against "
                          "binomial checkpointing with 32/64/128 state slots")
@@ -293,6 +300,8 @@ def main():
     if args.no_graph:
         ctx.set_tuning(use_graph=0)
     g, vel, w, shots = make_workload(args.nt_cap or None)
+    if args.surf:
+        g.surf_type, g.rec_type = 1, 1
     B = args.shots_per_step
     nsteps = args.warmup + args.steps
     # Shots of this rank: rank r takes every ws-th shot of the survey.

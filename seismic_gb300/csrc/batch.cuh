@@ -79,8 +79,12 @@ struct T2Shot {
   int ld1, lo2, n2p, nmin1, nmax1, nmin2, nmax2, nz, nx;
   int nsteps, tmin, tstep, snapi, adj2d, inj_on, bi0, bi1, bj0, bj1, extract_wave, imaging;
   int tcnt;
-  int inj_direct;         // 1: form injection terms in the tile (few entries)
-  int rigid;              // 1: no Higdon edges (exact-adjoint mode)
+  unsigned char inj_direct;  // 1: form injection terms in the tile (few entries)
+  unsigned char rigid;       // 1: no Higdon edges (exact-adjoint mode)
+  unsigned char surf;        // 1: free surface (no Higdon top edge, side lines from row 1)
+  unsigned char pad_;
+  int irow0;              // first row kept in snapshots and images (row 1, or the
+                          // surface row under a free surface)
   int off1, off2;         // tile origin: nmin1 - off1, nmin2 - off2
   int ntz, ntx;           // tiles along z and x
 };

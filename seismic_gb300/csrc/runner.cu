@@ -106,8 +106,16 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     if (g.surf_type != 0) tile.has_surf = 1;
     if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0) special = true;
   }
-  if (tile.has_rho || special) {
+  // The variable-density operator runs on the point tiles.  A free surface
+  // and mirror sources or receivers run on the single-step 2D tile kernel
+  // (k_bfree before it; the mirror terms are injection and extraction
+  // entries); in 3D on the point tiles.
+  if (tile.has_rho) {
     tile.stream2d = 0;
+    tile.stream3d = 0;
+  }
+  if (special) {
+    if (tile.stream2d != 0) tile.stream2d = 2;
     tile.stream3d = 0;
   }
   // Two time steps per launch (tile2d2.cuh) for 2D batches of up to
@@ -409,6 +417,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       h.adj2d = S.adj2d; h.inj_on = S.inj_on;
       h.inj_direct = S.inj_on && inj[b].ent.size() < kTermKernelMin;
       h.rigid = opt.rigid ? 1 : 0;
+      h.surf = S.surf ? 1 : 0;
+      h.irow0 = S.irow0;
       h.bi0 = S.bi0; h.bi1 = S.bi1; h.bj0 = S.bj0; h.bj1 = S.bj1;
       h.extract_wave = S.extract_wave; h.imaging = S.imaging;
       h.gz = S.gz; h.gx = S.gx;

@@ -169,12 +169,15 @@ __device__ __noinline__ float t2_snap_generic(const ShotDev &S, int it, int i, i
   const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[0] : 1.f;
   const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
                               : S.tcnt / S.snapi - (it - 1) / S.snapi;
+  // Rows above a free surface: stored as zero, no Born source or imaging.
+  const bool below = i >= S.irow0;
   // Injection_Born (Imaging.f90:747-788).
-  if (S.imaging == 4 && S.tstep > 0 && cnt <= S.ntsnap)
+  if (S.imaging == 4 && S.tstep > 0 && below && cnt <= S.ntsnap)
     se = se + (((2.0f * taper) * S.ref[pp]) * S.wave[(long long)(cnt - 1) * nphys + pp]) / vc;
   // Extraction_wavefield (Extraction.f90:562-601).
-  if (S.extract_wave && cnt <= S.ntsnap) S.wave[(long long)(cnt - 1) * nphys + pp] = u2c;
-  if (S.imaging == 3 && S.tstep < 0) {
+  if (S.extract_wave && cnt <= S.ntsnap)
+    S.wave[(long long)(cnt - 1) * nphys + pp] = below ? u2c : 0.f;
+  if (S.imaging == 3 && S.tstep < 0 && below) {
     const int index = S.ntsnap - cnt + 1;
     if (index >= 1) {
       const float wsn = S.wave[(long long)(index - 1) * nphys + pp];
@@ -265,9 +268,12 @@ __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp,
     for (int m = 0; m < 4; ++m) {
       const int r = tz + 16 * m, i = z0 + r;
       if (!t2_row_ok(h, i)) continue;
+      // Under a free surface the rows above it are stored as zero and take
+      // no imaging (Extraction.f90:580-592, Imaging.f90:248-258).
+      const bool below = i >= h.irow0;
       const float u = su[(jl + 4) * T2_SZ + 4 + r];
-      if (stp.extract) stp.wsave[pc + i] = u;
-      if (stp.img) {
+      if (stp.extract) stp.wsave[pc + i] = below ? u : 0.f;
+      if (stp.img && below) {
         const float wsn = P.w[hh][m];
         float im = P.im[hh][m];
         if (stp.img == 1) {
@@ -582,7 +588,8 @@ __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const fl
                                          int bar) {
   if (h.rigid) return;   // exact-adjoint mode: no absorbing boundary
   const int tzi = t2_tzi(e), txi = t2_txi(e);
-  const bool top = tzi == 0, bottom = tzi == h.ntz - 1;
+  // A free surface does not absorb at the top (Boundary.f90:104-108).
+  const bool top = tzi == 0 && !h.surf, bottom = tzi == h.ntz - 1;
   const bool left = txi == 0, right = txi == h.ntx - 1;
   if (!(top || bottom || left || right)) return;
   const int z0 = t2_z0(h, e), x0 = t2_x0(h, e);
@@ -625,7 +632,8 @@ __device__ __forceinline__ void t2_edges(const T2Shot &h, int s, int e, const fl
     const bool rgt = tid >= 64;
     const bool mine = tid < 128 && ((!rgt && left) || (rgt && right));
     const int r = tid & 63, i = z0 + r;
-    if (mine && i >= h.nmin1 && i <= h.nmax1) {
+    // Under a free surface the side lines start at row 1.
+    if (mine && i >= (h.surf ? 1 : h.nmin1) && i <= h.nmax1) {
       const int dir = rgt ? -1 : 1;
       const int p = rgt ? h.nmax2 - 3 : h.nmin2 + 3;      // innermost output column
       float c[8], U2[10], U1[10], out[8];
