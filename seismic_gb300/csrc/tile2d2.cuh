@@ -339,8 +339,7 @@ __device__ __forceinline__ void tf_tile(const BatchTables &t, const T2Shot &h, c
   const T2Pairs c = t2_pairs(h);
   const float *U2 = st;
   const float *V = st + TF_U2;
-  const float *U1 = V + tf_vel_floats<ADJ>();
-  const float *U0 = U1 + TF_EXT;
+  const float *U1 = V + tf_vel_floats<ADJ>();   // U0 follows at U1 + TF_EXT
   const bool liveb = sb.live;
   const bool inj_a = h.inj_on && !(z0 + TF_Z + 3 < h.bi0 || z0 - 4 > h.bi1 ||
                                    x0 + TF_X + 3 < h.bj0 || x0 - 4 > h.bj1);

@@ -20,6 +20,10 @@ value ranges of the benchmark configurations instead:
 * ``config3``: the Born / FWI-gradient grid, 1201 x 3401 at 6.25 m, dt
   0.5 ms, background = the layered-faulted generator (seed 3) smoothed by a
   150 m Gaussian, reflectivity = 1 % density spikes N(0, 0.05) relative.
+* ``config5``: the 3D survey, 200 (z) x 400 (x) x 400 (y) at 12.5 m, dt
+  0.9 ms (the stated 1 ms exceeds the 3D Courant limit), 3 s; 25 dipping
+  layers, 4 planar faults and a Gaussian salt body at 4500 m/s (seed 5);
+  64 shots on an 8 x 8 surface grid, receivers every 100 m over the model.
 """
 from __future__ import annotations
 
@@ -197,3 +201,69 @@ def config3(nt: int | None = None, rec_step: int = 2) -> dict:
     shots = [np.array([2 * d, x, 0.0], np.float32) for x in sx]
     return {"g": g, "vel": vel, "ref": ref, "rec": rec, "shots": shots,
             "wavelet": ricker(c["f0"], c["dt"], nt)}
+
+
+def layered_faulted_3d(nz: int, nx: int, ny: int, d: float, seed: int, nlayers: int = 25,
+                       nfaults: int = 4, vmin: float = 1500.0, vmax: float = 4700.0,
+                       salt_v: float = 4500.0) -> np.ndarray:
+    """Dipping layers (dips in x and y), planar normal faults with 20-80 m
+    throw and a Gaussian salt body (the region where an anisotropic
+    Gaussian exceeds 1/2) at salt_v.  Returns a C array (ny, nx, nz) =
+    Fortran a(nz, nx, ny)."""
+    rng = np.random.default_rng(seed)
+    zmax, xmax, ymax = (nz - 1) * d, (nx - 1) * d, (ny - 1) * d
+    Z, X, Y = np.meshgrid(np.arange(nz) * d, np.arange(nx) * d, np.arange(ny) * d,
+                          indexing="ij")
+    Zeff = Z.copy()
+    for _ in range(nfaults):
+        # A plane through (xf, yf) at the surface, dipping 55-70 degrees.
+        xf, yf = rng.uniform(0.2, 0.8) * xmax, rng.uniform(0.2, 0.8) * ymax
+        az = rng.uniform(0.0, math.pi)
+        nxv, nyv = math.cos(az), math.sin(az)
+        slope = math.tan(math.radians(rng.uniform(55.0, 70.0)))
+        throw = rng.uniform(20.0, 80.0)
+        hanging = (X - xf) * nxv + (Y - yf) * nyv > Z / slope
+        Zeff = np.where(hanging, Zeff - throw, Zeff)
+    depths = np.sort(rng.uniform(0.03, 0.97, nlayers)) * zmax
+    dx_, dy_ = rng.uniform(-0.08, 0.08, nlayers), rng.uniform(-0.08, 0.08, nlayers)
+    idx = np.zeros(Z.shape, np.int32)
+    for k in range(nlayers):
+        idx += (Zeff > depths[k] + dx_[k] * (X - 0.5 * xmax) + dy_[k] * (Y - 0.5 * ymax)).astype(
+            np.int32)
+    base = vmin + (vmax - 300.0 - vmin) * (np.arange(nlayers + 1) / nlayers)
+    vl = np.clip(base + rng.uniform(-100.0, 100.0, nlayers + 1), vmin, vmax)
+    v = vl[idx]
+    cz, cx, cy = rng.uniform(0.45, 0.65) * zmax, rng.uniform(0.35, 0.65) * xmax, \
+        rng.uniform(0.35, 0.65) * ymax
+    sz, sx, sy = rng.uniform(0.10, 0.15) * zmax, rng.uniform(0.10, 0.18) * xmax, \
+        rng.uniform(0.10, 0.18) * ymax
+    g = np.exp(-0.5 * (((Z - cz) / sz) ** 2 + ((X - cx) / sx) ** 2 + ((Y - cy) / sy) ** 2))
+    v = np.where(g > 0.5, salt_v, v)
+    return np.ascontiguousarray(np.transpose(v, (2, 1, 0)), dtype=np.float32)
+
+
+CONFIG5 = {"nz": 200, "nx": 400, "ny": 400, "d": 12.5, "dt": 9e-4, "t": 3.0, "snapi": 4,
+           "ntaper": 20, "f0": 15.0, "seed": 5, "rec_step": 8}
+
+
+def config5(nt: int | None = None) -> dict:
+    """Model genpar, velocity (ny, nx, nz), wavelet, the 64 shots (sources
+    on an 8 x 8 grid at 25 m depth) and the receiver patch every rec_step
+    cells at 12.5 m depth (6 km x 6 km patches cover the 5 km model, so
+    every shot records the whole grid)."""
+    from . import make_genpar
+    c = CONFIG5
+    nz, nx, ny, d = c["nz"], c["nx"], c["ny"], c["d"]
+    nt = nt or int(round(c["t"] / c["dt"]))
+    vel = layered_faulted_3d(nz, nx, ny, d, seed=c["seed"])
+    g = make_genpar(nz, nx, ny, dz=d, dx=d, dy=d, dt=c["dt"], nt=nt, ntaper=c["ntaper"],
+                    lsinc=7, snapi=c["snapi"], twoD=False, fmax=30.0)
+    st = c["rec_step"]
+    rx, ry = np.meshgrid(np.arange(0, nx, st) * d, np.arange(0, ny, st) * d, indexing="ij")
+    rec = np.zeros((rx.size, 3), np.float32)
+    rec[:, 0], rec[:, 1], rec[:, 2] = d, rx.ravel(), ry.ravel()
+    sx = np.linspace(0.1, 0.9, 8) * (nx - 1) * d
+    sy = np.linspace(0.1, 0.9, 8) * (ny - 1) * d
+    shots = [{"sou": np.array([2 * d, x, y], np.float32), "rec": rec, "nt": nt}
+             for y in sy for x in sx]
+    return {"g": g, "vel": vel, "wavelet": ricker(c["f0"], c["dt"], nt), "shots": shots}

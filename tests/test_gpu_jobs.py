@@ -367,3 +367,43 @@ def test_fwi_non_finite_data_is_reported(ctx):
     with pytest.raises(sw.SwaveError) as e:
         ctx.fwi_fct_gdt(d, vel, w, shots, vpmask=mask)
     assert e.value.code == sw.SW_NUMERIC
+
+
+def test_rtm_job_3d_window_bitexact(ctx, oracle):
+    """The multi-shot RTM job in 3D on a 60 x 90 x 80 model (10 m; compute
+    windows of about 0.6 million points): two shots of different source
+    position and receiver patch migrated in one batch by the pipelined 3D
+    kernel (Higdon z and x lines in the kernel), stacked image and
+    illumination bit-exact with the oracle's RTM_to_memory per window and
+    mod_copy_image (to_disk_to_memory_RTM.f90:358-492,
+    ExtractPadModel.f90:662-697)."""
+    from tests.cases import model3d
+    nz, nx, ny, d, dt, nt = 60, 90, 80, 10.0, 1.5e-3, 200
+    g = sw.make_genpar(nz, nx, ny, dz=d, dx=d, dy=d, dt=dt, nt=nt, ntaper=10, lsinc=7, snapi=4,
+                       twoD=False, fmax=30.0)
+    vel = model3d(nz, nx, ny, d, seed=4)
+    w = synth.ricker(12.0, dt, nt)
+    shots = []
+    for (sx, sy, half) in ((300.0 + 2.0, 350.0 - 1.0, 250.0), (560.0, 420.0 + 3.0, 200.0)):
+        gx, gy = np.meshgrid(np.arange(sx - half, sx + half, 30.0),
+                             np.arange(sy - half, sy + half, 30.0), indexing="ij")
+        keep = (gx >= 0) & (gx <= (nx - 1) * d) & (gy >= 0) & (gy <= (ny - 1) * d)
+        rec = np.zeros((int(keep.sum()), 3), np.float32)
+        rec[:, 0], rec[:, 1], rec[:, 2] = d + 1.0, gx[keep], gy[keep]
+        shots.append({"sou": np.array([25.0, sx, sy], np.float32), "rec": rec, "nt": nt})
+    mj = sw.RTMJob(ctx, g, vel, w, shots, aperture_x=100.0, aperture_y=100.0)
+    mj.set_batch(2)
+    data = mj.model()
+    mj.close()
+    job_shots = [{"sou": s["sou"], "rec": s["rec"], "data": dd} for s, dd in zip(shots, data)]
+    job = sw.RTMJob(ctx, g, vel, w, job_shots, aperture_x=100.0, aperture_y=100.0)
+    job.set_batch(2)
+    job.run()
+    im, il, _ = job.result()
+    b, pts = job.info()
+    job.close()
+    rim, ril, _ = oracle.rtm_job(g, vel, w, job_shots, aperture_x=100.0, aperture_y=100.0)
+    assert b == 2 and pts > 2 * 2 * nt * 400_000
+    assert np.abs(rim).max() > 0
+    np.testing.assert_array_equal(im, rim)
+    np.testing.assert_array_equal(il, ril)
