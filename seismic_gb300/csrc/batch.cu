@@ -502,7 +502,7 @@ __global__ void k_bhiggz(BatchTables t, int s_off) {
   const int b = find_shot(t.hz_start, t.nshots, q >> 1);
   const ShotDev &S = t.shots[b];
   const int s = *t.counter + s_off;
-  if (s >= S.nsteps || S.t3_edges) return;
+  if (s >= S.nsteps) return;
   const Geom &g = S.g;
   const int n2 = g.nmax2 - g.nmin2 + 1;
   const long long l = (q >> 1) - t.hz_start[b];
@@ -524,7 +524,6 @@ __global__ void k_bhiggx(BatchTables t, int s_off) {
   const long long cs = (long long)n1 * n3;
   const int i = g.nmin1 + (int)(l % n1), k = g.nmin3 + (int)(l / n1);
   if (S.surf && i < 1) return;   // side lines from row 1 under a free surface
-  if (S.t3_edges) return;        // the pipelined 3D kernel ran them
   const float *u1 = S.f[(s + 2) % 5], *u2 = S.f[(s + 3) % 5];
   float *u3 = S.f[(s + 4) % 5];
   const long long L = g.ld1;
@@ -875,7 +874,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   } else if (!has_3d && tile.fused_edges) {
     k_bedges2d<<<(tile.n_edge + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
-  } else if (!(has_3d && tile.stream3d == 2 && tile.t3_edges_all)) {
+  } else {
     k_bhiggz<<<(2 * n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
     k_bhiggx<<<(2 * n_hx + 127) / 128, 128, 0, s>>>(t, s_off);
     nl += 2;

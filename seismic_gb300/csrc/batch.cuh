@@ -46,9 +46,6 @@ struct ShotDev {
   int tmin, tstep, nsteps, nt, snapi, ntsnap;
   int tcnt;               // first time sample of the whole phase (snapshot counting)
   int t3_ty;              // planes per work unit of the pipelined 3D kernel
-  int t3_edges;           // 1: the pipelined 3D kernel runs this shot's Higdon z and x
-                          // lines itself (its first and last z and x tiles own >= 6
-                          // rows / columns); the y lines stay in k_bhiggy
   int extract_wave, imaging, adj2d, adj3d;
   float *wave;            // ntsnap*nz*nx*ny snapshots
   float *image, *illum;
@@ -218,17 +215,7 @@ struct StepTile {
   int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
   int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)
   int fuse2 = 0;       // 2D tiles: two time steps per launch (tile2d2.cuh)
-  int t3_edges_all = 0; // 3D tiles: every shot's z and x Higdon lines run in the tile kernel
 };
-
-// Whether the pipelined 3D kernel can run a shot's Higdon z and x lines:
-// 32-cell tiles start at nmin, so the last tile along z (x) owns
-// n - 32 * floor((n - 1) / 32) rows (columns); the lines of an edge read u3
-// two cells inside it, which must lie in the same tile.
-inline bool t3_edges_fusable(int n1, int n2) {
-  const int r1 = n1 - 32 * ((n1 - 1) / 32), r2 = n2 - 32 * ((n2 - 1) / 32);
-  return n1 >= 16 && n2 >= 16 && r1 >= 6 && r2 >= 6;
-}
 
 // Threads of the fused 2D edge kernel for one shot: four corner warps and
 // one thread per remaining half line, rounded to whole warps.  0 when the

@@ -1,6 +1,6 @@
 // higdon.cuh - the Higdon absorbing-boundary recurrence along one edge
-// line (Boundary_3d, Boundary.f90:89-184,366-447), shared by the separate
-// edge kernels (batch.cu) and the pipelined 3D step kernel (tile3d.cuh).
+// line (Boundary_3d, Boundary.f90:89-184,366-447) for the separate edge
+// kernels (batch.cu).
 #pragma once
 
 #include <cstdint>

@@ -328,12 +328,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     S.tmin = d.tmin;
     S.tcnt = io.tcnt ? io.tcnt : d.tmin;
     S.t3_ty = tile.ty;
-    // The pipelined 3D kernel runs the z and x Higdon lines of shots whose
-    // edge tiles hold them (not in the exact-adjoint mode, which has none,
-    // nor under a free surface, which runs on the point tiles).
-    S.t3_edges = (!g.twoD && t3 && !opt.rigid && !S.surf &&
-                  t3_edges_fusable(G[b].nmax1 - G[b].nmin1 + 1, G[b].nmax2 - G[b].nmin2 + 1))
-                     ? 1 : 0;
+
     S.tstep = d.tstep;
     S.nsteps = (d.tmax - d.tmin + d.tstep) / d.tstep;
     S.nt = g.nt;
@@ -558,9 +553,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   tile.fused_edges = fused_edges ? 1 : 0;
   tile.rigid = opt.rigid ? 1 : 0;
   tile.n_edge = edge[nb];
-  tile.t3_edges_all = 1;
-  for (auto &S : hs)
-    if (!S.g.twoD && !S.t3_edges) tile.t3_edges_all = 0;
+
   for (auto &S : hs) {
     if (S.g.twoD) {
       if (S.adj2d) tile.has_adj2d = 1;

@@ -15,7 +15,6 @@
 #pragma once
 
 #include "batch.cuh"
-#include "higdon.cuh"
 #include "tile2d.cuh"
 
 namespace swave {
@@ -192,11 +191,6 @@ __device__ __forceinline__ void tile3d_persistent(const BatchTables &t, int s_of
     float4 nxt = t3_col4<ADJ>(u2, S.vel, colbase + P * (k0 + 4 - g.lo3));
     const int it = S.tmin + s * S.tstep;
     const bool snapstep = (it % S.snapi) == 0 && (S.extract_wave || S.imaging != 0);
-    // Edge units of a shot whose Higdon z and x lines run here.
-    const bool top = t3_tzi(e) == 0, bot = z0 + T3_Z > g.nmax1;
-    const bool lft = t3_txi(e) == 0, rgt = x0 + T3_X > g.nmax2;
-    const bool edges = S.t3_edges && (top || bot || lft || rgt);
-    const int warp = tid >> 5, lane = tid & 31;
     const Coefs c = S.c;
     float *u3 = S.f[(s + 4) % 5];
     for (int p = 0; p < np; ++p) {
@@ -333,18 +327,6 @@ __device__ __forceinline__ void tile3d_persistent(const BatchTables &t, int s_of
         }
       }
       __syncthreads();   // the stage is free for plane p + S
-      // Higdon z and x lines of plane k in the units at the domain edges
-      // (z lines of the unit's columns, then x lines of its rows: the
-      // reference's order); the u3 cells they read inside the edge were
-      // stored above.  Warps 0-3 only; the others go on to the next plane.
-      if (edges && warp < 4) {
-        const float *u1g = S.f[(s + 2) % 5];
-        if (warp == 0 && top && x0 + lane <= g.nmax2) higdon_zline(S, x0 + lane, k, false, u1g, u2, u3);
-        if (warp == 1 && bot && x0 + lane <= g.nmax2) higdon_zline(S, x0 + lane, k, true, u1g, u2, u3);
-        asm volatile("bar.sync 1, 128;" ::: "memory");   // z lines before x lines
-        if (warp == 2 && lft && z0 + lane <= g.nmax1) higdon_xline(S, z0 + lane, k, false, u1g, u2, u3);
-        if (warp == 3 && rgt && z0 + lane <= g.nmax1) higdon_xline(S, z0 + lane, k, true, u1g, u2, u3);
-      }
 #pragma unroll
       for (int l = 0; l < 8; ++l) q[l] = q[l + 1];
     }

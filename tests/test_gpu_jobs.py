@@ -373,7 +373,7 @@ def test_rtm_job_3d_window_bitexact(ctx, oracle):
     """The multi-shot RTM job in 3D on a 60 x 90 x 80 model (10 m; compute
     windows of about 0.6 million points): two shots of different source
     position and receiver patch migrated in one batch by the pipelined 3D
-    kernel (Higdon z and x lines in the kernel), stacked image and
+    kernel, stacked image and
     illumination bit-exact with the oracle's RTM_to_memory per window and
     mod_copy_image (to_disk_to_memory_RTM.f90:358-492,
     ExtractPadModel.f90:662-697)."""

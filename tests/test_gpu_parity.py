@@ -248,11 +248,10 @@ def test_modeling_two_step_kernel(oracle, nt, rigid, shape):
 
 
 @pytest.mark.parametrize("nz", [30, 20])
-def test_modeling_3d_edges_in_tile_kernel_or_not(ctx, oracle, nz):
-    """3D modelling with the Higdon z and x lines inside the pipelined 3D
-    kernel (nz 30: compute domain 46 rows, its last 32-row tile owns 14) and
-    in the separate edge kernels (nz 20: the last tile owns 4 rows, too few
-    for the lines' inner cells): traces and final wavefield bit-exact."""
+def test_modeling_3d_partial_last_tile(ctx, oracle, nz):
+    """3D modelling whose last 32-row tile of the pipelined 3D kernel owns
+    14 rows (nz 30) or 4 rows (nz 20), the second inside the Higdon bottom
+    edge zone: traces and final wavefield bit-exact."""
     g, vel, sou, rec, w = case3d(nz=nz, nt=100)
     data, fu = ctx.modeling(g, vel, sou, w, rec, final_u2=True)
     ref, rfu = oracle.modeling(g, vel, sou, w, rec, final_u2=True)
