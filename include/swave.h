@@ -409,6 +409,55 @@ int sw_lbfgs_step(sw_lbfgs *s, double *x, double f, const double *g,
 /* Scalars of the last step: [iter, nfun, stp, gnorm, ys, yy, dginit, dg]. */
 int sw_lbfgs_diag(const sw_lbfgs *s, double *out8);
 
+/* ---- Out-of-core L-BFGS (libs/libnlinv/nlinv_lbfgs.f) ----------------------
+ * LBFGSOC / MCSRCHOC (lbfgs_type 1: per-parameter bounds, nlinv_lbfgs.f:
+ * 1-22,31-967) and LBFGSOLD / MCSRCHOLD (lbfgs_type 0: no bounds,
+ * :1066-1990), the solver of progs/inversion/L_BFGS.f90.  One call is one
+ * reverse-communication call of the reference: the caller keeps everything
+ * the solver saves between calls (the reference keeps it in files between
+ * program invocations: WorkArray.dat, Diag.dat, LbfgsDat.dat,
+ * McsrchDat.dat, Iflag.dat, Info.dat) and hands it back on the next call.
+ * The vectors run on the device in FP64 during the call. */
+typedef struct sw_lbfgs_oc_state {
+  /* LBFGSOC's SAVE scalars, in the order of LbfgsDat.dat
+   * (nlinv_lbfgs.f:277-281) */
+  double gtol, one, zero, gnorm, stp1, ftol, stpmin;
+  double stpmax, stp, ys, yy, sq, yr, beta, xnorm;
+  int mp, lp, iter, nfun, point, ispt, iypt, maxfev, info;
+  int bound, npt, cp, i, nfev, inmc, iycn, iscn;
+  int finish;
+  /* MCSRCHOC's SAVE scalars, in the order of McsrchDat.dat (:725-730) */
+  int infoc, j;
+  int brackt, stage1;
+  double dg, dgm, dginit, dgtest, dgx, dgxm, dgy, dgym;
+  double finit, ftest1, fm, fx, fxm, fy, fym, stx, sty;
+  double stmin, stmax, width, width1;
+} sw_lbfgs_oc_state;
+
+typedef struct sw_lbfgs_oc_desc {
+  int n;                  /* model size (all parameters)                    */
+  int m;                  /* corrections kept (MSAVE, 5 in L_BFGS.f90)       */
+  int nparam;             /* parameter blocks of n / nparam values           */
+  const double *xmin;     /* nparam lower bounds (lbfgs_type 1)              */
+  const double *xmax;     /* nparam upper bounds                             */
+  int lbfgs_type;         /* 0: LBFGSOLD, no clipping; 1: LBFGSOC            */
+  int bound_type;         /* 1: clip every trial model, 2: every new iterate */
+  int stp1_opt;           /* first trial step: 1: |x| / |g| / 100, else 1 / |g| */
+  double step_init;       /* 999999: none; else the first trial step          */
+  double eps, xtol;       /* 1e-20 and machine epsilon in L_BFGS.f90          */
+} sw_lbfgs_oc_desc;
+
+/* One LBFGSOC call.  x (n, in/out): the model; f and g (n): the objective
+ * and gradient at x; w (n(2m+1) + 2m) and diag (n): the working array and
+ * DIAG in the reference's layout; state, *iflag and *myinfo in and out.
+ * *iflag = 0 starts a new solve (w, diag and state are then written, not
+ * read).  Returns with *iflag = 1 (evaluate f, g at x and call again),
+ * 0 (converged) or < 0 (the reference's error codes); *myinfo = 1 when the
+ * call completed an iteration. */
+int sw_lbfgs_oc_step(sw_ctx *ctx, const sw_lbfgs_oc_desc *d, double *x, double f,
+                     const double *g, double *w, double *diag, sw_lbfgs_oc_state *state,
+                     int *iflag, int *myinfo);
+
 /* ---- Tuning (no counterpart in the reference: launch shape knobs) -------- */
 typedef struct sw_tuning {
   int step_kernel;   /* fused step: 0 = 32x8 point tiles, 1 = streaming, 2 = TMA-staged

@@ -128,6 +128,27 @@ module swave_iface
      real(c_float) :: mod_thresh, hin_thresh
   end type sw_reg_state
 
+  ! LBFGSOC / MCSRCHOC saved scalars (LbfgsDat.dat, McsrchDat.dat order)
+  type, bind(C) :: sw_lbfgs_oc_state
+     real(c_double) :: gtol, one, zero, gnorm, stp1, ftol, stpmin
+     real(c_double) :: stpmax, stp, ys, yy, sq, yr, beta, xnorm
+     integer(c_int) :: mp, lp, iter, nfun, point, ispt, iypt, maxfev, info
+     integer(c_int) :: bound, npt, cp, i, nfev, inmc, iycn, iscn
+     integer(c_int) :: finish
+     integer(c_int) :: infoc, j
+     integer(c_int) :: brackt, stage1
+     real(c_double) :: dg, dgm, dginit, dgtest, dgx, dgxm, dgy, dgym
+     real(c_double) :: finit, ftest1, fm, fx, fxm, fy, fym, stx, sty
+     real(c_double) :: stmin, stmax, width, width1
+  end type sw_lbfgs_oc_state
+
+  type, bind(C) :: sw_lbfgs_oc_desc
+     integer(c_int) :: n, m, nparam
+     type(c_ptr)    :: xmin, xmax       ! c_loc of nparam doubles each
+     integer(c_int) :: lbfgs_type, bound_type, stp1_opt
+     real(c_double) :: step_init, eps, xtol
+  end type sw_lbfgs_oc_desc
+
   type, bind(C) :: sw_tuning
      integer(c_int) :: step_kernel
      integer(c_int) :: tile_z
@@ -372,6 +393,17 @@ module swave_iface
        import :: c_int, c_ptr, c_double
        type(c_ptr), value :: s
        real(c_double)     :: out8(8)
+     end function
+     integer(c_int) function sw_lbfgs_oc_step(ctx, d, x, f, g, w, diag, st, iflag, myinfo) &
+          bind(C, name="sw_lbfgs_oc_step")
+       import :: c_int, c_ptr, c_double, sw_lbfgs_oc_desc, sw_lbfgs_oc_state
+       type(c_ptr), value      :: ctx
+       type(sw_lbfgs_oc_desc)  :: d
+       real(c_double)          :: x(*)
+       real(c_double), value   :: f
+       real(c_double)          :: g(*), w(*), diag(*)
+       type(sw_lbfgs_oc_state) :: st
+       integer(c_int)          :: iflag, myinfo
      end function
      ! ---- tuning, preconditioner, instrumentation ------------------------------
      integer(c_int) function sw_ctx_set_tuning(ctx, t) bind(C, name="sw_ctx_set_tuning")

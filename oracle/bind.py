@@ -74,6 +74,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         fn = getattr(lib, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    from seismic_gb300 import SwLbfgsOcDesc, SwLbfgsOcState
+    lib.oracle_lbfgs_oc_step.argtypes = [C.POINTER(SwLbfgsOcDesc), _dp, C.c_double, _dp, _dp,
+                                         _dp, C.POINTER(SwLbfgsOcState), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]
+    lib.oracle_lbfgs_oc_step.restype = C.c_int
     lib.oracle_mksinc.argtypes = [_fp, C.c_int, C.c_float]
     lib.oracle_mksinc.restype = None
     lib.oracle_lbfgs_create.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _fp, C.c_int,
@@ -447,3 +452,17 @@ def l_bfgs(fctgdt, x, niter, neval, xmin, xmax, vpmask=None, const_type=2, freez
     if not cont:
         x = xsave.astype(np.float32)
     return x, np.array(history, np.float32), models
+
+
+def lbfgs_oc_step(desc, x, f, g, w, diag, state, iflag, myinfo=0):
+    """LBFGSOC / LBFGSOLD (nlinv_lbfgs.f:31-613,1066-1636), one call: x, w,
+    diag (float64) and state (seismic_gb300.SwLbfgsOcState) updated in
+    place; returns (iflag, myinfo)."""
+    lib = load()
+    fl, mi = C.c_int(iflag), C.c_int(myinfo)
+    gg = np.ascontiguousarray(g, np.float64)
+    _chk(lib.oracle_lbfgs_oc_step(C.byref(desc), x.ctypes.data_as(_dp), float(f),
+                                  gg.ctypes.data_as(_dp), w.ctypes.data_as(_dp),
+                                  diag.ctypes.data_as(_dp), C.byref(state), C.byref(fl),
+                                  C.byref(mi)), "lbfgs_oc")
+    return fl.value, mi.value

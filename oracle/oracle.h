@@ -124,6 +124,9 @@ void oracle_lbfgs_destroy(or_lbfgs *s);
 int oracle_lbfgs_step(or_lbfgs *s, double *x, double f, const double *g,
                       double eps, double xtol, int *iflag, int *myinfo);
 void oracle_lbfgs_diag(const or_lbfgs *s, double *out8);
+int oracle_lbfgs_oc_step(const sw_lbfgs_oc_desc *d, double *x, double f, const double *g,
+                         double *w, double *diag, sw_lbfgs_oc_state *st, int *iflag,
+                         int *myinfo);
 
 /* triangle2 smoothing (libs/libwave/Smoothing.f90:87-138), in place. */
 int oracle_triangle2(float *uu, int n1, int n2, int n3, int rect1, int rect2,

@@ -1544,6 +1544,13 @@ struct or_lbfgs {
   std::vector<double> xinit;
   std::vector<double> w;     // 1-based, N*(2M+1)+2M
   std::vector<double> diag;  // 1-based
+  // libs/libnlinv's variant (LBFGSOC / LBFGSOLD): per-parameter bounds, the
+  // first-step options and its line-search constants.
+  bool oc = false;
+  int nparam = 1;
+  std::vector<double> pmin, pmax;
+  int stp1_opt = 1;
+  double step_init = 999999.0;
   // LBFGS SAVE state
   int iter = 0, nfun = 0, point = 0, ispt = 0, iypt = 0, npt = 0, bound = 0, info = 0,
       nfev = 0, maxfev = 20, cp = 0;
@@ -1574,8 +1581,23 @@ double ddot(int n, const double *dx, const double *dy) {
   return dtemp;
 }
 
+// FREEZE_XOC (nlinv_lbfgs.f:1-22): block j of n / nparam values clipped to
+// [xmin(j), xmax(j)].
+void freeze_xoc(const or_lbfgs &s, double *x) {
+  const int m = s.n / s.nparam;
+  for (int j = 0; j < s.nparam; ++j)
+    for (int i = j * m; i < j * m + m; ++i) {
+      x[i] = std::max(s.pmin[j], x[i]);
+      x[i] = std::min(s.pmax[j], x[i]);
+    }
+}
+
 // FREEZE_X (lbfgs.f:1-43).
 void freeze_x(const or_lbfgs &s, double *x) {
+  if (s.oc) {
+    freeze_xoc(s, x);
+    return;
+  }
   if (s.type) {
     for (int i = 0; i < s.n; ++i) {
       x[i] = std::max(s.xmin, x[i]);
@@ -1708,7 +1730,9 @@ void mcsrch(or_lbfgs &S, double *x, double f, const double *g, const double *s,
             double &stp, double ftol, double xtol, int maxfev, int &info, int &nfev,
             double *wa) {
   const int n = S.n;
-  const double p5 = 0.5, p66 = 0.66, xtrapf = 4.0, zero = 0.0;
+  // XTRAPF is 4.0D1 in libinv's MCSRCH (lbfgs.f:792) and 4.0D0 in libnlinv's
+  // MCSRCHOC / MCSRCHOLD (nlinv_lbfgs.f:752,1773).
+  const double p5 = 0.5, p66 = 0.66, xtrapf = S.oc ? 4.0 : 40.0, zero = 0.0;
   if (info == -1) goto L45;
   S.infoc = 1;
   if (n <= 0 || stp <= zero || ftol < zero || kGTOL < zero || xtol < zero ||
@@ -1804,7 +1828,12 @@ L10:
   S.iypt = S.ispt + n * m;
   for (int i = 1; i <= n; ++i) W[S.ispt + i] = -g[i - 1] * DIAG[i];
   S.gnorm = std::sqrt(ddot(n, g, g));
-  {
+  if (S.oc) {
+    // nlinv_lbfgs.f:333-341 (LBFGSOLD, :1366-1370: step_init or 1/|g|).
+    if (S.stp1_opt == 1) S.stp1 = std::sqrt(ddot(n, x, x)) / S.gnorm / 100;
+    else S.stp1 = 1.0 / S.gnorm;
+    if (S.step_init != 999999.0) S.stp1 = S.step_init;
+  } else {
     const double xnorm2 = std::sqrt(ddot(n, x, x));
     if (S.boundt == 0) S.stp1 = 1.0 / S.gnorm;
     else S.stp1 = xnorm2 / S.gnorm / 100;
@@ -2407,6 +2436,67 @@ int oracle_lbfgs_step(or_lbfgs *s, double *x, double f, const double *g, double 
                       double xtol, int *iflag, int *myinfo) {
   return lbfgs(*s, x, f, g, eps, xtol, *iflag, *myinfo);
 }
+// One LBFGSOC / LBFGSOLD call (nlinv_lbfgs.f:31-613,1066-1636) with the
+// saved state passed in and out, as L_BFGS.f90 keeps it in files.
+int oracle_lbfgs_oc_step(const sw_lbfgs_oc_desc *d, double *x, double f, const double *g,
+                         double *w, double *diag, sw_lbfgs_oc_state *st, int *iflag,
+                         int *myinfo) {
+  if (!d || d->n <= 0 || d->m <= 0 || d->nparam <= 0 || d->n % d->nparam) return SW_BAD_PARAM;
+  const int n = d->n, m = d->m;
+  or_lbfgs S;
+  S.n = n; S.m = m;
+  S.oc = true;
+  S.nparam = d->nparam;
+  S.type = false;
+  if (d->lbfgs_type == 1) {
+    if (!d->xmin || !d->xmax) return SW_BAD_PARAM;
+    S.pmin.assign(d->xmin, d->xmin + d->nparam);
+    S.pmax.assign(d->xmax, d->xmax + d->nparam);
+    S.boundt = d->bound_type;
+    S.stp1_opt = d->stp1_opt;
+  } else {
+    S.boundt = 0;
+    S.stp1_opt = 0;
+  }
+  S.step_init = d->step_init;
+  const size_t nw = (size_t)n * (2 * m + 1) + 2 * m;
+  S.w.assign(nw + 1, 0.0);
+  S.diag.assign((size_t)n + 1, 0.0);
+  if (*iflag != 0) {
+    std::copy(w, w + nw, S.w.begin() + 1);
+    std::copy(diag, diag + n, S.diag.begin() + 1);
+    S.gnorm = st->gnorm; S.stp1 = st->stp1; S.ftol = st->ftol; S.stp = st->stp;
+    S.ys = st->ys; S.yy = st->yy; S.xnorm = st->xnorm;
+    S.iter = st->iter; S.nfun = st->nfun; S.point = st->point; S.ispt = st->ispt;
+    S.iypt = st->iypt; S.maxfev = st->maxfev; S.info = st->info; S.bound = st->bound;
+    S.npt = st->npt; S.cp = st->cp; S.nfev = st->nfev; S.finish = st->finish != 0;
+    S.infoc = st->infoc; S.brackt = st->brackt != 0; S.stage1 = st->stage1 != 0;
+    S.dg = st->dg; S.dgm = st->dgm; S.dginit = st->dginit; S.dgtest = st->dgtest;
+    S.dgx = st->dgx; S.dgxm = st->dgxm; S.dgy = st->dgy; S.dgym = st->dgym;
+    S.finit = st->finit; S.ftest1 = st->ftest1; S.fm = st->fm; S.fx = st->fx;
+    S.fxm = st->fxm; S.fy = st->fy; S.fym = st->fym; S.stx = st->stx; S.sty = st->sty;
+    S.stmin = st->stmin; S.stmax = st->stmax; S.width = st->width; S.width1 = st->width1;
+  }
+  const int rc = lbfgs(S, x, f, g, d->eps, d->xtol, *iflag, *myinfo);
+  std::copy(S.w.begin() + 1, S.w.end(), w);
+  std::copy(S.diag.begin() + 1, S.diag.end(), diag);
+  std::memset(st, 0, sizeof(*st));
+  st->gtol = kGTOL; st->one = 1.0; st->zero = 0.0; st->gnorm = S.gnorm; st->stp1 = S.stp1;
+  st->ftol = S.ftol; st->stpmin = kSTPMIN; st->stpmax = kSTPMAX; st->stp = S.stp;
+  st->ys = S.ys; st->yy = S.yy; st->xnorm = S.xnorm;
+  st->mp = 6; st->lp = 6; st->iter = S.iter; st->nfun = S.nfun; st->point = S.point;
+  st->ispt = n + 2 * m; st->iypt = n + 2 * m + n * m; st->maxfev = S.maxfev;
+  st->info = S.info; st->bound = S.bound; st->npt = S.npt; st->cp = S.cp; st->nfev = S.nfev;
+  st->finish = S.finish ? 1 : 0;
+  st->infoc = S.infoc; st->brackt = S.brackt ? 1 : 0; st->stage1 = S.stage1 ? 1 : 0;
+  st->dg = S.dg; st->dgm = S.dgm; st->dginit = S.dginit; st->dgtest = S.dgtest;
+  st->dgx = S.dgx; st->dgxm = S.dgxm; st->dgy = S.dgy; st->dgym = S.dgym;
+  st->finit = S.finit; st->ftest1 = S.ftest1; st->fm = S.fm; st->fx = S.fx; st->fxm = S.fxm;
+  st->fy = S.fy; st->fym = S.fym; st->stx = S.stx; st->sty = S.sty;
+  st->stmin = S.stmin; st->stmax = S.stmax; st->width = S.width; st->width1 = S.width1;
+  return rc;
+}
+
 void oracle_lbfgs_diag(const or_lbfgs *s, double *o) {
   o[0] = s->iter; o[1] = s->nfun; o[2] = s->stp; o[3] = s->gnorm;
   o[4] = s->ys; o[5] = s->yy; o[6] = s->dginit; o[7] = s->dg;

@@ -116,6 +116,35 @@ class SwShot(C.Structure):
                 ("data", _fp), ("nt", C.c_int)]
 
 
+# LBFGSOC's and MCSRCHOC's saved scalars, in the order of the reference's
+# LbfgsDat.dat / McsrchDat.dat lines (nlinv_lbfgs.f:277-281, 725-730).
+LBFGS_OC_LINES = (("gtol", "one", "zero", "gnorm", "stp1", "ftol", "stpmin"),
+                  ("stpmax", "stp", "ys", "yy", "sq", "yr", "beta", "xnorm"),
+                  ("mp", "lp", "iter", "nfun", "point", "ispt", "iypt", "maxfev", "info"),
+                  ("bound", "npt", "cp", "i", "nfev", "inmc", "iycn", "iscn"),
+                  ("finish",))
+MCSRCH_OC_LINES = (("infoc", "j"), ("brackt", "stage1"),
+                   ("dg", "dgm", "dginit", "dgtest", "dgx", "dgxm", "dgy", "dgym"),
+                   ("finit", "ftest1", "fm", "fx", "fxm", "fy", "fym", "stx", "sty"),
+                   ("stmin", "stmax", "width", "width1"))
+_OC_INTS = {"mp", "lp", "iter", "nfun", "point", "ispt", "iypt", "maxfev", "info", "bound",
+            "npt", "cp", "i", "nfev", "inmc", "iycn", "iscn", "finish", "infoc", "j", "brackt",
+            "stage1"}
+
+
+class SwLbfgsOcState(C.Structure):
+    """sw_lbfgs_oc_state: the out-of-core L-BFGS's saved scalars."""
+    _fields_ = [(nm, C.c_int if nm in _OC_INTS else C.c_double)
+                for line in LBFGS_OC_LINES + MCSRCH_OC_LINES for nm in line]
+
+
+class SwLbfgsOcDesc(C.Structure):
+    _fields_ = [("n", C.c_int), ("m", C.c_int), ("nparam", C.c_int), ("xmin", _dp),
+                ("xmax", _dp), ("lbfgs_type", C.c_int), ("bound_type", C.c_int),
+                ("stp1_opt", C.c_int), ("step_init", C.c_double), ("eps", C.c_double),
+                ("xtol", C.c_double)]
+
+
 class SwTuning(C.Structure):
     _fields_ = [("step_kernel", C.c_int), ("tile_z", C.c_int), ("tile_x", C.c_int),
                 ("tile_y", C.c_int), ("graph_chunk", C.c_int), ("use_graph", C.c_int)]
@@ -162,6 +191,9 @@ _SIGS = {
     "sw_lbfgs_step": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, C.c_double, C.c_double,
                                 C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "sw_lbfgs_diag": (C.c_int, [C.c_void_p, _dp]),
+    "sw_lbfgs_oc_step": (C.c_int, [C.c_void_p, C.POINTER(SwLbfgsOcDesc), _dp, C.c_double, _dp,
+                                   _dp, _dp, C.POINTER(SwLbfgsOcState), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int)]),
     "sw_rtm_job_create": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), C.c_float, C.c_float, _fp,
                                     _fp, C.c_int, C.POINTER(SwShot), C.POINTER(C.c_void_p)]),
     "sw_rtm_job_set_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
@@ -410,6 +442,18 @@ class Context:
                                             arr, fptr(m), C.byref(f), fptr(grad), fptr(illum)))
         return (f.value, grad, illum, resids) if want_resid else (f.value, grad, illum)
 
+    def lbfgs_oc_step(self, desc: SwLbfgsOcDesc, x: np.ndarray, f: float, g, w: np.ndarray,
+                      diag: np.ndarray, state: SwLbfgsOcState, iflag: int,
+                      myinfo: int = 0) -> tuple[int, int]:
+        """sw_lbfgs_oc_step: one LBFGSOC call; x, w, diag (float64) and state
+        are updated in place; returns (iflag, myinfo)."""
+        fl, mi = C.c_int(iflag), C.c_int(myinfo)
+        self._check(self.lib.sw_lbfgs_oc_step(self.h, C.byref(desc), dptr(x), float(f),
+                                              dptr(np.ascontiguousarray(g, np.float64)),
+                                              dptr(w), dptr(diag), C.byref(state), C.byref(fl),
+                                              C.byref(mi)))
+        return fl.value, mi.value
+
     def fwi_regularize(self, desc: SwRegDesc, state: SwRegState, eval_, vel, f, grad,
                        vpmask=None, zweight=None):
         """compute_fct_gdt_reg's terms: returns (f, grad) after the sparse and
@@ -501,6 +545,18 @@ class RTMJob:
             self.close()
         except Exception:
             pass
+
+
+def lbfgs_oc_desc(n: int, m: int = 5, nparam: int = 1, xmin=None, xmax=None,
+                  lbfgs_type: int = 1, bound_type: int = 1, stp1_opt: int = 1,
+                  step_init: float = 999999.0, eps: float = 1.0e-20,
+                  xtol: float = float(np.finfo(np.float64).eps)) -> tuple:
+    """sw_lbfgs_oc_desc (and the bound arrays it points at, to keep alive)."""
+    lo = np.ascontiguousarray(np.zeros(nparam) if xmin is None else xmin, np.float64)
+    hi = np.ascontiguousarray(np.zeros(nparam) if xmax is None else xmax, np.float64)
+    d = SwLbfgsOcDesc(n, m, nparam, dptr(lo), dptr(hi), lbfgs_type, bound_type, stp1_opt,
+                      step_init, eps, xtol)
+    return d, (lo, hi)
 
 
 class LBFGS:

@@ -81,6 +81,7 @@ CLI_PROGRAMS = {
     "3DRTM.x": "rtm3d.c",
     "3DBORNMOD.x": "bornmod3d.c",
     "2DAFWI.x": "afwi2d.c",
+    "L_BFGS.x": "lbfgs.c",
 }
 
 

@@ -218,6 +218,18 @@ __global__ void k_freeze(long long n, int type, double xmin, double xmax, const 
   }
 }
 
+// FREEZE_XOC (nlinv_lbfgs.f:1-22): block j of m values clipped to
+// [pmin(j), pmax(j)].
+__global__ void k_freeze_blocks(long long n, long long m, const double *pmin, const double *pmax,
+                                double *x) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long j = q / m;
+    double v = fmax(pmin[j], x[q]);
+    x[q] = fmin(pmax[j], v);
+  }
+}
+
 inline int gsz(long long n) {
   long long b = (n + 255) / 256;
   return (int)std::max(1LL, std::min(b, 152LL * 8));
@@ -628,6 +640,14 @@ struct sw_lbfgs {
   double *x = nullptr, *g = nullptr;
   double *part = nullptr, *res = nullptr;
   std::vector<double> rho, alpha;   // W(N+1..N+M), W(N+M+1..N+2M)
+  // libs/libnlinv's variant (LBFGSOC / LBFGSOLD): per-parameter bounds
+  // (device arrays of nparam values), the first-step options and its
+  // line-search constants.
+  bool oc = false;
+  int nparam = 1;
+  double *pmin = nullptr, *pmax = nullptr;
+  int stp1_opt = 1;
+  double step_init = 999999.0;
   // LBFGS SAVE state
   int iter = 0, nfun = 0, point = 0, npt = 0, bound = 0, info = 0, nfev = 0, maxfev = 20, cp = 0;
   double stp = 0, stp1 = 0, ftol = 1e-4, gnorm = 0, xnorm = 0, ys = 0, yy = 0, diag = 1.0;
@@ -655,7 +675,10 @@ double ddot(sw_lbfgs &L, const double *a, const double *b) {
 }
 
 void freeze(sw_lbfgs &L, double *x) {
-  k_freeze<<<gsz(L.n), 256, 0, L.c->stream>>>(L.n, L.type, L.xmin, L.xmax, L.mask, L.xinit, x);
+  if (L.oc)
+    k_freeze_blocks<<<gsz(L.n), 256, 0, L.c->stream>>>(L.n, L.n / L.nparam, L.pmin, L.pmax, x);
+  else
+    k_freeze<<<gsz(L.n), 256, 0, L.c->stream>>>(L.n, L.type, L.xmin, L.xmax, L.mask, L.xinit, x);
   L.c->stats.launches_total++;
 }
 
@@ -750,7 +773,9 @@ void mcstep(double &stx, double &fx, double &dx, double &sty, double &fy, double
 
 // MCSRCH (lbfgs.f:652-982) with device vectors.
 void mcsrch(sw_lbfgs &L, double f, const double *s, double xtol) {
-  const double p5 = 0.5, p66 = 0.66, xtrapf = 4.0, zero = 0.0;
+  // XTRAPF is 4.0D1 in libinv's MCSRCH (lbfgs.f:792) and 4.0D0 in libnlinv's
+  // MCSRCHOC / MCSRCHOLD (nlinv_lbfgs.f:752,1773).
+  const double p5 = 0.5, p66 = 0.66, xtrapf = L.oc ? 4.0 : 40.0, zero = 0.0;
   cudaStream_t st = L.c->stream;
   if (L.info == -1) goto L45;
   L.infoc = 1;
@@ -825,7 +850,8 @@ L45:
 
 void free_lbfgs(sw_lbfgs *L) {
   for (void *q : {(void *)L->mask, (void *)L->xinit, (void *)L->S, (void *)L->Y, (void *)L->w0,
-                  (void *)L->wa, (void *)L->x, (void *)L->g, (void *)L->part, (void *)L->res})
+                  (void *)L->wa, (void *)L->x, (void *)L->g, (void *)L->part, (void *)L->res,
+                  (void *)L->pmin, (void *)L->pmax})
     if (q) cudaFree(q);
 }
 
@@ -909,7 +935,11 @@ L10:
   k_negmul<<<gsz(n), 256, 0, s>>>(n, L.g, L.diag, L.S);  // W(ISPT+I) = -G(I)*DIAG(I)
   c->stats.launches_total++;
   L.gnorm = std::sqrt(ddot(L, L.g, L.g));
-  {
+  if (L.oc) {
+    // nlinv_lbfgs.f:333-341 (LBFGSOLD, :1366-1370: step_init or 1/|g|).
+    L.stp1 = L.stp1_opt == 1 ? std::sqrt(ddot(L, L.x, L.x)) / L.gnorm / 100 : 1.0 / L.gnorm;
+    if (L.step_init != 999999.0) L.stp1 = L.step_init;
+  } else {
     const double xnorm2 = std::sqrt(ddot(L, L.x, L.x));
     L.stp1 = (L.boundt == 0) ? 1.0 / L.gnorm : xnorm2 / L.gnorm / 100;
   }
@@ -990,4 +1020,110 @@ L172:
     return SW_OK;
   }
   goto L80;
+}
+
+// One LBFGSOC / LBFGSOLD call (libs/libnlinv/nlinv_lbfgs.f:31-613,
+// 1066-1636): the saved state comes in from the caller's arrays, the
+// vectors run on the device, and the state goes back out in the
+// reference's layout.
+int sw_lbfgs_oc_step(sw_ctx *c, const sw_lbfgs_oc_desc *d, double *xh, double f,
+                     const double *gh, double *w, double *diag, sw_lbfgs_oc_state *st,
+                     int *iflag, int *myinfo) {
+  if (!c || !d || !xh || !gh || !w || !diag || !st || !iflag || !myinfo) return SW_BAD_PARAM;
+  if (d->n <= 0 || d->m <= 0 || d->nparam <= 0 || d->n % d->nparam != 0)
+    return fail(c, SW_BAD_PARAM, "L-BFGS: n=%d m=%d nparam=%d", d->n, d->m, d->nparam);
+  if (d->lbfgs_type == 1 && (!d->xmin || !d->xmax))
+    return fail(c, SW_BAD_PARAM, "L-BFGS: bounds missing");
+  cudaSetDevice(c->device);
+  const int n = d->n, m = d->m;
+  sw_lbfgs *L = new sw_lbfgs();
+  L->c = c;
+  L->n = n;
+  L->m = m;
+  L->oc = true;
+  L->nparam = d->nparam;
+  L->boundt = d->lbfgs_type == 1 ? d->bound_type : 0;
+  L->stp1_opt = d->lbfgs_type == 1 ? d->stp1_opt : 0;
+  L->step_init = d->step_init;
+  L->rho.assign(m + 1, 0.0);
+  L->alpha.assign(m + 1, 0.0);
+  const size_t nb = (size_t)n * sizeof(double);
+  const int np = d->nparam;
+  bool ok = cudaMalloc(&L->S, nb * m) == cudaSuccess && cudaMalloc(&L->Y, nb * m) == cudaSuccess &&
+            cudaMalloc(&L->w0, nb) == cudaSuccess && cudaMalloc(&L->wa, nb) == cudaSuccess &&
+            cudaMalloc(&L->x, nb) == cudaSuccess && cudaMalloc(&L->g, nb) == cudaSuccess &&
+            cudaMalloc(&L->part, kRedBlocks * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&L->res, sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&L->pmin, np * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&L->pmax, np * sizeof(double)) == cudaSuccess;
+  auto done = [&](int rc) {
+    cudaStreamSynchronize(c->stream);
+    free_lbfgs(L);
+    delete L;
+    return rc;
+  };
+  if (!ok) {
+    cudaGetLastError();
+    return done(fail(c, SW_OOM_ADMISSION, "L-BFGS state of n=%d m=%d does not fit", n, m));
+  }
+  cudaStream_t s = c->stream;
+  const std::vector<double> zeros(np, 0.0);
+  cudaMemcpyAsync(L->pmin, d->lbfgs_type == 1 ? d->xmin : zeros.data(), np * sizeof(double),
+                  cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(L->pmax, d->lbfgs_type == 1 ? d->xmax : zeros.data(), np * sizeof(double),
+                  cudaMemcpyHostToDevice, s);
+  // W: [0, n) the gradient / work vector, [n, n+m) rho, [n+m, n+2m) alpha,
+  // then the m search steps and the m gradient differences of n values.
+  const size_t ispt = (size_t)n + 2 * m, iypt = ispt + (size_t)n * m;
+  if (*iflag != 0) {
+    cudaMemcpyAsync(L->w0, w, nb, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(L->S, w + ispt, nb * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(L->Y, w + iypt, nb * m, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(L->wa, diag, nb, cudaMemcpyHostToDevice, s);
+    for (int q = 1; q <= m; ++q) {
+      L->rho[q] = w[n + q - 1];
+      L->alpha[q] = w[n + m + q - 1];
+    }
+    L->gnorm = st->gnorm; L->stp1 = st->stp1; L->ftol = st->ftol; L->stp = st->stp;
+    L->ys = st->ys; L->yy = st->yy; L->xnorm = st->xnorm;
+    L->iter = st->iter; L->nfun = st->nfun; L->point = st->point; L->maxfev = st->maxfev;
+    L->info = st->info; L->bound = st->bound; L->npt = st->npt; L->cp = st->cp;
+    L->nfev = st->nfev; L->finish = st->finish != 0;
+    L->infoc = st->infoc; L->brackt = st->brackt != 0; L->stage1 = st->stage1 != 0;
+    L->dg = st->dg; L->dgm = st->dgm; L->dginit = st->dginit; L->dgtest = st->dgtest;
+    L->dgx = st->dgx; L->dgxm = st->dgxm; L->dgy = st->dgy; L->dgym = st->dgym;
+    L->finit = st->finit; L->ftest1 = st->ftest1; L->fm = st->fm; L->fx = st->fx;
+    L->fxm = st->fxm; L->fy = st->fy; L->fym = st->fym; L->stx = st->stx; L->sty = st->sty;
+    L->stmin = st->stmin; L->stmax = st->stmax; L->width = st->width; L->width1 = st->width1;
+  } else {
+    cudaMemsetAsync(L->S, 0, nb * m, s);
+    cudaMemsetAsync(L->Y, 0, nb * m, s);
+  }
+  int rc = sw_lbfgs_step(L, xh, f, gh, d->eps, d->xtol, iflag, myinfo);
+  if (rc != SW_OK) return done(rc);
+  cudaMemcpyAsync(w, L->w0, nb, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(w + ispt, L->S, nb * m, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(w + iypt, L->Y, nb * m, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(diag, L->wa, nb, cudaMemcpyDeviceToHost, s);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return done(cuda_fail(c, e, "L-BFGS state"));
+  for (int q = 1; q <= m; ++q) {
+    w[n + q - 1] = L->rho[q];
+    w[n + m + q - 1] = L->alpha[q];
+  }
+  std::memset(st, 0, sizeof(*st));
+  st->gtol = kGTOL; st->one = 1.0; st->zero = 0.0; st->gnorm = L->gnorm; st->stp1 = L->stp1;
+  st->ftol = L->ftol; st->stpmin = kSTPMIN; st->stpmax = kSTPMAX; st->stp = L->stp;
+  st->ys = L->ys; st->yy = L->yy; st->xnorm = L->xnorm;
+  st->mp = 6; st->lp = 6; st->iter = L->iter; st->nfun = L->nfun; st->point = L->point;
+  st->ispt = (int)ispt; st->iypt = (int)iypt; st->maxfev = L->maxfev; st->info = L->info;
+  st->bound = L->bound; st->npt = L->npt; st->cp = L->cp; st->nfev = L->nfev;
+  st->finish = L->finish ? 1 : 0;
+  st->infoc = L->infoc; st->brackt = L->brackt ? 1 : 0; st->stage1 = L->stage1 ? 1 : 0;
+  st->dg = L->dg; st->dgm = L->dgm; st->dginit = L->dginit; st->dgtest = L->dgtest;
+  st->dgx = L->dgx; st->dgxm = L->dgxm; st->dgy = L->dgy; st->dgym = L->dgym;
+  st->finit = L->finit; st->ftest1 = L->ftest1; st->fm = L->fm; st->fx = L->fx;
+  st->fxm = L->fxm; st->fy = L->fy; st->fym = L->fym; st->stx = L->stx; st->sty = L->sty;
+  st->stmin = L->stmin; st->stmax = L->stmax; st->width = L->width; st->width1 = L->width1;
+  return done(SW_OK);
 }

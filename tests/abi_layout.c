@@ -62,6 +62,34 @@ int main(void) {
   F(sw_reg_state, eps); F(sw_reg_state, eps_log); F(sw_reg_state, mod_thresh);
   F(sw_reg_state, hin_thresh);
 
+  S(sw_lbfgs_oc_state);
+  F(sw_lbfgs_oc_state, gtol); F(sw_lbfgs_oc_state, one); F(sw_lbfgs_oc_state, zero);
+  F(sw_lbfgs_oc_state, gnorm); F(sw_lbfgs_oc_state, stp1); F(sw_lbfgs_oc_state, ftol);
+  F(sw_lbfgs_oc_state, stpmin); F(sw_lbfgs_oc_state, stpmax); F(sw_lbfgs_oc_state, stp);
+  F(sw_lbfgs_oc_state, ys); F(sw_lbfgs_oc_state, yy); F(sw_lbfgs_oc_state, sq);
+  F(sw_lbfgs_oc_state, yr); F(sw_lbfgs_oc_state, beta); F(sw_lbfgs_oc_state, xnorm);
+  F(sw_lbfgs_oc_state, mp); F(sw_lbfgs_oc_state, lp); F(sw_lbfgs_oc_state, iter);
+  F(sw_lbfgs_oc_state, nfun); F(sw_lbfgs_oc_state, point); F(sw_lbfgs_oc_state, ispt);
+  F(sw_lbfgs_oc_state, iypt); F(sw_lbfgs_oc_state, maxfev); F(sw_lbfgs_oc_state, info);
+  F(sw_lbfgs_oc_state, bound); F(sw_lbfgs_oc_state, npt); F(sw_lbfgs_oc_state, cp);
+  F(sw_lbfgs_oc_state, i); F(sw_lbfgs_oc_state, nfev); F(sw_lbfgs_oc_state, inmc);
+  F(sw_lbfgs_oc_state, iycn); F(sw_lbfgs_oc_state, iscn); F(sw_lbfgs_oc_state, finish);
+  F(sw_lbfgs_oc_state, infoc); F(sw_lbfgs_oc_state, j); F(sw_lbfgs_oc_state, brackt);
+  F(sw_lbfgs_oc_state, stage1); F(sw_lbfgs_oc_state, dg); F(sw_lbfgs_oc_state, dgm);
+  F(sw_lbfgs_oc_state, dginit); F(sw_lbfgs_oc_state, dgtest); F(sw_lbfgs_oc_state, dgx);
+  F(sw_lbfgs_oc_state, dgxm); F(sw_lbfgs_oc_state, dgy); F(sw_lbfgs_oc_state, dgym);
+  F(sw_lbfgs_oc_state, finit); F(sw_lbfgs_oc_state, ftest1); F(sw_lbfgs_oc_state, fm);
+  F(sw_lbfgs_oc_state, fx); F(sw_lbfgs_oc_state, fxm); F(sw_lbfgs_oc_state, fy);
+  F(sw_lbfgs_oc_state, fym); F(sw_lbfgs_oc_state, stx); F(sw_lbfgs_oc_state, sty);
+  F(sw_lbfgs_oc_state, stmin); F(sw_lbfgs_oc_state, stmax); F(sw_lbfgs_oc_state, width);
+  F(sw_lbfgs_oc_state, width1);
+
+  S(sw_lbfgs_oc_desc);
+  F(sw_lbfgs_oc_desc, n); F(sw_lbfgs_oc_desc, m); F(sw_lbfgs_oc_desc, nparam);
+  F(sw_lbfgs_oc_desc, xmin); F(sw_lbfgs_oc_desc, xmax); F(sw_lbfgs_oc_desc, lbfgs_type);
+  F(sw_lbfgs_oc_desc, bound_type); F(sw_lbfgs_oc_desc, stp1_opt); F(sw_lbfgs_oc_desc, step_init);
+  F(sw_lbfgs_oc_desc, eps); F(sw_lbfgs_oc_desc, xtol);
+
   S(sw_tuning);
   F(sw_tuning, step_kernel); F(sw_tuning, tile_z); F(sw_tuning, tile_x); F(sw_tuning, tile_y);
   F(sw_tuning, graph_chunk); F(sw_tuning, use_graph);

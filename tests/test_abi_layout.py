@@ -19,7 +19,8 @@ INC = os.path.join(ROOT, "include")
 CTYPES = {"sw_genpar": sw.SwGenpar, "sw_prop_desc": sw.SwPropDesc, "sw_prop_io": sw.SwPropIO,
           "sw_shot": sw.SwShot, "sw_window": sw.SwWindow, "sw_fwi_shot": sw.SwFwiShot,
           "sw_fwi_desc": sw.SwFwiDesc, "sw_reg_desc": sw.SwRegDesc,
-          "sw_reg_state": sw.SwRegState, "sw_tuning": sw.SwTuning, "sw_stats": sw.SwStats}
+          "sw_reg_state": sw.SwRegState, "sw_tuning": sw.SwTuning, "sw_stats": sw.SwStats,
+          "sw_lbfgs_oc_state": sw.SwLbfgsOcState, "sw_lbfgs_oc_desc": sw.SwLbfgsOcDesc}
 
 
 @pytest.fixture(scope="module")

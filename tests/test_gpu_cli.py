@@ -424,3 +424,88 @@ def test_afwi_program_task_inv(built, oracle, tmp_path, nrm):
     assert np.abs(rdm).max() > 1.0                    # the model moved
     assert rel_l2(dm, rdm) < 1e-5
     assert fun[-1] < fun[0]
+
+
+def _lbfgs_program_loop(built, oracle, tmp_path, lbfgs_type, nsteps=40):
+    """Drives L_BFGS.x as the reference's workflow does: write Model,
+    Function and Gradient, run the program in the state directory, rename
+    its *Out.dat files to the names it reads, evaluate at the model it wrote,
+    repeat.  The same loop on the oracle (state kept in memory, the model
+    rounded to FP32 between calls as the SEP files do)."""
+    import os
+    rng = np.random.default_rng(21)
+    n1, n2, n3 = 30, 20, 2                 # n3 < 5: a parameter axis (nparams = 2)
+    n = n1 * n2 * n3
+    t = np.concatenate([rng.uniform(1600.0, 2400.0, n // 2),
+                        rng.uniform(2100.0, 2500.0, n // 2)]).astype(np.float64)
+    a = rng.uniform(0.5, 2.0, n)
+    xmin, xmax = [1500.0, 2000.0], [2500.0, 2600.0]
+    x0 = np.full(n, 2000.0, np.float32)
+    run = tmp_path / "state"
+    run.mkdir()
+    shape = (n3, n2, n1)
+    sep.write(str(run / "init.H"), x0.reshape(shape))
+    sep.write(str(run / "mod.H"), x0.reshape(shape))
+    params = dict(Model=run / "mod.H", Function=run / "fct.H", Gradient=run / "grad.H",
+                  lbfgs_type=lbfgs_type, bound_type=1, stp1_opt=1)
+    if lbfgs_type == 1:
+        params.update(Initial_Model=run / "init.H", xmin=",".join(map(str, xmin)),
+                      xmax=",".join(map(str, xmax)))
+    models, flags = [], []
+    for _ in range(nsteps):
+        x, _ = sep.read(str(run / "mod.H"))
+        x = x.ravel().astype(np.float64)
+        r = x - t
+        sep.write(str(run / "fct.H"), np.array([0.5 * np.sum(a * r * r)], np.float32))
+        sep.write(str(run / "grad.H"), (a * r).astype(np.float32).reshape(shape))
+        res = subprocess.run(sep.command(built["L_BFGS.x"], **params), capture_output=True,
+                             text=True, timeout=300, cwd=run)
+        assert res.returncode == 0, res.stderr
+        for nm in ("Diag", "Iflag", "Info", "LbfgsDat", "McsrchDat", "WorkArray"):
+            os.replace(run / f"{nm}Out.dat", run / f"{nm}.dat")
+        iflag = int((run / "Iflag.dat").read_text().split()[0])
+        m, _ = sep.read(str(run / "mod.H"))
+        models.append(m.ravel().copy())
+        flags.append(iflag)
+        if iflag <= 0:
+            break
+    # The oracle over the same FP32 function / gradient / model round trips.
+    import seismic_gb300 as sw
+    d, keep = sw.lbfgs_oc_desc(n, 5, n3, xmin, xmax, lbfgs_type, 1, 1)
+    w = np.zeros(n * 11 + 10)
+    diag = np.zeros(n)
+    st = sw.SwLbfgsOcState()
+    iflag, rmodels, rflags = 0, [], []
+    x = x0.astype(np.float64)
+    for _ in range(len(models)):
+        r = x - t
+        f = float(np.float32(0.5 * np.sum(a * r * r)))
+        g = (a * r).astype(np.float32).astype(np.float64)
+        iflag, _ = oracle.lbfgs_oc_step(d, x, f, g, w, diag, st, iflag, 0)
+        x = x.astype(np.float32).astype(np.float64)
+        rmodels.append(x.astype(np.float32))
+        rflags.append(iflag)
+        if iflag <= 0:
+            break
+    return models, flags, rmodels, rflags, t
+
+
+@pytest.mark.parametrize("lbfgs_type", [1, 0])
+def test_lbfgs_program_multi_invocation(built, oracle, tmp_path, lbfgs_type):
+    """L_BFGS.x (progs/inversion/L_BFGS.f90) run once per function
+    evaluation with its state in the reference's files (Iflag, Info, Diag,
+    WorkArray, LbfgsDat, McsrchDat) against the oracle's LBFGSOC / LBFGSOLD
+    keeping the state in memory: the same iflag sequence, the same models
+    to FP32 rounding, the model approaching the minimum and, for
+    lbfgs_type 1, every model inside the per-parameter bounds."""
+    models, flags, rmodels, rflags, t = _lbfgs_program_loop(built, oracle, tmp_path, lbfgs_type)
+    assert flags == rflags and len(models) >= 10
+    for u, v in zip(models, rmodels):
+        assert np.abs(u - v).max() <= 1e-5 * np.abs(v).max()
+    first = np.abs(np.full_like(t, 2000.0) - t).max()
+    assert np.abs(models[-1] - t).max() < 0.05 * first
+    if lbfgs_type == 1:
+        half = t.size // 2
+        for m in models:
+            assert m[:half].min() >= 1500.0 and m[:half].max() <= 2500.0
+            assert m[half:].min() >= 2000.0 and m[half:].max() <= 2600.0

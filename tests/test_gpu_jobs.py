@@ -407,3 +407,30 @@ def test_rtm_job_3d_window_bitexact(ctx, oracle):
     assert np.abs(rim).max() > 0
     np.testing.assert_array_equal(im, rim)
     np.testing.assert_array_equal(il, ril)
+
+
+@pytest.mark.parametrize("lbfgs_type,bound_type", [(1, 1), (1, 2), (0, 1)])
+def test_lbfgs_oc_device_matches_oracle(ctx, oracle, lbfgs_type, bound_type):
+    """The out-of-core L-BFGS (LBFGSOC / LBFGSOLD, nlinv_lbfgs.f) on the
+    device against the oracle, each call starting from the state the
+    previous call returned (as L_BFGS.x does through its files): the same
+    number of calls and iterations, iterates equal to 1e-9 relative (FP64
+    dot products summed in another order)."""
+    from tests.test_oracle_lbfgs import _oc_run
+    rng = np.random.default_rng(12)
+    n, nparam = 2000, 2
+    t = np.concatenate([rng.uniform(1600.0, 2400.0, n // 2), rng.uniform(2100.0, 2500.0, n // 2)])
+    a = rng.uniform(0.5, 2.0, n)
+    xmin, xmax = np.array([1500.0, 2000.0]), np.array([2500.0, 2600.0])
+
+    def dev(d, x, f, g, w, diag, st, iflag, myinfo):
+        return ctx.lbfgs_oc_step(d, x, f, g, w, diag, st, iflag, myinfo)
+
+    rx, rfs, rxs, rtrial, rfl = _oc_run(oracle.lbfgs_oc_step, n, nparam, t, a, xmin, xmax,
+                                        lbfgs_type, bound_type, 1, max_calls=60)
+    x, fs, xs, trial, fl = _oc_run(dev, n, nparam, t, a, xmin, xmax, lbfgs_type, bound_type, 1,
+                                   max_calls=60)
+    assert len(trial) == len(rtrial) and len(xs) == len(rxs) >= 5 and fl == rfl
+    for u, v in zip(trial, rtrial):
+        assert np.abs(u - v).max() <= 1e-9 * np.abs(v).max()
+    assert rel_l2(fs, rfs) < 1e-9
