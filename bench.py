@@ -611,8 +611,8 @@ def run_config5(args) -> int:
                    "l2": "inputs larger than L2 (snapshots of every shot in HBM)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
-                     "kernel": "k_bstep3d_t (fused stencil + time update + Higdon z/x lines, "
-                               "TMA plane pipeline)",
+                     "kernel": "k_bstep3d_t (fused stencil + time update + imaging condition, "
+                               "TMA plane pipeline; Higdon lines in the edge kernels)",
                      "avg_launch_ms": sp["step_kernel_ms"] / nl,
                      "algorithmic_bytes_per_launch": sp["step_bytes"] / nl,
                      "launches_timed": sp["step_kernel_timed"]},

@@ -409,13 +409,18 @@ def test_rtm_job_3d_window_bitexact(ctx, oracle):
     np.testing.assert_array_equal(il, ril)
 
 
+def _oc_misfit(x, t, a):
+    r = x - t
+    return float(0.5 * np.sum(a * r * r))
+
+
 @pytest.mark.parametrize("lbfgs_type,bound_type", [(1, 1), (1, 2), (0, 1)])
 def test_lbfgs_oc_device_matches_oracle(ctx, oracle, lbfgs_type, bound_type):
     """The out-of-core L-BFGS (LBFGSOC / LBFGSOLD, nlinv_lbfgs.f) on the
     device against the oracle, each call starting from the state the
-    previous call returned (as L_BFGS.x does through its files): the same
-    number of calls and iterations, iterates equal to 1e-9 relative (FP64
-    dot products summed in another order)."""
+    previous call returned (as L_BFGS.x does through its files): trial
+    models and iterates equal to 1e-9 relative (FP64 dot products summed in
+    another order) down to rounding level, and both runs converged."""
     from tests.test_oracle_lbfgs import _oc_run
     rng = np.random.default_rng(12)
     n, nparam = 2000, 2
@@ -430,7 +435,16 @@ def test_lbfgs_oc_device_matches_oracle(ctx, oracle, lbfgs_type, bound_type):
                                         lbfgs_type, bound_type, 1, max_calls=60)
     x, fs, xs, trial, fl = _oc_run(dev, n, nparam, t, a, xmin, xmax, lbfgs_type, bound_type, 1,
                                    max_calls=60)
-    assert len(trial) == len(rtrial) and len(xs) == len(rxs) >= 5 and fl == rfl
-    for u, v in zip(trial, rtrial):
-        assert np.abs(u - v).max() <= 1e-9 * np.abs(v).max()
-    assert rel_l2(fs, rfs) < 1e-9
+    # Both runs drive the misfit from 1e8 to rounding level (1e-20 and
+    # below, where the last iterations' line searches act on differences
+    # of a few ulps); there the number of calls depends on summation
+    # order, so the trajectories are compared while the misfit is above
+    # 1e-12 of its start, and both must end converged.
+    f0 = _oc_misfit(rtrial[0], t, a)
+    keep = [i for i, v in enumerate(rtrial) if _oc_misfit(v, t, a) > 1e-12 * f0]
+    assert len(keep) >= 5 and len(trial) > keep[-1] and fl == rfl == 0
+    for i in keep:
+        assert np.abs(trial[i] - rtrial[i]).max() <= 1e-9 * np.abs(rtrial[i]).max()
+    nk = sum(1 for v in rfs if v > 1e-12 * f0)
+    assert nk >= 5 and rel_l2(fs[:nk], rfs[:nk]) < 1e-9
+    assert _oc_misfit(x, t, a) < 1e-12 * f0 and _oc_misfit(rx, t, a) < 1e-12 * f0
