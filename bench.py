@@ -243,14 +243,15 @@ def run_reference(args):
     return 0
 
 
-def workload_config(args, batch):
+def workload_config(args, batch, shots_per_batch=None):
     surf = bool(getattr(args, "surf", False))
     return {"workload": "batched 2D shot RTM with illumination-normalised stacking" +
                         (", free surface and mirror receivers" if surf else ""),
             "surf_type": 1 if surf else 0, "rec_type": 1 if surf else 0,
             "grid": [NZ, NX], "spacing_m": D, "dt_s": DT, "ntaper": NTAPER, "snapi": SNAPI,
             "record_s": [3.0, 4.0], "aperture_m": [3000, 6000], "shot_spacing_m": SPACING,
-            "survey_shots": NSHOT_SURVEY, "shots_per_step": batch, "ricker_hz": F0,
+            "survey_shots": NSHOT_SURVEY, "shots_per_step": batch,
+            "shots_per_batch": shots_per_batch, "ricker_hz": F0,
             "l2": "inputs larger than L2 (snapshots of every shot in HBM)",
             "bytes_per_point": BYTES_PER_POINT}
 
@@ -261,7 +262,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--shots-per-step", type=int, default=16)
+    ap.add_argument("--shots-per-step", type=int, default=0,
+                    help="shots per bench step (0: chosen by the autotuner)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner: default launch shape, 16 shots per step unless "
+                         "--shots-per-step says otherwise")
     ap.add_argument("--cpu-steps", type=int, default=0,
                     help="time samples of the CPU sample shot (0: its whole record)")
     ap.add_argument("--nt-cap", type=int, default=0, help="truncate records (debug)")
@@ -279,6 +284,16 @@ def main():
     ap.add_argument("--revolve-study", action="store_true",
                     help="FWI gradient memory modes on the 1201 x 3401 grid: store-all against "
                          "binomial checkpointing with 32/64/128 state slots")
+    ap.add_argument("--cnn-bench", action="store_true",
+                    help="time the preconditioner network's tensor-core kernels at 601 x 1801")
+    ap.add_argument("--config4-study", action="store_true",
+                    help="learned vs plain multiscale FWI on 601 x 1801 models (80 shots, "
+                         "3/6/9 Hz) instead of the RTM bench")
+    ap.add_argument("--c4-train", type=int, default=16, help="training models (301 x 901)")
+    ap.add_argument("--c4-train-shots", type=int, default=20, help="shots per training model")
+    ap.add_argument("--c4-evals", type=int, default=15, help="evaluations per stage (test)")
+    ap.add_argument("--c4-train-evals", type=int, default=10,
+                    help="evaluations per stage (training runs)")
     ap.add_argument("--no-graph", action="store_true",
                     help="launch every time step directly (profiling runs: every launch timed)")
     args = ap.parse_args()
@@ -286,6 +301,10 @@ def main():
         return run_reference(args)
     if args.precond_study:
         return run_precond_study()
+    if args.config4_study:
+        return run_config4_study(args)
+    if args.cnn_bench:
+        return run_cnn_bench(args)
     if args.model3d:
         return run_model3d(args)
     if args.revolve_study:
@@ -307,11 +326,23 @@ def main():
     g, vel, w, shots = make_workload(args.nt_cap or None)
     if args.surf:
         g.surf_type, g.rec_type = 1, 1
-    B = args.shots_per_step
-    nsteps = args.warmup + args.steps
     # Shots of this rank: rank r takes every ws-th shot of the survey.
     from seismic_gb300 import dist as sdist
     mine = [shots[i] for i in sdist.shard(len(shots), rank, ws)]
+    # Shots per step and launch shape: the autotuner (batch candidates
+    # capped by what HBM admits at full record length, timed on truncated
+    # records; then the launch shape at that batch), untimed.
+    tune = None
+    if not args.no_tune:
+        from seismic_gb300 import autotune
+        t0 = time.perf_counter()
+        tune = autotune.tune_survey(ctx, g, vel, w, mine, steps=64)
+        tune["tune_s"] = time.perf_counter() - t0
+        if args.no_graph:
+            ctx.set_tuning(use_graph=0)
+        log(f"[rank {rank}] autotune: {tune}")
+    B = args.shots_per_step or (tune["batch"] if tune else 16)
+    nsteps = args.warmup + args.steps
     per_step = [mine[(k * B + q) % len(mine)] for k in range(nsteps) for q in range(B)]
     # Observed data: batched forward modelling on each shot's window (untimed).
     distinct = {}
@@ -441,7 +472,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded faulted layered model, data modelled by the engine)",
-            "config": workload_config(args, last_batch),
+            "config": workload_config(args, B, last_batch),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "peak_kind": peak_kind, "kernel": "k_bstep2d_t (fused stencil + time update, pipelined 2D tiles)",
@@ -451,6 +482,7 @@ def main():
             "cpu_baseline": cpu, "parity": parity, "e2e": e2e_line, "clocks": clk,
             "gpu_launches": launches_timed_region,
             "timed_event_ms": ev_ms,
+            "autotune": tune,
         }
         print(json.dumps(line), flush=True)
     job.close()
@@ -703,6 +735,98 @@ def run_precond_study() -> int:
         row.pop("learned_curve")
     print(json.dumps({"study": "learned vs plain L-BFGS FWI", **r}), flush=True)
     ctx.close()
+    return 0
+
+
+def run_config4_study(args) -> int:
+    """Learned-preconditioned vs plain L-BFGS multiscale FWI at the 601 x 1801
+    benchmark size (80 shots, 3/6/9 Hz stages), the network trained on plain
+    runs over --c4-train seeded 301 x 901 models; one JSON line."""
+    import seismic_gb300 as sw
+    from seismic_gb300 import precond
+    ctx = sw.Context(0)
+    r = precond.run_config4_study(ctx, n_train=args.c4_train, train_nshot=args.c4_train_shots,
+                                  evals_per_stage=args.c4_evals,
+                                  train_evals_per_stage=args.c4_train_evals,
+                                  learned_kw={"max_learned": 3, "c1": 0.1}, log=log)
+    print(json.dumps({"study": "learned vs plain L-BFGS multiscale FWI", **r}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_cnn_bench(args) -> int:
+    """The preconditioner network at the FWI benchmark's test size (601 x 1801
+    image, 2 -> 32 -> 32 -> 32 -> 1 channels): inference and gradient passes
+    per second through the public API, and the event-timed roofline of the
+    tensor-core convolution and weight-gradient kernels (algorithmic bytes:
+    BF16 activations read once, outputs written once; FLOPs of the real
+    channels).  One JSON line."""
+    import torch
+
+    import seismic_gb300 as sw
+    torch.cuda.set_device(0)
+    ctx = sw.Context(0)
+    nz, nx, ch = 601, 1801, (2, 32, 32, 32, 1)
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((1, 2, nx, nz)).astype(np.float32)
+    t = rng.standard_normal((1, nx, nz)).astype(np.float32)
+    net = sw.CNN(ctx, ch, seed=0)
+    for _ in range(max(args.warmup, 1)):
+        net.forward(x[0])
+        net.gradient(x, t)
+    reps = max(args.steps, 1)
+    ctx.reset_stats()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.forward(x[0])
+    t_fwd = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        net.gradient(x, t)
+    t_grad = (time.perf_counter() - t0) / reps
+    clk = clocks.stop()
+    launches = int(ctx.stats()["launches_total"])
+    # Roofline pass: one gradient call with every tensor-core launch timed.
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    net.gradient(x, t)
+    ctx.set_profiling(False)
+    st = ctx.stats()
+    net.close()
+    ctx.close()
+    peak, peak_kind = measured_peak()
+    tf_peak = None
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        tf_peak = mp.get("bf16_tflops")
+    except Exception:
+        pass
+    secs = st["cnn_conv_ms"] / 1e3
+    gbs = st["cnn_conv_bytes"] / secs / 1e9 if secs > 0 else None
+    tfs = st["cnn_conv_flops"] / secs / 1e12 if secs > 0 else None
+    line = {
+        "metric": "cnn_gradient_passes_per_s", "value": 1.0 / t_grad, "unit": "passes/s",
+        "n_gpus": 1, "steps": reps, "warmup": args.warmup, "ms_per_step": t_grad * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded normal inputs and targets)",
+        "config": {"workload": "preconditioner network forward + backward on one image",
+                   "image": [nz, nx], "channels": list(ch),
+                   "l2": "activations (69 MB per 32-channel tensor) mostly L2-resident"},
+        "forward_ms": t_fwd * 1e3,
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                     "frac": gbs / peak if gbs else None, "peak_kind": peak_kind,
+                     "tensor_tflops": tfs, "tensor_peak_tflops": tf_peak,
+                     "tensor_frac": (tfs / tf_peak) if (tfs and tf_peak) else None,
+                     "kernel": "k_conv_tma + k_wgrad_umma (tcgen05, TMA-fed)",
+                     "launches_timed": st["cnn_conv_timed"],
+                     "avg_launch_ms": st["cnn_conv_ms"] / max(1, st["cnn_conv_timed"]),
+                     "algorithmic_bytes": st["cnn_conv_bytes"],
+                     "flops": st["cnn_conv_flops"]},
+        "clocks": clk, "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
     return 0
 
 

@@ -259,6 +259,14 @@ int sw_rtm_job_run(sw_rtm_job *job, int first, int count);
  * data[q] receives the nrec*nt traces of shot first+q.  Shots may have been
  * created without observed data (sw_shot.data = NULL). */
 int sw_rtm_job_model(sw_rtm_job *job, int first, int count, float *const *data);
+/* How many shots from shot `first` the admission above puts in one batch
+ * now (the job's max_shots and mem_fraction, the device memory free at the
+ * call, the job's arena counted as free), for an RTM run (modeling = 0:
+ * snapshots of every shot) or a modelling run (modeling = 1: traces).
+ * Host only.  SW_OOM_ADMISSION, with *count = 0, when shot `first` alone
+ * does not fit.  No counterpart in the reference (its shot loop holds one
+ * shot per thread). */
+int sw_rtm_job_admit(sw_rtm_job *job, int first, int modeling, int *count);
 /* Shots per batch used by the last run, and compute-domain point updates. */
 int sw_rtm_job_info(const sw_rtm_job *job, int *last_batch, uint64_t *points);
 /* image, illum: stacked nz*nx*ny sums; image_norm: image divided by the
@@ -477,12 +485,13 @@ int sw_ctx_get_tuning(const sw_ctx *ctx, sw_tuning *t);
 
 /* ---- Convolutional gradient preconditioner (N4) --------------------------- */
 /* No counterpart in the reference.  A stack of nlayers 3x3 convolutions
- * (zero padding, ReLU between layers, channels[0..nlayers], each 1..16,
+ * (zero padding, ReLU between layers, channels[0..nlayers], each 1..32,
  * the last 1) mapping planar FP32 input channels of an nz x nx image
- * (z fastest) to one output channel.  BF16 weights and activations on the
- * tcgen05 tensor cores with FP32 accumulation; FP32 master weights and
- * Adam state.  Weights are packed per layer as w[co][tap][ci] (tap =
- * 3 * (dx + 1) + (dz + 1)) followed by b[co]. */
+ * (z fastest) to one output channel.  BF16 weights, activations and
+ * back-propagated gradients on the tcgen05 tensor cores (convolutions,
+ * input gradients and weight gradients) with FP32 accumulation; FP32
+ * master weights and Adam state.  Weights are packed per layer as
+ * w[co][tap][ci] (tap = 3 * (dx + 1) + (dz + 1)) followed by b[co]. */
 typedef struct sw_cnn sw_cnn;
 int sw_cnn_create(sw_ctx *ctx, int nlayers, const int *channels, uint64_t seed, sw_cnn **out);
 int sw_cnn_destroy(sw_cnn *net);
@@ -491,6 +500,12 @@ int sw_cnn_get_weights(const sw_cnn *net, float *w);
 int sw_cnn_set_weights(sw_cnn *net, const float *w);
 /* in: channels[0] x nz x nx (planar), out: nz x nx. */
 int sw_cnn_forward(sw_cnn *net, int nz, int nx, const float *in, float *out);
+/* grad (sw_cnn_num_weights values, packed like the weights) receives the
+ * gradient of the mean over nbatch images of 0.5 * mean((out - target)^2)
+ * and *loss that mean loss; the weights do not change.  in: nbatch x
+ * channels[0] x nz x nx, target: nbatch x nz x nx. */
+int sw_cnn_gradient(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
+                    const float *target, float *grad, double *loss);
 /* One Adam step (lr; beta 0.9 / 0.999) on the mean over nbatch images of
  * 0.5 * mean((out - target)^2); *loss receives that mean loss. */
 int sw_cnn_train_step(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
@@ -531,6 +546,14 @@ typedef struct sw_stats {
   uint64_t steps_forward;       /* time steps of forward (tstep = +1) runs    */
   uint64_t steps_backward;      /* time steps of backward (tstep = -1) runs   */
   uint64_t ckpt_advances;       /* checkpoint-segment advances of FWI runs    */
+  double   cnn_conv_ms;         /* event-timed total of the preconditioner's
+                                   tensor-core convolution and weight-gradient
+                                   kernels (only while profiling is on)      */
+  uint64_t cnn_conv_timed;      /* number of those timed launches            */
+  uint64_t cnn_conv_bytes;      /* their algorithmic HBM bytes (activations
+                                   and gradients read once, outputs written)  */
+  uint64_t cnn_conv_flops;      /* their tensor-core FLOPs (2 x M x N x K of
+                                   the real channels)                        */
 } sw_stats;
 int sw_ctx_get_stats(const sw_ctx *ctx, sw_stats *out);
 int sw_ctx_reset_stats(sw_ctx *ctx);

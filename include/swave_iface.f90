@@ -168,6 +168,10 @@ module swave_iface
      integer(c_int64_t) :: steps_forward
      integer(c_int64_t) :: steps_backward
      integer(c_int64_t) :: ckpt_advances
+     real(c_double)     :: cnn_conv_ms
+     integer(c_int64_t) :: cnn_conv_timed
+     integer(c_int64_t) :: cnn_conv_bytes
+     integer(c_int64_t) :: cnn_conv_flops
   end type sw_stats
 
   interface
@@ -293,6 +297,13 @@ module swave_iface
        type(c_ptr), value    :: job
        integer(c_int), value :: first, count
        type(c_ptr)           :: dat(*)        ! c_loc of each shot's nrec*nt traces
+     end function
+     integer(c_int) function sw_rtm_job_admit(job, first, modeling, count) &
+          bind(C, name="sw_rtm_job_admit")
+       import :: c_int, c_ptr
+       type(c_ptr), value    :: job
+       integer(c_int), value :: first, modeling
+       integer(c_int)        :: count
      end function
      integer(c_int) function sw_rtm_job_info(job, last_batch, points) &
           bind(C, name="sw_rtm_job_info")
@@ -449,6 +460,14 @@ module swave_iface
        type(c_ptr), value    :: net
        integer(c_int), value :: nz, nx
        real(c_float)         :: in(*), out(*)
+     end function
+     integer(c_int) function sw_cnn_gradient(net, nbatch, nz, nx, in, target, grad, loss) &
+          bind(C, name="sw_cnn_gradient")
+       import :: c_int, c_ptr, c_float, c_double
+       type(c_ptr), value    :: net
+       integer(c_int), value :: nbatch, nz, nx
+       real(c_float)         :: in(*), target(*), grad(*)
+       real(c_double)        :: loss
      end function
      integer(c_int) function sw_cnn_train_step(net, nbatch, nz, nx, in, target, lr, loss) &
           bind(C, name="sw_cnn_train_step")

@@ -155,7 +155,9 @@ class SwStats(C.Structure):
                 ("points_updated", C.c_uint64), ("step_kernel_ms", C.c_double),
                 ("step_kernel_timed", C.c_uint64), ("step_bytes", C.c_uint64),
                 ("steps_forward", C.c_uint64), ("steps_backward", C.c_uint64),
-                ("ckpt_advances", C.c_uint64)]
+                ("ckpt_advances", C.c_uint64), ("cnn_conv_ms", C.c_double),
+                ("cnn_conv_timed", C.c_uint64), ("cnn_conv_bytes", C.c_uint64),
+                ("cnn_conv_flops", C.c_uint64)]
 
 
 # Every symbol of include/swave.h with its signature.
@@ -177,6 +179,8 @@ _SIGS = {
     "sw_cnn_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _fp, _fp]),
     "sw_cnn_train_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, C.c_float,
                                     C.POINTER(C.c_double)]),
+    "sw_cnn_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp,
+                                  C.POINTER(C.c_double)]),
     "sw_rtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
     "sw_born": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
     "sw_lsrtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
@@ -199,6 +203,7 @@ _SIGS = {
     "sw_rtm_job_set_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
     "sw_rtm_job_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "sw_rtm_job_model": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(_fp)]),
+    "sw_rtm_job_admit": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sw_rtm_job_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     "sw_rtm_job_result": (C.c_int, [C.c_void_p, _fp, _fp, _fp]),
     "sw_rtm_job_reset": (C.c_int, [C.c_void_p]),
@@ -520,6 +525,12 @@ class RTMJob:
         count = self.nshot - first if count is None else count
         self.ctx._check(self.ctx.lib.sw_rtm_job_run(self.h, first, count))
 
+    def admit(self, first: int = 0, modeling: bool = False) -> int:
+        """Shots from `first` that one batch takes now (sw_rtm_job_admit)."""
+        n = C.c_int()
+        self.ctx._check(self.ctx.lib.sw_rtm_job_admit(self.h, first, int(modeling), C.byref(n)))
+        return n.value
+
     def info(self) -> tuple[int, int]:
         b, p = C.c_int(), C.c_uint64()
         self.ctx._check(self.ctx.lib.sw_rtm_job_info(self.h, C.byref(b), C.byref(p)))
@@ -676,6 +687,17 @@ class CNN:
         out = np.zeros((nx, nz), np.float32)
         self.ctx._check(self.ctx.lib.sw_cnn_forward(self.h, nz, nx, fptr(x), fptr(out)))
         return out
+
+    def gradient(self, x, target) -> tuple[np.ndarray, float]:
+        """Gradient of the batch-mean loss (packed like the weights) and that
+        loss; x: (batch, channels[0], nx, nz), target: (batch, nx, nz)."""
+        x, t = _f32(x), _f32(target)
+        b, c, nx, nz = x.shape
+        g = np.zeros(self.num_weights, np.float32)
+        loss = C.c_double()
+        self.ctx._check(self.ctx.lib.sw_cnn_gradient(self.h, b, nz, nx, fptr(x), fptr(t), fptr(g),
+                                                     C.byref(loss)))
+        return g, loss.value
 
     def train_step(self, x, target, lr: float = 1e-3) -> float:
         """x: (batch, channels[0], nx, nz); target: (batch, nx, nz)."""

@@ -216,5 +216,52 @@ def tune_rtm(ctx, model, vel, wavelet, shots, steps: int = 48, batch: int | str 
     return dict(entry, batch=batch) if chosen else entry
 
 
+def tune_survey(ctx, model, vel, wavelet, shots, steps: int = 64, mem_fraction: float = 0.85,
+                cache_path: str | None = DEFAULT_CACHE, device_name: str | None = None,
+                force: bool = False) -> dict:
+    """Shots per launch and launch shape for the RTM of a whole survey.
+
+    `shots` carry "sou", "rec" and "nt" (full record length); "data" is not
+    needed.  The batch candidates are capped by what one batch of the
+    survey's full-length records admits in device memory now
+    (sw_rtm_job_admit with max_shots 64), and that cap is a candidate
+    itself; each candidate is timed on the first shots' truncated records
+    modelled by the engine (`steps` samples), then the launch shape is tuned
+    at the chosen batch (tune_rtm).  Applies the winning launch shape to
+    ctx and returns {"batch", "admit_cap", "tuning", "batch_seconds",
+    "seconds", "tried", "steps"}."""
+    import numpy as np
+
+    import seismic_gb300 as sw
+    g = sw.SwGenpar.from_buffer_copy(model)
+    full = sw.RTMJob(ctx, g, vel, wavelet, [{"sou": s["sou"], "rec": s["rec"], "nt": s["nt"]}
+                                            for s in shots])
+    try:
+        full.set_batch(max(BATCH_CANDIDATES), mem_fraction)
+        cap = full.admit(0)
+    finally:
+        full.close()
+    cands = sorted({b for b in BATCH_CANDIDATES if b <= cap} | {min(cap, len(shots))})
+    nsample = max(cands)
+    gs = sw.SwGenpar.from_buffer_copy(model)
+    gs.nt = steps
+    first = [shots[i % len(shots)] for i in range(nsample)]
+    mj = sw.RTMJob(ctx, gs, vel, np.ascontiguousarray(wavelet[:steps]),
+                   [{"sou": s["sou"], "rec": s["rec"], "nt": steps} for s in first])
+    try:
+        mj.set_batch(nsample)
+        data = mj.model()
+    finally:
+        mj.close()
+    sample = [{"sou": s["sou"], "rec": s["rec"], "data": d} for s, d in zip(first, data)]
+    b = tune_batch(ctx, gs, vel, wavelet, sample, steps=steps, cands=cands,
+                   cache_path=cache_path, device_name=device_name, force=force)
+    t = tune_rtm(ctx, gs, vel, wavelet, sample, steps=steps, batch=b["batch"],
+                 cache_path=cache_path, device_name=device_name, force=force)
+    return {"batch": b["batch"], "admit_cap": cap, "tuning": t["tuning"],
+            "batch_seconds": b["seconds"], "seconds": t["seconds"], "tried": t["tried"],
+            "steps": steps}
+
+
 def ctx_device(ctx) -> int:
     return 0

@@ -5,6 +5,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/swave.h"
 #include "swave_dev.cuh"
 
@@ -111,6 +113,8 @@ int fail(sw_ctx *c, int code, const char *fmt, ...);
       return ::swave::cuda_fail(c, sw_e_, #call " @ " __FILE__ ":" SW_STR(__LINE__)); \
   } while (0)
 int cuda_fail(sw_ctx *c, cudaError_t e, const char *what);
+// cuTensorMapEncodeTiled from the driver (null when it is missing).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 // Grow-only named device buffer of the context; a growth allocates
 // bytes + slack.
 void *dbuf(sw_ctx *c, const std::string &name, size_t bytes, int *st, size_t slack = 0);

@@ -321,6 +321,59 @@ struct ShotBufs {
   float *vpad, *vsmall, *image, *illum, *wave, *traces;
 };
 
+// Arena bytes of one shot of a batch: padded velocity, windowed velocity,
+// image, illumination, snapshots (RTM) or traces (modelling).
+size_t shot_arena_bytes(const sw_genpar &g, int nrec, bool modeling) {
+  const Geom G = make_geom(g);
+  const size_t nw = (size_t)g.nz * g.nx * g.ny;
+  const size_t ntsnap = modeling ? 0 : (size_t)std::max(1, g.nt / g.snapi);
+  size_t t = ((size_t)G.total() * 4 + 255) / 256 * 256;        // vel_pad
+  t += (nw * 4 + 255) / 256 * 256 * 3;                          // vsmall, image, illum
+  t += (nw * ntsnap * 4 + 255) / 256 * 256;                     // snapshots
+  t += ((size_t)nrec * g.nt * 4 + 255) / 256 * 256;             // traces
+  return t;
+}
+
+// The admission budget: mem_fraction of the free device memory, the job
+// arena already held counted as free.
+int admission_budget(sw_rtm_job *j, double *budget) {
+  sw_ctx *c = j->c;
+  size_t freeb = 0, totalb = 0;
+  SW_CK(cudaMemGetInfo(&freeb, &totalb));
+  size_t held = 0;
+  auto it = c->bufs.find("rtm_arena");
+  if (it != c->bufs.end()) held = it->second.cap;
+  *budget = (double)(freeb + held) * j->mem_fraction;
+  return SW_OK;
+}
+
+// Shots [next, end) admitted into one batch: at most max_batch, and within
+// the budget once the first is in.  Each shot also needs the fields and
+// plans of run_phases (7 padded grids).  Returns the count; *first_bytes
+// is the first shot's need (the caller fails when it alone exceeds the
+// budget).
+int admit_shots(const sw_rtm_job *j, int next, int end, bool modeling, double budget,
+                size_t *first_bytes) {
+  const sw_genpar &M = j->g;
+  size_t need = 0;
+  int n = 0;
+  *first_bytes = 0;
+  while (next + n < end && n < j->max_batch) {
+    const auto &S = j->shots[next + n];
+    const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
+    const size_t bsz = shot_arena_bytes(g, modeling ? S.s.nrec : 0, modeling) +
+                       (size_t)make_geom(g).total() * 4 * 7;
+    if (n == 0) *first_bytes = bsz;
+    if ((double)(need + bsz) > budget) {
+      if (n == 0) return 0;
+      break;
+    }
+    need += bsz;
+    ++n;
+  }
+  return n;
+}
+
 // Admits shots [next, end) into a batch by HBM footprint, carves their
 // buffers from one arena, windows and pads their velocity.  `modeling`
 // batches need trace buffers and no snapshots.
@@ -332,34 +385,20 @@ int prepare_batch(sw_rtm_job *j, int &next, int end, bool modeling, std::vector<
   int st = SW_OK;
   const sw_genpar &M = j->g;
   auto need_of = [&](const sw_genpar &g, int nrec) -> size_t {
-    const Geom G = make_geom(g);
-    const size_t nw = (size_t)g.nz * g.nx * g.ny;
-    const size_t ntsnap = modeling ? 0 : (size_t)std::max(1, g.nt / g.snapi);
-    size_t t = ((size_t)G.total() * 4 + 255) / 256 * 256;        // vel_pad
-    t += (nw * 4 + 255) / 256 * 256 * 3;                          // vsmall, image, illum
-    t += (nw * ntsnap * 4 + 255) / 256 * 256;                     // snapshots
-    t += ((size_t)nrec * g.nt * 4 + 255) / 256 * 256;             // traces
-    return t;
+    return shot_arena_bytes(g, nrec, modeling);
   };
-  size_t freeb = 0, totalb = 0;
-  SW_CK(cudaMemGetInfo(&freeb, &totalb));
   size_t held = 0;
   auto it = c->bufs.find("rtm_arena");
   if (it != c->bufs.end()) held = it->second.cap;
-  // The fields and plans of run_phases need (7 padded grids per shot).
-  const double budget = (double)(freeb + held) * j->mem_fraction;
+  double budget = 0.0;
+  if ((st = admission_budget(j, &budget))) return st;
   batch.clear();
-  size_t need = 0;
-  while (next < end && (int)batch.size() < j->max_batch) {
-    const auto &S = j->shots[next];
-    const sw_genpar g = shot_genpar(M, S.w, S.s.nt);
-    const size_t bsz = need_of(g, modeling ? S.s.nrec : 0) + (size_t)make_geom(g).total() * 4 * 7;
-    if (!batch.empty() && (double)(need + bsz) > budget) break;
-    if (batch.empty() && (double)bsz > budget)
-      return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, bsz, budget);
-    need += bsz;
-    batch.push_back(next++);
-  }
+  size_t first_bytes = 0;
+  const int nadm = admit_shots(j, next, end, modeling, budget, &first_bytes);
+  if (next < end && nadm == 0)
+    return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, first_bytes,
+                budget);
+  for (int q = 0; q < nadm; ++q) batch.push_back(next++);
   j->last_batch = (int)batch.size();
   std::vector<size_t> offs;
   size_t total = 0;
@@ -452,6 +491,20 @@ PhaseShot forward_phase(sw_rtm_job *j, const sw_rtm_job::Shot &S, const ShotBufs
 }
 
 }  // namespace
+
+int sw_rtm_job_admit(sw_rtm_job *j, int first, int modeling, int *count) {
+  if (!j || !count || first < 0 || first >= (int)j->shots.size()) return SW_BAD_PARAM;
+  cudaSetDevice(j->c->device);
+  double budget = 0.0;
+  int st = admission_budget(j, &budget);
+  if (st) return st;
+  size_t first_bytes = 0;
+  *count = admit_shots(j, first, (int)j->shots.size(), modeling != 0, budget, &first_bytes);
+  if (*count == 0)
+    return fail(j->c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", first,
+                first_bytes, budget);
+  return SW_OK;
+}
 
 int sw_rtm_job_run(sw_rtm_job *j, int first, int count) {
   if (!j || first < 0 || count < 1 || first + count > (int)j->shots.size()) return SW_BAD_PARAM;

@@ -17,8 +17,6 @@
 
 namespace swave {
 
-namespace {
-
 // cuTensorMapEncodeTiled from the driver, looked up once.
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -34,6 +32,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   }
   return fn;
 }
+
+namespace {
 
 // 2D FP32 tensor map over a padded field (ld1 rows x n2p columns) with a
 // box of bz rows x bx columns; out-of-range elements read as zero.

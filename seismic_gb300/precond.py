@@ -41,13 +41,14 @@ class Survey:
 
 def make_survey(ctx, seed: int, nz: int = 60, nx: int = 180, d: float = 10.0, nt: int = 900,
                 dt: float = 1e-3, nshot: int = 6, f0: float = 8.0, smooth_m: float = 120.0,
-                vmin: float = 1500.0, vmax: float = 3500.0) -> Survey:
+                vmin: float = 1500.0, vmax: float = 3500.0, nlayers: int = 8, nfaults: int = 2,
+                snapi: int = 2) -> Survey:
     """Seeded layered/faulted model, a smoothed start model and observed data
     modelled with the FWI forward operator (AMOD) on the true model."""
-    vtrue = synth.layered_faulted(nz, nx, d, seed=seed, nlayers=8, nfaults=2, vmin=vmin,
-                                  vmax=vmax)
+    vtrue = synth.layered_faulted(nz, nx, d, seed=seed, nlayers=nlayers, nfaults=nfaults,
+                                  vmin=vmin, vmax=vmax)
     v0 = synth.smooth(vtrue, d, smooth_m)
-    g = make_genpar(nz, nx, 1, dz=d, dx=d, dt=dt, nt=nt, ntaper=20, lsinc=7, snapi=2,
+    g = make_genpar(nz, nx, 1, dz=d, dx=d, dt=dt, nt=nt, ntaper=20, lsinc=7, snapi=snapi,
                     fmax=2.5 * f0)
     desc = SwFwiDesc()
     desc.g = g
@@ -244,7 +245,7 @@ def model_error(sv: Survey, x: np.ndarray) -> float:
 
 
 def run_study(ctx, train_seeds=tuple(range(1000, 1016)), test_seeds=(4, 5, 6), epochs: int = 400,
-              channels=(2, 16, 16, 16, 1), max_evals: int = 60, learned_kw=None,
+              channels=(2, 32, 32, 32, 1), max_evals: int = 60, learned_kw=None,
               **survey_kw) -> dict:
     """Trains the network on plain runs over train_seeds, then inverts every
     test model with both methods.  The target misfit is the best one the
@@ -302,3 +303,127 @@ def run_study(ctx, train_seeds=tuple(range(1000, 1016)), test_seeds=(4, 5, 6), e
     return {"pairs": int(len(x)), "step_scale": scale, "pair_seconds": t_pairs,
             "train_seconds": t_train, "train_loss_first": float(losses[0]),
             "train_loss_last": float(np.mean(losses[-20:])), "tests": rows}
+
+
+# The learned-preconditioner FWI benchmark: 601 x 1801 test models at 10 m
+# from the layered, faulted generator (40 dipping layers, 6 normal faults,
+# 3 % correlated noise, 1500-4700 m/s), start model the true model smoothed
+# by a Gaussian of 250 m, 80 shots, 4 s records, Ricker stages at 3, 6 and
+# 9 Hz; training pairs from plain runs on 301 x 901 models.  dt is 0.9 ms:
+# 1 ms exceeds the 2D Courant limit of the 8th-order scheme at 4700 m/s.
+CONFIG4 = {"test": (601, 1801), "train": (301, 901), "d": 10.0, "dt": 9e-4, "t": 4.0,
+           "nshot": 80, "stages": (3.0, 6.0, 9.0), "smooth_m": 250.0, "vmin": 1500.0,
+           "vmax": 4700.0, "nlayers": 40, "nfaults": 6, "snapi": 4}
+
+
+def _stage_survey(ctx, seed, shape, f0, nshot, cfg, v0=None) -> Survey:
+    nz, nx = shape
+    sv = make_survey(ctx, seed, nz=nz, nx=nx, d=cfg["d"], nt=int(round(cfg["t"] / cfg["dt"])),
+                     dt=cfg["dt"], nshot=nshot, f0=f0, smooth_m=cfg["smooth_m"],
+                     vmin=cfg["vmin"], vmax=cfg["vmax"], nlayers=cfg["nlayers"],
+                     nfaults=cfg["nfaults"], snapi=cfg["snapi"])
+    if v0 is not None:
+        sv.v0 = np.asarray(v0, np.float32).reshape(sv.v0.shape)
+    return sv
+
+
+def multiscale_fwi(ctx, seed: int, shape, nshot: int, cfg=CONFIG4, net=None, step_scale=None,
+                   evals_per_stage: int = 20, target: float = 0.01, record=None,
+                   learned_kw=None) -> dict:
+    """One inversion over the frequency stages: plain L-BFGS (net None) or
+    learned directions first with the L-BFGS fallback; each stage starts
+    from the previous stage's model and stops at `target` times its own
+    start misfit or after evals_per_stage evaluations.  The final misfit is
+    also stated relative to the last stage's misfit of the original start
+    model (one extra evaluation, not counted as solves)."""
+    x = None
+    stages = []
+    solves = 0
+    seconds = 0.0
+    sv = None
+    for f0 in cfg["stages"]:
+        sv = _stage_survey(ctx, seed, shape, f0, nshot, cfg, v0=x)
+        rec = None if record is None else (lambda xx, gd, il, f0=f0: record(f0, xx, gd, il))
+        if net is None:
+            h = plain_fwi(ctx, sv, target=target, max_evals=evals_per_stage, record=rec)
+        else:
+            h = learned_fwi(ctx, sv, net, step_scale, target=target, max_evals=evals_per_stage,
+                            **(learned_kw or {}))
+        x = h.x
+        solves += h.solves(nshot)
+        seconds += h.seconds
+        stages.append({"f0_hz": f0, "evals": h.evals, "solves": h.solves(nshot),
+                       "seconds": h.seconds, "rel_misfit_end": float(h.misfit[-1]),
+                       "rel_misfit_best": float(min(h.misfit)),
+                       "learned_steps": h.learned_steps, "fallback_steps": h.fallback_steps,
+                       "curve": [float(m) for m in h.misfit]})
+    # The last stage's misfit of the original start model.
+    sv0 = _stage_survey(ctx, seed, shape, cfg["stages"][-1], nshot, cfg)
+    f_start, _, _ = _Evaluator(ctx, sv0, History())(sv0.v0.astype(np.float64).ravel())
+    f_end, _, _ = _Evaluator(ctx, sv, History())(x)
+    return {"solves": solves, "seconds": seconds, "stages": stages,
+            "final_rel_misfit": float(f_end / f_start),
+            "model_err": model_error(sv0, x), "x": x}
+
+
+def run_config4_study(ctx, n_train: int = 64, train_nshot: int = 40, test_seeds=(7,),
+                      evals_per_stage: int = 20, train_evals_per_stage: int = 12,
+                      epochs: int = 600, channels=(2, 32, 32, 32, 1), cfg=CONFIG4,
+                      learned_kw=None, log=None) -> dict:
+    """Trains the network on pairs from multiscale plain runs over n_train
+    seeded models at the training size, then inverts each test model at the
+    test size with both methods; solves and wall time per method."""
+    from . import CNN
+    log = log or (lambda m: None)
+    t0 = time.perf_counter()
+    xs, ys, scales = [], [], []
+    for k, sd in enumerate(range(2000, 2000 + n_train)):
+        its = []
+        r = multiscale_fwi(ctx, sd, cfg["train"], train_nshot, cfg,
+                           evals_per_stage=train_evals_per_stage, target=0.0,
+                           record=lambda f0, x, gd, il: its.append((f0, x, gd, il)))
+        # Target of each iterate: the remaining update to its stage's end.
+        ends = {}
+        for f0, x, gd, il in its:
+            ends[f0] = x
+        shape = (cfg["train"][1], cfg["train"][0])
+        for f0, x, gd, il in its:
+            step = ends[f0] - x
+            s = np.abs(step).max()
+            if s > 0:
+                xs.append(_features(gd, il, shape))
+                ys.append((step / s).reshape(shape).astype(np.float32))
+                scales.append(s)
+        log(f"training model {k + 1}/{n_train}: {len(xs)} pairs, "
+            f"final rel misfit {r['final_rel_misfit']:.3g}")
+    t_pairs = time.perf_counter() - t0
+    x_tr, y_tr, scale = np.stack(xs), np.stack(ys), float(np.median(scales))
+    net = CNN(ctx, channels, seed=0)
+    rows = []
+    try:
+        t1 = time.perf_counter()
+        losses = train_cnn(net, x_tr, y_tr, epochs=epochs, batch=8)
+        t_train = time.perf_counter() - t1
+        log(f"trained: loss {losses[0]:.4g} -> {np.mean(losses[-20:]):.4g} in {t_train:.0f} s")
+        for sd in test_seeds:
+            hp = multiscale_fwi(ctx, sd, cfg["test"], cfg["nshot"], cfg,
+                                evals_per_stage=evals_per_stage)
+            log(f"test {sd} plain: {hp['solves']} solves, {hp['seconds']:.0f} s, "
+                f"rel misfit {hp['final_rel_misfit']:.3g}")
+            hl = multiscale_fwi(ctx, sd, cfg["test"], cfg["nshot"], cfg, net=net,
+                                step_scale=scale, evals_per_stage=evals_per_stage,
+                                learned_kw=learned_kw)
+            log(f"test {sd} learned: {hl['solves']} solves, {hl['seconds']:.0f} s, "
+                f"rel misfit {hl['final_rel_misfit']:.3g}")
+            for h in (hp, hl):
+                h.pop("x")
+            rows.append({"seed": sd, "plain": hp, "learned": hl})
+    finally:
+        net.close()
+    return {"train_models": n_train, "train_shape": list(cfg["train"]),
+            "train_nshot": train_nshot, "test_shape": list(cfg["test"]),
+            "test_nshot": cfg["nshot"], "stages_hz": list(cfg["stages"]), "dt_s": cfg["dt"],
+            "record_s": cfg["t"], "pairs": int(len(x_tr)), "step_scale": scale,
+            "pair_seconds": t_pairs, "train_seconds": t_train,
+            "train_loss_first": float(losses[0]), "train_loss_last": float(np.mean(losses[-20:])),
+            "channels": list(channels), "tests": rows}

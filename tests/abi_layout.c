@@ -98,5 +98,7 @@ int main(void) {
   F(sw_stats, launches_total); F(sw_stats, launches_step); F(sw_stats, points_updated);
   F(sw_stats, step_kernel_ms); F(sw_stats, step_kernel_timed); F(sw_stats, step_bytes);
   F(sw_stats, steps_forward); F(sw_stats, steps_backward); F(sw_stats, ckpt_advances);
+  F(sw_stats, cnn_conv_ms); F(sw_stats, cnn_conv_timed); F(sw_stats, cnn_conv_bytes);
+  F(sw_stats, cnn_conv_flops);
   return 0;
 }

@@ -325,6 +325,53 @@ def test_autotuner_chooses_shots_per_launch(oracle, tmp_path):
     np.testing.assert_array_equal(il, ril)
 
 
+def test_rtm_job_admit_matches_the_batch_run(ctx):
+    """sw_rtm_job_admit reports the batch that the next run takes: capped by
+    max_shots and by the end of the survey, and SW_OOM_ADMISSION when one
+    shot exceeds the memory budget."""
+    g, vel, w, shots = _survey(nshot=5, seed=4)
+    job = sw.RTMJob(ctx, g, vel, w, shots)
+    try:
+        job.set_batch(2)
+        assert job.admit(0) == 2 and job.admit(4) == 1
+        job.run(0, 2)
+        assert job.info()[0] == 2
+        job.set_batch(64)
+        assert job.admit(0) == 5 and job.admit(0, modeling=True) == 5
+        job.set_batch(64, 1e-9)
+        with pytest.raises(sw.SwaveError) as e:
+            job.admit(0)
+        assert e.value.code == sw.SW_OOM_ADMISSION
+    finally:
+        job.close()
+
+
+def test_tune_survey_on_device(oracle, tmp_path):
+    """tune_survey caps the batch candidates by the admission at full record
+    length, picks the shots per launch and then the launch shape; the survey
+    migrated with its choice stays bit-exact with the oracle."""
+    from seismic_gb300 import autotune
+    g, vel, w, shots = _survey(nshot=5, seed=21)
+    full = [dict(s, nt=s["data"].shape[1]) for s in shots]
+    c = sw.Context(0)
+    try:
+        entry = autotune.tune_survey(c, g, vel, w, full, steps=24,
+                                     cache_path=str(tmp_path / "tuning.json"))
+        assert entry["admit_cap"] == 5
+        assert entry["batch"] in (1, 2, 4, 5)
+        assert entry["tuning"] in autotune.candidates(True)
+        job = sw.RTMJob(c, g, vel, w, shots)
+        job.set_batch(entry["batch"])
+        job.run()
+        im, il, _ = job.result()
+        job.close()
+    finally:
+        c.close()
+    rim, ril, _ = oracle.rtm_job(g, vel, w, shots)
+    np.testing.assert_array_equal(im, rim)
+    np.testing.assert_array_equal(il, ril)
+
+
 def test_fwi_gradient_fd_check_on_device(oracle):
     """The device's raw FWI gradient against centred finite differences of
     the device's misfit along the 8 seeded smooth directions of the oracle's
