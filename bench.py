@@ -284,6 +284,9 @@ def main():
     ap.add_argument("--revolve-study", action="store_true",
                     help="FWI gradient memory modes on the 1201 x 3401 grid: store-all against "
                          "binomial checkpointing with 32/64/128 state slots")
+    ap.add_argument("--rho", action="store_true",
+                    help="time 2D modelling with variable density (and without) on the "
+                         "751 x 2301 grid instead of the RTM bench")
     ap.add_argument("--cnn-bench", action="store_true",
                     help="time the preconditioner network's tensor-core kernels at 601 x 1801")
     ap.add_argument("--config4-study", action="store_true",
@@ -305,6 +308,8 @@ def main():
         return run_config4_study(args)
     if args.cnn_bench:
         return run_cnn_bench(args)
+    if args.rho:
+        return run_rho_bench(args)
     if args.model3d:
         return run_model3d(args)
     if args.revolve_study:
@@ -556,6 +561,80 @@ def run_model3d(args) -> int:
         "clocks": clk, "gpu_launches": int(st["launches_total"]),
     }
     print(json.dumps(line))
+    return 0
+
+
+def run_rho_bench(args) -> int:
+    """Variable density: 2D modelling of one shot on the full 751 x 2301
+    model at 4 m (the RTM bench's grid and dt, 2000 steps, 2301 receivers)
+    through sw_propagate with a density model (withRho: gradient pass, then
+    the staggered divergence on the point-tile kernel) and, for scale, the
+    same run without it.  One JSON line."""
+    import torch
+
+    import seismic_gb300 as sw
+    from seismic_gb300 import synth
+    torch.cuda.set_device(0)
+    ctx = sw.Context(0)
+    c = synth.CONFIG2
+    nt = args.nt_cap or 2000
+    nz, nx, d = c["nz"], c["nx"], c["d"]
+    g = sw.make_genpar(nz, nx, 1, dz=d, dx=d, dt=c["dt"], nt=nt, ntaper=c["ntaper"], lsinc=7,
+                       snapi=4)
+    vel = synth.layered_faulted(nz, nx, d, seed=3)
+    rng = np.random.default_rng(3)
+    rho = np.ascontiguousarray(1.8 + 0.0004 * np.arange(nz)[None, :] * d +
+                               0.1 * rng.random(vel.shape), np.float32)
+    sou = np.array([2 * d, nx * d / 2, 0.0], np.float32)
+    rec = np.zeros((nx, 3), np.float32)
+    rec[:, 0], rec[:, 1] = 2 * d, np.arange(nx) * d
+    w = sw.rho_wavelet(synth.ricker(20.0, c["dt"], nt), 7)
+    desc = sw.SwPropDesc()
+    desc.g = g
+    desc.tmin, desc.tmax, desc.tstep = 1, nt, 1
+    desc.fd_scheme = sw.FD_FORWARD
+    desc.injection, desc.extraction = sw.INJ_SINC, sw.EXT_SINC
+    data = np.zeros((nx, nt), np.float32)
+
+    def run(with_rho):
+        ctx.propagate(desc, vel, sou[None], w[None], rec, data,
+                      rho=rho if with_rho else None)
+
+    out = {}
+    clk = None
+    for with_rho in (True, False):
+        for _ in range(max(1, args.warmup)):
+            run(with_rho)
+        ctx.reset_stats()
+        if with_rho:
+            clocks = ClockSampler(0)
+            clocks.start()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            run(with_rho)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        if with_rho:
+            clk = clocks.stop()
+        st = ctx.stats()
+        out[with_rho] = (float(st["points_updated"]) / secs / 1e9, secs / args.steps,
+                         int(st["launches_total"]))
+    line = {
+        "metric": "fd_gpts_per_s_2d_rho_modeling", "value": out[True][0], "unit": "Gpts/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": out[True][1] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded layered, faulted model; density 1.8-2.2 g/cc)",
+        "config": {"workload": "2D modelling of one shot with variable density through "
+                               "sw_propagate (host buffers)",
+                   "grid": [nz, nx], "spacing_m": d, "dt_s": c["dt"], "nt": nt,
+                   "receivers": nx},
+        "constant_density_gpts_per_s": out[False][0],
+        "clocks": clk, "gpu_launches": out[True][2],
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
     return 0
 
 

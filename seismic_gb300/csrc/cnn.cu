@@ -3,13 +3,15 @@
 // that maps the FWI gradient and the source illumination to a search
 // direction, with training and inference on the GPU.
 //
-// Activations and gradients are BF16, channels-last, with the channel count
-// stored rounded up to 8 (zeros above the layer's own count): pixel
-// p = x * nz + z holds Cs consecutive values.  One GEMM tile is a 32 (z) x
-// 4 (x) patch of 128 pixels; an 8-channel slice of it, shifted by a tap, is
-// one 3D tensor copy (box 8 x 32 x 4, zero fill outside the image) that
-// lands in shared memory as 128 rows of 16 bytes - exactly one K column of
-// core matrices of the tensor cores' no-swizzle layout (umma.cuh).
+// Activations and gradients are BF16 in channel-group planes: the channel
+// count is rounded up to 8 (zeros above the layer's own count) and group g
+// of 8 channels is a plane [x][z][8] of the image (pixel p = x * nz + z), so
+// element (p, c) sits at ((c / 8) * npix + p) * 8 + c % 8.  One GEMM tile is
+// a 32 (z) x 4 (x) patch of 128 pixels; an 8-channel slice of it, shifted by
+// a tap, is one tensor copy of 4 contiguous 512-byte rows (zero fill outside
+// the image) that lands in shared memory as 128 rows of 16 bytes - exactly
+// one K column of core matrices of the tensor cores' no-swizzle layout
+// (umma.cuh).
 //
 // * Convolution (forward, and the input gradient with mirrored taps and
 //   transposed weights): implicit GEMM D[pixel][n] = sum over (tap,
@@ -64,13 +66,16 @@ __device__ __forceinline__ void cnn_expect_tx(unsigned long long *bar, unsigned 
                "r"(bytes)
                : "memory");
 }
-// 3D tensor copy (channel, z, x) global -> shared memory on an mbarrier.
-__device__ __forceinline__ void cnn_tma3(void *dst, const CUtensorMap *map, int c, int z, int x,
+// Tensor copy of the 8-channel slice of channel group cg at pixels
+// z0..z0+31 x x0..x0+3 (global -> shared memory, on an mbarrier).  The map's
+// innermost dimension is (z, channel) flattened, so its coordinate 8 z is
+// a multiple of 16 bytes for every z.
+__device__ __forceinline__ void cnn_tma3(void *dst, const CUtensorMap *map, int cg, int z, int x,
                                          unsigned long long *bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(umma_su32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(c), "r"(z), "r"(x),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(8 * z), "r"(x), "r"(cg),
       "r"(umma_su32(bar))
       : "memory");
 }
@@ -103,8 +108,8 @@ struct ConvArgs {
   int nout;                      // output channels
   int cs_out;                    // stored output channels (BF16 outputs)
   float *out32;                  // kFwdLast: [p][nout]
-  __nv_bfloat16 *out16;          // kFwdHidden, kBwd: [p][cs_out]
-  const __nv_bfloat16 *mask;     // kBwd: layer input activations [p][cs_out]
+  __nv_bfloat16 *out16;          // kFwdHidden, kBwd: cs_out / 8 channel-group planes
+  const __nv_bfloat16 *mask;     // kBwd: layer input activations (cs_out / 8 planes)
   int *err;
 };
 
@@ -158,7 +163,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int tap = 0; tap < 9; ++tap) {
       const int dz = sgn * (tap % 3 - 1), dx = sgn * (tap / 3 - 1);
       for (int cg = 0; cg < A.Cs / 8; ++cg)
-        cnn_tma3(dst + (size_t)(tap * (A.Cs / 8) + cg) * kChunk, &amap, cg * 8, z0 + dz, x0 + dx,
+        cnn_tma3(dst + (size_t)(tap * (A.Cs / 8) + cg) * kChunk, &amap, cg, z0 + dz, x0 + dx,
                  &full[i & 1]);
     }
   };
@@ -208,7 +213,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int z = (t % A.tiles_z) * kTZ + (tid % kTZ);
       const int x = (t / A.tiles_z) * kTX + tid / kTZ;
       if (z < A.nz && x < A.nx) {
-        const size_t p = (size_t)x * A.nz + z;
+        const size_t p = (size_t)x * A.nz + z, npix = (size_t)A.nz * A.nx;
         if (MODE == kFwdLast) {
 #pragma unroll
           for (int n = 0; n < NP; ++n)
@@ -223,7 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1)
               for (int j = 0; j < 8; ++j)
                 v[j] = c0 + j < A.nout ? fmaxf(acc[c0 + j] + A.bias[c0 + j], 0.f) : 0.f;
             } else {
-              const uint4 mk = *reinterpret_cast<const uint4 *>(A.mask + p * A.cs_out + c0);
+              const uint4 mk =
+                  *reinterpret_cast<const uint4 *>(A.mask + ((size_t)(c0 / 8) * npix + p) * 8);
               const unsigned mw[4] = {mk.x, mk.y, mk.z, mk.w};
 #pragma unroll
               for (int j = 0; j < 8; ++j) {
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 v[j] = (c0 + j < A.nout && pos) ? acc[c0 + j] : 0.f;
               }
             }
-            *reinterpret_cast<uint4 *>(A.out16 + p * A.cs_out + c0) =
+            *reinterpret_cast<uint4 *>(A.out16 + ((size_t)(c0 / 8) * npix + p) * 8) =
                 make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
                            pack_bf16(v[6], v[7]));
           }
@@ -327,11 +333,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int tap = 0; tap < 9; ++tap) {
       const int dz = tap % 3 - 1, dx = tap / 3 - 1;
       for (int cg = 0; cg < A.Csi / 8; ++cg)
-        cnn_tma3(dst + (size_t)(tap * (A.Csi / 8) + cg) * kChunk, &amap, cg * 8, z0 + dz, x0 + dx,
+        cnn_tma3(dst + (size_t)(tap * (A.Csi / 8) + cg) * kChunk, &amap, cg, z0 + dz, x0 + dx,
                  &full[i & 1]);
     }
     for (int cg = 0; cg < A.Cso / 8; ++cg)
-      cnn_tma3(dst + (size_t)(G + 1 + cg) * kChunk, &dmap, cg * 8, z0, x0, &full[i & 1]);
+      cnn_tma3(dst + (size_t)(G + 1 + cg) * kChunk, &dmap, cg, z0, x0, &full[i & 1]);
   };
   if (tid == 0) {
     int issued = 0, consumed = 0, committed = 0;
@@ -422,20 +428,21 @@ __global__ void k_wgrad_sum(const float *__restrict__ part, int nchunk, int Cout
   else gw[((size_t)co * 9 + tap) * Cin + ci] += s;
 }
 
-// Planar FP32 channels (c, p) -> channels-last BF16 with Cs stored channels.
+// Planar FP32 channels (c, p) -> BF16 channel-group planes with Cs stored
+// channels (q = (g * npix + p) * 8 + c % 8).
 __global__ void k_pack_input(const float *__restrict__ in, int C, int Cs, int npix,
                              __nv_bfloat16 *__restrict__ out) {
   const long long n = (long long)Cs * npix;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
        q += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(q % Cs);
-    const long long p = q / Cs;
+    const int c = (int)(q / (8LL * npix)) * 8 + (int)(q % 8);
+    const long long p = (q / 8) % npix;
     out[q] = __float2bfloat16(c < C ? in[(size_t)c * npix + p] : 0.f);
   }
 }
 
 // Mean-square loss of a one-channel output: the output gradient
-// (out - target) / npix as BF16 in channel 0 of an 8-channel layout, and
+// (out - target) / npix as BF16 in channel 0 of one 8-channel plane, and
 // per-block FP64 partial sums of (out - target)^2.
 __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ tgt, int npix,
                        __nv_bfloat16 *__restrict__ db, double *__restrict__ part) {
@@ -493,13 +500,15 @@ __global__ void k_weights_bf16(const float *__restrict__ w, int Cout, int Cin, i
 
 int nblk(long long n) { return (int)std::min<long long>(4096, (n + 255) / 256); }
 
-// Channels-last BF16 tensor map (Cs, nz, nx), box 8 x 32 x 4, zero fill.
+// BF16 tensor map over Cs / 8 channel-group planes: dimensions (8 nz: z
+// and the 8 channels flattened, nx, Cs / 8), box 8 kTZ x kTX x 1 (kTX rows
+// of 512 bytes), zero fill outside.
 bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)Cs, (cuuint64_t)nz, (cuuint64_t)nx};
-  const cuuint64_t strides[2] = {(cuuint64_t)Cs * 2, (cuuint64_t)Cs * 2 * nz};
-  const cuuint32_t box[3] = {8, kTZ, kTX};
+  const cuuint64_t dims[3] = {(cuuint64_t)nz * 8, (cuuint64_t)nx, (cuuint64_t)Cs / 8};
+  const cuuint64_t strides[2] = {(cuuint64_t)nz * 16, (cuuint64_t)nz * nx * 16};
+  const cuuint32_t box[3] = {8 * kTZ, kTX, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims,
              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -599,8 +608,8 @@ struct sw_cnn {
   int step = 0;
   // Per-image buffers (grow-only).
   size_t cap = 0;
-  std::vector<__nv_bfloat16 *> a;      // layer inputs [p][r8(ch[l])]
-  __nv_bfloat16 *dz[2] = {nullptr, nullptr};   // gradients [p][r8(max ch)]
+  std::vector<__nv_bfloat16 *> a;      // layer inputs, r8(ch[l]) / 8 channel-group planes
+  __nv_bfloat16 *dz[2] = {nullptr, nullptr};   // gradients, up to r8(max ch) / 8 planes
   float *out32 = nullptr, *in32 = nullptr, *tgt = nullptr, *part = nullptr;
   double *lpart = nullptr;
   int *err = nullptr;

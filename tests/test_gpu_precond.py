@@ -49,10 +49,10 @@ def test_multiscale_study_driver_small(ctx):
     """The multiscale driver (stages of rising frequency, each starting from
     the previous stage's model) and the study around it, on a small copy of
     the benchmark geometry: misfits fall, solves are counted per stage."""
-    cfg = dict(pc.CONFIG4, test=(40, 120), train=(30, 90), nshot=3, t=0.5, dt=1e-3,
+    cfg = dict(pc.CONFIG4, test=(40, 120), train=(30, 90), nshot=3, t=0.5,
                stages=(4.0, 8.0), smooth_m=100.0, nlayers=8, nfaults=2)
     r = pc.run_config4_study(ctx, n_train=2, train_nshot=2, test_seeds=(3,), evals_per_stage=4,
-                             train_evals_per_stage=3, epochs=20, channels=(2, 32, 32, 1),
+                             train_evals_per_stage=6, epochs=20, channels=(2, 32, 32, 1),
                              cfg=cfg, learned_kw={"max_learned": 2, "c1": 0.1})
     assert r["pairs"] >= 2
     row = r["tests"][0]
