@@ -510,6 +510,17 @@ int sw_cnn_gradient(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
  * 0.5 * mean((out - target)^2); *loss receives that mean loss. */
 int sw_cnn_train_step(sw_cnn *net, int nbatch, int nz, int nx, const float *in,
                       const float *target, float lr, double *loss);
+/* The same network with 3 x 3 x 3 kernels on nz x nx x ny volumes (z
+ * fastest, then x): weights packed per layer as w[co][tap][ci] with tap =
+ * 9 * (dy + 1) + 3 * (dx + 1) + (dz + 1), then b[co].  The image entry
+ * points above take 3 x 3 networks only and these 3 x 3 x 3 networks only
+ * (SW_BAD_PARAM otherwise). */
+int sw_cnn_create3d(sw_ctx *ctx, int nlayers, const int *channels, uint64_t seed, sw_cnn **out);
+int sw_cnn_forward3d(sw_cnn *net, int nz, int nx, int ny, const float *in, float *out);
+int sw_cnn_gradient3d(sw_cnn *net, int nbatch, int nz, int nx, int ny, const float *in,
+                      const float *target, float *grad, double *loss);
+int sw_cnn_train_step3d(sw_cnn *net, int nbatch, int nz, int nx, int ny, const float *in,
+                        const float *target, float lr, double *loss);
 
 /* ---- Modelling without device allocation --------------------------------- */
 /* No counterpart in the reference (its modelling allocates the wavefields of

@@ -461,6 +461,39 @@ module swave_iface
        integer(c_int), value :: nz, nx
        real(c_float)         :: in(*), out(*)
      end function
+     integer(c_int) function sw_cnn_create3d(ctx, nlayers, channels, seed, net) &
+          bind(C, name="sw_cnn_create3d")
+       import :: c_int, c_ptr, c_int64_t
+       type(c_ptr), value        :: ctx
+       integer(c_int), value     :: nlayers
+       integer(c_int)            :: channels(*)
+       integer(c_int64_t), value :: seed
+       type(c_ptr)               :: net
+     end function
+     integer(c_int) function sw_cnn_forward3d(net, nz, nx, ny, in, out) &
+          bind(C, name="sw_cnn_forward3d")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value    :: net
+       integer(c_int), value :: nz, nx, ny
+       real(c_float)         :: in(*), out(*)
+     end function
+     integer(c_int) function sw_cnn_gradient3d(net, nbatch, nz, nx, ny, in, target, grad, &
+          loss) bind(C, name="sw_cnn_gradient3d")
+       import :: c_int, c_ptr, c_float, c_double
+       type(c_ptr), value    :: net
+       integer(c_int), value :: nbatch, nz, nx, ny
+       real(c_float)         :: in(*), target(*), grad(*)
+       real(c_double)        :: loss
+     end function
+     integer(c_int) function sw_cnn_train_step3d(net, nbatch, nz, nx, ny, in, target, lr, &
+          loss) bind(C, name="sw_cnn_train_step3d")
+       import :: c_int, c_ptr, c_float, c_double
+       type(c_ptr), value    :: net
+       integer(c_int), value :: nbatch, nz, nx, ny
+       real(c_float)         :: in(*), target(*)
+       real(c_float), value  :: lr
+       real(c_double)        :: loss
+     end function
      integer(c_int) function sw_cnn_gradient(net, nbatch, nz, nx, in, target, grad, loss) &
           bind(C, name="sw_cnn_gradient")
        import :: c_int, c_ptr, c_float, c_double

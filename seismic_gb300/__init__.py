@@ -181,6 +181,13 @@ _SIGS = {
                                     C.POINTER(C.c_double)]),
     "sw_cnn_gradient": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp,
                                   C.POINTER(C.c_double)]),
+    "sw_cnn_create3d": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_uint64,
+                                  C.POINTER(C.c_void_p)]),
+    "sw_cnn_forward3d": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _fp, _fp]),
+    "sw_cnn_gradient3d": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp,
+                                    _fp, C.POINTER(C.c_double)]),
+    "sw_cnn_train_step3d": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp,
+                                      C.c_float, C.POINTER(C.c_double)]),
     "sw_rtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
     "sw_born": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, _fp, C.c_int, _fp, _fp]),
     "sw_lsrtm": (C.c_int, [C.c_void_p, C.POINTER(SwGenpar), _fp, _fp, _fp, C.c_int, _fp, _fp, _fp, _fp]),
@@ -658,12 +665,17 @@ def window_scatter_add(model: SwGenpar, w: SwWindow, small, big: np.ndarray) -> 
 class CNN:
     """sw_cnn_*: the convolutional gradient preconditioner on the tensor cores."""
 
-    def __init__(self, ctx: "Context", channels=(2, 16, 16, 16, 1), seed: int = 0):
+    def __init__(self, ctx: "Context", channels=(2, 32, 32, 32, 1), seed: int = 0,
+                 three_d: bool = False):
+        """three_d: 3 x 3 x 3 kernels on (ny, nx, nz) volumes instead of 3 x 3
+        kernels on (nx, nz) images."""
         self.ctx = ctx
         self.channels = list(channels)
+        self.three_d = bool(three_d)
         ch = (C.c_int * len(channels))(*channels)
         h = C.c_void_p()
-        ctx._check(ctx.lib.sw_cnn_create(ctx.h, len(channels) - 1, ch, seed, C.byref(h)))
+        create = ctx.lib.sw_cnn_create3d if three_d else ctx.lib.sw_cnn_create
+        ctx._check(create(ctx.h, len(channels) - 1, ch, seed, C.byref(h)))
         self.h = h
 
     @property
@@ -681,8 +693,14 @@ class CNN:
         self.ctx._check(self.ctx.lib.sw_cnn_set_weights(self.h, fptr(w)))
 
     def forward(self, x) -> np.ndarray:
-        """x: (channels[0], nx, nz) planar image stack (z fastest)."""
+        """x: (channels[0], nx, nz) planar image stack (z fastest), or
+        (channels[0], ny, nx, nz) for a 3 x 3 x 3 network."""
         x = _f32(x)
+        if self.three_d:
+            c, ny, nx, nz = x.shape
+            out = np.zeros((ny, nx, nz), np.float32)
+            self.ctx._check(self.ctx.lib.sw_cnn_forward3d(self.h, nz, nx, ny, fptr(x), fptr(out)))
+            return out
         c, nx, nz = x.shape
         out = np.zeros((nx, nz), np.float32)
         self.ctx._check(self.ctx.lib.sw_cnn_forward(self.h, nz, nx, fptr(x), fptr(out)))
@@ -690,22 +708,32 @@ class CNN:
 
     def gradient(self, x, target) -> tuple[np.ndarray, float]:
         """Gradient of the batch-mean loss (packed like the weights) and that
-        loss; x: (batch, channels[0], nx, nz), target: (batch, nx, nz)."""
+        loss; x: (batch, channels[0], [ny,] nx, nz), target: (batch, [ny,] nx, nz)."""
         x, t = _f32(x), _f32(target)
-        b, c, nx, nz = x.shape
         g = np.zeros(self.num_weights, np.float32)
         loss = C.c_double()
-        self.ctx._check(self.ctx.lib.sw_cnn_gradient(self.h, b, nz, nx, fptr(x), fptr(t), fptr(g),
-                                                     C.byref(loss)))
+        if self.three_d:
+            b, c, ny, nx, nz = x.shape
+            self.ctx._check(self.ctx.lib.sw_cnn_gradient3d(self.h, b, nz, nx, ny, fptr(x), fptr(t),
+                                                           fptr(g), C.byref(loss)))
+        else:
+            b, c, nx, nz = x.shape
+            self.ctx._check(self.ctx.lib.sw_cnn_gradient(self.h, b, nz, nx, fptr(x), fptr(t),
+                                                         fptr(g), C.byref(loss)))
         return g, loss.value
 
     def train_step(self, x, target, lr: float = 1e-3) -> float:
-        """x: (batch, channels[0], nx, nz); target: (batch, nx, nz)."""
+        """x: (batch, channels[0], [ny,] nx, nz); target: (batch, [ny,] nx, nz)."""
         x, t = _f32(x), _f32(target)
-        b, c, nx, nz = x.shape
         loss = C.c_double()
-        self.ctx._check(self.ctx.lib.sw_cnn_train_step(self.h, b, nz, nx, fptr(x), fptr(t),
-                                                       float(lr), C.byref(loss)))
+        if self.three_d:
+            b, c, ny, nx, nz = x.shape
+            self.ctx._check(self.ctx.lib.sw_cnn_train_step3d(self.h, b, nz, nx, ny, fptr(x),
+                                                             fptr(t), float(lr), C.byref(loss)))
+        else:
+            b, c, nx, nz = x.shape
+            self.ctx._check(self.ctx.lib.sw_cnn_train_step(self.h, b, nz, nx, fptr(x), fptr(t),
+                                                           float(lr), C.byref(loss)))
         return loss.value
 
     def close(self):

@@ -51,8 +51,7 @@ constexpr int kMaxC = 32;                 // channels per layer
 constexpr int kTZ = 32, kTX = 4;          // pixel patch of one GEMM tile
 constexpr int kTile = kTZ * kTX;          // 128 pixels = GEMM M
 constexpr int kChunk = kTile * 16;        // one 8-channel slice: 2048 bytes
-constexpr int kThreads = 128;
-constexpr int kWgradSlots = 10 * kMaxC * kMaxC;   // partial sums per CTA
+constexpr int kWgradSlots = 28 * kMaxC * kMaxC;   // partial sums per CTA (27 taps + bias)
 
 int r8(int c) { return (c + 7) / 8 * 8; }
 int r16(int c) { return (c + 15) / 16 * 16; }
@@ -67,17 +66,24 @@ __device__ __forceinline__ void cnn_expect_tx(unsigned long long *bar, unsigned 
                : "memory");
 }
 // Tensor copy of the 8-channel slice of channel group cg at pixels
-// z0..z0+31 x x0..x0+3 (global -> shared memory, on an mbarrier).  The map's
-// innermost dimension is (z, channel) flattened, so its coordinate 8 z is
-// a multiple of 16 bytes for every z.
-__device__ __forceinline__ void cnn_tma3(void *dst, const CUtensorMap *map, int cg, int z, int x,
-                                         unsigned long long *bar) {
+// z..z+31 x x..x+3 of plane y (global -> shared memory, on an mbarrier).
+// The map's innermost dimension is (z, channel) flattened, so its
+// coordinate 8 z is a multiple of 16 bytes for every z.
+__device__ __forceinline__ void cnn_tma4(void *dst, const CUtensorMap *map, int cg, int z, int x,
+                                         int y, unsigned long long *bar) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(umma_su32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(8 * z), "r"(x), "r"(cg),
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(umma_su32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(8 * z), "r"(x), "r"(y), "r"(cg),
       "r"(umma_su32(bar))
       : "memory");
+}
+// Offsets of tap t of a 3 x 3 (taps = 9) or 3 x 3 x 3 (taps = 27) kernel:
+// t = 9 (dy + 1) + 3 (dx + 1) + (dz + 1).
+__device__ __forceinline__ void tap_off(int t, int taps, int &dz, int &dx, int &dy) {
+  dz = t % 3 - 1;
+  dx = (t / 3) % 3 - 1;
+  dy = taps == 27 ? t / 9 - 1 : 0;
 }
 // Instruction descriptor with both operands MN-major (transposed).
 __host__ __device__ constexpr uint32_t umma_idesc_bf16_mn(int M, int N) {
@@ -90,19 +96,63 @@ __device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
 }
 
 // ---------------------------------------------------------------------------
-// Implicit-GEMM 3x3 convolution.
+// Warp roles of both kernels (192 threads): warps 0-3 read the tensor-memory
+// accumulator (lane quadrant = warp) and run the epilogue, warp 4 issues
+// the tensor copies into a ring of shared-memory stages, warp 5 issues the
+// tensor-core instructions.  Every wait is bounded; a wait that gives up
+// sets the error flag and the CTA's abort flag, and every role leaves its
+// loop at its next wait.
+// ---------------------------------------------------------------------------
+constexpr int kEpiWarps = 4, kProducerWarp = 4, kMmaWarp = 5;
+constexpr int kWsThreads = 192;
+
+// Bounded wait that also gives up once another role has aborted.
+__device__ __forceinline__ bool cnn_wait(unsigned long long *bar, unsigned parity,
+                                         volatile int *abort_flag) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(umma_su32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 63) == 63 && *abort_flag) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void cnn_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma_su32(bar)) : "memory");
+}
+__device__ __forceinline__ void cnn_bar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(umma_su32(bar)), "r"(count)
+               : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Implicit-GEMM 3x3 (or 3x3x3) convolution.
 //   D[p][n] = sum_{tap, c} in[p + s * off(tap)][c] * W[n][tap * Cs + c]
 // with s = +1 (forward) or -1 (input gradient) and zero padding outside
-// the image.  W: NP x kp BF16 in the tensor cores' K-major layout.
+// the image.  W: NP x kp BF16 in the tensor cores' K-major layout.  One
+// ring stage holds two 8-channel slices (one K = 16 step, 4 KB); the
+// slices of a tile run over (tap, channel group), and the K padding slice
+// (when 9 Cs / 8 is odd) is a copy from far outside the image (all zero).
+// Two accumulators in tensor memory let the products of the next tile run
+// while the epilogue reads the last one.
 // ---------------------------------------------------------------------------
 enum { kFwdHidden = 0, kFwdLast = 1, kBwd = 2 };
+constexpr int kConvStage = 2 * kChunk;
+constexpr int kMaxRing = 32;
 
 struct ConvArgs {
   int Cs;                        // stored input channels (multiple of 8)
-  int nz, nx;
-  int kp;                        // GEMM K: 9 Cs rounded up to 16
-  int ntiles, tiles_z;
+  int nz, nx, ny;
+  int taps;                      // 9 (2D) or 27 (3D)
+  int kp;                        // GEMM K: taps Cs rounded up to 16
+  int ntiles, tiles_z, tiles_x;
   int mirror;
+  int ring;                      // shared-memory stages (<= kMaxRing)
   const __nv_bfloat16 *W;
   const float *bias;             // forward: nout biases
   int nout;                      // output channels
@@ -113,39 +163,42 @@ struct ConvArgs {
   int *err;
 };
 
-size_t conv_smem_bytes(int NP, int kp) {
-  const size_t wbytes = ((size_t)NP * kp * 2 + 1023) / 1024 * 1024;
-  return 1024 + wbytes + 2 * (size_t)(kp / 8) * kChunk;
+__host__ __device__ inline size_t conv_wbytes(int NP, int kp) { return ((size_t)NP * kp * 2 + 1023) / 1024 * 1024; }
+size_t conv_smem_bytes(int NP, int kp, int ring) {
+  return 1024 + conv_wbytes(NP, kp) + (size_t)ring * kConvStage;
 }
 
 template <int NP, int MODE>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kWsThreads, 1)
     k_conv_tma(const __grid_constant__ CUtensorMap amap, const ConvArgs A) {
   extern __shared__ unsigned char cnn_smem[];
-  __shared__ __align__(8) unsigned long long full[2], mdone;
+  __shared__ __align__(8) unsigned long long full[kMaxRing], empty[kMaxRing];
+  __shared__ __align__(8) unsigned long long acc_full[2], acc_empty[2];
   __shared__ unsigned tmem_base;
-  __shared__ int abort_flag;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nch = A.kp / 8, nload = 9 * (A.Cs / 8);
+  __shared__ volatile int abort_flag;
+  __shared__ volatile int mma_stages;             // stages the MMA warp has consumed
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nst = A.kp / 16;                      // ring stages per tile
+  const int nload = A.taps * (A.Cs / 8);          // slices with data
   unsigned char *base = align1024(cnn_smem);
   unsigned char *sW = base;
-  unsigned char *st0 = base + ((size_t)NP * A.kp * 2 + 1023) / 1024 * 1024;
-  const size_t sbytes = (size_t)nch * kChunk;
+  unsigned char *ring = base + conv_wbytes(NP, A.kp);
   if (tid == 0) {
-    umma_mbar_init(&full[0]);
-    umma_mbar_init(&full[1]);
-    umma_mbar_init(&mdone);
-    abort_flag = 0;
-  }
-  if (warp == 0) umma_alloc(&tmem_base, 32);
-  for (int q = tid; q < NP * A.kp / 8; q += kThreads)
-    reinterpret_cast<uint4 *>(sW)[q] = reinterpret_cast<const uint4 *>(A.W)[q];
-  // K padding (one chunk when 9 Cs / 8 is odd) stays zero in both stages.
-  for (int c = nload; c < nch; ++c)
-    for (int q = tid; q < kChunk / 16; q += kThreads) {
-      reinterpret_cast<uint4 *>(st0 + (size_t)c * kChunk)[q] = make_uint4(0, 0, 0, 0);
-      reinterpret_cast<uint4 *>(st0 + sbytes + (size_t)c * kChunk)[q] = make_uint4(0, 0, 0, 0);
+    for (int q = 0; q < A.ring; ++q) {
+      cnn_bar_init(&full[q], 1);
+      cnn_bar_init(&empty[q], 1);
     }
+    for (int q = 0; q < 2; ++q) {
+      cnn_bar_init(&acc_full[q], 1);
+      cnn_bar_init(&acc_empty[q], kEpiWarps);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+    mma_stages = 0;
+  }
+  if (warp == kMmaWarp) umma_alloc(&tmem_base, 64);
+  for (int q = tid; q < NP * A.kp / 8; q += kWsThreads)
+    reinterpret_cast<uint4 *>(sW)[q] = reinterpret_cast<const uint4 *>(A.W)[q];
   umma_fence_smem();
   umma_fence_before();
   __syncthreads();
@@ -153,71 +206,111 @@ __global__ void __launch_bounds__(kThreads, 1)
   const unsigned tmem = tmem_base;
   const int first = blockIdx.x, stride = gridDim.x;
   const int nmine = first < A.ntiles ? (A.ntiles - 1 - first) / stride + 1 : 0;
-  int issued = 0, consumed = 0, committed = 0;   // thread 0's counters
-  auto issue = [&](int i) {
-    const int t = first + i * stride;
-    const int z0 = (t % A.tiles_z) * kTZ, x0 = (t / A.tiles_z) * kTX;
-    unsigned char *dst = st0 + (size_t)(i & 1) * sbytes;
-    cnn_expect_tx(&full[i & 1], (unsigned)(nload * kChunk));
-    const int sgn = A.mirror ? -1 : 1;
-    for (int tap = 0; tap < 9; ++tap) {
-      const int dz = sgn * (tap % 3 - 1), dx = sgn * (tap / 3 - 1);
-      for (int cg = 0; cg < A.Cs / 8; ++cg)
-        cnn_tma3(dst + (size_t)(tap * (A.Cs / 8) + cg) * kChunk, &amap, cg, z0 + dz, x0 + dx,
-                 &full[i & 1]);
-    }
-  };
-  if (tid == 0 && nmine > 0) {
-    issue(0);
-    issued = 1;
-  }
-  for (int i = 0; i < nmine; ++i) {
-    if (tid == 0) {
-      // Stage (i + 1) & 1 held tile i - 1, whose products were waited for.
-      if (i + 1 < nmine) {
-        issue(i + 1);
-        issued = i + 2;
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      const int sgn = A.mirror ? -1 : 1;
+      const int ng = A.Cs / 8;
+      int q = 0;
+      bool ok = true;
+      for (int i = 0; i < nmine && ok; ++i) {
+        const int t = first + i * stride;
+        const int z0 = (t % A.tiles_z) * kTZ, x0 = ((t / A.tiles_z) % A.tiles_x) * kTX;
+        const int y0 = t / (A.tiles_z * A.tiles_x);
+        for (int k = 0; k < nst; ++k, ++q) {
+          const int slot = q % A.ring;
+          if (q >= A.ring && !(ok = cnn_wait(&empty[slot], ((q / A.ring) - 1) & 1, &abort_flag)))
+            break;
+          unsigned char *dst = ring + (size_t)slot * kConvStage;
+          cnn_expect_tx(&full[slot], kConvStage);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int c = 2 * k + h;
+            if (c < nload) {
+              const int tap = c / ng, cg = c % ng;
+              int dz, dx, dy;
+              tap_off(tap, A.taps, dz, dx, dy);
+              cnn_tma4(dst + h * kChunk, &amap, cg, z0 + sgn * dz, x0 + sgn * dx, y0 + sgn * dy,
+                       &full[slot]);
+            } else {
+              cnn_tma4(dst + h * kChunk, &amap, 0, -(1 << 20), -(1 << 20), 0, &full[slot]);
+            }
+          }
+        }
       }
-      if (!umma_mbar_wait(&full[i & 1], (i >> 1) & 1)) {
+      if (!ok) {
         abort_flag = 1;
         atomicOr(A.err, 1);
-      } else {
-        consumed = i + 1;
-        umma_fence_after();
-        constexpr uint32_t idesc = umma_idesc_bf16(kTile, NP);
-        const unsigned sa = umma_su32(st0 + (size_t)(i & 1) * sbytes), sb = umma_su32(sW);
-        for (int ks = 0; ks < A.kp / 16; ++ks) {
-          const uint64_t ad = umma_smem_desc(sa + ks * 2 * kChunk, kChunk, 128);
-          const uint64_t bd = umma_smem_desc(sb + ks * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
-          umma_bf16(tmem, ad, bd, idesc, ks > 0);
-        }
-        umma_commit(&mdone);
-        committed = i + 1;
       }
+      // After a give-up, copies the MMA warp did not consume complete
+      // before the CTA leaves (at most one ring of them).
+      if (abort_flag)
+        for (int r = max(mma_stages, q - A.ring); r < q; ++r)
+          umma_mbar_wait(&full[r % A.ring], (r / A.ring) & 1);
     }
-    __syncthreads();
-    if (abort_flag) break;
-    bool ok = umma_mbar_wait(&mdone, i & 1);
-    ok = __all_sync(0xffffffffu, ok);
-    if (!ok) {
-      abort_flag = 1;
-      atomicOr(A.err, 1);
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = umma_idesc_bf16(kTile, NP);
+      const unsigned sb = umma_su32(sW);
+      int q = 0, committed = -1;
+      bool ok = true;
+      for (int i = 0; i < nmine && ok; ++i) {
+        const int acc = i & 1;
+        if (i >= 2 && !(ok = cnn_wait(&acc_empty[acc], ((i >> 1) - 1) & 1, &abort_flag))) break;
+        umma_fence_after();
+        const unsigned d = tmem + acc * NP;
+        for (int k = 0; k < nst; ++k, ++q) {
+          const int slot = q % A.ring;
+          if (!(ok = cnn_wait(&full[slot], (q / A.ring) & 1, &abort_flag))) break;
+          mma_stages = q + 1;
+          umma_fence_after();
+          const unsigned sa = umma_su32(ring + (size_t)slot * kConvStage);
+          const uint64_t ad = umma_smem_desc(sa, kChunk, 128);
+          const uint64_t bd = umma_smem_desc(sb + k * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
+          umma_bf16(d, ad, bd, idesc, k > 0);
+          umma_commit(&empty[slot]);
+        }
+        if (!ok) break;
+        umma_commit(&acc_full[acc]);
+        committed = i;
+      }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(A.err, 1);
+      }
+      if (committed >= 0) umma_mbar_wait(&acc_full[committed & 1], (committed >> 1) & 1);
     }
-    umma_fence_after();
-    if (ok) {
-      float acc[NP];
-      const unsigned ta = tmem + ((unsigned)(warp * 32) << 16);
-      umma_ld16(ta, acc);
-      if (NP == 32) umma_ld16(ta + 16, acc + 16);
+  } else {
+    // Epilogue: thread = accumulator lane = pixel row of the tile.
+    for (int i = 0; i < nmine; ++i) {
+      const int acc = i & 1;
+      bool ok = cnn_wait(&acc_full[acc], (i >> 1) & 1, &abort_flag);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) {
+        if (lane == 0) {
+          abort_flag = 1;
+          atomicOr(A.err, 1);
+        }
+        break;
+      }
+      umma_fence_after();
+      float accv[NP];
+      const unsigned ta = tmem + ((unsigned)(warp * 32) << 16) + acc * NP;
+      umma_ld16(ta, accv);
+      if (NP == 32) umma_ld16(ta + 16, accv + 16);
+      umma_fence_before();
+      __syncwarp();
+      if (lane == 0) cnn_arrive(&acc_empty[acc]);
       const int t = first + i * stride;
       const int z = (t % A.tiles_z) * kTZ + (tid % kTZ);
-      const int x = (t / A.tiles_z) * kTX + tid / kTZ;
+      const int x = ((t / A.tiles_z) % A.tiles_x) * kTX + tid / kTZ;
+      const int y = t / (A.tiles_z * A.tiles_x);
       if (z < A.nz && x < A.nx) {
-        const size_t p = (size_t)x * A.nz + z, npix = (size_t)A.nz * A.nx;
+        const size_t p = ((size_t)y * A.nx + x) * A.nz + z;
+        const size_t npix = (size_t)A.nz * A.nx * A.ny;
         if (MODE == kFwdLast) {
 #pragma unroll
           for (int n = 0; n < NP; ++n)
-            if (n < A.nout) A.out32[p * A.nout + n] = acc[n] + A.bias[n];
+            if (n < A.nout) A.out32[p * A.nout + n] = accv[n] + A.bias[n];
         } else {
 #pragma unroll
           for (int c0 = 0; c0 < NP; c0 += 8) {
@@ -226,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (MODE == kFwdHidden) {
 #pragma unroll
               for (int j = 0; j < 8; ++j)
-                v[j] = c0 + j < A.nout ? fmaxf(acc[c0 + j] + A.bias[c0 + j], 0.f) : 0.f;
+                v[j] = c0 + j < A.nout ? fmaxf(accv[c0 + j] + A.bias[c0 + j], 0.f) : 0.f;
             } else {
               const uint4 mk =
                   *reinterpret_cast<const uint4 *>(A.mask + ((size_t)(c0 / 8) * npix + p) * 8);
@@ -235,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               for (int j = 0; j < 8; ++j) {
                 const unsigned short bits = (unsigned short)(mw[j >> 1] >> (16 * (j & 1)));
                 const bool pos = __bfloat162float(__ushort_as_bfloat16(bits)) > 0.f;
-                v[j] = (c0 + j < A.nout && pos) ? acc[c0 + j] : 0.f;
+                v[j] = (c0 + j < A.nout && pos) ? accv[c0 + j] : 0.f;
               }
             }
             *reinterpret_cast<uint4 *>(A.out16 + ((size_t)(c0 / 8) * npix + p) * 8) =
@@ -245,187 +338,190 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
-    umma_fence_before();
-    __syncthreads();
-    if (abort_flag) break;
-  }
-  // After a give-up: wait (bounded) for this CTA's copies and products in
-  // flight before the tensor memory and the CTA go away.
-  if (tid == 0) {
-    for (int j = consumed; j < issued; ++j) umma_mbar_wait(&full[j & 1], (j >> 1) & 1);
-    if (committed > 0) umma_mbar_wait(&mdone, (committed - 1) & 1);
   }
   umma_fence_before();
   __syncthreads();
   umma_fence_after();
-  if (warp == 0) umma_dealloc(tmem, 32);
+  if (warp == kMmaWarp) umma_dealloc(tmem, 64);
 }
 
 // ---------------------------------------------------------------------------
 // Weight and bias gradient of one layer on the tensor cores.
 //   D[m][co] = sum_p A[m][p] * dz[p][co],  m = tap * Csi + ci  (A[m][p] =
-//   a[p + off(tap)][ci]),  m = 9 Csi: a row of ones (bias gradient).
+//   a[p + off(tap)][ci]),  m = taps Csi: a row of ones (bias gradient).
 // Both operands MN-major: each 8-channel slice copied by TMA is one MN
 // group of 8 rows x 128 pixels (core matrices 128 bytes apart along K, MN
-// groups one 2048-byte slice apart).
-// Stage layout: 9 Csi / 8 activation groups, the ones group, Cso / 8
-// gradient groups, 2048 bytes each.  The M = 128 slices beyond the real
-// rows read whatever shared memory follows (rows that are never stored).
+// groups one 2048-byte slice apart).  One ring stage serves one M = 128
+// slice of the rows for one tile: its 16 row groups (activation slices,
+// the ones slice copied from a constant array, stale data for rows past
+// the end, never stored) and the tile's Cout / 8 gradient slices.  Each
+// CTA accumulates its tiles in tensor memory (one accumulator per M
+// slice) and writes one partial sum.
 // ---------------------------------------------------------------------------
 struct WgradArgs {
   int Csi, Cin, Cso, Cout;
-  int nz, nx, ntiles, tiles_z;
-  int nmma;                      // M = 128 slices: ceil((9 Csi + 8) / 128)
-  size_t stage_bytes;
+  int nz, nx, ny, taps, ntiles, tiles_z, tiles_x;
+  int nmma;                      // M = 128 slices: ceil((taps Csi + 8) / 128)
+  int ring;                      // shared-memory stages (<= kMaxRing)
   float *part;                   // [cta][10][kMaxC][kMaxC]
   int *err;
 };
+constexpr int kWgradStage = 20 * kChunk;   // 16 row groups + up to 4 gradient groups
 
-size_t wgrad_stage_bytes(int Csi, int Cso) {
-  return (size_t)(9 * Csi / 8 + 1 + Cso / 8) * kChunk;
-}
-size_t wgrad_smem_bytes(int Csi, int Cso, int NPO) {
-  const size_t sb = wgrad_stage_bytes(Csi, Cso);
-  const int nmma = (9 * Csi + 8 + 127) / 128;
-  const size_t reach = std::max({sb, (size_t)nmma * 16 * kChunk,
-                                 (size_t)(9 * Csi / 8 + 1 + NPO / 8) * kChunk});
-  return 1024 + sb + reach;
-}
+size_t wgrad_smem_bytes(int ring) { return 1024 + (size_t)ring * kWgradStage; }
 
 template <int NPO>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kWsThreads, 1)
     k_wgrad_umma(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap dmap,
-                 const WgradArgs A) {
+                 const __grid_constant__ CUtensorMap onemap, const WgradArgs A) {
   extern __shared__ unsigned char cnn_smem[];
-  __shared__ __align__(8) unsigned long long full[2], mdone[2];
+  __shared__ __align__(8) unsigned long long full[kMaxRing], empty[kMaxRing], done;
   __shared__ unsigned tmem_base;
-  __shared__ int abort_flag;
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int G = 9 * A.Csi / 8;
-  unsigned char *st0 = align1024(cnn_smem);
+  __shared__ volatile int abort_flag;
+  __shared__ volatile int mma_stages;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int G = A.taps * A.Csi / 8;               // activation groups; group G = ones
+  unsigned char *ring = align1024(cnn_smem);
   if (tid == 0) {
-    umma_mbar_init(&full[0]);
-    umma_mbar_init(&full[1]);
-    umma_mbar_init(&mdone[0]);
-    umma_mbar_init(&mdone[1]);
+    for (int q = 0; q < A.ring; ++q) {
+      cnn_bar_init(&full[q], 1);
+      cnn_bar_init(&empty[q], 1);
+    }
+    cnn_bar_init(&done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
+    mma_stages = 0;
   }
-  if (warp == 0) umma_alloc(&tmem_base, 128);
-  // The ones group of both stages (BF16 1.0 = 0x3f80).
-  for (int q = tid; q < kChunk / 16; q += kThreads) {
-    const uint4 one = make_uint4(0x3f803f80u, 0x3f803f80u, 0x3f803f80u, 0x3f803f80u);
-    reinterpret_cast<uint4 *>(st0 + (size_t)G * kChunk)[q] = one;
-    reinterpret_cast<uint4 *>(st0 + A.stage_bytes + (size_t)G * kChunk)[q] = one;
-  }
-  umma_fence_smem();
+  if (warp == kMmaWarp) umma_alloc(&tmem_base, 256);
   umma_fence_before();
   __syncthreads();
   umma_fence_after();
   const unsigned tmem = tmem_base;
   const int first = blockIdx.x, stride = gridDim.x;
   const int nmine = first < A.ntiles ? (A.ntiles - 1 - first) / stride + 1 : 0;
-  const unsigned txb = (unsigned)((G + A.Cso / 8) * kChunk);
-  auto issue = [&](int i) {
-    const int t = first + i * stride;
-    const int z0 = (t % A.tiles_z) * kTZ, x0 = (t / A.tiles_z) * kTX;
-    unsigned char *dst = st0 + (size_t)(i & 1) * A.stage_bytes;
-    cnn_expect_tx(&full[i & 1], txb);
-    for (int tap = 0; tap < 9; ++tap) {
-      const int dz = tap % 3 - 1, dx = tap / 3 - 1;
-      for (int cg = 0; cg < A.Csi / 8; ++cg)
-        cnn_tma3(dst + (size_t)(tap * (A.Csi / 8) + cg) * kChunk, &amap, cg, z0 + dz, x0 + dx,
-                 &full[i & 1]);
-    }
-    for (int cg = 0; cg < A.Cso / 8; ++cg)
-      cnn_tma3(dst + (size_t)(G + 1 + cg) * kChunk, &dmap, cg, z0, x0, &full[i & 1]);
-  };
-  if (tid == 0) {
-    int issued = 0, consumed = 0, committed = 0;
-    bool ok = true;
-    if (nmine > 0) {
-      issue(0);
-      issued = 1;
-    }
-    constexpr uint32_t idesc = umma_idesc_bf16_mn(kTile, NPO);
-    for (int i = 0; i < nmine && ok; ++i) {
-      if (i + 1 < nmine) {
-        // Stage (i + 1) & 1 is free once tile i - 1's products are done.
-        if (i >= 1) ok = umma_mbar_wait(&mdone[(i - 1) & 1], ((i - 1) >> 1) & 1);
-        if (!ok) break;
-        issue(i + 1);
-        issued = i + 2;
-      }
-      ok = umma_mbar_wait(&full[i & 1], (i >> 1) & 1);
-      if (!ok) break;
-      consumed = i + 1;
-      umma_fence_after();
-      const unsigned sa = umma_su32(st0 + (size_t)(i & 1) * A.stage_bytes);
-      const unsigned sb = sa + (unsigned)((G + 1) * kChunk);
-      for (int ks = 0; ks < kTile / 16; ++ks)
-        for (int j = 0; j < A.nmma; ++j) {
-          // MN-major, no swizzle: the leading byte offset is the step between
-          // 8-row core-matrix groups along K (128 bytes here), the stride
-          // byte offset the step between 8-element groups along M / N (one
-          // 2048-byte slice).
-          const uint64_t ad = umma_smem_desc(sa + j * 16 * kChunk + ks * 256, 128, kChunk);
-          const uint64_t bd = umma_smem_desc(sb + ks * 256, 128, kChunk);
-          umma_bf16(tmem + j * NPO, ad, bd, idesc, i > 0 || ks > 0);
+  if (warp == kProducerWarp) {
+    if (lane == 0) {
+      const int ng = A.Csi / 8;
+      int q = 0;
+      bool ok = true;
+      for (int i = 0; i < nmine && ok; ++i) {
+        const int t = first + i * stride;
+        const int z0 = (t % A.tiles_z) * kTZ, x0 = ((t / A.tiles_z) % A.tiles_x) * kTX;
+        const int y0 = t / (A.tiles_z * A.tiles_x);
+        for (int j = 0; j < A.nmma; ++j, ++q) {
+          const int slot = q % A.ring;
+          if (q >= A.ring && !(ok = cnn_wait(&empty[slot], ((q / A.ring) - 1) & 1, &abort_flag)))
+            break;
+          unsigned char *dst = ring + (size_t)slot * kWgradStage;
+          const int g1 = min(16 * j + 16, G + 1);
+          cnn_expect_tx(&full[slot], (unsigned)((g1 - 16 * j + A.Cso / 8) * kChunk));
+          for (int g = 16 * j; g < g1; ++g) {
+            unsigned char *gd = dst + (size_t)(g - 16 * j) * kChunk;
+            if (g < G) {
+              const int tap = g / ng, cg = g % ng;
+              int dz, dx, dy;
+              tap_off(tap, A.taps, dz, dx, dy);
+              cnn_tma4(gd, &amap, cg, z0 + dz, x0 + dx, y0 + dy, &full[slot]);
+            } else {
+              cnn_tma4(gd, &onemap, 0, 0, 0, 0, &full[slot]);
+            }
+          }
+          for (int cg = 0; cg < A.Cso / 8; ++cg)
+            cnn_tma4(dst + (size_t)(16 + cg) * kChunk, &dmap, cg, z0, x0, y0, &full[slot]);
         }
-      umma_commit(&mdone[i & 1]);
-      committed = i + 1;
+      }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(A.err, 1);
+      }
+      if (abort_flag)
+        for (int r = max(mma_stages, q - A.ring); r < q; ++r)
+          umma_mbar_wait(&full[r % A.ring], (r / A.ring) & 1);
     }
-    if (!ok) {
-      abort_flag = 1;
-      atomicOr(A.err, 1);
-      for (int j = consumed; j < issued; ++j) umma_mbar_wait(&full[j & 1], (j >> 1) & 1);
+  } else if (warp == kMmaWarp) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = umma_idesc_bf16_mn(kTile, NPO);
+      int q = 0;
+      bool ok = true, any = false;
+      for (int i = 0; i < nmine && ok; ++i)
+        for (int j = 0; j < A.nmma; ++j, ++q) {
+          const int slot = q % A.ring;
+          if (!(ok = cnn_wait(&full[slot], (q / A.ring) & 1, &abort_flag))) break;
+          mma_stages = q + 1;
+          umma_fence_after();
+          const unsigned sa = umma_su32(ring + (size_t)slot * kWgradStage);
+          const unsigned sb = sa + 16 * kChunk;
+          // MN-major, no swizzle: the leading byte offset is the step
+          // between 8-row core-matrix groups along K (128 bytes here), the
+          // stride byte offset the step between 8-element groups along M / N
+          // (one 2048-byte slice).
+#pragma unroll
+          for (int ks = 0; ks < kTile / 16; ++ks)
+            umma_bf16(tmem + j * NPO, umma_smem_desc(sa + ks * 256, 128, kChunk),
+                      umma_smem_desc(sb + ks * 256, 128, kChunk), idesc, i > 0 || ks > 0);
+          umma_commit(&empty[slot]);
+          any = true;
+        }
+      if (!ok) {
+        abort_flag = 1;
+        atomicOr(A.err, 1);
+      }
+      if (any) umma_commit(&done);
+      else cnn_arrive(&done);
     }
-    // Products complete in order: the last commit covers them all.
-    if (committed > 0 && !umma_mbar_wait(&mdone[(committed - 1) & 1], ((committed - 1) >> 1) & 1)) {
-      abort_flag = 1;
-      atomicOr(A.err, 1);
-    }
-  }
-  umma_fence_before();
-  __syncthreads();
-  umma_fence_after();
-  if (!abort_flag && nmine > 0) {
-    float *P = A.part + (size_t)blockIdx.x * kWgradSlots;
-    for (int j = 0; j < A.nmma; ++j) {
-      float acc[NPO];
-      const unsigned ta = tmem + ((unsigned)(warp * 32) << 16) + j * NPO;
-      umma_ld16(ta, acc);
-      if (NPO == 32) umma_ld16(ta + 16, acc + 16);
-      const int m = j * kTile + tid;
-      if (m < 9 * A.Csi) {
-        const int tap = m / A.Csi, ci = m % A.Csi;
-        if (ci < A.Cin)
+  } else if (nmine > 0) {
+    // Epilogue: thread = accumulator lane = row (tap, ci) within a slice.
+    bool ok = cnn_wait(&done, 0, &abort_flag) && !abort_flag;
+    ok = __all_sync(0xffffffffu, ok);
+    umma_fence_after();
+    if (ok) {
+      float *P = A.part + (size_t)blockIdx.x * kWgradSlots;
+      for (int j = 0; j < A.nmma; ++j) {
+        float accv[NPO];
+        const unsigned ta = tmem + ((unsigned)(warp * 32) << 16) + j * NPO;
+        umma_ld16(ta, accv);
+        if (NPO == 32) umma_ld16(ta + 16, accv + 16);
+        const int m = j * kTile + tid;
+        if (m < A.taps * A.Csi) {
+          const int tap = m / A.Csi, ci = m % A.Csi;
+          if (ci < A.Cin)
+#pragma unroll
+            for (int co = 0; co < NPO; ++co)
+              if (co < A.Cout) P[(size_t)tap * kMaxC * kMaxC + co * kMaxC + ci] = accv[co];
+        } else if (m == A.taps * A.Csi) {
 #pragma unroll
           for (int co = 0; co < NPO; ++co)
-            if (co < A.Cout) P[(size_t)tap * kMaxC * kMaxC + co * kMaxC + ci] = acc[co];
-      } else if (m == 9 * A.Csi) {
-#pragma unroll
-        for (int co = 0; co < NPO; ++co)
-          if (co < A.Cout) P[(size_t)9 * kMaxC * kMaxC + co * kMaxC] = acc[co];
+            if (co < A.Cout) P[(size_t)A.taps * kMaxC * kMaxC + co * kMaxC] = accv[co];
+        }
       }
+    } else if (lane == 0) {
+      abort_flag = 1;
+      atomicOr(A.err, 1);
     }
   }
   umma_fence_before();
   __syncthreads();
   umma_fence_after();
-  if (warp == 0) umma_dealloc(tmem, 128);
+  if (warp == kMmaWarp) {
+    // A give-up left products in flight: wait (bounded) for the last commit.
+    if (abort_flag && lane == 0) umma_mbar_wait(&done, 0);
+    __syncwarp();
+    umma_dealloc(tmem, 256);
+  }
 }
 
 // Sums the per-CTA partials in CTA order into the layer's gradient buffer
-// (FP32, [co][tap][ci] then bias[co]) - added to what it holds.
+// (FP32, [co][tap][ci] then bias[co]) - added to what it holds.  Block
+// `taps` is the bias.
 __global__ void k_wgrad_sum(const float *__restrict__ part, int nchunk, int Cout, int Cin,
-                            float *__restrict__ gw) {
+                            int taps, float *__restrict__ gw) {
   const int tap = blockIdx.x, t = threadIdx.x;
   const int co = t / kMaxC, ci = t % kMaxC;
-  if (co >= Cout || (tap == 9 ? ci != 0 : ci >= Cin)) return;
+  if (co >= Cout || (tap == taps ? ci != 0 : ci >= Cin)) return;
   float s = 0.f;
   for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * kWgradSlots + tap * kMaxC * kMaxC + t];
-  if (tap == 9) gw[(size_t)Cout * 9 * Cin + co] += s;
-  else gw[((size_t)co * 9 + tap) * Cin + ci] += s;
+  if (tap == taps) gw[(size_t)Cout * taps * Cin + co] += s;
+  else gw[((size_t)co * taps + tap) * Cin + ci] += s;
 }
 
 // Planar FP32 channels (c, p) -> BF16 channel-group planes with Cs stored
@@ -480,20 +576,20 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
 // layout: forward NPo x KPf, element (co, tap * Csi + ci); input gradient
 // NPi x KPb, element (ci, tap * Cso + co).  Zero outside the layer.
 __global__ void k_weights_bf16(const float *__restrict__ w, int Cout, int Cin, int Csi, int Cso,
-                               int NPo, int KPf, int NPi, int KPb,
+                               int taps, int NPo, int KPf, int NPi, int KPb,
                                __nv_bfloat16 *__restrict__ wf, __nv_bfloat16 *__restrict__ wb) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < NPo * KPf; q += gridDim.x * blockDim.x) {
     const int n = q / KPf, k = q % KPf;
     const int tap = k / Csi, ci = k % Csi;
     float v = 0.f;
-    if (n < Cout && tap < 9 && ci < Cin) v = w[((size_t)n * 9 + tap) * Cin + ci];
+    if (n < Cout && tap < taps && ci < Cin) v = w[((size_t)n * taps + tap) * Cin + ci];
     wf[umma_off(n, k, NPo) >> 1] = __float2bfloat16(v);
   }
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < NPi * KPb; q += gridDim.x * blockDim.x) {
     const int n = q / KPb, k = q % KPb;
     const int tap = k / Cso, co = k % Cso;
     float v = 0.f;
-    if (n < Cin && tap < 9 && co < Cout) v = w[((size_t)co * 9 + tap) * Cin + n];
+    if (n < Cin && tap < taps && co < Cout) v = w[((size_t)co * taps + tap) * Cin + n];
     wb[umma_off(n, k, NPi) >> 1] = __float2bfloat16(v);
   }
 }
@@ -501,16 +597,18 @@ __global__ void k_weights_bf16(const float *__restrict__ w, int Cout, int Cin, i
 int nblk(long long n) { return (int)std::min<long long>(4096, (n + 255) / 256); }
 
 // BF16 tensor map over Cs / 8 channel-group planes: dimensions (8 nz: z
-// and the 8 channels flattened, nx, Cs / 8), box 8 kTZ x kTX x 1 (kTX rows
-// of 512 bytes), zero fill outside.
-bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx) {
+// and the 8 channels flattened, nx, ny, Cs / 8), box 8 kTZ x kTX x 1 x 1
+// (kTX rows of 512 bytes), zero fill outside.
+bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx, int ny) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
-  const cuuint64_t dims[3] = {(cuuint64_t)nz * 8, (cuuint64_t)nx, (cuuint64_t)Cs / 8};
-  const cuuint64_t strides[2] = {(cuuint64_t)nz * 16, (cuuint64_t)nz * nx * 16};
-  const cuuint32_t box[3] = {8 * kTZ, kTX, 1};
-  const cuuint32_t estr[3] = {1, 1, 1};
-  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16 *>(base), dims,
+  const cuuint64_t dims[4] = {(cuuint64_t)nz * 8, (cuuint64_t)nx, (cuuint64_t)ny,
+                              (cuuint64_t)Cs / 8};
+  const cuuint64_t strides[3] = {(cuuint64_t)nz * 16, (cuuint64_t)nz * nx * 16,
+                                 (cuuint64_t)nz * nx * ny * 16};
+  const cuuint32_t box[4] = {8 * kTZ, kTX, 1, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(base), dims,
              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -528,23 +626,29 @@ cudaError_t launch_big(K kernel, int grid, size_t smem, cudaStream_t s, const CU
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  kernel<<<grid, kThreads, smem, s>>>(m0, a);
+  kernel<<<grid, kWsThreads, smem, s>>>(m0, a);
   return cudaGetLastError();
 }
 
 // One convolution: input tensor (Cs channels) -> MODE's outputs.
 cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int Cs, int nz, int nx,
-                        ConvArgs a, cudaStream_t s) {
+                        int ny, int taps, ConvArgs a, cudaStream_t s) {
   CUtensorMap m;
-  if (!encode_act_map(&m, in, Cs, nz, nx)) return cudaErrorInvalidValue;
+  if (!encode_act_map(&m, in, Cs, nz, nx, ny)) return cudaErrorInvalidValue;
   a.Cs = Cs;
   a.nz = nz;
   a.nx = nx;
-  a.kp = r16(9 * Cs);
+  a.ny = ny;
+  a.taps = taps;
+  a.kp = r16(taps * Cs);
   a.tiles_z = (nz + kTZ - 1) / kTZ;
-  a.ntiles = a.tiles_z * ((nx + kTX - 1) / kTX);
-  const size_t smem = conv_smem_bytes(NP, a.kp);
-  const int per_sm = std::max<int>(1, std::min<int>(4, (int)((227u * 1024u) / smem)));
+  a.tiles_x = (nx + kTX - 1) / kTX;
+  a.ntiles = a.tiles_z * a.tiles_x * ny;
+  // A ring of about 110 KB per CTA: two CTAs per SM.
+  a.ring = (int)std::min<size_t>(kMaxRing, (110u * 1024u - 1024u - conv_wbytes(NP, a.kp)) /
+                                               kConvStage);
+  const size_t smem = conv_smem_bytes(NP, a.kp, a.ring);
+  const int per_sm = std::max<int>(1, std::min<int>(2, (int)((227u * 1024u) / smem)));
   const int grid = std::min(a.ntiles, num_sms(dev) * per_sm);
   if (NP == 16) {
     if (mode == kFwdHidden) return launch_big(k_conv_tma<16, kFwdHidden>, grid, smem, s, m, a);
@@ -558,7 +662,8 @@ cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int 
 
 // Weight-gradient partials of one layer; returns the number of partials.
 cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bfloat16 *dz,
-                         int Cout, int nz, int nx, float *part, int *err, cudaStream_t s,
+                         int Cout, int nz, int nx, int ny, int taps,
+                         const __nv_bfloat16 *ones, float *part, int *err, cudaStream_t s,
                          int *nchunk) {
   WgradArgs w;
   w.Csi = r8(Cin);
@@ -567,17 +672,21 @@ cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bf
   w.Cout = Cout;
   w.nz = nz;
   w.nx = nx;
+  w.ny = ny;
+  w.taps = taps;
   w.tiles_z = (nz + kTZ - 1) / kTZ;
-  w.ntiles = w.tiles_z * ((nx + kTX - 1) / kTX);
-  w.nmma = (9 * w.Csi + 8 + kTile - 1) / kTile;
-  w.stage_bytes = wgrad_stage_bytes(w.Csi, w.Cso);
+  w.tiles_x = (nx + kTX - 1) / kTX;
+  w.ntiles = w.tiles_z * w.tiles_x * ny;
+  w.nmma = (taps * w.Csi + 8 + kTile - 1) / kTile;
+  w.ring = 5;
   w.part = part;
   w.err = err;
-  CUtensorMap ma, md;
-  if (!encode_act_map(&ma, a, w.Csi, nz, nx) || !encode_act_map(&md, dz, w.Cso, nz, nx))
+  CUtensorMap ma, md, mo;
+  if (!encode_act_map(&ma, a, w.Csi, nz, nx, ny) || !encode_act_map(&md, dz, w.Cso, nz, nx, ny) ||
+      !encode_act_map(&mo, ones, 8, kTZ, kTX, 1))
     return cudaErrorInvalidValue;
   const int NPO = r16(Cout);
-  const size_t smem = wgrad_smem_bytes(w.Csi, w.Cso, NPO);
+  const size_t smem = wgrad_smem_bytes(w.ring);
   const int grid = std::min(w.ntiles, num_sms(dev));
   *nchunk = grid;
   cudaError_t e;
@@ -585,12 +694,12 @@ cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bf
     e = cudaFuncSetAttribute(k_wgrad_umma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return e;
-    k_wgrad_umma<16><<<grid, kThreads, smem, s>>>(ma, md, w);
+    k_wgrad_umma<16><<<grid, kWsThreads, smem, s>>>(ma, md, mo, w);
   } else {
     e = cudaFuncSetAttribute(k_wgrad_umma<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
     if (e != cudaSuccess) return e;
-    k_wgrad_umma<32><<<grid, kThreads, smem, s>>>(ma, md, w);
+    k_wgrad_umma<32><<<grid, kWsThreads, smem, s>>>(ma, md, mo, w);
   }
   return cudaGetLastError();
 }
@@ -600,6 +709,7 @@ cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bf
 struct sw_cnn {
   sw_ctx *ctx = nullptr;
   int nl = 0;
+  int taps = 9;                        // 9: 3 x 3 kernels on images, 27: 3 x 3 x 3 on volumes
   std::vector<int> ch;                 // nl + 1 channel counts
   std::vector<size_t> woff;            // offset of layer l in the packed weights
   size_t nw = 0;                       // packed FP32 weights (w then b per layer)
@@ -613,6 +723,7 @@ struct sw_cnn {
   float *out32 = nullptr, *in32 = nullptr, *tgt = nullptr, *part = nullptr;
   double *lpart = nullptr;
   int *err = nullptr;
+  __nv_bfloat16 *ones = nullptr;       // one 8-channel tile of BF16 ones (bias gradient)
 };
 
 namespace {
@@ -694,19 +805,22 @@ int refresh_bf16(sw_cnn *n) {
   cudaStream_t s = n->ctx->stream;
   for (int l = 0; l < n->nl; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
-    k_weights_bf16<<<8, 256, 0, s>>>(n->w + n->woff[l], Cout, Cin, r8(Cin), r8(Cout), r16(Cout),
-                                     r16(9 * r8(Cin)), r16(Cin), r16(9 * r8(Cout)), n->wf[l],
-                                     n->wb[l]);
+    const int T = n->taps;
+    k_weights_bf16<<<16, 256, 0, s>>>(n->w + n->woff[l], Cout, Cin, r8(Cin), r8(Cout), T,
+                                      r16(Cout), r16(T * r8(Cin)), r16(Cin), r16(T * r8(Cout)),
+                                      n->wf[l], n->wb[l]);
     n->ctx->stats.launches_total++;
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? SW_OK : cnn_fail(n, e, "cnn weights");
 }
 
-// Forward pass of one image already packed into n->a[0]; output in n->out32.
-int forward(sw_cnn *n, int nz, int nx) {
+// Forward pass of one image (volume) already packed into n->a[0]; output
+// in n->out32.
+int forward(sw_cnn *n, int nz, int nx, int ny) {
   cudaStream_t s = n->ctx->stream;
   const int dev = n->ctx->device;
+  const int T = n->taps;
   cudaError_t e;
   for (int l = 0; l < n->nl; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
@@ -714,17 +828,17 @@ int forward(sw_cnn *n, int nz, int nx) {
     ConvArgs a{};
     a.mirror = 0;
     a.W = n->wf[l];
-    a.bias = n->w + n->woff[l] + (size_t)Cout * 9 * Cin;
+    a.bias = n->w + n->woff[l] + (size_t)Cout * T * Cin;
     a.nout = Cout;
     a.cs_out = r8(Cout);
     a.out32 = last ? n->out32 : nullptr;
     a.out16 = last ? nullptr : n->a[l + 1];
     a.err = n->err;
-    const uint64_t np = (uint64_t)nz * nx;
+    const uint64_t np = (uint64_t)nz * nx * ny;
     const uint64_t bytes = np * r8(Cin) * 2 + (last ? np * Cout * 4 : np * r8(Cout) * 2);
-    if ((e = timed_launch(n, bytes, 2 * np * Cout * 9 * Cin, [&] {
+    if ((e = timed_launch(n, bytes, 2 * np * Cout * T * Cin, [&] {
            return launch_conv(dev, last ? kFwdLast : kFwdHidden, r16(Cout), n->a[l], r8(Cin), nz,
-                              nx, a, s);
+                              nx, ny, T, a, s);
          })) != cudaSuccess)
       return cnn_fail(n, e, "cnn conv");
   }
@@ -745,11 +859,12 @@ int check_err(sw_cnn *n) {
 
 // Sum over the batch of the weight gradient into n->g (zeroed first); the
 // batch-mean loss into *loss.
-int gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float *target,
+int gradient(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in, const float *target,
              double *loss) {
   cudaStream_t s = n->ctx->stream;
   const int dev = n->ctx->device;
-  const size_t npix = (size_t)nz * nx;
+  const int T = n->taps;
+  const size_t npix = (size_t)nz * nx * ny;
   int st = ensure_images(n, npix);
   if (st) return st;
   cudaError_t e;
@@ -767,7 +882,7 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float
     k_pack_input<<<nblk((long long)npix * r8(n->ch[0])), 256, 0, s>>>(
         n->in32, n->ch[0], r8(n->ch[0]), (int)npix, n->a[0]);
     n->ctx->stats.launches_total++;
-    if ((st = forward(n, nz, nx))) return st;
+    if ((st = forward(n, nz, nx, ny))) return st;
     // d loss / d output (one channel), FP64 loss partials.
     int cur = 0;
     k_loss<<<lblocks, 256, 0, s>>>(n->out32, n->tgt, (int)npix, n->dz[cur], n->lpart);
@@ -776,12 +891,13 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float
       const int Cin = n->ch[l], Cout = n->ch[l + 1];
       int nchunk = 0;
       const uint64_t np = (uint64_t)npix;
-      if ((e = timed_launch(n, np * (r8(Cin) + r8(Cout)) * 2, 2 * np * 9 * Cin * Cout, [&] {
-             return launch_wgrad(dev, n->a[l], Cin, n->dz[cur], Cout, nz, nx, n->part, n->err, s,
-                                 &nchunk);
+      if ((e = timed_launch(n, np * (r8(Cin) + r8(Cout)) * 2, 2 * np * T * Cin * Cout, [&] {
+             return launch_wgrad(dev, n->a[l], Cin, n->dz[cur], Cout, nz, nx, ny, T, n->ones,
+                                 n->part, n->err, s, &nchunk);
            })) != cudaSuccess)
         return cnn_fail(n, e, "cnn wgrad");
-      k_wgrad_sum<<<10, kMaxC * kMaxC, 0, s>>>(n->part, nchunk, Cout, Cin, n->g + n->woff[l]);
+      k_wgrad_sum<<<T + 1, kMaxC * kMaxC, 0, s>>>(n->part, nchunk, Cout, Cin, T,
+                                                  n->g + n->woff[l]);
       n->ctx->stats.launches_total++;
       if (l == 0) break;
       // Input gradient: mirrored taps, transposed weights, then ReLU' of
@@ -795,8 +911,8 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float
       a.out16 = n->dz[cur ^ 1];
       a.mask = n->a[l];
       a.err = n->err;
-      if ((e = timed_launch(n, np * (r8(Cout) + 2 * r8(Cin)) * 2, 2 * np * Cin * 9 * Cout, [&] {
-             return launch_conv(dev, kBwd, r16(Cin), n->dz[cur], r8(Cout), nz, nx, a, s);
+      if ((e = timed_launch(n, np * (r8(Cout) + 2 * r8(Cin)) * 2, 2 * np * Cin * T * Cout, [&] {
+             return launch_conv(dev, kBwd, r16(Cin), n->dz[cur], r8(Cout), nz, nx, ny, T, a, s);
            })) != cudaSuccess)
         return cnn_fail(n, e, "cnn dgrad");
       cur ^= 1;
@@ -814,11 +930,8 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float
   return SW_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int sw_cnn_create(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw_cnn **out) {
+int create_net(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, int taps,
+               sw_cnn **out) {
   if (!c || !channels || !out || nlayers < 1 || nlayers > 16) return SW_BAD_PARAM;
   *out = nullptr;
   for (int l = 0; l <= nlayers; ++l)
@@ -828,18 +941,19 @@ int sw_cnn_create(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw
   sw_cnn *n = new sw_cnn();
   n->ctx = c;
   n->nl = nlayers;
+  n->taps = taps;
   n->ch.assign(channels, channels + nlayers + 1);
   for (int l = 0; l < nlayers; ++l) {
     n->woff.push_back(n->nw);
-    n->nw += (size_t)n->ch[l + 1] * 9 * n->ch[l] + n->ch[l + 1];
+    n->nw += (size_t)n->ch[l + 1] * taps * n->ch[l] + n->ch[l + 1];
   }
   // He initialisation, zero biases.
   std::vector<float> h(n->nw, 0.f);
   std::mt19937_64 rng(seed);
   for (int l = 0; l < nlayers; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
-    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (9.f * Cin)));
-    for (int q = 0; q < Cout * 9 * Cin; ++q) h[n->woff[l] + q] = nd(rng);
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / ((float)taps * Cin)));
+    for (int q = 0; q < Cout * taps * Cin; ++q) h[n->woff[l] + q] = nd(rng);
   }
   auto ck = [](cudaError_t e) { return e == cudaSuccess; };
   bool ok = ck(cudaMalloc(&n->w, n->nw * 4)) && ck(cudaMalloc(&n->g, n->nw * 4)) &&
@@ -849,9 +963,12 @@ int sw_cnn_create(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw
   n->wb.assign(nlayers, nullptr);
   for (int l = 0; l < nlayers && ok; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
-    ok = ck(cudaMalloc(&n->wf[l], (size_t)r16(Cout) * r16(9 * r8(Cin)) * 2)) &&
-         ck(cudaMalloc(&n->wb[l], (size_t)r16(Cin) * r16(9 * r8(Cout)) * 2));
+    ok = ck(cudaMalloc(&n->wf[l], (size_t)r16(Cout) * r16(taps * r8(Cin)) * 2)) &&
+         ck(cudaMalloc(&n->wb[l], (size_t)r16(Cin) * r16(taps * r8(Cout)) * 2));
   }
+  const std::vector<unsigned short> one(8 * kTile, (unsigned short)0x3f80);   // BF16 1.0
+  ok = ok && ck(cudaMalloc(&n->ones, one.size() * 2)) &&
+       ck(cudaMemcpy(n->ones, one.data(), one.size() * 2, cudaMemcpyHostToDevice));
   ok = ok && ck(cudaMemcpy(n->w, h.data(), n->nw * 4, cudaMemcpyHostToDevice)) &&
        ck(cudaMemset(n->m, 0, n->nw * 4)) && ck(cudaMemset(n->v, 0, n->nw * 4)) &&
        ck(cudaMemset(n->err, 0, sizeof(int)));
@@ -864,12 +981,80 @@ int sw_cnn_create(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw
   return SW_OK;
 }
 
+// Shared body of the image (ny = 1, 3 x 3 network) and volume (3 x 3 x 3
+// network) entry points.
+int cnn_forward(sw_cnn *n, int nz, int nx, int ny, const float *in, float *out) {
+  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
+  cudaSetDevice(n->ctx->device);
+  cudaStream_t s = n->ctx->stream;
+  const size_t npix = (size_t)nz * nx * ny;
+  int st = ensure_images(n, npix);
+  if (st) return st;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(n->in32, in, npix * n->ch[0] * 4, cudaMemcpyHostToDevice, s)) !=
+      cudaSuccess)
+    return cnn_fail(n, e, "cnn input");
+  k_pack_input<<<nblk((long long)npix * r8(n->ch[0])), 256, 0, s>>>(n->in32, n->ch[0],
+                                                                     r8(n->ch[0]), (int)npix,
+                                                                     n->a[0]);
+  n->ctx->stats.launches_total++;
+  if ((st = forward(n, nz, nx, ny))) return st;
+  if ((e = cudaMemcpyAsync(out, n->out32, npix * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cnn_fail(n, e, "cnn output");
+  return check_err(n);
+}
+
+int cnn_gradient(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in,
+                 const float *target, float *grad, double *loss) {
+  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
+  cudaSetDevice(n->ctx->device);
+  int st = gradient(n, nbatch, nz, nx, ny, in, target, loss);
+  if (st) return st;
+  if ((st = check_err(n))) return st;
+  std::vector<float> h(n->nw);
+  if (cudaMemcpy(h.data(), n->g, n->nw * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return SW_CUDA_ERR;
+  for (size_t q = 0; q < n->nw; ++q) grad[q] = h[q] / (float)nbatch;
+  return SW_OK;
+}
+
+int cnn_train_step(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in,
+                   const float *target, float lr, double *loss) {
+  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
+  cudaSetDevice(n->ctx->device);
+  cudaStream_t s = n->ctx->stream;
+  int st = gradient(n, nbatch, nz, nx, ny, in, target, loss);
+  if (st) return st;
+  // Adam (b1 0.9, b2 0.999, eps 1e-8) on the batch-mean gradient.
+  n->step += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)n->step), c2 = 1.f - std::pow(b2, (float)n->step);
+  k_adam<<<(int)((n->nw + 255) / 256), 256, 0, s>>>(n->w, n->g, n->m, n->v, (int)n->nw, lr, b1, b2,
+                                                    1e-8f, c1, c2, 1.f / (float)nbatch);
+  n->ctx->stats.launches_total++;
+  if ((st = refresh_bf16(n))) return st;
+  return check_err(n);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sw_cnn_create(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw_cnn **out) {
+  return create_net(c, nlayers, channels, seed, 9, out);
+}
+
+int sw_cnn_create3d(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, sw_cnn **out) {
+  return create_net(c, nlayers, channels, seed, 27, out);
+}
+
 int sw_cnn_destroy(sw_cnn *n) {
   if (!n) return SW_OK;
   cudaSetDevice(n->ctx->device);
   cudaStreamSynchronize(n->ctx->stream);
   free_images(n);
   cudaFree(n->w); cudaFree(n->g); cudaFree(n->m); cudaFree(n->v); cudaFree(n->err);
+  cudaFree(n->ones);
   for (auto p : n->wf) cudaFree(p);
   for (auto p : n->wb) cudaFree(p);
   delete n;
@@ -896,58 +1081,43 @@ int sw_cnn_set_weights(sw_cnn *n, const float *w) {
 
 int sw_cnn_forward(sw_cnn *n, int nz, int nx, const float *in, float *out) {
   if (!n || !in || !out || nz < 1 || nx < 1) return SW_BAD_PARAM;
-  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
-  cudaSetDevice(n->ctx->device);
-  cudaStream_t s = n->ctx->stream;
-  const size_t npix = (size_t)nz * nx;
-  int st = ensure_images(n, npix);
-  if (st) return st;
-  cudaError_t e;
-  if ((e = cudaMemcpyAsync(n->in32, in, npix * n->ch[0] * 4, cudaMemcpyHostToDevice, s)) !=
-      cudaSuccess)
-    return cnn_fail(n, e, "cnn input");
-  k_pack_input<<<nblk((long long)npix * r8(n->ch[0])), 256, 0, s>>>(n->in32, n->ch[0],
-                                                                     r8(n->ch[0]), (int)npix,
-                                                                     n->a[0]);
-  n->ctx->stats.launches_total++;
-  if ((st = forward(n, nz, nx))) return st;
-  if ((e = cudaMemcpyAsync(out, n->out32, npix * 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-    return cnn_fail(n, e, "cnn output");
-  return check_err(n);
+  if (n->taps != 9) return fail(n->ctx, SW_BAD_PARAM, "a 3x3x3 network takes volumes");
+  return cnn_forward(n, nz, nx, 1, in, out);
 }
 
 int sw_cnn_gradient(sw_cnn *n, int nbatch, int nz, int nx, const float *in, const float *target,
                     float *grad, double *loss) {
   if (!n || !in || !target || !grad || nbatch < 1 || nz < 1 || nx < 1) return SW_BAD_PARAM;
-  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
-  cudaSetDevice(n->ctx->device);
-  int st = gradient(n, nbatch, nz, nx, in, target, loss);
-  if (st) return st;
-  if ((st = check_err(n))) return st;
-  std::vector<float> h(n->nw);
-  if (cudaMemcpy(h.data(), n->g, n->nw * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
-    return SW_CUDA_ERR;
-  for (size_t q = 0; q < n->nw; ++q) grad[q] = h[q] / (float)nbatch;
-  return SW_OK;
+  if (n->taps != 9) return fail(n->ctx, SW_BAD_PARAM, "a 3x3x3 network takes volumes");
+  return cnn_gradient(n, nbatch, nz, nx, 1, in, target, grad, loss);
 }
 
 int sw_cnn_train_step(sw_cnn *n, int nbatch, int nz, int nx, const float *in,
                       const float *target, float lr, double *loss) {
   if (!n || !in || !target || nbatch < 1 || nz < 1 || nx < 1) return SW_BAD_PARAM;
-  if (n->ch[n->nl] != 1) return fail(n->ctx, SW_BAD_PARAM, "cnn output must have one channel");
-  cudaSetDevice(n->ctx->device);
-  cudaStream_t s = n->ctx->stream;
-  int st = gradient(n, nbatch, nz, nx, in, target, loss);
-  if (st) return st;
-  // Adam (b1 0.9, b2 0.999, eps 1e-8) on the batch-mean gradient.
-  n->step += 1;
-  const float b1 = 0.9f, b2 = 0.999f;
-  const float c1 = 1.f - std::pow(b1, (float)n->step), c2 = 1.f - std::pow(b2, (float)n->step);
-  k_adam<<<(int)((n->nw + 255) / 256), 256, 0, s>>>(n->w, n->g, n->m, n->v, (int)n->nw, lr, b1, b2,
-                                                    1e-8f, c1, c2, 1.f / (float)nbatch);
-  n->ctx->stats.launches_total++;
-  if ((st = refresh_bf16(n))) return st;
-  return check_err(n);
+  if (n->taps != 9) return fail(n->ctx, SW_BAD_PARAM, "a 3x3x3 network takes volumes");
+  return cnn_train_step(n, nbatch, nz, nx, 1, in, target, lr, loss);
+}
+
+int sw_cnn_forward3d(sw_cnn *n, int nz, int nx, int ny, const float *in, float *out) {
+  if (!n || !in || !out || nz < 1 || nx < 1 || ny < 1) return SW_BAD_PARAM;
+  if (n->taps != 27) return fail(n->ctx, SW_BAD_PARAM, "a 3x3 network takes images");
+  return cnn_forward(n, nz, nx, ny, in, out);
+}
+
+int sw_cnn_gradient3d(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in,
+                      const float *target, float *grad, double *loss) {
+  if (!n || !in || !target || !grad || nbatch < 1 || nz < 1 || nx < 1 || ny < 1)
+    return SW_BAD_PARAM;
+  if (n->taps != 27) return fail(n->ctx, SW_BAD_PARAM, "a 3x3 network takes images");
+  return cnn_gradient(n, nbatch, nz, nx, ny, in, target, grad, loss);
+}
+
+int sw_cnn_train_step3d(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in,
+                        const float *target, float lr, double *loss) {
+  if (!n || !in || !target || nbatch < 1 || nz < 1 || nx < 1 || ny < 1) return SW_BAD_PARAM;
+  if (n->taps != 27) return fail(n->ctx, SW_BAD_PARAM, "a 3x3 network takes images");
+  return cnn_train_step(n, nbatch, nz, nx, ny, in, target, lr, loss);
 }
 
 }  // extern "C"

@@ -104,6 +104,9 @@ def plain_fwi(ctx, sv: Survey, target: float = 0.01, max_evals: int = 60, record
     """L-BFGS (M = 5) until the misfit falls below target * initial misfit
     or max_evals evaluations; when LBFGS stops (IFLAG <= 0, e.g. a failed
     line search) it restarts with empty memory from the current model.
+    Trial models of the line search are clipped to [vmin, vmax] (FREEZE_X
+    on every trial, bound_type 1): an unclipped trial step can leave the
+    velocity range for which the time step is stable.
     record(x, gd, illum) is called at the start model and after every
     completed iteration."""
     from . import LBFGS
@@ -116,7 +119,7 @@ def plain_fwi(ctx, sv: Survey, target: float = 0.01, max_evals: int = 60, record
         record(x.copy(), gd.copy(), il.copy())
     restarts = 0
     while hist.evals < max_evals and f > target * hist.f0 and restarts < 4:
-        lb = LBFGS(ctx, x.size, 5, sv.vmin, sv.vmax, xinit=x)
+        lb = LBFGS(ctx, x.size, 5, sv.vmin, sv.vmax, bound_type=1, xinit=x)
         progressed = False
         try:
             while hist.evals < max_evals and f > target * hist.f0:
@@ -217,7 +220,7 @@ def learned_fwi(ctx, sv: Survey, net, step_scale: float, target: float = 0.01,
     # Plain L-BFGS from the model the learned steps reached.
     restarts = 0
     while hist.evals < max_evals and f > target * hist.f0 and restarts < 4:
-        lb = LBFGS(ctx, x.size, 5, sv.vmin, sv.vmax, xinit=x)
+        lb = LBFGS(ctx, x.size, 5, sv.vmin, sv.vmax, bound_type=1, xinit=x)
         progressed = False
         try:
             while hist.evals < max_evals and f > target * hist.f0:

@@ -27,30 +27,36 @@ def _round_bf16(t):
     return t.to(torch.bfloat16).to(torch.float64)
 
 
-def _unpack(w, channels):
-    """Packed w[co][tap][ci], b[co] per layer -> torch (Cout, Cin, kx, kz) weights."""
+def _unpack(w, channels, three_d=False):
+    """Packed w[co][tap][ci], b[co] per layer -> torch (Cout, Cin, kx, kz) weights
+    (tap = 3*(dx+1) + (dz+1)), or (Cout, Cin, ky, kx, kz) for 3 x 3 x 3 kernels
+    (tap = 9*(dy+1) + 3*(dx+1) + (dz+1))."""
+    taps = 27 if three_d else 9
     out, o = [], 0
     for cin, cout in zip(channels[:-1], channels[1:]):
-        wl = w[o:o + cout * 9 * cin].reshape(cout, 3, 3, cin)   # tap = 3*(dx+1) + (dz+1)
-        o += cout * 9 * cin
+        wl = w[o:o + cout * taps * cin].reshape((cout,) + (3,) * (3 if three_d else 2) + (cin,))
+        o += cout * taps * cin
         b = w[o:o + cout]
         o += cout
-        out.append((np.transpose(wl, (0, 3, 1, 2)).copy(), b.copy()))
+        perm = (0, 4, 1, 2, 3) if three_d else (0, 3, 1, 2)
+        out.append((np.transpose(wl, perm).copy(), b.copy()))
     return out
 
 
-def _ref_forward(x, w, channels, requires_grad=False):
-    """float64 reference of one image x (C, nx, nz): BF16 inputs, weights and
-    activations (straight-through), and with requires_grad the gradient
-    reaching each layer's output rounded to BF16 as the device stores it."""
-    layers = _unpack(w, channels)
+def _ref_forward(x, w, channels, requires_grad=False, three_d=False):
+    """float64 reference of one image x (C, nx, nz) or volume (C, ny, nx, nz):
+    BF16 inputs, weights and activations (straight-through), and with
+    requires_grad the gradient reaching each layer's output rounded to BF16
+    as the device stores it."""
+    layers = _unpack(w, channels, three_d)
+    conv = F.conv3d if three_d else F.conv2d
     h = _bf16(x)[None]
     params = []
     for l, (wl, b) in enumerate(layers):
         wt = _bf16(wl).requires_grad_(requires_grad)
         bt = torch.as_tensor(b, dtype=torch.float64).requires_grad_(requires_grad)
         params += [wt, bt]
-        z = F.conv2d(h, wt, bt, padding=1)
+        z = conv(h, wt, bt, padding=1)
         if requires_grad:
             z.register_hook(_round_bf16)
         if l + 1 < len(layers):
@@ -61,16 +67,17 @@ def _ref_forward(x, w, channels, requires_grad=False):
     return h[0, 0], params
 
 
-def _ref_gradient(x, t, w, channels):
+def _ref_gradient(x, t, w, channels, three_d=False):
     """Batch-mean gradient (packed like the weights) and loss."""
+    perm = (0, 2, 3, 4, 1) if three_d else (0, 2, 3, 1)
     grads, losses = [], []
     for xi, ti in zip(x, t):
-        out, params = _ref_forward(xi, w, channels, requires_grad=True)
+        out, params = _ref_forward(xi, w, channels, requires_grad=True, three_d=three_d)
         loss = 0.5 * torch.mean((out - torch.as_tensor(ti, dtype=torch.float64)) ** 2)
         loss.backward()
         g = []
         for wt, bt in zip(params[0::2], params[1::2]):
-            g.append(np.transpose(wt.grad.numpy(), (0, 2, 3, 1)).ravel())  # [co][tap][ci]
+            g.append(np.transpose(wt.grad.numpy(), perm).ravel())  # [co][tap][ci]
             g.append(bt.grad.numpy().ravel())
         grads.append(np.concatenate(g))
         losses.append(float(loss))
@@ -167,6 +174,65 @@ def test_cnn_training_reduces_loss(ctx):
     finally:
         net.close()
     assert np.isfinite(last) and last < first / 10
+
+
+@pytest.mark.parametrize("ch,shape", [([2, 32, 32, 1], (5, 9, 37)), ([2, 16, 8, 1], (3, 4, 70))])
+def test_cnn3d_forward_and_gradient_match_reference(ctx, ch, shape):
+    """The 3 x 3 x 3 network on volumes (ny, nx, nz): forward output and the
+    weight and bias gradients of a two-volume batch against float64 conv3d
+    with the same BF16 rounding points."""
+    rng = np.random.default_rng(21)
+    ny, nx, nz = shape
+    x = rng.standard_normal((2, ch[0], ny, nx, nz)).astype(np.float32)
+    t = rng.standard_normal((2, ny, nx, nz)).astype(np.float32)
+    net = sw.CNN(ctx, ch, seed=4, three_d=True)
+    try:
+        w = net.get_weights()
+        assert w.size == sum(co * 27 * ci + co for ci, co in zip(ch[:-1], ch[1:]))
+        out = net.forward(x[0])
+        g, loss = net.gradient(x, t)
+    finally:
+        net.close()
+    ref, _ = _ref_forward(x[0], w, ch, three_d=True)
+    ferr = rel_l2(out, ref.detach().numpy())
+    rg, rloss = _ref_gradient(x, t, w, ch, three_d=True)
+    gerr = rel_l2(g, rg)
+    print(f"cnn3d {ch} {shape} forward rel L2 {ferr:.2e}, gradient rel L2 {gerr:.2e}")
+    assert np.abs(out).max() > 0
+    assert ferr < TOL and gerr < TOL
+    assert abs(loss - rloss) <= 1e-3 * rloss
+
+
+def test_cnn3d_training_reduces_loss(ctx):
+    """A 3 x 3 x 3 network learns a 3 x 3 x 3 smoothing of its first channel."""
+    rng = np.random.default_rng(7)
+    nb, ny, nx, nz = 2, 6, 10, 40
+    x = rng.standard_normal((nb, 2, ny, nx, nz)).astype(np.float32)
+    k = np.ones((3, 3, 3), np.float32) / 27.0
+    t = np.stack([F.conv3d(torch.as_tensor(x[i, :1])[None], torch.as_tensor(k)[None, None],
+                           padding=1)[0, 0].numpy() for i in range(nb)])
+    net = sw.CNN(ctx, [2, 16, 16, 1], seed=3, three_d=True)
+    try:
+        first = net.train_step(x, t, lr=3e-3)
+        for _ in range(120):
+            last = net.train_step(x, t, lr=3e-3)
+    finally:
+        net.close()
+    assert np.isfinite(last) and last < first / 10
+
+
+def test_cnn_image_and_volume_entry_points_do_not_mix(ctx):
+    net2, net3 = sw.CNN(ctx, [2, 8, 1]), sw.CNN(ctx, [2, 8, 1], three_d=True)
+    try:
+        with pytest.raises(sw.SwaveError):
+            net3.three_d = False
+            net3.forward(np.zeros((2, 5, 40), np.float32))
+        with pytest.raises(sw.SwaveError):
+            net2.three_d = True
+            net2.forward(np.zeros((2, 3, 5, 40), np.float32))
+    finally:
+        net2.close()
+        net3.close()
 
 
 def test_cnn_rejects_more_than_32_channels(ctx):
