@@ -736,9 +736,12 @@ __global__ void k_counter_add(int *counter, int add) {
 // sub = 1 forms the terms of the second step of a two-step launch (step
 // s_off - 1 + 1 of the counter) into the second block of inj_term.
 __global__ void k_bterms(BatchTables t, int s_off, int sub) {
-  // The previous step kernel still reads the terms this kernel overwrites.
-  pdl_wait();
+  // The next (step) kernel may start at once: it reads nothing this kernel
+  // or the previous step writes before its own wait, which returns only
+  // after this kernel completes - and this kernel completes only after the
+  // previous step kernel, which still reads the terms overwritten here.
   pdl_launch_dependents();
+  pdl_wait();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= t.term_start[t.nshots]) return;
   const int b = find_shot(t.term_start, t.nshots, q);

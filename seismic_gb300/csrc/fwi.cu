@@ -310,6 +310,205 @@ long long sw_revolve_advances_internal(long long l, int s) { return revolve_adva
 // ---------------------------------------------------------------------------
 // compute_fct_gdt
 // ---------------------------------------------------------------------------
+namespace {
+
+// Compute_OF_RES_ADJ (Objective_Function_Residual_Adjsource.f90:17-40) of
+// one shot: the modelled traces dmod become the adjoint source in place,
+// part receives the per-receiver FP64 misfit terms, sh.resid (if given) the
+// residual.
+int shot_residual(sw_ctx *c, const sw_fwi_desc &d, int ntype, const sw_fwi_shot &sh, int nt,
+                  float *dmod, std::vector<double> &part) {
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int st = SW_OK;
+  void *p = nullptr;
+  float *ddobs = nullptr, *dmute = nullptr, *dres = nullptr;
+  if ((st = upload(c, "dobs", sh.dobs, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
+  ddobs = (float *)p;
+  if (sh.mute) {
+    if ((st = upload(c, "mute", sh.mute, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
+    dmute = (float *)p;
+  }
+  if (sh.resid) {
+    dres = (float *)dbuf(c, "resid", (size_t)sh.nrec * nt * sizeof(float), &st);
+    if (!dres) return st;
+  }
+  double *dpart = (double *)dbuf(c, "fpart", (size_t)sh.nrec * sizeof(double), &st);
+  if (!dpart) return st;
+  if (ntype == SW_NRM_L2) {
+    if ((e = launch_residual(sh.nrec, nt, ddobs, dmute, dmod, dres, dpart, s)) != cudaSuccess)
+      return cuda_fail(c, e, "residual");
+    c->stats.launches_total++;
+  } else {
+    float *dmax = (float *)dbuf(c, "fmaxabs", (size_t)sh.nrec * sizeof(float), &st);
+    if (!dmax) return st;
+    if ((e = launch_residual_nrm(ntype, d.dat_thresh, sh.nrec, nt, ddobs, dmute, dmod, dres,
+                                 dpart, dmax, s)) != cudaSuccess)
+      return cuda_fail(c, e, "residual");
+    c->stats.launches_total += (ntype != SW_NRM_L1 && d.dat_thresh == 0.f) ? 2 : 1;
+  }
+  part.resize(sh.nrec);
+  if ((st = download(c, part.data(), dpart, (size_t)sh.nrec * sizeof(double)))) return st;
+  if (sh.resid && (st = download(c, sh.resid, dres, (size_t)sh.nrec * nt * sizeof(float))))
+    return st;
+  return SW_OK;
+}
+
+constexpr int kFwiBatch = 16;   // shots per batch of the store-all gradient
+
+// The store-all gradient (every snapshot of a shot in HBM) for several
+// shots at a time: shots are admitted into a batch by device-memory
+// footprint (like the RTM job), the batch's forward passes (AMOD_to_memory)
+// run as one multi-shot propagation, then each shot's residual, then the
+// backward passes with the AFWI imaging condition (AGRAD_to_memory) as one
+// propagation, then the windowed images are added into the full grid in
+// shot order (mod_copy_image).  Per shot the operations are those of the
+// one-shot loop, so misfit and gradient equal it bit for bit.
+int fct_gdt_batched(sw_ctx *c, const sw_fwi_desc &d, int ntype, const float *vel,
+                    const float *dvel, const float *dwav, int nshot, const sw_fwi_shot *shots,
+                    float *dgrad, float *dill, double &fsum, long long &ntotal) {
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  int st = SW_OK;
+  const sw_genpar &G = d.g;
+  const int nt = G.nt;
+  struct Info {
+    Window w;
+    sw_genpar g;
+    size_t nw, nf;
+    int ntsnap;
+  };
+  std::vector<Info> info(nshot);
+  for (int is = 0; is < nshot; ++is) {
+    const sw_fwi_shot &sh = shots[is];
+    if (!sh.dobs) return fail(c, SW_BAD_PARAM, "shot %d without observed data", is);
+    Info &I = info[is];
+    if ((st = compute_window(c, G, d.aperture_x, d.aperture_y, sh.sou_coord, sh.nrec,
+                             sh.rec_coord, I.w)))
+      return st;
+    I.g = G;
+    I.g.nx = I.w.nxw;
+    I.g.ny = I.w.nyw;
+    I.g.ox = I.w.oxw;
+    I.g.oy = I.w.oyw;
+    I.nw = (size_t)I.g.nz * I.g.nx * I.g.ny;
+    I.nf = (size_t)make_geom(I.g).total();
+    I.ntsnap = nt / I.g.snapi;
+  }
+  auto r256 = [](size_t b) { return (b + 255) / 256 * 256; };
+  auto arena_of = [&](int is) -> size_t {
+    const Info &I = info[is];
+    return r256(I.nw * 4) * 3 + r256(I.nf * 4) +
+           r256(I.nw * (size_t)std::max(I.ntsnap, 1) * 4) + r256((size_t)shots[is].nrec * nt * 4);
+  };
+  std::vector<std::vector<float>> hv;
+  std::vector<double> part;
+  int next = 0;
+  while (next < nshot) {
+    size_t freeb = 0, totalb = 0;
+    SW_CK(cudaMemGetInfo(&freeb, &totalb));
+    size_t held = 0;
+    auto it = c->bufs.find("fwi_arena");
+    if (it != c->bufs.end()) held = it->second.cap;
+    const double budget = (double)(freeb + held) * 0.85;
+    int end = next;
+    size_t need = 0, arena = 0;
+    while (end < nshot && end - next < kFwiBatch) {
+      const size_t a = arena_of(end), b = a + info[end].nf * 4 * 7;   // + run_phases fields
+      if (end > next && (double)(need + b) > budget) break;
+      need += b;
+      arena += a;
+      ++end;
+    }
+    if ((double)need > budget)
+      return fail(c, SW_OOM_ADMISSION, "shot %d needs %zu bytes, budget %.0f", next, need, budget);
+    char *cur = (char *)dbuf(c, "fwi_arena", arena, &st);
+    if (!cur) return st;
+    const int nb = end - next;
+    std::vector<PhaseShot> fwd(nb), bwd(nb);
+    std::vector<float *> rtr(nb), img(nb), ill(nb);
+    hv.assign(nb, {});
+    for (int q = 0; q < nb; ++q) {
+      const int is = next + q;
+      const Info &I = info[is];
+      const sw_fwi_shot &sh = shots[is];
+      float *vsmall = (float *)cur; cur += r256(I.nw * 4);
+      float *vpad = (float *)cur; cur += r256(I.nf * 4);
+      img[q] = (float *)cur; cur += r256(I.nw * 4);
+      ill[q] = (float *)cur; cur += r256(I.nw * 4);
+      float *wave = (float *)cur; cur += r256(I.nw * (size_t)std::max(I.ntsnap, 1) * 4);
+      rtr[q] = (float *)cur; cur += r256((size_t)sh.nrec * nt * 4);
+      // copy_window_vel_gath: window the model on the device, then pad.
+      if ((e = launch_window_vel(G.nz, G.nx, G.ny, G.ox, G.oy, G.dx, G.dy, I.w.nxw, I.w.nyw,
+                                 I.w.oxw, I.w.oyw, dvel, vsmall, s)) != cudaSuccess)
+        return cuda_fail(c, e, "window vel");
+      if ((e = launch_pad_velocity(make_geom(I.g), vsmall, vpad, s)) != cudaSuccess)
+        return cuda_fail(c, e, "pad");
+      c->stats.launches_total += 2;
+      SW_CK(cudaMemsetAsync(rtr[q], 0, (size_t)sh.nrec * nt * 4, s));
+      SW_CK(cudaMemsetAsync(wave, 0, I.nw * (size_t)std::max(I.ntsnap, 1) * 4, s));
+      SW_CK(cudaMemsetAsync(img[q], 0, I.nw * 4, s));
+      SW_CK(cudaMemsetAsync(ill[q], 0, I.nw * 4, s));
+      window_host(G, I.w, vel, hv[q]);
+      // AMOD_to_memory (to_disk_to_memory_AMOD.f90:27-82).
+      PhaseShot &F = fwd[q];
+      std::memset(&F.d, 0, sizeof(F.d));
+      F.d.g = I.g;
+      F.d.tmin = 1; F.d.tmax = nt; F.d.tstep = 1;
+      F.d.fd_scheme = SW_FD_FORWARD;
+      F.d.injection = SW_INJ_SINC;
+      F.d.extraction = SW_EXT_SIMPLE_AFWI;
+      F.d.extract_wave = 1;
+      F.io.vel_pad = vpad;
+      F.io.vel_phys_host = hv[q].data();
+      F.io.nsou = 1;
+      F.io.sou_coord = sh.sou_coord;
+      F.io.sou_trace_dev = dwav;
+      F.io.nrec = sh.nrec;
+      F.io.rec_coord = sh.rec_coord;
+      F.io.rec_trace_dev = rtr[q];
+      F.io.wave_dev = wave;
+      // AGRAD_to_memory (to_disk_to_memory_AGRAD.f90:27-79).
+      PhaseShot &B = bwd[q];
+      std::memset(&B.d, 0, sizeof(B.d));
+      B.d.g = I.g;
+      B.d.tmin = nt; B.d.tmax = 1; B.d.tstep = -1;
+      B.d.fd_scheme = SW_FD_FORWARD;
+      B.d.injection = SW_INJ_SIMPLE;
+      B.d.imaging = SW_IMG_AFWI;
+      B.io.vel_pad = vpad;
+      B.io.vel_phys_host = hv[q].data();
+      B.io.nsou = sh.nrec;
+      B.io.sou_coord = sh.rec_coord;
+      B.io.sou_trace_dev = rtr[q];
+      B.io.wave_dev = wave;
+      B.io.image_dev = img[q];
+      B.io.illum_dev = ill[q];
+    }
+    if ((st = run_phases(c, fwd, c->run_opts))) return st;
+    std::vector<std::vector<double>> parts(nb);
+    for (int q = 0; q < nb; ++q)
+      if ((st = shot_residual(c, d, ntype, shots[next + q], nt, rtr[q], parts[q]))) return st;
+    if ((st = run_phases(c, bwd, c->run_opts))) return st;
+    // mod_copy_image (ExtractPadModel.f90:662-697), shots in order.
+    for (int q = 0; q < nb; ++q) {
+      const Info &I = info[next + q];
+      if ((e = launch_copy_image(G.nz, G.nx, G.ny, G.ox, G.oy, G.dx, G.dy, I.w.nxw, I.w.nyw,
+                                 I.w.oxw, I.w.oyw, img[q], ill[q], dgrad, dill, s)) !=
+          cudaSuccess)
+        return cuda_fail(c, e, "copy image");
+      c->stats.launches_total++;
+      for (int r = 0; r < shots[next + q].nrec; ++r) fsum = fsum + parts[q][r];
+      ntotal += shots[next + q].nrec;
+    }
+    SW_CK(cudaStreamSynchronize(s));
+    next = end;
+  }
+  return SW_OK;
+}
+
+}  // namespace
+
 int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const float *wavelet,
                    int nshot, const sw_fwi_shot *shots, const float *vpmask, double *f,
                    float *grad, float *illum) {
@@ -341,7 +540,12 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
   long long ntotal = 0;
   std::vector<float> hv;
   std::vector<double> part;
-  for (int is = 0; is < nshot; ++is) {
+  // Every snapshot in HBM: several shots per propagation.
+  const bool batched = d.checkpoint_snaps <= 0 && nshot > 1;
+  if (batched &&
+      (st = fct_gdt_batched(c, d, ntype, vel, dvel, dwav, nshot, shots, dgrad, dill, fsum, ntotal)))
+    return st;
+  for (int is = 0; is < (batched ? 0 : nshot); ++is) {
     const sw_fwi_shot &sh = shots[is];
     Window w;
     if ((st = compute_window(c, G, d.aperture_x, d.aperture_y, sh.sou_coord, sh.nrec, sh.rec_coord, w)))
@@ -427,36 +631,7 @@ int sw_fwi_fct_gdt(sw_ctx *c, const sw_fwi_desc *dp, const float *vel, const flo
     // with the binomial schedule it runs once the first pass has reached
     // the end of the record.
     auto residual = [&]() -> int {
-    float *ddobs = nullptr, *dmute = nullptr, *dres = nullptr;
-    if ((st = upload(c, "dobs", sh.dobs, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
-    ddobs = (float *)p;
-    if (sh.mute) {
-      if ((st = upload(c, "mute", sh.mute, (size_t)sh.nrec * nt * sizeof(float), &p))) return st;
-      dmute = (float *)p;
-    }
-    if (sh.resid) {
-      dres = (float *)dbuf(c, "resid", (size_t)sh.nrec * nt * sizeof(float), &st);
-      if (!dres) return st;
-    }
-    double *dpart = (double *)dbuf(c, "fpart", (size_t)sh.nrec * sizeof(double), &st);
-    if (!dpart) return st;
-    if (ntype == SW_NRM_L2) {
-      if ((e = launch_residual(sh.nrec, nt, ddobs, dmute, a.rec_trace_dev, dres, dpart, s)) !=
-          cudaSuccess)
-        return cuda_fail(c, e, "residual");
-      c->stats.launches_total++;
-    } else {
-      float *dmax = (float *)dbuf(c, "fmaxabs", (size_t)sh.nrec * sizeof(float), &st);
-      if (!dmax) return st;
-      if ((e = launch_residual_nrm(ntype, d.dat_thresh, sh.nrec, nt, ddobs, dmute,
-                                   a.rec_trace_dev, dres, dpart, dmax, s)) != cudaSuccess)
-        return cuda_fail(c, e, "residual");
-      c->stats.launches_total += (ntype != SW_NRM_L1 && d.dat_thresh == 0.f) ? 2 : 1;
-    }
-    part.resize(sh.nrec);
-    if ((st = download(c, part.data(), dpart, (size_t)sh.nrec * sizeof(double)))) return st;
-    if (sh.resid && (st = download(c, sh.resid, dres, (size_t)sh.nrec * nt * sizeof(float)))) return st;
-    return SW_OK;
+      return shot_residual(c, d, ntype, sh, nt, a.rec_trace_dev, part);
     };
     if (!revolve && (st = residual())) return st;
     // AGRAD_to_memory (to_disk_to_memory_AGRAD.f90:27-79).

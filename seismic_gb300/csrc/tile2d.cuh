@@ -139,19 +139,33 @@ __device__ __forceinline__ int t2_x0(const T2Shot &h, int e) {
 // cells before the compute domain), so they may be negative for the first
 // tiles; elements outside the array read 0 and only feed outputs that are
 // never stored.  The row coordinate is a multiple of 4 (16 bytes).
+// The copies split in two: t2_issue_old (the whole stage's byte count,
+// then every input that older launches wrote: u1, u0, u_1 and the
+// velocity) and t2_issue_u2 (u2, the level the previous launch writes).
 template <bool ADJ>
-__device__ __forceinline__ void t2_issue(const T2Maps &M, const T2Shot &h, int s, int e,
-                                         float *st, unsigned long long *bar) {
+__device__ __forceinline__ void t2_issue_old(const T2Maps &M, const T2Shot &h, int s, int e,
+                                             float *st, unsigned long long *bar) {
   constexpr unsigned bytes = 4u * (unsigned)t2_stage_floats<ADJ>();
   const int zi = t2_tzi(e) * T2_Z - h.off1, xi = t2_txi(e) * T2_X - h.off2;
   mbar_expect_tx(bar, bytes);
-  tma_2d(st, &M.m[2 * ((s + 3) % 5)], zi, xi, bar);
   if (ADJ) tma_2d(st + T2_HALO, &M.m[10], zi, xi, bar);
   float *cst = st + (ADJ ? 2 : 1) * T2_HALO;
   tma_2d(cst, &M.m[2 * ((s + 2) % 5) + 1], zi + 4, xi + 4, bar);
   tma_2d(cst + T2_CORE, &M.m[2 * ((s + 1) % 5) + 1], zi + 4, xi + 4, bar);
   tma_2d(cst + 2 * T2_CORE, &M.m[2 * (s % 5) + 1], zi + 4, xi + 4, bar);
   if (!ADJ) tma_2d(cst + 3 * T2_CORE, &M.m[11], zi + 4, xi + 4, bar);
+}
+template <bool ADJ>
+__device__ __forceinline__ void t2_issue_u2(const T2Maps &M, const T2Shot &h, int s, int e,
+                                            float *st, unsigned long long *bar) {
+  const int zi = t2_tzi(e) * T2_Z - h.off1, xi = t2_txi(e) * T2_X - h.off2;
+  tma_2d(st, &M.m[2 * ((s + 3) % 5)], zi, xi, bar);
+}
+template <bool ADJ>
+__device__ __forceinline__ void t2_issue(const T2Maps &M, const T2Shot &h, int s, int e,
+                                         float *st, unsigned long long *bar) {
+  t2_issue_old<ADJ>(M, h, s, e, st, bar);
+  t2_issue_u2<ADJ>(M, h, s, e, st, bar);
 }
 
 __device__ __forceinline__ float f4get(const float4 &a, int e) {
@@ -707,10 +721,10 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
       *abort_flag = 0;
     }
   }
-  // Everything after this reads what the previous kernels of the step
-  // sequence wrote (fields, injection terms, the step counter).
-  pdl_wait();
-  pdl_launch_dependents();
+  // Before the wait on the previous kernel: the step counter (changed only
+  // between replays of a chunk of steps), the per-shot step scalars, this
+  // step's tile list and the first tile's copies of the levels that older
+  // launches wrote; this overlaps the tail of the previous step's kernel.
   const int s = *t.counter + s_off;
   __syncthreads();
   if (tid < t.nshots) steps[tid] = t2_step_of<ADJ>(t, shots[tid], tid, s);
@@ -724,9 +738,16 @@ __device__ __forceinline__ void tile2d_persistent(const BatchTables &t, int s_of
     }
     *nlist = n;
     if (n > 0)
-      t2_issue<ADJ>(t.t2maps[t2_b(list[0])], shots[t2_b(list[0])], s, list[0], t2_smem,
-                    &full[0]);
+      t2_issue_old<ADJ>(t.t2maps[t2_b(list[0])], shots[t2_b(list[0])], s, list[0], t2_smem,
+                        &full[0]);
   }
+  // Everything after this reads what the previous kernels of the step
+  // sequence wrote (u2, injection terms, the image of the last step).
+  pdl_wait();
+  pdl_launch_dependents();
+  if (tid == 0 && *nlist > 0)
+    t2_issue_u2<ADJ>(t.t2maps[t2_b(list[0])], shots[t2_b(list[0])], s, list[0], t2_smem,
+                     &full[0]);
   __syncthreads();
   const int n = *nlist;
   for (int k = 0; k < n; ++k) {
