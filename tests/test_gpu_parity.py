@@ -74,6 +74,26 @@ def test_rtm_bitexact(ctx, oracle, twoD):
     np.testing.assert_array_equal(il, ril)
 
 
+@pytest.mark.parametrize("nz", [32, 28])
+def test_rtm_lsrtm_3d_vector_snapshot_path(ctx, oracle, nz):
+    """3D RTM and LSRTM where every column's snapshot rows are 16-byte
+    aligned (nz = 32, 28 with an 8-cell taper: the 16-byte snapshot and
+    imaging accesses of the step kernel) against the oracle, bit for bit;
+    case3d's nz = 30 mixes aligned and unaligned columns."""
+    g, vel, sou, rec, w = case3d(nz=nz, nt=80)
+    data = oracle.modeling(g, vel, sou, w, rec)
+    im, il = ctx.rtm(g, vel, sou, w, rec, data)
+    rim, ril = oracle.rtm(g, vel, sou, w, rec, data)
+    assert np.abs(rim).max() > 0
+    np.testing.assert_array_equal(im, rim)
+    np.testing.assert_array_equal(il, ril)
+    w2 = sw.born_wavelet(w, g.dt)
+    im, il = ctx.lsrtm(g, vel, sou, w2, rec, data)
+    rim, ril = oracle.lsrtm(g, vel, sou, w2, rec, data)
+    np.testing.assert_array_equal(im, rim)
+    np.testing.assert_array_equal(il, ril)
+
+
 @pytest.mark.parametrize("twoD", [True, False])
 def test_born_lsrtm_bitexact(ctx, oracle, twoD):
     g, vel, sou, rec, w = case2d(nt=240) if twoD else case3d(nt=80)
