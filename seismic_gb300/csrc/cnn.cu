@@ -4,14 +4,14 @@
 // direction, with training and inference on the GPU.
 //
 // Activations and gradients are BF16 in channel-group planes: the channel
-// count is rounded up to 8 (zeros above the layer's own count) and group g
+// count is rounded up to 16 (zeros above the layer's own count) and group g
 // of 8 channels is a plane [x][z][8] of the image (pixel p = x * nz + z), so
 // element (p, c) sits at ((c / 8) * npix + p) * 8 + c % 8.  One GEMM tile is
-// a 32 (z) x 4 (x) patch of 128 pixels; an 8-channel slice of it, shifted by
-// a tap, is one tensor copy of 4 contiguous 512-byte rows (zero fill outside
-// the image) that lands in shared memory as 128 rows of 16 bytes - exactly
-// one K column of core matrices of the tensor cores' no-swizzle layout
-// (umma.cuh).
+// a 32 (z) x 4 (x) patch of 128 pixels; the 8-channel slice of a tap-shifted
+// patch is 4 contiguous 512-byte rows that land in shared memory as 128 rows
+// of 16 bytes - exactly one K column of core matrices of the tensor cores'
+// no-swizzle layout (umma.cuh) - and one tensor copy fetches the slices of
+// all channel groups of a tap (zero fill outside the image).
 //
 // * Convolution (forward, and the input gradient with mirrored taps and
 //   transposed weights): implicit GEMM D[pixel][n] = sum over (tap,
@@ -53,7 +53,10 @@ constexpr int kTile = kTZ * kTX;          // 128 pixels = GEMM M
 constexpr int kChunk = kTile * 16;        // one 8-channel slice: 2048 bytes
 constexpr int kWgradSlots = 28 * kMaxC * kMaxC;   // partial sums per CTA (27 taps + bias)
 
-int r8(int c) { return (c + 7) / 8 * 8; }
+int r16(int c);
+// Stored channels of a tensor: a multiple of 16, so that one tap of a
+// layer's input is a whole number of K = 16 steps.
+int cstore(int c) { return (c + 15) / 16 * 16; }
 int r16(int c) { return (c + 15) / 16 * 16; }
 
 __device__ __forceinline__ unsigned char *align1024(unsigned char *p) {
@@ -135,21 +138,19 @@ __device__ __forceinline__ void cnn_bar_init(unsigned long long *bar, unsigned c
 //   D[p][n] = sum_{tap, c} in[p + s * off(tap)][c] * W[n][tap * Cs + c]
 // with s = +1 (forward) or -1 (input gradient) and zero padding outside
 // the image.  W: NP x kp BF16 in the tensor cores' K-major layout.  One
-// ring stage holds two 8-channel slices (one K = 16 step, 4 KB); the
-// slices of a tile run over (tap, channel group), and the K padding slice
-// (when 9 Cs / 8 is odd) is a copy from far outside the image (all zero).
-// Two accumulators in tensor memory let the products of the next tile run
+// ring stage holds one tap: the Cs / 8 channel-group slices of the shifted
+// patch, fetched by a single tensor copy (Cs / 16 K = 16 steps).  Two
+// accumulators in tensor memory let the products of the next tile run
 // while the epilogue reads the last one.
 // ---------------------------------------------------------------------------
 enum { kFwdHidden = 0, kFwdLast = 1, kBwd = 2 };
-constexpr int kConvStage = 2 * kChunk;
 constexpr int kMaxRing = 32;
 
 struct ConvArgs {
-  int Cs;                        // stored input channels (multiple of 8)
+  int Cs;                        // stored input channels (multiple of 16)
   int nz, nx, ny;
   int taps;                      // 9 (2D) or 27 (3D)
-  int kp;                        // GEMM K: taps Cs rounded up to 16
+  int kp;                        // GEMM K: taps Cs
   int ntiles, tiles_z, tiles_x;
   int mirror;
   int ring;                      // shared-memory stages (<= kMaxRing)
@@ -164,8 +165,8 @@ struct ConvArgs {
 };
 
 __host__ __device__ inline size_t conv_wbytes(int NP, int kp) { return ((size_t)NP * kp * 2 + 1023) / 1024 * 1024; }
-size_t conv_smem_bytes(int NP, int kp, int ring) {
-  return 1024 + conv_wbytes(NP, kp) + (size_t)ring * kConvStage;
+size_t conv_smem_bytes(int NP, int kp, int Cs, int ring) {
+  return 1024 + conv_wbytes(NP, kp) + (size_t)ring * (Cs / 8) * kChunk;
 }
 
 template <int NP, int MODE>
@@ -178,8 +179,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   __shared__ volatile int abort_flag;
   __shared__ volatile int mma_stages;             // stages the MMA warp has consumed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nst = A.kp / 16;                      // ring stages per tile
-  const int nload = A.taps * (A.Cs / 8);          // slices with data
+  const int nst = A.taps;                         // ring stages (taps) per tile
+  const size_t sbytes = (size_t)(A.Cs / 8) * kChunk;   // one tap
   unsigned char *base = align1024(cnn_smem);
   unsigned char *sW = base;
   unsigned char *ring = base + conv_wbytes(NP, A.kp);
@@ -209,7 +210,6 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   if (warp == kProducerWarp) {
     if (lane == 0) {
       const int sgn = A.mirror ? -1 : 1;
-      const int ng = A.Cs / 8;
       int q = 0;
       bool ok = true;
       for (int i = 0; i < nmine && ok; ++i) {
@@ -220,21 +220,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           const int slot = q % A.ring;
           if (q >= A.ring && !(ok = cnn_wait(&empty[slot], ((q / A.ring) - 1) & 1, &abort_flag)))
             break;
-          unsigned char *dst = ring + (size_t)slot * kConvStage;
-          cnn_expect_tx(&full[slot], kConvStage);
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int c = 2 * k + h;
-            if (c < nload) {
-              const int tap = c / ng, cg = c % ng;
-              int dz, dx, dy;
-              tap_off(tap, A.taps, dz, dx, dy);
-              cnn_tma4(dst + h * kChunk, &amap, cg, z0 + sgn * dz, x0 + sgn * dx, y0 + sgn * dy,
-                       &full[slot]);
-            } else {
-              cnn_tma4(dst + h * kChunk, &amap, 0, -(1 << 20), -(1 << 20), 0, &full[slot]);
-            }
-          }
+          unsigned char *dst = ring + (size_t)slot * sbytes;
+          cnn_expect_tx(&full[slot], (unsigned)sbytes);
+          int dz, dx, dy;
+          tap_off(k, A.taps, dz, dx, dy);
+          cnn_tma4(dst, &amap, 0, z0 + sgn * dz, x0 + sgn * dx, y0 + sgn * dy, &full[slot]);
         }
       }
       if (!ok) {
@@ -263,10 +253,13 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           if (!(ok = cnn_wait(&full[slot], (q / A.ring) & 1, &abort_flag))) break;
           mma_stages = q + 1;
           umma_fence_after();
-          const unsigned sa = umma_su32(ring + (size_t)slot * kConvStage);
-          const uint64_t ad = umma_smem_desc(sa, kChunk, 128);
-          const uint64_t bd = umma_smem_desc(sb + k * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
-          umma_bf16(d, ad, bd, idesc, k > 0);
+          const unsigned sa = umma_su32(ring + (size_t)slot * sbytes);
+          for (int h = 0; h < A.Cs / 16; ++h) {
+            const int ks = k * (A.Cs / 16) + h;
+            const uint64_t ad = umma_smem_desc(sa + h * 2 * kChunk, kChunk, 128);
+            const uint64_t bd = umma_smem_desc(sb + ks * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
+            umma_bf16(d, ad, bd, idesc, ks > 0);
+          }
           umma_commit(&empty[slot]);
         }
         if (!ok) break;
@@ -415,19 +408,19 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           unsigned char *dst = ring + (size_t)slot * kWgradStage;
           const int g1 = min(16 * j + 16, G + 1);
           cnn_expect_tx(&full[slot], (unsigned)((g1 - 16 * j + A.Cso / 8) * kChunk));
-          for (int g = 16 * j; g < g1; ++g) {
+          // One tensor copy per tap (its ng channel-group slices; 16 is a
+          // multiple of ng), the ones slice, then the gradient's slices.
+          for (int g = 16 * j; g < g1; g += (g < G ? ng : 1)) {
             unsigned char *gd = dst + (size_t)(g - 16 * j) * kChunk;
             if (g < G) {
-              const int tap = g / ng, cg = g % ng;
               int dz, dx, dy;
-              tap_off(tap, A.taps, dz, dx, dy);
-              cnn_tma4(gd, &amap, cg, z0 + dz, x0 + dx, y0 + dy, &full[slot]);
+              tap_off(g / ng, A.taps, dz, dx, dy);
+              cnn_tma4(gd, &amap, 0, z0 + dz, x0 + dx, y0 + dy, &full[slot]);
             } else {
               cnn_tma4(gd, &onemap, 0, 0, 0, 0, &full[slot]);
             }
           }
-          for (int cg = 0; cg < A.Cso / 8; ++cg)
-            cnn_tma4(dst + (size_t)(16 + cg) * kChunk, &dmap, cg, z0, x0, y0, &full[slot]);
+          cnn_tma4(dst + (size_t)16 * kChunk, &dmap, 0, z0, x0, y0, &full[slot]);
         }
       }
       if (!ok) {
@@ -538,8 +531,9 @@ __global__ void k_pack_input(const float *__restrict__ in, int C, int Cs, int np
 }
 
 // Mean-square loss of a one-channel output: the output gradient
-// (out - target) / npix as BF16 in channel 0 of one 8-channel plane, and
-// per-block FP64 partial sums of (out - target)^2.
+// (out - target) / npix as BF16 in channel 0 of a 16-channel tensor (two
+// planes, zero elsewhere), and per-block FP64 partial sums of
+// (out - target)^2.
 __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ tgt, int npix,
                        __nv_bfloat16 *__restrict__ db, double *__restrict__ part) {
   __shared__ double red[256];
@@ -547,7 +541,9 @@ __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ 
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
     const float e = out[p] - tgt[p];
     s += (double)e * (double)e;
-    *reinterpret_cast<uint4 *>(db + (size_t)p * 8) = make_uint4(pack_bf16(e / (float)npix, 0.f), 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(db + (size_t)p * 8) =
+        make_uint4(pack_bf16(e / (float)npix, 0.f), 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(db + ((size_t)npix + p) * 8) = make_uint4(0u, 0u, 0u, 0u);
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -597,16 +593,17 @@ __global__ void k_weights_bf16(const float *__restrict__ w, int Cout, int Cin, i
 int nblk(long long n) { return (int)std::min<long long>(4096, (n + 255) / 256); }
 
 // BF16 tensor map over Cs / 8 channel-group planes: dimensions (8 nz: z
-// and the 8 channels flattened, nx, ny, Cs / 8), box 8 kTZ x kTX x 1 x 1
-// (kTX rows of 512 bytes), zero fill outside.
-bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx, int ny) {
+// and the 8 channels flattened, nx, ny, Cs / 8), box 8 kTZ x kTX x 1 x
+// planes (kTX rows of 512 bytes per plane), zero fill outside.
+bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx, int ny,
+                    int planes) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
   const cuuint64_t dims[4] = {(cuuint64_t)nz * 8, (cuuint64_t)nx, (cuuint64_t)ny,
                               (cuuint64_t)Cs / 8};
   const cuuint64_t strides[3] = {(cuuint64_t)nz * 16, (cuuint64_t)nz * nx * 16,
                                  (cuuint64_t)nz * nx * ny * 16};
-  const cuuint32_t box[4] = {8 * kTZ, kTX, 1, 1};
+  const cuuint32_t box[4] = {8 * kTZ, kTX, 1, (cuuint32_t)planes};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(base), dims,
              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -634,7 +631,7 @@ cudaError_t launch_big(K kernel, int grid, size_t smem, cudaStream_t s, const CU
 cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int Cs, int nz, int nx,
                         int ny, int taps, ConvArgs a, cudaStream_t s) {
   CUtensorMap m;
-  if (!encode_act_map(&m, in, Cs, nz, nx, ny)) return cudaErrorInvalidValue;
+  if (!encode_act_map(&m, in, Cs, nz, nx, ny, Cs / 8)) return cudaErrorInvalidValue;
   a.Cs = Cs;
   a.nz = nz;
   a.nx = nx;
@@ -644,10 +641,11 @@ cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int 
   a.tiles_z = (nz + kTZ - 1) / kTZ;
   a.tiles_x = (nx + kTX - 1) / kTX;
   a.ntiles = a.tiles_z * a.tiles_x * ny;
-  // A ring of about 110 KB per CTA: two CTAs per SM.
-  a.ring = (int)std::min<size_t>(kMaxRing, (110u * 1024u - 1024u - conv_wbytes(NP, a.kp)) /
-                                               kConvStage);
-  const size_t smem = conv_smem_bytes(NP, a.kp, a.ring);
+  // A ring of about 110 KB per CTA (two CTAs per SM); stages of one tap.
+  const size_t stage = (size_t)(Cs / 8) * kChunk;
+  a.ring = (int)std::max<size_t>(
+      2, std::min<size_t>(kMaxRing, (110u * 1024u - 1024u - conv_wbytes(NP, a.kp)) / stage));
+  const size_t smem = conv_smem_bytes(NP, a.kp, Cs, a.ring);
   const int per_sm = std::max<int>(1, std::min<int>(2, (int)((227u * 1024u) / smem)));
   const int grid = std::min(a.ntiles, num_sms(dev) * per_sm);
   if (NP == 16) {
@@ -666,9 +664,9 @@ cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bf
                          const __nv_bfloat16 *ones, float *part, int *err, cudaStream_t s,
                          int *nchunk) {
   WgradArgs w;
-  w.Csi = r8(Cin);
+  w.Csi = cstore(Cin);
   w.Cin = Cin;
-  w.Cso = r8(Cout);
+  w.Cso = cstore(Cout);
   w.Cout = Cout;
   w.nz = nz;
   w.nx = nx;
@@ -682,8 +680,9 @@ cudaError_t launch_wgrad(int dev, const __nv_bfloat16 *a, int Cin, const __nv_bf
   w.part = part;
   w.err = err;
   CUtensorMap ma, md, mo;
-  if (!encode_act_map(&ma, a, w.Csi, nz, nx, ny) || !encode_act_map(&md, dz, w.Cso, nz, nx, ny) ||
-      !encode_act_map(&mo, ones, 8, kTZ, kTX, 1))
+  if (!encode_act_map(&ma, a, w.Csi, nz, nx, ny, w.Csi / 8) ||
+      !encode_act_map(&md, dz, w.Cso, nz, nx, ny, w.Cso / 8) ||
+      !encode_act_map(&mo, ones, 8, kTZ, kTX, 1, 1))
     return cudaErrorInvalidValue;
   const int NPO = r16(Cout);
   const size_t smem = wgrad_smem_bytes(w.ring);
@@ -718,8 +717,8 @@ struct sw_cnn {
   int step = 0;
   // Per-image buffers (grow-only).
   size_t cap = 0;
-  std::vector<__nv_bfloat16 *> a;      // layer inputs, r8(ch[l]) / 8 channel-group planes
-  __nv_bfloat16 *dz[2] = {nullptr, nullptr};   // gradients, up to r8(max ch) / 8 planes
+  std::vector<__nv_bfloat16 *> a;      // layer inputs, cstore(ch[l]) / 8 channel-group planes
+  __nv_bfloat16 *dz[2] = {nullptr, nullptr};   // gradients, up to cstore(max ch) / 8 planes
   float *out32 = nullptr, *in32 = nullptr, *tgt = nullptr, *part = nullptr;
   double *lpart = nullptr;
   int *err = nullptr;
@@ -749,10 +748,10 @@ int ensure_images(sw_cnn *n, size_t npix) {
   auto ck = [&](cudaError_t e) { return e == cudaSuccess; };
   bool ok = true;
   int cmax = 8;
-  for (int c : n->ch) cmax = std::max(cmax, r8(c));
+  for (int c : n->ch) cmax = std::max(cmax, cstore(c));
   n->a.assign(n->nl, nullptr);
   for (int l = 0; l < n->nl && ok; ++l)
-    ok = ck(cudaMalloc(&n->a[l], npix * r8(n->ch[l]) * sizeof(__nv_bfloat16)));
+    ok = ck(cudaMalloc(&n->a[l], npix * cstore(n->ch[l]) * sizeof(__nv_bfloat16)));
   ok = ok && ck(cudaMalloc(&n->dz[0], npix * cmax * sizeof(__nv_bfloat16))) &&
        ck(cudaMalloc(&n->dz[1], npix * cmax * sizeof(__nv_bfloat16))) &&
        ck(cudaMalloc(&n->out32, npix * sizeof(float))) &&
@@ -806,8 +805,8 @@ int refresh_bf16(sw_cnn *n) {
   for (int l = 0; l < n->nl; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
     const int T = n->taps;
-    k_weights_bf16<<<16, 256, 0, s>>>(n->w + n->woff[l], Cout, Cin, r8(Cin), r8(Cout), T,
-                                      r16(Cout), r16(T * r8(Cin)), r16(Cin), r16(T * r8(Cout)),
+    k_weights_bf16<<<16, 256, 0, s>>>(n->w + n->woff[l], Cout, Cin, cstore(Cin), cstore(Cout), T,
+                                      r16(Cout), r16(T * cstore(Cin)), r16(Cin), r16(T * cstore(Cout)),
                                       n->wf[l], n->wb[l]);
     n->ctx->stats.launches_total++;
   }
@@ -830,14 +829,14 @@ int forward(sw_cnn *n, int nz, int nx, int ny) {
     a.W = n->wf[l];
     a.bias = n->w + n->woff[l] + (size_t)Cout * T * Cin;
     a.nout = Cout;
-    a.cs_out = r8(Cout);
+    a.cs_out = cstore(Cout);
     a.out32 = last ? n->out32 : nullptr;
     a.out16 = last ? nullptr : n->a[l + 1];
     a.err = n->err;
     const uint64_t np = (uint64_t)nz * nx * ny;
-    const uint64_t bytes = np * r8(Cin) * 2 + (last ? np * Cout * 4 : np * r8(Cout) * 2);
+    const uint64_t bytes = np * cstore(Cin) * 2 + (last ? np * Cout * 4 : np * cstore(Cout) * 2);
     if ((e = timed_launch(n, bytes, 2 * np * Cout * T * Cin, [&] {
-           return launch_conv(dev, last ? kFwdLast : kFwdHidden, r16(Cout), n->a[l], r8(Cin), nz,
+           return launch_conv(dev, last ? kFwdLast : kFwdHidden, r16(Cout), n->a[l], cstore(Cin), nz,
                               nx, ny, T, a, s);
          })) != cudaSuccess)
       return cnn_fail(n, e, "cnn conv");
@@ -879,8 +878,8 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in, con
             cudaSuccess ||
         (e = cudaMemcpyAsync(n->tgt, tin, npix * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cnn_fail(n, e, "cnn batch");
-    k_pack_input<<<nblk((long long)npix * r8(n->ch[0])), 256, 0, s>>>(
-        n->in32, n->ch[0], r8(n->ch[0]), (int)npix, n->a[0]);
+    k_pack_input<<<nblk((long long)npix * cstore(n->ch[0])), 256, 0, s>>>(
+        n->in32, n->ch[0], cstore(n->ch[0]), (int)npix, n->a[0]);
     n->ctx->stats.launches_total++;
     if ((st = forward(n, nz, nx, ny))) return st;
     // d loss / d output (one channel), FP64 loss partials.
@@ -891,7 +890,7 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in, con
       const int Cin = n->ch[l], Cout = n->ch[l + 1];
       int nchunk = 0;
       const uint64_t np = (uint64_t)npix;
-      if ((e = timed_launch(n, np * (r8(Cin) + r8(Cout)) * 2, 2 * np * T * Cin * Cout, [&] {
+      if ((e = timed_launch(n, np * (cstore(Cin) + cstore(Cout)) * 2, 2 * np * T * Cin * Cout, [&] {
              return launch_wgrad(dev, n->a[l], Cin, n->dz[cur], Cout, nz, nx, ny, T, n->ones,
                                  n->part, n->err, s, &nchunk);
            })) != cudaSuccess)
@@ -907,12 +906,12 @@ int gradient(sw_cnn *n, int nbatch, int nz, int nx, int ny, const float *in, con
       a.W = n->wb[l];
       a.bias = nullptr;
       a.nout = Cin;
-      a.cs_out = r8(Cin);
+      a.cs_out = cstore(Cin);
       a.out16 = n->dz[cur ^ 1];
       a.mask = n->a[l];
       a.err = n->err;
-      if ((e = timed_launch(n, np * (r8(Cout) + 2 * r8(Cin)) * 2, 2 * np * Cin * T * Cout, [&] {
-             return launch_conv(dev, kBwd, r16(Cin), n->dz[cur], r8(Cout), nz, nx, ny, T, a, s);
+      if ((e = timed_launch(n, np * (cstore(Cout) + 2 * cstore(Cin)) * 2, 2 * np * Cin * T * Cout, [&] {
+             return launch_conv(dev, kBwd, r16(Cin), n->dz[cur], cstore(Cout), nz, nx, ny, T, a, s);
            })) != cudaSuccess)
         return cnn_fail(n, e, "cnn dgrad");
       cur ^= 1;
@@ -963,8 +962,8 @@ int create_net(sw_ctx *c, int nlayers, const int *channels, uint64_t seed, int t
   n->wb.assign(nlayers, nullptr);
   for (int l = 0; l < nlayers && ok; ++l) {
     const int Cin = n->ch[l], Cout = n->ch[l + 1];
-    ok = ck(cudaMalloc(&n->wf[l], (size_t)r16(Cout) * r16(taps * r8(Cin)) * 2)) &&
-         ck(cudaMalloc(&n->wb[l], (size_t)r16(Cin) * r16(taps * r8(Cout)) * 2));
+    ok = ck(cudaMalloc(&n->wf[l], (size_t)r16(Cout) * r16(taps * cstore(Cin)) * 2)) &&
+         ck(cudaMalloc(&n->wb[l], (size_t)r16(Cin) * r16(taps * cstore(Cout)) * 2));
   }
   const std::vector<unsigned short> one(8 * kTile, (unsigned short)0x3f80);   // BF16 1.0
   ok = ok && ck(cudaMalloc(&n->ones, one.size() * 2)) &&
@@ -994,8 +993,8 @@ int cnn_forward(sw_cnn *n, int nz, int nx, int ny, const float *in, float *out) 
   if ((e = cudaMemcpyAsync(n->in32, in, npix * n->ch[0] * 4, cudaMemcpyHostToDevice, s)) !=
       cudaSuccess)
     return cnn_fail(n, e, "cnn input");
-  k_pack_input<<<nblk((long long)npix * r8(n->ch[0])), 256, 0, s>>>(n->in32, n->ch[0],
-                                                                     r8(n->ch[0]), (int)npix,
+  k_pack_input<<<nblk((long long)npix * cstore(n->ch[0])), 256, 0, s>>>(n->in32, n->ch[0],
+                                                                     cstore(n->ch[0]), (int)npix,
                                                                      n->a[0]);
   n->ctx->stats.launches_total++;
   if ((st = forward(n, nz, nx, ny))) return st;
