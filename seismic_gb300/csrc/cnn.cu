@@ -138,10 +138,13 @@ __device__ __forceinline__ void cnn_bar_init(unsigned long long *bar, unsigned c
 //   D[p][n] = sum_{tap, c} in[p + s * off(tap)][c] * W[n][tap * Cs + c]
 // with s = +1 (forward) or -1 (input gradient) and zero padding outside
 // the image.  W: NP x kp BF16 in the tensor cores' K-major layout.  One
-// ring stage holds one tap: the Cs / 8 channel-group slices of the shifted
-// patch, fetched by a single tensor copy (Cs / 16 K = 16 steps).  Two
-// accumulators in tensor memory let the products of the next tile run
-// while the epilogue reads the last one.
+// ring stage holds one kernel row (a dz, and a dy in 3D): a single tensor
+// copy of the patch shifted by dz and widened to 6 columns (x0 - 1 ..
+// x0 + 4), every channel group.  In a plane of that copy ([6 x][32 z][8])
+// the patch shifted by dx is the contiguous run of 128 rows from column
+// dx + 1, so the three dx taps are three A operands of the same stage
+// (3 Cs / 16 K = 16 steps).  Two accumulators in tensor memory let the
+// products of the next tile run while the epilogue reads the last one.
 // ---------------------------------------------------------------------------
 enum { kFwdHidden = 0, kFwdLast = 1, kBwd = 2 };
 constexpr int kMaxRing = 32;
@@ -165,8 +168,10 @@ struct ConvArgs {
 };
 
 __host__ __device__ inline size_t conv_wbytes(int NP, int kp) { return ((size_t)NP * kp * 2 + 1023) / 1024 * 1024; }
+constexpr int kConvCols = kTX + 2;                 // copy width: the patch and its x halo
+constexpr int kConvPlane = kConvCols * kTZ * 16;   // bytes of one channel group in a stage
 size_t conv_smem_bytes(int NP, int kp, int Cs, int ring) {
-  return 1024 + conv_wbytes(NP, kp) + (size_t)ring * (Cs / 8) * kChunk;
+  return 1024 + conv_wbytes(NP, kp) + (size_t)ring * (Cs / 8) * kConvPlane;
 }
 
 template <int NP, int MODE>
@@ -179,8 +184,8 @@ __global__ void __launch_bounds__(kWsThreads, 1)
   __shared__ volatile int abort_flag;
   __shared__ volatile int mma_stages;             // stages the MMA warp has consumed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nst = A.taps;                         // ring stages (taps) per tile
-  const size_t sbytes = (size_t)(A.Cs / 8) * kChunk;   // one tap
+  const int nst = A.taps / 3;                     // ring stages (kernel rows) per tile
+  const size_t sbytes = (size_t)(A.Cs / 8) * kConvPlane;   // one kernel row
   unsigned char *base = align1024(cnn_smem);
   unsigned char *sW = base;
   unsigned char *ring = base + conv_wbytes(NP, A.kp);
@@ -222,9 +227,9 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             break;
           unsigned char *dst = ring + (size_t)slot * sbytes;
           cnn_expect_tx(&full[slot], (unsigned)sbytes);
-          int dz, dx, dy;
-          tap_off(k, A.taps, dz, dx, dy);
-          cnn_tma4(dst, &amap, 0, z0 + sgn * dz, x0 + sgn * dx, y0 + sgn * dy, &full[slot]);
+          // Kernel row k: dz = k % 3 - 1, dy = k / 3 - 1 (3D).
+          const int dz = k % 3 - 1, dy = A.taps == 27 ? k / 3 - 1 : 0;
+          cnn_tma4(dst, &amap, 0, z0 + sgn * dz, x0 - 1, y0 + sgn * dy, &full[slot]);
         }
       }
       if (!ok) {
@@ -254,11 +259,18 @@ __global__ void __launch_bounds__(kWsThreads, 1)
           mma_stages = q + 1;
           umma_fence_after();
           const unsigned sa = umma_su32(ring + (size_t)slot * sbytes);
-          for (int h = 0; h < A.Cs / 16; ++h) {
-            const int ks = k * (A.Cs / 16) + h;
-            const uint64_t ad = umma_smem_desc(sa + h * 2 * kChunk, kChunk, 128);
-            const uint64_t bd = umma_smem_desc(sb + ks * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
-            umma_bf16(d, ad, bd, idesc, ks > 0);
+          const int dz = k % 3 - 1, dy = A.taps == 27 ? k / 3 - 1 : 0;
+          for (int dx = -1; dx <= 1; ++dx) {
+            // Tap of (dz, dx, dy); its A operand starts at column s dx + 1.
+            const int t = 9 * (dy + 1) + 3 * (dx + 1) + (dz + 1) - (A.taps == 27 ? 0 : 9);
+            const unsigned col = (unsigned)((A.mirror ? -dx : dx) + 1) * kTZ * 16;
+            for (int h = 0; h < A.Cs / 16; ++h) {
+              const int ks = t * (A.Cs / 16) + h;
+              const uint64_t ad = umma_smem_desc(sa + h * 2 * kConvPlane + col, kConvPlane, 128);
+              const uint64_t bd =
+                  umma_smem_desc(sb + ks * 2 * (NP / 8) * 128, (NP / 8) * 128, 128);
+              umma_bf16(d, ad, bd, idesc, k > 0 || dx > -1 || h > 0);
+            }
           }
           umma_commit(&empty[slot]);
         }
@@ -593,17 +605,17 @@ __global__ void k_weights_bf16(const float *__restrict__ w, int Cout, int Cin, i
 int nblk(long long n) { return (int)std::min<long long>(4096, (n + 255) / 256); }
 
 // BF16 tensor map over Cs / 8 channel-group planes: dimensions (8 nz: z
-// and the 8 channels flattened, nx, ny, Cs / 8), box 8 kTZ x kTX x 1 x
-// planes (kTX rows of 512 bytes per plane), zero fill outside.
+// and the 8 channels flattened, nx, ny, Cs / 8), box 8 kTZ x cols x 1 x
+// planes (cols rows of 512 bytes per plane), zero fill outside.
 bool encode_act_map(CUtensorMap *m, const __nv_bfloat16 *base, int Cs, int nz, int nx, int ny,
-                    int planes) {
+                    int planes, int cols = kTX) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
   const cuuint64_t dims[4] = {(cuuint64_t)nz * 8, (cuuint64_t)nx, (cuuint64_t)ny,
                               (cuuint64_t)Cs / 8};
   const cuuint64_t strides[3] = {(cuuint64_t)nz * 16, (cuuint64_t)nz * nx * 16,
                                  (cuuint64_t)nz * nx * ny * 16};
-  const cuuint32_t box[4] = {8 * kTZ, kTX, 1, (cuuint32_t)planes};
+  const cuuint32_t box[4] = {8 * kTZ, (cuuint32_t)cols, 1, (cuuint32_t)planes};
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16 *>(base), dims,
              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -631,7 +643,7 @@ cudaError_t launch_big(K kernel, int grid, size_t smem, cudaStream_t s, const CU
 cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int Cs, int nz, int nx,
                         int ny, int taps, ConvArgs a, cudaStream_t s) {
   CUtensorMap m;
-  if (!encode_act_map(&m, in, Cs, nz, nx, ny, Cs / 8)) return cudaErrorInvalidValue;
+  if (!encode_act_map(&m, in, Cs, nz, nx, ny, Cs / 8, kConvCols)) return cudaErrorInvalidValue;
   a.Cs = Cs;
   a.nz = nz;
   a.nx = nx;
@@ -642,7 +654,7 @@ cudaError_t launch_conv(int dev, int mode, int NP, const __nv_bfloat16 *in, int 
   a.tiles_x = (nx + kTX - 1) / kTX;
   a.ntiles = a.tiles_z * a.tiles_x * ny;
   // A ring of about 110 KB per CTA (two CTAs per SM); stages of one tap.
-  const size_t stage = (size_t)(Cs / 8) * kChunk;
+  const size_t stage = (size_t)(Cs / 8) * kConvPlane;
   a.ring = (int)std::max<size_t>(
       2, std::min<size_t>(kMaxRing, (110u * 1024u - 1024u - conv_wbytes(NP, a.kp)) / stage));
   const size_t smem = conv_smem_bytes(NP, a.kp, Cs, a.ring);
