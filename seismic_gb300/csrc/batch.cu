@@ -264,6 +264,58 @@ __global__ void k_bv2u(BatchTables t, int s_off) {
   }
 }
 
+// Snapshot save and RTM / LSRTM / AFWI imaging of step s for the 3D shots
+// of the pipelined kernel (the post-update part of t3_extras, which that
+// kernel leaves to this one): one thread per physical point, z fastest, on
+// u2 of the step (the level the step kernel read, unchanged by it).  Per
+// element the operations of Propagator.f90:182-218 and Imaging.f90 as in
+// t3_extras.
+__global__ void k_bsnap3d(BatchTables t, int s_off) {
+  const int b = find_shot(t.snap_blocks, t.nshots, blockIdx.x);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;
+  const int it = S.tmin + s * S.tstep;
+  if ((it % S.snapi) != 0) return;
+  const Geom &g = S.g;
+  const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
+                              : S.tcnt / S.snapi - (it - 1) / S.snapi;
+  const bool save = S.extract_wave && cnt <= S.ntsnap;
+  const int index = S.ntsnap - cnt + 1;
+  const bool img = S.imaging >= 1 && S.imaging <= 3 && S.tstep < 0 && index >= 1;
+  if (!save && !img) return;
+  const float *__restrict__ u2 = S.f[(s + 3) % S.nbuf];
+  const long long nphys = (long long)g.nz * g.nx * g.ny;
+  const int nb = t.snap_blocks[b + 1] - t.snap_blocks[b];
+  for (long long q = (long long)(blockIdx.x - t.snap_blocks[b]) * blockDim.x + threadIdx.x;
+       q < nphys; q += (long long)nb * blockDim.x) {
+    const int i = (int)(q % g.nz) + 1;
+    const long long r = q / g.nz;
+    const int j = (int)(r % g.nx) + 1, k = (int)(r / g.nx) + 1;
+    const long long p = g.idx(i, j, k);
+    const float u2c = u2[p];
+    if (save) S.wave[(long long)(cnt - 1) * nphys + q] = u2c;
+    if (!img) continue;
+    const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[k - 1] : 1.f;
+    const float vc = S.vel[p];
+    const float wsn = S.wave[(long long)(index - 1) * nphys + q];
+    float im = S.image[q];
+    if (S.imaging == 1) {
+      im = im + (u2c * wsn) * taper;
+    } else if (S.imaging == 2) {
+      im = im + (((2.0f * taper) * u2c) * wsn) / vc;
+    } else {
+      const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
+      const float tt = ((S.wave[(long long)(im1 - 1) * nphys + q] - 2.0f * wsn) +
+                        S.wave[(long long)(ip1 - 1) * nphys + q]) /
+                       (S.dt2snap * ((vc * vc) * vc));
+      im = im + (u2c * tt) * taper;
+    }
+    S.image[q] = im;
+    S.illum[q] = S.illum[q] + (wsn * wsn) * taper;
+  }
+}
+
 // Staggered gradient of u2 scaled by delp = 1/rho2 for the variable-density
 // operator (FDderivatives.f90:277-336 3D, 601-640 2D): the 8th-order
 // difference at half cells inside the compute domain, a first-order
@@ -869,6 +921,11 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
   if (ev_after) {
     cudaError_t ec = record(ev_after);
     if (ec != cudaSuccess) return ec;
+  }
+  // Snapshot saves and imaging of the pipelined 3D kernel's shots.
+  if (has_3d && tile.stream3d == 2 && tile.n_snap3d > 0) {
+    k_bsnap3d<<<tile.n_snap3d, 256, 0, s>>>(t, s_off);
+    ++nl;
   }
   if (tile.rigid) {
     // Exact-adjoint mode: no absorbing boundary, the halo stays zero.

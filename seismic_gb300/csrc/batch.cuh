@@ -35,6 +35,7 @@ struct ShotDev {
                           // (two-step launches: a second block of inj_nterm
                           // entries for the step after it)
   int inj_nterm;
+  int inj_pre;            // the terms of this step are in inj_term (k_bterms ran)
   const float *src_tr;    // nsrc*nt
   // extraction
   int ext_mode, nrec, ext_half;
@@ -184,6 +185,7 @@ struct BatchTables {
   const int *tile_tab;    // pipelined 2D kernel: (shot << 24) | (tzi << 12) | txi per tile
   const int *edge_start;  // nshots+1: threads of the fused 2D edge kernel
   const int *term_start;  // nshots+1: injection entries (per-step term kernel)
+  const int *snap_blocks; // nshots+1: blocks of the 3D snapshot / imaging kernel
   const T2Maps *t2maps;   // nshots tensor-map sets (pipelined 2D kernel)
   const T2FMaps *tfmaps;  // nshots tensor-map sets (two-step 2D kernel)
   const T3Maps *t3maps;   // nshots tensor-map sets (pipelined 3D kernel)
@@ -211,6 +213,7 @@ struct StepTile {
   int nsm = 152;       // SMs of the device (persistent grids)
   int fused_edges = 0; // 2D: one launch for the z and x Higdon edges (set by the runner)
   int n_edge = 0;      // threads of that launch
+  int n_snap3d = 0;    // blocks of k_bsnap3d (pipelined 3D kernel with snapshots / imaging)
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
   int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
   int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)

@@ -199,7 +199,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     bytes += rup(ext[b].ic.size() * 4) + 2 * rup(ext[b].wz.size() * 4);
     bytes += 2 * rup(std::max<size_t>(tx[b].size(), ty[b].size()) * 4 + 4);
   }
-  bytes += rup(nb * sizeof(ShotDev)) + 8 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
+  bytes += rup(nb * sizeof(ShotDev)) + 9 * rup((nb + 1) * sizeof(int)) + rup(sizeof(int));
   if (t2) {
     size_t ntile = 0;
     for (int b = 0; b < nb; ++b) ntile += (size_t)step_ctas(G[b], tile);
@@ -220,7 +220,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // ---- carve and fill ----
   std::vector<ShotDev> hs(nb);
   std::vector<int> step_tiles(nb + 1, 0), rec_start(nb + 1, 0), hz(nb + 1, 0), hx(nb + 1, 0),
-      hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0), term(nb + 1, 0);
+      hy(nb + 1, 0), v2b(nb + 1, 0), edge(nb + 1, 0), term(nb + 1, 0), snapb(nb + 1, 0);
   // The fused 2D edge kernel needs n1, n2 >= 16 in every shot.
   bool fused_edges = !has_3d && !tile.has_surf;
   for (int b = 0; b < nb && fused_edges; ++b) fused_edges = edge_threads_2d(G[b]) > 0;
@@ -375,16 +375,24 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     // The pipelined 2D kernel adds injection terms computed per step by
     // k_bterms when a shot has many entries (receiver-side injection);
     // a few source entries are formed in the tile.
-    term[b + 1] = term[b] + (t2 && inj[b].on && inj[b].ent.size() >= kTermKernelMin
+    term[b + 1] = term[b] + ((t2 || t3) && inj[b].on && inj[b].ent.size() >= kTermKernelMin
                                  ? (int)inj[b].ent.size() : 0);
+    // The pipelined 3D kernel leaves a shot's snapshot saves and imaging to
+    // k_bsnap3d (one thread per physical point).
+    S.inj_pre = term[b + 1] > term[b];
+    snapb[b + 1] = snapb[b] + ((t3 && (S.extract_wave || S.imaging != 0))
+                                   ? (int)std::min<long long>(
+                                         8192, ((long long)g.nz * g.nx * g.ny + 255) / 256)
+                                   : 0);
     v2b[b + 1] = v2b[b] + (((S.adj3d && !tile.stream3d) || S.rho_on)
                                ? (int)std::min<long long>(4096, (G[b].total() + 255) / 256)
                                : 0);
   }
   ShotDev *dshots = carve<ShotDev>(cur, nb);
-  int *dtab[8];
-  std::vector<int> *htab[8] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b, &edge, &term};
-  for (int q = 0; q < 8; ++q) {
+  int *dtab[9];
+  std::vector<int> *htab[9] = {&step_tiles, &rec_start, &hz, &hx, &hy, &v2b, &edge, &term,
+                               &snapb};
+  for (int q = 0; q < 9; ++q) {
     dtab[q] = carve<int>(cur, nb + 1);
     SW_CK(cudaMemcpyAsync(dtab[q], htab[q]->data(), (nb + 1) * 4, cudaMemcpyHostToDevice, s));
   }
@@ -527,6 +535,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   t.v2u_blocks = dtab[5];
   t.edge_start = dtab[6];
   t.term_start = dtab[7];
+  t.snap_blocks = dtab[8];
   t.t2shots = d2;
   t.tile_tab = dtile;
   t.t2maps = dmaps;
@@ -543,6 +552,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   const int n_term = term[nb];
   const int n_tiles = step_tiles[nb], n_rec = rec_start[nb], n_hz = hz[nb], n_hx = hx[nb],
             n_hy = hy[nb], n_v2u = v2b[nb];
+  tile.n_snap3d = snapb[nb];
   {
     int dev = 0, nsm = 0;
     SW_CK(cudaGetDevice(&dev));
@@ -584,6 +594,7 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     for (auto &S : hs) {
       if (sidx >= S.nsteps) continue;
       by += (uint64_t)S.npts * 24ull;
+      if (t3) continue;   // snapshots and imaging: k_bsnap3d
       const int it = S.tmin + sidx * S.tstep;
       if (it % S.snapi != 0) continue;
       const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi

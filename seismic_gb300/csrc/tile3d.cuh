@@ -72,9 +72,9 @@ __device__ __forceinline__ void t3_issue(const T3Maps &M, int s, int zi, int xi,
 // the sources added.  The snapshot / imaging part runs after the update
 // (post = true) with u2c the element's u2.
 __device__ __noinline__ float t3_extras(const ShotDev &S, int it, int i, int j, int k, float se,
-                                        float vc, bool post, float u2c) {
+                                        float vc, bool post, float u2c, bool inj = true) {
   const Geom &g = S.g;
-  if (!post) {
+  if (!post && inj) {
     if (S.inj_on && i >= S.bi0 && i <= S.bi1 && j >= S.bj0 && j <= S.bj1 && k >= S.bk0 &&
         k <= S.bk1) {
       const int bx =
@@ -131,42 +131,6 @@ __device__ __forceinline__ float4 t3_col4(const float *u2, const float *vel, lon
     u = make_float4((v.x * v.x) * u.x, (v.y * v.y) * u.y, (v.z * v.z) * u.z, (v.w * v.w) * u.w);
   }
   return u;
-}
-
-// Snapshot save (wsave0) and RTM / LSRTM imaging (wimg0: the snapshot
-// slot read) of rows i0..i0+3 at column (j, k) with 16-byte accesses; the
-// per-element operations of t3_extras.  Returns false, doing nothing, when
-// a row is outside the physical model or an address is not 16-byte aligned.
-__device__ __noinline__ bool t3_snap4(const ShotDev &S, int i0, int j, int k, float4 u2c4,
-                                      float4 vc4, float *wsave0, const float *wimg0) {
-  const Geom &g = S.g;
-  if (i0 < 1 || i0 + 3 > g.nz || j < 1 || j > g.nx || k < 1 || k > g.ny) return false;
-  const long long pp = g.pidx(i0, j, k);
-  float *ws = wsave0 ? wsave0 + pp : nullptr;
-  const float *wr = wimg0 ? wimg0 + pp : nullptr;
-  if (((reinterpret_cast<uintptr_t>(ws) | reinterpret_cast<uintptr_t>(wr) |
-        reinterpret_cast<uintptr_t>(S.image + pp) | reinterpret_cast<uintptr_t>(S.illum + pp)) &
-       15) != 0)
-    return false;
-  if (ws) *reinterpret_cast<float4 *>(ws) = u2c4;
-  if (wr) {
-    const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[k - 1] : 1.f;
-    const float4 w4 = *reinterpret_cast<const float4 *>(wr);
-    const float4 m4 = *reinterpret_cast<const float4 *>(S.image + pp);
-    const float4 l4 = *reinterpret_cast<const float4 *>(S.illum + pp);
-    const float wsn[4] = {w4.x, w4.y, w4.z, w4.w}, u2c[4] = {u2c4.x, u2c4.y, u2c4.z, u2c4.w};
-    const float vc[4] = {vc4.x, vc4.y, vc4.z, vc4.w};
-    float im[4] = {m4.x, m4.y, m4.z, m4.w}, il[4] = {l4.x, l4.y, l4.z, l4.w};
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      if (S.imaging == 1) im[r] = im[r] + (u2c[r] * wsn[r]) * taper;
-      else im[r] = im[r] + (((2.0f * taper) * u2c[r]) * wsn[r]) / vc[r];
-      il[r] = il[r] + (wsn[r] * wsn[r]) * taper;
-    }
-    *reinterpret_cast<float4 *>(S.image + pp) = make_float4(im[0], im[1], im[2], im[3]);
-    *reinterpret_cast<float4 *>(S.illum + pp) = make_float4(il[0], il[1], il[2], il[3]);
-  }
-  return true;
 }
 
 template <bool ADJ>
@@ -227,21 +191,6 @@ __device__ __forceinline__ void tile3d_persistent(const BatchTables &t, int s_of
     float4 nxt = t3_col4<ADJ>(u2, S.vel, colbase + P * (k0 + 4 - g.lo3));
     const int it = S.tmin + s * S.tstep;
     const bool snapstep = (it % S.snapi) == 0 && (S.extract_wave || S.imaging != 0);
-    // The unit's snapshot work (t3_extras' counting): the slot a snapshot
-    // is saved to and / or the slot the RTM (1) or LSRTM (2) imaging
-    // condition reads; other imaging conditions stay element by element.
-    float *wsave0 = nullptr;
-    const float *wimg0 = nullptr;
-    const bool snap_vec = snapstep && (S.imaging == 0 || S.imaging == 1 || S.imaging == 2);
-    if (snap_vec) {
-      const long long nphys = (long long)g.nz * g.nx * g.ny;
-      const int cnt = S.tstep > 0 ? it / S.snapi - (S.tcnt - 1) / S.snapi
-                                  : S.tcnt / S.snapi - (it - 1) / S.snapi;
-      const int index = S.ntsnap - cnt + 1;
-      if (S.extract_wave && cnt <= S.ntsnap) wsave0 = S.wave + (long long)(cnt - 1) * nphys;
-      if (S.imaging != 0 && S.tstep < 0 && index >= 1)
-        wimg0 = S.wave + (long long)(index - 1) * nphys;
-    }
     const Coefs c = S.c;
     float *u3 = S.f[(s + 4) % 5];
     for (int p = 0; p < np; ++p) {
@@ -338,14 +287,38 @@ __device__ __forceinline__ void tile3d_persistent(const BatchTables &t, int s_of
         }
         const float4 u2c4 = *reinterpret_cast<const float4 *>(col + 4);
         const float u2c[4] = {u2c4.x, u2c4.y, u2c4.z, u2c4.w};
-        // Sources (injection box, Born source): element by element.
+        // Injection (Injection.f90:151-456): each cell's entries in order,
+        // their terms precomputed for this step by k_bterms, or formed here
+        // (the same operations) for a shot with few entries.
         const bool inj = S.inj_on && k >= S.bk0 && k <= S.bk1 && j >= S.bj0 && j <= S.bj1 &&
                          i0 + 3 >= S.bi0 && i0 <= S.bi1;
-        if (inj || (snapstep && S.imaging == 4)) {
+        if (inj) {
+          const int nbi = S.bi1 - S.bi0 + 1;
+          const int cb = nbi * ((j - S.bj0) + (S.bj1 - S.bj0 + 1) * (k - S.bk0));
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            const int i = i0 + r;
+            if (i > g.nmax1 || i < S.bi0 || i > S.bi1) continue;
+            const int e1 = S.inj_off[cb + (i - S.bi0) + 1];
+            for (int e = S.inj_off[cb + (i - S.bi0)]; e < e1; ++e) {
+              float tv;
+              if (S.inj_pre) {
+                tv = S.inj_term[e];
+              } else {
+                const InjEntry E = S.inj_ent[e];
+                const float tr = S.src_tr[(long long)E.tr * S.nt + (it - 1)];
+                tv = (((E.v2r * tr) * E.wz) * E.wx) * E.wy;
+              }
+              sv[r] = sv[r] + tv;
+            }
+          }
+        }
+        // The Born source (imaging 4): element by element.
+        if (snapstep && S.imaging == 4) {
 #pragma unroll
           for (int r = 0; r < 4; ++r)
             if (i0 + r <= g.nmax1)
-              sv[r] = t3_extras(S, it, i0 + r, j, k, sv[r], vcen[r], false, 0.f);
+              sv[r] = t3_extras(S, it, i0 + r, j, k, sv[r], vcen[r], false, 0.f, false);
         }
         // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
         const float4 a1 = *reinterpret_cast<const float4 *>(cc);
@@ -371,19 +344,8 @@ __device__ __forceinline__ void tile3d_persistent(const BatchTables &t, int s_of
           for (int r = 0; r < 4; ++r)
             if (i0 + r <= g.nmax1) u3[off + r] = o[r];
         }
-        if (snapstep) {
-          // Snapshot save and RTM / LSRTM imaging of the thread's 4 rows with
-          // 16-byte accesses when all 4 are physical and aligned (t3_snap4);
-          // t3_extras handles the rest element by element.
-          const bool done = snap_vec && t3_snap4(S, i0, j, k, u2c4,
-                                                 make_float4(vcen[0], vcen[1], vcen[2], vcen[3]),
-                                                 wsave0, wimg0);
-          if (!done) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-              if (i0 + r <= g.nmax1) t3_extras(S, it, i0 + r, j, k, 0.f, vcen[r], true, u2c[r]);
-          }
-        }
+        // Snapshot saves and imaging of this step: k_bsnap3d, after the
+        // launch.
       }
       __syncthreads();   // the stage is free for plane p + S
 #pragma unroll
