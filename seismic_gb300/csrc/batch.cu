@@ -286,33 +286,81 @@ __global__ void k_bsnap3d(BatchTables t, int s_off) {
   if (!save && !img) return;
   const float *__restrict__ u2 = S.f[(s + 3) % S.nbuf];
   const long long nphys = (long long)g.nz * g.nx * g.ny;
-  const int nb = t.snap_blocks[b + 1] - t.snap_blocks[b];
-  for (long long q = (long long)(blockIdx.x - t.snap_blocks[b]) * blockDim.x + threadIdx.x;
-       q < nphys; q += (long long)nb * blockDim.x) {
-    const int i = (int)(q % g.nz) + 1;
-    const long long r = q / g.nz;
-    const int j = (int)(r % g.nx) + 1, k = (int)(r / g.nx) + 1;
+  float *ws = save ? S.wave + (long long)(cnt - 1) * nphys : nullptr;
+  const float *wr = img ? S.wave + (long long)(index - 1) * nphys : nullptr;
+  const float *wrm = nullptr, *wrp = nullptr;
+  if (img && S.imaging == 3) {
+    wrm = S.wave + (long long)(max(index - 1, 1) - 1) * nphys;
+    wrp = S.wave + (long long)(min(index + 1, S.ntsnap) - 1) * nphys;
+  }
+  // One element: its u2 (and velocity), the saved snapshot, the image and
+  // illumination update.
+  auto point = [&](long long q, int i, int j, int k) {
     const long long p = g.idx(i, j, k);
     const float u2c = u2[p];
-    if (save) S.wave[(long long)(cnt - 1) * nphys + q] = u2c;
-    if (!img) continue;
+    if (ws) ws[q] = u2c;
+    if (!wr) return;
     const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[k - 1] : 1.f;
-    const float vc = S.vel[p];
-    const float wsn = S.wave[(long long)(index - 1) * nphys + q];
+    const float wsn = wr[q];
     float im = S.image[q];
     if (S.imaging == 1) {
       im = im + (u2c * wsn) * taper;
     } else if (S.imaging == 2) {
-      im = im + (((2.0f * taper) * u2c) * wsn) / vc;
+      im = im + (((2.0f * taper) * u2c) * wsn) / S.vel[p];
     } else {
-      const int ip1 = min(index + 1, S.ntsnap), im1 = max(index - 1, 1);
-      const float tt = ((S.wave[(long long)(im1 - 1) * nphys + q] - 2.0f * wsn) +
-                        S.wave[(long long)(ip1 - 1) * nphys + q]) /
-                       (S.dt2snap * ((vc * vc) * vc));
+      const float vc = S.vel[p];
+      const float tt = ((wrm[q] - 2.0f * wsn) + wrp[q]) / (S.dt2snap * ((vc * vc) * vc));
       im = im + (u2c * tt) * taper;
     }
     S.image[q] = im;
     S.illum[q] = S.illum[q] + (wsn * wsn) * taper;
+  };
+  const int nb = t.snap_blocks[b + 1] - t.snap_blocks[b];
+  const long long first = (long long)(blockIdx.x - t.snap_blocks[b]) * blockDim.x + threadIdx.x;
+  const long long stride = (long long)nb * blockDim.x;
+  if ((g.nz & 3) == 0 && nphys < (1LL << 31)) {
+    // 4 consecutive rows of a column per thread, 32-bit index arithmetic.
+    const unsigned nz = (unsigned)g.nz, nx = (unsigned)g.nx;
+    const bool al = ((reinterpret_cast<uintptr_t>(ws) | reinterpret_cast<uintptr_t>(wr) |
+                      reinterpret_cast<uintptr_t>(wrm) | reinterpret_cast<uintptr_t>(wrp) |
+                      reinterpret_cast<uintptr_t>(S.image) | reinterpret_cast<uintptr_t>(S.illum)) &
+                     15) == 0;
+    for (long long w = first; w < nphys / 4; w += stride) {
+      const unsigned q = 4u * (unsigned)w;
+      const unsigned col = q / nz;
+      const int i0 = (int)(q - col * nz) + 1, j = (int)(col % nx) + 1, k = (int)(col / nx) + 1;
+      if (!al || S.imaging == 3) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) point((long long)q + r, i0 + r, j, k);
+        continue;
+      }
+      // 16-byte snapshot, image and illumination accesses; per element the
+      // operations of point().
+      const long long p = g.idx(i0, j, k);
+      const float u[4] = {u2[p], u2[p + 1], u2[p + 2], u2[p + 3]};
+      if (ws) *reinterpret_cast<float4 *>(ws + q) = make_float4(u[0], u[1], u[2], u[3]);
+      if (!wr) continue;
+      const float taper = S.taperx ? S.taperx[j - 1] * S.tapery[k - 1] : 1.f;
+      const float4 w4 = *reinterpret_cast<const float4 *>(wr + q);
+      const float4 m4 = *reinterpret_cast<const float4 *>(S.image + q);
+      const float4 l4 = *reinterpret_cast<const float4 *>(S.illum + q);
+      const float wsn[4] = {w4.x, w4.y, w4.z, w4.w};
+      float im[4] = {m4.x, m4.y, m4.z, m4.w}, il[4] = {l4.x, l4.y, l4.z, l4.w};
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (S.imaging == 1) im[r] = im[r] + (u[r] * wsn[r]) * taper;
+        else im[r] = im[r] + (((2.0f * taper) * u[r]) * wsn[r]) / S.vel[p + r];
+        il[r] = il[r] + (wsn[r] * wsn[r]) * taper;
+      }
+      *reinterpret_cast<float4 *>(S.image + q) = make_float4(im[0], im[1], im[2], im[3]);
+      *reinterpret_cast<float4 *>(S.illum + q) = make_float4(il[0], il[1], il[2], il[3]);
+    }
+  } else {
+    for (long long q = first; q < nphys; q += stride) {
+      const int i = (int)(q % g.nz) + 1;
+      const long long r = q / g.nz;
+      point(q, i, (int)(r % g.nx) + 1, (int)(r / g.nx) + 1);
+    }
   }
 }
 

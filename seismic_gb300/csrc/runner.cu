@@ -484,15 +484,27 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   std::vector<T3Maps> hmaps3;
   T3Maps *dmaps3 = nullptr;
   if (t3) {
+    // Units that meet a shot's injection box (the receiver layer of a
+    // backward pass: several times the work of the others) come first, so
+    // that the round-robin assignment gives every CTA at most its share of
+    // them; the rest follow in the same z-fastest order.
+    std::vector<int> light;
     for (int b = 0; b < nb; ++b) {
       const Geom &g = G[b];
       const int n1t = (g.nmax1 - g.nmin1 + 32) / 32, n2t = (g.nmax2 - g.nmin2 + 32) / 32;
       const int n3t = (g.nmax3 - g.nmin3 + tile.ty) / tile.ty;
+      const InjPlan &P = inj[b];
       for (int ky = 0; ky < n3t; ++ky)
         for (int xi = 0; xi < n2t; ++xi)
-          for (int zi = 0; zi < n1t; ++zi)
-            htile.push_back((b << 24) | (zi << 16) | (xi << 8) | ky);
+          for (int zi = 0; zi < n1t; ++zi) {
+            const int e = (b << 24) | (zi << 16) | (xi << 8) | ky;
+            const int z0 = g.nmin1 + 32 * zi, x0 = g.nmin2 + 32 * xi, y0 = g.nmin3 + ky * tile.ty;
+            const bool heavy = P.on && z0 <= P.bi1 && z0 + 31 >= P.bi0 && x0 <= P.bj1 &&
+                               x0 + 31 >= P.bj0 && y0 <= P.bk1 && y0 + tile.ty - 1 >= P.bk0;
+            (heavy ? htile : light).push_back(e);
+          }
     }
+    htile.insert(htile.end(), light.begin(), light.end());
     if ((int)htile.size() != step_tiles[nb]) return fail(c, SW_CUDA_ERR, "unit table size");
     hmaps3.resize(nb);
     for (int b = 0; b < nb; ++b) {
