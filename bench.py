@@ -287,6 +287,8 @@ def main():
     ap.add_argument("--rho", action="store_true",
                     help="time 2D modelling with variable density (and without) on the "
                          "751 x 2301 grid instead of the RTM bench")
+    ap.add_argument("--fwi-bench", action="store_true",
+                    help="time one 80-shot FWI misfit and gradient evaluation on 601 x 1801")
     ap.add_argument("--cnn-bench", action="store_true",
                     help="time the preconditioner network's tensor-core kernels at 601 x 1801")
     ap.add_argument("--config4-study", action="store_true",
@@ -308,6 +310,8 @@ def main():
         return run_config4_study(args)
     if args.cnn_bench:
         return run_cnn_bench(args)
+    if args.fwi_bench:
+        return run_fwi_bench(args)
     if args.rho:
         return run_rho_bench(args)
     if args.model3d:
@@ -829,6 +833,51 @@ def run_config4_study(args) -> int:
                                   train_evals_per_stage=args.c4_train_evals,
                                   learned_kw={"max_learned": 3, "c1": 0.1}, log=log)
     print(json.dumps({"study": "learned vs plain L-BFGS multiscale FWI", **r}), flush=True)
+    ctx.close()
+    return 0
+
+
+def run_fwi_bench(args) -> int:
+    """One FWI misfit and gradient evaluation (compute_fct_gdt: forward
+    modelling, residual, adjoint propagation with the AFWI imaging
+    condition, every snapshot in HBM) of the learned-preconditioner study's
+    test survey: 601 x 1801 model at 10 m, 80 shots, 4 s at dt 0.9 ms,
+    6 Hz Ricker, start model smoothed by 250 m; observed data modelled on
+    the true model.  Shots run in HBM-admitted batches.  One JSON line."""
+    import torch
+
+    import seismic_gb300 as sw
+    from seismic_gb300 import precond
+    torch.cuda.set_device(0)
+    ctx = sw.Context(0)
+    cfg = precond.CONFIG4
+    sv = precond._stage_survey(ctx, 7, cfg["test"], 6.0, cfg["nshot"], cfg)
+    x = sv.v0.astype(np.float32)
+    for _ in range(max(1, args.warmup)):
+        ctx.fwi_fct_gdt(sv.desc, x, sv.wavelet, sv.shots)
+    ctx.reset_stats()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.fwi_fct_gdt(sv.desc, x, sv.wavelet, sv.shots)
+    secs = (time.perf_counter() - t0) / args.steps
+    clk = clocks.stop()
+    st = ctx.stats()
+    line = {
+        "metric": "fwi_gradient_gpts_per_s", "value": st["points_updated"] / args.steps / secs / 1e9,
+        "unit": "Gpts/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak", "dtype": "f32",
+        "vs_baseline": None, "data": "synthetic (seeded layered, faulted model; data modelled "
+                                     "by the engine)",
+        "config": {"workload": "FWI misfit and gradient of 80 shots (store-all snapshots)",
+                   "grid": list(cfg["test"]), "spacing_m": cfg["d"], "dt_s": cfg["dt"],
+                   "record_s": cfg["t"], "shots": cfg["nshot"], "ricker_hz": 6.0},
+        "seconds_per_evaluation": secs,
+        "solves_per_second": 2 * cfg["nshot"] / secs,
+        "clocks": clk, "gpu_launches": int(st["launches_total"]) // args.steps,
+    }
+    print(json.dumps(line), flush=True)
     ctx.close()
     return 0
 
