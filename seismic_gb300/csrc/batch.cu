@@ -66,25 +66,6 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
   const int i = g.nmin1 + tz * 32 + threadIdx.x;
   const int j = g.nmin2 + tx * 8 + threadIdx.y;
   const int k = TWO_D ? 1 : g.nmin3 + kk;
-  // 2D variable density: the block's rows of sz (with the z halo the
-  // divergence reads, rows -4..+3) and columns of sx (x halo, columns
-  // -4..+3) staged in shared memory by the whole block, indices clamped to
-  // the padded array (clamped values feed no stored output).
-  __shared__ float ssz[8][40], ssx[15][32];
-  if (TWO_D && S.rho_on) {
-    const int z0 = g.nmin1 + tz * 32, x0 = g.nmin2 + tx * 8;
-    const int zlo = g.lo1, zhi = g.lo1 + g.ld1 - 1, xlo = g.lo2, xhi = g.lo2 + g.n2p - 1;
-    const int tid = threadIdx.y * 32 + threadIdx.x;
-    for (int q = tid; q < 8 * 39; q += 256) {
-      const int c = q / 39, r = q - c * 39;
-      ssz[c][r] = S.sz[g.idx(min(max(z0 - 4 + r, zlo), zhi), min(x0 + c, xhi), 1)];
-    }
-    for (int q = tid; q < 15 * 32; q += 256) {
-      const int c = q >> 5, r = q & 31;
-      ssx[c][r] = S.sx[g.idx(min(z0 + r, zhi), min(max(x0 - 4 + c, xlo), xhi), 1)];
-    }
-    __syncthreads();
-  }
   if (i > g.nmax1 || j > g.nmax2) return;
   const int it = S.tmin + s * S.tstep;
   const float *__restrict__ um1 = S.f[s % 5];
@@ -102,29 +83,14 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
     const Coefs &r = S.cr;
     const float *__restrict__ sz = S.sz;
     const float *__restrict__ sx = S.sx;
-    float tz, tx;
-    if (TWO_D) {
-      // sz[p + m] = ssz[column][row + 4 + m], sx[p + m L] = ssx[column + 4 + m][row].
-      const float *cz = &ssz[threadIdx.y][threadIdx.x + 4];
-      const int rw = threadIdx.x, cx = threadIdx.y + 4;
-      tz = r.c1z * (cz[0] - cz[-1]);
-      tz = tz + r.c2z * (cz[1] - cz[-2]);
-      tz = tz + r.c3z * (cz[2] - cz[-3]);
-      tz = tz + r.c4z * (cz[3] - cz[-4]);
-      tx = r.c1x * (ssx[cx][rw] - ssx[cx - 1][rw]);
-      tx = tx + r.c2x * (ssx[cx + 1][rw] - ssx[cx - 2][rw]);
-      tx = tx + r.c3x * (ssx[cx + 2][rw] - ssx[cx - 3][rw]);
-      tx = tx + r.c4x * (ssx[cx + 3][rw] - ssx[cx - 4][rw]);
-    } else {
-      tz = r.c1z * (sz[p] - sz[p - 1]);
-      tz = tz + r.c2z * (sz[p + 1] - sz[p - 2]);
-      tz = tz + r.c3z * (sz[p + 2] - sz[p - 3]);
-      tz = tz + r.c4z * (sz[p + 3] - sz[p - 4]);
-      tx = r.c1x * (sx[p] - sx[p - L]);
-      tx = tx + r.c2x * (sx[p + L] - sx[p - 2 * L]);
-      tx = tx + r.c3x * (sx[p + 2 * L] - sx[p - 3 * L]);
-      tx = tx + r.c4x * (sx[p + 3 * L] - sx[p - 4 * L]);
-    }
+    float tz = r.c1z * (sz[p] - sz[p - 1]);
+    tz = tz + r.c2z * (sz[p + 1] - sz[p - 2]);
+    tz = tz + r.c3z * (sz[p + 2] - sz[p - 3]);
+    tz = tz + r.c4z * (sz[p + 3] - sz[p - 4]);
+    float tx = r.c1x * (sx[p] - sx[p - L]);
+    tx = tx + r.c2x * (sx[p + L] - sx[p - 2 * L]);
+    tx = tx + r.c3x * (sx[p + 2 * L] - sx[p - 3 * L]);
+    tx = tx + r.c4x * (sx[p + 3 * L] - sx[p - 4 * L]);
     const float vv = S.vel[p];
     const float vr = (vv * vv) * S.rho[p];
     if (TWO_D) {
