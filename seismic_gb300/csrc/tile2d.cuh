@@ -39,8 +39,8 @@ struct T2Step {
   int live;            // the shot steps in this launch with this stencil variant
   int snap;            // snapshot step with snapshot or imaging work
   int extract;         // save the snapshot this step
-  int img;             // RTM (1) or LSRTM (2) imaging this step, else 0
-  int pad_;
+  int img;             // RTM (1), LSRTM (2) or AFWI (3) imaging this step, else 0
+  float dt2snap;       // AFWI: (dt snapi)^2
   float *wsave;        // snapshot slot written this step
   const float *wimg;   // snapshot slot read by the imaging
   float *image, *illum;
@@ -261,7 +261,7 @@ __device__ __forceinline__ void t2_img_load(const T2Shot &h, const T2Step &stp, 
   }
 }
 
-// Snapshot saving (Extraction.f90:562-601) and RTM / LSRTM imaging
+// Snapshot saving (Extraction.f90:562-601) and RTM / LSRTM / AFWI imaging
 // (Imaging.f90:265 and 735) of a thread's elements; su is the staged u2 halo
 // tile and svel the staged velocity: the halo tile for the adjoint stencil,
 // the core tile (column stride T2_Z) for the forward one (the backward pass
@@ -292,9 +292,18 @@ __device__ __forceinline__ void t2_snap_tile(const T2Shot &h, const T2Step &stp,
         float im = P.im[hh][m];
         if (stp.img == 1) {
           im = im + (u * wsn) * taper;
-        } else {
+        } else if (stp.img == 2) {
           const float v = ADJ ? svel[(jl + 4) * T2_SZ + 4 + r] : svel[jl * T2_Z + r];
           im = im + (((2.0f * taper) * u) * wsn) / v;
+        } else {
+          // AFWI (Imaging.f90:410-411): second time difference of the
+          // snapshots over v^3.
+          const float v = ADJ ? svel[(jl + 4) * T2_SZ + 4 + r] : svel[jl * T2_Z + r];
+          const long long np = (long long)h.nz * h.nx;
+          const float *wm = stp.wimg - ((stp.img & 16) ? np : 0);
+          const float *wp = stp.wimg + ((stp.img & 32) ? np : 0);
+          const float tt = ((wm[pc + i] - 2.0f * wsn) + wp[pc + i]) / (stp.dt2snap * ((v * v) * v));
+          im = im + (u * tt) * taper;
         }
         stp.image[pc + i] = im;
         stp.illum[pc + i] = P.il[hh][m] + (wsn * wsn) * taper;
@@ -435,10 +444,9 @@ __device__ __forceinline__ void t2_compute(const BatchTables &t, const T2Shot &h
   const int zl = z0 + T2_Z - 1, xl = x0 + T2_X - 1;
   const bool inj_tile = h.inj_on && !(zl < h.bi0 || z0 > h.bi1 || xl < h.bj0 || x0 > h.bj1);
   const bool snap_tile = stp.snap && t2_phys_tile(h, e);
-  // Snapshot saving and RTM / LSRTM imaging take the vectorised path after
-  // the update; injection, Born source and AFWI imaging go element by
-  // element.
-  const bool snap_fast = snap_tile && h.imaging <= 2;
+  // Snapshot saving and RTM / LSRTM / AFWI imaging take the vectorised path
+  // after the update; injection and the Born source go element by element.
+  const bool snap_fast = snap_tile && h.imaging <= 3;
   const bool snap_slow = snap_tile && !snap_fast;
   const bool slow_extras = inj_tile || snap_slow;
   const float *su = st;
@@ -681,14 +689,17 @@ __device__ __forceinline__ T2Step t2_step_of(const BatchTables &t, const T2Shot 
   st.extract = st.snap && h.extract_wave && cnt <= S.ntsnap && h.imaging <= 2;
   st.wsave = st.extract ? S.wave + (long long)(cnt - 1) * nphys : nullptr;
   const int index = S.ntsnap - cnt + 1;
-  st.img = (st.snap && (h.imaging == 1 || h.imaging == 2) && h.tstep < 0 && index >= 1)
+  st.img = (st.snap && h.imaging >= 1 && h.imaging <= 3 && h.tstep < 0 && index >= 1)
                ? h.imaging : 0;
   st.wimg = st.img ? S.wave + (long long)(index - 1) * nphys : nullptr;
+  // AFWI reads the slots before and after (clamped to the first and last):
+  // bit 4 of img when index - 1 >= 1, bit 5 when index + 1 <= ntsnap.
+  if (st.img == 3) st.img |= (index > 1 ? 16 : 0) | (index < S.ntsnap ? 32 : 0);
+  st.dt2snap = S.dt2snap;
   st.image = S.image;
   st.illum = S.illum;
   st.taperx = S.taperx;
   st.tapery0 = S.taperx ? S.tapery[0] : 1.f;
-  st.pad_ = 0;
   return st;
 }
 
