@@ -294,7 +294,7 @@ def main():
     ap.add_argument("--config4-study", action="store_true",
                     help="learned vs plain multiscale FWI on 601 x 1801 models (80 shots, "
                          "3/6/9 Hz) instead of the RTM bench")
-    ap.add_argument("--c4-train", type=int, default=16, help="training models (301 x 901)")
+    ap.add_argument("--c4-train", type=int, default=64, help="training models (301 x 901)")
     ap.add_argument("--c4-train-shots", type=int, default=20, help="shots per training model")
     ap.add_argument("--c4-evals", type=int, default=15, help="evaluations per stage (test)")
     ap.add_argument("--c4-train-evals", type=int, default=10,
