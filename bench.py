@@ -571,9 +571,9 @@ def run_model3d(args) -> int:
 def run_rho_bench(args) -> int:
     """Variable density: 2D modelling of one shot on the full 751 x 2301
     model at 4 m (the RTM bench's grid and dt, 2000 steps, 2301 receivers)
-    through sw_propagate with a density model (withRho: gradient pass, then
-    the staggered divergence on the point-tile kernel) and, for scale, the
-    same run without it.  One JSON line."""
+    through sw_propagate with a density model (withRho: the one-pass
+    staggered operator, k_brho2d) and, for scale, the same run without it.
+    One JSON line with the density step kernel's roofline."""
     import torch
 
     import seismic_gb300 as sw
@@ -624,6 +624,18 @@ def run_rho_bench(args) -> int:
         st = ctx.stats()
         out[with_rho] = (float(st["points_updated"]) / secs / 1e9, secs / args.steps,
                          int(st["launches_total"]))
+    # The density step kernel's duration from CUDA events around it in one
+    # more (untimed) run.
+    ctx.reset_stats()
+    ctx.set_profiling(True)
+    run(True)
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
+    sp = ctx.stats()
+    peak, peak_kind = measured_peak()
+    nl = max(1, sp["step_kernel_timed"])
+    kern_s = sp["step_kernel_ms"] / 1e3
+    achieved = (sp["step_bytes"] / nl) / (kern_s / nl) / 1e9 if kern_s > 0 else None
     line = {
         "metric": "fd_gpts_per_s_2d_rho_modeling", "value": out[True][0], "unit": "Gpts/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -635,6 +647,12 @@ def run_rho_bench(args) -> int:
                    "grid": [nz, nx], "spacing_m": d, "dt_s": c["dt"], "nt": nt,
                    "receivers": nx},
         "constant_density_gpts_per_s": out[False][0],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
+                     "kernel": "k_brho2d (one-pass staggered gradient, divergence and time "
+                               "update, 32 B per point)",
+                     "avg_launch_ms": sp["step_kernel_ms"] / nl,
+                     "algorithmic_bytes_per_launch": sp["step_bytes"] / nl},
         "clocks": clk, "gpu_launches": out[True][2],
     }
     print(json.dumps(line), flush=True)

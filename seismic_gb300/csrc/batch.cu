@@ -45,6 +45,11 @@ __device__ __forceinline__ float lap_axis(const float *__restrict__ u, long long
   return t;
 }
 
+__device__ __forceinline__ void step_tail(const ShotDev &S, const Geom &g, int i, int j, int k,
+                                          long long p, int it, float sv, float u2c, float u1c,
+                                          float u0c, float um1c, const float *__restrict__ u2,
+                                          float *__restrict__ u3, bool snapstep, bool maybe_inj);
+
 // ---------------------------------------------------------------------------
 // Fused step: stencil -> injection -> Born source -> 5-level time update,
 // with the snapshot and imaging reads of u2 (Propagator.f90:182-218).
@@ -151,8 +156,22 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
       }
     }
   }
+  step_tail(S, g, i, j, k, p, it, sv, u2[p], u1[p], u0[p], um1[p], u2, u3, (it % S.snapi) == 0,
+            true);
+}
+
+// The part of a point update after the spatial operator sv: injection, the
+// Born source, the 5-level time update of u3, the snapshot save and the
+// imaging conditions on u2, for the point (i, j, k) at padded offset p of
+// step it.  u2c, u1c, u0c, um1c are the point's values of u2, u1, u0 and
+// u_1; snapstep says whether it is a multiple of snapi; maybe_inj false
+// says the point lies outside the shot's injection box.
+__device__ __forceinline__ void step_tail(const ShotDev &S, const Geom &g, int i, int j, int k,
+                                          long long p, int it, float sv, float u2c, float u1c,
+                                          float u0c, float um1c, const float *__restrict__ u2,
+                                          float *__restrict__ u3, bool snapstep, bool maybe_inj) {
   // Injection (Injection.f90:151-456, 561-591): contributions in source order.
-  if (S.inj_on && i >= S.bi0 && i <= S.bi1 && j >= S.bj0 && j <= S.bj1 && k >= S.bk0 &&
+  if (maybe_inj && S.inj_on && i >= S.bi0 && i <= S.bi1 && j >= S.bj0 && j <= S.bj1 && k >= S.bk0 &&
       k <= S.bk1) {
     const int bx = (i - S.bi0) + (S.bi1 - S.bi0 + 1) * ((j - S.bj0) + (S.bj1 - S.bj0 + 1) * (k - S.bk0));
     const int e1 = S.inj_off[bx + 1];
@@ -166,7 +185,6 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
   // Under a free surface the rows above it are stored as zero and take no
   // imaging or Born source (Extraction.f90:580-592, Imaging.f90:248-258).
   const bool below = i >= S.irow0;
-  const bool snapstep = (it % S.snapi) == 0;
   int cnt = 0;
   long long pp = 0;
   float taper = 1.f;
@@ -182,11 +200,10 @@ __global__ void __launch_bounds__(256) k_bstep(BatchTables t, int s_off) {
     sv = sv + (((2.0f * taper) * S.ref[pp]) * w0[pp]) / S.vel[p];
   }
   // FD_2nd_time_derivative_grid (FDderivatives.f90:960-982).
-  const float u2c = u2[p];
   float a = 20.0f * u2c;
-  a = a - 6.0f * u1[p];
-  a = a - 4.0f * u0[p];
-  a = a + um1[p];
+  a = a - 6.0f * u1c;
+  a = a - 4.0f * u0c;
+  a = a + um1c;
   a = a + S.k12 * sv;
   u3[p] = a * S.div11;
   if (phys && snapstep) {
@@ -431,6 +448,283 @@ __global__ void k_brho_grad(BatchTables t, int s_off) {
       }
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// The 2D variable-density step in one pass (FDderivatives.f90:601-657 and
+// the time update): each block owns a tile of 64 (z) x 32 (x) outputs.  At
+// its start it issues asynchronous 16-byte copies (cp.async, zero-filled
+// outside the padded array) of every input into shared memory: u2 with an
+// 8-cell halo (80 x 48), delp with a 4-cell halo (72 x 40), and the tile's
+// v, rho, u1, u0 and u_1 (64 x 32 each).  It then forms the staggered
+// gradients the tile's divergence reads - sz on rows z0-4..z0+67 of the
+// tile's columns, sx on columns x0-4..x0+35 of its rows - with the
+// operations and padding-cell rules of k_brho_grad, and finally the
+// divergence times v^2*rho and the rest of the point update (step_tail).
+// sz and sx never go through HBM: 32 bytes per point (u2, delp, v, rho, u1,
+// u0, u_1 read, u3 written) instead of the two passes' 52.
+// ---------------------------------------------------------------------------
+constexpr int R2_Z = 64, R2_X = 32;
+constexpr int R2_UZ = R2_Z + 16, R2_UX = R2_X + 16;   // staged u2: rows z0-8.., columns x0-8..
+constexpr int R2_GZ = R2_Z + 8, R2_GX = R2_X + 8;     // delp and sz rows z0-4.., sx columns x0-4..
+constexpr int R2_CORE = R2_Z * R2_X;
+// Shared-memory layout in floats, every array [column][row].
+constexpr int R2_SU = 0;                                // u2, R2_UX x R2_UZ
+constexpr int R2_SDP = R2_SU + R2_UX * R2_UZ;           // delp, R2_GX x R2_GZ
+constexpr int R2_SC = R2_SDP + R2_GX * R2_GZ;           // v, rho, u1, u0, u_1: 5 x R2_CORE
+constexpr int R2_SSZ = R2_SC + 5 * R2_CORE;             // sz, R2_X x R2_GZ
+constexpr int R2_SSX = R2_SSZ + R2_X * R2_GZ;           // sx, R2_GX x R2_Z
+constexpr int R2_FLOATS = R2_SSX + R2_GX * R2_Z;
+constexpr size_t R2_SMEM = sizeof(float) * R2_FLOATS;   // 87 296 bytes: two blocks per SM
+// 16-byte chunks of the staged arrays.
+constexpr int R2_QU = R2_UX * (R2_UZ / 4), R2_QD = R2_GX * (R2_GZ / 4), R2_QC = R2_X * (R2_Z / 4);
+
+// 16-byte asynchronous global -> shared copy; with in false nothing is read
+// and the destination is zero-filled.
+__device__ __forceinline__ void cp_async16(float *dst, const float *src, bool in) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(in ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// step_tail of one point of k_brho2d's tiles that carry injection or
+// snapshot work, kept out of line so that the common path stays small.
+__device__ __noinline__ void rho_tail(const ShotDev &S, int i, int j, int p, int it, float sv,
+                                      float u2c, float u1c, float u0c, float um1c,
+                                      const float *u2, float *u3, bool snapstep, bool inj) {
+  step_tail(S, S.g, i, j, 1, p, it, sv, u2c, u1c, u0c, um1c, u2, u3, snapstep, inj);
+}
+
+// Four consecutive shared-memory floats (16-byte aligned) into r[0..3].
+__device__ __forceinline__ void lds4_to(float *r, const float *p) {
+  const float4 v = *reinterpret_cast<const float4 *>(p);
+  r[0] = v.x;
+  r[1] = v.y;
+  r[2] = v.z;
+  r[3] = v.w;
+}
+
+__global__ void __launch_bounds__(256, 2) k_brho2d(BatchTables t, int s_off) {
+  extern __shared__ __align__(16) float r2s[];
+  float *su = r2s + R2_SU, *sdp = r2s + R2_SDP, *sc = r2s + R2_SC;
+  float *ssz = r2s + R2_SSZ, *ssx = r2s + R2_SSX;
+  const int b = find_shot(t.step_tiles, t.nshots, blockIdx.x);
+  const ShotDev &S = t.shots[b];
+  const int s = *t.counter + s_off;
+  if (s >= S.nsteps) return;   // the whole block
+  const Geom &g = S.g;
+  const int nmin1 = g.nmin1, nmax1 = g.nmax1, nmin2 = g.nmin2, nmax2 = g.nmax2;
+  const int lo1 = g.lo1, lo2 = g.lo2, ld = g.ld1, n2p = g.n2p;
+  const int ntz = (nmax1 - nmin1 + R2_Z) / R2_Z;
+  const int local = blockIdx.x - t.step_tiles[b];
+  const int z0 = nmin1 + (local % ntz) * R2_Z, x0 = nmin2 + (local / ntz) * R2_X;
+  const int tid = threadIdx.x;
+  const float *__restrict__ u2 = S.f[(s + 3) % 5];
+  float *__restrict__ u3 = S.f[(s + 4) % 5];
+  // 32-bit offsets in the padded array (fewer than 2^31 points per shot,
+  // checked when the batch is set up).
+  auto off = [&](int i, int j) { return (i - lo1) + ld * (j - lo2); };
+  // Every chunk starts 4k rows after the padded array's first row (z0 - lo1
+  // = 64 t + 4), so a chunk lies wholly inside a column's ld1 rows or wholly
+  // outside them; the arrays are 256-byte aligned and ld1 is a multiple of
+  // 32, so every source address is 16-byte aligned.  Cells beyond the
+  // padded array (zero-filled, or rows n1p..ld1-1 of a column) feed no value
+  // that a stored output depends on: the gradients read rows
+  // nmin1-3..nmax1+4 and columns nmin2-3..nmax2+4 of u2.
+  auto stage = [&](float *dst, const float *src, int i0, int j) {
+    const bool in = i0 >= lo1 && i0 < lo1 + ld && j >= lo2 && j < lo2 + n2p;
+    cp_async16(dst, in ? src + off(i0, j) : src, in);
+  };
+  for (int q = tid; q < R2_QU; q += 256) {
+    const int cc = q / (R2_UZ / 4), k = q - cc * (R2_UZ / 4);
+    stage(su + cc * R2_UZ + 4 * k, u2, z0 - 8 + 4 * k, x0 - 8 + cc);
+  }
+  for (int q = tid; q < R2_QD; q += 256) {
+    const int cc = q / (R2_GZ / 4), k = q - cc * (R2_GZ / 4);
+    stage(sdp + cc * R2_GZ + 4 * k, S.delp, z0 - 4 + 4 * k, x0 - 4 + cc);
+  }
+  {
+    // v, rho, then u1, u0, u_1 (levels s+2, s+1, s of the 5-level ring):
+    // two chunks of each per thread.
+    static_assert(R2_QC == 2 * 256, "core chunks per thread");
+#pragma unroll
+    for (int a = 0; a < 5; ++a) {
+      const float *src = a == 0 ? S.vel : a == 1 ? S.rho : S.f[(s + 4 - a) % 5];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = tid + 256 * h, cc = q >> 4, k = q & 15;
+        stage(sc + a * R2_CORE + cc * R2_Z + 4 * k, src, z0 + 4 * k, x0 + cc);
+      }
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const Coefs &cf = S.cr;
+  const float c1z = cf.c1z, c2z = cf.c2z, c3z = cf.c3z, c4z = cf.c4z;
+  const float c1x = cf.c1x, c2x = cf.c2x, c3x = cf.c3x, c4x = cf.c4x;
+  const float dzi = S.dzi, dxi = S.dxi;
+  // sz at rows z0-4+rr..+3 of column x0+cc, four rows per item: the
+  // 8th-order difference times delp inside the compute domain, the
+  // first-order one times delp of the face in the three padding cells, 0
+  // beyond (the fourth padding cell, which the reference reads and never
+  // writes) and off the compute columns.  delp at (i, j) is
+  // sdp[(j - x0 + 4) * R2_GZ + i - z0 + 4]; a face row or column that a
+  // padding cell of the tile needs lies inside the staged 72 x 40 block
+  // (z0 >= nmin1, x0 >= nmin2).
+  for (int q = tid; q < R2_X * (R2_GZ / 4); q += 256) {
+    const int cc = q / (R2_GZ / 4), rr = 4 * (q - cc * (R2_GZ / 4));
+    const int i0 = z0 - 4 + rr, j = x0 + cc;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (j <= nmax2) {
+      // u2 at rows i0-3..i0+7 of column j: staged rows rr+1..rr+11.
+      float U[12], D[4];
+      const float *col = su + (cc + 8) * R2_UZ + rr;
+      lds4_to(U, col);
+      lds4_to(U + 4, col + 4);
+      lds4_to(U + 8, col + 8);
+      const float *dcol = sdp + (cc + 4) * R2_GZ;
+      lds4_to(D, dcol + rr);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int i = i0 + e;
+        if (i >= nmin1 && i <= nmax1) {
+          float a = c1z * (U[e + 5] - U[e + 4]);
+          a = a + c2z * (U[e + 6] - U[e + 3]);
+          a = a + c3z * (U[e + 7] - U[e + 2]);
+          a = a + c4z * (U[e + 8] - U[e + 1]);
+          v[e] = a * D[e];
+        } else if (i >= nmin1 - 3 && i <= nmax1 + 3) {
+          const int ie = i < nmin1 ? nmin1 : nmax1;
+          v[e] = (dzi * (U[e + 5] - U[e + 4])) * dcol[ie - z0 + 4];
+        }
+      }
+    }
+    *reinterpret_cast<float4 *>(ssz + cc * R2_GZ + rr) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  // sx at rows z0+rr..+3 of column x0-4+cc, by the same rules along x.
+  for (int q = tid; q < R2_GX * (R2_Z / 4); q += 256) {
+    const int cc = q >> 4, rr = 4 * (q & 15);
+    const int i0 = z0 + rr, j = x0 - 4 + cc;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    const bool jin = j >= nmin2 && j <= nmax2;
+    if (i0 <= nmax1 && (jin || (j >= nmin2 - 3 && j <= nmax2 + 3))) {
+      // u2 at columns j-3..j+4 of rows i0..i0+3: V[m] is column j-3+m.
+      float V[8][4], D[4];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) lds4_to(V[m], su + (cc + 1 + m) * R2_UZ + rr + 8);
+      const int je = jin ? j : (j < nmin2 ? nmin2 : nmax2);
+      lds4_to(D, sdp + (je - x0 + 4) * R2_GZ + rr + 4);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (i0 + e > nmax1) continue;
+        if (jin) {
+          float a = c1x * (V[4][e] - V[3][e]);
+          a = a + c2x * (V[5][e] - V[2][e]);
+          a = a + c3x * (V[6][e] - V[1][e]);
+          a = a + c4x * (V[7][e] - V[0][e]);
+          v[e] = a * D[e];
+        } else {
+          v[e] = (dxi * (V[4][e] - V[3][e])) * D[e];
+        }
+      }
+    }
+    *reinterpret_cast<float4 *>(ssx + cc * R2_Z + rr) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  __syncthreads();
+  // Divergence times v^2*rho (FDderivatives.f90:642-655) and the point
+  // update, four rows per item: lanes 0-15 of a warp take the 16 row
+  // groups of one column, lanes 16-31 those of the next.
+  const int it = S.tmin + s * S.tstep;
+  const bool snapstep = (it % S.snapi) == 0;
+  const bool inj_tile = S.inj_on && !(z0 + R2_Z - 1 < S.bi0 || z0 > S.bi1 ||
+                                      x0 + R2_X - 1 < S.bj0 || x0 > S.bj1);
+  // Without injection in the tile and without snapshot or imaging work in
+  // the step, step_tail reduces to the time update (FDderivatives.f90:
+  // 960-982), done here on the four rows at once.
+  const bool heavy = inj_tile || (snapstep && (S.imaging != 0 || S.extract_wave));
+  const float k12 = S.k12, div11 = S.div11;
+  const int rr = 4 * (tid & 15);
+#pragma unroll 1
+  for (int h = 0; h < 2; ++h) {
+    const int cc = (tid >> 4) + 16 * h, j = x0 + cc, i0 = z0 + rr;
+    if (j > nmax2 || i0 > nmax1) continue;
+    // sz at rows i0-4..i0+7: Z[m] is row i0-4+m.
+    float Z[12];
+    const float *zc = ssz + cc * R2_GZ + rr;
+    lds4_to(Z, zc);
+    lds4_to(Z + 4, zc + 4);
+    lds4_to(Z + 8, zc + 8);
+    // sx at columns j-4..j+3: X[m] is column j-4+m.
+    float X[8][4];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) lds4_to(X[m], ssx + (cc + m) * R2_Z + rr);
+    float VV[4], RH[4], A1[4], A0[4], AM[4], U2[4];
+    const float *cv = sc + cc * R2_Z + rr;
+    lds4_to(VV, cv);
+    lds4_to(RH, cv + R2_CORE);
+    lds4_to(A1, cv + 2 * R2_CORE);
+    lds4_to(A0, cv + 3 * R2_CORE);
+    lds4_to(AM, cv + 4 * R2_CORE);
+    lds4_to(U2, su + (cc + 8) * R2_UZ + rr + 8);
+    float sv[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      float tz = c1z * (Z[e + 4] - Z[e + 3]);
+      tz = tz + c2z * (Z[e + 5] - Z[e + 2]);
+      tz = tz + c3z * (Z[e + 6] - Z[e + 1]);
+      tz = tz + c4z * (Z[e + 7] - Z[e + 0]);
+      float tx = c1x * (X[4][e] - X[3][e]);
+      tx = tx + c2x * (X[5][e] - X[2][e]);
+      tx = tx + c3x * (X[6][e] - X[1][e]);
+      tx = tx + c4x * (X[7][e] - X[0][e]);
+      const float vr = (VV[e] * VV[e]) * RH[e];
+      sv[e] = vr * (tx + tz);
+    }
+    const int p0 = off(i0, j);
+    if (heavy) {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (i0 + e <= nmax1)
+          rho_tail(S, i0 + e, j, p0 + e, it, sv[e], U2[e], A1[e], A0[e], AM[e], u2, u3, snapstep,
+                   inj_tile);
+      continue;
+    }
+    float o[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      float a = 20.0f * U2[e];
+      a = a - 6.0f * A1[e];
+      a = a - 4.0f * A0[e];
+      a = a + AM[e];
+      a = a + k12 * sv[e];
+      o[e] = a * div11;
+    }
+    if (i0 + 3 <= nmax1) {
+      *reinterpret_cast<float4 *>(u3 + p0) = make_float4(o[0], o[1], o[2], o[3]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        if (i0 + e <= nmax1) u3[p0 + e] = o[e];
+    }
+  }
+}
+
+static cudaError_t launch_rho2d(const BatchTables &t, int s_off, int n_tiles, cudaStream_t s) {
+  // The shared-memory opt-in is a per-device function attribute.
+  static unsigned long long attr_set = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 64 || !(attr_set & (1ull << dev))) {
+    e = cudaFuncSetAttribute(k_brho2d, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)R2_SMEM);
+    if (e != cudaSuccess) return e;
+    if (dev < 64) attr_set |= 1ull << dev;
+  }
+  k_brho2d<<<n_tiles, 256, R2_SMEM, s>>>(t, s_off);
+  return cudaGetLastError();
 }
 
 // Sinc gather of one receiver in the loop order of Extraction_1trace_sinc_xy
@@ -892,7 +1186,7 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     k_bfree<<<(n_hz + 127) / 128, 128, 0, s>>>(t, s_off);
     ++nl;
   }
-  if (tile.has_rho && n_v2u > 0) {
+  if (tile.has_rho && n_v2u > 0 && !tile.rho2d) {
     k_brho_grad<<<n_v2u, 256, 0, s>>>(t, s_off);
     ++nl;
   }
@@ -965,6 +1259,10 @@ cudaError_t launch_batch_step(const BatchTables &t, int s_off, int n_step_tiles,
     if (tile.tz == 128) launch_stream2d<128>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
     else if (tile.tz == 32) launch_stream2d<32>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
     else launch_stream2d<64>(t, s_off, n_step_tiles, tile, hf, ha, s, &nl);
+  } else if (tile.rho2d) {
+    cudaError_t e = launch_rho2d(t, s_off, n_step_tiles, s);
+    if (e != cudaSuccess) return e;
+    ++nl;
   } else {
     k_bstep<true><<<n_step_tiles, bs, 0, s>>>(t, s_off);
     ++nl;

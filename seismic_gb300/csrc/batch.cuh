@@ -216,6 +216,7 @@ struct StepTile {
   int n_snap3d = 0;    // blocks of k_bsnap3d (pipelined 3D kernel with snapshots / imaging)
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
   int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
+  int rho2d = 0;       // every shot is 2D with a density: the one-pass k_brho2d
   int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)
   int fuse2 = 0;       // 2D tiles: two time steps per launch (tile2d2.cuh)
 };
@@ -232,6 +233,7 @@ inline int edge_threads_2d(const Geom &g) {
 // Number of fused-step CTAs a shot needs with this tile shape.
 inline int step_ctas(const Geom &g, const StepTile &tile) {
   const int n1 = g.nmax1 - g.nmin1 + 1, n2 = g.nmax2 - g.nmin2 + 1, n3 = g.nmax3 - g.nmin3 + 1;
+  if (g.twoD && tile.rho2d) return ((n1 + 63) / 64) * ((n2 + 31) / 32);
   if (g.twoD && tile.fuse2) {
     int o1, o2, nz, nx;
     return tf_origin(n1, n2, &o1, &o2, &nz, &nx) ? nz * nx : 0;

@@ -93,26 +93,32 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
   // and packs tile coordinates into 12 bits each; larger batches, grids
   // beyond that or domains below 16 cells use the streaming kernel.
   StepTile tile = opt.tile;
-  // The variable-density operator runs on the point-tile step kernel after a
-  // gradient pass (k_brho_grad).
-  // So do the free surface (k_bfree before the step) and mirror sources and
-  // receivers.
+  // The variable-density operator: in 2D one pass per step (k_brho2d) when
+  // every shot of the batch has a density, else the point-tile step kernel
+  // after a gradient pass (k_brho_grad).  A free surface and mirror sources
+  // or receivers run on the single-step 2D tile kernel (k_bfree before it;
+  // the mirror terms are injection and extraction entries); in 3D on the
+  // point tiles.
   tile.has_rho = 0;
+  tile.rho2d = 0;
   tile.has_surf = 0;
-  bool special = false;
+  bool special = false, all_rho2d = true;
   for (int b = 0; b < nb; ++b) {
     const sw_genpar &g = shots[b].d.g;
     if (shots[b].io.rho_pad) tile.has_rho = 1;
+    // k_brho2d copies 16-byte chunks of v, rho and delp (and of the level
+    // buffers, carved at 256-byte boundaries).
+    const uintptr_t al = reinterpret_cast<uintptr_t>(shots[b].io.rho_pad) |
+                         reinterpret_cast<uintptr_t>(shots[b].io.delp) |
+                         reinterpret_cast<uintptr_t>(shots[b].io.vel_pad);
+    if (!shots[b].io.rho_pad || !g.twoD || (al & 15) != 0) all_rho2d = false;
     if (g.surf_type != 0) tile.has_surf = 1;
     if (g.surf_type != 0 || g.shot_type != 0 || g.rec_type != 0) special = true;
   }
-  // The variable-density operator runs on the point tiles.  A free surface
-  // and mirror sources or receivers run on the single-step 2D tile kernel
-  // (k_bfree before it; the mirror terms are injection and extraction
-  // entries); in 3D on the point tiles.
   if (tile.has_rho) {
     tile.stream2d = 0;
     tile.stream3d = 0;
+    tile.rho2d = all_rho2d ? 1 : 0;
   }
   if (special) {
     if (tile.stream2d != 0) tile.stream2d = 2;
@@ -605,7 +611,12 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
     uint64_t by = 0;
     for (auto &S : hs) {
       if (sidx >= S.nsteps) continue;
-      by += (uint64_t)S.npts * 24ull;
+      // 24 B per point (u2, u1, u0, u_1, v read, u3 written); with a density
+      // also rho and delp read (one pass, k_brho2d), or on the point tiles
+      // the gradient arrays instead of delp (sz, sx and in 3D sy).
+      uint64_t per_pt = 24;
+      if (S.rho_on) per_pt = tile.rho2d ? 32 : (S.g.twoD ? 36 : 40);
+      by += (uint64_t)S.npts * per_pt;
       if (t3) continue;   // snapshots and imaging: k_bsnap3d
       const int it = S.tmin + sidx * S.tstep;
       if (it % S.snapi != 0) continue;

@@ -49,6 +49,23 @@ def test_rho_modeling_bitexact(ctx, oracle, three_d):
     assert np.abs(c - a).max() > 1e-3 * np.abs(a).max()
 
 
+@pytest.mark.parametrize("nz,nx", [(70, 129), (43, 20)])
+def test_rho_modeling_ragged_tiles_bitexact(ctx, oracle, nz, nx):
+    """The one-pass 2D density step on grids whose compute domain is not a
+    multiple of its 64 x 32 tile, with the source near a tile corner."""
+    g, vel, sou, rec, w = case2d(nz=nz, nx=nx, nt=160, seed=2)
+    sou = np.array([(nz // 2) * 10.0 + 1.3, 31.0 * 10.0 if nx > 40 else 95.0, 0.0], np.float32)
+    rho = _rho(vel.shape, 9)
+    w = sw.rho_wavelet(w, g.lsinc)
+    d = _desc(g, injection=sw.INJ_SINC, extraction=sw.EXT_SINC)
+    a = np.zeros((rec.shape[0], g.nt), np.float32)
+    b = np.zeros_like(a)
+    ctx.propagate(d, vel, sou, w, rec, a, rho=rho)
+    oracle.propagate(d, vel, sou, w, rec, b, rho=rho)
+    assert np.abs(b).max() > 0
+    np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("three_d", [False, True])
 def test_rho_rtm_bitexact(ctx, oracle, three_d):
     """RTM_to_memory's withRho branch: forward with snapshots and the
