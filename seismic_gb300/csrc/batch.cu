@@ -486,8 +486,13 @@ __device__ __forceinline__ void cp_async16(float *dst, const float *src, bool in
                "r"(in ? 16 : 0)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// Waits until at most N of this thread's committed groups are in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 // step_tail of one point of k_brho2d's tiles that carry injection or
@@ -546,6 +551,7 @@ __global__ void __launch_bounds__(256, 2) k_brho2d(BatchTables t, int s_off) {
     const int cc = q / (R2_GZ / 4), k = q - cc * (R2_GZ / 4);
     stage(sdp + cc * R2_GZ + 4 * k, S.delp, z0 - 4 + 4 * k, x0 - 4 + cc);
   }
+  cp_async_commit();   // group 1: what the gradients read
   {
     // v, rho, then u1, u0, u_1 (levels s+2, s+1, s of the 5-level ring):
     // two chunks of each per thread.
@@ -560,12 +566,23 @@ __global__ void __launch_bounds__(256, 2) k_brho2d(BatchTables t, int s_off) {
       }
     }
   }
-  cp_async_wait_all();
-  __syncthreads();
+  cp_async_commit();   // group 2: the point update's inputs
+  // The shot's scalars, loaded while the copies are in flight.
   const Coefs &cf = S.cr;
   const float c1z = cf.c1z, c2z = cf.c2z, c3z = cf.c3z, c4z = cf.c4z;
   const float c1x = cf.c1x, c2x = cf.c2x, c3x = cf.c3x, c4x = cf.c4x;
   const float dzi = S.dzi, dxi = S.dxi;
+  const int it = S.tmin + s * S.tstep;
+  const bool snapstep = (it % S.snapi) == 0;
+  const bool inj_tile = S.inj_on && !(z0 + R2_Z - 1 < S.bi0 || z0 > S.bi1 ||
+                                      x0 + R2_X - 1 < S.bj0 || x0 > S.bj1);
+  // Without injection in the tile and without snapshot or imaging work in
+  // the step, step_tail reduces to the time update (FDderivatives.f90:
+  // 960-982), done below on four rows at once.
+  const bool heavy = inj_tile || (snapstep && (S.imaging != 0 || S.extract_wave));
+  const float k12 = S.k12, div11 = S.div11;
+  cp_async_wait<1>();
+  __syncthreads();
   // sz at rows z0-4+rr..+3 of column x0+cc, four rows per item: the
   // 8th-order difference times delp inside the compute domain, the
   // first-order one times delp of the face in the three padding cells, 0
@@ -633,19 +650,11 @@ __global__ void __launch_bounds__(256, 2) k_brho2d(BatchTables t, int s_off) {
     }
     *reinterpret_cast<float4 *>(ssx + cc * R2_Z + rr) = make_float4(v[0], v[1], v[2], v[3]);
   }
+  cp_async_wait<0>();
   __syncthreads();
   // Divergence times v^2*rho (FDderivatives.f90:642-655) and the point
   // update, four rows per item: lanes 0-15 of a warp take the 16 row
   // groups of one column, lanes 16-31 those of the next.
-  const int it = S.tmin + s * S.tstep;
-  const bool snapstep = (it % S.snapi) == 0;
-  const bool inj_tile = S.inj_on && !(z0 + R2_Z - 1 < S.bi0 || z0 > S.bi1 ||
-                                      x0 + R2_X - 1 < S.bj0 || x0 > S.bj1);
-  // Without injection in the tile and without snapshot or imaging work in
-  // the step, step_tail reduces to the time update (FDderivatives.f90:
-  // 960-982), done here on the four rows at once.
-  const bool heavy = inj_tile || (snapstep && (S.imaging != 0 || S.extract_wave));
-  const float k12 = S.k12, div11 = S.div11;
   const int rr = 4 * (tid & 15);
 #pragma unroll 1
   for (int h = 0; h < 2; ++h) {
