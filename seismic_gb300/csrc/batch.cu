@@ -591,64 +591,106 @@ __global__ void __launch_bounds__(256, 2) k_brho2d(BatchTables t, int s_off) {
   // sdp[(j - x0 + 4) * R2_GZ + i - z0 + 4]; a face row or column that a
   // padding cell of the tile needs lies inside the staged 72 x 40 block
   // (z0 >= nmin1, x0 >= nmin2).
-  for (int q = tid; q < R2_X * (R2_GZ / 4); q += 256) {
-    const int cc = q / (R2_GZ / 4), rr = 4 * (q - cc * (R2_GZ / 4));
-    const int i0 = z0 - 4 + rr, j = x0 + cc;
-    float v[4] = {0.f, 0.f, 0.f, 0.f};
-    if (j <= nmax2) {
-      // u2 at rows i0-3..i0+7 of column j: staged rows rr+1..rr+11.
-      float U[12], D[4];
+  // A tile whose gradient cells all lie inside the compute domain (most of
+  // them) takes the 8th-order difference everywhere, without the per-cell
+  // domain and padding tests.
+  const bool interior = z0 - 4 >= nmin1 && z0 + R2_Z + 3 <= nmax1 && x0 - 4 >= nmin2 &&
+                        x0 + R2_X + 3 <= nmax2;
+  if (interior) {
+    for (int q = tid; q < R2_X * (R2_GZ / 4); q += 256) {
+      const int cc = q / (R2_GZ / 4), rr = 4 * (q - cc * (R2_GZ / 4));
+      float U[12], D[4], v[4];
       const float *col = su + (cc + 8) * R2_UZ + rr;
       lds4_to(U, col);
       lds4_to(U + 4, col + 4);
       lds4_to(U + 8, col + 8);
-      const float *dcol = sdp + (cc + 4) * R2_GZ;
-      lds4_to(D, dcol + rr);
+      lds4_to(D, sdp + (cc + 4) * R2_GZ + rr);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int i = i0 + e;
-        if (i >= nmin1 && i <= nmax1) {
-          float a = c1z * (U[e + 5] - U[e + 4]);
-          a = a + c2z * (U[e + 6] - U[e + 3]);
-          a = a + c3z * (U[e + 7] - U[e + 2]);
-          a = a + c4z * (U[e + 8] - U[e + 1]);
-          v[e] = a * D[e];
-        } else if (i >= nmin1 - 3 && i <= nmax1 + 3) {
-          const int ie = i < nmin1 ? nmin1 : nmax1;
-          v[e] = (dzi * (U[e + 5] - U[e + 4])) * dcol[ie - z0 + 4];
-        }
+        float a = c1z * (U[e + 5] - U[e + 4]);
+        a = a + c2z * (U[e + 6] - U[e + 3]);
+        a = a + c3z * (U[e + 7] - U[e + 2]);
+        a = a + c4z * (U[e + 8] - U[e + 1]);
+        v[e] = a * D[e];
       }
+      *reinterpret_cast<float4 *>(ssz + cc * R2_GZ + rr) = make_float4(v[0], v[1], v[2], v[3]);
     }
-    *reinterpret_cast<float4 *>(ssz + cc * R2_GZ + rr) = make_float4(v[0], v[1], v[2], v[3]);
-  }
-  // sx at rows z0+rr..+3 of column x0-4+cc, by the same rules along x.
-  for (int q = tid; q < R2_GX * (R2_Z / 4); q += 256) {
-    const int cc = q >> 4, rr = 4 * (q & 15);
-    const int i0 = z0 + rr, j = x0 - 4 + cc;
-    float v[4] = {0.f, 0.f, 0.f, 0.f};
-    const bool jin = j >= nmin2 && j <= nmax2;
-    if (i0 <= nmax1 && (jin || (j >= nmin2 - 3 && j <= nmax2 + 3))) {
-      // u2 at columns j-3..j+4 of rows i0..i0+3: V[m] is column j-3+m.
-      float V[8][4], D[4];
+    for (int q = tid; q < R2_GX * (R2_Z / 4); q += 256) {
+      const int cc = q >> 4, rr = 4 * (q & 15);
+      float V[8][4], D[4], v[4];
 #pragma unroll
       for (int m = 0; m < 8; ++m) lds4_to(V[m], su + (cc + 1 + m) * R2_UZ + rr + 8);
-      const int je = jin ? j : (j < nmin2 ? nmin2 : nmax2);
-      lds4_to(D, sdp + (je - x0 + 4) * R2_GZ + rr + 4);
+      lds4_to(D, sdp + cc * R2_GZ + rr + 4);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        if (i0 + e > nmax1) continue;
-        if (jin) {
-          float a = c1x * (V[4][e] - V[3][e]);
-          a = a + c2x * (V[5][e] - V[2][e]);
-          a = a + c3x * (V[6][e] - V[1][e]);
-          a = a + c4x * (V[7][e] - V[0][e]);
-          v[e] = a * D[e];
-        } else {
-          v[e] = (dxi * (V[4][e] - V[3][e])) * D[e];
+        float a = c1x * (V[4][e] - V[3][e]);
+        a = a + c2x * (V[5][e] - V[2][e]);
+        a = a + c3x * (V[6][e] - V[1][e]);
+        a = a + c4x * (V[7][e] - V[0][e]);
+        v[e] = a * D[e];
+      }
+      *reinterpret_cast<float4 *>(ssx + cc * R2_Z + rr) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+  } else {
+    for (int q = tid; q < R2_X * (R2_GZ / 4); q += 256) {
+      const int cc = q / (R2_GZ / 4), rr = 4 * (q - cc * (R2_GZ / 4));
+      const int i0 = z0 - 4 + rr, j = x0 + cc;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      if (j <= nmax2) {
+        // u2 at rows i0-3..i0+7 of column j: staged rows rr+1..rr+11.
+        float U[12], D[4];
+        const float *col = su + (cc + 8) * R2_UZ + rr;
+        lds4_to(U, col);
+        lds4_to(U + 4, col + 4);
+        lds4_to(U + 8, col + 8);
+        const float *dcol = sdp + (cc + 4) * R2_GZ;
+        lds4_to(D, dcol + rr);
+  #pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int i = i0 + e;
+          if (i >= nmin1 && i <= nmax1) {
+            float a = c1z * (U[e + 5] - U[e + 4]);
+            a = a + c2z * (U[e + 6] - U[e + 3]);
+            a = a + c3z * (U[e + 7] - U[e + 2]);
+            a = a + c4z * (U[e + 8] - U[e + 1]);
+            v[e] = a * D[e];
+          } else if (i >= nmin1 - 3 && i <= nmax1 + 3) {
+            const int ie = i < nmin1 ? nmin1 : nmax1;
+            v[e] = (dzi * (U[e + 5] - U[e + 4])) * dcol[ie - z0 + 4];
+          }
         }
       }
+      *reinterpret_cast<float4 *>(ssz + cc * R2_GZ + rr) = make_float4(v[0], v[1], v[2], v[3]);
     }
-    *reinterpret_cast<float4 *>(ssx + cc * R2_Z + rr) = make_float4(v[0], v[1], v[2], v[3]);
+    // sx at rows z0+rr..+3 of column x0-4+cc, by the same rules along x.
+    for (int q = tid; q < R2_GX * (R2_Z / 4); q += 256) {
+      const int cc = q >> 4, rr = 4 * (q & 15);
+      const int i0 = z0 + rr, j = x0 - 4 + cc;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
+      const bool jin = j >= nmin2 && j <= nmax2;
+      if (i0 <= nmax1 && (jin || (j >= nmin2 - 3 && j <= nmax2 + 3))) {
+        // u2 at columns j-3..j+4 of rows i0..i0+3: V[m] is column j-3+m.
+        float V[8][4], D[4];
+  #pragma unroll
+        for (int m = 0; m < 8; ++m) lds4_to(V[m], su + (cc + 1 + m) * R2_UZ + rr + 8);
+        const int je = jin ? j : (j < nmin2 ? nmin2 : nmax2);
+        lds4_to(D, sdp + (je - x0 + 4) * R2_GZ + rr + 4);
+  #pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (i0 + e > nmax1) continue;
+          if (jin) {
+            float a = c1x * (V[4][e] - V[3][e]);
+            a = a + c2x * (V[5][e] - V[2][e]);
+            a = a + c3x * (V[6][e] - V[1][e]);
+            a = a + c4x * (V[7][e] - V[0][e]);
+            v[e] = a * D[e];
+          } else {
+            v[e] = (dxi * (V[4][e] - V[3][e])) * D[e];
+          }
+        }
+      }
+      *reinterpret_cast<float4 *>(ssx + cc * R2_Z + rr) = make_float4(v[0], v[1], v[2], v[3]);
+    }
   }
   cp_async_wait<0>();
   __syncthreads();
