@@ -215,7 +215,7 @@ struct StepTile {
   int n_edge = 0;      // threads of that launch
   int n_snap3d = 0;    // blocks of k_bsnap3d (pipelined 3D kernel with snapshots / imaging)
   int rigid = 0;       // skip the Higdon boundary (exact-adjoint mode)
-  int has_rho = 0;     // some shot runs the variable-density operator (point tiles)
+  int has_rho = 0;     // some shot runs the variable-density operator
   int rho2d = 0;       // every shot is 2D with a density: the one-pass k_brho2d
   int has_surf = 0;    // some shot has a free surface (point tiles, k_bfree)
   int fuse2 = 0;       // 2D tiles: two time steps per launch (tile2d2.cuh)

@@ -198,7 +198,8 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
                     n3 = G[b].nmax3 - G[b].nmin3 + 1;
     bytes += (tile.fuse2 ? 6 : 5) * rup(fb);
     if (!d.g.twoD && d.fd_scheme == SW_FD_ADJOINT && !tile.stream3d) bytes += rup(fb);
-    if (io.rho_pad) bytes += (d.g.twoD ? 2 : 3) * rup(fb);
+    // The staggered gradient arrays of the two-pass density operator.
+    if (io.rho_pad && !tile.rho2d) bytes += (d.g.twoD ? 2 : 3) * rup(fb);
     bytes += rup(16 * n2 * n3 * 4) + rup(16 * n1 * n3 * 4) + rup(16 * n1 * n2 * 4);
     bytes += rup(inj[b].off.size() * 4) + rup(inj[b].ent.size() * sizeof(InjEntry)) +
              rup((tile.fuse2 ? 2 : 1) * inj[b].ent.size() * sizeof(float));
@@ -268,13 +269,17 @@ int run_phases(sw_ctx *c, std::vector<PhaseShot> &shots, const RunOpts &opt) {
       S.dzi = 1.f / g.dz;
       S.dxi = 1.f / g.dx;
       S.dyi = 1.f / g.dy;
-      S.sz = carve<float>(cur, nf);
-      S.sx = carve<float>(cur, nf);
-      SW_CK(cudaMemsetAsync(S.sz, 0, nf * sizeof(float), s));
-      SW_CK(cudaMemsetAsync(S.sx, 0, nf * sizeof(float), s));
-      if (!g.twoD) {
-        S.sy = carve<float>(cur, nf);
-        SW_CK(cudaMemsetAsync(S.sy, 0, nf * sizeof(float), s));
+      // k_brho2d forms sz and sx in shared memory; the two-pass operator
+      // (k_brho_grad, then the point tiles) keeps them in HBM.
+      if (!tile.rho2d) {
+        S.sz = carve<float>(cur, nf);
+        S.sx = carve<float>(cur, nf);
+        SW_CK(cudaMemsetAsync(S.sz, 0, nf * sizeof(float), s));
+        SW_CK(cudaMemsetAsync(S.sx, 0, nf * sizeof(float), s));
+        if (!g.twoD) {
+          S.sy = carve<float>(cur, nf);
+          SW_CK(cudaMemsetAsync(S.sy, 0, nf * sizeof(float), s));
+        }
       }
     }
     const long long n1 = G[b].nmax1 - G[b].nmin1 + 1, n2 = G[b].nmax2 - G[b].nmin2 + 1,
