@@ -68,6 +68,30 @@ def test_rho_modeling_ragged_tiles_bitexact(ctx, oracle, nz, nx):
     np.testing.assert_array_equal(a, b)
 
 
+def test_rho_modeling_more_tiles_than_sms_bitexact(ctx, oracle):
+    """A compute domain of 720 x 421 points is 12 x 14 = 168 tiles, more
+    than the device has SMs.  The source sits in tile 152 (rows 503-566,
+    columns 375-406 of the compute domain), deep in the model; every
+    snapshot of the whole field and the traces of a receiver line through
+    the source equal the oracle's."""
+    nz, nx = 700, 401
+    g, vel, sou, rec, w = case2d(nz=nz, nx=nx, nt=64, seed=3, dt=5e-4)
+    sou = np.array([5500.0 + 1.3, 3900.0 + 2.1, 0.0], np.float32)
+    rec[:, 0] = 5450.0 + 2.3
+    rho = _rho(vel.shape, 11)
+    w = sw.rho_wavelet(w, g.lsinc)
+    d = _desc(g, injection=sw.INJ_SINC, extraction=sw.EXT_SINC, extract_wave=1)
+    out = {}
+    for name, api in (("gpu", ctx), ("oracle", oracle)):
+        data = np.zeros((rec.shape[0], g.nt), np.float32)
+        wave = np.zeros((g.nt // g.snapi) * vel.size, np.float32)
+        api.propagate(d, vel, sou, w, rec, data, wave=wave, rho=rho)
+        out[name] = (data, wave)
+    for a, b in zip(out["gpu"], out["oracle"]):
+        assert np.abs(b).max() > 0
+        np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("three_d", [False, True])
 def test_rho_rtm_bitexact(ctx, oracle, three_d):
     """RTM_to_memory's withRho branch: forward with snapshots and the
