@@ -287,6 +287,9 @@ def main():
     ap.add_argument("--rho", action="store_true",
                     help="time 2D modelling with variable density (and without) on the "
                          "751 x 2301 grid instead of the RTM bench")
+    ap.add_argument("--rho3d", action="store_true",
+                    help="with --rho: 3D modelling on the 200 x 400 x 400 grid at 12.5 m "
+                         "(the two-pass density operator on the point tiles)")
     ap.add_argument("--fwi-bench", action="store_true",
                     help="time one 80-shot FWI misfit and gradient evaluation on 601 x 1801")
     ap.add_argument("--cnn-bench", action="store_true",
@@ -573,32 +576,58 @@ def run_rho_bench(args) -> int:
     model at 4 m (the RTM bench's grid and dt, 2000 steps, 2301 receivers)
     through sw_propagate with a density model (withRho: the one-pass
     staggered operator, k_brho2d) and, for scale, the same run without it.
-    One JSON line with the density step kernel's roofline."""
+    With --rho3d: 3D modelling on the 200 x 400 x 400 grid at 12.5 m (400
+    steps, 2304 receivers), where the density operator is the gradient
+    pass plus the point-tile step.  One JSON line with the density step
+    kernel's roofline."""
     import torch
 
     import seismic_gb300 as sw
     from seismic_gb300 import synth
     torch.cuda.set_device(0)
     ctx = sw.Context(0)
-    c = synth.CONFIG2
-    nt = args.nt_cap or 2000
-    nz, nx, d = c["nz"], c["nx"], c["d"]
-    g = sw.make_genpar(nz, nx, 1, dz=d, dx=d, dt=c["dt"], nt=nt, ntaper=c["ntaper"], lsinc=7,
-                       snapi=4)
-    vel = synth.layered_faulted(nz, nx, d, seed=3)
     rng = np.random.default_rng(3)
-    rho = np.ascontiguousarray(1.8 + 0.0004 * np.arange(nz)[None, :] * d +
-                               0.1 * rng.random(vel.shape), np.float32)
-    sou = np.array([2 * d, nx * d / 2, 0.0], np.float32)
-    rec = np.zeros((nx, 3), np.float32)
-    rec[:, 0], rec[:, 1] = 2 * d, np.arange(nx) * d
-    w = sw.rho_wavelet(synth.ricker(20.0, c["dt"], nt), 7)
+    if args.rho3d:
+        nz, nx, ny, d, dt = 200, 400, 400, 12.5, 9e-4
+        nt = args.nt_cap or 400
+        g = sw.make_genpar(nz, nx, ny, dz=d, dx=d, dy=d, dt=dt, nt=nt, ntaper=20, lsinc=7,
+                           snapi=4, twoD=False, fmax=20.0)
+        z = np.arange(nz)[None, None, :] * d
+        vel = np.ascontiguousarray(np.broadcast_to(1500.0 + 1.0 * z, (ny, nx, nz)), np.float32)
+        rho = np.ascontiguousarray(1.8 + 0.0004 * z + 0.1 * rng.random(vel.shape), np.float32)
+        sou = np.array([25.0, nx * d / 2, ny * d / 2], np.float32)
+        rx, ry = np.meshgrid(np.arange(10, nx - 10, 8) * d, np.arange(10, ny - 10, 8) * d,
+                             indexing="ij")
+        rec = np.zeros((rx.size, 3), np.float32)
+        rec[:, 0], rec[:, 1], rec[:, 2] = 12.5, rx.ravel(), ry.ravel()
+        w = sw.rho_wavelet(synth.ricker(10.0, dt, nt), 7)
+        workload = ("3D modelling of one shot with variable density through sw_propagate "
+                    "(host buffers)")
+        grid, kernel = [nz, nx, ny], ("k_bstep<false> after k_brho_grad (two-pass density "
+                                      "operator on the point tiles, 40 B per point)")
+    else:
+        c = synth.CONFIG2
+        nt = args.nt_cap or 2000
+        nz, nx, d, dt = c["nz"], c["nx"], c["d"], c["dt"]
+        g = sw.make_genpar(nz, nx, 1, dz=d, dx=d, dt=dt, nt=nt, ntaper=c["ntaper"], lsinc=7,
+                           snapi=4)
+        vel = synth.layered_faulted(nz, nx, d, seed=3)
+        rho = np.ascontiguousarray(1.8 + 0.0004 * np.arange(nz)[None, :] * d +
+                                   0.1 * rng.random(vel.shape), np.float32)
+        sou = np.array([2 * d, nx * d / 2, 0.0], np.float32)
+        rec = np.zeros((nx, 3), np.float32)
+        rec[:, 0], rec[:, 1] = 2 * d, np.arange(nx) * d
+        w = sw.rho_wavelet(synth.ricker(20.0, dt, nt), 7)
+        workload = ("2D modelling of one shot with variable density through sw_propagate "
+                    "(host buffers)")
+        grid, kernel = [nz, nx], ("k_brho2d (one-pass staggered gradient, divergence and time "
+                                  "update, 32 B per point)")
     desc = sw.SwPropDesc()
     desc.g = g
     desc.tmin, desc.tmax, desc.tstep = 1, nt, 1
     desc.fd_scheme = sw.FD_FORWARD
     desc.injection, desc.extraction = sw.INJ_SINC, sw.EXT_SINC
-    data = np.zeros((nx, nt), np.float32)
+    data = np.zeros((rec.shape[0], nt), np.float32)
 
     def run(with_rho):
         ctx.propagate(desc, vel, sou[None], w[None], rec, data,
@@ -637,20 +666,19 @@ def run_rho_bench(args) -> int:
     kern_s = sp["step_kernel_ms"] / 1e3
     achieved = (sp["step_bytes"] / nl) / (kern_s / nl) / 1e9 if kern_s > 0 else None
     line = {
-        "metric": "fd_gpts_per_s_2d_rho_modeling", "value": out[True][0], "unit": "Gpts/s",
+        "metric": "fd_gpts_per_s_%s_rho_modeling" % ("3d" if args.rho3d else "2d"),
+        "value": out[True][0], "unit": "Gpts/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": out[True][1] * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded layered, faulted model; density 1.8-2.2 g/cc)",
-        "config": {"workload": "2D modelling of one shot with variable density through "
-                               "sw_propagate (host buffers)",
-                   "grid": [nz, nx], "spacing_m": d, "dt_s": c["dt"], "nt": nt,
-                   "receivers": nx},
+        "data": ("synthetic (linear velocity gradient; density 1.8-2.9 g/cc)" if args.rho3d
+                 else "synthetic (seeded layered, faulted model; density 1.8-2.2 g/cc)"),
+        "config": {"workload": workload, "grid": grid, "spacing_m": d, "dt_s": dt, "nt": nt,
+                   "receivers": int(rec.shape[0])},
         "constant_density_gpts_per_s": out[False][0],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None, "peak_kind": peak_kind,
-                     "kernel": "k_brho2d (one-pass staggered gradient, divergence and time "
-                               "update, 32 B per point)",
+                     "kernel": kernel,
                      "avg_launch_ms": sp["step_kernel_ms"] / nl,
                      "algorithmic_bytes_per_launch": sp["step_bytes"] / nl},
         "clocks": clk, "gpu_launches": out[True][2],
