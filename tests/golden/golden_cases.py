@@ -97,7 +97,33 @@ def make_inputs() -> dict[str, dict]:
         fwi[f"shot{i}_dobs"] = _f32(rng.standard_normal((34, g4.nt)) * 1e-2)
         fwi[f"shot{i}_mute"] = _f32(rng.random((34, g4.nt)) > 0.1)
     out["fwi2d"] = fwi
+    # Variable density (withRho): 2D modelling and the rho-v AFWI imaging
+    # condition, 3D modelling.
+    g5 = sw.make_genpar(52, 70, 1, dz=d, dx=d, dt=dt, nt=200, ntaper=10, lsinc=7, snapi=4)
+    vel5 = _model(52, 70, 1, d, 4)
+    rho5 = _f32(1.8 + 0.0008 * np.arange(52)[None, :] * d + 0.15 * rng.random(vel5.shape))
+    rec5 = np.zeros((35, 3), np.float32)
+    rec5[:, 0] = d + 2.3
+    rec5[:, 1] = np.linspace(4.0, 686.0, 35)
+    base5 = {"genpar": _genpar_json(g5), "vel": vel5, "rho": rho5, "sou": _f32([24.1, 333.3, 0.0]),
+             "rec": rec5, "wavelet": _f32(sw.rho_wavelet(synth.ricker(12.0, dt, g5.nt), 7))}
+    out["rho_modeling2d"] = dict(base5, kind="rho_modeling")
+    out["rho_afwi2d"] = dict(base5, kind="rho_afwi",
+                             data=_f32(rng.standard_normal((35, g5.nt)) * 1e-2))
+    rho3 = _f32(1.8 + 0.15 * rng.random(vel3.shape))
+    out["rho_modeling3d"] = dict(base3, kind="rho_modeling", rho=rho3,
+                                 wavelet=_f32(sw.rho_wavelet(base3["wavelet"], 7)))
     return out
+
+
+def _prop_desc(g, forward: bool, **kw):
+    d = sw.SwPropDesc()
+    d.g = g
+    d.tmin, d.tmax, d.tstep = (1, g.nt, 1) if forward else (g.nt, 1, -1)
+    d.fd_scheme = sw.FD_FORWARD
+    for k, v in kw.items():
+        setattr(d, k, v)
+    return d
 
 
 def run(api, inp: dict) -> dict[str, np.ndarray]:
@@ -129,4 +155,19 @@ def run(api, inp: dict) -> dict[str, np.ndarray]:
         f, grad, illum = api.fwi_fct_gdt(desc, vel, w, shots, vpmask=inp["vpmask"])
         return {"out_misfit": np.array([f], np.float64), "out_gradient": grad,
                 "out_illum": illum}
+    if kind == "rho_modeling":
+        data = np.zeros((inp["rec"].shape[0], g.nt), np.float32)
+        api.propagate(_prop_desc(g, True, injection=sw.INJ_SINC, extraction=sw.EXT_SINC), vel,
+                      inp["sou"], w, inp["rec"], data, rho=inp["rho"])
+        return {"out_data": data}
+    if kind == "rho_afwi":
+        n = vel.size
+        wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+        api.propagate(_prop_desc(g, True, injection=sw.INJ_SINC, extract_wave=1), vel,
+                      inp["sou"], w, wave=wave, rho=inp["rho"])
+        im, im2, il = (np.zeros(n, np.float32) for _ in range(3))
+        api.propagate(_prop_desc(g, False, injection=sw.INJ_SINC, imaging=sw.IMG_AFWI_RHO), vel,
+                      inp["rec"], np.array(inp["data"]), wave=wave, image=im, illum=il,
+                      rho=inp["rho"], image2=im2)
+        return {"out_image": im, "out_image2": im2, "out_illum": il}
     raise ValueError(kind)

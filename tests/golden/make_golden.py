@@ -1,6 +1,7 @@
 """Writes the golden fixtures (tests/golden/*.npz) from the FP32 oracle.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py rho_afwi2d # the named cases only
 
 Each fixture holds a case's inputs and the oracle's outputs (arrays named
 out_*).  The oracle's parity with the reference is unpinned (the Fortran
@@ -20,9 +21,15 @@ from seismic_gb300.build import build_oracle  # noqa: E402
 from tests.golden.golden_cases import make_inputs, run  # noqa: E402
 
 
-def main():
+def main(names):
     build_oracle()
-    for name, inp in make_inputs().items():
+    cases = make_inputs()
+    unknown = set(names) - set(cases)
+    if unknown:
+        raise SystemExit(f"unknown cases: {sorted(unknown)}")
+    for name, inp in cases.items():
+        if names and name not in names:
+            continue
         out = run(bind, inp)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **inp, **out)
@@ -30,4 +37,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
