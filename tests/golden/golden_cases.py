@@ -98,7 +98,7 @@ def make_inputs() -> dict[str, dict]:
         fwi[f"shot{i}_mute"] = _f32(rng.random((34, g4.nt)) > 0.1)
     out["fwi2d"] = fwi
     # Variable density (withRho): 2D modelling and the rho-v AFWI imaging
-    # condition, 3D modelling.
+    # condition, 3D modelling (below).
     g5 = sw.make_genpar(52, 70, 1, dz=d, dx=d, dt=dt, nt=200, ntaper=10, lsinc=7, snapi=4)
     vel5 = _model(52, 70, 1, d, 4)
     rho5 = _f32(1.8 + 0.0008 * np.arange(52)[None, :] * d + 0.15 * rng.random(vel5.shape))
@@ -110,6 +110,13 @@ def make_inputs() -> dict[str, dict]:
     out["rho_modeling2d"] = dict(base5, kind="rho_modeling")
     out["rho_afwi2d"] = dict(base5, kind="rho_afwi",
                              data=_f32(rng.standard_normal((35, g5.nt)) * 1e-2))
+    # A free surface between grid rows (sinc mirror) with a mirror source.
+    g6 = sw.make_genpar(44, 60, 1, dz=d, dx=d, dt=dt, nt=260, ntaper=10, lsinc=7, snapi=4)
+    g6.surf_type, g6.shot_type, g6.rec_type, g6.oz = 1, 1, 0, -4.0
+    rec6 = rec2.copy()
+    rec6[:, 0] = 20.7
+    out["surface_modeling2d"] = dict(base2, kind="surface_modeling", genpar=_genpar_json(g6),
+                                     sou=_f32([20.4, 291.7, 0.0]), rec=rec6)
     rho3 = _f32(1.8 + 0.15 * rng.random(vel3.shape))
     out["rho_modeling3d"] = dict(base3, kind="rho_modeling", rho=rho3,
                                  wavelet=_f32(sw.rho_wavelet(base3["wavelet"], 7)))
@@ -155,10 +162,10 @@ def run(api, inp: dict) -> dict[str, np.ndarray]:
         f, grad, illum = api.fwi_fct_gdt(desc, vel, w, shots, vpmask=inp["vpmask"])
         return {"out_misfit": np.array([f], np.float64), "out_gradient": grad,
                 "out_illum": illum}
-    if kind == "rho_modeling":
+    if kind in ("rho_modeling", "surface_modeling"):
         data = np.zeros((inp["rec"].shape[0], g.nt), np.float32)
         api.propagate(_prop_desc(g, True, injection=sw.INJ_SINC, extraction=sw.EXT_SINC), vel,
-                      inp["sou"], w, inp["rec"], data, rho=inp["rho"])
+                      inp["sou"], w, inp["rec"], data, rho=inp.get("rho"))
         return {"out_data": data}
     if kind == "rho_afwi":
         n = vel.size

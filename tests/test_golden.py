@@ -21,7 +21,8 @@ def _load(path):
 
 def test_fixture_set_is_complete():
     assert set(NAMES) >= {"modeling2d", "modeling3d", "rtm2d", "rtm3d", "born2d", "lsrtm2d",
-                          "fwi2d", "rho_modeling2d", "rho_afwi2d", "rho_modeling3d"}
+                          "fwi2d", "rho_modeling2d", "rho_afwi2d", "rho_modeling3d",
+                          "surface_modeling2d"}
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=NAMES)
