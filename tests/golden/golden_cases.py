@@ -120,6 +120,15 @@ def make_inputs() -> dict[str, dict]:
     rho3 = _f32(1.8 + 0.15 * rng.random(vel3.shape))
     out["rho_modeling3d"] = dict(base3, kind="rho_modeling", rho=rho3,
                                  wavelet=_f32(sw.rho_wavelet(base3["wavelet"], 7)))
+    # The AFWI imaging condition (second time difference of the snapshots).
+    out["afwi2d"] = dict(base2, kind="afwi",
+                         data=_f32(rng.standard_normal((30, g2.nt)) * 1e-2))
+    # Born and LSRTM in 3D.
+    refl3 = _f32(rng.standard_normal(vel3.shape) * (rng.random(vel3.shape) < 0.05))
+    wb3 = _f32(sw.born_wavelet(base3["wavelet"], g3.dt))
+    out["born3d"] = dict(base3, kind="born", ref=refl3, wavelet=wb3)
+    out["lsrtm3d"] = dict(base3, kind="lsrtm", wavelet=wb3,
+                          data=_f32(rng.standard_normal((rec3.shape[0], g3.nt)) * 1e-2))
     return out
 
 
@@ -167,6 +176,15 @@ def run(api, inp: dict) -> dict[str, np.ndarray]:
         api.propagate(_prop_desc(g, True, injection=sw.INJ_SINC, extraction=sw.EXT_SINC), vel,
                       inp["sou"], w, inp["rec"], data, rho=inp.get("rho"))
         return {"out_data": data}
+    if kind == "afwi":
+        n = vel.size
+        wave = np.zeros((g.nt // g.snapi) * n, np.float32)
+        api.propagate(_prop_desc(g, True, injection=sw.INJ_SINC, extract_wave=1), vel,
+                      inp["sou"], w, wave=wave)
+        im, il = np.zeros(n, np.float32), np.zeros(n, np.float32)
+        api.propagate(_prop_desc(g, False, injection=sw.INJ_SINC, imaging=sw.IMG_AFWI), vel,
+                      inp["rec"], np.array(inp["data"]), wave=wave, image=im, illum=il)
+        return {"out_image": im, "out_illum": il}
     if kind == "rho_afwi":
         n = vel.size
         wave = np.zeros((g.nt // g.snapi) * n, np.float32)

@@ -22,7 +22,7 @@ def _load(path):
 def test_fixture_set_is_complete():
     assert set(NAMES) >= {"modeling2d", "modeling3d", "rtm2d", "rtm3d", "born2d", "lsrtm2d",
                           "fwi2d", "rho_modeling2d", "rho_afwi2d", "rho_modeling3d",
-                          "surface_modeling2d"}
+                          "surface_modeling2d", "afwi2d", "born3d", "lsrtm3d"}
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=NAMES)
